@@ -1,0 +1,72 @@
+/* olliptic_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of the reference's (WuShichao/OllipticID) FAS multigrid
+ * solve of the puncture Hamiltonian constraint.  It is the checker for the
+ * GPU library: only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline may load it.  The product (libolgpu) never links or calls it.
+ *
+ * Every routine follows the reference's arithmetic in the same order, so that
+ * on the same host it reproduces the reference's iterates (pinned against the
+ * reference itself by tests/golden/, which oracle/ref_harness.cc generated).
+ */
+#ifndef OLLIPTIC_ORACLE_H
+#define OLLIPTIC_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_MAX_BH 16
+
+typedef struct {
+  int equation;            /* 0 = Punctures, 1 = Punctures_scalar_field   */
+  int numbh;
+  double mp[ORC_MAX_BH];
+  double x[ORC_MAX_BH], y[ORC_MAX_BH], z[ORC_MAX_BH];
+  double px[ORC_MAX_BH], py[ORC_MAX_BH], pz[ORC_MAX_BH];
+  double sx[ORC_MAX_BH], sy[ORC_MAX_BH], sz[ORC_MAX_BH];
+  int n;                   /* -N  (snapped by Valid_N)                      */
+  double L;                /* -L  full domain length                        */
+  int order;               /* -O  2/4/6/8                                   */
+  int levels;              /* -l  refinement levels incl. the base grid     */
+  int nu1, nu2;            /* -nu1 / -nu2                                   */
+  double tol;              /* -s                                            */
+  /* scalar field (-psc -phi0 -r0 -sigma -a2) */
+  int ps_case;
+  double ps_phi0, ps_r0, ps_sigma, ps_a2;
+} orc_problem;
+
+typedef struct orc_solver orc_solver;
+
+typedef struct {
+  int level, nx, ny, nz, buf, order;
+  double xi, yi, zi, xf, yf, zf, dx, dy, dz, cx, cy, cz;
+  double gxi, gyi, gzi, gxf, gyf, gzf;
+} orc_box_info;
+
+void orc_problem_defaults(orc_problem *p);
+orc_solver *orc_create(const orc_problem *p);
+void orc_destroy(orc_solver *s);
+int orc_num_boxes(const orc_solver *s);
+int orc_num_levels(const orc_solver *s);
+int orc_mgrid_levels(const orc_solver *s);
+void orc_box(const orc_solver *s, int box, orc_box_info *out);
+/* field names: "u" "b" "c" "d" "e" "rho" "r" "w" "ww" "v"; lexicographic, i fastest */
+int orc_get_field(const orc_solver *s, int box, const char *name, double *out);
+int orc_set_field(orc_solver *s, int box, const char *name, const double *in);
+/* one FAS V-cycle from the top level (elliptic::FASN); returns the top-level norm */
+double orc_vcycle(orc_solver *s);
+/* elliptic::Vcycle: cycles while res > eps && res < res_prev; returns cycles run */
+int orc_solve(orc_solver *s, int max_cycles, double *final_res);
+/* ADM masses computed at the end of every top-level cycle */
+void orc_adm(const orc_solver *s, double *out);
+/* Single-box building blocks, exposed for unit tests. */
+double orc_smooth(orc_solver *s, int level, int ibox, int nu);
+void orc_robin(orc_solver *s, int level, int ibox);
+/* Valid_N restated (src/interface.cc:883-945) */
+int orc_valid_n(int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
