@@ -1,0 +1,145 @@
+/* olgpu.h -- C ABI of the GB300 puncture FAS solver (libolgpu.so).
+ *
+ * Plain C types only: no C++ types and no exceptions cross this boundary.
+ * Every call returns an olgpu_status; olgpu_last_error() describes the last
+ * failure of the calling thread.  A hierarchy handle owns all of its device
+ * memory, is bound to one CUDA stream and must be used by one host thread at
+ * a time.  Host buffers are owned by the caller and only touched during the
+ * call that receives them.
+ *
+ * Reference interfaces replaced (WuShichao/OllipticID):
+ *   olgpu_hierarchy_create  elliptic::elliptic(interface*) -> Make, Set_Grids,
+ *                           Set_Equation, Set_Coefficients
+ *                           (src/elliptic.cc:30-221, 299-921;
+ *                            src/operator.cc:22-621, 629-1668)
+ *   olgpu_box / olgpu_num_*  multigrid::Get_num_dom, domain getters
+ *                           (include/multigrid.h:246, include/domain.h:457-727)
+ *   olgpu_upload/download   multigrid::Get_ffunction(level, box, name) field
+ *                           access (include/multigrid.h:98)
+ *   olgpu_vcycle            elliptic::FASN(levels-1, levels-1, false, c)
+ *                           (src/elliptic.cc:1468-1968)
+ *   olgpu_solve             elliptic::Solve -> elliptic::Vcycle
+ *                           (include/elliptic.h:331-334, src/elliptic.cc:1251-1342)
+ *   olgpu_adm_mass          elliptic::Compute_ADM_Mass, puncture part
+ *                           (src/elliptic.cc:2447-2469)
+ */
+#ifndef OLGPU_H
+#define OLGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OLGPU_MAX_BH 16
+
+typedef enum {
+  OLGPU_OK = 0,
+  OLGPU_ERR_INVALID_ARG = 1,
+  OLGPU_ERR_OOM = 2,
+  OLGPU_ERR_CUDA = 3,
+  OLGPU_ERR_NAN = 4,          /* the smoother produced NaN (reference: exit(0)) */
+  OLGPU_ERR_DIVERGED = 5,
+  OLGPU_ERR_TIMEOUT = 6,
+  OLGPU_ERR_GEOMETRY = 7,     /* too few points for multigrid (reference: exit(1)) */
+  OLGPU_ERR_NO_DEVICE = 8
+} olgpu_status;
+
+typedef enum { OLGPU_EQ_PUNCTURES = 0, OLGPU_EQ_PUNCTURES_SCALAR = 1 } olgpu_equation;
+
+/* The Olliptic.x parameters of the puncture problem (src/interface.cc:73-273,
+ * 748-856); -L is the full domain length and dx = L/(N-1). */
+typedef struct {
+  int equation;                 /* olgpu_equation                       */
+  int numbh;                    /* -NumBH                               */
+  double mp[OLGPU_MAX_BH];      /* -bhmp<i>                             */
+  double x[OLGPU_MAX_BH], y[OLGPU_MAX_BH], z[OLGPU_MAX_BH];      /* -bhx<i> ... */
+  double px[OLGPU_MAX_BH], py[OLGPU_MAX_BH], pz[OLGPU_MAX_BH];   /* -bhpx<i> ...*/
+  double sx[OLGPU_MAX_BH], sy[OLGPU_MAX_BH], sz[OLGPU_MAX_BH];   /* -bhsx<i> ...*/
+  int n;                        /* -N                                   */
+  double L;                     /* -L                                   */
+  int order;                    /* -O  2, 4, 6 or 8                     */
+  int levels;                   /* -l                                   */
+  int nu1, nu2;                 /* -nu1, -nu2                           */
+  double tol;                   /* -s                                   */
+  int ps_case;                  /* -psc                                 */
+  double ps_phi0, ps_r0, ps_sigma, ps_a2;   /* -phi0 -r0 -sigma -a2     */
+} olgpu_problem;
+
+typedef struct {
+  int level, nx, ny, nz;        /* points per axis, ghost layers included */
+  int buf;                      /* ghost width max(order/2, 1)            */
+  int order;                    /* stencil order of this box              */
+  double xi, yi, zi;            /* coordinate of point (0,0,0)            */
+  double dx, dy, dz;
+  double cx, cy, cz;            /* box centre                             */
+} olgpu_box_info;
+
+/* Stop rules for olgpu_solve. */
+typedef enum {
+  OLGPU_STOP_REFERENCE = 0,     /* while res > tol && res < res_prev (src/elliptic.cc:1330) */
+  OLGPU_STOP_TOLERANCE = 1,     /* while res > tol                                          */
+  OLGPU_STOP_FIXED = 2          /* exactly max_cycles cycles                                */
+} olgpu_stop_kind;
+
+typedef struct {
+  int stop;                     /* olgpu_stop_kind                        */
+  int max_cycles;               /* hard cap on V-cycles (> 0)             */
+  double tol;                   /* <= 0: the problem's -s tolerance       */
+} olgpu_stop_rule;
+
+typedef struct {
+  int cycles;                   /* V-cycles run                           */
+  int status;                   /* olgpu_status of the solve              */
+  double final_res;             /* top-level residual norm of the last cycle */
+  double adm[OLGPU_MAX_BH];     /* ADM masses after the last cycle        */
+  double res[256];              /* per-cycle top-level norms (first 256)  */
+} olgpu_report;
+
+typedef struct olgpu_hierarchy olgpu_hierarchy;
+
+/* Default parameter values of Olliptic.x. */
+void olgpu_problem_defaults(olgpu_problem *p);
+
+/* Geometry only, no GPU needed: the boxes elliptic::Set_Grids builds for p
+ * (src/elliptic.cc:299-921), level-major.  Writes up to cap entries into out
+ * (out may be NULL) and the totals into the non-NULL count pointers. */
+olgpu_status olgpu_plan_boxes(const olgpu_problem *p, olgpu_box_info *out, int cap, int *nboxes,
+                              int *nlevels, int *mgrid_levels);
+
+/* Builds the nested-box hierarchy of the problem (Set_Grids), allocates every
+ * field in device memory, evaluates the coefficients and the initial guess
+ * u = 0 on the device.  device < 0 keeps the current device. */
+olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hierarchy **out);
+olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h);
+
+int olgpu_num_boxes(const olgpu_hierarchy *h);
+int olgpu_num_levels(const olgpu_hierarchy *h);
+int olgpu_mgrid_levels(const olgpu_hierarchy *h);
+olgpu_status olgpu_box(const olgpu_hierarchy *h, int box, olgpu_box_info *out);
+
+/* Field access by reference name: "u" "b" "c" "d" "e" "rho" (the source
+ * rho0), "r", "w", "ww", "v".  Host arrays hold nx*ny*nz doubles in
+ * lexicographic order, i fastest. */
+olgpu_status olgpu_upload(olgpu_hierarchy *h, int box, const char *field, const double *host);
+olgpu_status olgpu_download(olgpu_hierarchy *h, int box, const char *field, double *host);
+
+/* One FAS V-cycle from the finest level; *res receives the top-level norm. */
+olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res);
+/* Repeated V-cycles under a stop rule; rule NULL = the reference's rule. */
+olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out);
+olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
+
+/* Reset u to the initial guess (0) and the work fields, keeping the geometry
+ * and coefficients, so that one hierarchy can serve repeated solves. */
+olgpu_status olgpu_reset(olgpu_hierarchy *h);
+
+/* Timing aid: device time of the last olgpu_solve / olgpu_vcycle in ms. */
+double olgpu_last_device_ms(const olgpu_hierarchy *h);
+
+const char *olgpu_last_error(void);
+const char *olgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OLGPU_H */

@@ -1,0 +1,218 @@
+"""ollipticid_gb300 -- GB300-native FAS multigrid solve of the puncture
+Hamiltonian constraint on nested mesh-refinement boxes.
+
+Python host mirror of the reference's elliptic/multigrid surface
+(WuShichao/OllipticID include/elliptic.h, include/multigrid.h) over the C ABI
+of libolgpu.so (include/olgpu.h).  All numerical work runs in CUDA kernels on
+the GPU; there is no CPU path.  If the library cannot be built or loaded, or
+no GPU is present, constructing an `Elliptic` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List, Sequence
+
+import numpy as np
+
+from . import _abi
+from ._abi import OlgpuError, check
+
+__all__ = ["Problem", "Elliptic", "parse_olliptic_args", "OlgpuError", "FIELDS"]
+
+FIELDS = ("u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v")
+
+
+@dataclass
+class Problem:
+    """The Olliptic.x parameters of a puncture problem (src/interface.cc:73-273)."""
+    equation: str = "Punctures"          # or "Punctures_scalar_field"
+    mp: List[float] = field(default_factory=lambda: [0.0])
+    x: List[float] = field(default_factory=lambda: [0.0])
+    y: List[float] = field(default_factory=lambda: [0.0])
+    z: List[float] = field(default_factory=lambda: [0.0])
+    px: List[float] = field(default_factory=lambda: [0.0])
+    py: List[float] = field(default_factory=lambda: [0.0])
+    pz: List[float] = field(default_factory=lambda: [0.0])
+    sx: List[float] = field(default_factory=lambda: [0.0])
+    sy: List[float] = field(default_factory=lambda: [0.0])
+    sz: List[float] = field(default_factory=lambda: [0.0])
+    n: int = 30
+    L: float = 2.0
+    order: int = 4
+    levels: int = 1
+    nu1: int = 3
+    nu2: int = 3
+    tol: float = 1e-8
+    ps_case: int = 1
+    ps_phi0: float = 0.025
+    ps_r0: float = 120.0
+    ps_sigma: float = 8.0
+    ps_a2: float = 1.0
+
+    @property
+    def numbh(self) -> int:
+        return len(self.mp)
+
+    def to_c(self) -> _abi.Problem:
+        p = _abi.Problem()
+        p.equation = 0 if self.equation == "Punctures" else 1
+        p.numbh = self.numbh
+        if not 1 <= p.numbh <= _abi.MAX_BH:
+            raise ValueError("NumBH must be in 1..16")
+        for name in ("mp", "x", "y", "z", "px", "py", "pz", "sx", "sy", "sz"):
+            vals = list(getattr(self, name)) + [0.0] * _abi.MAX_BH
+            arr = getattr(p, name)
+            for i in range(_abi.MAX_BH):
+                arr[i] = float(vals[i]) if i < p.numbh else 0.0
+        for name in ("n", "order", "levels", "nu1", "nu2", "ps_case"):
+            setattr(p, name, int(getattr(self, name)))
+        for name in ("L", "tol", "ps_phi0", "ps_r0", "ps_sigma", "ps_a2"):
+            setattr(p, name, float(getattr(self, name)))
+        return p
+
+    def oracle_dict(self) -> dict:
+        d = {k: getattr(self, k) for k in ("mp", "x", "y", "z", "px", "py", "pz", "sx", "sy", "sz", "n", "L",
+                                           "order", "levels", "nu1", "nu2", "tol", "ps_case", "ps_phi0", "ps_r0",
+                                           "ps_sigma", "ps_a2")}
+        d["equation"] = 0 if self.equation == "Punctures" else 1
+        return d
+
+
+def parse_olliptic_args(argv: Sequence[str]) -> Problem:
+    """Olliptic.x command line -> Problem.  Flags outside the puncture FAS path
+    are accepted and ignored, as the reference ignores unknown flags."""
+    a = list(argv)
+    kv = {}
+    for i in range(len(a) - 1):
+        kv.setdefault(a[i], a[i + 1])
+
+    def get(keys, conv, default):
+        for k in keys:
+            if k in kv:
+                return conv(kv[k])
+        return default
+
+    eq = get(["-eq", "--equation"], str, "Punctures")
+    if eq not in ("Punctures", "Punctures_scalar_field"):
+        raise ValueError(f"equation {eq!r} is not on the puncture FAS path")
+    nb = get(["-NumBH", "--num-bh"], int, 1)
+    P = Problem(equation=eq)
+    for name, flag in (("mp", "-bhmp"), ("x", "-bhx"), ("y", "-bhy"), ("z", "-bhz"), ("px", "-bhpx"),
+                       ("py", "-bhpy"), ("pz", "-bhpz"), ("sx", "-bhsx"), ("sy", "-bhsy"), ("sz", "-bhsz")):
+        setattr(P, name, [get([f"{flag}{i + 1}"], float, 0.0) for i in range(nb)])
+    P.n = get(["-N", "-n"], int, 30)
+    P.L = get(["-L", "--length"], float, 2.0)
+    P.order = get(["-O", "--order"], int, 4)
+    P.levels = get(["-l", "--levels"], int, 1)
+    P.nu1 = get(["-nu1", "--pre-smooth"], int, 3)
+    P.nu2 = get(["-nu2", "--post-smooth"], int, 3)
+    P.tol = get(["-s", "--tolerance"], float, 1e-8)
+    P.ps_case = get(["-psc", "-ps_case"], int, 1)
+    P.ps_phi0 = get(["-phi0", "--phi0_sf"], float, 0.025)
+    P.ps_r0 = get(["-r0", "--radius_sf_r0"], float, 120.0)
+    P.ps_sigma = get(["-sigma", "--sigma_sf"], float, 8.0)
+    P.ps_a2 = get(["-a2", "--a2_sf"], float, 1.0)
+    return P
+
+
+@dataclass
+class Box:
+    level: int
+    n: tuple
+    buf: int
+    order: int
+    origin: tuple
+    d: tuple
+    center: tuple
+
+
+class Elliptic:
+    """Device-resident hierarchy of one puncture problem (elliptic::elliptic,
+    src/elliptic.cc:30-221) with the reference's solve entry points."""
+
+    def __init__(self, problem: Problem, device: int = 0):
+        self.lib = _abi.load()
+        self.problem = problem
+        self._cp = problem.to_c()
+        h = C.c_void_p()
+        check(self.lib.olgpu_hierarchy_create(C.byref(self._cp), int(device), C.byref(h)))
+        self._h = h
+        self.levels = self.lib.olgpu_num_levels(h)
+        self.mgrid_levels = self.lib.olgpu_mgrid_levels(h)
+        self.boxes: List[Box] = []
+        for g in range(self.lib.olgpu_num_boxes(h)):
+            bi = _abi.BoxInfo()
+            check(self.lib.olgpu_box(h, g, C.byref(bi)))
+            self.boxes.append(Box(bi.level, (bi.nx, bi.ny, bi.nz), bi.buf, bi.order, (bi.xi, bi.yi, bi.zi),
+                                  (bi.dx, bi.dy, bi.dz), (bi.cx, bi.cy, bi.cz)))
+        self.last_report = None
+
+    # -- lifecycle ----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.olgpu_hierarchy_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- geometry -----------------------------------------------------------
+    def Get_num_dom(self, level: int) -> int:
+        return sum(1 for b in self.boxes if b.level == level)
+
+    def box_index(self, level: int, ibox: int) -> int:
+        return [g for g, b in enumerate(self.boxes) if b.level == level][ibox]
+
+    # -- fields -------------------------------------------------------------
+    def get_field(self, box: int, name: str = "u") -> np.ndarray:
+        nx, ny, nz = self.boxes[box].n
+        out = np.empty((nz, ny, nx), dtype=np.float64)
+        check(self.lib.olgpu_download(self._h, box, name.encode(), out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def set_field(self, box: int, name: str, values: np.ndarray):
+        nx, ny, nz = self.boxes[box].n
+        arr = np.ascontiguousarray(values, dtype=np.float64).reshape(nz, ny, nx)
+        check(self.lib.olgpu_upload(self._h, box, name.encode(), arr.ctypes.data_as(C.c_void_p)))
+
+    def Get_ffunction(self, level: int, ibox: int, name: str = "u") -> np.ndarray:
+        return self.get_field(self.box_index(level, ibox), name)
+
+    # -- solve --------------------------------------------------------------
+    def FASN(self) -> float:
+        """One V-cycle from the finest level (elliptic::FASN)."""
+        r = C.c_double()
+        check(self.lib.olgpu_vcycle(self._h, C.byref(r)))
+        return r.value
+
+    def Solve(self, stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000, tol: float = 0.0) -> "_abi.Report":
+        """elliptic::Solve -> Vcycle with the reference stop rule by default."""
+        rule = _abi.StopRule(stop, max_cycles, tol)
+        rep = _abi.Report()
+        st = self.lib.olgpu_solve(self._h, C.byref(rule), C.byref(rep))
+        self.last_report = rep
+        check(st)
+        return rep
+
+    def reset(self):
+        check(self.lib.olgpu_reset(self._h))
+
+    @property
+    def ADM_mass(self) -> List[float]:
+        out = (C.c_double * _abi.MAX_BH)()
+        check(self.lib.olgpu_adm_mass(self._h, out))
+        return [out[i] for i in range(self.problem.numbh)]
+
+    @property
+    def last_device_ms(self) -> float:
+        return self.lib.olgpu_last_device_ms(self._h)

@@ -1,0 +1,77 @@
+// device.cuh -- data layout shared by the host driver and the kernels.
+//
+// Every field of every box lives in one device arena: field f of box g
+// starts at arena + f * total_points + box[g].off and is stored
+// lexicographically (i fastest) with the ghost layers included, so that a
+// point's neighbours along x, y, z are at +-1, +-nx, +-nx*ny.
+#pragma once
+
+#include <cstdint>
+
+namespace olgpu {
+
+// F_T is a work field of the device solver (full-weighted W), not a
+// reference field.
+enum Field { F_U = 0, F_B, F_C, F_D, F_E, F_RHO, F_R, F_W, F_WW, F_V, F_T, F_NUM };
+
+constexpr int kMaxBoxesPerLevel = 32;
+constexpr int kMaxInterpPoints = 10;   // Lagrange order 9 (order 8 ghosts)
+
+struct DevBox {
+  int n[3];
+  int buf;
+  int order;
+  int level;
+  long long off;        // element offset inside each field arena
+  int coord_off;        // offset of this box's x, y, z tables in coords[]
+  int pad;
+  double idx[3];        // 1/dx
+  double idx2[3];       // 1/dx^2
+  double dulap;         // diagonal of the Laplacian stencil
+};
+
+struct DevFields {
+  double *f[F_NUM];
+};
+
+// Boxes of one level handled by one launch; blocks are split between boxes
+// by the prefix sums in blk.
+struct BoxList {
+  int first;
+  int count;
+  int blk[kMaxBoxesPerLevel + 1];
+};
+
+// Interpolation table entry for one target index along one axis.
+struct AxisEntry {
+  int sel;        // the target coordinate is inside the source (nb or all)
+  int exact;      // coincides with source node `node` (3-epsilon test)
+  int node;       // source node for the exact copy
+  int start;      // first source index of the interpolation window
+  double w[kMaxInterpPoints];
+};
+
+enum XferMethod { XM_LINEAR = 0, XM_LAGRANGE = 1, XM_COPY = 2 };
+enum IterKind { IT_ALL = 0, IT_INSIDE = 1, IT_BOUNDARY = 2 };
+
+// One (target box, source box, target sub-region) piece of a transfer.
+struct XferJob {
+  int tbox, sbox;
+  int tfield, sfield;
+  int method, ord, to_zero, iter;
+  int r0[3], r1[3];     // visited target index box [r0, r1)
+  int tab[3];           // AxisEntry offset of target index 0 on each axis
+  long long blk0;       // first block of this job in the launch
+};
+
+struct PunctureParams {
+  int numbh;
+  int equation;
+  int ps_case;
+  int pad;
+  double mp[16], x[16], y[16], z[16];
+  double px[16], py[16], pz[16], sx[16], sy[16], sz[16];
+  double ps_phi0, ps_r0, ps_isigma, ps_d1, ps_e1, ps_e2, ps_de1;
+};
+
+}  // namespace olgpu

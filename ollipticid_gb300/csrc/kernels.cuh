@@ -1,0 +1,757 @@
+// kernels.cuh -- sm_103a kernels of the FP64 puncture FAS V-cycle.
+//
+// Reference path (WuShichao/OllipticID):
+//   smoother          elliptic::Smooth              src/elliptic.cc:1126-1242
+//   operator          puncture_OP / puncture_duOP   include/elliptic.h:405-445
+//   stencils          Lapc2/4/6/8, duLapc*          include/ffunction.h:1290-1524,
+//                                                   src/diff_4th.cc:392-410, src/diff_8th.cc:596-674
+//   Robin boundary    App_Bound, Boundary_*         src/boundary.cc:447-1101
+//   Robin operator    App_Boundary_Operator         src/boundary.cc:1118-1710
+//   one-sided d/dx    dx2, dx4 (+ du*)              src/diff_2nd.cc:238-335, src/diff_4th.cc:6-89
+//   residual          App_Ell_Operator              src/elliptic.cc:943-991
+//   transfers         Transferir, Set_In            src/ffunction.cc:2435-2849
+//   interpolation     Lagrange/Linear_Interpol_In   src/interpolation.cc:124-375
+//   coefficients      punctures_b/_c, scalar d/e    src/operator.cc:2193-2380
+//
+// The smoother is multicolour (red-black for order 2) instead of
+// lexicographic: every colour pass updates its points in parallel.  That
+// changes the iterates but not the discrete fixed point, which is what the
+// solver is compared on.
+#pragma once
+
+#include "device.cuh"
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+namespace olgpu {
+
+__device__ __forceinline__ long long pidx(const DevBox &B, int i, int j, int k)
+{
+  return ((long long)k * B.n[1] + j) * B.n[0] + i;
+}
+
+// Finds the box of this block inside a BoxList launch.
+__device__ __forceinline__ int list_box(const BoxList &L, long long &local_block)
+{
+  int b = 0;
+  while (b + 1 < L.count && (long long)blockIdx.x >= L.blk[b + 1]) b++;
+  local_block = (long long)blockIdx.x - L.blk[b];
+  return L.first + b;
+}
+
+// ----------------------------------------------------------------------------
+// stencils
+// ----------------------------------------------------------------------------
+template <int ORD>
+__device__ __forceinline__ double lap(const double *__restrict__ u, long long p, long long sy,
+                                      long long sz, const DevBox &B)
+{
+  const double c = u[p];
+  const double ix2 = B.idx2[0], iy2 = B.idx2[1], iz2 = B.idx2[2];
+  if (ORD == 2) {
+    return (u[p + 1] - 2.0 * c + u[p - 1]) * ix2 + (u[p + sy] - 2.0 * c + u[p - sy]) * iy2 +
+           (u[p + sz] - 2.0 * c + u[p - sz]) * iz2;
+  } else if (ORD == 4) {
+    return ((-(u[p + 2] + u[p - 2]) + 16.0 * (u[p + 1] + u[p - 1]) - 30.0 * c) * ix2 +
+            (-(u[p + 2 * sy] + u[p - 2 * sy]) + 16.0 * (u[p + sy] + u[p - sy]) - 30.0 * c) * iy2 +
+            (-(u[p + 2 * sz] + u[p - 2 * sz]) + 16.0 * (u[p + sz] + u[p - sz]) - 30.0 * c) * iz2) /
+           12.0;
+  } else if (ORD == 6) {
+    const double i180 = 1.0 / 180;
+    return (2.0 * (u[p + 3] + u[p - 3]) - 27.0 * (u[p + 2] + u[p - 2] - 10.0 * (u[p + 1] + u[p - 1])) -
+            490.0 * c) * ix2 * i180 +
+           (2.0 * (u[p + 3 * sy] + u[p - 3 * sy]) -
+            27.0 * (u[p + 2 * sy] + u[p - 2 * sy] - 10.0 * (u[p + sy] + u[p - sy])) - 490.0 * c) * iy2 * i180 +
+           (2.0 * (u[p + 3 * sz] + u[p - 3 * sz]) -
+            27.0 * (u[p + 2 * sz] + u[p - 2 * sz] - 10.0 * (u[p + sz] + u[p - sz])) - 490.0 * c) * iz2 * i180;
+  } else {
+    return (-9.0 * (u[p + 4] + u[p - 4]) + 128.0 * (u[p + 3] + u[p - 3]) - 1008.0 * (u[p + 2] + u[p - 2]) +
+            8064.0 * (u[p + 1] + u[p - 1]) - 14350.0 * c) * ix2 / 5040.0 +
+           (-9.0 * (u[p + 4 * sy] + u[p - 4 * sy]) + 128.0 * (u[p + 3 * sy] + u[p - 3 * sy]) -
+            1008.0 * (u[p + 2 * sy] + u[p - 2 * sy]) + 8064.0 * (u[p + sy] + u[p - sy]) - 14350.0 * c) * iy2 / 5040.0 +
+           (-9.0 * (u[p + 4 * sz] + u[p - 4 * sz]) + 128.0 * (u[p + 3 * sz] + u[p - 3 * sz]) -
+            1008.0 * (u[p + 2 * sz] + u[p - 2 * sz]) + 8064.0 * (u[p + sz] + u[p - sz]) - 14350.0 * c) * iz2 / 5040.0;
+  }
+}
+
+// Pointwise operator value and its derivative in u (puncture, optionally with
+// the scalar-field terms d (c+u) + e (c+u)^5).  Integer powers by products;
+// one division.
+template <int EQ>
+__device__ __forceinline__ void point_op(double lapv, double dl, double uu, double bb, double cc,
+                                         double dd, double ee, double &op, double &dop)
+{
+  const double q = cc + uu;
+  const double iq = 1.0 / q;
+  const double iq2 = iq * iq;
+  const double iq4 = iq2 * iq2;
+  const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
+  op = lapv + t7;
+  dop = dl - 7.0 * t7 * iq;                  // -7 b / (c+u)^8
+  if (EQ == 1) {
+    const double q2 = q * q;
+    const double q4 = q2 * q2;
+    op = op + dd * q + ee * (q4 * q);
+    dop = dop + dd + 5.0 * ee * q4;
+  }
+}
+
+// One-sided first derivative for the Robin condition: dx2 for order 2
+// (one-sided 2nd order at the ends, centred inside), dx4 for orders 4/6/8
+// (5-point one-sided pointing inward).
+template <int ORD>
+__device__ __forceinline__ double deriv(const double *__restrict__ u, long long p, long long s, int i,
+                                        int n, double id, double &du)
+{
+  if (ORD == 2) {
+    if (i == 0) {
+      du = -3.0 * 0.5 * id;
+      return (-3.0 * u[p] + 4.0 * u[p + s] - u[p + 2 * s]) * 0.5 * id;
+    }
+    if (i == n - 1) {
+      du = 3.0 * 0.5 * id;
+      return (3.0 * u[p] - 4.0 * u[p - s] + u[p - 2 * s]) * 0.5 * id;
+    }
+    du = 0.0;
+    return (u[p + s] - u[p - s]) * 0.5 * id;
+  } else {
+    const int nm = n % 2 == 0 ? n / 2 : (n - 1) / 2;
+    if (i <= nm) {
+      du = -25 * id / 12.0;
+      return (-(25 * u[p] - 48 * u[p + s] + 36 * u[p + 2 * s] - 16 * u[p + 3 * s] + 3 * u[p + 4 * s]) * id / 12.0);
+    }
+    du = 25 * id / 12.0;
+    return ((25 * u[p] - 48 * u[p - s] + 36 * u[p - 2 * s] - 16 * u[p - 3 * s] + 3 * u[p - 4 * s]) * id / 12.0);
+  }
+}
+
+// Robin term r^2/n * sum_a (du/dx_a)/x_a for the axes in mask (n = 1), grouped
+// like Boundary_Face (one axis) and Boundary_Edge/Corner (two/three axes).
+template <int ORD>
+__device__ __forceinline__ double robin_term(const double *__restrict__ u, const DevBox &B,
+                                             const double *__restrict__ crd, int mask, int i, int j,
+                                             int k, double &dF)
+{
+  const double x = crd[B.coord_off + i];
+  const double y = crd[B.coord_off + B.n[0] + j];
+  const double z = crd[B.coord_off + B.n[0] + B.n[1] + k];
+  const double r2 = x * x + y * y + z * z;
+  const long long p = pidx(B, i, j, k);
+  const long long st[3] = {1, (long long)B.n[0], (long long)B.n[0] * B.n[1]};
+  const int ijk[3] = {i, j, k};
+  const double xyz[3] = {x, y, z};
+  double t = 0.0, dt = 0.0;
+  int na = 0;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (!(mask & (1 << a))) continue;
+    double du;
+    const double dv = deriv<ORD>(u, p, st[a], ijk[a], B.n[a], B.idx[a], du);
+    if (na == 0 && mask == (1 << a)) {          // face
+      dF = r2 * du / xyz[a] + 1.0;
+      return r2 * dv / xyz[a];
+    }
+    t = na == 0 ? dv / xyz[a] : t + dv / xyz[a];
+    dt = na == 0 ? du / xyz[a] : dt + du / xyz[a];
+    na++;
+  }
+  dF = r2 * dt + 1.0;
+  return r2 * t;
+}
+
+// mode 0: Newton update u -= F/dF with F = term + u - S   (App_Bound)
+// mode 1: R = term + u                                     (App_Boundary_Operator)
+template <int ORD>
+__device__ __forceinline__ void robin_point(const DevBox &B, const DevFields &F,
+                                            const double *__restrict__ crd, int mode, int mask, int i,
+                                            int j, int k)
+{
+  double *u = F.f[F_U] + B.off;
+  const long long p = pidx(B, i, j, k);
+  double dF;
+  const double t = robin_term<ORD>(u, B, crd, mask, i, j, k, dF);
+  if (mode == 0) {
+    const double Fv = t + u[p] - F.f[F_RHO][B.off + p];
+    u[p] = u[p] - Fv / dF;
+  } else {
+    F.f[F_R][B.off + p] = t + u[p];
+  }
+}
+
+// ----------------------------------------------------------------------------
+// reductions
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void block_max_atomic(double v, unsigned long long *slot)
+{
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    v = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0 && v > 0.0) atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// ----------------------------------------------------------------------------
+// K1: multicolour nonlinear Gauss-Seidel-Newton pass.  Colour of a point is
+// (i + j + k) mod NC with NC = ORD/2 + 1, so that no two points of a colour
+// are within the stencil reach of each other: a colour pass is a true
+// Gauss-Seidel pass in any thread order (red-black for order 2).
+// ----------------------------------------------------------------------------
+template <int ORD>
+__host__ __device__ constexpr int num_colors() { return ORD / 2 + 1; }
+
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *__restrict__ boxes,
+                                                      DevFields F, int color,
+                                                      unsigned long long *norm_slot, int *nan_flag)
+{
+  constexpr int NC = num_colors<ORD>();
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
+  const int H = (m0 + NC - 1) / NC;
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long total = (long long)H * m1 * m2;
+  double rabs = 0.0;
+  if (t < total) {
+    const int ih = (int)(t % H);
+    const long long r = t / H;
+    const int j = b + (int)(r % m1);
+    const int k = b + (int)(r / m1);
+    const int delta = (((color - b - j - k) % NC) + NC) % NC;
+    const int i = b + delta + NC * ih;
+    if (i < B.n[0] - b) {
+      double *u = F.f[F_U] + B.off;
+      const long long sy = B.n[0], sz = (long long)B.n[0] * B.n[1];
+      const long long p = pidx(B, i, j, k);
+      const double lv = lap<ORD>(u, p, sy, sz, B);
+      double op, dop;
+      point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
+                   EQ ? F.f[F_D][B.off + p] : 0.0, EQ ? F.f[F_E][B.off + p] : 0.0, op, dop);
+      const double R = op - F.f[F_RHO][B.off + p];
+      const double un = u[p] - R / dop;
+      u[p] = un;
+      rabs = fabs(R);
+      if (!(un == un)) atomicOr(nan_flag, 1);
+    }
+  }
+  block_max_atomic(rabs, norm_slot);
+}
+
+// R = OP(u) on the INSIDE points (App_Ell_Operator).
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_apply_op(BoxList L, const DevBox *__restrict__ boxes, DevFields F)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
+  const long long t = lb * blockDim.x + threadIdx.x;
+  if (t >= (long long)m0 * m1 * m2) return;
+  const int i = b + (int)(t % m0);
+  const long long r = t / m0;
+  const int j = b + (int)(r % m1);
+  const int k = b + (int)(r / m1);
+  const double *u = F.f[F_U] + B.off;
+  const long long p = pidx(B, i, j, k);
+  const double lv = lap<ORD>(u, p, B.n[0], (long long)B.n[0] * B.n[1], B);
+  double op, dop;
+  point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
+               EQ ? F.f[F_D][B.off + p] : 0.0, EQ ? F.f[F_E][B.off + p] : 0.0, op, dop);
+  F.f[F_R][B.off + p] = op;
+}
+
+// ----------------------------------------------------------------------------
+// Robin boundary: faces (one thread per normal column, layers inner -> outer)
+// ----------------------------------------------------------------------------
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin_faces(BoxList L, const DevBox *__restrict__ boxes,
+                                                     DevFields F, const double *__restrict__ crd, int mode)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  long long t = lb * blockDim.x + threadIdx.x;
+  for (int f = 0; f < 6; f++) {
+    const int a = f >> 1, hi = f & 1;
+    const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+    const int m1 = B.n[a1] - 2 * b, m2 = B.n[a2] - 2 * b;
+    const long long cols = (long long)m1 * m2;
+    if (t < cols) {
+      int ijk[3];
+      ijk[a1] = b + (int)(t % m1);
+      ijk[a2] = b + (int)(t / m1);
+      for (int l = 0; l < b; l++) {
+        ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
+        robin_point<ORD>(B, F, crd, mode, 1 << a, ijk[0], ijk[1], ijk[2]);
+      }
+      return;
+    }
+    t -= cols;
+  }
+}
+
+// Edges then corners of one box per block.
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin_edges_corners(BoxList L, const DevBox *__restrict__ boxes,
+                                                             DevFields F, const double *__restrict__ crd,
+                                                             int mode)
+{
+  const DevBox B = boxes[L.first + blockIdx.x];
+  const int b = B.buf;
+  const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int pi = 0; pi < 3; pi++) {
+    const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
+    const int m = B.n[fa] - 2 * b;
+    for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
+      const int e = t / m, q = t % m;
+      const int ha = e >> 1, hc = e & 1;
+      int ijk[3];
+      ijk[fa] = b + q;
+      for (int ta = 0; ta < b; ta++)
+        for (int tc = 0; tc < b; tc++) {
+          ijk[a] = ha ? B.n[a] - b + ta : b - 1 - ta;
+          ijk[c] = hc ? B.n[c] - b + tc : b - 1 - tc;
+          robin_point<ORD>(B, F, crd, mode, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+        }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
+    for (int tk = 0; tk < b; tk++)
+      for (int tj = 0; tj < b; tj++)
+        for (int ti = 0; ti < b; ti++) {
+          const int i = hx ? B.n[0] - b + ti : b - 1 - ti;
+          const int j = hy ? B.n[1] - b + tj : b - 1 - tj;
+          const int k = hz ? B.n[2] - b + tk : b - 1 - tk;
+          robin_point<ORD>(B, F, crd, mode, 7, i, j, k);
+        }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// element-wise field updates over ALL points of a level
+// ----------------------------------------------------------------------------
+enum EwOp { EW_W_EQ_S_MINUS_R = 0, EW_S_EQ_W_PLUS_R, EW_W_PLUS_EQ_R, EW_WW_EQ_U, EW_V_EQ_U_MINUS_WW,
+            EW_U_PLUS_EQ_V };
+
+__global__ void __launch_bounds__(256) k_elementwise(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                     int op)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const long long p = B.off + t;
+  switch (op) {
+  case EW_W_EQ_S_MINUS_R: F.f[F_W][p] = F.f[F_RHO][p] - F.f[F_R][p]; break;
+  case EW_S_EQ_W_PLUS_R: F.f[F_RHO][p] = F.f[F_W][p] + F.f[F_R][p]; break;
+  case EW_W_PLUS_EQ_R: F.f[F_W][p] = F.f[F_W][p] + F.f[F_R][p]; break;
+  case EW_WW_EQ_U: F.f[F_WW][p] = F.f[F_U][p]; break;
+  case EW_V_EQ_U_MINUS_WW: F.f[F_V][p] = F.f[F_U][p] - F.f[F_WW][p]; break;
+  case EW_U_PLUS_EQ_V: F.f[F_U][p] = F.f[F_U][p] + F.f[F_V][p]; break;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// T = W averaged with (1,2,1)^3/64 weights on INSIDE points (a neighbour
+// outside INSIDE contributes the centre value), T = W elsewhere.  The tau
+// defect W is then moved to the coarse level from T: with a multicolour
+// smoother the defect alternates in sign between colours, and the reference's
+// injection would hand the coarse level a single colour.  W vanishes at the
+// fixed point, so the averaging changes the path, not the solution.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_full_weight(BoxList L, const DevBox *__restrict__ boxes, DevFields F)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int b = B.buf;
+  const int i = (int)(t % B.n[0]);
+  const long long r = t / B.n[0];
+  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const double *w = F.f[F_W] + B.off;
+  const double c = w[t];
+  const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
+  if (!inside) {
+    F.f[F_T][B.off + t] = c;
+    return;
+  }
+  double acc = 0.0;
+  for (int dk = -1; dk <= 1; dk++)
+    for (int dj = -1; dj <= 1; dj++)
+      for (int di = -1; di <= 1; di++) {
+        const int ii = i + di, jj = j + dj, kk = k + dk;
+        const double wt = (double)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (1.0 / 64.0);
+        const bool in = ii >= b && ii < B.n[0] - b && jj >= b && jj < B.n[1] - b && kk >= b && kk < B.n[2] - b;
+        acc += wt * (in ? w[pidx(B, ii, jj, kk)] : c);
+      }
+  F.f[F_T][B.off + t] = acc;
+}
+
+// ----------------------------------------------------------------------------
+// generic inter-box transfer (restriction, tau transfer, prolongation, ghost
+// fill, tau mask) driven by host-built per-axis interpolation tables
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_transfer(const XferJob *__restrict__ jobs, int njobs,
+                                                  const DevBox *__restrict__ boxes, DevFields F,
+                                                  const AxisEntry *__restrict__ tab)
+{
+  int jb = 0;
+  {
+    int lo = 0, hi = njobs - 1;   // last job with blk0 <= blockIdx.x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+      else hi = mid - 1;
+    }
+    jb = lo;
+  }
+  const XferJob J = jobs[jb];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox T = boxes[J.tbox];
+  if (J.iter != IT_ALL) {
+    const int b = T.buf;
+    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+    if ((J.iter == IT_INSIDE) != inside) return;
+  }
+  double *dst = F.f[J.tfield] + T.off;
+  const long long tp = pidx(T, i, j, k);
+  const AxisEntry &ax = tab[J.tab[0] + i];
+  const AxisEntry &ay = tab[J.tab[1] + j];
+  const AxisEntry &az = tab[J.tab[2] + k];
+  if (!(ax.sel && ay.sel && az.sel)) {
+    if (J.to_zero) dst[tp] = 0.0;
+    return;
+  }
+  const DevBox S = boxes[J.sbox];
+  const double *src = F.f[J.sfield] + S.off;
+  if (J.method == XM_COPY || (ax.exact && ay.exact && az.exact)) {
+    dst[tp] = src[pidx(S, ax.node, ay.node, az.node)];
+    return;
+  }
+  if (J.method == XM_LINEAR) {
+    // ((v000 dxi + v100 dxf) dyi + (v010 dxi + v110 dxf) dyf) dzi + (...) dzf
+    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
+    const double dxi = ax.w[0], dxf = ax.w[1], dyi = ay.w[0], dyf = ay.w[1], dzi = az.w[0], dzf = az.w[1];
+    const double v000 = src[pidx(S, i0, j0, k0)], v100 = src[pidx(S, i0 + 1, j0, k0)];
+    const double v010 = src[pidx(S, i0, j0 + 1, k0)], v110 = src[pidx(S, i0 + 1, j0 + 1, k0)];
+    const double v001 = src[pidx(S, i0, j0, k0 + 1)], v101 = src[pidx(S, i0 + 1, j0, k0 + 1)];
+    const double v011 = src[pidx(S, i0, j0 + 1, k0 + 1)], v111 = src[pidx(S, i0 + 1, j0 + 1, k0 + 1)];
+    dst[tp] = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
+              ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
+    return;
+  }
+  // tensor Lagrange: z innermost, then y, then x
+  const int ord = J.ord;
+  double fx = 0.0;
+  for (int I = 0; I <= ord; I++) {
+    double uy = 0.0;
+    for (int Jj = 0; Jj <= ord; Jj++) {
+      double uz = 0.0;
+      const double *col = src + pidx(S, ax.start + I, ay.start + Jj, az.start);
+      const long long sz = (long long)S.n[0] * S.n[1];
+      for (int K = 0; K <= ord; K++) uz += col[K * sz] * az.w[K];
+      uy += uz * ay.w[Jj];
+    }
+    fx += uy * ax.w[I];
+  }
+  dst[tp] = fx;
+}
+
+// ----------------------------------------------------------------------------
+// K5: coarsest-grid solve in one CTA: repeat { Robin; one red-black sweep }
+// until the sweep norm <= eps or stops changing (src/elliptic.cc:1782-1816),
+// or drops below rtol times the first sweep's norm, or max_it sweeps ran.
+// The interior update is over-relaxed (red-black SOR): only the coarse
+// problem's solution enters the V-cycle, not the sweep that reaches it.
+// u lives in shared memory; b, c, S (and d, e) are read through L1.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void cs_robin_point(const DevBox &B, double *u, const double *rho,
+                                               const double *crd, int mask, int i, int j, int k)
+{
+  const long long p = pidx(B, i, j, k);
+  double dF;
+  const double t = robin_term<2>(u, B, crd, mask, i, j, k, dF);
+  const double Fv = t + u[p] - rho[p];
+  u[p] = u[p] - Fv / dF;
+}
+
+template <int EQ>
+__global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict__ boxes, int box, DevFields F,
+                                                       const double *__restrict__ crd, double eps, int max_it,
+                                                       double omega, double rtol, double *norm_out,
+                                                       int *iters_out, int *nan_flag)
+{
+  extern __shared__ double su[];
+  __shared__ double red[32];
+  __shared__ double s_norm;
+  __shared__ int s_nan;
+  const DevBox B = boxes[box];
+  const long long np = (long long)B.n[0] * B.n[1] * B.n[2];
+  double *gu = F.f[F_U] + B.off;
+  const double *gb = F.f[F_B] + B.off, *gc = F.f[F_C] + B.off, *gs = F.f[F_RHO] + B.off;
+  const double *gd = EQ ? F.f[F_D] + B.off : nullptr, *ge = EQ ? F.f[F_E] + B.off : nullptr;
+  for (long long p = threadIdx.x; p < np; p += blockDim.x) su[p] = gu[p];
+  __syncthreads();
+  const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+  const int m0 = n0 - 2, m1 = n1 - 2, m2 = n2 - 2;   // ghost width 1 on coarse grids
+  const long long sy = n0, sz = (long long)n0 * n1;
+  double norm = 1.0, prev, first = -1.0;
+  int it = 0;
+  do {
+    prev = norm;
+    // Robin update: faces, edges, corners
+    for (int f = 0; f < 6; f++) {
+      const int a = f >> 1, hi = f & 1, a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+      const int c1 = B.n[a1] - 2, c2 = B.n[a2] - 2;
+      for (int t = threadIdx.x; t < c1 * c2; t += blockDim.x) {
+        int ijk[3];
+        ijk[a] = hi ? B.n[a] - 1 : 0;
+        ijk[a1] = 1 + t % c1;
+        ijk[a2] = 1 + t / c1;
+        cs_robin_point(B, su, gs, crd, 1 << a, ijk[0], ijk[1], ijk[2]);
+      }
+    }
+    __syncthreads();
+    {
+      const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+      for (int pi = 0; pi < 3; pi++) {
+        const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
+        const int m = B.n[fa] - 2;
+        for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
+          const int e = t / m, q = t % m;
+          int ijk[3];
+          ijk[fa] = 1 + q;
+          ijk[a] = (e >> 1) ? B.n[a] - 1 : 0;
+          ijk[c] = (e & 1) ? B.n[c] - 1 : 0;
+          cs_robin_point(B, su, gs, crd, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+      const int i = (threadIdx.x & 1) ? n0 - 1 : 0;
+      const int j = ((threadIdx.x >> 1) & 1) ? n1 - 1 : 0;
+      const int k = (threadIdx.x >> 2) ? n2 - 1 : 0;
+      cs_robin_point(B, su, gs, crd, 7, i, j, k);
+    }
+    __syncthreads();
+    // one red-black sweep
+    double rmax = 0.0;
+    const int H = (m0 + 1) / 2;
+    for (int color = 0; color < 2; color++) {
+      for (int t = threadIdx.x; t < H * m1 * m2; t += blockDim.x) {
+        const int ih = t % H, r = t / H;
+        const int j = 1 + r % m1, k = 1 + r / m1;
+        const int i = 1 + ((color + 1 + j + k) & 1) + 2 * ih;
+        if (i >= n0 - 1) continue;
+        const long long p = pidx(B, i, j, k);
+        const double lv = lap<2>(su, p, sy, sz, B);
+        double op, dop;
+        point_op<EQ>(lv, B.dulap, su[p], gb[p], gc[p], EQ ? gd[p] : 0.0, EQ ? ge[p] : 0.0, op, dop);
+        const double R = op - gs[p];
+        su[p] = su[p] - omega * (R / dop);
+        rmax = fmax(rmax, fabs(R));
+        if (!(su[p] == su[p])) atomicOr(nan_flag, 1);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = rmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmax(m, red[w]);
+      s_norm = m;
+      s_nan = *(volatile int *)nan_flag;
+    }
+    __syncthreads();
+    norm = s_norm;
+    const int stop_nan = s_nan;
+    __syncthreads();
+    it++;
+    if (first < 0.0) first = norm;
+    if (stop_nan) break;                           // uniform across the block
+    if (rtol > 0.0 && norm <= rtol * first) break;
+  } while (norm > eps && prev != norm && it < max_it);
+  for (long long p = threadIdx.x; p < np; p += blockDim.x) gu[p] = su[p];
+  if (threadIdx.x == 0) {
+    *norm_out = norm;
+    *iters_out = it;
+  }
+}
+
+// ----------------------------------------------------------------------------
+// K6: coefficients b, c (and d, e) at every point of every box
+// ----------------------------------------------------------------------------
+__device__ double dev_punctures_c(const PunctureParams &P, double X, double Y, double Z)
+{
+  double cval = 1;
+  for (int i = 0; i < P.numbh; i++) {
+    const double x = X - P.x[i], y = Y - P.y[i], z = Z - P.z[i];
+    double r = sqrt(x * x + y * y + z * z);
+    if (r < 2 * 2.220446049250313e-16) r = 2 * 2.220446049250313e-16;
+    cval += 0.5 * P.mp[i] / r;
+  }
+  return cval;
+}
+
+__device__ double dev_punctures_b(const PunctureParams &P, double X, double Y, double Z)
+{
+  double A00 = 0, A11 = 0, A22 = 0, A01 = 0, A02 = 0, A12 = 0;
+  for (int i = 0; i < P.numbh; i++) {
+    const double x = X - P.x[i], y = Y - P.y[i], z = Z - P.z[i];
+    const double x2 = x * x, y2 = y * y, z2 = z * z;
+    double r2 = x2 + y2 + z2;
+    if (r2 < 2 * 2.220446049250313e-16) r2 = 2 * 2.220446049250313e-16;
+    const double r = sqrt(r2);
+    const double ir5 = 1.0 / (r2 * r2 * r);
+    const double px = P.px[i], py = P.py[i], pz = P.pz[i], sx = P.sx[i], sy = P.sy[i], sz = P.sz[i];
+    A00 += 1.5 * ir5 * (px * x * (x2 + r2) + py * y * (x2 - r2) + pz * z * (x2 - r2) + 4.0 * x * (sy * z - sz * y));
+    A11 += 1.5 * ir5 * (px * x * (y2 - r2) + py * y * (y2 + r2) + pz * z * (y2 - r2) + 4.0 * y * (sz * x - sx * z));
+    A22 += 1.5 * ir5 * (px * x * (z2 - r2) + py * y * (z2 - r2) + pz * z * (z2 + r2) + 4.0 * z * (sx * y - sy * x));
+    A01 += 1.5 * ir5 * (px * y * (r2 + x2) + py * x * (r2 + y2) + pz * x * y * z - 2.0 * sx * x * z +
+                        2.0 * sy * y * z + 2.0 * sz * (x2 - y2));
+    A02 += 1.5 * ir5 * (px * z * (r2 + x2) + py * x * y * z + pz * x * (r2 + z2) + 2.0 * sx * x * y +
+                        2.0 * sy * (z2 - x2) - 2.0 * sz * y * z);
+    A12 += 1.5 * ir5 * (px * x * y * z + py * z * (r2 + y2) + pz * y * (r2 + z2) + 2.0 * sx * (y2 - z2) -
+                        2.0 * sy * x * y + 2.0 * sz * x * z);
+  }
+  // sum over i,j of A_ij^2 in row-major order
+  double bval = 0.0;
+  bval += A00 * A00; bval += A01 * A01; bval += A02 * A02;
+  bval += A01 * A01; bval += A11 * A11; bval += A12 * A12;
+  bval += A02 * A02; bval += A12 * A12; bval += A22 * A22;
+  return 0.125 * bval;
+}
+
+__device__ double dev_scalar_d(const PunctureParams &P, double X, double Y, double Z)
+{
+  const double r = sqrt(X * X + Y * Y + Z * Z);
+  const double r0 = P.ps_r0, is = P.ps_isigma;
+  switch (P.ps_case) {
+  case 1: return P.ps_d1 / pow(cosh((r - r0) * is), 4.0);
+  case 2: return P.ps_de1 * (r - r0) * (r - r0) * exp(-2 * is * (r - r0) * (r - r0));
+  case 3: {
+    const double l2 = 10000, x = r;
+    const double s = 0.0581545 * (x - 1.8039e-08) * 0.0481646 * exp(-0.0581545 * (x - 1.8039e-08) * (x - 1.8039e-08) / l2) +
+                     0.111412 * (x + 9.6741e-09) * 0.298408 * exp(-0.111412 * (x + 9.6741e-09) * (x + 9.6741e-09) / l2) +
+                     0.207156 * (x - 1.09822e-08) * 0.42755 * exp(-0.207156 * (x - 1.09822e-08) * (x - 1.09822e-08) / l2) +
+                     0.37742 * (x + 2.13778e-08) * 0.204229 * exp(-0.37742 * (x + 2.13778e-08) * (x + 2.13778e-08) / l2) +
+                     0.68406 * (x - 8.78608e-08) * 0.021649 * exp(-0.68406 * (x - 8.78608e-08) * (x - 8.78608e-08) / l2);
+    const double g = -2 * s / (l2 * l2);
+    return CUDART_PI * g * g;
+  }
+  default: {
+    const double a = 1. / cosh((r + r0) * is), c = 1. / cosh((r - r0) * is);
+    const double q = a * a - c * c;
+    return P.ps_de1 * 0.25 * q * q;
+  }
+  }
+}
+
+__device__ double dev_scalar_e(const PunctureParams &P, double X, double Y, double Z)
+{
+  const int c = P.ps_case;
+  if (c == 2 || c == 3 || c == 4) {
+    const double r = sqrt(X * X + Y * Y + Z * Z);
+    const double r0 = P.ps_r0, is = P.ps_isigma;
+    double phi;
+    if (c == 2) {
+      phi = P.ps_phi0 * exp(-(r - r0) * (r - r0) * is);
+    } else if (c == 3) {
+      const double l2 = 0.6, x = r;
+      phi = (0.0481646 * exp(-0.0581545 * (x - 1.8039e-08) * (x - 1.8039e-08) / (l2)) +
+             0.298408 * exp(-0.111412 * (x + 9.6741e-09) * (x + 9.6741e-09) / l2) +
+             0.42755 * exp(-0.207156 * (x - 1.09822e-08) * (x - 1.09822e-08) / l2) +
+             0.204229 * exp(-0.37742 * (x + 2.13778e-08) * (x + 2.13778e-08) / l2) +
+             0.021649 * exp(-0.68406 * (x - 8.78608e-08) * (x - 8.78608e-08) / l2)) * l2;
+    } else {
+      phi = P.ps_phi0 * 0.5 * (tanh((r + r0) * is) - tanh((r - r0) * is));
+    }
+    const double ff = P.ps_e2 * phi;
+    const double g = 1 - exp(ff);
+    return P.ps_e1 * g * g * exp(-2 * ff);
+  }
+  return 0.0;
+}
+
+__global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                      const double *__restrict__ crd, PunctureParams P)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int i = (int)(t % B.n[0]);
+  const long long r = t / B.n[0];
+  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
+               z = crd[B.coord_off + B.n[0] + B.n[1] + k];
+  F.f[F_B][B.off + t] = dev_punctures_b(P, x, y, z);
+  F.f[F_C][B.off + t] = dev_punctures_c(P, x, y, z);
+  if (P.equation == 1) {
+    F.f[F_D][B.off + t] = dev_scalar_d(P, x, y, z);
+    F.f[F_E][B.off + t] = dev_scalar_e(P, x, y, z);
+  }
+}
+
+// ----------------------------------------------------------------------------
+// K7: u at each puncture by 4th-order Lagrange on the finest box (ADM mass)
+// ----------------------------------------------------------------------------
+struct AdmJob {
+  int box;
+  int exact;
+  int node[3];
+  int start[3];
+  double w[3][5];
+};
+
+__global__ void k_adm(const AdmJob *__restrict__ jobs, int n, const DevBox *__restrict__ boxes, DevFields F,
+                      double *out)
+{
+  const int q = threadIdx.x;
+  if (q >= n) return;
+  const AdmJob J = jobs[q];
+  const DevBox S = boxes[J.box];
+  const double *u = F.f[F_U] + S.off;
+  if (J.exact) {
+    out[q] = u[pidx(S, J.node[0], J.node[1], J.node[2])];
+    return;
+  }
+  double fx = 0.0;
+  for (int I = 0; I <= 4; I++) {
+    double uy = 0.0;
+    for (int Jj = 0; Jj <= 4; Jj++) {
+      double uz = 0.0;
+      for (int K = 0; K <= 4; K++) uz += u[pidx(S, J.start[0] + I, J.start[1] + Jj, J.start[2] + K)] * J.w[2][K];
+      uy += uz * J.w[1][Jj];
+    }
+    fx += uy * J.w[0][I];
+  }
+  out[q] = fx;
+}
+
+}  // namespace olgpu

@@ -1,0 +1,836 @@
+// olgpu.cu -- C ABI of the GB300 puncture FAS solver and its host driver.
+//
+// The driver mirrors elliptic::FASN (WuShichao/OllipticID,
+// src/elliptic.cc:1468-1968) step by step, but every step is a device kernel
+// over all boxes of a level, and the whole V-cycle is recorded once into a
+// CUDA graph that is replayed for every cycle.  Host work per cycle: one graph
+// launch and one small device-to-host copy of the cycle's norms.
+#include "../../include/olgpu.h"
+#include "device.cuh"
+#include "grid.h"
+#include "kernels.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace olgpu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+olgpu_status fail(olgpu_status s, const std::string &msg)
+{
+  g_last_error = msg;
+  return s;
+}
+
+#define CUDA_TRY(expr)                                                                       \
+  do {                                                                                       \
+    cudaError_t e_ = (expr);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(e_ == cudaErrorMemoryAllocation ? OLGPU_ERR_OOM : OLGPU_ERR_CUDA,          \
+                  std::string(#expr) + ": " + cudaGetErrorString(e_));                       \
+  } while (0)
+
+constexpr int kThreads = 256;
+
+// Host copy of one transfer: its jobs, their block prefix and the device copy.
+struct Transfer {
+  std::vector<XferJob> jobs;
+  long long blocks = 0;
+  XferJob *d_jobs = nullptr;
+};
+
+struct Stats {                      // device scalars read back after a cycle
+  unsigned long long slots[128];    // smoother norms, 2 per level (pre/post)
+  double coarse_norm;
+  int coarse_iters;
+  int nan_flag;
+  double adm_u[OLGPU_MAX_BH];
+};
+
+}  // namespace
+
+struct olgpu_hierarchy {
+  olgpu_problem P{};
+  hierarchy_geometry G;
+  int device = 0;
+  int equation = 0;
+  std::vector<DevBox> hboxes;
+  long long total_pts = 0;
+  DevBox *d_boxes = nullptr;
+  double *d_arena = nullptr;
+  DevFields F{};
+  std::vector<double> hcoords;
+  double *d_coords = nullptr;
+  std::vector<AxisEntry> htab;
+  AxisEntry *d_tab = nullptr;
+  // per level k >= 1
+  std::vector<Transfer> restrict_u, xfer_w, set_in, prolong_v, ghost_u;
+  std::vector<AdmJob> hadm;
+  AdmJob *d_adm = nullptr;
+  Stats *d_stats = nullptr;
+  Stats *h_stats = nullptr;         // pinned
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  double adm[OLGPU_MAX_BH] = {0};
+  int coarse_max_iters = 2000;
+  double coarse_omega = 1.85;
+  double coarse_rtol = 1e-5;
+  double eps_solv = 0, eps_coarse = 0;
+};
+
+namespace {
+
+BoxList level_list(const olgpu_hierarchy *h, int level, long long (*blocks_of)(const DevBox &))
+{
+  BoxList L{};
+  L.first = h->G.first_box[level];
+  L.count = h->G.boxes_in_level[level];
+  long long acc = 0;
+  for (int b = 0; b < L.count; b++) {
+    L.blk[b] = (int)acc;
+    acc += blocks_of(h->hboxes[L.first + b]);
+  }
+  L.blk[L.count] = (int)acc;
+  return L;
+}
+
+long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
+
+long long blocks_all(const DevBox &B) { return cdiv((long long)B.n[0] * B.n[1] * B.n[2], kThreads); }
+
+long long blocks_inside(const DevBox &B)
+{
+  const int b = B.buf;
+  return cdiv((long long)(B.n[0] - 2 * b) * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kThreads);
+}
+
+long long blocks_color(const DevBox &B)
+{
+  const int b = B.buf;
+  const int nc = b + 1;   // colours: order/2 + 1 (2 for the order-2 boxes)
+  const long long H = (B.n[0] - 2 * b + nc - 1) / nc;
+  return cdiv(H * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kThreads);
+}
+
+long long blocks_faces(const DevBox &B)
+{
+  const int b = B.buf;
+  long long cols = 0;
+  for (int a = 0; a < 3; a++) cols += 2LL * (B.n[(a + 1) % 3] - 2 * b) * (B.n[(a + 2) % 3] - 2 * b);
+  return cdiv(cols, kThreads);   // one thread per normal column of each face
+}
+
+// LagrangePoly (src/interpolation.cc:308-375)
+double lagrange_poly(const domain &D, int a, double t, int i, int ni, int nf)
+{
+  double lp = 1.0;
+  const double ti = D.coord(a, i);
+  for (int j = ni; j < i; j++) lp *= (t - D.coord(a, j)) / (ti - D.coord(a, j));
+  for (int j = i + 1; j <= nf; j++) lp *= (t - D.coord(a, j)) / (ti - D.coord(a, j));
+  return lp;
+}
+
+// Interpolation table of target axis a for source box S; returns its offset.
+int build_axis(olgpu_hierarchy *h, const domain &T, const domain &S, int a, int method, int ord, bool all,
+               const domain *mask_fine)
+{
+  const int off = (int)h->htab.size();
+  for (int t = 0; t < T.n[a]; t++) {
+    AxisEntry e{};
+    const double x = T.coord(a, t);
+    if (method == XM_COPY) {
+      // Set_In: inside the box's own nb region and the fine box's nb region
+      e.sel = S.is_in_nb_axis(a, x) && mask_fine && mask_fine->is_in_nb_axis(a, x);
+      e.exact = 1;
+      e.node = t;
+      e.start = t;
+    } else {
+      e.sel = all ? S.is_in_axis(a, x) : S.is_in_nb_axis(a, x);
+      const int node = S.locate(a, x);
+      e.node = node;
+      e.exact = dcomp(x, S.coord(a, node));
+      if (method == XM_LAGRANGE) {
+        int s = ord % 2 == 0 ? node - ord / 2 : node - (ord + 1) / 2;
+        if (s < 0) s = 0;
+        else if (s + ord >= S.n[a]) s = S.n[a] - ord - 1;
+        e.start = s;
+        for (int I = 0; I <= ord; I++) e.w[I] = lagrange_poly(S, a, x, s + I, s, s + ord);
+      } else {
+        const int nn = node == 0 ? 1 : node;
+        e.start = nn - 1;
+        const double dxf = (x - S.coord(a, nn - 1)) * (1.0 / S.d[a]);
+        e.w[0] = 1 - dxf;
+        e.w[1] = dxf;
+      }
+    }
+    h->htab.push_back(e);
+  }
+  return off;
+}
+
+void add_region_jobs(Transfer &X, XferJob base, const domain &T, const int sel_lo[3], const int sel_hi[3])
+{
+  const int b = T.buf;
+  const int *n = T.n;
+  std::vector<std::pair<std::array<int, 3>, std::array<int, 3>>> regs;
+  auto box = [&](int i0, int i1, int j0, int j1, int k0, int k1) {
+    regs.push_back({{i0, j0, k0}, {i1, j1, k1}});
+  };
+  if (base.to_zero || base.iter == IT_ALL) {
+    box(0, n[0], 0, n[1], 0, n[2]);
+  } else if (base.iter == IT_INSIDE) {
+    box(b, n[0] - b, b, n[1] - b, b, n[2] - b);
+  } else {   // the ghost shell as six slabs
+    box(0, n[0], 0, n[1], 0, b);
+    box(0, n[0], 0, n[1], n[2] - b, n[2]);
+    box(0, n[0], 0, b, b, n[2] - b);
+    box(0, n[0], n[1] - b, n[1], b, n[2] - b);
+    box(0, b, b, n[1] - b, b, n[2] - b);
+    box(n[0] - b, n[0], b, n[1] - b, b, n[2] - b);
+  }
+  for (auto &r : regs) {
+    XferJob J = base;
+    bool empty = false;
+    for (int a = 0; a < 3; a++) {
+      J.r0[a] = r.first[a];
+      J.r1[a] = r.second[a];
+      if (!base.to_zero) {
+        J.r0[a] = std::max(J.r0[a], sel_lo[a]);
+        J.r1[a] = std::min(J.r1[a], sel_hi[a]);
+      }
+      if (J.r1[a] <= J.r0[a]) empty = true;
+    }
+    if (empty) continue;
+    const long long vol = (long long)(J.r1[0] - J.r0[0]) * (J.r1[1] - J.r0[1]) * (J.r1[2] - J.r0[2]);
+    J.blk0 = X.blocks;
+    X.blocks += cdiv(vol, kThreads);
+    X.jobs.push_back(J);
+  }
+}
+
+// Transferir(from, sfield, to, tfield, iter, method, ord, all, to_zero):
+// every (source box, target box) pair of the two levels.
+Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfield, int iter, int method, int ord,
+                       bool all, bool to_zero)
+{
+  Transfer X;
+  const auto &G = h->G;
+  for (int sb = 0; sb < G.boxes_in_level[from]; sb++)
+    for (int tb = 0; tb < G.boxes_in_level[to]; tb++) {
+      const int gs = G.first_box[from] + sb, gt = G.first_box[to] + tb;
+      const domain &S = G.boxes[gs], &T = G.boxes[gt];
+      XferJob J{};
+      J.tbox = gt;
+      J.sbox = gs;
+      J.tfield = tfield;
+      J.sfield = sfield;
+      J.method = method;
+      J.ord = ord;
+      J.to_zero = to_zero;
+      J.iter = iter;
+      int lo[3], hi[3];
+      for (int a = 0; a < 3; a++) {
+        J.tab[a] = build_axis(h, T, S, a, method, ord, all, nullptr);
+        lo[a] = T.n[a];
+        hi[a] = 0;
+        for (int t = 0; t < T.n[a]; t++)
+          if (h->htab[J.tab[a] + t].sel) {
+            lo[a] = std::min(lo[a], t);
+            hi[a] = std::max(hi[a], t + 1);
+          }
+      }
+      add_region_jobs(X, J, T, lo, hi);
+    }
+  return X;
+}
+
+// S.Set_In(W, fine box, false) for every coarse box and fine box of level k.
+Transfer make_set_in(olgpu_hierarchy *h, int k)
+{
+  Transfer X;
+  const auto &G = h->G;
+  for (int cb = 0; cb < G.boxes_in_level[k - 1]; cb++) {
+    const int gc = G.first_box[k - 1] + cb;
+    const domain &C = G.boxes[gc];
+    for (int fb = 0; fb < G.boxes_in_level[k]; fb++) {
+      const domain &Fd = G.boxes[G.first_box[k] + fb];
+      XferJob J{};
+      J.tbox = gc;
+      J.sbox = gc;
+      J.tfield = F_RHO;
+      J.sfield = F_W;
+      J.method = XM_COPY;
+      J.iter = IT_ALL;
+      int lo[3], hi[3];
+      for (int a = 0; a < 3; a++) {
+        J.tab[a] = build_axis(h, C, C, a, XM_COPY, 0, false, &Fd);
+        lo[a] = C.n[a];
+        hi[a] = 0;
+        for (int t = 0; t < C.n[a]; t++)
+          if (h->htab[J.tab[a] + t].sel) {
+            lo[a] = std::min(lo[a], t);
+            hi[a] = std::max(hi[a], t + 1);
+          }
+      }
+      add_region_jobs(X, J, C, lo, hi);
+    }
+  }
+  return X;
+}
+
+template <int ORD, int EQ>
+void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
+{
+  const BoxList L = level_list(h, level, blocks_color);
+  const int nb = L.blk[L.count];
+  for (int s = 0; s < nu; s++)
+    for (int color = 0; color < num_colors<ORD>(); color++)
+      k_smooth_color<ORD, EQ><<<nb, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, color,
+                                                              &h->d_stats->slots[slot], &h->d_stats->nan_flag);
+}
+
+template <int ORD, int EQ>
+void launch_apply_op(olgpu_hierarchy *h, int level)
+{
+  const BoxList L = level_list(h, level, blocks_inside);
+  k_apply_op<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F);
+}
+
+template <int ORD>
+void launch_robin(olgpu_hierarchy *h, int level, int mode)
+{
+  const BoxList L = level_list(h, level, blocks_faces);
+  k_robin_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
+  k_robin_edges_corners<ORD><<<L.count, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
+}
+
+void launch_ew(olgpu_hierarchy *h, int level, int op)
+{
+  const BoxList L = level_list(h, level, blocks_all);
+  k_elementwise<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, op);
+}
+
+void launch_transfer(olgpu_hierarchy *h, const Transfer &X)
+{
+  if (X.jobs.empty()) return;
+  k_transfer<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F,
+                                                            h->d_tab);
+}
+
+int level_order(const olgpu_hierarchy *h, int level) { return h->G.boxes[h->G.first_box[level]].order; }
+
+template <int EQ>
+void dispatch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
+{
+  switch (level_order(h, level)) {
+  case 2: launch_smooth<2, EQ>(h, level, nu, slot); break;
+  case 4: launch_smooth<4, EQ>(h, level, nu, slot); break;
+  case 6: launch_smooth<6, EQ>(h, level, nu, slot); break;
+  default: launch_smooth<8, EQ>(h, level, nu, slot); break;
+  }
+}
+
+template <int EQ>
+void dispatch_apply_op(olgpu_hierarchy *h, int level)
+{
+  switch (level_order(h, level)) {
+  case 2: launch_apply_op<2, EQ>(h, level); break;
+  case 4: launch_apply_op<4, EQ>(h, level); break;
+  case 6: launch_apply_op<6, EQ>(h, level); break;
+  default: launch_apply_op<8, EQ>(h, level); break;
+  }
+}
+
+void dispatch_robin(olgpu_hierarchy *h, int level, int mode)
+{
+  if (level_order(h, level) == 2) launch_robin<2>(h, level, mode);
+  else launch_robin<4>(h, level, mode);   // orders 4, 6, 8 share dx4 (src/ffunction.cc:197-282)
+}
+
+template <int EQ>
+void emit_fasn(olgpu_hierarchy *h, int k, int top)
+{
+  const int mg = h->G.mgrid_levels;
+  if (k <= mg) dispatch_robin(h, k, 0);
+  dispatch_smooth<EQ>(h, k, h->P.nu1, 2 * k);
+  launch_transfer(h, h->restrict_u[k]);
+  dispatch_apply_op<EQ>(h, k - 1);
+  if (k <= mg) dispatch_robin(h, k - 1, 1);
+  dispatch_apply_op<EQ>(h, k);
+  if (k <= mg) dispatch_robin(h, k, 1);
+  launch_ew(h, k, EW_W_EQ_S_MINUS_R);
+  {
+    const BoxList L = level_list(h, k, blocks_all);
+    k_full_weight<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F);
+  }
+  launch_transfer(h, h->xfer_w[k]);
+  if (k <= mg) {
+    launch_ew(h, k - 1, EW_S_EQ_W_PLUS_R);
+  } else {
+    launch_ew(h, k - 1, EW_W_PLUS_EQ_R);
+    launch_transfer(h, h->set_in[k]);
+  }
+  launch_ew(h, k - 1, EW_WW_EQ_U);
+  if (k == 1) {
+    const DevBox &B = h->hboxes[h->G.first_box[0]];
+    const size_t smem = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
+    k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
+                                                     h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
+                                                     h->coarse_rtol, &h->d_stats->coarse_norm,
+                                                     &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+  } else {
+    emit_fasn<EQ>(h, k - 1, top);
+  }
+  launch_ew(h, k - 1, EW_V_EQ_U_MINUS_WW);
+  launch_transfer(h, h->prolong_v[k]);
+  launch_ew(h, k, EW_U_PLUS_EQ_V);
+  if (k > mg) launch_transfer(h, h->ghost_u[k]);
+  if (k <= mg) dispatch_robin(h, k, 0);
+  dispatch_smooth<EQ>(h, k, h->P.nu2, 2 * k + 1);
+  if (k == top && !h->hadm.empty())
+    k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
+}
+
+olgpu_status build_graph(olgpu_hierarchy *h)
+{
+  const int top = h->G.levels - 1;
+  cudaGraph_t g;
+  CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
+  if (h->equation == 1) emit_fasn<1>(h, top, top);
+  else emit_fasn<0>(h, top, top);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return OLGPU_OK;
+}
+
+int field_id(const char *name)
+{
+  static const char *names[F_NUM] = {"u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v", "t"};
+  if (!name) return -1;
+  for (int f = 0; f < F_NUM; f++)
+    if (!std::strcmp(name, names[f])) return f;
+  return -1;
+}
+
+double elapsed_ms(cudaEvent_t a, cudaEvent_t b)
+{
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+}  // namespace
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+const char *olgpu_last_error(void) { return g_last_error.c_str(); }
+const char *olgpu_version(void) { return "olgpu 0.1 (sm_103a, FP64 FAS)"; }
+
+void olgpu_problem_defaults(olgpu_problem *p)
+{
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->equation = OLGPU_EQ_PUNCTURES;
+  p->numbh = 1;
+  p->n = 30;
+  p->L = 2.0;
+  p->order = 4;
+  p->levels = 1;
+  p->nu1 = 3;
+  p->nu2 = 3;
+  p->tol = 1e-8;
+  p->ps_case = 1;
+  p->ps_phi0 = 0.025;
+  p->ps_r0 = 120;
+  p->ps_sigma = 8;
+  p->ps_a2 = 1;
+}
+
+static void fill_box_info(const domain &D, olgpu_box_info *o)
+{
+  o->level = D.level;
+  o->nx = D.n[0];
+  o->ny = D.n[1];
+  o->nz = D.n[2];
+  o->buf = D.buf;
+  o->order = D.order;
+  o->xi = D.lo[0];
+  o->yi = D.lo[1];
+  o->zi = D.lo[2];
+  o->dx = D.d[0];
+  o->dy = D.d[1];
+  o->dz = D.d[2];
+  o->cx = D.c[0];
+  o->cy = D.c[1];
+  o->cz = D.c[2];
+}
+
+olgpu_status olgpu_plan_boxes(const olgpu_problem *p, olgpu_box_info *out, int cap, int *nboxes, int *nlevels,
+                              int *mgrid_levels)
+{
+  if (!p) return fail(OLGPU_ERR_INVALID_ARG, "null problem");
+  if (p->numbh < 1 || p->numbh > OLGPU_MAX_BH) return fail(OLGPU_ERR_INVALID_ARG, "numbh out of range 1..16");
+  if (!(p->order == 2 || p->order == 4 || p->order == 6 || p->order == 8))
+    return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
+  if (p->levels < 1) return fail(OLGPU_ERR_INVALID_ARG, "levels must be >= 1");
+  hierarchy_geometry G;
+  puncture_set bh{p->numbh, p->x, p->y, p->z};
+  if (!set_grids(p->n, p->L, p->order, p->levels, bh, G))
+    return fail(OLGPU_ERR_GEOMETRY, "not enough grid points for multigrid");
+  if (nboxes) *nboxes = (int)G.boxes.size();
+  if (nlevels) *nlevels = G.levels;
+  if (mgrid_levels) *mgrid_levels = G.mgrid_levels;
+  if (out)
+    for (int g = 0; g < (int)G.boxes.size() && g < cap; g++) fill_box_info(G.boxes[g], &out[g]);
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hierarchy **out)
+{
+  if (!p || !out) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  if (p->numbh < 1 || p->numbh > OLGPU_MAX_BH) return fail(OLGPU_ERR_INVALID_ARG, "numbh out of range 1..16");
+  if (!(p->order == 2 || p->order == 4 || p->order == 6 || p->order == 8))
+    return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
+  if (p->levels < 1) return fail(OLGPU_ERR_INVALID_ARG, "levels must be >= 1");
+  if (p->nu1 < 0 || p->nu2 < 0) return fail(OLGPU_ERR_INVALID_ARG, "negative sweep count");
+  if (p->equation != 0 && p->equation != 1) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
+  if (p->equation == 1 && !(p->ps_case >= 1 && p->ps_case <= 4))
+    return fail(OLGPU_ERR_INVALID_ARG, "ps_case must be 1..4");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OLGPU_ERR_NO_DEVICE, "no CUDA device");
+  if (device >= 0) CUDA_TRY(cudaSetDevice(device));
+
+  auto *h = new olgpu_hierarchy();
+  h->P = *p;
+  h->equation = p->equation;
+  CUDA_TRY(cudaGetDevice(&h->device));
+  h->eps_coarse = 2 * 2.220446049250313e-16;
+  h->eps_solv = p->tol < h->eps_coarse ? h->eps_coarse : p->tol;
+  puncture_set bh{p->numbh, p->x, p->y, p->z};
+  if (!set_grids(p->n, p->L, p->order, p->levels, bh, h->G)) {
+    delete h;
+    return fail(OLGPU_ERR_GEOMETRY, "not enough grid points for multigrid");
+  }
+  if (h->G.levels > 64) {
+    delete h;
+    return fail(OLGPU_ERR_INVALID_ARG, "too many levels");
+  }
+  for (int l = 0; l < h->G.levels; l++)
+    if (h->G.boxes_in_level[l] > kMaxBoxesPerLevel) {
+      delete h;
+      return fail(OLGPU_ERR_INVALID_ARG, "too many boxes on one level");
+    }
+  // device box table and coordinate tables
+  long long off = 0;
+  int coff = 0;
+  for (const domain &D : h->G.boxes) {
+    DevBox B{};
+    for (int a = 0; a < 3; a++) {
+      B.n[a] = D.n[a];
+      B.idx[a] = 1.0 / D.d[a];
+      B.idx2[a] = B.idx[a] * B.idx[a];
+    }
+    B.buf = D.buf;
+    B.order = D.order;
+    B.level = D.level;
+    B.off = off;
+    B.coord_off = coff;
+    const double s = B.idx2[0] + B.idx2[1] + B.idx2[2];
+    switch (D.order) {   // duLapc2/4/6/8
+    case 2: B.dulap = -2.0 * s; break;
+    case 4: B.dulap = -2.5 * s; break;
+    case 6: B.dulap = -490 * s * (1.0 / 180); break;
+    default: B.dulap = -205 * s / 72.0; break;
+    }
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < D.n[a]; i++) h->hcoords.push_back(D.coord(a, i));
+    coff += D.n[0] + D.n[1] + D.n[2];
+    off += D.npts();
+    h->hboxes.push_back(B);
+  }
+  h->total_pts = off;
+  // transfer plans for every level k >= 1 (FASN steps 2, 5, 6, 10, 12)
+  const int L = h->G.levels, mg = h->G.mgrid_levels, order = p->order;
+  h->restrict_u.resize(L);
+  h->xfer_w.resize(L);
+  h->set_in.resize(L);
+  h->prolong_v.resize(L);
+  h->ghost_u.resize(L);
+  for (int k = 1; k < L; k++) {
+    h->restrict_u[k] = make_transfer(h, k, F_U, k - 1, F_U, IT_INSIDE, XM_LAGRANGE, 3, false, false);
+    h->xfer_w[k] = make_transfer(h, k, F_T, k - 1, F_W, IT_ALL, XM_LAGRANGE, 2, k - 1 <= mg, false);
+    if (k > mg) h->set_in[k] = make_set_in(h, k);
+    if (k <= mg)
+      h->prolong_v[k] = make_transfer(h, k - 1, F_V, k, F_V, IT_ALL, XM_LINEAR, 1, true, true);
+    else
+      h->prolong_v[k] = make_transfer(h, k - 1, F_V, k, F_V, IT_INSIDE, XM_LINEAR, 1, true, false);
+    if (k > mg) h->ghost_u[k] = make_transfer(h, k - 1, F_U, k, F_U, IT_BOUNDARY, XM_LAGRANGE, order + 1, true, false);
+  }
+  // ADM: 4th-order Lagrange at each puncture on finest box i (box 0 if absent)
+  {
+    const int top = L - 1;
+    for (int i = 0; i < p->numbh; i++) {
+      const int g = h->G.first_box[top] + (i < h->G.boxes_in_level[top] ? i : 0);
+      const domain &S = h->G.boxes[g];
+      AdmJob J{};
+      J.box = g;
+      const double pt[3] = {p->x[i], p->y[i], p->z[i]};
+      int ex = 1;
+      for (int a = 0; a < 3; a++) {
+        const int node = S.locate(a, pt[a]);
+        J.node[a] = node;
+        ex = ex && dcomp(pt[a], S.coord(a, node));
+        int s = node - 2;
+        if (s < 0) s = 0;
+        else if (s + 4 >= S.n[a]) s = S.n[a] - 5;
+        J.start[a] = s;
+        for (int I = 0; I <= 4; I++) J.w[a][I] = lagrange_poly(S, a, pt[a], s + I, s, s + 4);
+      }
+      J.exact = ex;
+      h->hadm.push_back(J);
+    }
+  }
+  // device memory
+  olgpu_status st = OLGPU_OK;
+  auto cleanup = [&](olgpu_status s) {
+    olgpu_hierarchy_destroy(h);
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+    return cleanup(fail(OLGPU_ERR_CUDA, "stream/event creation failed"));
+  const size_t arena = sizeof(double) * (size_t)h->total_pts * F_NUM;
+  cudaError_t e = cudaMalloc(&h->d_arena, arena);
+  if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_OOM, "device arena allocation failed"));
+  for (int f = 0; f < F_NUM; f++) h->F.f[f] = h->d_arena + (size_t)f * h->total_pts;
+  if (h->equation == 0) h->F.f[F_D] = h->F.f[F_E] = nullptr;
+  auto up = [&](void **dst, const void *src, size_t bytes) -> bool {
+    if (bytes == 0) return true;
+    if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
+    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  bool ok = up((void **)&h->d_boxes, h->hboxes.data(), sizeof(DevBox) * h->hboxes.size()) &&
+            up((void **)&h->d_coords, h->hcoords.data(), sizeof(double) * h->hcoords.size()) &&
+            up((void **)&h->d_tab, h->htab.data(), sizeof(AxisEntry) * h->htab.size()) &&
+            up((void **)&h->d_adm, h->hadm.data(), sizeof(AdmJob) * h->hadm.size());
+  for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
+    for (auto &X : *vec)
+      ok = ok && up((void **)&X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size());
+  ok = ok && cudaMalloc(&h->d_stats, sizeof(Stats)) == cudaSuccess &&
+       cudaMallocHost(&h->h_stats, sizeof(Stats)) == cudaSuccess;
+  if (!ok) return cleanup(fail(OLGPU_ERR_OOM, "device allocation failed"));
+  // coarsest box must fit in shared memory
+  {
+    const DevBox &B0 = h->hboxes[h->G.first_box[0]];
+    const size_t smem = sizeof(double) * (size_t)B0.n[0] * B0.n[1] * B0.n[2];
+    if (smem > 200 * 1024) return cleanup(fail(OLGPU_ERR_INVALID_ARG, "coarsest grid too large"));
+    cudaError_t e1 = cudaFuncSetAttribute(k_coarse_solve<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e2 = cudaFuncSetAttribute(k_coarse_solve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e1 != cudaSuccess || e2 != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, "shared memory opt-in failed"));
+  }
+  st = olgpu_reset(h);
+  if (st != OLGPU_OK) return cleanup(st);
+  // coefficients on the device
+  {
+    PunctureParams PP{};
+    PP.numbh = p->numbh;
+    PP.equation = p->equation;
+    PP.ps_case = p->ps_case;
+    for (int i = 0; i < p->numbh; i++) {
+      PP.mp[i] = p->mp[i]; PP.x[i] = p->x[i]; PP.y[i] = p->y[i]; PP.z[i] = p->z[i];
+      PP.px[i] = p->px[i]; PP.py[i] = p->py[i]; PP.pz[i] = p->pz[i];
+      PP.sx[i] = p->sx[i]; PP.sy[i] = p->sy[i]; PP.sz[i] = p->sz[i];
+    }
+    // scalar-field constants (src/elliptic.cc:71-81)
+    PP.ps_r0 = p->ps_r0;
+    PP.ps_isigma = 1 / p->ps_sigma;
+    const double a2 = p->ps_a2;
+    PP.ps_phi0 = (a2 * a2 / (1 + a2 * a2)) * p->ps_phi0;
+    PP.ps_d1 = M_PI * PP.ps_phi0 * PP.ps_phi0 * PP.ps_isigma * PP.ps_isigma;
+    PP.ps_e1 = 1 / (16 * p->ps_a2);
+    PP.ps_e2 = 4 * std::sqrt(M_PI / 3);
+    PP.ps_de1 = 4 * M_PI * PP.ps_phi0 * PP.ps_phi0 * PP.ps_isigma * PP.ps_isigma;
+    for (int l = 0; l < L; l++) {
+      const BoxList BL = level_list(h, l, blocks_all);
+      k_coefficients<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords, PP);
+    }
+    e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, std::string("coefficients: ") + cudaGetErrorString(e)));
+  }
+  st = build_graph(h);
+  if (st != OLGPU_OK) return cleanup(st);
+  *out = h;
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
+{
+  if (!h) return OLGPU_OK;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
+    for (auto &X : *vec) cudaFree(X.d_jobs);
+  cudaFree(h->d_arena);
+  cudaFree(h->d_boxes);
+  cudaFree(h->d_coords);
+  cudaFree(h->d_tab);
+  cudaFree(h->d_adm);
+  cudaFree(h->d_stats);
+  if (h->h_stats) cudaFreeHost(h->h_stats);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete h;
+  return OLGPU_OK;
+}
+
+int olgpu_num_boxes(const olgpu_hierarchy *h) { return h ? (int)h->G.boxes.size() : 0; }
+int olgpu_num_levels(const olgpu_hierarchy *h) { return h ? h->G.levels : 0; }
+int olgpu_mgrid_levels(const olgpu_hierarchy *h) { return h ? h->G.mgrid_levels : 0; }
+
+olgpu_status olgpu_box(const olgpu_hierarchy *h, int box, olgpu_box_info *o)
+{
+  if (!h || !o || box < 0 || box >= (int)h->G.boxes.size()) return fail(OLGPU_ERR_INVALID_ARG, "bad box");
+  fill_box_info(h->G.boxes[box], o);
+  return OLGPU_OK;
+}
+
+static olgpu_status field_copy(olgpu_hierarchy *h, int box, const char *field, void *host, bool upload)
+{
+  if (!h || !host || box < 0 || box >= (int)h->G.boxes.size()) return fail(OLGPU_ERR_INVALID_ARG, "bad box");
+  const int f = field_id(field);
+  if (f < 0 || !h->F.f[f]) return fail(OLGPU_ERR_INVALID_ARG, std::string("unknown field ") + (field ? field : ""));
+  CUDA_TRY(cudaSetDevice(h->device));
+  const DevBox &B = h->hboxes[box];
+  double *d = h->F.f[f] + B.off;
+  const size_t bytes = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
+  if (upload)
+    CUDA_TRY(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, h->stream));
+  else
+    CUDA_TRY(cudaMemcpyAsync(host, d, bytes, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_upload(olgpu_hierarchy *h, int box, const char *field, const double *host)
+{
+  return field_copy(h, box, field, const_cast<double *>(host), true);
+}
+
+olgpu_status olgpu_download(olgpu_hierarchy *h, int box, const char *field, double *host)
+{
+  return field_copy(h, box, field, host, false);
+}
+
+olgpu_status olgpu_reset(olgpu_hierarchy *h)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const size_t n = sizeof(double) * (size_t)h->total_pts;
+  for (int f : {F_U, F_RHO, F_R, F_W, F_WW, F_V, F_T}) CUDA_TRY(cudaMemsetAsync(h->F.f[f], 0, n, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  std::fill(h->adm, h->adm + OLGPU_MAX_BH, 0.0);
+  return OLGPU_OK;
+}
+
+static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
+{
+  CUDA_TRY(cudaGraphLaunch(h->graph, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->h_stats, h->d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const int top = h->G.levels - 1;
+  std::memcpy(res, &h->h_stats->slots[2 * top + 1], sizeof(double));
+  const olgpu_problem &P = h->P;
+  for (int i = 0; i < P.numbh; i++) {
+    double bhmj = 0;
+    for (int j = 0; j < P.numbh; j++)
+      if (j != i)
+        bhmj += 0.5 * P.mp[j] / std::sqrt((P.x[i] - P.x[j]) * (P.x[i] - P.x[j]) + (P.y[i] - P.y[j]) * (P.y[i] - P.y[j]) +
+                                          (P.z[i] - P.z[j]) * (P.z[i] - P.z[j]));
+    h->adm[i] = P.mp[i] * (1 + bhmj + h->h_stats->adm_u[i]);
+  }
+  if (h->h_stats->nan_flag) return fail(OLGPU_ERR_NAN, "NaN in the smoother");
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res)
+{
+  if (!h || !res) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+  olgpu_status s = run_cycle(h, res);
+  cudaEventRecord(h->ev1, h->stream);
+  cudaEventSynchronize(h->ev1);
+  h->last_ms = elapsed_ms(h->ev0, h->ev1);
+  return s;
+}
+
+olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  olgpu_stop_rule R{OLGPU_STOP_REFERENCE, 100000, 0.0};
+  if (rule) R = *rule;
+  if (R.max_cycles <= 0) return fail(OLGPU_ERR_INVALID_ARG, "max_cycles must be > 0");
+  const double tol = R.tol > 0 ? R.tol : h->eps_solv;
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+  double res = 1e12, res_prev;
+  int c = 0;
+  olgpu_status s = OLGPU_OK;
+  olgpu_report rep{};
+  for (;;) {
+    res_prev = res;
+    s = run_cycle(h, &res);
+    if (c < 256) rep.res[c] = res;
+    c++;
+    if (s != OLGPU_OK) break;
+    if (c >= R.max_cycles) break;
+    if (R.stop == OLGPU_STOP_FIXED) continue;
+    if (!(res > tol)) break;
+    if (R.stop == OLGPU_STOP_REFERENCE && !(res < res_prev)) break;
+  }
+  cudaEventRecord(h->ev1, h->stream);
+  cudaEventSynchronize(h->ev1);
+  h->last_ms = elapsed_ms(h->ev0, h->ev1);
+  rep.cycles = c;
+  rep.status = s;
+  rep.final_res = res;
+  for (int i = 0; i < h->P.numbh; i++) rep.adm[i] = h->adm[i];
+  if (out) *out = rep;
+  return s;
+}
+
+olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
+{
+  if (!h || !out) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  for (int i = 0; i < h->P.numbh; i++) out[i] = h->adm[i];
+  return OLGPU_OK;
+}
+
+double olgpu_last_device_ms(const olgpu_hierarchy *h) { return h ? h->last_ms : 0.0; }
+
+}  // extern "C"

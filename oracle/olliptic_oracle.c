@@ -216,6 +216,15 @@ struct orc_solver {
   /* scalar field constants, src/elliptic.cc:71-81 */
   double ps_isigma, ps_phi0, ps_d1, ps_e1, ps_e2, ps_de1;
   int nan_flag;
+  /* checker options (not part of the reference algorithm) */
+  int multicolor;    /* 1: visit points by colour (i+j+k) mod (buf+1), as the GPU does */
+  long coarse_cap;   /* cap on coarsest-grid sweeps per V-cycle */
+  long coarse_iters; /* sweeps used by the last coarse solve */
+  int wsmooth;       /* 1: full-weight W over INSIDE points before its transfer */
+  double coarse_omega; /* over-relaxation of the coarsest-solve sweeps (1 = reference) */
+  double coarse_rtol;  /* also stop once the sweep norm <= rtol * first sweep norm (0 = off) */
+  double lnorm[64][2]; /* last cycle: smoother norms per level (pre, post) */
+  double coarse_norm;
 };
 
 static inline long IDX(const obox *B, int i, int j, int k)
@@ -564,7 +573,9 @@ static inline double duop_at(const orc_solver *S, const obox *B, long p, double 
 /* elliptic::Smooth, src/elliptic.cc:1126-1242: lexicographic nonlinear
  * Gauss-Seidel-Newton over INSIDE points; returns the max over the nu sweeps
  * of the L-infinity norm of the pre-update point residuals. */
-static double smooth_box(orc_solver *S, obox *B, int nu)
+static double smooth_box_w(orc_solver *S, obox *B, int nu, double omega);
+static double smooth_box(orc_solver *S, obox *B, int nu) { return smooth_box_w(S, B, nu, 1.0); }
+static double smooth_box_w(orc_solver *S, obox *B, int nu, double omega)
 {
   double gLinf = 0;
   const int b = B->D.buf;
@@ -572,16 +583,24 @@ static double smooth_box(orc_solver *S, obox *B, int nu)
   double *u = B->f[F_U], *R = B->f[F_R];
   const double *rho = B->f[F_RHO];
   const double dl = dulap(B);
+  /* multicolor: bit 0 = multigrid levels above the coarsest (Robin boxes),
+   * bit 1 = coarsest solve, bit 2 = refinement levels */
+  const int lv = B->D.level;
+  const int mc = lv == 0 ? (S->multicolor >> 1) & 1
+                         : (lv <= S->mgrid_levels ? S->multicolor & 1 : (S->multicolor >> 2) & 1);
+  const int NC = mc ? b + 1 : 1;
   for (int kk = 0; kk < nu; kk++) {
     double Linf = 0;
+    for (int color = 0; color < NC; color++)
     for (int k = b; k < nz - b; k++)
       for (int j = b; j < ny - b; j++)
         for (int i = b; i < nx - b; i++) {
+          if (NC > 1 && (i + j + k) % NC != color) continue;
           long p = IDX(B, i, j, k);
           double r = op_at(S, B, p, lap_at(B, u, i, j, k)) - rho[p];
           R[p] = r;
           double dr = duop_at(S, B, p, dl);
-          u[p] = u[p] - R[p] / dr;
+          u[p] = omega == 1.0 ? u[p] - R[p] / dr : u[p] - omega * (R[p] / dr);
           double f = fabs(R[p]);
           if (Linf < f) Linf = f;
           if (!(u[p] == u[p])) S->nan_flag = 1;
@@ -864,6 +883,34 @@ static void axpy_all(obox *B, int dst, int a, double sa, int b)   /* dst = a + s
   for (long p = 0; p < B->npts; p++) B->f[dst][p] = B->f[a][p] + sa * B->f[b][p];
 }
 
+/* Checker option: replace W on the INSIDE points of a box by its
+ * (1,2,1)^3/64 average, where a neighbour outside INSIDE contributes the
+ * centre value.  W vanishes at the fixed point, so this changes the path of
+ * the iteration, not its fixed point. */
+static void full_weight_w(obox *B)
+{
+  const int b = B->D.buf, nx = B->D.n[0], ny = B->D.n[1], nz = B->D.n[2];
+  double *w = B->f[F_W];
+  double *t = (double *)malloc(sizeof(double) * B->npts);
+  memcpy(t, w, sizeof(double) * B->npts);
+  for (int k = b; k < nz - b; k++)
+    for (int j = b; j < ny - b; j++)
+      for (int i = b; i < nx - b; i++) {
+        const double c = t[IDX(B, i, j, k)];
+        double acc = 0;
+        for (int dk = -1; dk <= 1; dk++)
+          for (int dj = -1; dj <= 1; dj++)
+            for (int di = -1; di <= 1; di++) {
+              const int ii = i + di, jj = j + dj, kk = k + dk;
+              const double wt = (double)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) / 64.0;
+              const int in = ii >= b && ii < nx - b && jj >= b && jj < ny - b && kk >= b && kk < nz - b;
+              acc += wt * (in ? t[IDX(B, ii, jj, kk)] : c);
+            }
+        w[IDX(B, i, j, k)] = acc;
+      }
+  free(t);
+}
+
 /* elliptic::FASN with Wcycle = false, src/elliptic.cc:1468-1968 */
 static double fasn(orc_solver *S, int k, int k_top)
 {
@@ -879,6 +926,7 @@ static double fasn(orc_solver *S, int k, int k_top)
     double n = smooth_box(S, &Bk[i], S->P.nu1);
     norm_k = n > norm_k ? n : norm_k;
   }
+  if (k < 64) S->lnorm[k][0] = norm_k;
   transferir(S, k, F_U, k - 1, F_U, IT_INSIDE, M_LAGRANGE, 3, 0, 0);   /* 1543-1546 */
   for (int j = 0; j < nc; j++) {                                  /* 1582-1594 */
     app_ell_operator(S, &Bc[j]);
@@ -890,6 +938,8 @@ static double fasn(orc_solver *S, int k, int k_top)
   }
   for (int i = 0; i < nk; i++)                                    /* 1625-1649 */
     for (long p = 0; p < Bk[i].npts; p++) Bk[i].f[F_W][p] = Bk[i].f[F_RHO][p] - Bk[i].f[F_R][p];
+  if (S->wsmooth)
+    for (int i = 0; i < nk; i++) full_weight_w(&Bk[i]);
   if (k - 1 <= mg)                                                /* 1660-1676 */
     transferir(S, k, F_W, k - 1, F_W, IT_ALL, M_LAGRANGE, 2, 1, 0);
   else
@@ -908,13 +958,19 @@ static double fasn(orc_solver *S, int k, int k_top)
     for (int j = 0; j < nc; j++) {
       double norm_prev;
       norm_km1 = 1;
-      int guard = 0;
+      long guard = 0;
+      double first = -1.0;
       do {
         norm_prev = norm_km1;
         robin_walk(S, &Bc[j], robin_update_pt);
-        norm_km1 = smooth_box(S, &Bc[j], 1);
-        if (S->nan_flag || ++guard > 1000000) break;
-      } while (norm_km1 > S->eps_coarse && norm_prev != norm_km1);
+        norm_km1 = smooth_box_w(S, &Bc[j], 1, S->coarse_omega);
+        if (first < 0) first = norm_km1;
+        ++guard;
+        if (S->nan_flag) break;
+        if (S->coarse_rtol > 0 && norm_km1 <= S->coarse_rtol * first) break;
+      } while (norm_km1 > S->eps_coarse && norm_prev != norm_km1 && guard < S->coarse_cap);
+      S->coarse_iters = guard;
+      S->coarse_norm = norm_km1;
     }
   } else {
     norm_km1 = fasn(S, k - 1, k_top);
@@ -935,6 +991,7 @@ static double fasn(orc_solver *S, int k, int k_top)
     double n = smooth_box(S, &Bk[i], S->P.nu2);
     norm_k = n > norm_k ? n : norm_k;
   }
+  if (k < 64) S->lnorm[k][1] = norm_k;
   if (k == k_top) compute_adm(S);                                 /* 1939-1941 */
   return norm_k;
 }
@@ -968,6 +1025,8 @@ orc_solver *orc_create(const orc_problem *p)
   orc_solver *S = (orc_solver *)calloc(1, sizeof(orc_solver));
   S->P = *p;
   S->eps_coarse = 2 * EPS;                          /* src/elliptic.cc:62 */
+  S->coarse_cap = 1000000000L;
+  S->coarse_omega = 1.0;
   S->eps_solv = p->tol < S->eps_coarse ? S->eps_coarse : p->tol;
   S->ps_isigma = 1 / p->ps_sigma;                   /* src/elliptic.cc:71-81 */
   double a2 = p->ps_a2;
@@ -1093,6 +1152,18 @@ void orc_adm(const orc_solver *S, double *out)
 double orc_smooth(orc_solver *S, int level, int ibox, int nu)
 {
   return smooth_box(S, &S->box[S->first[level] + ibox], nu);
+}
+
+void orc_set_multicolor(orc_solver *S, int on) { S->multicolor = on; }
+void orc_set_wsmooth(orc_solver *S, int on) { S->wsmooth = on; }
+void orc_set_coarse_omega(orc_solver *S, double w) { S->coarse_omega = w; }
+void orc_set_coarse_rtol(orc_solver *S, double r) { S->coarse_rtol = r; }
+void orc_set_coarse_cap(orc_solver *S, long cap) { S->coarse_cap = cap > 0 ? cap : 1000000000L; }
+long orc_coarse_iters(const orc_solver *S) { return S->coarse_iters; }
+double orc_level_norm(const orc_solver *S, int level, int post)
+{
+  if (level == 0) return S->coarse_norm;
+  return (level > 0 && level < 64) ? S->lnorm[level][post ? 1 : 0] : -1.0;
 }
 
 void orc_robin(orc_solver *S, int level, int ibox)

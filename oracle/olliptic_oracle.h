@@ -63,6 +63,18 @@ void orc_adm(const orc_solver *s, double *out);
 /* Single-box building blocks, exposed for unit tests. */
 double orc_smooth(orc_solver *s, int level, int ibox, int nu);
 void orc_robin(orc_solver *s, int level, int ibox);
+/* Checker options outside the reference algorithm: visit smoother points by
+ * colour (i+j+k) mod (ghost width + 1) like the GPU, and cap the coarsest-grid
+ * sweeps per V-cycle.  Neither changes the discrete fixed point. */
+void orc_set_multicolor(orc_solver *s, int on);
+void orc_set_coarse_cap(orc_solver *s, long cap);
+void orc_set_wsmooth(orc_solver *s, int on);
+void orc_set_coarse_omega(orc_solver *s, double omega);
+void orc_set_coarse_rtol(orc_solver *s, double rtol);
+long orc_coarse_iters(const orc_solver *s);
+/* last cycle's smoother norm on a level (post = 0 pre-, 1 post-smoothing);
+ * level 0 gives the coarsest-solve norm */
+double orc_level_norm(const orc_solver *s, int level, int post);
 /* Valid_N restated (src/interface.cc:883-945) */
 int orc_valid_n(int n);
 
