@@ -1,0 +1,315 @@
+"""Benchmark: puncture FAS solves/s on one GB300 (BASELINE configs[1]).
+
+Workload (one step = one full solve): the equal-mass binary of the reference's
+pars/Punctures/TestBH.run at 4th order -- two punctures m=0.487209 at
+y=+-5.5 with momenta (-+0.0901099, -+0.000703975, 0), Robin boundary, N=65,
+9 refinement levels, L=1000, 20 post-smoothing sweeps, solved from u = 0
+until the top-level residual is <= 1e-11.  Plain FP64 on the GPU.  Inputs are
+synthetic (the reference ships no data set; the problem is defined by its
+command line).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+--impl reference times the reference algorithm on the host CPU cores (the
+oracle port, a bit-exact restatement of the reference's CPU solver) on the
+same workload.  With torchrun (N > 1) every rank solves its own copies of the
+workload on its own GPU (replicas: one solve never spans GPUs) and rank 0
+prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD_ARGS = ("-eq Punctures -B Robin -BA 0.0 -Bn 1 -NumBH 2 -bhmp1 0.487209 -bhy1 5.5 -bhpx1 -0.0901099 "
+                 "-bhpy1 -0.000703975 -bhmp2 0.487209 -bhy2 -5.5 -bhpx2 0.0901099 -bhpy2 0.000703975 "
+                 "-L 1000 -N 65 -O 4 -l 9 -s 1e-11 -Dp 0.05 -nu2 20")
+WORKLOAD_NAME = "binary_O4_N65_l9_L1000_tol1e-11"
+METRIC = "puncture solves/s to 1e-10 (served FP32/FP64 vs plain FP64); p99 latency; GB/s"
+UNIT = "solves/s"
+# The reference's own stop rule (src/elliptic.cc:1330) ends this workload
+# after 17 V-cycles at 9.95e-12 (lexicographic CPU solver, measured here with
+# the oracle, which reproduces the reference's iterates bit for bit).
+CPU_CYCLES_PER_SOLVE = 17
+SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------
+# CPU side (oracle port of the reference solver)
+# ----------------------------------------------------------------------------
+def _cpu_worker(args):
+    n_warm, n_cycles, q = args
+    from oracle import oracle as O
+    import ollipticid_gb300 as og
+    P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
+    orc = O.Oracle(P.oracle_dict())
+    for _ in range(n_warm):
+        orc.vcycle()
+    times = []
+    for _ in range(n_cycles):
+        t0 = time.perf_counter()
+        orc.vcycle()
+        times.append(time.perf_counter() - t0)
+    q.put(times)
+
+
+def cpu_throughput(n_warm: int, n_cycles: int, procs: int):
+    """Solves/s of `procs` concurrent single-threaded oracle solvers, from
+    timed V-cycles scaled by the cycles a full CPU solve needs."""
+    from oracle import oracle as O
+    O.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_cpu_worker, args=((n_warm, n_cycles, q),)) for _ in range(procs)]
+    for p in ps:
+        p.start()
+    res = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    per_proc = [sum(t) / len(t) for t in res]                  # s per V-cycle
+    solves_per_s = sum(1.0 / (t * CPU_CYCLES_PER_SOLVE) for t in per_proc)
+    return solves_per_s, per_proc
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    n_cycles = max(1, min(args.steps, 4))
+    n_warm = 0 if args.warmup <= 0 else 1
+    sps, per_proc = cpu_throughput(n_warm, n_cycles, procs)
+    line = {
+        "impl": "reference",
+        "metric": METRIC, "value": sps, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * procs / sps if sps > 0 else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD_NAME, "args": WORKLOAD_ARGS},
+        "cpu_baseline": {"value": sps, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{procs} concurrent single-threaded oracle solvers, {n_warm} warm-up + "
+                                   f"{n_cycles} timed V-cycles each, scaled by {CPU_CYCLES_PER_SOLVE} cycles/solve; "
+                                   f"mean s/cycle per process {sum(per_proc) / len(per_proc):.3f}"},
+        "e2e": {"value": sps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------------------
+# GPU side
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nme, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nme)
+        if not sm:
+            return None
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _flush_l2(dev):
+    import torch
+    buf = getattr(_flush_l2, "buf", None)
+    if buf is None:
+        buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+        _flush_l2.buf = buf
+    buf.fill_(1.0)
+    torch.cuda.synchronize(dev)
+
+
+def run_gpu(args, rank: int, world: int, local: int):
+    import numpy as np
+    import torch
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
+    E = og.Elliptic(P, device=local)
+    nboxes = len(E.boxes)
+    total_pts = sum(b.n[0] * b.n[1] * b.n[2] for b in E.boxes)
+
+    def solve():
+        E.reset()
+        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
+        if rep.final_res > P.tol:
+            raise RuntimeError(f"solve did not reach {P.tol}: {rep.final_res}")
+        return rep
+
+    for _ in range(args.warmup):
+        solve()
+    # ---- timed region: K solves (device time from CUDA events on the solver's stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    t_wall0 = time.perf_counter()
+    dev_ms, cycles = 0.0, 0
+    reps = []
+    for _ in range(args.steps):
+        _flush_l2(dev)
+        rep = solve()
+        dev_ms += E.last_device_ms
+        cycles += rep.cycles
+        reps.append(rep)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t_wall0
+    if world > 1:
+        t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms_per_step = dev_ms / args.steps
+    value = world * args.steps / (dev_ms / 1000.0)
+    launches = E.kernels_per_cycle * cycles
+
+    # ---- end to end through the C ABI with host buffers
+    hb = [E.get_field(g, "b") for g in range(nboxes)]
+    hc = [E.get_field(g, "c") for g in range(nboxes)]
+    hu0 = [np.zeros_like(x) for x in hb]
+    hu = [np.empty_like(x) for x in hb]
+    e2e_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for g in range(nboxes):
+            E.set_field(g, "b", hb[g])
+            E.set_field(g, "c", hc[g])
+        E.reset()
+        for g in range(nboxes):
+            E.set_field(g, "u", hu0[g])
+        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
+        for g in range(nboxes):
+            hu[g] = E.get_field(g, "u")
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * total_pts,
+           "d2h_bytes_per_step": 8 * total_pts}
+
+    # ---- roofline of the dominant kernel (multicolour smoother), all levels
+    peak, peak_kind = _peaks()
+    tot_bytes, tot_ms, tot_launch = 0.0, 0.0, 0
+    for lev in range(1, E.levels):
+        E.time_smoother(lev, 2)                      # warm
+        ms, nl = E.time_smoother(lev, 10)
+        tot_bytes += E.interior_points(lev) * SMOOTH_BYTES_PER_POINT * 10
+        tot_ms += ms
+        tot_launch += nl
+    achieved = tot_bytes / (tot_ms / 1000.0) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind, "traffic": None, "kernel": "k_smooth_color (all levels)",
+            "launches_timed": tot_launch}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n_cycles = 2
+        sps, per_proc = cpu_throughput(0, n_cycles, 1)
+        cpu = {"value": sps, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"one single-threaded oracle solver, {n_cycles} timed V-cycles of this workload "
+                         f"({per_proc[0]:.2f} s/cycle) scaled by {CPU_CYCLES_PER_SOLVE} cycles/solve"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "args": WORKLOAD_ARGS, "precision": "plain FP64",
+                       "stop": "top-level residual <= 1e-11", "cycles_per_solve": cycles / args.steps,
+                       "final_res": reps[-1].final_res, "adm": [reps[-1].adm[0], reps[-1].adm[1]],
+                       "l2": "256 MiB buffer written before every timed solve", "boxes": nboxes,
+                       "points": total_pts, "wall_s": wall},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    E.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-cycle", action="store_true",
+                    help="run two V-cycles of the workload and exit (for the ncu launch list)")
+    args = ap.parse_args()
+    if args.profile_cycle:
+        import ollipticid_gb300 as og
+        E = og.Elliptic(og.parse_olliptic_args(WORKLOAD_ARGS.split()))
+        r = [E.FASN() for _ in range(2)]
+        print(json.dumps({"profile_cycles": 2, "res": r, "kernels_per_cycle": E.kernels_per_cycle}))
+        E.close()
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    run_gpu(args, rank, world, local)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

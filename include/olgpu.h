@@ -133,8 +133,17 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
  * and coefficients, so that one hierarchy can serve repeated solves. */
 olgpu_status olgpu_reset(olgpu_hierarchy *h);
 
-/* Timing aid: device time of the last olgpu_solve / olgpu_vcycle in ms. */
+/* Timing aids. */
+/* device time of the last olgpu_solve / olgpu_vcycle in ms */
 double olgpu_last_device_ms(const olgpu_hierarchy *h);
+/* kernel launches in one V-cycle (the captured graph's kernel nodes) */
+int olgpu_kernels_per_cycle(const olgpu_hierarchy *h);
+/* INSIDE points of a level, summed over its boxes (algorithmic work unit) */
+long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level);
+/* Times `sweeps` full smoother sweeps (every colour pass) on one level with
+ * CUDA events on the hierarchy's stream; *ms gets the elapsed device time and
+ * *launches the number of smoother kernels it launched.  Changes u. */
+olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, double *ms, int *launches);
 
 const char *olgpu_last_error(void);
 const char *olgpu_version(void);

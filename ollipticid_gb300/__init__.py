@@ -216,3 +216,17 @@ class Elliptic:
     @property
     def last_device_ms(self) -> float:
         return self.lib.olgpu_last_device_ms(self._h)
+
+    @property
+    def kernels_per_cycle(self) -> int:
+        return self.lib.olgpu_kernels_per_cycle(self._h)
+
+    def interior_points(self, level: int) -> int:
+        return int(self.lib.olgpu_level_interior_points(self._h, level))
+
+    def time_smoother(self, level: int, sweeps: int):
+        """(device ms, kernel launches) of `sweeps` smoother sweeps on a level."""
+        ms = C.c_double()
+        n = C.c_int()
+        check(self.lib.olgpu_time_smoother(self._h, level, sweeps, C.byref(ms), C.byref(n)))
+        return ms.value, n.value

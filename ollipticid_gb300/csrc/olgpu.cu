@@ -88,6 +88,7 @@ struct olgpu_hierarchy {
   double coarse_omega = 1.85;
   double coarse_rtol = 1e-5;
   double eps_solv = 0, eps_coarse = 0;
+  int launches = 0;               // kernels emitted while capturing the V-cycle
 };
 
 namespace {
@@ -298,7 +299,8 @@ void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++)
       k_smooth_color<ORD, EQ><<<nb, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, color,
-                                                              &h->d_stats->slots[slot], &h->d_stats->nan_flag);
+                                                              &h->d_stats->slots[slot], &h->d_stats->nan_flag),
+          h->launches++;
 }
 
 template <int ORD, int EQ>
@@ -306,6 +308,7 @@ void launch_apply_op(olgpu_hierarchy *h, int level)
 {
   const BoxList L = level_list(h, level, blocks_inside);
   k_apply_op<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F);
+  h->launches++;
 }
 
 template <int ORD>
@@ -314,12 +317,14 @@ void launch_robin(olgpu_hierarchy *h, int level, int mode)
   const BoxList L = level_list(h, level, blocks_faces);
   k_robin_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
   k_robin_edges_corners<ORD><<<L.count, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
+  h->launches += 2;
 }
 
 void launch_ew(olgpu_hierarchy *h, int level, int op)
 {
   const BoxList L = level_list(h, level, blocks_all);
   k_elementwise<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, op);
+  h->launches++;
 }
 
 void launch_transfer(olgpu_hierarchy *h, const Transfer &X)
@@ -327,6 +332,7 @@ void launch_transfer(olgpu_hierarchy *h, const Transfer &X)
   if (X.jobs.empty()) return;
   k_transfer<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F,
                                                             h->d_tab);
+  h->launches++;
 }
 
 int level_order(const olgpu_hierarchy *h, int level) { return h->G.boxes[h->G.first_box[level]].order; }
@@ -374,6 +380,7 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   {
     const BoxList L = level_list(h, k, blocks_all);
     k_full_weight<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F);
+    h->launches++;
   }
   launch_transfer(h, h->xfer_w[k]);
   if (k <= mg) {
@@ -390,6 +397,7 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
                                                      h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
                                                      h->coarse_rtol, &h->d_stats->coarse_norm,
                                                      &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+    h->launches++;
   } else {
     emit_fasn<EQ>(h, k - 1, top);
   }
@@ -400,7 +408,10 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   if (k <= mg) dispatch_robin(h, k, 0);
   dispatch_smooth<EQ>(h, k, h->P.nu2, 2 * k + 1);
   if (k == top && !h->hadm.empty())
+  {
     k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
+    h->launches++;
+  }
 }
 
 olgpu_status build_graph(olgpu_hierarchy *h)
@@ -409,6 +420,7 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
+  h->launches = 0;
   if (h->equation == 1) emit_fasn<1>(h, top, top);
   else emit_fasn<0>(h, top, top);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
@@ -832,5 +844,36 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
 }
 
 double olgpu_last_device_ms(const olgpu_hierarchy *h) { return h ? h->last_ms : 0.0; }
+
+int olgpu_kernels_per_cycle(const olgpu_hierarchy *h) { return h ? h->launches : 0; }
+
+long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level)
+{
+  if (!h || level < 0 || level >= h->G.levels) return 0;
+  long long n = 0;
+  for (int i = 0; i < h->G.boxes_in_level[level]; i++) {
+    const domain &D = h->G.boxes[h->G.first_box[level] + i];
+    n += (long long)(D.n[0] - 2 * D.buf) * (D.n[1] - 2 * D.buf) * (D.n[2] - 2 * D.buf);
+  }
+  return n;
+}
+
+olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, double *ms, int *launches)
+{
+  if (!h || !ms || level < 1 || level >= h->G.levels || sweeps < 1)
+    return fail(OLGPU_ERR_INVALID_ARG, "bad smoother timing request");
+  CUDA_TRY(cudaSetDevice(h->device));
+  const int before = h->launches;
+  CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+  if (h->equation == 1) dispatch_smooth<1>(h, level, sweeps, 0);
+  else dispatch_smooth<0>(h, level, sweeps, 0);
+  CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+  CUDA_TRY(cudaEventSynchronize(h->ev1));
+  CUDA_TRY(cudaGetLastError());
+  *ms = elapsed_ms(h->ev0, h->ev1);
+  if (launches) *launches = h->launches - before;
+  h->launches = before;
+  return OLGPU_OK;
+}
 
 }  // extern "C"
