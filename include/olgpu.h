@@ -145,6 +145,43 @@ long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level);
  * *launches the number of smoother kernels it launched.  Changes u. */
 olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, double *ms, int *launches);
 
+/* One box whose fields the caller already holds in device memory (all
+ * nx*ny*nz doubles, lexicographic, i fastest, ghost layers included). */
+typedef struct {
+  double *u;                    /* in/out: the solution                   */
+  const double *b, *c;          /* puncture coefficients                  */
+  const double *s;              /* source (the reference's rho0 / tau)    */
+  const double *d, *e;          /* scalar-field coefficients, or both NULL */
+  int nx, ny, nz;
+  int order;                    /* 2, 4, 6 or 8; ghost width max(order/2,1) */
+  double dx, dy, dz;
+} olgpu_box_fields;
+
+#define OLGPU_NOALLOC_MAX_SWEEPS 64
+
+/* Non-allocating variant of the multicolour Gauss-Seidel-Newton smoother
+ * (no counterpart in the reference).  Some callers cannot call cudaMalloc:
+ * host codes that hand out all device memory from their own pre-reserved
+ * pool, or serving processes that fix their memory budget at start-up and
+ * must not grow it per request.  This entry point allocates nothing: the
+ * caller passes the box's fields, and the kernel's scratch (the box
+ * descriptor, one residual-norm accumulator per sweep and a NaN flag) lives
+ * in a fixed 2 KiB array in the library's device memory, which every GPU that
+ * loads the library holds until the process exits.
+ *   sweeps: 1..OLGPU_NOALLOC_MAX_SWEEPS (64); more is rejected with
+ *           OLGPU_ERR_INVALID_ARG.
+ *   norms:  host array of `sweeps` doubles, the L-infinity norm of the
+ *           pre-update point residuals of each sweep (may be NULL).
+ *   stream: cudaStream_t to run on (NULL = the default stream); the call
+ *           returns after that stream has finished the sweeps.
+ * The first call on a device looks up the scratch array's device address
+ * (set-up once per device); make that first call before any stream capture.
+ * Every call on a device shares the one scratch array, and the call clears
+ * the parts that must start at zero: calls that overlap on the GPU (from
+ * several host threads or streams) race on it and must be serialised by the
+ * caller. */
+olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int sweeps, double *norms, void *stream);
+
 const char *olgpu_last_error(void);
 const char *olgpu_version(void);
 

@@ -18,7 +18,7 @@ import numpy as np
 from . import _abi
 from ._abi import OlgpuError, check
 
-__all__ = ["Problem", "Elliptic", "parse_olliptic_args", "OlgpuError", "FIELDS"]
+__all__ = ["Problem", "Elliptic", "parse_olliptic_args", "OlgpuError", "FIELDS", "smooth_box_noalloc"]
 
 FIELDS = ("u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v")
 
@@ -230,3 +230,18 @@ class Elliptic:
         n = C.c_int()
         check(self.lib.olgpu_time_smoother(self._h, level, sweeps, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+
+def smooth_box_noalloc(u: int, b: int, c: int, s: int, n, order: int, d, sweeps: int,
+                       dfield: int = 0, efield: int = 0, stream: int = 0) -> List[float]:
+    """Multicolour smoother sweeps on one caller-owned box, without any device
+    allocation by the library (olgpu_smooth_box_noalloc).  u, b, c, s (and
+    the scalar-field d, e) are device addresses of nx*ny*nz doubles; n is
+    (nx, ny, nz), d the spacing (dx, dy, dz).  Returns the per-sweep residual
+    norms.  For callers that own all device memory themselves."""
+    lib = _abi.load()
+    f = _abi.BoxFields(u, b, c, s, dfield or None, efield or None, int(n[0]), int(n[1]), int(n[2]), int(order),
+                       float(d[0]), float(d[1]), float(d[2]))
+    norms = (C.c_double * max(1, int(sweeps)))()
+    check(lib.olgpu_smooth_box_noalloc(C.byref(f), int(sweeps), norms, C.c_void_p(stream or None)))
+    return [norms[i] for i in range(int(sweeps))]

@@ -46,6 +46,17 @@ class Report(C.Structure):
     ]
 
 
+class BoxFields(C.Structure):
+    _fields_ = [
+        ("u", C.c_void_p), ("b", C.c_void_p), ("c", C.c_void_p), ("s", C.c_void_p),
+        ("d", C.c_void_p), ("e", C.c_void_p),
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("order", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+    ]
+
+
+NOALLOC_MAX_SWEEPS = 64
+
 # every exported entry point: name -> (restype, argtypes)
 SIGNATURES = {
     "olgpu_problem_defaults": (None, [C.POINTER(Problem)]),
@@ -67,6 +78,7 @@ SIGNATURES = {
     "olgpu_kernels_per_cycle": (C.c_int, [C.c_void_p]),
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),
     "olgpu_time_smoother": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "olgpu_smooth_box_noalloc": (C.c_int, [C.POINTER(BoxFields), C.c_int, C.POINTER(C.c_double), C.c_void_p]),
     "olgpu_last_error": (C.c_char_p, []),
     "olgpu_version": (C.c_char_p, []),
 }

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -877,3 +878,139 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Non-allocating single-box smoother (olgpu_smooth_box_noalloc)
+//
+// Its scratch is one fixed file-scope device array: the box descriptor the
+// kernel reads, one norm accumulator per sweep and the NaN flag.  In host code
+// the symbol is only a stand-in, so each device's address of it is looked up
+// once with cudaGetSymbolAddress (with that device current) and passed to the
+// kernels.
+// ============================================================================
+namespace {
+
+constexpr int kNoAllocWords = 256;                    // 2 KiB
+constexpr int kNoAllocBoxWords = 32;                  // DevBox, rounded up
+constexpr int kNoAllocNormOff = kNoAllocBoxWords;     // OLGPU_NOALLOC_MAX_SWEEPS slots
+constexpr int kNoAllocNanOff = kNoAllocNormOff + OLGPU_NOALLOC_MAX_SWEEPS;
+static_assert(sizeof(DevBox) <= kNoAllocBoxWords * sizeof(unsigned long long), "box slot too small");
+static_assert(kNoAllocNanOff + 1 <= kNoAllocWords, "scratch too small");
+
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned long long *g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of the scratch array on the current device (set-up once).
+olgpu_status noalloc_scratch(unsigned long long **out)
+{
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(OLGPU_ERR_INVALID_ARG, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(OLGPU_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_addr[dev] = static_cast<unsigned long long *>(p);
+  }
+  *out = g_noalloc_addr[dev];
+  return OLGPU_OK;
+}
+
+template <int ORD, int EQ>
+void noalloc_sweeps(const BoxList &L, const DevBox *box, const DevFields &F, int sweeps, unsigned long long *scr,
+                    cudaStream_t st)
+{
+  for (int s = 0; s < sweeps; s++)
+    for (int color = 0; color < num_colors<ORD>(); color++)
+      k_smooth_color<ORD, EQ><<<L.blk[L.count], kThreads, 0, st>>>(L, box, F, color, scr + kNoAllocNormOff + s,
+                                                                   reinterpret_cast<int *>(scr + kNoAllocNanOff));
+}
+
+template <int EQ>
+void noalloc_dispatch(int order, const BoxList &L, const DevBox *box, const DevFields &F, int sweeps,
+                      unsigned long long *scr, cudaStream_t st)
+{
+  switch (order) {
+  case 2: noalloc_sweeps<2, EQ>(L, box, F, sweeps, scr, st); break;
+  case 4: noalloc_sweeps<4, EQ>(L, box, F, sweeps, scr, st); break;
+  case 6: noalloc_sweeps<6, EQ>(L, box, F, sweeps, scr, st); break;
+  default: noalloc_sweeps<8, EQ>(L, box, F, sweeps, scr, st); break;
+  }
+}
+
+}  // namespace
+
+extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int sweeps, double *norms, void *stream)
+{
+  if (!f || !f->u || !f->b || !f->c || !f->s) return fail(OLGPU_ERR_INVALID_ARG, "null field pointer");
+  if (!(f->order == 2 || f->order == 4 || f->order == 6 || f->order == 8))
+    return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
+  if ((f->d == nullptr) != (f->e == nullptr))
+    return fail(OLGPU_ERR_INVALID_ARG, "d and e must both be given (scalar field) or both be NULL");
+  if (sweeps < 1 || sweeps > OLGPU_NOALLOC_MAX_SWEEPS)
+    return fail(OLGPU_ERR_INVALID_ARG, "sweeps must be 1.." + std::to_string(OLGPU_NOALLOC_MAX_SWEEPS) +
+                                           ": the fixed scratch holds one norm accumulator per sweep");
+  const int buf = f->order / 2;
+  if (f->nx < 2 * buf + 1 || f->ny < 2 * buf + 1 || f->nz < 2 * buf + 1)
+    return fail(OLGPU_ERR_INVALID_ARG, "box has no interior point for this order");
+  if (!(f->dx > 0 && f->dy > 0 && f->dz > 0)) return fail(OLGPU_ERR_INVALID_ARG, "spacing must be > 0");
+  unsigned long long *scr = nullptr;
+  olgpu_status st = noalloc_scratch(&scr);
+  if (st != OLGPU_OK) return st;
+  cudaStream_t cs = static_cast<cudaStream_t>(stream);
+
+  DevBox B{};
+  B.n[0] = f->nx;
+  B.n[1] = f->ny;
+  B.n[2] = f->nz;
+  B.buf = buf;
+  B.order = f->order;
+  B.off = 0;
+  const double d[3] = {f->dx, f->dy, f->dz};
+  for (int a = 0; a < 3; a++) {
+    B.idx[a] = 1.0 / d[a];
+    B.idx2[a] = B.idx[a] * B.idx[a];
+  }
+  const double sum = B.idx2[0] + B.idx2[1] + B.idx2[2];
+  switch (f->order) {
+  case 2: B.dulap = -2.0 * sum; break;
+  case 4: B.dulap = -2.5 * sum; break;
+  case 6: B.dulap = -490 * sum * (1.0 / 180); break;
+  default: B.dulap = -205 * sum / 72.0; break;
+  }
+  // the descriptor and the zeroed accumulators go into the fixed scratch
+  CUDA_TRY(cudaMemcpyAsync(scr, &B, sizeof(DevBox), cudaMemcpyHostToDevice, cs));
+  CUDA_TRY(cudaMemsetAsync(scr + kNoAllocNormOff, 0,
+                           sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1), cs));
+  DevFields F{};
+  F.f[F_U] = f->u;
+  F.f[F_B] = const_cast<double *>(f->b);
+  F.f[F_C] = const_cast<double *>(f->c);
+  F.f[F_RHO] = const_cast<double *>(f->s);
+  F.f[F_D] = const_cast<double *>(f->d);
+  F.f[F_E] = const_cast<double *>(f->e);
+  BoxList L{};
+  L.first = 0;
+  L.count = 1;
+  L.blk[0] = 0;
+  L.blk[1] = (int)blocks_color(B);
+  const DevBox *dbox = reinterpret_cast<const DevBox *>(scr);
+  if (f->d) noalloc_dispatch<1>(f->order, L, dbox, F, sweeps, scr, cs);
+  else noalloc_dispatch<0>(f->order, L, dbox, F, sweeps, scr, cs);
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long host[OLGPU_NOALLOC_MAX_SWEEPS + 1];
+  CUDA_TRY(cudaMemcpyAsync(host, scr + kNoAllocNormOff, sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1),
+                           cudaMemcpyDeviceToHost, cs));
+  CUDA_TRY(cudaStreamSynchronize(cs));
+  if (norms)
+    for (int s = 0; s < sweeps; s++) std::memcpy(&norms[s], &host[s], sizeof(double));
+  int nan_flag = 0;
+  std::memcpy(&nan_flag, &host[OLGPU_NOALLOC_MAX_SWEEPS], sizeof(int));
+  if (nan_flag) return fail(OLGPU_ERR_NAN, "NaN in the smoother");
+  return OLGPU_OK;
+}
