@@ -43,6 +43,10 @@ __device__ __forceinline__ int list_box(const BoxList &L, long long &local_block
 // ----------------------------------------------------------------------------
 // stencils
 // ----------------------------------------------------------------------------
+// The reference divides by 12 (order 4) and by 5040 (order 8, once per
+// axis); here those are multiplications by the rounded reciprocal -- a
+// 1-ulp difference, where an FP64 division costs the GB300 FP64 pipe about as
+// much as the rest of the stencil.
 template <int ORD>
 __device__ __forceinline__ double lap(const double *__restrict__ u, long long p, long long sy,
                                       long long sz, const DevBox &B)
@@ -55,8 +59,8 @@ __device__ __forceinline__ double lap(const double *__restrict__ u, long long p,
   } else if (ORD == 4) {
     return ((-(u[p + 2] + u[p - 2]) + 16.0 * (u[p + 1] + u[p - 1]) - 30.0 * c) * ix2 +
             (-(u[p + 2 * sy] + u[p - 2 * sy]) + 16.0 * (u[p + sy] + u[p - sy]) - 30.0 * c) * iy2 +
-            (-(u[p + 2 * sz] + u[p - 2 * sz]) + 16.0 * (u[p + sz] + u[p - sz]) - 30.0 * c) * iz2) /
-           12.0;
+            (-(u[p + 2 * sz] + u[p - 2 * sz]) + 16.0 * (u[p + sz] + u[p - sz]) - 30.0 * c) * iz2) *
+           (1.0 / 12.0);
   } else if (ORD == 6) {
     const double i180 = 1.0 / 180;
     return (2.0 * (u[p + 3] + u[p - 3]) - 27.0 * (u[p + 2] + u[p - 2] - 10.0 * (u[p + 1] + u[p - 1])) -
@@ -66,24 +70,25 @@ __device__ __forceinline__ double lap(const double *__restrict__ u, long long p,
            (2.0 * (u[p + 3 * sz] + u[p - 3 * sz]) -
             27.0 * (u[p + 2 * sz] + u[p - 2 * sz] - 10.0 * (u[p + sz] + u[p - sz])) - 490.0 * c) * iz2 * i180;
   } else {
-    return (-9.0 * (u[p + 4] + u[p - 4]) + 128.0 * (u[p + 3] + u[p - 3]) - 1008.0 * (u[p + 2] + u[p - 2]) +
-            8064.0 * (u[p + 1] + u[p - 1]) - 14350.0 * c) * ix2 / 5040.0 +
-           (-9.0 * (u[p + 4 * sy] + u[p - 4 * sy]) + 128.0 * (u[p + 3 * sy] + u[p - 3 * sy]) -
-            1008.0 * (u[p + 2 * sy] + u[p - 2 * sy]) + 8064.0 * (u[p + sy] + u[p - sy]) - 14350.0 * c) * iy2 / 5040.0 +
-           (-9.0 * (u[p + 4 * sz] + u[p - 4 * sz]) + 128.0 * (u[p + 3 * sz] + u[p - 3 * sz]) -
-            1008.0 * (u[p + 2 * sz] + u[p - 2 * sz]) + 8064.0 * (u[p + sz] + u[p - sz]) - 14350.0 * c) * iz2 / 5040.0;
+    return ((-9.0 * (u[p + 4] + u[p - 4]) + 128.0 * (u[p + 3] + u[p - 3]) - 1008.0 * (u[p + 2] + u[p - 2]) +
+             8064.0 * (u[p + 1] + u[p - 1]) - 14350.0 * c) * ix2 +
+            (-9.0 * (u[p + 4 * sy] + u[p - 4 * sy]) + 128.0 * (u[p + 3 * sy] + u[p - 3 * sy]) -
+             1008.0 * (u[p + 2 * sy] + u[p - 2 * sy]) + 8064.0 * (u[p + sy] + u[p - sy]) - 14350.0 * c) * iy2 +
+            (-9.0 * (u[p + 4 * sz] + u[p - 4 * sz]) + 128.0 * (u[p + 3 * sz] + u[p - 3 * sz]) -
+             1008.0 * (u[p + 2 * sz] + u[p - 2 * sz]) + 8064.0 * (u[p + sz] + u[p - sz]) - 14350.0 * c) * iz2) *
+           (1.0 / 5040.0);
   }
 }
 
 // Pointwise operator value and its derivative in u (puncture, optionally with
-// the scalar-field terms d (c+u) + e (c+u)^5).  Integer powers by products;
-// one division.
+// the scalar-field terms d (c+u) + e (c+u)^5).  Integer powers by products of
+// one correctly rounded reciprocal.
 template <int EQ>
 __device__ __forceinline__ void point_op(double lapv, double dl, double uu, double bb, double cc,
                                          double dd, double ee, double &op, double &dop)
 {
   const double q = cc + uu;
-  const double iq = 1.0 / q;
+  const double iq = __drcp_rn(q);
   const double iq2 = iq * iq;
   const double iq4 = iq2 * iq2;
   const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
@@ -199,6 +204,16 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long *s
   }
 }
 
+// Inverse of the Newton diagonal dOP/du for the smoother's step.  The step
+// u -= R / dOP only needs the diagonal approximately: a relative error of
+// 2^-23 in it scales the step by 1 +- 1e-7 and leaves the fixed point (R = 0)
+// where it is, so the FP32 reciprocal replaces an FP64 division (the FP64
+// pipe is the bottleneck of this kernel on GB300).
+__device__ __forceinline__ double step_inverse(double dop)
+{
+  return (double)__frcp_rn((float)dop);
+}
+
 // ----------------------------------------------------------------------------
 // K1: multicolour nonlinear Gauss-Seidel-Newton pass.  Colour of a point is
 // (i + j + k) mod NC with NC = ORD/2 + 1, so that no two points of a colour
@@ -238,7 +253,7 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
       point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
                    EQ ? F.f[F_D][B.off + p] : 0.0, EQ ? F.f[F_E][B.off + p] : 0.0, op, dop);
       const double R = op - F.f[F_RHO][B.off + p];
-      const double un = u[p] - R / dop;
+      const double un = u[p] - R * step_inverse(dop);
       u[p] = un;
       rabs = fabs(R);
       if (!(un == un)) atomicOr(nan_flag, 1);
@@ -570,7 +585,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
         double op, dop;
         point_op<EQ>(lv, B.dulap, su[p], gb[p], gc[p], EQ ? gd[p] : 0.0, EQ ? ge[p] : 0.0, op, dop);
         const double R = op - gs[p];
-        su[p] = su[p] - omega * (R / dop);
+        su[p] = su[p] - omega * (R * step_inverse(dop));
         rmax = fmax(rmax, fabs(R));
         if (!(su[p] == su[p])) atomicOr(nan_flag, 1);
       }
