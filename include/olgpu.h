@@ -129,6 +129,17 @@ olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res);
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out);
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
 
+/* Arithmetic of the V-cycle.  OLGPU_PREC_FP64 runs the reference's FAS
+ * cycle in FP64 throughout.  OLGPU_PREC_MIXED keeps u, the defect, the
+ * singular puncture terms b/(c+u)^7 and 1/(c+u), the update and the
+ * convergence norm in FP64 and runs the V-cycle itself (smoothing, Robin
+ * updates, transfers, coarse solve) in FP32 on a correction e to u; it
+ * converges to the same FP64 fixed point.  In mixed mode the cycle's norm
+ * (stop rule, report) is the FP64 L-infinity defect of the finest level after
+ * the update. */
+typedef enum { OLGPU_PREC_FP64 = 0, OLGPU_PREC_MIXED = 1 } olgpu_precision;
+olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision);
+
 /* Reset u to the initial guess (0) and the work fields, keeping the geometry
  * and coefficients, so that one hierarchy can serve repeated solves. */
 olgpu_status olgpu_reset(olgpu_hierarchy *h);

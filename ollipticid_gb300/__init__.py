@@ -204,6 +204,10 @@ class Elliptic:
         check(st)
         return rep
 
+    def set_precision(self, mixed: bool):
+        """FP64 throughout (False) or FP32 correction cycles around FP64 (True)."""
+        check(self.lib.olgpu_set_precision(self._h, _abi.PREC_MIXED if mixed else _abi.PREC_FP64))
+
     def reset(self):
         check(self.lib.olgpu_reset(self._h))
 

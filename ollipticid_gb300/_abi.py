@@ -8,6 +8,7 @@ MAX_BH = 16
 
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_TIMEOUT, ERR_GEOMETRY, ERR_NO_DEVICE = range(9)
 STOP_REFERENCE, STOP_TOLERANCE, STOP_FIXED = range(3)
+PREC_FP64, PREC_MIXED = range(2)
 
 _D16 = C.c_double * MAX_BH
 
@@ -74,6 +75,7 @@ SIGNATURES = {
     "olgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(StopRule), C.POINTER(Report)]),
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_reset": (C.c_int, [C.c_void_p]),
+    "olgpu_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_last_device_ms": (C.c_double, [C.c_void_p]),
     "olgpu_kernels_per_cycle": (C.c_int, [C.c_void_p]),
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),

@@ -1,0 +1,615 @@
+// mixed.cuh -- FP32 inner V-cycle of the mixed-precision solve.
+//
+// The FP64 state u is frozen during a cycle; the cycle solves in FP32 for a
+// correction e on every level with the reference's FAS algorithm
+// (src/elliptic.cc:1468-1968) applied to the correction problem
+//     N(u + e) - N(u) = S - N(u),
+// whose right-hand side (the FP64 defect) and whose per-point coefficients
+// A = b/(c+u)^7 and 1/(c+u) are evaluated in FP64 before the cycle.  With
+// x = e/(c+u) and y = 1/(1+x) the puncture term of the correction operator is
+//     A [(1+x)^-7 - 1] = -A x y (1 + y + ... + y^6),
+// which has no cancellation for small x, so FP32 resolves the correction to
+// FP32 precision relative to the correction itself; the FP64 update u += e
+// then converges to the FP64 fixed point.  The singular factor b/(c+u)^7 is
+// only ever formed in FP64 (at a puncture on a node c+u ~ 1e14 and its 7th
+// power overflows FP32).
+#pragma once
+
+#include "kernels.cuh"
+
+namespace olgpu {
+
+// FP32 work fields of the correction cycle.
+enum Field32 { G_E = 0, G_S, G_A, G_IQ, G_R, G_W, G_WW, G_V, G_T, G_D, G_E5, G_NUM };
+
+struct DevFields32 {
+  float *f[G_NUM];
+};
+
+template <int ORD>
+__device__ __forceinline__ float lapf(const float *__restrict__ u, long long p, long long sy, long long sz,
+                                      const DevBox &B)
+{
+  const float c = u[p];
+  const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
+  if (ORD == 2) {
+    return (u[p + 1] - 2.0f * c + u[p - 1]) * ix2 + (u[p + sy] - 2.0f * c + u[p - sy]) * iy2 +
+           (u[p + sz] - 2.0f * c + u[p - sz]) * iz2;
+  } else if (ORD == 4) {
+    return ((-(u[p + 2] + u[p - 2]) + 16.0f * (u[p + 1] + u[p - 1]) - 30.0f * c) * ix2 +
+            (-(u[p + 2 * sy] + u[p - 2 * sy]) + 16.0f * (u[p + sy] + u[p - sy]) - 30.0f * c) * iy2 +
+            (-(u[p + 2 * sz] + u[p - 2 * sz]) + 16.0f * (u[p + sz] + u[p - sz]) - 30.0f * c) * iz2) *
+           (1.0f / 12.0f);
+  } else if (ORD == 6) {
+    auto ax = [&](long long s) {
+      return 2.0f * (u[p + 3 * s] + u[p - 3 * s]) - 27.0f * (u[p + 2 * s] + u[p - 2 * s]) +
+             270.0f * (u[p + s] + u[p - s]) - 490.0f * c;
+    };
+    return (ax(1) * ix2 + ax(sy) * iy2 + ax(sz) * iz2) * (1.0f / 180.0f);
+  } else {
+    auto ax = [&](long long s) {
+      return -9.0f * (u[p + 4 * s] + u[p - 4 * s]) + 128.0f * (u[p + 3 * s] + u[p - 3 * s]) -
+             1008.0f * (u[p + 2 * s] + u[p - 2 * s]) + 8064.0f * (u[p + s] + u[p - s]) - 14350.0f * c;
+    };
+    return (ax(1) * ix2 + ax(sy) * iy2 + ax(sz) * iz2) * (1.0f / 5040.0f);
+  }
+}
+
+// Correction operator N(u+e) - N(u) at one point and its derivative in e.
+template <int EQ>
+__device__ __forceinline__ void corr_op(float lapv, float dl, float e, float A, float iq, float D, float E5,
+                                        float &op, float &dop)
+{
+  const float x = e * iq;
+  const float y = __frcp_rn(1.0f + x);
+  const float y2 = y * y, y4 = y2 * y2;
+  const float s = 1.0f + y + y2 + y2 * y + y4 + y4 * y + y4 * y2;   // sum_{k=0..6} y^k
+  op = lapv - A * x * y * s;                                        // A ((1+x)^-7 - 1)
+  dop = dl - 7.0f * A * iq * (y4 * y4);                             // -7 A iq (1+x)^-8
+  if (EQ == 1) {
+    // d e + E5 ((1+x)^5 - 1),  E5 = e_coef (c+u)^5
+    op += D * e + E5 * x * (5.0f + x * (10.0f + x * (10.0f + x * (5.0f + x))));
+    const float x1 = 1.0f + x, x2 = x1 * x1;
+    dop += D + 5.0f * E5 * iq * (x2 * x2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 preparation: coefficients of the correction operator on ALL points
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_mx_coeffs(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                   DevFields32 G, int eq)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const long long p = B.off + t;
+  const double q = F.f[F_C][p] + F.f[F_U][p];
+  const double iq = __drcp_rn(q);
+  const double iq2 = iq * iq, iq4 = iq2 * iq2;
+  G.f[G_A][p] = (float)(F.f[F_B][p] * (iq4 * iq2 * iq));
+  G.f[G_IQ][p] = (float)iq;
+  if (eq == 1) {
+    const double q2 = q * q;
+    G.f[G_D][p] = (float)F.f[F_D][p];
+    G.f[G_E5][p] = (float)(F.f[F_E][p] * (q2 * q2 * q));
+  }
+}
+
+// FP64 defect S - OP(u) on INSIDE points into the FP32 source; the other
+// points get S (the operator value there is written by the Robin kernels in
+// mode 2 on boxes with a physical boundary, and stays 0 on refinement ghosts,
+// as the reference's r field does).  Optionally the L-infinity norm.
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                   DevFields32 G, unsigned long long *norm_slot)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  double rabs = 0.0;
+  if (t < n) {
+    const int b = B.buf;
+    const int i = (int)(t % B.n[0]);
+    const long long r = t / B.n[0];
+    const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+    const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
+    const double *u = F.f[F_U] + B.off;
+    double d = F.f[F_RHO][B.off + t];
+    if (inside) {
+      const double lv = lap<ORD>(u, t, B.n[0], (long long)B.n[0] * B.n[1], B);
+      double op, dop;
+      point_op<EQ>(lv, B.dulap, u[t], F.f[F_B][B.off + t], F.f[F_C][B.off + t],
+                   EQ ? F.f[F_D][B.off + t] : 0.0, EQ ? F.f[F_E][B.off + t] : 0.0, op, dop);
+      d = d - op;
+      rabs = fabs(d);
+    }
+    G.f[G_S][B.off + t] = (float)d;
+  }
+  if (norm_slot) block_max_atomic(rabs, norm_slot);
+}
+
+// Robin defect on the physical boundary: S32 = S - (term(u) + u) (FP64).
+template <int ORD>
+__device__ __forceinline__ void mx_robin_defect_point(const DevBox &B, const DevFields &F, const DevFields32 &G,
+                                                      const double *__restrict__ crd, int mask, int i, int j, int k)
+{
+  const double *u = F.f[F_U] + B.off;
+  const long long p = pidx(B, i, j, k);
+  double dF;
+  const double t = robin_term<ORD>(u, B, crd, mask, i, j, k, dF);
+  G.f[G_S][B.off + p] = (float)(F.f[F_RHO][B.off + p] - (t + u[p]));
+}
+
+template <int ORD>
+__global__ void __launch_bounds__(256) k_mx_robin_defect(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                         DevFields32 G, const double *__restrict__ crd)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  // every ghost point of the box: classify by how many axes are in the band
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int i = (int)(t % B.n[0]);
+  const long long r = t / B.n[0];
+  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const int ijk[3] = {i, j, k};
+  int mask = 0;
+  for (int a = 0; a < 3; a++)
+    if (ijk[a] < b || ijk[a] >= B.n[a] - b) mask |= 1 << a;
+  if (mask) mx_robin_defect_point<ORD>(B, F, G, crd, mask, i, j, k);
+}
+
+// u += e over ALL points (the FP64 outer update)
+__global__ void __launch_bounds__(256) k_mx_update(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                   DevFields32 G)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const long long p = B.off + t;
+  F.f[F_U][p] = F.f[F_U][p] + (double)G.f[G_E][p];
+}
+
+// ---------------------------------------------------------------------------
+// FP32 correction cycle
+// ---------------------------------------------------------------------------
+template <int EQ>
+__device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, long long p, float lv, float &op,
+                                        float &dop)
+{
+  const long long q = B.off + p;
+  corr_op<EQ>(lv, (float)B.dulap, G.f[G_E][q], G.f[G_A][q], G.f[G_IQ][q], EQ ? G.f[G_D][q] : 0.0f,
+              EQ ? G.f[G_E5][q] : 0.0f, op, dop);
+}
+
+// One multicolour pass on e (colour (i+j+k) mod (order/2+1)).
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
+                                                  int color, int *nan_flag)
+{
+  constexpr int NC = num_colors<ORD>();
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
+  const int H = (m0 + NC - 1) / NC;
+  const long long t = lb * blockDim.x + threadIdx.x;
+  if (t >= (long long)H * m1 * m2) return;
+  const int ih = (int)(t % H);
+  const long long r = t / H;
+  const int j = b + (int)(r % m1);
+  const int k = b + (int)(r / m1);
+  const int delta = (((color - b - j - k) % NC) + NC) % NC;
+  const int i = b + delta + NC * ih;
+  if (i >= B.n[0] - b) return;
+  float *e = G.f[G_E] + B.off;
+  const long long p = pidx(B, i, j, k);
+  const float lv = lapf<ORD>(e, p, B.n[0], (long long)B.n[0] * B.n[1], B);
+  float op, dop;
+  corr_at<EQ>(B, G, p, lv, op, dop);
+  const float R = op - G.f[G_S][B.off + p];
+  const float en = e[p] - R * __frcp_rn(dop);
+  e[p] = en;
+  if (!(en == en)) atomicOr(nan_flag, 1);
+}
+
+// R = N^u(e) on INSIDE points
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_apply_op32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
+  const long long t = lb * blockDim.x + threadIdx.x;
+  if (t >= (long long)m0 * m1 * m2) return;
+  const int i = b + (int)(t % m0);
+  const long long r = t / m0;
+  const int j = b + (int)(r % m1);
+  const int k = b + (int)(r / m1);
+  const long long p = pidx(B, i, j, k);
+  const float lv = lapf<ORD>(G.f[G_E] + B.off, p, B.n[0], (long long)B.n[0] * B.n[1], B);
+  float op, dop;
+  corr_at<EQ>(B, G, p, lv, op, dop);
+  G.f[G_R][B.off + p] = op;
+}
+
+// one-sided derivative of e along an axis (dx2 for order 2, dx4 otherwise)
+template <int ORD>
+__device__ __forceinline__ float derivf(const float *__restrict__ u, long long p, long long s, int i, int n,
+                                        float id, float &du)
+{
+  if (ORD == 2) {
+    if (i == 0) {
+      du = -1.5f * id;
+      return (-3.0f * u[p] + 4.0f * u[p + s] - u[p + 2 * s]) * 0.5f * id;
+    }
+    if (i == n - 1) {
+      du = 1.5f * id;
+      return (3.0f * u[p] - 4.0f * u[p - s] + u[p - 2 * s]) * 0.5f * id;
+    }
+    du = 0.0f;
+    return (u[p + s] - u[p - s]) * 0.5f * id;
+  } else {
+    const int nm = n % 2 == 0 ? n / 2 : (n - 1) / 2;
+    if (i <= nm) {
+      du = -25.0f * id * (1.0f / 12.0f);
+      return -(25.0f * u[p] - 48.0f * u[p + s] + 36.0f * u[p + 2 * s] - 16.0f * u[p + 3 * s] + 3.0f * u[p + 4 * s]) *
+             id * (1.0f / 12.0f);
+    }
+    du = 25.0f * id * (1.0f / 12.0f);
+    return (25.0f * u[p] - 48.0f * u[p - s] + 36.0f * u[p - 2 * s] - 16.0f * u[p - 3 * s] + 3.0f * u[p - 4 * s]) *
+           id * (1.0f / 12.0f);
+  }
+}
+
+// Robin on e: mode 0 Newton update with source G_S, mode 1 operator into G_R.
+// The condition is linear, so its correction form is the condition itself.
+template <int ORD>
+__device__ __forceinline__ void robin32_point(const DevBox &B, const DevFields32 &G, const double *__restrict__ crd,
+                                              int mode, int mask, int i, int j, int k)
+{
+  float *e = G.f[G_E] + B.off;
+  const float x = (float)crd[B.coord_off + i];
+  const float y = (float)crd[B.coord_off + B.n[0] + j];
+  const float z = (float)crd[B.coord_off + B.n[0] + B.n[1] + k];
+  const float r2 = x * x + y * y + z * z;
+  const long long p = pidx(B, i, j, k);
+  const long long st[3] = {1, (long long)B.n[0], (long long)B.n[0] * B.n[1]};
+  const int ijk[3] = {i, j, k};
+  const float xyz[3] = {x, y, z};
+  float t = 0.0f, dt = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    if (!(mask & (1 << a))) continue;
+    float du;
+    const float dv = derivf<ORD>(e, p, st[a], ijk[a], B.n[a], (float)B.idx[a], du);
+    t += dv / xyz[a];
+    dt += du / xyz[a];
+  }
+  if (mode == 0) {
+    const float Fv = r2 * t + e[p] - G.f[G_S][B.off + p];
+    e[p] = e[p] - Fv / (r2 * dt + 1.0f);
+  } else {
+    G.f[G_R][B.off + p] = r2 * t + e[p];
+  }
+}
+
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin32_faces(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
+                                                       const double *__restrict__ crd, int mode)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const int b = B.buf;
+  long long t = lb * blockDim.x + threadIdx.x;
+  for (int f = 0; f < 6; f++) {
+    const int a = f >> 1, hi = f & 1;
+    const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+    const int m1 = B.n[a1] - 2 * b, m2 = B.n[a2] - 2 * b;
+    const long long cols = (long long)m1 * m2;
+    if (t < cols) {
+      int ijk[3];
+      ijk[a1] = b + (int)(t % m1);
+      ijk[a2] = b + (int)(t / m1);
+      for (int l = 0; l < b; l++) {
+        ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
+        robin32_point<ORD>(B, G, crd, mode, 1 << a, ijk[0], ijk[1], ijk[2]);
+      }
+      return;
+    }
+    t -= cols;
+  }
+}
+
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin32_edges_corners(BoxList L, const DevBox *__restrict__ boxes,
+                                                               DevFields32 G, const double *__restrict__ crd,
+                                                               int mode)
+{
+  const DevBox B = boxes[L.first + blockIdx.x];
+  const int b = B.buf;
+  const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+  for (int pi = 0; pi < 3; pi++) {
+    const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
+    const int m = B.n[fa] - 2 * b;
+    for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
+      const int e = t / m, q = t % m;
+      const int ha = e >> 1, hc = e & 1;
+      int ijk[3];
+      ijk[fa] = b + q;
+      for (int ta = 0; ta < b; ta++)
+        for (int tc = 0; tc < b; tc++) {
+          ijk[a] = ha ? B.n[a] - b + ta : b - 1 - ta;
+          ijk[c] = hc ? B.n[c] - b + tc : b - 1 - tc;
+          robin32_point<ORD>(B, G, crd, mode, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+        }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 8) {
+    const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
+    for (int tk = 0; tk < b; tk++)
+      for (int tj = 0; tj < b; tj++)
+        for (int ti = 0; ti < b; ti++) {
+          const int i = hx ? B.n[0] - b + ti : b - 1 - ti;
+          const int j = hy ? B.n[1] - b + tj : b - 1 - tj;
+          const int k = hz ? B.n[2] - b + tk : b - 1 - tk;
+          robin32_point<ORD>(B, G, crd, mode, 7, i, j, k);
+        }
+  }
+}
+
+enum Ew32Op { EW32_W_EQ_S_MINUS_R = 0, EW32_S_EQ_W_PLUS_R, EW32_W_PLUS_EQ_R, EW32_WW_EQ_E, EW32_V_EQ_E_MINUS_WW,
+              EW32_E_PLUS_EQ_V };
+
+__global__ void __launch_bounds__(256) k_elementwise32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
+                                                       int op)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const long long p = B.off + t;
+  switch (op) {
+  case EW32_W_EQ_S_MINUS_R: G.f[G_W][p] = G.f[G_S][p] - G.f[G_R][p]; break;
+  case EW32_S_EQ_W_PLUS_R: G.f[G_S][p] = G.f[G_W][p] + G.f[G_R][p]; break;
+  case EW32_W_PLUS_EQ_R: G.f[G_W][p] = G.f[G_W][p] + G.f[G_R][p]; break;
+  case EW32_WW_EQ_E: G.f[G_WW][p] = G.f[G_E][p]; break;
+  case EW32_V_EQ_E_MINUS_WW: G.f[G_V][p] = G.f[G_E][p] - G.f[G_WW][p]; break;
+  case EW32_E_PLUS_EQ_V: G.f[G_E][p] = G.f[G_E][p] + G.f[G_V][p]; break;
+  }
+}
+
+// T = (1,2,1)^3/64 average of W on INSIDE points (see k_full_weight)
+__global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int b = B.buf;
+  const int i = (int)(t % B.n[0]);
+  const long long r = t / B.n[0];
+  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const float *w = G.f[G_W] + B.off;
+  const float c = w[t];
+  const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
+  if (!inside) {
+    G.f[G_T][B.off + t] = c;
+    return;
+  }
+  float acc = 0.0f;
+  for (int dk = -1; dk <= 1; dk++)
+    for (int dj = -1; dj <= 1; dj++)
+      for (int di = -1; di <= 1; di++) {
+        const int ii = i + di, jj = j + dj, kk = k + dk;
+        const float wt = (float)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (1.0f / 64.0f);
+        const bool in = ii >= b && ii < B.n[0] - b && jj >= b && jj < B.n[1] - b && kk >= b && kk < B.n[2] - b;
+        acc += wt * (in ? w[pidx(B, ii, jj, kk)] : c);
+      }
+  G.f[G_T][B.off + t] = acc;
+}
+
+// The generic transfer of kernels.cuh on FP32 fields (weights rounded to FP32).
+__global__ void __launch_bounds__(256) k_transfer32(const XferJob *__restrict__ jobs, int njobs,
+                                                    const DevBox *__restrict__ boxes, DevFields32 G,
+                                                    const AxisEntry *__restrict__ tab)
+{
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox T = boxes[J.tbox];
+  if (J.iter != IT_ALL) {
+    const int b = T.buf;
+    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+    if ((J.iter == IT_INSIDE) != inside) return;
+  }
+  float *dst = G.f[J.tfield] + T.off;
+  const long long tp = pidx(T, i, j, k);
+  const AxisEntry &ax = tab[J.tab[0] + i];
+  const AxisEntry &ay = tab[J.tab[1] + j];
+  const AxisEntry &az = tab[J.tab[2] + k];
+  if (!(ax.sel && ay.sel && az.sel)) {
+    if (J.to_zero) dst[tp] = 0.0f;
+    return;
+  }
+  const DevBox S = boxes[J.sbox];
+  const float *src = G.f[J.sfield] + S.off;
+  if (J.method == XM_COPY || (ax.exact && ay.exact && az.exact)) {
+    dst[tp] = src[pidx(S, ax.node, ay.node, az.node)];
+    return;
+  }
+  if (J.method == XM_LINEAR) {
+    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
+    const float dxi = (float)ax.w[0], dxf = (float)ax.w[1], dyi = (float)ay.w[0], dyf = (float)ay.w[1];
+    const float dzi = (float)az.w[0], dzf = (float)az.w[1];
+    dst[tp] = ((src[pidx(S, i0, j0, k0)] * dxi + src[pidx(S, i0 + 1, j0, k0)] * dxf) * dyi +
+               (src[pidx(S, i0, j0 + 1, k0)] * dxi + src[pidx(S, i0 + 1, j0 + 1, k0)] * dxf) * dyf) * dzi +
+              ((src[pidx(S, i0, j0, k0 + 1)] * dxi + src[pidx(S, i0 + 1, j0, k0 + 1)] * dxf) * dyi +
+               (src[pidx(S, i0, j0 + 1, k0 + 1)] * dxi + src[pidx(S, i0 + 1, j0 + 1, k0 + 1)] * dxf) * dyf) * dzf;
+    return;
+  }
+  const int ord = J.ord;
+  const long long sz = (long long)S.n[0] * S.n[1];
+  float fx = 0.0f;
+  for (int I = 0; I <= ord; I++) {
+    float uy = 0.0f;
+    for (int Jj = 0; Jj <= ord; Jj++) {
+      const float *col = src + pidx(S, ax.start + I, ay.start + Jj, az.start);
+      float uz = 0.0f;
+      for (int K = 0; K <= ord; K++) uz += col[K * sz] * (float)az.w[K];
+      uy += uz * (float)ay.w[Jj];
+    }
+    fx += uy * (float)ax.w[I];
+  }
+  dst[tp] = fx;
+}
+
+// Coarsest correction problem in one CTA: repeat { Robin; one red-black SOR
+// sweep } until the sweep norm <= rtol * first, stops changing, or max_it.
+template <int EQ>
+__global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ boxes, int box, DevFields32 G,
+                                                   const double *__restrict__ crd, int max_it, float omega, float rtol,
+                                                   int *iters_out, int *nan_flag)
+{
+  extern __shared__ float se[];
+  __shared__ float red[32];
+  __shared__ float s_norm;
+  __shared__ int s_nan;
+  const DevBox B = boxes[box];
+  const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+  const long long np = (long long)n0 * n1 * n2;
+  float *ge = G.f[G_E] + B.off;
+  const float *gs = G.f[G_S] + B.off, *ga = G.f[G_A] + B.off, *giq = G.f[G_IQ] + B.off;
+  const float *gd = EQ ? G.f[G_D] + B.off : nullptr, *ge5 = EQ ? G.f[G_E5] + B.off : nullptr;
+  for (long long p = threadIdx.x; p < np; p += blockDim.x) se[p] = ge[p];
+  __syncthreads();
+  const int m0 = n0 - 2, m1 = n1 - 2, m2 = n2 - 2;
+  const long long sy = n0, sz = (long long)n0 * n1;
+  const float dl = (float)B.dulap;
+  const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
+  auto robin = [&](int mask, int i, int j, int k) {
+    const float x = (float)crd[B.coord_off + i], y = (float)crd[B.coord_off + n0 + j];
+    const float z = (float)crd[B.coord_off + n0 + n1 + k];
+    const float r2 = x * x + y * y + z * z;
+    const long long p = pidx(B, i, j, k);
+    const long long st[3] = {1, sy, sz};
+    const int ijk[3] = {i, j, k};
+    const float xyz[3] = {x, y, z};
+    float t = 0.0f, dt = 0.0f;
+    for (int a = 0; a < 3; a++) {
+      if (!(mask & (1 << a))) continue;
+      float du;
+      const float dv = derivf<2>(se, p, st[a], ijk[a], B.n[a], (float)B.idx[a], du);
+      t += dv / xyz[a];
+      dt += du / xyz[a];
+    }
+    const float Fv = r2 * t + se[p] - gs[p];
+    se[p] = se[p] - Fv / (r2 * dt + 1.0f);
+  };
+  float norm = 1.0f, prev, first = -1.0f;
+  int it = 0;
+  do {
+    prev = norm;
+    for (int f = 0; f < 6; f++) {
+      const int a = f >> 1, hi = f & 1, a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+      const int c1 = B.n[a1] - 2, c2 = B.n[a2] - 2;
+      for (int t = threadIdx.x; t < c1 * c2; t += blockDim.x) {
+        int ijk[3];
+        ijk[a] = hi ? B.n[a] - 1 : 0;
+        ijk[a1] = 1 + t % c1;
+        ijk[a2] = 1 + t / c1;
+        robin(1 << a, ijk[0], ijk[1], ijk[2]);
+      }
+    }
+    __syncthreads();
+    {
+      const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+      for (int pi = 0; pi < 3; pi++) {
+        const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
+        const int m = B.n[fa] - 2;
+        for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
+          const int e = t / m, q = t % m;
+          int ijk[3];
+          ijk[fa] = 1 + q;
+          ijk[a] = (e >> 1) ? B.n[a] - 1 : 0;
+          ijk[c] = (e & 1) ? B.n[c] - 1 : 0;
+          robin((1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 8)
+      robin(7, (threadIdx.x & 1) ? n0 - 1 : 0, ((threadIdx.x >> 1) & 1) ? n1 - 1 : 0, (threadIdx.x >> 2) ? n2 - 1 : 0);
+    __syncthreads();
+    float rmax = 0.0f;
+    int nan_seen = 0;
+    const int H = (m0 + 1) / 2;
+    for (int color = 0; color < 2; color++) {
+      for (int t = threadIdx.x; t < H * m1 * m2; t += blockDim.x) {
+        const int ih = t % H, r = t / H;
+        const int j = 1 + r % m1, k = 1 + r / m1;
+        const int i = 1 + ((color + 1 + j + k) & 1) + 2 * ih;
+        if (i >= n0 - 1) continue;
+        const long long p = pidx(B, i, j, k);
+        const float c0 = se[p];
+        const float lv = (se[p + 1] - 2.0f * c0 + se[p - 1]) * ix2 + (se[p + sy] - 2.0f * c0 + se[p - sy]) * iy2 +
+                         (se[p + sz] - 2.0f * c0 + se[p - sz]) * iz2;
+        float op, dop;
+        corr_op<EQ>(lv, dl, c0, ga[p], giq[p], EQ ? gd[p] : 0.0f, EQ ? ge5[p] : 0.0f, op, dop);
+        const float R = op - gs[p];
+        const float en = c0 - omega * (R * __frcp_rn(dop));
+        se[p] = en;
+        rmax = fmaxf(rmax, fabsf(R));
+        if (!(en == en)) nan_seen = 1;
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    nan_seen = __syncthreads_or(nan_seen);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = rmax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float m = 0.0f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmaxf(m, red[w]);
+      s_norm = m;
+      s_nan = nan_seen;
+      if (nan_seen) atomicOr(nan_flag, 1);
+    }
+    __syncthreads();
+    norm = s_norm;
+    const int stop_nan = s_nan;
+    __syncthreads();
+    it++;
+    if (first < 0.0f) first = norm;
+    if (stop_nan) break;
+    if (norm <= rtol * first) break;
+  } while (norm > 0.0f && prev != norm && it < max_it);
+  for (long long p = threadIdx.x; p < np; p += blockDim.x) ge[p] = se[p];
+  if (threadIdx.x == 0) *iters_out = it;
+}
+
+}  // namespace olgpu

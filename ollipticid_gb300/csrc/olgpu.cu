@@ -9,6 +9,8 @@
 #include "device.cuh"
 #include "grid.h"
 #include "kernels.cuh"
+#include "coarse_cluster.cuh"
+#include "mixed.cuh"
 
 #include <cuda_runtime.h>
 
@@ -16,6 +18,7 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -86,10 +89,19 @@ struct olgpu_hierarchy {
   double last_ms = 0.0;
   double adm[OLGPU_MAX_BH] = {0};
   int coarse_max_iters = 2000;
+  int coarse_ncta = 0;            // blocks of the coarse-solve cluster (0: one block)
+  size_t coarse_cluster_smem = 0;
   double coarse_omega = 1.85;
   double coarse_rtol = 1e-5;
   double eps_solv = 0, eps_coarse = 0;
   int launches = 0;               // kernels emitted while capturing the V-cycle
+  // mixed precision (FP32 correction cycle around the FP64 state)
+  int precision = OLGPU_PREC_FP64;
+  float *d_arena32 = nullptr;
+  DevFields32 F32{};
+  std::vector<Transfer> restrict_e, xfer_w32, set_in32, prolong_v32, ghost_e;
+  cudaGraphExec_t graph_mixed = nullptr;
+  int launches_mixed = 0;
 };
 
 namespace {
@@ -366,6 +378,84 @@ void dispatch_robin(olgpu_hierarchy *h, int level, int mode)
   else launch_robin<4>(h, level, mode);   // orders 4, 6, 8 share dx4 (src/ffunction.cc:197-282)
 }
 
+template <int EQ, int NCTA>
+cudaError_t launch_coarse_cluster_n(olgpu_hierarchy *h)
+{
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(NCTA, 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = h->coarse_cluster_smem;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = NCTA;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_coarse_cluster<EQ, NCTA>, (const DevBox *)h->d_boxes, h->G.first_box[0], h->F,
+                            (const double *)h->d_coords, h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
+                            h->coarse_rtol, &h->d_stats->coarse_norm, &h->d_stats->coarse_iters,
+                            &h->d_stats->nan_flag);
+}
+
+template <int EQ>
+void launch_coarse_cluster(olgpu_hierarchy *h)
+{
+  if (h->coarse_ncta == 16) launch_coarse_cluster_n<EQ, 16>(h);
+  else launch_coarse_cluster_n<EQ, 8>(h);
+}
+
+// Largest supported cluster for the coarse solve: 16 blocks (non-portable
+// size), else 8, else 0 (one block).
+template <int EQ, int NCTA>
+bool cluster_fits(olgpu_hierarchy *h, size_t smem)
+{
+  auto kern = k_coarse_cluster<EQ, NCTA>;
+  if (NCTA > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(NCTA, 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = NCTA;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n >= 1;
+}
+
+void choose_coarse_cluster(olgpu_hierarchy *h)
+{
+  const DevBox &B = h->hboxes[h->G.first_box[0]];
+  if (B.n[2] > 64 || B.buf != 1) return;
+  for (int ncta : {16, 8}) {
+    const int planes = (B.n[2] + ncta - 1) / ncta;
+    const size_t smem = sizeof(double) * (size_t)planes * B.n[0] * B.n[1];
+    const bool ok = ncta == 16 ? (cluster_fits<0, 16>(h, smem) && cluster_fits<1, 16>(h, smem))
+                               : (cluster_fits<0, 8>(h, smem) && cluster_fits<1, 8>(h, smem));
+    if (ok) {
+      h->coarse_ncta = ncta;
+      h->coarse_cluster_smem = smem;
+      return;
+    }
+  }
+}
+
 template <int EQ>
 void emit_fasn(olgpu_hierarchy *h, int k, int top)
 {
@@ -394,10 +484,13 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   if (k == 1) {
     const DevBox &B = h->hboxes[h->G.first_box[0]];
     const size_t smem = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
-    k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
-                                                     h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
-                                                     h->coarse_rtol, &h->d_stats->coarse_norm,
-                                                     &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+    if (h->coarse_ncta > 0)
+      launch_coarse_cluster<EQ>(h);
+    else
+      k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
+                                                       h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
+                                                       h->coarse_rtol, &h->d_stats->coarse_norm,
+                                                       &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
     h->launches++;
   } else {
     emit_fasn<EQ>(h, k - 1, top);
@@ -413,6 +506,236 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
     k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
     h->launches++;
   }
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision: FP64 preparation, FP32 correction cycle, FP64 update
+// ---------------------------------------------------------------------------
+void launch_transfer32(olgpu_hierarchy *h, const Transfer &X)
+{
+  if (X.jobs.empty()) return;
+  k_transfer32<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32,
+                                                              h->d_tab);
+  h->launches_mixed++;
+}
+
+void launch_ew32(olgpu_hierarchy *h, int level, int op)
+{
+  const BoxList L = level_list(h, level, blocks_all);
+  k_elementwise32<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, op);
+  h->launches_mixed++;
+}
+
+template <int ORD, int EQ>
+void launch_mx_defect(olgpu_hierarchy *h, int level, unsigned long long *slot)
+{
+  const BoxList L = level_list(h, level, blocks_all);
+  k_mx_defect<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->F32, slot);
+  h->launches_mixed++;
+}
+
+template <int EQ>
+void dispatch_mx_defect(olgpu_hierarchy *h, int level, unsigned long long *slot)
+{
+  switch (level_order(h, level)) {
+  case 2: launch_mx_defect<2, EQ>(h, level, slot); break;
+  case 4: launch_mx_defect<4, EQ>(h, level, slot); break;
+  case 6: launch_mx_defect<6, EQ>(h, level, slot); break;
+  default: launch_mx_defect<8, EQ>(h, level, slot); break;
+  }
+}
+
+template <int ORD, int EQ>
+void launch_smooth32(olgpu_hierarchy *h, int level, int nu)
+{
+  const BoxList L = level_list(h, level, blocks_color);
+  for (int s = 0; s < nu; s++)
+    for (int color = 0; color < num_colors<ORD>(); color++) {
+      k_smooth32<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, color,
+                                                                       &h->d_stats->nan_flag);
+      h->launches_mixed++;
+    }
+}
+
+template <int ORD, int EQ>
+void launch_apply_op32(olgpu_hierarchy *h, int level)
+{
+  const BoxList L = level_list(h, level, blocks_inside);
+  k_apply_op32<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32);
+  h->launches_mixed++;
+}
+
+template <int EQ>
+void dispatch_smooth32(olgpu_hierarchy *h, int level, int nu)
+{
+  switch (level_order(h, level)) {
+  case 2: launch_smooth32<2, EQ>(h, level, nu); break;
+  case 4: launch_smooth32<4, EQ>(h, level, nu); break;
+  case 6: launch_smooth32<6, EQ>(h, level, nu); break;
+  default: launch_smooth32<8, EQ>(h, level, nu); break;
+  }
+}
+
+template <int EQ>
+void dispatch_apply_op32(olgpu_hierarchy *h, int level)
+{
+  switch (level_order(h, level)) {
+  case 2: launch_apply_op32<2, EQ>(h, level); break;
+  case 4: launch_apply_op32<4, EQ>(h, level); break;
+  case 6: launch_apply_op32<6, EQ>(h, level); break;
+  default: launch_apply_op32<8, EQ>(h, level); break;
+  }
+}
+
+template <int ORD>
+void launch_robin32(olgpu_hierarchy *h, int level, int mode)
+{
+  const BoxList L = level_list(h, level, blocks_faces);
+  k_robin32_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);
+  k_robin32_edges_corners<ORD><<<L.count, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);
+  h->launches_mixed += 2;
+}
+
+void dispatch_robin32(olgpu_hierarchy *h, int level, int mode)
+{
+  if (level_order(h, level) == 2) launch_robin32<2>(h, level, mode);
+  else launch_robin32<4>(h, level, mode);
+}
+
+template <int EQ>
+void emit_fasn32(olgpu_hierarchy *h, int k)
+{
+  const int mg = h->G.mgrid_levels;
+  if (k <= mg) dispatch_robin32(h, k, 0);
+  dispatch_smooth32<EQ>(h, k, h->P.nu1);
+  launch_transfer32(h, h->restrict_e[k]);
+  dispatch_apply_op32<EQ>(h, k - 1);
+  if (k <= mg) dispatch_robin32(h, k - 1, 1);
+  dispatch_apply_op32<EQ>(h, k);
+  if (k <= mg) dispatch_robin32(h, k, 1);
+  launch_ew32(h, k, EW32_W_EQ_S_MINUS_R);
+  {
+    const BoxList L = level_list(h, k, blocks_all);
+    k_full_weight32<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32);
+    h->launches_mixed++;
+  }
+  launch_transfer32(h, h->xfer_w32[k]);
+  if (k <= mg) {
+    launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R);
+  } else {
+    launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R);
+    launch_transfer32(h, h->set_in32[k]);
+  }
+  launch_ew32(h, k - 1, EW32_WW_EQ_E);
+  if (k == 1) {
+    const DevBox &B = h->hboxes[h->G.first_box[0]];
+    const size_t smem = sizeof(float) * (size_t)B.n[0] * B.n[1] * B.n[2];
+    k_coarse32<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F32, h->d_coords,
+                                                 h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+                                                 &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+    h->launches_mixed++;
+  } else {
+    emit_fasn32<EQ>(h, k - 1);
+  }
+  launch_ew32(h, k - 1, EW32_V_EQ_E_MINUS_WW);
+  launch_transfer32(h, h->prolong_v32[k]);
+  launch_ew32(h, k, EW32_E_PLUS_EQ_V);
+  if (k > mg) launch_transfer32(h, h->ghost_e[k]);
+  if (k <= mg) dispatch_robin32(h, k, 0);
+  dispatch_smooth32<EQ>(h, k, h->P.nu2);
+}
+
+template <int EQ>
+void emit_mixed_cycle(olgpu_hierarchy *h)
+{
+  const int L = h->G.levels, top = L - 1, mg = h->G.mgrid_levels;
+  // FP64: restrict u top-down and refill refinement ghosts bottom-up, so that
+  // the FP32 cycle's transfers of e are exact corrections of those of u
+  for (int k = top; k >= 1; k--) launch_transfer(h, h->restrict_u[k]);
+  for (int k = mg + 1; k <= top; k++) launch_transfer(h, h->ghost_u[k]);
+  // FP64: coefficients of the correction operator and the defect source
+  for (int l = 0; l < L; l++) {
+    const BoxList BL = level_list(h, l, blocks_all);
+    k_mx_coeffs<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, EQ);
+    dispatch_mx_defect<EQ>(h, l, nullptr);
+    if (l <= mg) {
+      if (level_order(h, l) == 2)
+        k_mx_robin_defect<2><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, h->d_coords);
+      else
+        k_mx_robin_defect<4><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, h->d_coords);
+      h->launches_mixed++;
+    }
+    h->launches_mixed++;
+  }
+  const size_t n32 = sizeof(float) * (size_t)h->total_pts;
+  for (int f : {G_E, G_R, G_V}) cudaMemsetAsync(h->F32.f[f], 0, n32, h->stream);
+  // FP32 correction V-cycle
+  emit_fasn32<EQ>(h, top);
+  // FP64 update and the FP64 defect of the finest level as the cycle's norm
+  for (int l = 0; l < L; l++) {
+    const BoxList BL = level_list(h, l, blocks_all);
+    k_mx_update<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32);
+    h->launches_mixed++;
+  }
+  dispatch_mx_defect<EQ>(h, top, &h->d_stats->slots[127]);
+  if (!h->hadm.empty()) {
+    k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
+    h->launches_mixed++;
+  }
+}
+
+Transfer remap(const Transfer &X, int sfield, int tfield)
+{
+  Transfer Y;
+  Y.jobs = X.jobs;
+  Y.blocks = X.blocks;
+  for (auto &J : Y.jobs) {
+    J.sfield = sfield;
+    J.tfield = tfield;
+  }
+  return Y;
+}
+
+// Allocates the FP32 fields and plans and captures the mixed cycle (once).
+olgpu_status build_mixed(olgpu_hierarchy *h)
+{
+  if (h->graph_mixed) return OLGPU_OK;
+  const size_t bytes = sizeof(float) * (size_t)h->total_pts * G_NUM;
+  if (cudaMalloc(&h->d_arena32, bytes) != cudaSuccess) return fail(OLGPU_ERR_OOM, "FP32 arena allocation failed");
+  CUDA_TRY(cudaMemset(h->d_arena32, 0, bytes));
+  for (int f = 0; f < G_NUM; f++) h->F32.f[f] = h->d_arena32 + (size_t)f * h->total_pts;
+  const int L = h->G.levels;
+  h->restrict_e.resize(L);
+  h->xfer_w32.resize(L);
+  h->set_in32.resize(L);
+  h->prolong_v32.resize(L);
+  h->ghost_e.resize(L);
+  for (int k = 1; k < L; k++) {
+    h->restrict_e[k] = remap(h->restrict_u[k], G_E, G_E);
+    h->xfer_w32[k] = remap(h->xfer_w[k], G_T, G_W);
+    h->set_in32[k] = remap(h->set_in[k], G_W, G_S);
+    h->prolong_v32[k] = remap(h->prolong_v[k], G_V, G_V);
+    h->ghost_e[k] = remap(h->ghost_u[k], G_E, G_E);
+  }
+  for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
+    for (auto &X : *vec) {
+      if (X.jobs.empty()) continue;
+      if (cudaMalloc(&X.d_jobs, sizeof(XferJob) * X.jobs.size()) != cudaSuccess)
+        return fail(OLGPU_ERR_OOM, "transfer plan allocation failed");
+      CUDA_TRY(cudaMemcpy(X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size(), cudaMemcpyHostToDevice));
+    }
+  cudaGraph_t g;
+  CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
+  h->launches_mixed = 0;
+  if (h->equation == 1) emit_mixed_cycle<1>(h);
+  else emit_mixed_cycle<0>(h);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("mixed graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph_mixed, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("mixed graph instantiate: ") + cudaGetErrorString(e));
+  return OLGPU_OK;
 }
 
 olgpu_status build_graph(olgpu_hierarchy *h)
@@ -661,6 +984,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     cudaError_t e2 = cudaFuncSetAttribute(k_coarse_solve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e1 != cudaSuccess || e2 != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, "shared memory opt-in failed"));
   }
+  if (!std::getenv("OLGPU_COARSE_ONE_BLOCK")) choose_coarse_cluster(h);
   st = olgpu_reset(h);
   if (st != OLGPU_OK) return cleanup(st);
   // coefficients on the device
@@ -704,6 +1028,10 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->graph_mixed) cudaGraphExecDestroy(h->graph_mixed);
+  for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
+    for (auto &X : *vec) cudaFree(X.d_jobs);
+  cudaFree(h->d_arena32);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   cudaFree(h->d_arena);
@@ -772,11 +1100,12 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h)
 
 static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
 {
-  CUDA_TRY(cudaGraphLaunch(h->graph, h->stream));
+  const bool mixed = h->precision == OLGPU_PREC_MIXED;
+  CUDA_TRY(cudaGraphLaunch(mixed ? h->graph_mixed : h->graph, h->stream));
   CUDA_TRY(cudaMemcpyAsync(h->h_stats, h->d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   const int top = h->G.levels - 1;
-  std::memcpy(res, &h->h_stats->slots[2 * top + 1], sizeof(double));
+  std::memcpy(res, &h->h_stats->slots[mixed ? 127 : 2 * top + 1], sizeof(double));
   const olgpu_problem &P = h->P;
   for (int i = 0; i < P.numbh; i++) {
     double bhmj = 0;
@@ -846,7 +1175,25 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
 
 double olgpu_last_device_ms(const olgpu_hierarchy *h) { return h ? h->last_ms : 0.0; }
 
-int olgpu_kernels_per_cycle(const olgpu_hierarchy *h) { return h ? h->launches : 0; }
+int olgpu_kernels_per_cycle(const olgpu_hierarchy *h)
+{
+  if (!h) return 0;
+  return h->precision == OLGPU_PREC_MIXED ? h->launches_mixed : h->launches;
+}
+
+olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (precision != OLGPU_PREC_FP64 && precision != OLGPU_PREC_MIXED)
+    return fail(OLGPU_ERR_INVALID_ARG, "precision must be OLGPU_PREC_FP64 or OLGPU_PREC_MIXED");
+  CUDA_TRY(cudaSetDevice(h->device));
+  if (precision == OLGPU_PREC_MIXED) {
+    olgpu_status st = build_mixed(h);
+    if (st != OLGPU_OK) return st;
+  }
+  h->precision = precision;
+  return OLGPU_OK;
+}
 
 long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level)
 {

@@ -223,6 +223,7 @@ struct orc_solver {
   int wsmooth;       /* 1: full-weight W over INSIDE points before its transfer */
   double coarse_omega; /* over-relaxation of the coarsest-solve sweeps (1 = reference) */
   double coarse_rtol;  /* also stop once the sweep norm <= rtol * first sweep norm (0 = off) */
+  int extra_coarse;    /* checker option: keep coarsening below 12 points (down to >= 5) */
   double lnorm[64][2]; /* last cycle: smoother norms per level (pre, post) */
   double coarse_norm;
 };
@@ -260,7 +261,7 @@ static int set_grids(orc_solver *S, domvec *Dv, int **ndl_out, int *nlev_out)
   const orc_problem *P = &S->P;
   int Nx = orc_valid_n(P->n);
   double Dx = fabs(P->L) / (double)(Nx - 1.0);   /* src/interface.cc:1061 */
-  int base = 12;                                  /* full domain, :502-506 */
+  int base = S->extra_coarse ? 5 : 12;             /* full domain, :502-506 */
   int cap = 64;
   int *nx = (int *)malloc(sizeof(int) * cap);
   double *dxs = (double *)malloc(sizeof(double) * cap);
@@ -1018,12 +1019,16 @@ void orc_problem_defaults(orc_problem *p)
   p->ps_a2 = 1;
 }
 
-orc_solver *orc_create(const orc_problem *p)
+static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse);
+orc_solver *orc_create(const orc_problem *p) { return orc_create_opt(p, 0); }
+orc_solver *orc_create_extra_coarse(const orc_problem *p) { return orc_create_opt(p, 1); }
+static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
 {
   if (p->numbh < 1 || p->numbh > ORC_MAX_BH) return NULL;
   if (!(p->order == 2 || p->order == 4 || p->order == 6 || p->order == 8)) return NULL;
   orc_solver *S = (orc_solver *)calloc(1, sizeof(orc_solver));
   S->P = *p;
+  S->extra_coarse = extra_coarse;
   S->eps_coarse = 2 * EPS;                          /* src/elliptic.cc:62 */
   S->coarse_cap = 1000000000L;
   S->coarse_omega = 1.0;

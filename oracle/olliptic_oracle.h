@@ -46,6 +46,8 @@ typedef struct {
 
 void orc_problem_defaults(orc_problem *p);
 orc_solver *orc_create(const orc_problem *p);
+/* checker variant: multigrid coarsening continues below 12 points (to >= 5) */
+orc_solver *orc_create_extra_coarse(const orc_problem *p);
 void orc_destroy(orc_solver *s);
 int orc_num_boxes(const orc_solver *s);
 int orc_num_levels(const orc_solver *s);

@@ -58,6 +58,8 @@ def load():
         L.orc_create.restype = C.c_void_p
         L.orc_create.argtypes = [C.POINTER(OrcProblem)]
         L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_create_extra_coarse.restype = C.c_void_p
+        L.orc_create_extra_coarse.argtypes = [C.POINTER(OrcProblem)]
         for f in ("orc_num_boxes", "orc_num_levels", "orc_mgrid_levels"):
             getattr(L, f).restype = C.c_int
             getattr(L, f).argtypes = [C.c_void_p]
@@ -87,7 +89,7 @@ def load():
 class Oracle:
     """One CPU hierarchy, driven like the reference's elliptic object."""
 
-    def __init__(self, params: dict):
+    def __init__(self, params: dict, extra_coarse: bool = False):
         L = load()
         p = OrcProblem()
         p.equation = int(params.get("equation", 0))
@@ -105,7 +107,7 @@ class Oracle:
         p.ps_sigma = float(params.get("ps_sigma", 8.0)); p.ps_a2 = float(params.get("ps_a2", 1.0))
         self.numbh = p.numbh
         self._p = p
-        self._s = L.orc_create(C.byref(p))
+        self._s = (L.orc_create_extra_coarse if extra_coarse else L.orc_create)(C.byref(p))
         if not self._s:
             raise ValueError("oracle could not build the hierarchy")
         self.L = L
