@@ -170,6 +170,65 @@ def _flush_l2(dev):
     torch.cuda.synchronize(dev)
 
 
+def pinned_max_diff(E, a, b):
+    """max |a - b| over the points the discrete system fixes (all points of
+    the base and refinement levels, the interior of coarser multigrid levels)."""
+    worst = 0.0
+    for g, box in enumerate(E.boxes):
+        x, y = a[g], b[g]
+        if box.level < E.mgrid_levels:
+            w = box.buf
+            x, y = x[w:-w, w:-w, w:-w], y[w:-w, w:-w, w:-w]
+        worst = max(worst, float(abs(x - y).max()))
+    return worst
+
+
+def fixed_point(E, tol=1e-14, max_cycles=120):
+    """Drive the FP64 cycle until u stops changing (untimed reference state)."""
+    from ollipticid_gb300 import _abi
+    E.set_precision(False)
+    E.reset()
+    E.Solve(stop=_abi.STOP_FIXED, max_cycles=20)
+    prev = [E.get_field(g) for g in range(len(E.boxes))]
+    for _ in range(max_cycles):
+        E.FASN()
+        cur = [E.get_field(g) for g in range(len(E.boxes))]
+        d = max(float(abs(x - y).max()) for x, y in zip(cur, prev))
+        prev = cur
+        if d <= tol:
+            break
+    return prev
+
+
+def run_mixed(E, P, args, dev, u_fix, adm_fix):
+    """Solves/s of the mixed-precision cycle on the same workload, stopped at
+    the same tolerance on the FP64 defect of the finest level, with its
+    deviation from the FP64 fixed point."""
+    import torch
+    from ollipticid_gb300 import _abi
+    E.set_precision(True)
+    for _ in range(args.warmup):
+        E.reset()
+        E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
+    ms, cycles = 0.0, 0
+    for _ in range(args.steps):
+        _flush_l2(dev)
+        E.reset()
+        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
+        ms += E.last_device_ms
+        cycles += rep.cycles
+    u = [E.get_field(g) for g in range(len(E.boxes))]
+    out = {"value": args.steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / args.steps,
+           "cycles_per_solve": cycles / args.steps, "final_fp64_defect": rep.final_res,
+           "max_abs_u_minus_fp64_fixed_point": pinned_max_diff(E, u, u_fix),
+           "adm_minus_fp64_fixed_point": [a - b for a, b in zip(rep.adm[:2], adm_fix)],
+           "kernels_per_cycle": E.kernels_per_cycle,
+           "dtype": "FP32 inner V-cycle (smoothing, Robin, transfers, coarse solve) on a correction; "
+                    "FP64 defect, singular terms, update and norm"}
+    E.set_precision(False)
+    return out
+
+
 def run_gpu(args, rank: int, world: int, local: int):
     import numpy as np
     import torch
@@ -240,6 +299,16 @@ def run_gpu(args, rank: int, world: int, local: int):
     e2e = {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * total_pts,
            "d2h_bytes_per_step": 8 * total_pts}
 
+    # ---- accuracy of the timed solve against the converged FP64 fixed point
+    u_stop = [E.get_field(g) for g in range(nboxes)]
+    adm_stop = list(reps[-1].adm[:2])
+    u_fix = fixed_point(E)
+    adm_fix = E.ADM_mass
+    err_fp64 = pinned_max_diff(E, u_stop, u_fix)
+
+    # ---- the same workload with the mixed-precision cycle
+    mixed = run_mixed(E, P, args, dev, u_fix, adm_fix)
+
     # ---- roofline of the dominant kernel (multicolour smoother), all levels
     peak, peak_kind = _peaks()
     tot_bytes, tot_ms, tot_launch = 0.0, 0.0, 0
@@ -271,6 +340,9 @@ def run_gpu(args, rank: int, world: int, local: int):
                        "final_res": reps[-1].final_res, "adm": [reps[-1].adm[0], reps[-1].adm[1]],
                        "l2": "256 MiB buffer written before every timed solve", "boxes": nboxes,
                        "points": total_pts, "wall_s": wall},
+            "accuracy": {"max_abs_u_minus_fixed_point": err_fp64,
+                         "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
+            "mixed": mixed,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
         }
@@ -287,10 +359,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-cycle", action="store_true",
                     help="run two V-cycles of the workload and exit (for the ncu launch list)")
+    ap.add_argument("--mixed", action="store_true", help="with --profile-cycle: the mixed-precision cycle")
     args = ap.parse_args()
     if args.profile_cycle:
         import ollipticid_gb300 as og
         E = og.Elliptic(og.parse_olliptic_args(WORKLOAD_ARGS.split()))
+        E.set_precision(args.mixed)
         r = [E.FASN() for _ in range(2)]
         print(json.dumps({"profile_cycles": 2, "res": r, "kernels_per_cycle": E.kernels_per_cycle}))
         E.close()

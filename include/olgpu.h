@@ -135,10 +135,18 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
  * convergence norm in FP64 and runs the V-cycle itself (smoothing, Robin
  * updates, transfers, coarse solve) in FP32 on a correction e to u; it
  * converges to the same FP64 fixed point.  In mixed mode the cycle's norm
- * (stop rule, report) is the FP64 L-infinity defect of the finest level after
- * the update. */
+ * (stop rule, report) is the larger of the FP64 L-infinity defect of the
+ * finest level after the update and the largest correction |e| applied to a
+ * point the discrete system fixes, so that stopping at tol also bounds the
+ * remaining error in u on every level. */
 typedef enum { OLGPU_PREC_FP64 = 0, OLGPU_PREC_MIXED = 1 } olgpu_precision;
 olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision);
+/* Anderson acceleration of the mixed-precision outer iteration with a
+ * history of `depth` corrections (0 = off, 1..4; default 4).  Each cycle's
+ * update becomes u + f - (dU + dF) gamma with gamma the least-squares fit of
+ * the newest correction f by the last `depth` correction differences; the
+ * fixed point is unchanged.  Applies to OLGPU_PREC_MIXED only. */
+olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth);
 
 /* Reset u to the initial guess (0) and the work fields, keeping the geometry
  * and coefficients, so that one hierarchy can serve repeated solves. */

@@ -208,6 +208,10 @@ class Elliptic:
         """FP64 throughout (False) or FP32 correction cycles around FP64 (True)."""
         check(self.lib.olgpu_set_precision(self._h, _abi.PREC_MIXED if mixed else _abi.PREC_FP64))
 
+    def set_acceleration(self, depth: int):
+        """Anderson history depth of the mixed outer iteration (0 = off, 1..4)."""
+        check(self.lib.olgpu_set_acceleration(self._h, int(depth)))
+
     def reset(self):
         check(self.lib.olgpu_reset(self._h))
 

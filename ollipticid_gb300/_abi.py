@@ -76,6 +76,7 @@ SIGNATURES = {
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_reset": (C.c_int, [C.c_void_p]),
     "olgpu_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
+    "olgpu_set_acceleration": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_last_device_ms": (C.c_double, [C.c_void_p]),
     "olgpu_kernels_per_cycle": (C.c_int, [C.c_void_p]),
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),

@@ -165,17 +165,32 @@ __global__ void __launch_bounds__(256) k_mx_robin_defect(BoxList L, const DevBox
   if (mask) mx_robin_defect_point<ORD>(B, F, G, crd, mask, i, j, k);
 }
 
-// u += e over ALL points (the FP64 outer update)
+// u += e over ALL points (the FP64 outer update), and max |e| over the points
+// the discrete system fixes (every point of levels >= mg, the interior of the
+// coarser multigrid levels, whose ghost values are not fixed).
 __global__ void __launch_bounds__(256) k_mx_update(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                   DevFields32 G)
+                                                   DevFields32 G, int mg, unsigned long long *norm_slot)
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
-  if (t >= n) return;
-  const long long p = B.off + t;
-  F.f[F_U][p] = F.f[F_U][p] + (double)G.f[G_E][p];
+  double eabs = 0.0;
+  if (t < n) {
+    const long long p = B.off + t;
+    const double e = (double)G.f[G_E][p];
+    F.f[F_U][p] = F.f[F_U][p] + e;
+    bool pinned = B.level >= mg;
+    if (!pinned) {
+      const int b = B.buf;
+      const int i = (int)(t % B.n[0]);
+      const long long r = t / B.n[0];
+      const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+      pinned = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
+    }
+    if (pinned) eabs = fabs(e);
+  }
+  block_max_atomic(eabs, norm_slot);
 }
 
 // ---------------------------------------------------------------------------
@@ -610,6 +625,150 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
   } while (norm > 0.0f && prev != norm && it < max_it);
   for (long long p = threadIdx.x; p < np; p += blockDim.x) ge[p] = se[p];
   if (threadIdx.x == 0) *iters_out = it;
+}
+
+}  // namespace olgpu
+
+namespace olgpu {
+
+// ---------------------------------------------------------------------------
+// Anderson acceleration of the outer iteration u_{k+1} = Phi(u_k) (one mixed
+// cycle).  With f_k = Phi(u_k) - u_k (the cycle's correction e) and the last
+// m differences dU_j = u_j - u_{j-1}, dF_j = f_j - f_{j-1}:
+//     gamma = argmin || f_k - dF gamma ||_2   (over the pinned points)
+//     u_{k+1} = u_k + f_k - (dU + dF) gamma.
+// A fixed point of Phi is a fixed point of this iteration, so the solution is
+// the same; the slow smooth mode of the FAS-FAC cycle (about 0.65 per cycle
+// on the coarse levels under the refinement boxes) is damped much faster.
+// Differences are stored in FP32 (they are correction-sized); sums in FP64.
+// ---------------------------------------------------------------------------
+constexpr int kAndMax = 4;
+
+struct AndersonState {
+  int k;            // outer iterations done since the last reset
+  int m;            // history depth (<= kAndMax)
+  int k_used;       // iteration the last solve was for
+  int pad;
+  double gram[kAndMax * kAndMax];
+  double rhs[kAndMax];
+  double gamma[kAndMax];
+};
+
+// dF_k = f_k - f_{k-1} into its ring slot, f_prev = f_k, and the normal
+// equations (dF^T dF, dF^T f_k) over pinned points; also max |f_k| pinned.
+__global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__restrict__ f, float *fprev,
+                                                    float *DF, const unsigned char *__restrict__ pinned,
+                                                    AndersonState *st, unsigned long long *fmax_slot)
+{
+  const int k = st->k, m = st->m;
+  const int nc = k < m ? k : m;
+  const int newest = (k + m - 1) % m;   // ring slot of dF_k (k >= 1)
+  double g[kAndMax * (kAndMax + 1) / 2], r[kAndMax];
+  for (int i = 0; i < kAndMax * (kAndMax + 1) / 2; i++) g[i] = 0.0;
+  for (int i = 0; i < kAndMax; i++) r[i] = 0.0;
+  double fm = 0.0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const float fk = f[p];
+    if (k >= 1) DF[(long long)newest * n + p] = fk - fprev[p];
+    fprev[p] = fk;
+    if (!pinned[p]) continue;
+    fm = fmax(fm, (double)fabsf(fk));
+    if (nc == 0) continue;
+    double c[kAndMax];
+    for (int i = 0; i < nc; i++) {
+      const int slot = (newest - i + m) % m;
+      c[i] = (double)DF[(long long)slot * n + p];
+      r[i] += c[i] * (double)fk;
+    }
+    int q = 0;
+    for (int i = 0; i < nc; i++)
+      for (int j = 0; j <= i; j++) g[q++] += c[i] * c[j];
+  }
+  __shared__ double red[32];
+  auto block_sum = [&](double v) -> double {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+    __syncthreads();
+    return s;
+  };
+  int q = 0;
+  for (int i = 0; i < nc; i++) {
+    const double s = block_sum(r[i]);
+    if (threadIdx.x == 0) atomicAdd(&st->rhs[i], s);
+    for (int j = 0; j <= i; j++) {
+      const double t = block_sum(g[q++]);
+      if (threadIdx.x == 0) atomicAdd(&st->gram[i * kAndMax + j], t);
+    }
+  }
+  block_max_atomic(fm, fmax_slot);
+}
+
+// Solves the regularised normal equations for gamma (one thread).
+__global__ void k_and_solve(AndersonState *st)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = st->k, m = st->m;
+  const int nc = k < m ? k : m;
+  double A[kAndMax][kAndMax], b[kAndMax];
+  double tr = 0.0;
+  for (int i = 0; i < nc; i++) {
+    for (int j = 0; j <= i; j++) A[i][j] = A[j][i] = st->gram[i * kAndMax + j];
+    b[i] = st->rhs[i];
+    tr += A[i][i];
+  }
+  for (int i = 0; i < nc; i++) A[i][i] += 1e-10 * tr / (nc > 0 ? nc : 1);
+  bool ok = nc > 0 && tr > 0.0;
+  for (int c = 0; c < nc && ok; c++) {           // Gaussian elimination, partial pivoting
+    int piv = c;
+    for (int i = c + 1; i < nc; i++)
+      if (fabs(A[i][c]) > fabs(A[piv][c])) piv = i;
+    if (!(fabs(A[piv][c]) > 1e-300)) { ok = false; break; }
+    for (int j = 0; j < nc; j++) { const double t = A[c][j]; A[c][j] = A[piv][j]; A[piv][j] = t; }
+    { const double t = b[c]; b[c] = b[piv]; b[piv] = t; }
+    for (int i = c + 1; i < nc; i++) {
+      const double fct = A[i][c] / A[c][c];
+      for (int j = c; j < nc; j++) A[i][j] -= fct * A[c][j];
+      b[i] -= fct * b[c];
+    }
+  }
+  for (int i = nc - 1; i >= 0 && ok; i--) {
+    double s = b[i];
+    for (int j = i + 1; j < nc; j++) s -= A[i][j] * st->gamma[j];
+    st->gamma[i] = s / A[i][i];
+    if (!(st->gamma[i] == st->gamma[i])) ok = false;
+  }
+  if (!ok)
+    for (int i = 0; i < kAndMax; i++) st->gamma[i] = 0.0;
+  for (int i = nc; i < kAndMax; i++) st->gamma[i] = 0.0;
+  st->k_used = k;
+  for (int i = 0; i < kAndMax * kAndMax; i++) st->gram[i] = 0.0;
+  for (int i = 0; i < kAndMax; i++) st->rhs[i] = 0.0;
+  st->k = k + 1;
+}
+
+// u_{k+1} = u_k + f_k - sum gamma_i (dU_i + dF_i); stores dU_{k+1}.
+__global__ void __launch_bounds__(256) k_and_update(long long n, double *u, const float *__restrict__ f, float *DU,
+                                                    const float *__restrict__ DF, const AndersonState *st)
+{
+  const int k = st->k_used, m = st->m;
+  const int nc = k < m ? k : m;
+  const int newest = (k + m - 1) % m;
+  const int out = k % m;                  // ring slot of dU_{k+1}
+  double gam[kAndMax];
+  for (int i = 0; i < kAndMax; i++) gam[i] = st->gamma[i];
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    double step = (double)f[p];
+    for (int i = 0; i < nc; i++) {
+      const int slot = (newest - i + m) % m;
+      step -= gam[i] * ((double)DU[(long long)slot * n + p] + (double)DF[(long long)slot * n + p]);
+    }
+    u[p] = u[p] + step;
+    DU[(long long)out * n + p] = (float)step;
+  }
 }
 
 }  // namespace olgpu

@@ -102,6 +102,12 @@ struct olgpu_hierarchy {
   std::vector<Transfer> restrict_e, xfer_w32, set_in32, prolong_v32, ghost_e;
   cudaGraphExec_t graph_mixed = nullptr;
   int launches_mixed = 0;
+  double last_defect = 0, last_correction = 0;   // parts of the last mixed cycle's norm
+  // Anderson acceleration of the mixed outer iteration
+  int anderson_m = kAndMax;
+  float *d_and = nullptr;               // DU[m], DF[m], fprev (FP32, total_pts each)
+  unsigned char *d_pinned = nullptr;    // points the discrete system fixes
+  AndersonState *d_and_state = nullptr;
 };
 
 namespace {
@@ -672,10 +678,22 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   // FP32 correction V-cycle
   emit_fasn32<EQ>(h, top);
   // FP64 update and the FP64 defect of the finest level as the cycle's norm
-  for (int l = 0; l < L; l++) {
-    const BoxList BL = level_list(h, l, blocks_all);
-    k_mx_update<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32);
-    h->launches_mixed++;
+  if (h->anderson_m > 0) {
+    const long long n = h->total_pts;
+    float *DU = h->d_and, *DF = h->d_and + (size_t)kAndMax * n, *fprev = h->d_and + (size_t)2 * kAndMax * n;
+    const int nblk = 152 * 4;
+    k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E], fprev, DF, h->d_pinned, h->d_and_state,
+                                                    &h->d_stats->slots[126]);
+    k_and_solve<<<1, 32, 0, h->stream>>>(h->d_and_state);
+    k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U], h->F32.f[G_E], DU, DF, h->d_and_state);
+    h->launches_mixed += 3;
+  } else {
+    for (int l = 0; l < L; l++) {
+      const BoxList BL = level_list(h, l, blocks_all);
+      k_mx_update<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, mg,
+                                                                &h->d_stats->slots[126]);
+      h->launches_mixed++;
+    }
   }
   dispatch_mx_defect<EQ>(h, top, &h->d_stats->slots[127]);
   if (!h->hadm.empty()) {
@@ -694,6 +712,16 @@ Transfer remap(const Transfer &X, int sfield, int tfield)
     J.tfield = tfield;
   }
   return Y;
+}
+
+olgpu_status reset_anderson(olgpu_hierarchy *h)
+{
+  if (!h->d_and_state) return OLGPU_OK;
+  AndersonState st{};
+  st.m = h->anderson_m > 0 ? h->anderson_m : 1;
+  CUDA_TRY(cudaMemcpyAsync(h->d_and_state, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return OLGPU_OK;
 }
 
 // Allocates the FP32 fields and plans and captures the mixed cycle (once).
@@ -724,6 +752,27 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
         return fail(OLGPU_ERR_OOM, "transfer plan allocation failed");
       CUDA_TRY(cudaMemcpy(X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size(), cudaMemcpyHostToDevice));
     }
+  {
+    const size_t n = (size_t)h->total_pts;
+    if (cudaMalloc(&h->d_and, sizeof(float) * n * (2 * kAndMax + 1)) != cudaSuccess ||
+        cudaMalloc(&h->d_pinned, n) != cudaSuccess || cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess)
+      return fail(OLGPU_ERR_OOM, "Anderson history allocation failed");
+    std::vector<unsigned char> pin(n, 1);
+    for (const DevBox &B : h->hboxes) {
+      if (B.level >= h->G.mgrid_levels) continue;
+      for (int k = 0; k < B.n[2]; k++)
+        for (int j = 0; j < B.n[1]; j++)
+          for (int i = 0; i < B.n[0]; i++) {
+            const bool in = i >= B.buf && i < B.n[0] - B.buf && j >= B.buf && j < B.n[1] - B.buf && k >= B.buf &&
+                            k < B.n[2] - B.buf;
+            if (!in) pin[B.off + ((size_t)k * B.n[1] + j) * B.n[0] + i] = 0;
+          }
+    }
+    CUDA_TRY(cudaMemcpy(h->d_pinned, pin.data(), n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(h->d_and, 0, sizeof(float) * n * (2 * kAndMax + 1)));
+    olgpu_status st = reset_anderson(h);
+    if (st != OLGPU_OK) return st;
+  }
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
@@ -1032,6 +1081,9 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   cudaFree(h->d_arena32);
+  cudaFree(h->d_and);
+  cudaFree(h->d_pinned);
+  cudaFree(h->d_and_state);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   cudaFree(h->d_arena);
@@ -1095,7 +1147,7 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h)
   for (int f : {F_U, F_RHO, F_R, F_W, F_WW, F_V, F_T}) CUDA_TRY(cudaMemsetAsync(h->F.f[f], 0, n, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   std::fill(h->adm, h->adm + OLGPU_MAX_BH, 0.0);
-  return OLGPU_OK;
+  return reset_anderson(h);
 }
 
 static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
@@ -1106,6 +1158,13 @@ static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   const int top = h->G.levels - 1;
   std::memcpy(res, &h->h_stats->slots[mixed ? 127 : 2 * top + 1], sizeof(double));
+  if (mixed) {   // norm of a mixed cycle: max(finest FP64 defect, max |correction|)
+    double corr;
+    std::memcpy(&corr, &h->h_stats->slots[126], sizeof(double));
+    h->last_defect = *res;
+    h->last_correction = corr;
+    if (corr > *res) *res = corr;
+  }
   const olgpu_problem &P = h->P;
   for (int i = 0; i < P.numbh; i++) {
     double bhmj = 0;
@@ -1179,6 +1238,31 @@ int olgpu_kernels_per_cycle(const olgpu_hierarchy *h)
 {
   if (!h) return 0;
   return h->precision == OLGPU_PREC_MIXED ? h->launches_mixed : h->launches;
+}
+
+olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (depth < 0 || depth > kAndMax) return fail(OLGPU_ERR_INVALID_ARG, "acceleration depth must be 0..4");
+  CUDA_TRY(cudaSetDevice(h->device));
+  if (h->graph_mixed && (depth > 0) != (h->anderson_m > 0)) {   // the graph's shape changes
+    cudaGraphExecDestroy(h->graph_mixed);
+    h->graph_mixed = nullptr;
+    h->anderson_m = depth;
+    for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
+      for (auto &X : *vec) { cudaFree(X.d_jobs); X.d_jobs = nullptr; }
+    cudaFree(h->d_arena32); h->d_arena32 = nullptr;
+    cudaFree(h->d_and); h->d_and = nullptr;
+    cudaFree(h->d_pinned); h->d_pinned = nullptr;
+    cudaFree(h->d_and_state); h->d_and_state = nullptr;
+    if (h->precision == OLGPU_PREC_MIXED) {
+      olgpu_status st = build_mixed(h);
+      if (st != OLGPU_OK) return st;
+    }
+    return OLGPU_OK;
+  }
+  h->anderson_m = depth;
+  return reset_anderson(h);
 }
 
 olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
