@@ -129,6 +129,19 @@ olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res);
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out);
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
 
+/* Asynchronous stepping, for hosts that drive several solves at once (each
+ * hierarchy has its own CUDA stream, so cycles of different hierarchies run
+ * concurrently on the GPU).  olgpu_cycle_launch enqueues one V-cycle and
+ * returns; olgpu_cycle_poll reports whether it finished (wait != 0 blocks)
+ * and then its norm (*res) -- the same norm olgpu_vcycle returns. */
+olgpu_status olgpu_cycle_launch(olgpu_hierarchy *h);
+olgpu_status olgpu_cycle_poll(olgpu_hierarchy *h, int wait, int *done, double *res);
+/* Solves n problems concurrently, each under the same stop rule (rule NULL =
+ * the reference's), stepping every unfinished one each round; reports[i]
+ * (may be NULL) gets the i-th problem's report.  Returns the first failure
+ * status, if any. */
+olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule *rule, olgpu_report *reports);
+
 /* Arithmetic of the V-cycle.  OLGPU_PREC_FP64 runs the reference's FAS
  * cycle in FP64 throughout.  OLGPU_PREC_MIXED keeps u, the defect, the
  * singular puncture terms b/(c+u)^7 and 1/(c+u), the update and the

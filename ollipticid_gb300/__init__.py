@@ -18,7 +18,8 @@ import numpy as np
 from . import _abi
 from ._abi import OlgpuError, check
 
-__all__ = ["Problem", "Elliptic", "parse_olliptic_args", "OlgpuError", "FIELDS", "smooth_box_noalloc"]
+__all__ = ["Problem", "Elliptic", "parse_olliptic_args", "OlgpuError", "FIELDS", "smooth_box_noalloc",
+           "solve_many"]
 
 FIELDS = ("u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v")
 
@@ -212,6 +213,16 @@ class Elliptic:
         """Anderson history depth of the mixed outer iteration (0 = off, 1..4)."""
         check(self.lib.olgpu_set_acceleration(self._h, int(depth)))
 
+    def cycle_launch(self):
+        """Enqueue one V-cycle without waiting (see cycle_poll)."""
+        check(self.lib.olgpu_cycle_launch(self._h))
+
+    def cycle_poll(self, wait: bool = False):
+        """(done, norm) of the last launched cycle."""
+        done, r = C.c_int(), C.c_double()
+        check(self.lib.olgpu_cycle_poll(self._h, int(wait), C.byref(done), C.byref(r)))
+        return bool(done.value), r.value
+
     def reset(self):
         check(self.lib.olgpu_reset(self._h))
 
@@ -253,3 +264,17 @@ def smooth_box_noalloc(u: int, b: int, c: int, s: int, n, order: int, d, sweeps:
     norms = (C.c_double * max(1, int(sweeps)))()
     check(lib.olgpu_smooth_box_noalloc(C.byref(f), int(sweeps), norms, C.c_void_p(stream or None)))
     return [norms[i] for i in range(int(sweeps))]
+
+
+def solve_many(solvers: Sequence["Elliptic"], stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000,
+               tol: float = 0.0) -> List["_abi.Report"]:
+    """Solve several problems concurrently on the GPU (olgpu_solve_many)."""
+    lib = _abi.load()
+    n = len(solvers)
+    hs = (C.c_void_p * n)(*[s._h.value if isinstance(s._h, C.c_void_p) else s._h for s in solvers])
+    reps = (_abi.Report * n)()
+    rule = _abi.StopRule(stop, max_cycles, tol)
+    check(lib.olgpu_solve_many(hs, n, C.byref(rule), reps))
+    for s, r in zip(solvers, reps):
+        s.last_report = r
+    return list(reps)

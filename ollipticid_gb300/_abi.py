@@ -74,6 +74,9 @@ SIGNATURES = {
     "olgpu_vcycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(StopRule), C.POINTER(Report)]),
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "olgpu_cycle_launch": (C.c_int, [C.c_void_p]),
+    "olgpu_cycle_poll": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "olgpu_solve_many": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(StopRule), C.POINTER(Report)]),
     "olgpu_reset": (C.c_int, [C.c_void_p]),
     "olgpu_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_set_acceleration": (C.c_int, [C.c_void_p, C.c_int]),

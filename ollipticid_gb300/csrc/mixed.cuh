@@ -656,9 +656,14 @@ struct AndersonState {
 
 // dF_k = f_k - f_{k-1} into its ring slot, f_prev = f_k, and the normal
 // equations (dF^T dF, dF^T f_k) over pinned points; also max |f_k| pinned.
+// Per-block partial sums go to part[blockIdx.x * kAndPart + ...] and are added
+// in block order by k_and_solve, so the result does not depend on scheduling.
+constexpr int kAndPart = kAndMax * (kAndMax + 1) / 2 + kAndMax;
+
 __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__restrict__ f, float *fprev,
                                                     float *DF, const unsigned char *__restrict__ pinned,
-                                                    AndersonState *st, unsigned long long *fmax_slot)
+                                                    const AndersonState *st, double *part,
+                                                    unsigned long long *fmax_slot)
 {
   const int k = st->k, m = st->m;
   const int nc = k < m ? k : m;
@@ -695,29 +700,39 @@ __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__
     __syncthreads();
     return s;
   };
+  double *mine = part + (long long)blockIdx.x * kAndPart;
   int q = 0;
   for (int i = 0; i < nc; i++) {
     const double s = block_sum(r[i]);
-    if (threadIdx.x == 0) atomicAdd(&st->rhs[i], s);
+    if (threadIdx.x == 0) mine[kAndMax * (kAndMax + 1) / 2 + i] = s;
     for (int j = 0; j <= i; j++) {
-      const double t = block_sum(g[q++]);
-      if (threadIdx.x == 0) atomicAdd(&st->gram[i * kAndMax + j], t);
+      const double t = block_sum(g[q]);
+      if (threadIdx.x == 0) mine[q] = t;
+      q++;
     }
   }
   block_max_atomic(fm, fmax_slot);
 }
 
 // Solves the regularised normal equations for gamma (one thread).
-__global__ void k_and_solve(AndersonState *st)
+__global__ void k_and_solve(AndersonState *st, const double *__restrict__ part, int nblocks)
 {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int k = st->k, m = st->m;
   const int nc = k < m ? k : m;
   double A[kAndMax][kAndMax], b[kAndMax];
   double tr = 0.0;
+  int q = 0;
   for (int i = 0; i < nc; i++) {
-    for (int j = 0; j <= i; j++) A[i][j] = A[j][i] = st->gram[i * kAndMax + j];
-    b[i] = st->rhs[i];
+    double s = 0.0;
+    for (int blk = 0; blk < nblocks; blk++) s += part[(long long)blk * kAndPart + kAndMax * (kAndMax + 1) / 2 + i];
+    b[i] = s;
+    for (int j = 0; j <= i; j++) {
+      double t = 0.0;
+      for (int blk = 0; blk < nblocks; blk++) t += part[(long long)blk * kAndPart + q];
+      A[i][j] = A[j][i] = t;
+      q++;
+    }
     tr += A[i][i];
   }
   for (int i = 0; i < nc; i++) A[i][i] += 1e-10 * tr / (nc > 0 ? nc : 1);

@@ -86,6 +86,7 @@ struct olgpu_hierarchy {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_cycle = nullptr;   // end of the last enqueued cycle
   double last_ms = 0.0;
   double adm[OLGPU_MAX_BH] = {0};
   int coarse_max_iters = 2000;
@@ -108,6 +109,7 @@ struct olgpu_hierarchy {
   float *d_and = nullptr;               // DU[m], DF[m], fprev (FP32, total_pts each)
   unsigned char *d_pinned = nullptr;    // points the discrete system fixes
   AndersonState *d_and_state = nullptr;
+  double *d_and_part = nullptr;         // per-block partial sums of the Anderson fit
 };
 
 namespace {
@@ -683,8 +685,8 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     float *DU = h->d_and, *DF = h->d_and + (size_t)kAndMax * n, *fprev = h->d_and + (size_t)2 * kAndMax * n;
     const int nblk = 152 * 4;
     k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E], fprev, DF, h->d_pinned, h->d_and_state,
-                                                    &h->d_stats->slots[126]);
-    k_and_solve<<<1, 32, 0, h->stream>>>(h->d_and_state);
+                                                    h->d_and_part, &h->d_stats->slots[126]);
+    k_and_solve<<<1, 32, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
     k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U], h->F32.f[G_E], DU, DF, h->d_and_state);
     h->launches_mixed += 3;
   } else {
@@ -755,7 +757,8 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
   {
     const size_t n = (size_t)h->total_pts;
     if (cudaMalloc(&h->d_and, sizeof(float) * n * (2 * kAndMax + 1)) != cudaSuccess ||
-        cudaMalloc(&h->d_pinned, n) != cudaSuccess || cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess)
+        cudaMalloc(&h->d_pinned, n) != cudaSuccess || cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess ||
+        cudaMalloc(&h->d_and_part, sizeof(double) * 152 * 4 * kAndPart) != cudaSuccess)
       return fail(OLGPU_ERR_OOM, "Anderson history allocation failed");
     std::vector<unsigned char> pin(n, 1);
     for (const DevBox &B : h->hboxes) {
@@ -1002,7 +1005,8 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     return s;
   };
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_cycle, cudaEventDisableTiming) != cudaSuccess)
     return cleanup(fail(OLGPU_ERR_CUDA, "stream/event creation failed"));
   const size_t arena = sizeof(double) * (size_t)h->total_pts * F_NUM;
   cudaError_t e = cudaMalloc(&h->d_arena, arena);
@@ -1084,6 +1088,7 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   cudaFree(h->d_and);
   cudaFree(h->d_pinned);
   cudaFree(h->d_and_state);
+  cudaFree(h->d_and_part);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   cudaFree(h->d_arena);
@@ -1095,6 +1100,7 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   if (h->h_stats) cudaFreeHost(h->h_stats);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->ev_cycle) cudaEventDestroy(h->ev_cycle);
   if (h->stream) cudaStreamDestroy(h->stream);
   if (prev >= 0) cudaSetDevice(prev);
   delete h;
@@ -1150,12 +1156,21 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h)
   return reset_anderson(h);
 }
 
-static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
+// Enqueues one cycle (graph + copy of its norms to pinned host memory) and
+// records h->ev_cycle after it; returns at once.
+static olgpu_status cycle_enqueue(olgpu_hierarchy *h)
 {
   const bool mixed = h->precision == OLGPU_PREC_MIXED;
   CUDA_TRY(cudaGraphLaunch(mixed ? h->graph_mixed : h->graph, h->stream));
   CUDA_TRY(cudaMemcpyAsync(h->h_stats, h->d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, h->stream));
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaEventRecord(h->ev_cycle, h->stream));
+  return OLGPU_OK;
+}
+
+// Reads a finished cycle's norms: the cycle's norm, the ADM masses, NaN.
+static olgpu_status cycle_finish(olgpu_hierarchy *h, double *res)
+{
+  const bool mixed = h->precision == OLGPU_PREC_MIXED;
   const int top = h->G.levels - 1;
   std::memcpy(res, &h->h_stats->slots[mixed ? 127 : 2 * top + 1], sizeof(double));
   if (mixed) {   // norm of a mixed cycle: max(finest FP64 defect, max |correction|)
@@ -1178,6 +1193,40 @@ static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
   return OLGPU_OK;
 }
 
+static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
+{
+  olgpu_status st = cycle_enqueue(h);
+  if (st != OLGPU_OK) return st;
+  CUDA_TRY(cudaEventSynchronize(h->ev_cycle));
+  return cycle_finish(h, res);
+}
+
+// Stop-rule bookkeeping shared by olgpu_solve and olgpu_solve_many.
+struct SolveTrack {
+  olgpu_stop_rule R;
+  double tol;
+  double res = 1e12, res_prev = 1e12;
+  int cycles = 0;
+  bool done = false;
+  olgpu_status status = OLGPU_OK;
+  olgpu_report rep{};
+
+  // Records one finished cycle; returns true once the rule stops the solve.
+  bool step(olgpu_status s, double r)
+  {
+    res_prev = res;
+    res = r;
+    if (cycles < 256) rep.res[cycles] = r;
+    cycles++;
+    status = s;
+    if (s != OLGPU_OK || cycles >= R.max_cycles) return true;
+    if (R.stop == OLGPU_STOP_FIXED) return false;
+    if (!(res > tol)) return true;
+    if (R.stop == OLGPU_STOP_REFERENCE && !(res < res_prev)) return true;
+    return false;
+  }
+};
+
 olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res)
 {
   if (!h || !res) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
@@ -1190,39 +1239,99 @@ olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res)
   return s;
 }
 
+static olgpu_status make_track(olgpu_hierarchy *h, const olgpu_stop_rule *rule, SolveTrack &T)
+{
+  T.R = olgpu_stop_rule{OLGPU_STOP_REFERENCE, 100000, 0.0};
+  if (rule) T.R = *rule;
+  if (T.R.max_cycles <= 0) return fail(OLGPU_ERR_INVALID_ARG, "max_cycles must be > 0");
+  T.tol = T.R.tol > 0 ? T.R.tol : h->eps_solv;
+  return OLGPU_OK;
+}
+
+static void close_track(olgpu_hierarchy *h, SolveTrack &T, olgpu_report *out)
+{
+  T.rep.cycles = T.cycles;
+  T.rep.status = T.status;
+  T.rep.final_res = T.res;
+  for (int i = 0; i < h->P.numbh; i++) T.rep.adm[i] = h->adm[i];
+  if (out) *out = T.rep;
+}
+
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out)
 {
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
-  olgpu_stop_rule R{OLGPU_STOP_REFERENCE, 100000, 0.0};
-  if (rule) R = *rule;
-  if (R.max_cycles <= 0) return fail(OLGPU_ERR_INVALID_ARG, "max_cycles must be > 0");
-  const double tol = R.tol > 0 ? R.tol : h->eps_solv;
+  SolveTrack T;
+  olgpu_status st = make_track(h, rule, T);
+  if (st != OLGPU_OK) return st;
   CUDA_TRY(cudaSetDevice(h->device));
   CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
-  double res = 1e12, res_prev;
-  int c = 0;
-  olgpu_status s = OLGPU_OK;
-  olgpu_report rep{};
   for (;;) {
-    res_prev = res;
-    s = run_cycle(h, &res);
-    if (c < 256) rep.res[c] = res;
-    c++;
-    if (s != OLGPU_OK) break;
-    if (c >= R.max_cycles) break;
-    if (R.stop == OLGPU_STOP_FIXED) continue;
-    if (!(res > tol)) break;
-    if (R.stop == OLGPU_STOP_REFERENCE && !(res < res_prev)) break;
+    double r = 0;
+    olgpu_status s = run_cycle(h, &r);
+    if (T.step(s, r)) break;
   }
   cudaEventRecord(h->ev1, h->stream);
   cudaEventSynchronize(h->ev1);
   h->last_ms = elapsed_ms(h->ev0, h->ev1);
-  rep.cycles = c;
-  rep.status = s;
-  rep.final_res = res;
-  for (int i = 0; i < h->P.numbh; i++) rep.adm[i] = h->adm[i];
-  if (out) *out = rep;
-  return s;
+  close_track(h, T, out);
+  return T.status;
+}
+
+olgpu_status olgpu_cycle_launch(olgpu_hierarchy *h)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  CUDA_TRY(cudaSetDevice(h->device));
+  return cycle_enqueue(h);
+}
+
+olgpu_status olgpu_cycle_poll(olgpu_hierarchy *h, int wait, int *done, double *res)
+{
+  if (!h || !done || !res) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  CUDA_TRY(cudaSetDevice(h->device));
+  *done = 0;
+  if (wait) {
+    CUDA_TRY(cudaEventSynchronize(h->ev_cycle));
+  } else {
+    const cudaError_t e = cudaEventQuery(h->ev_cycle);
+    if (e == cudaErrorNotReady) return OLGPU_OK;
+    if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("cycle: ") + cudaGetErrorString(e));
+  }
+  *done = 1;
+  return cycle_finish(h, res);
+}
+
+olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule *rule, olgpu_report *reports)
+{
+  if (!hs || n <= 0) return fail(OLGPU_ERR_INVALID_ARG, "no hierarchies");
+  std::vector<SolveTrack> T(n);
+  for (int i = 0; i < n; i++) {
+    if (!hs[i]) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy in the set");
+    olgpu_status st = make_track(hs[i], rule, T[i]);
+    if (st != OLGPU_OK) return st;
+  }
+  olgpu_status worst = OLGPU_OK;
+  for (;;) {
+    int active = 0;
+    for (int i = 0; i < n; i++)   // enqueue every unfinished solve: their streams overlap on the GPU
+      if (!T[i].done) {
+        olgpu_status st = olgpu_cycle_launch(hs[i]);
+        if (st != OLGPU_OK) return st;
+        active++;
+      }
+    if (!active) break;
+    for (int i = 0; i < n; i++)
+      if (!T[i].done) {
+        int done = 0;
+        double r = 0;
+        olgpu_status s = olgpu_cycle_poll(hs[i], 1, &done, &r);
+        if (T[i].step(s, r)) {
+          T[i].done = true;
+          if (s != OLGPU_OK) worst = s;
+        }
+      }
+  }
+  for (int i = 0; i < n; i++) close_track(hs[i], T[i], reports ? &reports[i] : nullptr);
+  return worst;
 }
 
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
@@ -1255,6 +1364,7 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
     cudaFree(h->d_and); h->d_and = nullptr;
     cudaFree(h->d_pinned); h->d_pinned = nullptr;
     cudaFree(h->d_and_state); h->d_and_state = nullptr;
+    cudaFree(h->d_and_part); h->d_and_part = nullptr;
     if (h->precision == OLGPU_PREC_MIXED) {
       olgpu_status st = build_mixed(h);
       if (st != OLGPU_OK) return st;

@@ -1,0 +1,39 @@
+"""The continuous-batching server: requests that arrive while others are on
+the GPU are admitted as slots free up, run concurrently, and each result is
+the same as the same request solved alone (bit for bit: no kernel's
+arithmetic depends on scheduling); memory admission refuses a request that
+can never fit."""
+import numpy as np
+import pytest
+
+from tests.cases import problem
+
+NAMES = ["o2_single", "o4_spin", "o4_binary_merge", "sf_binary", "o6_boost_y"]
+
+
+@pytest.mark.gpu
+def test_served_results_match_solo_solves():
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    from ollipticid_gb300.serve import Server
+    probs = [problem(n) for n in NAMES]
+    stream = [(0.002 * i, p) for i, p in enumerate(probs)]
+    rep = Server(max_active=3, keep_u=True, tol=1e-11).run(stream)
+    assert rep["completed"] == len(probs)
+    assert rep["peak_concurrent_solves"] >= 2          # the work overlapped
+    for p, r in zip(probs, rep["results"]):
+        with og.Elliptic(p) as E:
+            E.set_precision(True)
+            solo = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-11)
+            u = [E.get_field(g) for g in range(len(E.boxes))]
+        assert r.status == 0 and r.cycles == solo.cycles
+        err = max(float(np.max(np.abs(a - b))) for a, b in zip(u, r.u))
+        assert err == 0.0, err
+
+
+@pytest.mark.gpu
+def test_request_larger_than_the_budget_is_refused():
+    from ollipticid_gb300 import _abi
+    from ollipticid_gb300.serve import Server
+    rep = Server(mem_budget=1 << 20).run([(0.0, problem("o4_spin"))])
+    assert rep["results"][0].status == _abi.ERR_OOM
