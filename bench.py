@@ -229,6 +229,53 @@ def run_mixed(E, P, args, dev, u_fix, adm_fix):
     return out
 
 
+def run_batched(args, count: int = 16, group: int = 8):
+    """Seeded batched binaries (mixed precision, tol 1e-10): solves/s when
+    `group` solves run concurrently, and the same instances one at a time."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi, workloads
+    probs = workloads.batched_binaries(256)[:count]
+    seq_s, con_s, cycles = 0.0, 0.0, []
+    for g0 in range(0, count, group):
+        sol = [og.Elliptic(p) for p in probs[g0:g0 + group]]
+        for E in sol:
+            E.set_precision(True)
+        for E in sol:                                   # warm-up
+            E.reset()
+        og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+        t = time.perf_counter()
+        for E in sol:
+            E.reset()
+            E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+        seq_s += time.perf_counter() - t
+        for E in sol:
+            E.reset()
+        t = time.perf_counter()
+        reps = og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+        con_s += time.perf_counter() - t
+        cycles += [r.cycles for r in reps]
+        for E in sol:
+            E.close()
+    return {"workload": f"first {count} of 256 seeded binaries (N in {{33,49,65,97}}, 6-10 levels, O4), "
+                        f"mixed precision to 1e-10", "concurrent_solves": group,
+            "value": count / con_s, "unit": UNIT, "one_at_a_time": count / seq_s,
+            "cycles_mean": sum(cycles) / len(cycles), "timing": "host wall clock around the solves"}
+
+
+def run_served(rates=(4.0, 16.0), count: int = 24):
+    """Poisson request streams (NumBH 1-4, N 33-129, orders 2-8, 6-10
+    levels, 10% scalar field) served with memory admission."""
+    from ollipticid_gb300 import workloads
+    from ollipticid_gb300.serve import Server
+    out = []
+    for rate in rates:
+        rep = Server(mem_budget=120 << 30, max_active=16).run(workloads.served_stream(count, rate))
+        out.append({"rate_hz": rate, "requests": count,
+                    **{k: rep[k] for k in ("throughput_solves_per_s", "latency_p50_s", "latency_p99_s",
+                                           "latency_max_s", "cycles_mean", "peak_concurrent_solves", "makespan_s")}})
+    return out
+
+
 def run_gpu(args, rank: int, world: int, local: int):
     import numpy as np
     import torch
@@ -309,6 +356,11 @@ def run_gpu(args, rank: int, world: int, local: int):
     # ---- the same workload with the mixed-precision cycle
     mixed = run_mixed(E, P, args, dev, u_fix, adm_fix)
 
+    batched = served = None
+    if rank == 0 and world == 1 and not args.no_extra:
+        batched = run_batched(args)
+        served = run_served()
+
     # ---- roofline of the dominant kernel (multicolour smoother), all levels
     peak, peak_kind = _peaks()
     tot_bytes, tot_ms, tot_launch = 0.0, 0.0, 0
@@ -342,7 +394,7 @@ def run_gpu(args, rank: int, world: int, local: int):
                        "points": total_pts, "wall_s": wall},
             "accuracy": {"max_abs_u_minus_fixed_point": err_fp64,
                          "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
-            "mixed": mixed,
+            "mixed": mixed, "batched": batched, "served": served,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
         }
@@ -357,6 +409,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched and served sub-results")
     ap.add_argument("--profile-cycle", action="store_true",
                     help="run two V-cycles of the workload and exit (for the ncu launch list)")
     ap.add_argument("--mixed", action="store_true", help="with --profile-cycle: the mixed-precision cycle")
