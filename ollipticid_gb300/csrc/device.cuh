@@ -48,6 +48,9 @@ struct AxisEntry {
   int exact;      // coincides with source node `node` (3-epsilon test)
   int node;       // source node for the exact copy
   int start;      // first source index of the interpolation window
+  int lo, hi;     // window terms [lo, hi] to sum: one term when the weights
+                  // are exactly one-hot (then the sum equals that term bit for bit)
+  int pad[2];
   double w[kMaxInterpPoints];
 };
 

@@ -421,9 +421,67 @@ __global__ void __launch_bounds__(256) k_full_weight(BoxList L, const DevBox *__
 // generic inter-box transfer (restriction, tau transfer, prolongation, ghost
 // fill, tau mask) driven by host-built per-axis interpolation tables
 // ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_transfer(const XferJob *__restrict__ jobs, int njobs,
-                                                  const DevBox *__restrict__ boxes, DevFields F,
-                                                  const AxisEntry *__restrict__ tab)
+// Tensor Lagrange sum over the window at `base`: z innermost, then y, then x
+// (the reference's order); the terms of an axis outside its [lo, hi] (all but
+// one where the weights are exactly one-hot) are skipped, which leaves the sum
+// unchanged bit for bit.  P points per axis are unrolled at compile time, so
+// the window's loads are independent and issue together instead of one per
+// accumulation step.
+template <class T, int P>
+__device__ __forceinline__ T tensor_sum(const T *__restrict__ base, long long sy, long long sz, const AxisEntry &ax,
+                                        const AxisEntry &ay, const AxisEntry &az)
+{
+  T wz[P];
+#pragma unroll
+  for (int K = 0; K < P; K++) wz[K] = (T)az.w[K];
+  T fx = T(0);
+#pragma unroll
+  for (int I = 0; I < P; I++) {
+    if (I < ax.lo || I > ax.hi) continue;
+    T uy = T(0);
+#pragma unroll
+    for (int Jj = 0; Jj < P; Jj++) {
+      if (Jj < ay.lo || Jj > ay.hi) continue;
+      const T *col = base + I + Jj * sy;
+      T uz = T(0);
+#pragma unroll
+      for (int K = 0; K < P; K++)
+        if (K >= az.lo && K <= az.hi) uz += col[K * sz] * wz[K];
+      uy += uz * (T)ay.w[Jj];
+    }
+    fx += uy * (T)ax.w[I];
+  }
+  return fx;
+}
+
+// The same sum for any window width (at most kMaxInterpPoints).
+template <class T>
+__device__ __forceinline__ T tensor_sum_any(const T *__restrict__ base, long long sy, long long sz,
+                                            const AxisEntry &ax, const AxisEntry &ay, const AxisEntry &az)
+{
+  T fx = T(0);
+  for (int I = ax.lo; I <= ax.hi; I++) {
+    T uy = T(0);
+    for (int Jj = ay.lo; Jj <= ay.hi; Jj++) {
+      const T *col = base + I + Jj * sy;
+      T uz = T(0);
+      for (int K = az.lo; K <= az.hi; K++) uz += col[K * sz] * (T)az.w[K];
+      uy += uz * (T)ay.w[Jj];
+    }
+    fx += uy * (T)ax.w[I];
+  }
+  return fx;
+}
+
+// One launch runs every job of a transfer plan; V is the field type (double
+// for the FP64 fields, float for the FP32 correction fields).  P is the
+// plan's Lagrange window width (0: the plan has copy / linear jobs only, -1:
+// a width without its own instantiation), so each width is a kernel of its
+// own with its own register budget.
+template <class V, class Fields, int P>
+__global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, int njobs,
+                                              const DevBox *__restrict__ boxes, Fields F,
+                                              const AxisEntry *__restrict__ tab)
 {
   int jb = 0;
   {
@@ -449,48 +507,53 @@ __global__ void __launch_bounds__(256) k_transfer(const XferJob *__restrict__ jo
     const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
     if ((J.iter == IT_INSIDE) != inside) return;
   }
-  double *dst = F.f[J.tfield] + T.off;
+  V *dst = F.f[J.tfield] + T.off;
   const long long tp = pidx(T, i, j, k);
   const AxisEntry &ax = tab[J.tab[0] + i];
   const AxisEntry &ay = tab[J.tab[1] + j];
   const AxisEntry &az = tab[J.tab[2] + k];
   if (!(ax.sel && ay.sel && az.sel)) {
-    if (J.to_zero) dst[tp] = 0.0;
+    if (J.to_zero) dst[tp] = V(0);
     return;
   }
   const DevBox S = boxes[J.sbox];
-  const double *src = F.f[J.sfield] + S.off;
+  const V *src = F.f[J.sfield] + S.off;
   if (J.method == XM_COPY || (ax.exact && ay.exact && az.exact)) {
     dst[tp] = src[pidx(S, ax.node, ay.node, az.node)];
     return;
   }
-  if (J.method == XM_LINEAR) {
+  if (J.method == XM_LINEAR || P == 0) {
     // ((v000 dxi + v100 dxf) dyi + (v010 dxi + v110 dxf) dyf) dzi + (...) dzf
     const int i0 = ax.start, j0 = ay.start, k0 = az.start;
-    const double dxi = ax.w[0], dxf = ax.w[1], dyi = ay.w[0], dyf = ay.w[1], dzi = az.w[0], dzf = az.w[1];
-    const double v000 = src[pidx(S, i0, j0, k0)], v100 = src[pidx(S, i0 + 1, j0, k0)];
-    const double v010 = src[pidx(S, i0, j0 + 1, k0)], v110 = src[pidx(S, i0 + 1, j0 + 1, k0)];
-    const double v001 = src[pidx(S, i0, j0, k0 + 1)], v101 = src[pidx(S, i0 + 1, j0, k0 + 1)];
-    const double v011 = src[pidx(S, i0, j0 + 1, k0 + 1)], v111 = src[pidx(S, i0 + 1, j0 + 1, k0 + 1)];
+    const V dxi = (V)ax.w[0], dxf = (V)ax.w[1], dyi = (V)ay.w[0], dyf = (V)ay.w[1], dzi = (V)az.w[0],
+            dzf = (V)az.w[1];
+    const V v000 = src[pidx(S, i0, j0, k0)], v100 = src[pidx(S, i0 + 1, j0, k0)];
+    const V v010 = src[pidx(S, i0, j0 + 1, k0)], v110 = src[pidx(S, i0 + 1, j0 + 1, k0)];
+    const V v001 = src[pidx(S, i0, j0, k0 + 1)], v101 = src[pidx(S, i0 + 1, j0, k0 + 1)];
+    const V v011 = src[pidx(S, i0, j0 + 1, k0 + 1)], v111 = src[pidx(S, i0 + 1, j0 + 1, k0 + 1)];
     dst[tp] = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
               ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
     return;
   }
-  // tensor Lagrange: z innermost, then y, then x
-  const int ord = J.ord;
-  double fx = 0.0;
-  for (int I = 0; I <= ord; I++) {
-    double uy = 0.0;
-    for (int Jj = 0; Jj <= ord; Jj++) {
-      double uz = 0.0;
-      const double *col = src + pidx(S, ax.start + I, ay.start + Jj, az.start);
-      const long long sz = (long long)S.n[0] * S.n[1];
-      for (int K = 0; K <= ord; K++) uz += col[K * sz] * az.w[K];
-      uy += uz * ay.w[Jj];
-    }
-    fx += uy * ax.w[I];
+  const V *base = src + pidx(S, ax.start, ay.start, az.start);
+  const long long sy = S.n[0], sz = (long long)S.n[0] * S.n[1];
+  if (P > 0) dst[tp] = tensor_sum<V, (P > 0 ? P : 1)>(base, sy, sz, ax, ay, az);
+  else dst[tp] = tensor_sum_any<V>(base, sy, sz, ax, ay, az);
+}
+
+// Window width P of a plan's kernel: 0 without Lagrange jobs, the Lagrange
+// order + 1 when it has an instantiation, else -1.
+inline int xfer_width(const XferJob *jobs, size_t n)
+{
+  int w = 0;
+  for (size_t q = 0; q < n; q++) {
+    if (jobs[q].method != XM_LAGRANGE) continue;
+    const int p = jobs[q].ord + 1;
+    const int pw = (p == 3 || p == 4 || p == 6 || p == 8 || p == 10) ? p : -1;
+    if (w == 0) w = pw;
+    else if (w != pw) w = -1;
   }
-  dst[tp] = fx;
+  return w;
 }
 
 // ----------------------------------------------------------------------------

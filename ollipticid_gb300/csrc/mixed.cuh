@@ -436,72 +436,6 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
   G.f[G_T][B.off + t] = acc;
 }
 
-// The generic transfer of kernels.cuh on FP32 fields (weights rounded to FP32).
-__global__ void __launch_bounds__(256) k_transfer32(const XferJob *__restrict__ jobs, int njobs,
-                                                    const DevBox *__restrict__ boxes, DevFields32 G,
-                                                    const AxisEntry *__restrict__ tab)
-{
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
-    else hi = mid - 1;
-  }
-  const XferJob J = jobs[lo];
-  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
-  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
-  if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
-  const DevBox T = boxes[J.tbox];
-  if (J.iter != IT_ALL) {
-    const int b = T.buf;
-    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
-    if ((J.iter == IT_INSIDE) != inside) return;
-  }
-  float *dst = G.f[J.tfield] + T.off;
-  const long long tp = pidx(T, i, j, k);
-  const AxisEntry &ax = tab[J.tab[0] + i];
-  const AxisEntry &ay = tab[J.tab[1] + j];
-  const AxisEntry &az = tab[J.tab[2] + k];
-  if (!(ax.sel && ay.sel && az.sel)) {
-    if (J.to_zero) dst[tp] = 0.0f;
-    return;
-  }
-  const DevBox S = boxes[J.sbox];
-  const float *src = G.f[J.sfield] + S.off;
-  if (J.method == XM_COPY || (ax.exact && ay.exact && az.exact)) {
-    dst[tp] = src[pidx(S, ax.node, ay.node, az.node)];
-    return;
-  }
-  if (J.method == XM_LINEAR) {
-    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
-    const float dxi = (float)ax.w[0], dxf = (float)ax.w[1], dyi = (float)ay.w[0], dyf = (float)ay.w[1];
-    const float dzi = (float)az.w[0], dzf = (float)az.w[1];
-    dst[tp] = ((src[pidx(S, i0, j0, k0)] * dxi + src[pidx(S, i0 + 1, j0, k0)] * dxf) * dyi +
-               (src[pidx(S, i0, j0 + 1, k0)] * dxi + src[pidx(S, i0 + 1, j0 + 1, k0)] * dxf) * dyf) * dzi +
-              ((src[pidx(S, i0, j0, k0 + 1)] * dxi + src[pidx(S, i0 + 1, j0, k0 + 1)] * dxf) * dyi +
-               (src[pidx(S, i0, j0 + 1, k0 + 1)] * dxi + src[pidx(S, i0 + 1, j0 + 1, k0 + 1)] * dxf) * dyf) * dzf;
-    return;
-  }
-  const int ord = J.ord;
-  const long long sz = (long long)S.n[0] * S.n[1];
-  float fx = 0.0f;
-  for (int I = 0; I <= ord; I++) {
-    float uy = 0.0f;
-    for (int Jj = 0; Jj <= ord; Jj++) {
-      const float *col = src + pidx(S, ax.start + I, ay.start + Jj, az.start);
-      float uz = 0.0f;
-      for (int K = 0; K <= ord; K++) uz += col[K * sz] * (float)az.w[K];
-      uy += uz * (float)ay.w[Jj];
-    }
-    fx += uy * (float)ax.w[I];
-  }
-  dst[tp] = fx;
-}
-
 // Coarsest correction problem in one CTA: repeat { Robin; one red-black SOR
 // sweep } until the sweep norm <= rtol * first, stops changing, or max_it.
 template <int EQ>

@@ -50,6 +50,7 @@ constexpr int kThreads = 256;
 struct Transfer {
   std::vector<XferJob> jobs;
   long long blocks = 0;
+  int width = 0;                    // kernel variant (xfer_width of the jobs)
   XferJob *d_jobs = nullptr;
 };
 
@@ -189,6 +190,14 @@ int build_axis(olgpu_hierarchy *h, const domain &T, const domain &S, int a, int 
         else if (s + ord >= S.n[a]) s = S.n[a] - ord - 1;
         e.start = s;
         for (int I = 0; I <= ord; I++) e.w[I] = lagrange_poly(S, a, x, s + I, s, s + ord);
+        e.lo = 0;
+        e.hi = ord;
+        int ones = 0, nonzero = 0, at = 0;
+        for (int I = 0; I <= ord; I++) {
+          if (e.w[I] != 0.0) nonzero++;
+          if (e.w[I] == 1.0) { ones++; at = I; }
+        }
+        if (ones == 1 && nonzero == 1) e.lo = e.hi = at;
       } else {
         const int nn = node == 0 ? 1 : node;
         e.start = nn - 1;
@@ -275,6 +284,7 @@ Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfi
       }
       add_region_jobs(X, J, T, lo, hi);
     }
+  X.width = xfer_width(X.jobs.data(), X.jobs.size());
   return X;
 }
 
@@ -309,6 +319,7 @@ Transfer make_set_in(olgpu_hierarchy *h, int k)
       add_region_jobs(X, J, C, lo, hi);
     }
   }
+  X.width = xfer_width(X.jobs.data(), X.jobs.size());
   return X;
 }
 
@@ -348,11 +359,28 @@ void launch_ew(olgpu_hierarchy *h, int level, int op)
   h->launches++;
 }
 
+// Launches k_xfer for plan X on fields F (double or float fields).
+template <class V, class Fields>
+void launch_xfer(olgpu_hierarchy *h, const Transfer &X, const Fields &F)
+{
+  if (X.jobs.empty()) return;
+  const unsigned nb = (unsigned)X.blocks;
+  const int nj = (int)X.jobs.size();
+  switch (X.width) {
+  case 0: k_xfer<V, Fields, 0><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  case 3: k_xfer<V, Fields, 3><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  case 4: k_xfer<V, Fields, 4><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  case 6: k_xfer<V, Fields, 6><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  case 8: k_xfer<V, Fields, 8><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  case 10: k_xfer<V, Fields, 10><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  default: k_xfer<V, Fields, -1><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+  }
+}
+
 void launch_transfer(olgpu_hierarchy *h, const Transfer &X)
 {
   if (X.jobs.empty()) return;
-  k_transfer<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F,
-                                                            h->d_tab);
+  launch_xfer<double>(h, X, h->F);
   h->launches++;
 }
 
@@ -522,8 +550,7 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
 void launch_transfer32(olgpu_hierarchy *h, const Transfer &X)
 {
   if (X.jobs.empty()) return;
-  k_transfer32<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32,
-                                                              h->d_tab);
+  launch_xfer<float>(h, X, h->F32);
   h->launches_mixed++;
 }
 
@@ -709,6 +736,7 @@ Transfer remap(const Transfer &X, int sfield, int tfield)
   Transfer Y;
   Y.jobs = X.jobs;
   Y.blocks = X.blocks;
+  Y.width = X.width;
   for (auto &J : Y.jobs) {
     J.sfield = sfield;
     J.tfield = tfield;
