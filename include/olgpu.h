@@ -161,6 +161,14 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision);
  * fixed point is unchanged.  Applies to OLGPU_PREC_MIXED only. */
 olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth);
 
+/* Pre- and post-smoothing sweeps of the FP32 correction cycle of
+ * OLGPU_PREC_MIXED (default: the problem's nu1 / nu2).  No reference
+ * counterpart: the reference has no inner cycle.  The FP64 fixed point does
+ * not depend on them, only the work per outer cycle and the number of outer
+ * cycles do.  Re-captures the mixed cycle if it is built and clears the
+ * acceleration history; call between solves.  0 <= nu1 <= 64, 1 <= nu2 <= 64. */
+olgpu_status olgpu_set_inner_sweeps(olgpu_hierarchy *h, int nu1, int nu2);
+
 /* Reset u to the initial guess (0) and the work fields, keeping the geometry
  * and coefficients, so that one hierarchy can serve repeated solves. */
 olgpu_status olgpu_reset(olgpu_hierarchy *h);
@@ -170,11 +178,15 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h);
 double olgpu_last_device_ms(const olgpu_hierarchy *h);
 /* kernel launches in one V-cycle (the captured graph's kernel nodes) */
 int olgpu_kernels_per_cycle(const olgpu_hierarchy *h);
+/* iterations of the coarsest-level solve in the last finished cycle (the
+ * reference prints no such count; diagnostic only) */
+int olgpu_last_coarse_iters(const olgpu_hierarchy *h);
 /* INSIDE points of a level, summed over its boxes (algorithmic work unit) */
 long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level);
 /* Times `sweeps` full smoother sweeps (every colour pass) on one level with
  * CUDA events on the hierarchy's stream; *ms gets the elapsed device time and
- * *launches the number of smoother kernels it launched.  Changes u. */
+ * *launches the number of smoother kernels it launched.  Changes u (FP64
+ * precision) or the FP32 correction e (mixed precision: its smoother). */
 olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, double *ms, int *launches);
 
 /* One box whose fields the caller already holds in device memory (all

@@ -209,6 +209,10 @@ class Elliptic:
         """FP64 throughout (False) or FP32 correction cycles around FP64 (True)."""
         check(self.lib.olgpu_set_precision(self._h, _abi.PREC_MIXED if mixed else _abi.PREC_FP64))
 
+    def set_inner_sweeps(self, nu1: int, nu2: int):
+        """Pre-/post-smoothing sweeps of the FP32 correction cycle (mixed precision)."""
+        check(self.lib.olgpu_set_inner_sweeps(self._h, int(nu1), int(nu2)))
+
     def set_acceleration(self, depth: int):
         """Anderson history depth of the mixed outer iteration (0 = off, 1..4)."""
         check(self.lib.olgpu_set_acceleration(self._h, int(depth)))
@@ -239,6 +243,11 @@ class Elliptic:
     @property
     def kernels_per_cycle(self) -> int:
         return self.lib.olgpu_kernels_per_cycle(self._h)
+
+    @property
+    def last_coarse_iters(self) -> int:
+        """Iterations of the coarsest-level solve in the last finished cycle."""
+        return self.lib.olgpu_last_coarse_iters(self._h)
 
     def interior_points(self, level: int) -> int:
         return int(self.lib.olgpu_level_interior_points(self._h, level))

@@ -25,7 +25,7 @@ CXX = os.environ.get("CXX", "g++")
 
 CU_SOURCES = ["olgpu.cu"]
 CPP_SOURCES = ["grid.cpp"]
-HEADERS = ["device.cuh", "kernels.cuh", "coarse_cluster.cuh", "mixed.cuh", "grid.h", "../../include/olgpu.h"]
+HEADERS = ["device.cuh", "kernels.cuh", "coarse_cluster.cuh", "mixed.cuh", "smooth_cluster.cuh", "grid.h", "../../include/olgpu.h"]
 
 
 def _run(cmd):

@@ -26,33 +26,52 @@ struct DevFields32 {
   float *f[G_NUM];
 };
 
+// Laplacian of e on one point from an accessor at(axis, offset) of its
+// neighbours; every FP32 stencil (global or shared-memory resident) evaluates
+// this one expression, so their results agree bit for bit.
+template <int ORD, class Acc>
+__device__ __forceinline__ float lapf_acc(float c, Acc at, float ix2, float iy2, float iz2)
+{
+  if (ORD == 2) {
+    return (at(0, 1) - 2.0f * c + at(0, -1)) * ix2 + (at(1, 1) - 2.0f * c + at(1, -1)) * iy2 +
+           (at(2, 1) - 2.0f * c + at(2, -1)) * iz2;
+  } else if (ORD == 4) {
+    return ((-(at(0, 2) + at(0, -2)) + 16.0f * (at(0, 1) + at(0, -1)) - 30.0f * c) * ix2 +
+            (-(at(1, 2) + at(1, -2)) + 16.0f * (at(1, 1) + at(1, -1)) - 30.0f * c) * iy2 +
+            (-(at(2, 2) + at(2, -2)) + 16.0f * (at(2, 1) + at(2, -1)) - 30.0f * c) * iz2) *
+           (1.0f / 12.0f);
+  } else if (ORD == 6) {
+    auto ax = [&](int a) {
+      return 2.0f * (at(a, 3) + at(a, -3)) - 27.0f * (at(a, 2) + at(a, -2)) + 270.0f * (at(a, 1) + at(a, -1)) -
+             490.0f * c;
+    };
+    return (ax(0) * ix2 + ax(1) * iy2 + ax(2) * iz2) * (1.0f / 180.0f);
+  } else {
+    auto ax = [&](int a) {
+      return -9.0f * (at(a, 4) + at(a, -4)) + 128.0f * (at(a, 3) + at(a, -3)) - 1008.0f * (at(a, 2) + at(a, -2)) +
+             8064.0f * (at(a, 1) + at(a, -1)) - 14350.0f * c;
+    };
+    return (ax(0) * ix2 + ax(1) * iy2 + ax(2) * iz2) * (1.0f / 5040.0f);
+  }
+}
+
 template <int ORD>
 __device__ __forceinline__ float lapf(const float *__restrict__ u, long long p, long long sy, long long sz,
                                       const DevBox &B)
 {
-  const float c = u[p];
-  const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
-  if (ORD == 2) {
-    return (u[p + 1] - 2.0f * c + u[p - 1]) * ix2 + (u[p + sy] - 2.0f * c + u[p - sy]) * iy2 +
-           (u[p + sz] - 2.0f * c + u[p - sz]) * iz2;
-  } else if (ORD == 4) {
-    return ((-(u[p + 2] + u[p - 2]) + 16.0f * (u[p + 1] + u[p - 1]) - 30.0f * c) * ix2 +
-            (-(u[p + 2 * sy] + u[p - 2 * sy]) + 16.0f * (u[p + sy] + u[p - sy]) - 30.0f * c) * iy2 +
-            (-(u[p + 2 * sz] + u[p - 2 * sz]) + 16.0f * (u[p + sz] + u[p - sz]) - 30.0f * c) * iz2) *
-           (1.0f / 12.0f);
-  } else if (ORD == 6) {
-    auto ax = [&](long long s) {
-      return 2.0f * (u[p + 3 * s] + u[p - 3 * s]) - 27.0f * (u[p + 2 * s] + u[p - 2 * s]) +
-             270.0f * (u[p + s] + u[p - s]) - 490.0f * c;
-    };
-    return (ax(1) * ix2 + ax(sy) * iy2 + ax(sz) * iz2) * (1.0f / 180.0f);
-  } else {
-    auto ax = [&](long long s) {
-      return -9.0f * (u[p + 4 * s] + u[p - 4 * s]) + 128.0f * (u[p + 3 * s] + u[p - 3 * s]) -
-             1008.0f * (u[p + 2 * s] + u[p - 2 * s]) + 8064.0f * (u[p + s] + u[p - s]) - 14350.0f * c;
-    };
-    return (ax(1) * ix2 + ax(sy) * iy2 + ax(sz) * iz2) * (1.0f / 5040.0f);
-  }
+  const long long st[3] = {1, sy, sz};
+  return lapf_acc<ORD>(u[p], [&](int a, int d) { return u[p + d * st[a]]; }, (float)B.idx2[0], (float)B.idx2[1],
+                       (float)B.idx2[2]);
+}
+
+// Hardware approximate reciprocal (PTX rcp.approx.ftz.f32, error within
+// about one ulp).  The FP32 correction cycle only has to converge: the FP64
+// defect that drives it fixes the solution.
+__device__ __forceinline__ float rcp_fast(float x)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
 // Correction operator N(u+e) - N(u) at one point and its derivative in e.
@@ -61,7 +80,7 @@ __device__ __forceinline__ void corr_op(float lapv, float dl, float e, float A, 
                                         float &op, float &dop)
 {
   const float x = e * iq;
-  const float y = __frcp_rn(1.0f + x);
+  const float y = rcp_fast(1.0f + x);
   const float y2 = y * y, y4 = y2 * y2;
   const float s = 1.0f + y + y2 + y2 * y + y4 + y4 * y + y4 * y2;   // sum_{k=0..6} y^k
   op = lapv - A * x * y * s;                                        // A ((1+x)^-7 - 1)
@@ -231,7 +250,7 @@ __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__res
   float op, dop;
   corr_at<EQ>(B, G, p, lv, op, dop);
   const float R = op - G.f[G_S][B.off + p];
-  const float en = e[p] - R * __frcp_rn(dop);
+  const float en = e[p] - R * rcp_fast(dop);
   e[p] = en;
   if (!(en == en)) atomicOr(nan_flag, 1);
 }
@@ -529,7 +548,7 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
         float op, dop;
         corr_op<EQ>(lv, dl, c0, ga[p], giq[p], EQ ? gd[p] : 0.0f, EQ ? ge5[p] : 0.0f, op, dop);
         const float R = op - gs[p];
-        const float en = c0 - omega * (R * __frcp_rn(dop));
+        const float en = c0 - omega * (R * rcp_fast(dop));
         se[p] = en;
         rmax = fmaxf(rmax, fabsf(R));
         if (!(en == en)) nan_seen = 1;

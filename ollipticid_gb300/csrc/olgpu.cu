@@ -11,6 +11,7 @@
 #include "kernels.cuh"
 #include "coarse_cluster.cuh"
 #include "mixed.cuh"
+#include "smooth_cluster.cuh"
 
 #include <cuda_runtime.h>
 
@@ -111,6 +112,13 @@ struct olgpu_hierarchy {
   unsigned char *d_pinned = nullptr;    // points the discrete system fixes
   AndersonState *d_and_state = nullptr;
   double *d_and_part = nullptr;         // per-block partial sums of the Anderson fit
+  // per level: blocks of the cluster that keeps e resident through all sweeps
+  // of the FP32 smoother (0: one launch per colour and sweep) and its shared
+  // memory per block
+  std::vector<int> sc_ncta;
+  std::vector<size_t> sc_smem;
+  // pre-/post-smoothing sweeps of the FP32 correction cycle (-1: nu1/nu2)
+  int inner_nu1 = -1, inner_nu2 = -1;
 };
 
 namespace {
@@ -600,9 +608,130 @@ void launch_apply_op32(olgpu_hierarchy *h, int level)
   h->launches_mixed++;
 }
 
+template <int ORD, int EQ>
+void launch_smooth32_cluster(olgpu_hierarchy *h, int level, int nu)
+{
+  const int ncta = h->sc_ncta[level];
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)(ncta * h->G.boxes_in_level[level]), 1, 1);
+  cfg.blockDim = dim3(kSmoothClusterThreads, 1, 1);
+  cfg.dynamicSmemBytes = h->sc_smem[level];
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ncta;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_smooth32_cluster<ORD, EQ>, (const DevBox *)h->d_boxes, h->G.first_box[level], h->F32,
+                     nu, &h->d_stats->nan_flag);
+  h->launches_mixed++;
+}
+
+// Whether a cluster of ncta blocks of `threads` threads with `smem` bytes of
+// dynamic shared memory each can be resident for kernel `kern`; also raises
+// the kernel's shared-memory limit to the device's opt-in maximum.
+bool cluster_launchable(const void *kern, int ncta, int threads, size_t smem)
+{
+  cudaFuncAttributes fa{};
+  int dev = 0, optin = 0;
+  if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const size_t limit = (size_t)optin - fa.sharedSizeBytes;
+  if (smem > limit) return false;
+  if ((ncta > 8 && cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(ncta, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ncta;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n >= 1;
+}
+
+const void *smooth32_cluster_kernel(int ord, int eq)
+{
+  switch (ord) {
+  case 2: return eq ? (const void *)k_smooth32_cluster<2, 1> : (const void *)k_smooth32_cluster<2, 0>;
+  case 4: return eq ? (const void *)k_smooth32_cluster<4, 1> : (const void *)k_smooth32_cluster<4, 0>;
+  case 6: return eq ? (const void *)k_smooth32_cluster<6, 1> : (const void *)k_smooth32_cluster<6, 0>;
+  default: return eq ? (const void *)k_smooth32_cluster<8, 1> : (const void *)k_smooth32_cluster<8, 0>;
+  }
+}
+
+// Per level: the cluster that keeps e resident through the FP32 smoother, or
+// none.  Every box needs its ghost band at least as wide as the stencil's
+// reach, at most kMaxClusterPlanes planes, one interior plane per block and
+// its largest slab in shared memory.  Of the sizes 8..16 whose largest share
+// of interior planes is smallest (the critical path between two barriers),
+// the fewest blocks are taken: the other SMs stay free for other work.
+void choose_smooth_clusters(olgpu_hierarchy *h)
+{
+  const int L = h->G.levels;
+  h->sc_ncta.assign(L, 0);
+  h->sc_smem.assign(L, 0);
+  if (std::getenv("OLGPU_SMOOTH32_LAUNCHES")) return;
+  for (int l = 0; l < L; l++) {
+    const int ord = level_order(h, l);
+    const void *kern = smooth32_cluster_kernel(ord, h->equation);
+    int best = 0, best_share = 1 << 30;
+    size_t best_smem = 0;
+    for (int ncta = 16; ncta >= 8; ncta--) {
+      size_t smem = 0;
+      int share = 0;
+      bool ok = true;
+      for (int g = h->G.first_box[l]; g < h->G.first_box[l] + h->G.boxes_in_level[l]; g++) {
+        const DevBox &B = h->hboxes[g];
+        const int m2 = B.n[2] - 2 * B.buf;
+        if (m2 < ncta || B.n[2] > kMaxClusterPlanes || B.buf < ord / 2 || B.order != ord) ok = false;
+        share = std::max(share, (m2 + ncta - 1) / ncta);
+        smem = std::max(smem, sizeof(float) * (size_t)slab_max_planes(B.n[2], B.buf, ncta) * B.n[0] * B.n[1]);
+      }
+      if (!ok || share > best_share) continue;
+      if (!cluster_launchable(kern, ncta, kSmoothClusterThreads, smem)) continue;
+      best = ncta;
+      best_share = share;
+      best_smem = smem;
+    }
+    h->sc_ncta[l] = best;
+    h->sc_smem[l] = best_smem;
+    if (std::getenv("OLGPU_VERBOSE"))
+      std::fprintf(stderr, "olgpu: level %d FP32 smoother: %s (%d blocks, %zu B shared memory per block)\n", l,
+                   best ? "cluster-resident" : "one launch per colour", best, best_smem);
+  }
+}
+
 template <int EQ>
 void dispatch_smooth32(olgpu_hierarchy *h, int level, int nu)
 {
+  if (nu <= 0) return;
+  if (h->sc_ncta[level] > 0) {
+    switch (level_order(h, level)) {
+    case 2: launch_smooth32_cluster<2, EQ>(h, level, nu); break;
+    case 4: launch_smooth32_cluster<4, EQ>(h, level, nu); break;
+    case 6: launch_smooth32_cluster<6, EQ>(h, level, nu); break;
+    default: launch_smooth32_cluster<8, EQ>(h, level, nu); break;
+    }
+    return;
+  }
   switch (level_order(h, level)) {
   case 2: launch_smooth32<2, EQ>(h, level, nu); break;
   case 4: launch_smooth32<4, EQ>(h, level, nu); break;
@@ -642,7 +771,7 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
 {
   const int mg = h->G.mgrid_levels;
   if (k <= mg) dispatch_robin32(h, k, 0);
-  dispatch_smooth32<EQ>(h, k, h->P.nu1);
+  dispatch_smooth32<EQ>(h, k, h->inner_nu1 >= 0 ? h->inner_nu1 : h->P.nu1);
   launch_transfer32(h, h->restrict_e[k]);
   dispatch_apply_op32<EQ>(h, k - 1);
   if (k <= mg) dispatch_robin32(h, k - 1, 1);
@@ -677,7 +806,7 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   launch_ew32(h, k, EW32_E_PLUS_EQ_V);
   if (k > mg) launch_transfer32(h, h->ghost_e[k]);
   if (k <= mg) dispatch_robin32(h, k, 0);
-  dispatch_smooth32<EQ>(h, k, h->P.nu2);
+  dispatch_smooth32<EQ>(h, k, h->inner_nu2 >= 0 ? h->inner_nu2 : h->P.nu2);
 }
 
 template <int EQ>
@@ -686,8 +815,11 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   const int L = h->G.levels, top = L - 1, mg = h->G.mgrid_levels;
   // FP64: restrict u top-down and refill refinement ghosts bottom-up, so that
   // the FP32 cycle's transfers of e are exact corrections of those of u
+  const int fp64_before = h->launches;
   for (int k = top; k >= 1; k--) launch_transfer(h, h->restrict_u[k]);
   for (int k = mg + 1; k <= top; k++) launch_transfer(h, h->ghost_u[k]);
+  h->launches_mixed += h->launches - fp64_before;
+  h->launches = fp64_before;
   // FP64: coefficients of the correction operator and the defect source
   for (int l = 0; l < L; l++) {
     const BoxList BL = level_list(h, l, blocks_all);
@@ -754,6 +886,8 @@ olgpu_status reset_anderson(olgpu_hierarchy *h)
   return OLGPU_OK;
 }
 
+olgpu_status capture_mixed(olgpu_hierarchy *h);
+
 // Allocates the FP32 fields and plans and captures the mixed cycle (once).
 olgpu_status build_mixed(olgpu_hierarchy *h)
 {
@@ -803,6 +937,17 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
     CUDA_TRY(cudaMemset(h->d_and, 0, sizeof(float) * n * (2 * kAndMax + 1)));
     olgpu_status st = reset_anderson(h);
     if (st != OLGPU_OK) return st;
+  }
+  choose_smooth_clusters(h);
+  return capture_mixed(h);
+}
+
+// Captures the mixed cycle into h->graph_mixed (replacing an earlier one).
+olgpu_status capture_mixed(olgpu_hierarchy *h)
+{
+  if (h->graph_mixed) {
+    CUDA_TRY(cudaGraphExecDestroy(h->graph_mixed));
+    h->graph_mixed = nullptr;
   }
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -1417,6 +1562,22 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
   return OLGPU_OK;
 }
 
+olgpu_status olgpu_set_inner_sweeps(olgpu_hierarchy *h, int nu1, int nu2)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (nu1 < 0 || nu1 > 64 || nu2 < 1 || nu2 > 64)
+    return fail(OLGPU_ERR_INVALID_ARG, "inner sweeps must satisfy 0 <= nu1 <= 64, 1 <= nu2 <= 64");
+  CUDA_TRY(cudaSetDevice(h->device));
+  h->inner_nu1 = nu1;
+  h->inner_nu2 = nu2;
+  if (!h->graph_mixed) return OLGPU_OK;   // used when the mixed cycle is built
+  olgpu_status st = capture_mixed(h);
+  if (st != OLGPU_OK) return st;
+  return reset_anderson(h);
+}
+
+int olgpu_last_coarse_iters(const olgpu_hierarchy *h) { return h && h->h_stats ? h->h_stats->coarse_iters : 0; }
+
 long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level)
 {
   if (!h || level < 0 || level >= h->G.levels) return 0;
@@ -1433,16 +1594,23 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
   if (!h || !ms || level < 1 || level >= h->G.levels || sweeps < 1)
     return fail(OLGPU_ERR_INVALID_ARG, "bad smoother timing request");
   CUDA_TRY(cudaSetDevice(h->device));
-  const int before = h->launches;
+  const bool mixed = h->precision == OLGPU_PREC_MIXED;
+  int &count = mixed ? h->launches_mixed : h->launches;
+  const int before = count;
   CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
-  if (h->equation == 1) dispatch_smooth<1>(h, level, sweeps, 0);
-  else dispatch_smooth<0>(h, level, sweeps, 0);
+  if (mixed) {   // the FP32 correction smoother on e
+    if (h->equation == 1) dispatch_smooth32<1>(h, level, sweeps);
+    else dispatch_smooth32<0>(h, level, sweeps);
+  } else {
+    if (h->equation == 1) dispatch_smooth<1>(h, level, sweeps, 0);
+    else dispatch_smooth<0>(h, level, sweeps, 0);
+  }
   CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
   CUDA_TRY(cudaEventSynchronize(h->ev1));
   CUDA_TRY(cudaGetLastError());
   *ms = elapsed_ms(h->ev0, h->ev1);
-  if (launches) *launches = h->launches - before;
-  h->launches = before;
+  if (launches) *launches = count - before;
+  count = before;
   return OLGPU_OK;
 }
 

@@ -67,3 +67,50 @@ def test_mixed_stop_rule_bounds_the_error(oracle_mod):
                 w = box.buf
                 a, b = a[w:-w, w:-w, w:-w], b[w:-w, w:-w, w:-w]
             assert float(np.max(np.abs(a - b))) <= U_TOL, g
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["o4_binary_merge", "o8_offset", "sf_binary"])
+def test_cluster_smoother_equals_colour_launches(case, monkeypatch):
+    """The FP32 smoother with e resident in a thread-block cluster's shared
+    memory (every sweep of a level in one launch) gives the per-colour
+    launches' result bit for bit."""
+    import ollipticid_gb300 as og
+    P = problem(case)
+    out = {}
+    for mode in ("cluster", "launches"):
+        if mode == "launches":
+            monkeypatch.setenv("OLGPU_SMOOTH32_LAUNCHES", "1")
+        with og.Elliptic(P) as E:
+            E.set_precision(True)
+            for _ in range(3):
+                E.FASN()
+            out[mode] = ([E.get_field(g) for g in range(len(E.boxes))], E.kernels_per_cycle)
+    (u_cl, k_cl), (u_la, k_la) = out["cluster"], out["launches"]
+    assert k_cl < k_la, "no level took the cluster smoother"
+    for g, (a, b) in enumerate(zip(u_cl, u_la)):
+        assert np.array_equal(a, b), f"box {g}: max diff {float(np.max(np.abs(a - b))):.3e}"
+
+
+@pytest.mark.gpu
+def test_inner_sweeps_keep_the_fixed_point(oracle_mod):
+    """A lighter FP32 inner schedule changes the work per cycle, not the
+    solution: stopped at 1e-11 it is within 1e-10 of the oracle's fixed point."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    P = problem("o4_binary_merge")
+    orc = oracle_mod.Oracle(P.oracle_dict())
+    orc.fixed_point(tol=1e-14)
+    with og.Elliptic(P) as E:
+        E.set_precision(True)
+        E.set_inner_sweeps(2, 4)
+        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-11)
+        assert rep.final_res <= 1e-11
+        for g, (a, b) in enumerate(zip([E.get_field(g) for g in range(len(E.boxes))], orc.all_u())):
+            box = E.boxes[g]
+            if box.level < E.mgrid_levels:
+                w = box.buf
+                a, b = a[w:-w, w:-w, w:-w], b[w:-w, w:-w, w:-w]
+            assert float(np.max(np.abs(a - b))) <= U_TOL, g
+        with pytest.raises(og.OlgpuError if hasattr(og, "OlgpuError") else Exception):
+            E.set_inner_sweeps(0, 0)
