@@ -457,76 +457,117 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
 
 // Coarsest correction problem in one CTA: repeat { Robin; one red-black SOR
 // sweep } until the sweep norm <= rtol * first, stops changing, or max_it.
-template <int EQ>
+// e lives in shared memory; with SMEM the read-only coefficients (A, 1/(c+u),
+// source, and d, E5 for the scalar field) are staged there too, so an
+// iteration touches no global memory.
+template <int EQ, bool SMEM>
 __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ boxes, int box, DevFields32 G,
                                                    const double *__restrict__ crd, int max_it, float omega, float rtol,
                                                    int *iters_out, int *nan_flag)
 {
-  extern __shared__ float se[];
+  extern __shared__ float4 s_coarse4[];
+  float *se = reinterpret_cast<float *>(s_coarse4);
   __shared__ float red[32];
   __shared__ float s_norm;
   __shared__ int s_nan;
+  __shared__ float s_x[3][64], s_ix[3][64];   // node coordinates and their reciprocals
   const DevBox B = boxes[box];
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
-  const long long np = (long long)n0 * n1 * n2;
+  const int np = n0 * n1 * n2;
   float *ge = G.f[G_E] + B.off;
   const float *gs = G.f[G_S] + B.off, *ga = G.f[G_A] + B.off, *giq = G.f[G_IQ] + B.off;
   const float *gd = EQ ? G.f[G_D] + B.off : nullptr, *ge5 = EQ ? G.f[G_E5] + B.off : nullptr;
-  for (long long p = threadIdx.x; p < np; p += blockDim.x) se[p] = ge[p];
+  float *cs = se + np, *ca = se + 2 * np, *ciq = se + 3 * np, *cd = se + 4 * np, *ce5 = se + 5 * np;
+  for (int p = threadIdx.x; p < np; p += blockDim.x) {
+    se[p] = ge[p];
+    if (SMEM) {
+      cs[p] = gs[p];
+      ca[p] = ga[p];
+      ciq[p] = giq[p];
+      if (EQ) {
+        cd[p] = gd[p];
+        ce5[p] = ge5[p];
+      }
+    }
+  }
+  const float *S_ = SMEM ? cs : gs, *A_ = SMEM ? ca : ga, *IQ_ = SMEM ? ciq : giq;
+  const float *D_ = SMEM ? cd : gd, *E5_ = SMEM ? ce5 : ge5;
+  for (int t = threadIdx.x; t < n0 + n1 + n2; t += blockDim.x) {
+    const int a = t < n0 ? 0 : t < n0 + n1 ? 1 : 2;
+    const int i = t - (a == 0 ? 0 : a == 1 ? n0 : n0 + n1);
+    const float x = (float)crd[B.coord_off + t];
+    s_x[a][i] = x;
+    s_ix[a][i] = x != 0.0f ? rcp_fast(x) : 0.0f;
+  }
   __syncthreads();
   const int m0 = n0 - 2, m1 = n1 - 2, m2 = n2 - 2;
-  const long long sy = n0, sz = (long long)n0 * n1;
+  const int sy = n0, sz = n0 * n1;
   const float dl = (float)B.dulap;
   const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
+  const float idx[3] = {(float)B.idx[0], (float)B.idx[1], (float)B.idx[2]};
+  const int nn[3] = {n0, n1, n2};
+  const int st[3] = {1, sy, sz};
   auto robin = [&](int mask, int i, int j, int k) {
-    const float x = (float)crd[B.coord_off + i], y = (float)crd[B.coord_off + n0 + j];
-    const float z = (float)crd[B.coord_off + n0 + n1 + k];
-    const float r2 = x * x + y * y + z * z;
-    const long long p = pidx(B, i, j, k);
-    const long long st[3] = {1, sy, sz};
     const int ijk[3] = {i, j, k};
-    const float xyz[3] = {x, y, z};
+    const float r2 = s_x[0][i] * s_x[0][i] + s_x[1][j] * s_x[1][j] + s_x[2][k] * s_x[2][k];
+    const int p = (k * n1 + j) * n0 + i;
     float t = 0.0f, dt = 0.0f;
+#pragma unroll
     for (int a = 0; a < 3; a++) {
       if (!(mask & (1 << a))) continue;
       float du;
-      const float dv = derivf<2>(se, p, st[a], ijk[a], B.n[a], (float)B.idx[a], du);
-      t += dv / xyz[a];
-      dt += du / xyz[a];
+      const float dv = derivf<2>(se, p, st[a], ijk[a], nn[a], idx[a], du);
+      t += dv * s_ix[a][ijk[a]];
+      dt += du * s_ix[a][ijk[a]];
     }
-    const float Fv = r2 * t + se[p] - gs[p];
-    se[p] = se[p] - Fv / (r2 * dt + 1.0f);
+    const float Fv = r2 * t + se[p] - S_[p];
+    se[p] = se[p] - Fv * rcp_fast(r2 * dt + 1.0f);
+  };
+  auto nof = [&](int a) { return a == 0 ? n0 : a == 1 ? n1 : n2; };
+  // point with coordinate va on axis a, vb on axis b2, vc on the third
+  auto at = [&](int a, int va, int b2, int vb, int vc, int mask) {
+    const int i = a == 0 ? va : b2 == 0 ? vb : vc;
+    const int j = a == 1 ? va : b2 == 1 ? vb : vc;
+    const int k = a == 2 ? va : b2 == 2 ? vb : vc;
+    robin(mask, i, j, k);
   };
   float norm = 1.0f, prev, first = -1.0f;
   int it = 0;
   do {
     prev = norm;
-    for (int f = 0; f < 6; f++) {
-      const int a = f >> 1, hi = f & 1, a1 = (a + 1) % 3, a2 = (a + 2) % 3;
-      const int c1 = B.n[a1] - 2, c2 = B.n[a2] - 2;
-      for (int t = threadIdx.x; t < c1 * c2; t += blockDim.x) {
-        int ijk[3];
-        ijk[a] = hi ? B.n[a] - 1 : 0;
-        ijk[a1] = 1 + t % c1;
-        ijk[a2] = 1 + t / c1;
-        robin(1 << a, ijk[0], ijk[1], ijk[2]);
+    // faces (2 per axis), then edges, then corners
+    {
+      const int f0 = m1 * m2, f1 = m0 * m2, f2 = m0 * m1;
+      for (int t = threadIdx.x; t < 2 * (f0 + f1 + f2); t += blockDim.x) {
+        int q = t, a;
+        if (q < 2 * f0) a = 0;
+        else if ((q -= 2 * f0) < 2 * f1) a = 1;
+        else {
+          q -= 2 * f1;
+          a = 2;
+        }
+        const int cnt = a == 0 ? f0 : a == 1 ? f1 : f2;
+        const int hi = q >= cnt ? 1 : 0;
+        q -= hi * cnt;
+        const int a1 = a == 2 ? 0 : a + 1;
+        const int c1 = nof(a1) - 2;
+        at(a, hi ? nof(a) - 1 : 0, a1, 1 + q % c1, 1 + q / c1, 1 << a);
       }
     }
     __syncthreads();
-    {
-      const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-      for (int pi = 0; pi < 3; pi++) {
-        const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
-        const int m = B.n[fa] - 2;
-        for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
-          const int e = t / m, q = t % m;
-          int ijk[3];
-          ijk[fa] = 1 + q;
-          ijk[a] = (e >> 1) ? B.n[a] - 1 : 0;
-          ijk[c] = (e & 1) ? B.n[c] - 1 : 0;
-          robin((1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
-        }
+    for (int t = threadIdx.x; t < 4 * (m0 + m1 + m2); t += blockDim.x) {
+      // edges along axis fa (4 each): XY edges (fa = 2), XZ (1), YZ (0)
+      int q = t, fa;
+      if (q < 4 * m2) fa = 2;
+      else if ((q -= 4 * m2) < 4 * m1) fa = 1;
+      else {
+        q -= 4 * m1;
+        fa = 0;
       }
+      const int m = nof(fa) - 2;
+      const int e = q / m, r = q % m;
+      const int a = fa == 0 ? 1 : 0, c = fa == 2 ? 1 : 2;
+      at(a, (e >> 1) ? nof(a) - 1 : 0, c, (e & 1) ? nof(c) - 1 : 0, 1 + r, (1 << a) | (1 << c));
     }
     __syncthreads();
     if (threadIdx.x < 8)
@@ -541,13 +582,13 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
         const int j = 1 + r % m1, k = 1 + r / m1;
         const int i = 1 + ((color + 1 + j + k) & 1) + 2 * ih;
         if (i >= n0 - 1) continue;
-        const long long p = pidx(B, i, j, k);
+        const int p = (k * n1 + j) * n0 + i;
         const float c0 = se[p];
         const float lv = (se[p + 1] - 2.0f * c0 + se[p - 1]) * ix2 + (se[p + sy] - 2.0f * c0 + se[p - sy]) * iy2 +
                          (se[p + sz] - 2.0f * c0 + se[p - sz]) * iz2;
         float op, dop;
-        corr_op<EQ>(lv, dl, c0, ga[p], giq[p], EQ ? gd[p] : 0.0f, EQ ? ge5[p] : 0.0f, op, dop);
-        const float R = op - gs[p];
+        corr_op<EQ>(lv, dl, c0, A_[p], IQ_[p], EQ ? D_[p] : 0.0f, EQ ? E5_[p] : 0.0f, op, dop);
+        const float R = op - S_[p];
         const float en = c0 - omega * (R * rcp_fast(dop));
         se[p] = en;
         rmax = fmaxf(rmax, fabsf(R));
@@ -576,7 +617,7 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
     if (stop_nan) break;
     if (norm <= rtol * first) break;
   } while (norm > 0.0f && prev != norm && it < max_it);
-  for (long long p = threadIdx.x; p < np; p += blockDim.x) ge[p] = se[p];
+  for (int p = threadIdx.x; p < np; p += blockDim.x) ge[p] = se[p];
   if (threadIdx.x == 0) *iters_out = it;
 }
 
@@ -621,25 +662,35 @@ __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__
   const int k = st->k, m = st->m;
   const int nc = k < m ? k : m;
   const int newest = (k + m - 1) % m;   // ring slot of dF_k (k >= 1)
-  double g[kAndMax * (kAndMax + 1) / 2], r[kAndMax];
-  for (int i = 0; i < kAndMax * (kAndMax + 1) / 2; i++) g[i] = 0.0;
-  for (int i = 0; i < kAndMax; i++) r[i] = 0.0;
-  double fm = 0.0;
+  // column i of the fit is dF at ring slot (newest - i) mod m
+  const float *dfc[kAndMax];
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) dfc[i] = DF + (long long)((newest - i + 2 * kAndMax * m) % m) * n;
+  float *dfw = DF + (long long)newest * n;
+  // a thread's products are summed in FP32 (a few dozen points each), the
+  // thread partials in FP64
+  float g[kAndMax * (kAndMax + 1) / 2], r[kAndMax];
+#pragma unroll
+  for (int i = 0; i < kAndMax * (kAndMax + 1) / 2; i++) g[i] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) r[i] = 0.0f;
+  float fm = 0.0f;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
     const float fk = f[p];
-    if (k >= 1) DF[(long long)newest * n + p] = fk - fprev[p];
+    if (k >= 1) dfw[p] = fk - fprev[p];
     fprev[p] = fk;
     if (!pinned[p]) continue;
-    fm = fmax(fm, (double)fabsf(fk));
-    if (nc == 0) continue;
-    double c[kAndMax];
-    for (int i = 0; i < nc; i++) {
-      const int slot = (newest - i + m) % m;
-      c[i] = (double)DF[(long long)slot * n + p];
-      r[i] += c[i] * (double)fk;
+    fm = fmaxf(fm, fabsf(fk));
+    float c[kAndMax];
+#pragma unroll
+    for (int i = 0; i < kAndMax; i++) {
+      c[i] = i < nc ? dfc[i][p] : 0.0f;
+      r[i] += c[i] * fk;
     }
     int q = 0;
-    for (int i = 0; i < nc; i++)
+#pragma unroll
+    for (int i = 0; i < kAndMax; i++)
+#pragma unroll
       for (int j = 0; j <= i; j++) g[q++] += c[i] * c[j];
   }
   __shared__ double red[32];
@@ -655,35 +706,46 @@ __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__
   };
   double *mine = part + (long long)blockIdx.x * kAndPart;
   int q = 0;
-  for (int i = 0; i < nc; i++) {
-    const double s = block_sum(r[i]);
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) {
+    const double s = block_sum((double)r[i]);
     if (threadIdx.x == 0) mine[kAndMax * (kAndMax + 1) / 2 + i] = s;
+#pragma unroll
     for (int j = 0; j <= i; j++) {
-      const double t = block_sum(g[q]);
+      const double t = block_sum((double)g[q]);
       if (threadIdx.x == 0) mine[q] = t;
       q++;
     }
   }
-  block_max_atomic(fm, fmax_slot);
+  block_max_atomic((double)fm, fmax_slot);
 }
 
-// Solves the regularised normal equations for gamma (one thread).
-__global__ void k_and_solve(AndersonState *st, const double *__restrict__ part, int nblocks)
+// Solves the regularised normal equations for gamma.  Launched with
+// kAndPart warps: warp v adds partial v of every block (lane l takes blocks
+// l, l + 32, ...; then a fixed butterfly), so the sums do not depend on
+// scheduling; thread 0 then eliminates.
+__global__ void __launch_bounds__(32 * kAndPart) k_and_solve(AndersonState *st, const double *__restrict__ part,
+                                                             int nblocks)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double tot[kAndPart];
+  const int v = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (v < kAndPart) {
+    double s = 0.0;
+    for (int blk = lane; blk < nblocks; blk += 32) s += part[(long long)blk * kAndPart + v];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[v] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
   const int k = st->k, m = st->m;
   const int nc = k < m ? k : m;
   double A[kAndMax][kAndMax], b[kAndMax];
   double tr = 0.0;
   int q = 0;
   for (int i = 0; i < nc; i++) {
-    double s = 0.0;
-    for (int blk = 0; blk < nblocks; blk++) s += part[(long long)blk * kAndPart + kAndMax * (kAndMax + 1) / 2 + i];
-    b[i] = s;
+    b[i] = tot[kAndMax * (kAndMax + 1) / 2 + i];
     for (int j = 0; j <= i; j++) {
-      double t = 0.0;
-      for (int blk = 0; blk < nblocks; blk++) t += part[(long long)blk * kAndPart + q];
-      A[i][j] = A[j][i] = t;
+      A[i][j] = A[j][i] = tot[q];
       q++;
     }
     tr += A[i][i];
@@ -725,17 +787,24 @@ __global__ void __launch_bounds__(256) k_and_update(long long n, double *u, cons
   const int k = st->k_used, m = st->m;
   const int nc = k < m ? k : m;
   const int newest = (k + m - 1) % m;
-  const int out = k % m;                  // ring slot of dU_{k+1}
-  double gam[kAndMax];
-  for (int i = 0; i < kAndMax; i++) gam[i] = st->gamma[i];
+  float *du_out = DU + (long long)(k % m) * n;   // ring slot of dU_{k+1}
+  const float *duc[kAndMax], *dfc[kAndMax];
+  float gam[kAndMax];
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) {
+    const long long slot = (newest - i + 2 * kAndMax * m) % m;
+    duc[i] = DU + slot * n;
+    dfc[i] = DF + slot * n;
+    gam[i] = i < nc ? (float)st->gamma[i] : 0.0f;
+  }
+  // the step is a correction: FP32 is enough for it; u accumulates in FP64
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
-    double step = (double)f[p];
-    for (int i = 0; i < nc; i++) {
-      const int slot = (newest - i + m) % m;
-      step -= gam[i] * ((double)DU[(long long)slot * n + p] + (double)DF[(long long)slot * n + p]);
-    }
-    u[p] = u[p] + step;
-    DU[(long long)out * n + p] = (float)step;
+    float step = f[p];
+#pragma unroll
+    for (int i = 0; i < kAndMax; i++)
+      if (i < nc) step -= gam[i] * (duc[i][p] + dfc[i][p]);
+    u[p] = u[p] + (double)step;
+    du_out[p] = step;
   }
 }
 

@@ -46,6 +46,7 @@ olgpu_status fail(olgpu_status s, const std::string &msg)
   } while (0)
 
 constexpr int kThreads = 256;
+constexpr size_t kCoarseSmemMax = 200 * 1024;   // dynamic shared memory of the coarse solves
 
 // Host copy of one transfer: its jobs, their block prefix and the device copy.
 struct Transfer {
@@ -793,10 +794,16 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   launch_ew32(h, k - 1, EW32_WW_EQ_E);
   if (k == 1) {
     const DevBox &B = h->hboxes[h->G.first_box[0]];
-    const size_t smem = sizeof(float) * (size_t)B.n[0] * B.n[1] * B.n[2];
-    k_coarse32<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F32, h->d_coords,
-                                                 h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
-                                                 &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+    const size_t np = (size_t)B.n[0] * B.n[1] * B.n[2];
+    const size_t staged = sizeof(float) * np * (EQ ? 6 : 4);
+    if (staged <= kCoarseSmemMax)
+      k_coarse32<EQ, true><<<1, 1024, staged, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F32, h->d_coords,
+                                                            h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+                                                            &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+    else
+      k_coarse32<EQ, false><<<1, 1024, sizeof(float) * np, h->stream>>>(
+          h->d_boxes, h->G.first_box[0], h->F32, h->d_coords, h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+          &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
     h->launches_mixed++;
   } else {
     emit_fasn32<EQ>(h, k - 1);
@@ -845,7 +852,7 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     const int nblk = 152 * 4;
     k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E], fprev, DF, h->d_pinned, h->d_and_state,
                                                     h->d_and_part, &h->d_stats->slots[126]);
-    k_and_solve<<<1, 32, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
+    k_and_solve<<<1, 32 * kAndPart, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
     k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U], h->F32.f[G_E], DU, DF, h->d_and_state);
     h->launches_mixed += 3;
   } else {
@@ -938,6 +945,9 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
     olgpu_status st = reset_anderson(h);
     if (st != OLGPU_OK) return st;
   }
+  for (const void *kern : {(const void *)k_coarse32<0, true>, (const void *)k_coarse32<1, true>,
+                           (const void *)k_coarse32<0, false>, (const void *)k_coarse32<1, false>})
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoarseSmemMax));
   choose_smooth_clusters(h);
   return capture_mixed(h);
 }
@@ -1205,9 +1215,13 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   {
     const DevBox &B0 = h->hboxes[h->G.first_box[0]];
     const size_t smem = sizeof(double) * (size_t)B0.n[0] * B0.n[1] * B0.n[2];
-    if (smem > 200 * 1024) return cleanup(fail(OLGPU_ERR_INVALID_ARG, "coarsest grid too large"));
-    cudaError_t e1 = cudaFuncSetAttribute(k_coarse_solve<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaError_t e2 = cudaFuncSetAttribute(k_coarse_solve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > kCoarseSmemMax || B0.n[0] > 64 || B0.n[1] > 64 || B0.n[2] > 64)
+      return cleanup(fail(OLGPU_ERR_INVALID_ARG, "coarsest grid too large"));
+    // the limit is per kernel and process-wide: always the same maximum, so
+    // hierarchies with different coarse grids never lower it for each other
+    const int lim = (int)kCoarseSmemMax;
+    cudaError_t e1 = cudaFuncSetAttribute(k_coarse_solve<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaError_t e2 = cudaFuncSetAttribute(k_coarse_solve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     if (e1 != cudaSuccess || e2 != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, "shared memory opt-in failed"));
   }
   if (!std::getenv("OLGPU_COARSE_ONE_BLOCK")) choose_coarse_cluster(h);
