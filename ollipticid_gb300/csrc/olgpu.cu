@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <thread>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -1497,25 +1499,34 @@ olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule
     if (st != OLGPU_OK) return st;
   }
   olgpu_status worst = OLGPU_OK;
-  for (;;) {
-    int active = 0;
-    for (int i = 0; i < n; i++)   // enqueue every unfinished solve: their streams overlap on the GPU
-      if (!T[i].done) {
-        olgpu_status st = olgpu_cycle_launch(hs[i]);
-        if (st != OLGPU_OK) return st;
-        active++;
+  // Every solve has its own stream; a solve's next cycle is enqueued as soon
+  // as its last one has finished (no lockstep rounds), so the GPU always has
+  // the other solves' work queued while the host reads one cycle's norms.
+  int active = 0;
+  for (int i = 0; i < n; i++) {
+    olgpu_status st = olgpu_cycle_launch(hs[i]);
+    if (st != OLGPU_OK) return st;
+    active++;
+  }
+  while (active > 0) {
+    bool progressed = false;
+    for (int i = 0; i < n; i++) {
+      if (T[i].done) continue;
+      int done = 0;
+      double r = 0;
+      olgpu_status s = olgpu_cycle_poll(hs[i], 0, &done, &r);
+      if (!done && s == OLGPU_OK) continue;
+      progressed = true;
+      if (T[i].step(s, r)) {
+        T[i].done = true;
+        active--;
+        if (s != OLGPU_OK) worst = s;
+        continue;
       }
-    if (!active) break;
-    for (int i = 0; i < n; i++)
-      if (!T[i].done) {
-        int done = 0;
-        double r = 0;
-        olgpu_status s = olgpu_cycle_poll(hs[i], 1, &done, &r);
-        if (T[i].step(s, r)) {
-          T[i].done = true;
-          if (s != OLGPU_OK) worst = s;
-        }
-      }
+      olgpu_status st = olgpu_cycle_launch(hs[i]);
+      if (st != OLGPU_OK) return st;
+    }
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
   for (int i = 0; i < n; i++) close_track(hs[i], T[i], reports ? &reports[i] : nullptr);
   return worst;
