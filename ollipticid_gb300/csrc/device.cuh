@@ -65,6 +65,9 @@ struct XferJob {
   int r0[3], r1[3];     // visited target index box [r0, r1)
   int tab[3];           // AxisEntry offset of target index 0 on each axis
   long long blk0;       // first block of this job in the launch
+  int row_axis;         // row kernel: rows run along x (0) or y (1)
+  int pad_;
+  long long rblk0;      // row kernel: first block of this job
 };
 
 struct PunctureParams {

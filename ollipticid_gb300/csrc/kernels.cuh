@@ -541,6 +541,143 @@ __global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, 
   else dst[tp] = tensor_sum_any<V>(base, sy, sz, ax, ay, az);
 }
 
+// ----------------------------------------------------------------------------
+// Separable form of the tensor Lagrange transfer, one warp per target row.
+// Along a row in x (fixed j, k) every target shares ay and az, so the inner
+// sums of the tensor sum, uy(I') = sum_J wy_J sum_K wz_K src(I', J, K), are
+// the same for every target that reaches source column I'; the warp forms
+// them once per column in shared memory and each target then adds its x
+// terms, fx = sum_I wx_I uy(start_x + I).  Along a row in y (the two-wide
+// x-slabs of a ghost shell) the targets share ax and az: the warp forms
+// uz(I, J') = sum_K wz_K src(start_x + I, J', K) and each target adds
+// sum_I wx_I sum_J wy_J uz(I, start_y + J).  The terms, their order and
+// their rounding are those of tensor_sum, so the result is the same bit for
+// bit, with about P/2 instead of P^3 multiply-adds per target.
+// ----------------------------------------------------------------------------
+constexpr int kRowWarps = 4;     // rows in flight per block
+constexpr int kRowBuf = 1024;    // shared partial sums per row
+
+template <class V, class Fields, int P>
+__global__ void __launch_bounds__(32 * kRowWarps) k_xfer_rows(const XferJob *__restrict__ jobs, int njobs,
+                                                              const DevBox *__restrict__ boxes, Fields F,
+                                                              const AxisEntry *__restrict__ tab)
+{
+  __shared__ V sbuf[kRowWarps][kRowBuf];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int lo = 0, hi = njobs - 1;   // last job with rblk0 <= blockIdx.x
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].rblk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1];
+  const int ra = J.row_axis;
+  const long long row = ((long long)blockIdx.x - J.rblk0) * kRowWarps + warp;
+  const int across = ra == 0 ? e1 : e0;   // rows per plane
+  if (row >= (long long)across * (J.r1[2] - J.r0[2])) return;   // the whole warp leaves together
+  const int k = J.r0[2] + (int)(row / across);
+  const int fixed = (ra == 0 ? J.r0[1] : J.r0[0]) + (int)(row % across);
+  const int len = ra == 0 ? e0 : e1, first = ra == 0 ? J.r0[0] : J.r0[1];
+  const DevBox T = boxes[J.tbox], S = boxes[J.sbox];
+  V *dst = F.f[J.tfield] + T.off;
+  const V *src = F.f[J.sfield] + S.off;
+  const long long sy = S.n[0], sz = (long long)S.n[0] * S.n[1];
+  const AxisEntry &az = tab[J.tab[2] + k];
+  const AxisEntry &af = tab[J.tab[ra == 0 ? 1 : 0] + fixed];   // the row's fixed x or y entry
+  V *buf = sbuf[warp];
+
+  // pass 0: copies, zeros and the source span of the targets that need a sum
+  int smin = 1 << 30, smax = -1;
+  for (int t = lane; t < len; t += 32) {
+    const int i = ra == 0 ? first + t : fixed, j = ra == 0 ? fixed : first + t;
+    if (J.iter != IT_ALL) {
+      const int b = T.buf;
+      const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+      if ((J.iter == IT_INSIDE) != inside) continue;
+    }
+    const AxisEntry &ax = tab[J.tab[0] + i];
+    const AxisEntry &ay = tab[J.tab[1] + j];
+    const long long tp = pidx(T, i, j, k);
+    if (!(ax.sel && ay.sel && az.sel)) {
+      if (J.to_zero) dst[tp] = V(0);
+      continue;
+    }
+    if (J.method == XM_COPY || (ax.exact && ay.exact && az.exact)) {
+      dst[tp] = src[pidx(S, ax.node, ay.node, az.node)];
+      continue;
+    }
+    const AxisEntry &ar = ra == 0 ? ax : ay;
+    smin = min(smin, ar.start + ar.lo);
+    smax = max(smax, ar.start + ar.hi);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    smin = min(smin, __shfl_xor_sync(0xffffffffu, smin, o));
+    smax = max(smax, __shfl_xor_sync(0xffffffffu, smax, o));
+  }
+  if (smax < smin) return;
+  const int span = smax - smin + 1;
+  const int nI = ra == 0 ? 1 : af.hi - af.lo + 1;
+  const bool shared = span * nI <= kRowBuf;
+
+  // pass 1: the shared partial sums
+  if (shared) {
+    if (ra == 0) {
+      for (int c = lane; c < span; c += 32) {
+        const V *col0 = src + (long long)(smin + c) + (long long)af.start * sy + (long long)az.start * sz;
+        V uy = V(0);
+        for (int Jj = af.lo; Jj <= af.hi; Jj++) {
+          const V *col = col0 + Jj * sy;
+          V uz = V(0);
+          for (int K = az.lo; K <= az.hi; K++) uz += col[K * sz] * (V)az.w[K];
+          uy += uz * (V)af.w[Jj];
+        }
+        buf[c] = uy;
+      }
+    } else {
+      for (int q = lane; q < span * nI; q += 32) {
+        const int I = af.lo + q / span, c = q % span;
+        const V *col = src + (long long)(af.start + I) + (long long)(smin + c) * sy + (long long)az.start * sz;
+        V uz = V(0);
+        for (int K = az.lo; K <= az.hi; K++) uz += col[K * sz] * (V)az.w[K];
+        buf[q] = uz;
+      }
+    }
+  }
+  __syncwarp();
+
+  // pass 2: every target's own terms
+  for (int t = lane; t < len; t += 32) {
+    const int i = ra == 0 ? first + t : fixed, j = ra == 0 ? fixed : first + t;
+    if (J.iter != IT_ALL) {
+      const int b = T.buf;
+      const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+      if ((J.iter == IT_INSIDE) != inside) continue;
+    }
+    const AxisEntry &ax = tab[J.tab[0] + i];
+    const AxisEntry &ay = tab[J.tab[1] + j];
+    if (!(ax.sel && ay.sel && az.sel) || J.method == XM_COPY || (ax.exact && ay.exact && az.exact)) continue;
+    const long long tp = pidx(T, i, j, k);
+    if (!shared) {
+      dst[tp] = tensor_sum_any<V>(src + pidx(S, ax.start, ay.start, az.start), sy, sz, ax, ay, az);
+      continue;
+    }
+    V fx = V(0);
+    if (ra == 0) {
+      for (int I = ax.lo; I <= ax.hi; I++) fx += buf[ax.start + I - smin] * (V)ax.w[I];
+    } else {
+      for (int I = ax.lo; I <= ax.hi; I++) {
+        const V *uzI = buf + (I - ax.lo) * span - smin;
+        V uy = V(0);
+        for (int Jj = ay.lo; Jj <= ay.hi; Jj++) uy += uzI[ay.start + Jj] * (V)ay.w[Jj];
+        fx += uy * (V)ax.w[I];
+      }
+    }
+    dst[tp] = fx;
+  }
+}
+
 // Window width P of a plan's kernel: 0 without Lagrange jobs, the Lagrange
 // order + 1 when it has an instantiation, else -1.
 inline int xfer_width(const XferJob *jobs, size_t n)
@@ -554,6 +691,16 @@ inline int xfer_width(const XferJob *jobs, size_t n)
     else if (w != pw) w = -1;
   }
   return w;
+}
+
+// Whether a plan runs on the row kernel: Lagrange jobs only, with a window of
+// at least 4 points (the order 3 restriction and the order+1 ghost fills).
+inline bool xfer_rows(const XferJob *jobs, size_t n, int width)
+{
+  if (width < 4) return false;
+  for (size_t q = 0; q < n; q++)
+    if (jobs[q].method != XM_LAGRANGE) return false;
+  return true;
 }
 
 // ----------------------------------------------------------------------------

@@ -54,7 +54,9 @@ constexpr size_t kCoarseSmemMax = 200 * 1024;   // dynamic shared memory of the 
 struct Transfer {
   std::vector<XferJob> jobs;
   long long blocks = 0;
+  long long row_blocks = 0;         // blocks of the row kernel (k_xfer_rows)
   int width = 0;                    // kernel variant (xfer_width of the jobs)
+  bool rows = false;                // run on k_xfer_rows
   XferJob *d_jobs = nullptr;
 };
 
@@ -255,9 +257,13 @@ void add_region_jobs(Transfer &X, XferJob base, const domain &T, const int sel_l
       if (J.r1[a] <= J.r0[a]) empty = true;
     }
     if (empty) continue;
-    const long long vol = (long long)(J.r1[0] - J.r0[0]) * (J.r1[1] - J.r0[1]) * (J.r1[2] - J.r0[2]);
+    const long long e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
     J.blk0 = X.blocks;
-    X.blocks += cdiv(vol, kThreads);
+    X.blocks += cdiv(e0 * e1 * e2, kThreads);
+    // rows for the row kernel: along the longer of x and y
+    J.row_axis = e0 >= e1 ? 0 : 1;
+    J.rblk0 = X.row_blocks;
+    X.row_blocks += cdiv((J.row_axis == 0 ? e1 : e0) * e2, kRowWarps);
     X.jobs.push_back(J);
   }
 }
@@ -296,6 +302,7 @@ Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfi
       add_region_jobs(X, J, T, lo, hi);
     }
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
+  X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
   return X;
 }
 
@@ -331,6 +338,7 @@ Transfer make_set_in(olgpu_hierarchy *h, int k)
     }
   }
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
+  X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
   return X;
 }
 
@@ -375,8 +383,19 @@ template <class V, class Fields>
 void launch_xfer(olgpu_hierarchy *h, const Transfer &X, const Fields &F)
 {
   if (X.jobs.empty()) return;
-  const unsigned nb = (unsigned)X.blocks;
   const int nj = (int)X.jobs.size();
+  if (X.rows) {
+    const unsigned nr = (unsigned)X.row_blocks;
+    const int th = 32 * kRowWarps;
+    switch (X.width) {
+    case 4: k_xfer_rows<V, Fields, 4><<<nr, th, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+    case 6: k_xfer_rows<V, Fields, 6><<<nr, th, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+    case 8: k_xfer_rows<V, Fields, 8><<<nr, th, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+    default: k_xfer_rows<V, Fields, 10><<<nr, th, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
+    }
+    return;
+  }
+  const unsigned nb = (unsigned)X.blocks;
   switch (X.width) {
   case 0: k_xfer<V, Fields, 0><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
   case 3: k_xfer<V, Fields, 3><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, F, h->d_tab); break;
@@ -878,6 +897,8 @@ Transfer remap(const Transfer &X, int sfield, int tfield)
   Y.jobs = X.jobs;
   Y.blocks = X.blocks;
   Y.width = X.width;
+  Y.rows = X.rows;
+  Y.row_blocks = X.row_blocks;
   for (auto &J : Y.jobs) {
     J.sfield = sfield;
     J.tfield = tfield;

@@ -73,3 +73,24 @@ def test_coefficients_match_oracle(oracle_mod):
                 a, b = E.get_field(g, name), orc.field(g, name)
                 scale = max(1.0, float(np.max(np.abs(b))))
                 assert float(np.max(np.abs(a - b))) <= 1e-13 * scale, (g, name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["o4_binary_merge", "o8_offset", "sf_binary"])
+@pytest.mark.parametrize("mixed", [False, True])
+def test_row_transfers_equal_point_transfers(case, mixed, monkeypatch):
+    """The separable row kernel (shared inner sums per target row) gives the
+    per-point tensor sum's ghost fills and restrictions bit for bit."""
+    import ollipticid_gb300 as og
+    P = problem(case)
+    out = []
+    for points in (False, True):
+        if points:
+            monkeypatch.setenv("OLGPU_XFER_POINTS", "1")
+        with og.Elliptic(P) as E:
+            E.set_precision(mixed)
+            for _ in range(3):
+                E.FASN()
+            out.append([E.get_field(g) for g in range(len(E.boxes))])
+    for g, (a, b) in enumerate(zip(*out)):
+        assert np.array_equal(a, b), f"box {g}: max diff {float(np.max(np.abs(a - b))):.3e}"
