@@ -80,15 +80,44 @@ __device__ __forceinline__ double lap(const double *__restrict__ u, long long p,
   }
 }
 
+// NaN test on the bits (integer pipe).
+__device__ __forceinline__ bool is_nan_bits(double x)
+{
+  return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+
+// Hardware approximate FP32 reciprocal (PTX rcp.approx.ftz.f32, error within
+// about one ulp).
+__device__ __forceinline__ float rcp_fast(float x)
+{
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// 1/q in FP64 for 1e-37 < |q| < 1e37: the FP32 reciprocal as a seed (relative
+// error below 2e-7) refined by two Newton steps r <- r + r (1 - q r), which
+// square the error each (below 1e-13, then at the FP64 rounding level).  Four
+// FP64 multiply-adds instead of a correctly rounded reciprocal; the result is
+// within about an ulp of it.
+__device__ __forceinline__ double rcp_newton(double q)
+{
+  double r = (double)rcp_fast((float)q);
+  double e = fma(-q, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-q, r, 1.0);
+  return fma(r, e, r);
+}
+
 // Pointwise operator value and its derivative in u (puncture, optionally with
 // the scalar-field terms d (c+u) + e (c+u)^5).  Integer powers by products of
-// one correctly rounded reciprocal.
+// one reciprocal (rcp_newton).
 template <int EQ>
 __device__ __forceinline__ void point_op(double lapv, double dl, double uu, double bb, double cc,
                                          double dd, double ee, double &op, double &dop)
 {
   const double q = cc + uu;
-  const double iq = __drcp_rn(q);
+  const double iq = rcp_newton(q);
   const double iq2 = iq * iq;
   const double iq4 = iq2 * iq2;
   const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
@@ -187,22 +216,34 @@ __device__ __forceinline__ void robin_point(const DevBox &B, const DevFields &F,
 // ----------------------------------------------------------------------------
 // reductions
 // ----------------------------------------------------------------------------
+// v >= 0: a non-negative double orders like its bit pattern read as an
+// unsigned integer, so the block maximum is taken on the bits with integer
+// instructions and the FP64 pipe (the smoothers' bottleneck on GB300) stays
+// free.  A NaN compares above every finite value and reaches the slot.
 __device__ __forceinline__ void block_max_atomic(double v, unsigned long long *slot)
 {
-  __shared__ double red[32];
+  __shared__ unsigned long long red[32];
+  unsigned long long m = (unsigned long long)__double_as_longlong(v);
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = x > m ? x : m;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) red[warp] = v;
+  if (lane == 0) red[warp] = m;
   __syncthreads();
   if (warp == 0) {
     const int nw = (blockDim.x + 31) >> 5;
-    v = lane < nw ? red[lane] : 0.0;
+    m = lane < nw ? red[lane] : 0ull;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0 && v > 0.0) atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+      m = x > m ? x : m;
+    }
+    if (lane == 0 && m > 0ull) atomicMax(slot, m);
   }
 }
+
 
 // Inverse of the Newton diagonal dOP/du for the smoother's step.  The step
 // u -= R / dOP only needs the diagonal approximately: a relative error of
@@ -256,7 +297,7 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
       const double un = u[p] - R * step_inverse(dop);
       u[p] = un;
       rabs = fabs(R);
-      if (!(un == un)) atomicOr(nan_flag, 1);
+      if (is_nan_bits(un)) atomicOr(nan_flag, 1);
     }
   }
   block_max_atomic(rabs, norm_slot);

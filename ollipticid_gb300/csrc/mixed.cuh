@@ -64,15 +64,6 @@ __device__ __forceinline__ float lapf(const float *__restrict__ u, long long p, 
                        (float)B.idx2[2]);
 }
 
-// Hardware approximate reciprocal (PTX rcp.approx.ftz.f32, error within
-// about one ulp).  The FP32 correction cycle only has to converge: the FP64
-// defect that drives it fixes the solution.
-__device__ __forceinline__ float rcp_fast(float x)
-{
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  return r;
-}
 
 // Correction operator N(u+e) - N(u) at one point and its derivative in e.
 template <int EQ>
@@ -106,7 +97,7 @@ __global__ void __launch_bounds__(256) k_mx_coeffs(BoxList L, const DevBox *__re
   if (t >= n) return;
   const long long p = B.off + t;
   const double q = F.f[F_C][p] + F.f[F_U][p];
-  const double iq = __drcp_rn(q);
+  const double iq = rcp_newton(q);
   const double iq2 = iq * iq, iq4 = iq2 * iq2;
   G.f[G_A][p] = (float)(F.f[F_B][p] * (iq4 * iq2 * iq));
   G.f[G_IQ][p] = (float)iq;
