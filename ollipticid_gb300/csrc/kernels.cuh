@@ -95,14 +95,22 @@ __device__ __forceinline__ float rcp_fast(float x)
   return r;
 }
 
-// 1/q in FP64 for 1e-37 < |q| < 1e37: the FP32 reciprocal as a seed (relative
-// error below 2e-7) refined by two Newton steps r <- r + r (1 - q r), which
-// square the error each (below 1e-13, then at the FP64 rounding level).  Four
-// FP64 multiply-adds instead of a correctly rounded reciprocal; the result is
-// within about an ulp of it.
+// Approximate FP64 reciprocal (PTX rcp.approx.ftz.f64: about 20 correct
+// bits, one special-function instruction, no FP32 round trip).
+__device__ __forceinline__ double rcp_approx64(double x)
+{
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  return r;
+}
+
+// 1/q in FP64: the approximate reciprocal refined by two Newton steps
+// r <- r + r (1 - q r), each of which squares the relative error (about 1e-6,
+// 1e-12, then the FP64 rounding level).  Four FP64 multiply-adds instead of a
+// correctly rounded reciprocal; the result is within about an ulp of it.
 __device__ __forceinline__ double rcp_newton(double q)
 {
-  double r = (double)rcp_fast((float)q);
+  double r = rcp_approx64(q);
   double e = fma(-q, r, 1.0);
   r = fma(r, e, r);
   e = fma(-q, r, 1.0);
@@ -247,12 +255,12 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long *s
 
 // Inverse of the Newton diagonal dOP/du for the smoother's step.  The step
 // u -= R / dOP only needs the diagonal approximately: a relative error of
-// 2^-23 in it scales the step by 1 +- 1e-7 and leaves the fixed point (R = 0)
-// where it is, so the FP32 reciprocal replaces an FP64 division (the FP64
-// pipe is the bottleneck of this kernel on GB300).
+// about 1e-6 in it scales the step by 1 +- 1e-6 and leaves the fixed point
+// (R = 0) where it is, so one approximate reciprocal replaces an FP64
+// division (the FP64 pipe is the bottleneck of this kernel on GB300).
 __device__ __forceinline__ double step_inverse(double dop)
 {
-  return (double)__frcp_rn((float)dop);
+  return rcp_approx64(dop);
 }
 
 // ----------------------------------------------------------------------------
