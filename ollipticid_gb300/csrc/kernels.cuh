@@ -364,21 +364,20 @@ __global__ void __launch_bounds__(256) k_robin_faces(BoxList L, const DevBox *__
   }
 }
 
-// Edges then corners of one box per block.
+// Robin points on the ghost edges (part 0) or corners (part 1; launched
+// after the edges, whose values the corners read).
 template <int ORD>
-__global__ void __launch_bounds__(256) k_robin_edges_corners(BoxList L, const DevBox *__restrict__ boxes,
-                                                             DevFields F, const double *__restrict__ crd,
-                                                             int mode)
+__global__ void __launch_bounds__(64) k_robin_edges_corners(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                            const double *__restrict__ crd, int mode, int part)
 {
-  const DevBox B = boxes[L.first + blockIdx.x];
-  const int b = B.buf;
-  const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-  for (int pi = 0; pi < 3; pi++) {
-    const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
-    const int m = B.n[fa] - 2 * b;
-    for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
-      const int e = t / m, q = t % m;
-      const int ha = e >> 1, hc = e & 1;
+  if (part == 0) {
+    // one block per (box, edge): 12 edges a box, (a, c) the edge's ghost axes
+    const DevBox B = boxes[L.first + blockIdx.x / 12];
+    const int e12 = blockIdx.x % 12, pi = e12 >> 2, e = e12 & 3;
+    const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
+    const int b = B.buf, m = B.n[fa] - 2 * b;
+    const int ha = e >> 1, hc = e & 1;
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
       int ijk[3];
       ijk[fa] = b + q;
       for (int ta = 0; ta < b; ta++)
@@ -388,8 +387,11 @@ __global__ void __launch_bounds__(256) k_robin_edges_corners(BoxList L, const De
           robin_point<ORD>(B, F, crd, mode, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
         }
     }
+    return;
   }
-  __syncthreads();
+  // corners, after every edge (a launch of their own), one block per box
+  const DevBox B = boxes[L.first + blockIdx.x];
+  const int b = B.buf;
   if (threadIdx.x < 8) {
     const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
     for (int tk = 0; tk < b; tk++)

@@ -356,30 +356,31 @@ __global__ void __launch_bounds__(256) k_robin32_faces(BoxList L, const DevBox *
 }
 
 template <int ORD>
-__global__ void __launch_bounds__(256) k_robin32_edges_corners(BoxList L, const DevBox *__restrict__ boxes,
-                                                               DevFields32 G, const double *__restrict__ crd,
-                                                               int mode)
+__global__ void __launch_bounds__(64) k_robin32_edges_corners(BoxList L, const DevBox *__restrict__ boxes, DevFields32 F,
+                                            const double *__restrict__ crd, int mode, int part)
 {
-  const DevBox B = boxes[L.first + blockIdx.x];
-  const int b = B.buf;
-  const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-  for (int pi = 0; pi < 3; pi++) {
-    const int a = pairs[pi][0], c = pairs[pi][1], fa = 3 - a - c;
-    const int m = B.n[fa] - 2 * b;
-    for (int t = threadIdx.x; t < 4 * m; t += blockDim.x) {
-      const int e = t / m, q = t % m;
-      const int ha = e >> 1, hc = e & 1;
+  if (part == 0) {
+    // one block per (box, edge): 12 edges a box, (a, c) the edge's ghost axes
+    const DevBox B = boxes[L.first + blockIdx.x / 12];
+    const int e12 = blockIdx.x % 12, pi = e12 >> 2, e = e12 & 3;
+    const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
+    const int b = B.buf, m = B.n[fa] - 2 * b;
+    const int ha = e >> 1, hc = e & 1;
+    for (int q = threadIdx.x; q < m; q += blockDim.x) {
       int ijk[3];
       ijk[fa] = b + q;
       for (int ta = 0; ta < b; ta++)
         for (int tc = 0; tc < b; tc++) {
           ijk[a] = ha ? B.n[a] - b + ta : b - 1 - ta;
           ijk[c] = hc ? B.n[c] - b + tc : b - 1 - tc;
-          robin32_point<ORD>(B, G, crd, mode, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+          robin32_point<ORD>(B, F, crd, mode, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
         }
     }
+    return;
   }
-  __syncthreads();
+  // corners, after every edge (a launch of their own), one block per box
+  const DevBox B = boxes[L.first + blockIdx.x];
+  const int b = B.buf;
   if (threadIdx.x < 8) {
     const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
     for (int tk = 0; tk < b; tk++)
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(256) k_robin32_edges_corners(BoxList L, const 
           const int i = hx ? B.n[0] - b + ti : b - 1 - ti;
           const int j = hy ? B.n[1] - b + tj : b - 1 - tj;
           const int k = hz ? B.n[2] - b + tk : b - 1 - tk;
-          robin32_point<ORD>(B, G, crd, mode, 7, i, j, k);
+          robin32_point<ORD>(B, F, crd, mode, 7, i, j, k);
         }
   }
 }

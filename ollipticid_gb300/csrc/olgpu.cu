@@ -367,8 +367,9 @@ void launch_robin(olgpu_hierarchy *h, int level, int mode)
 {
   const BoxList L = level_list(h, level, blocks_faces);
   k_robin_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
-  k_robin_edges_corners<ORD><<<L.count, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
-  h->launches += 2;
+  k_robin_edges_corners<ORD><<<12 * L.count, 64, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode, 0);
+  k_robin_edges_corners<ORD><<<L.count, 32, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode, 1);
+  h->launches += 3;
 }
 
 void launch_ew(olgpu_hierarchy *h, int level, int op)
@@ -778,8 +779,9 @@ void launch_robin32(olgpu_hierarchy *h, int level, int mode)
 {
   const BoxList L = level_list(h, level, blocks_faces);
   k_robin32_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);
-  k_robin32_edges_corners<ORD><<<L.count, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);
-  h->launches_mixed += 2;
+  k_robin32_edges_corners<ORD><<<12 * L.count, 64, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode, 0);
+  k_robin32_edges_corners<ORD><<<L.count, 32, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode, 1);
+  h->launches_mixed += 3;
 }
 
 void dispatch_robin32(olgpu_hierarchy *h, int level, int mode)
