@@ -605,8 +605,10 @@ __global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, 
 // their rounding are those of tensor_sum, so the result is the same bit for
 // bit, with about P/2 instead of P^3 multiply-adds per target.
 // ----------------------------------------------------------------------------
-constexpr int kRowWarps = 4;     // rows in flight per block
-constexpr int kRowBuf = 1024;    // shared partial sums per row
+// 16 rows per block: the kernel is latency-bound with few rows, so packing
+// them onto fewer SMs costs little time and leaves the other SMs to other work
+constexpr int kRowWarps = 16;    // rows in flight per block
+constexpr int kRowBuf = 320;     // shared partial sums per row (else direct sums)
 
 template <class V, class Fields, int P>
 __global__ void __launch_bounds__(32 * kRowWarps) k_xfer_rows(const XferJob *__restrict__ jobs, int njobs,

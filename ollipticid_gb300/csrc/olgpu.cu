@@ -853,8 +853,12 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   // FP64: coefficients of the correction operator and the defect source
   for (int l = 0; l < L; l++) {
     const BoxList BL = level_list(h, l, blocks_all);
-    k_mx_coeffs<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, EQ);
-    dispatch_mx_defect<EQ>(h, l, nullptr);
+    switch (level_order(h, l)) {
+    case 2: k_mx_prep<2, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
+    case 4: k_mx_prep<4, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
+    case 6: k_mx_prep<6, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
+    default: k_mx_prep<8, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
+    }
     if (l <= mg) {
       if (level_order(h, l) == 2)
         k_mx_robin_defect<2><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, h->d_coords);
