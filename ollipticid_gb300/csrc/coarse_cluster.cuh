@@ -7,9 +7,19 @@
 // the box's z-planes are split between the NCTA blocks of one cluster, each
 // holding its slab of u in shared memory.  Stencil reads of neighbouring
 // planes go to the owning block's shared memory through distributed shared
-// memory; every write is to the writer's own slab.  Phases are separated by
-// cluster barriers.  On GB300 one SM issues only a few FP64 FMAs per clock, so
-// a 17^3 FP64 sweep in one block is ~60 us; sixteen blocks divide that.
+// memory; every write is to the writer's own slab.  On GB300 one SM issues
+// only a few FP64 FMAs per clock, so the sweeps are spread over the cluster.
+//
+// Ownership keeps the Robin update local: block 0 owns the low ghost plane
+// and the two interior planes above it, the last block the mirror image, and
+// the others share the planes in between.  A face point reads interior points
+// of its own plane (or, on a z face, the two planes next to it); an edge
+// point reads face points, a corner edge points, all in planes its block
+// owns.  So faces -> edges -> corners need only block barriers, and since
+// the Robin update writes no interior point, colour 0 may follow at once.
+// Two cluster barriers per iteration remain: after colour 0 (colour 1 reads
+// its z neighbours) and after colour 1 (the norm, and the next iteration's
+// colour 0).  The updates are the same as with one barrier per phase.
 #pragma once
 
 #include "kernels.cuh"
@@ -17,6 +27,19 @@
 #include <cooperative_groups.h>
 
 namespace olgpu {
+
+// First plane of block r: block 0 holds [0, 3), block ncta-1 holds
+// [n2-3, n2), blocks 1..ncta-2 share [3, n2-3) evenly.  Needs n2 >= 6, a
+// ghost band of one plane and ncta >= 3.
+__host__ __device__ inline int cslab_begin(int r, int n2, int ncta)
+{
+  if (r <= 0) return 0;
+  if (r >= ncta) return n2;
+  if (r == ncta - 1) return n2 - 3;
+  const int m = n2 - 6, k = ncta - 2, rr = r - 1;
+  const int base = m / k, rem = m % k;
+  return 3 + rr * base + (rr < rem ? rr : rem);
+}
 
 template <int EQ, int NCTA>
 __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict__ boxes, int box, DevFields F,
@@ -28,42 +51,35 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
   cg::cluster_group cl = cg::this_cluster();
   const int rank = (int)cl.block_rank();
   extern __shared__ double su[];
-  __shared__ double *slab[NCTA];
-  __shared__ int z0s[NCTA + 1];
-  __shared__ unsigned char owner[64];
-  __shared__ double red[8], red_nan[8];   // one slot per warp (256 threads)
-  __shared__ double s_part[2];   // [0] this block's max |R|, [1] NaN seen (0/1)
-  __shared__ double s_norm;
-  __shared__ int s_stop;
+  __shared__ double *plane[64];
+  __shared__ double red[8];                // one slot per warp (256 threads)
+  __shared__ int red_nan[8];
+  __shared__ double s_part[2][2];          // per iteration parity: [0] max |R| of this block, [1] NaN seen
+  __shared__ double s_x[3][64], s_ix[3][64];   // node coordinates and their reciprocals
 
   const DevBox B = boxes[box];
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
   const int n01 = n0 * n1;
-  if (threadIdx.x == 0) {
-    const int base = n2 / NCTA, rem = n2 % NCTA;
-    int z = 0;
-    for (int r = 0; r < NCTA; r++) {
-      z0s[r] = z;
-      const int cnt = base + (r < rem ? 1 : 0);
-      for (int k = z; k < z + cnt; k++) owner[k] = (unsigned char)r;
-      z += cnt;
-    }
-    z0s[NCTA] = z;
+  const int kz0 = cslab_begin(rank, n2, NCTA), kz1 = cslab_begin(rank + 1, n2, NCTA);
+  for (int k = threadIdx.x; k < n2; k += blockDim.x) {
+    int r = 0;
+    while (cslab_begin(r + 1, n2, NCTA) <= k) r++;
+    plane[k] = cl.map_shared_rank(su, r) + (k - cslab_begin(r, n2, NCTA)) * n01;
   }
-  if (threadIdx.x < NCTA) slab[threadIdx.x] = cl.map_shared_rank(su, (int)threadIdx.x);
-  __syncthreads();
-  const int kz0 = z0s[rank], kz1 = z0s[rank + 1];
   double *gu = F.f[F_U] + B.off;
   const double *gb = F.f[F_B] + B.off, *gc = F.f[F_C] + B.off, *gs = F.f[F_RHO] + B.off;
   const double *gd = EQ ? F.f[F_D] + B.off : nullptr, *ge = EQ ? F.f[F_E] + B.off : nullptr;
   for (int p = threadIdx.x; p < (kz1 - kz0) * n01; p += blockDim.x) su[p] = gu[(long long)kz0 * n01 + p];
+  for (int t = threadIdx.x; t < n0 + n1 + n2; t += blockDim.x) {
+    const int a = t < n0 ? 0 : t < n0 + n1 ? 1 : 2;
+    const int i = t - (a == 0 ? 0 : a == 1 ? n0 : n0 + n1);
+    const double x = crd[B.coord_off + t];
+    s_x[a][i] = x;
+    s_ix[a][i] = 1.0 / x;   // ghost nodes lie on the outer faces, never at 0
+  }
   cl.sync();
 
-  auto U = [&](int i, int j, int k) -> double & {
-    const int r = owner[k];
-    return slab[r][(k - z0s[r]) * n01 + j * n0 + i];
-  };
-  const double *cx = crd + B.coord_off, *cy = cx + n0, *cz = cy + n1;
+  auto U = [&](int i, int j, int k) -> double & { return plane[k][j * n0 + i]; };
   // one-sided order-2 derivative along axis a at a ghost position
   auto d1 = [&](int a, int i, int j, int k, double &du) -> double {
     const int idx[3] = {i, j, k};
@@ -80,32 +96,38 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
     du = 3.0 * 0.5 * id;
     return (3.0 * u0 - 4.0 * u1 + u2) * 0.5 * id;
   };
-  // Newton update of one Robin point (Boundary_Face/Edge/Corner grouping)
+  // Newton update of one Robin point (Boundary_Face/Edge/Corner grouping).
+  // The divisions by the coordinate are products with its reciprocal (within
+  // an ulp); the Newton step divides by an approximate reciprocal of the
+  // derivative, which only sizes the step (F = 0 stays the solution).
   auto robin = [&](int mask, int i, int j, int k) {
-    const double x = cx[i], y = cy[j], z = cz[k];
-    const double r2 = x * x + y * y + z * z;
-    const double xyz[3] = {x, y, z};
-    double t = 0.0, dt = 0.0, tF = 0.0, dF = 0.0;
+    const double r2 = s_x[0][i] * s_x[0][i] + s_x[1][j] * s_x[1][j] + s_x[2][k] * s_x[2][k];
+    const int ijk[3] = {i, j, k};
+    double tF = 0.0, dF = 1.0, t = 0.0, dt = 0.0;
     int na = 0;
+    const bool face = mask == 1 || mask == 2 || mask == 4;
+#pragma unroll
     for (int a = 0; a < 3; a++) {
       if (!(mask & (1 << a))) continue;
       double du;
       const double dv = d1(a, i, j, k, du);
-      if (mask == (1 << a)) {
-        tF = r2 * dv / xyz[a];
-        dF = r2 * du / xyz[a] + 1.0;
+      const double ia = s_ix[a][ijk[a]];
+      if (face) {
+        tF = r2 * dv * ia;
+        dF = r2 * du * ia + 1.0;
+      } else {
+        t = na == 0 ? dv * ia : t + dv * ia;
+        dt = na == 0 ? du * ia : dt + du * ia;
+        na++;
       }
-      t = na == 0 ? dv / xyz[a] : t + dv / xyz[a];
-      dt = na == 0 ? du / xyz[a] : dt + du / xyz[a];
-      na++;
     }
-    if (na > 1) {
+    if (!face) {
       tF = r2 * t;
       dF = r2 * dt + 1.0;
     }
     double &uu = U(i, j, k);
     const double Fv = tF + uu - gs[((long long)k * n1 + j) * n0 + i];
-    uu = uu - Fv / dF;
+    uu = uu - Fv * rcp_approx64(dF);
   };
 
   double norm = 1.0, prev, first = -1.0;
@@ -113,7 +135,7 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
   const int mi0 = n0 - 2, mi1 = n1 - 2;
   do {
     prev = norm;
-    // faces
+    // Robin update of this block's planes: faces, edges, corners
     for (int k = kz0; k < kz1; k++) {
       if (k == 0 || k == n2 - 1) {
         for (int t = threadIdx.x; t < mi0 * mi1; t += blockDim.x) robin(4, 1 + t % mi0, 1 + t / mi0, k);
@@ -127,8 +149,7 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         }
       }
     }
-    cl.sync();
-    // edges
+    __syncthreads();
     for (int k = kz0; k < kz1; k++) {
       if (k == 0 || k == n2 - 1) {
         for (int t = threadIdx.x; t < 2 * mi1 + 2 * mi0; t += blockDim.x) {
@@ -142,14 +163,14 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         robin(3, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);   // XY edges
       }
     }
-    cl.sync();
-    // corners
+    __syncthreads();
     for (int k = kz0; k < kz1; k++)
       if ((k == 0 || k == n2 - 1) && threadIdx.x < 4)
         robin(7, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);
-    cl.sync();
+    __syncthreads();
     // one red-black SOR sweep over the interior points of this block's planes
-    double rmax = 0.0, nan_seen = 0.0;
+    double rmax = 0.0;
+    int nan_seen = 0;
     const int ka = kz0 > 1 ? kz0 : 1, kb = kz1 < n2 - 1 ? kz1 : n2 - 1;
     const int H = (mi0 + 1) / 2;
     for (int color = 0; color < 2; color++) {
@@ -169,48 +190,48 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         const double un = c0 - omega * (R * step_inverse(dop));
         U(i, j, k) = un;
         rmax = fmax(rmax, fabs(R));
-        if (!(un == un)) nan_seen = 1.0;
+        if (is_nan_bits(un)) nan_seen = 1;
       }
-      cl.sync();
+      if (color == 0) cl.sync();   // colour 1 reads colour 0 of the neighbouring blocks
     }
-    // cluster-wide max of the sweep norm and of the NaN flag
+    // this block's partial norm into the slot of this iteration's parity
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-      nan_seen = fmax(nan_seen, __shfl_xor_sync(0xffffffffu, nan_seen, o));
+      nan_seen |= __shfl_xor_sync(0xffffffffu, nan_seen, o);
     }
     if ((threadIdx.x & 31) == 0) {
       red[threadIdx.x >> 5] = rmax;
       red_nan[threadIdx.x >> 5] = nan_seen;
     }
     __syncthreads();
+    const int par = it & 1;
     if (threadIdx.x == 0) {
-      double m = 0.0, nn = 0.0;
+      double m = 0.0;
+      int nn = 0;
       for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
         m = fmax(m, red[w]);
-        nn = fmax(nn, red_nan[w]);
+        nn |= red_nan[w];
       }
-      s_part[0] = m;
-      s_part[1] = nn;
+      s_part[par][0] = m;
+      s_part[par][1] = nn ? 1.0 : 0.0;
     }
-    cl.sync();
-    if (threadIdx.x == 0) {
-      double m = 0.0, nn = 0.0;
-      for (int r = 0; r < NCTA; r++) {
-        const double *pr = cl.map_shared_rank(s_part, r);
-        m = fmax(m, pr[0]);
-        nn = fmax(nn, pr[1]);
-      }
-      s_norm = m;
-      s_stop = nn > 0.0;
-      if (nn > 0.0 && rank == 0) atomicOr(nan_flag, 1);
+    cl.sync();   // every block's colour 1 and partial norm are done
+    // Every block reads all partials of this parity in the same order, so all
+    // take the same decision.  The slot is written again two iterations later,
+    // after two more cluster barriers this block must reach first.
+    double m = 0.0, nn = 0.0;
+#pragma unroll
+    for (int r = 0; r < NCTA; r++) {
+      const double *pr = cl.map_shared_rank(&s_part[par][0], r);
+      m = fmax(m, pr[0]);
+      nn = fmax(nn, pr[1]);
     }
-    __syncthreads();
-    norm = s_norm;
-    const int stop_nan = s_stop;
+    norm = m;
+    if (nn > 0.0 && rank == 0 && threadIdx.x == 0) atomicOr(nan_flag, 1);
     it++;
     if (first < 0.0) first = norm;
-    if (stop_nan) break;                           // the same decision in every block
+    if (nn > 0.0) break;                           // the same decision in every block
     if (rtol > 0.0 && norm <= rtol * first) break;
   } while (norm > eps && prev != norm && it < max_it);
   cl.sync();   // every block is done reading its neighbours' shared memory

@@ -509,9 +509,23 @@ bool cluster_fits(olgpu_hierarchy *h, size_t smem)
 void choose_coarse_cluster(olgpu_hierarchy *h)
 {
   const DevBox &B = h->hboxes[h->G.first_box[0]];
-  if (B.n[2] > 64 || B.buf != 1) return;
-  for (int ncta : {16, 8}) {
-    const int planes = (B.n[2] + ncta - 1) / ncta;
+  if (B.n[2] > 64 || B.n[2] < 6 || B.buf != 1) return;
+  // the critical path between two barriers is the largest number of interior
+  // planes a block sweeps; of equal ones the smaller cluster is taken
+  auto crit = [&](int ncta) {
+    int m = 0;
+    for (int r = 0; r < ncta; r++) {
+      const int a = std::max(cslab_begin(r, B.n[2], ncta), 1), b = std::min(cslab_begin(r + 1, B.n[2], ncta), B.n[2] - 1);
+      m = std::max(m, b - a);
+    }
+    return m;
+  };
+  const int c8 = crit(8), c16 = crit(16);
+  const int order[2] = {c16 < c8 ? 16 : 8, c16 < c8 ? 8 : 16};
+  for (int ncta : order) {
+    int planes = 0;
+    for (int r = 0; r < ncta; r++)
+      planes = std::max(planes, cslab_begin(r + 1, B.n[2], ncta) - cslab_begin(r, B.n[2], ncta));
     const size_t smem = sizeof(double) * (size_t)planes * B.n[0] * B.n[1];
     const bool ok = ncta == 16 ? (cluster_fits<0, 16>(h, smem) && cluster_fits<1, 16>(h, smem))
                                : (cluster_fits<0, 8>(h, smem) && cluster_fits<1, 8>(h, smem));
