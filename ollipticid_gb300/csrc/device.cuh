@@ -24,7 +24,7 @@ struct DevBox {
   int level;
   long long off;        // element offset inside each field arena
   int coord_off;        // offset of this box's x, y, z tables in coords[]
-  int pad;
+  int iso;              // the same spacing on every axis (1/dx^2 equal)
   double idx[3];        // 1/dx
   double idx2[3];       // 1/dx^2
   double dulap;         // diagonal of the Laplacian stencil

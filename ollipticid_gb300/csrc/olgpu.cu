@@ -48,6 +48,9 @@ olgpu_status fail(olgpu_status s, const std::string &msg)
   } while (0)
 
 constexpr int kThreads = 256;
+// blocks of the per-colour smoothers: one colour of a level is about one
+// wave of 256-thread blocks, so smaller blocks spread it more evenly
+constexpr int kSmoothThreads = 128;
 constexpr size_t kCoarseSmemMax = 200 * 1024;   // dynamic shared memory of the coarse solves
 
 // Host copy of one transfer: its jobs, their block prefix and the device copy.
@@ -157,7 +160,7 @@ long long blocks_color(const DevBox &B)
   const int b = B.buf;
   const int nc = b + 1;   // colours: order/2 + 1 (2 for the order-2 boxes)
   const long long H = (B.n[0] - 2 * b + nc - 1) / nc;
-  return cdiv(H * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kThreads);
+  return cdiv(H * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kSmoothThreads);
 }
 
 long long blocks_faces(const DevBox &B)
@@ -349,7 +352,7 @@ void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
   const int nb = L.blk[L.count];
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++)
-      k_smooth_color<ORD, EQ><<<nb, kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, color,
+      k_smooth_color<ORD, EQ><<<nb, kSmoothThreads, 0, h->stream>>>(L, h->d_boxes, h->F, color,
                                                               &h->d_stats->slots[slot], &h->d_stats->nan_flag),
           h->launches++;
 }
@@ -631,7 +634,7 @@ void launch_smooth32(olgpu_hierarchy *h, int level, int nu)
   const BoxList L = level_list(h, level, blocks_color);
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
-      k_smooth32<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, color,
+      k_smooth32<ORD, EQ><<<L.blk[L.count], kSmoothThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, color,
                                                                        &h->d_stats->nan_flag);
       h->launches_mixed++;
     }
@@ -1169,6 +1172,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     B.level = D.level;
     B.off = off;
     B.coord_off = coff;
+    B.iso = B.idx2[0] == B.idx2[1] && B.idx2[1] == B.idx2[2];
     const double s = B.idx2[0] + B.idx2[1] + B.idx2[2];
     switch (D.order) {   // duLapc2/4/6/8
     case 2: B.dulap = -2.0 * s; break;
@@ -1730,7 +1734,7 @@ void noalloc_sweeps(const BoxList &L, const DevBox *box, const DevFields &F, int
 {
   for (int s = 0; s < sweeps; s++)
     for (int color = 0; color < num_colors<ORD>(); color++)
-      k_smooth_color<ORD, EQ><<<L.blk[L.count], kThreads, 0, st>>>(L, box, F, color, scr + kNoAllocNormOff + s,
+      k_smooth_color<ORD, EQ><<<L.blk[L.count], kSmoothThreads, 0, st>>>(L, box, F, color, scr + kNoAllocNormOff + s,
                                                                    reinterpret_cast<int *>(scr + kNoAllocNanOff));
 }
 
@@ -1779,6 +1783,7 @@ extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int 
     B.idx[a] = 1.0 / d[a];
     B.idx2[a] = B.idx[a] * B.idx[a];
   }
+  B.iso = B.idx2[0] == B.idx2[1] && B.idx2[1] == B.idx2[2];
   const double sum = B.idx2[0] + B.idx2[1] + B.idx2[2];
   switch (f->order) {
   case 2: B.dulap = -2.0 * sum; break;
