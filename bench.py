@@ -239,7 +239,7 @@ def run_concurrent(E_ref, P, u_fix, adm_fix, plain_value, n: int = 16):
     try:
         for E in sol:
             E.set_precision(True)
-            E.set_inner_sweeps(choice.nu1, choice.nu2)
+            choice.apply(E)
         for E in sol:
             E.reset()
         og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200)           # warm-up
@@ -256,7 +256,8 @@ def run_concurrent(E_ref, P, u_fix, adm_fix, plain_value, n: int = 16):
         value = n / best
         return {"workload": f"{n} copies of {WORKLOAD_NAME} at once (solve_many), mixed precision",
                 "concurrent_solves": n, "value": value, "unit": UNIT,
-                "inner_sweeps": [choice.nu1, choice.nu2], "autotune_table": choice.table,
+                "inner_sweeps": [choice.nu1, choice.nu2], "smoother_blocks": choice.blocks,
+                "autotune_table": choice.table,
                 "cycles_per_solve": reps[0].cycles, "final_fp64_defect": max(r.final_res for r in reps),
                 "max_abs_u_minus_fp64_fixed_point": worst_err,
                 "adm_minus_fp64_fixed_point": [a - b for a, b in zip(reps[0].adm[:2], adm_fix)],
@@ -399,7 +400,7 @@ def run_gpu(args, rank: int, world: int, local: int):
     if rank == 0 and world == 1 and not args.no_extra:
         concurrent = run_concurrent(E, P, u_fix, adm_fix, value / world)
         batched = run_batched(args)
-        served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))
+        served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]) + (concurrent["smoother_blocks"],))
 
     # ---- roofline of the dominant kernel (multicolour smoother), all levels
     peak, peak_kind = _peaks()

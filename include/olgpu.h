@@ -169,6 +169,13 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth);
  * acceleration history; call between solves.  0 <= nu1 <= 64, 1 <= nu2 <= 64. */
 olgpu_status olgpu_set_inner_sweeps(olgpu_hierarchy *h, int nu1, int nu2);
 
+/* Largest thread-block cluster (8..16 blocks) that keeps a box's FP32
+ * correction resident through all sweeps of the mixed cycle's smoother, or 0
+ * for one launch per colour and sweep (default 16).  No reference
+ * counterpart.  Smaller clusters leave more of the GPU to other solves; the
+ * result is the same bit for bit.  Re-captures the mixed cycle if built. */
+olgpu_status olgpu_set_smoother_blocks(olgpu_hierarchy *h, int max_blocks);
+
 /* Reset u to the initial guess (0) and the work fields, keeping the geometry
  * and coefficients, so that one hierarchy can serve repeated solves. */
 olgpu_status olgpu_reset(olgpu_hierarchy *h);

@@ -213,6 +213,10 @@ class Elliptic:
         """Pre-/post-smoothing sweeps of the FP32 correction cycle (mixed precision)."""
         check(self.lib.olgpu_set_inner_sweeps(self._h, int(nu1), int(nu2)))
 
+    def set_smoother_blocks(self, max_blocks: int):
+        """Largest cluster (8..16 blocks, or 0: per-colour launches) of the FP32 smoother."""
+        check(self.lib.olgpu_set_smoother_blocks(self._h, int(max_blocks)))
+
     def set_acceleration(self, depth: int):
         """Anderson history depth of the mixed outer iteration (0 = off, 1..4)."""
         check(self.lib.olgpu_set_acceleration(self._h, int(depth)))

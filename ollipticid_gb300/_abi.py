@@ -83,6 +83,7 @@ SIGNATURES = {
     "olgpu_last_device_ms": (C.c_double, [C.c_void_p]),
     "olgpu_last_coarse_iters": (C.c_int, [C.c_void_p]),
     "olgpu_set_inner_sweeps": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "olgpu_set_smoother_blocks": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_kernels_per_cycle": (C.c_int, [C.c_void_p]),
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),
     "olgpu_time_smoother": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),

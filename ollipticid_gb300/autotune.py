@@ -1,4 +1,4 @@
-"""Sweep-schedule autotuner for the mixed-precision solve.
+"""Sweep-schedule and smoother-layout autotuner for the mixed-precision solve.
 
 The FP32 correction cycle of a mixed-precision solve may use any number of
 pre- and post-smoothing sweeps: the FP64 defect that drives it fixes the
@@ -8,7 +8,11 @@ depends on the problem's shape and on how many solves share the GPU (with
 many concurrent solves the GPU is full and fewer sweeps per cycle win; a
 solve alone is bound by launch latency).  `tune` measures a small set of
 candidates on the problem itself, `concurrency` copies at a time through
-`solve_many`, each to the same stop rule, and returns the fastest.  Results
+`solve_many`, each to the same stop rule, and returns the fastest.  The
+candidates also choose the FP32 smoother's layout (`olgpu_set_smoother_blocks`):
+a thread-block cluster per box keeping the correction in shared memory for
+every sweep (blocks = 16), or one launch per colour and sweep (blocks = 0),
+which wins for a solve alone.  Results
 are cached per problem shape (equation, order, N, levels, punctures) and
 concurrency, in memory and optionally in a JSON file.
 """
@@ -23,8 +27,10 @@ from typing import Dict, List, Optional, Sequence, Tuple
 
 from . import Elliptic, Problem, _abi, solve_many
 
-# (nu1, nu2) candidates: the reference's own (3, 20) and lighter schedules
-CANDIDATES: Tuple[Tuple[int, int], ...] = ((3, 20), (3, 12), (3, 8), (2, 6), (2, 4))
+# (nu1, nu2, smoother cluster blocks) candidates: the reference's own (3, 20)
+# and lighter schedules, cluster-resident or per-colour smoothing
+CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((3, 20, 16), (3, 12, 16), (3, 8, 16), (2, 4, 16), (3, 8, 0),
+                                                (2, 4, 0))
 
 _lock = threading.Lock()
 _memo: Dict[str, "Choice"] = {}
@@ -34,13 +40,23 @@ _memo: Dict[str, "Choice"] = {}
 class Choice:
     nu1: int
     nu2: int
+    blocks: int
     solves_per_s: float
     cycles: int
     table: List[dict] = field(default_factory=list)   # every candidate's measurement
 
     def to_dict(self) -> dict:
-        return {"nu1": self.nu1, "nu2": self.nu2, "solves_per_s": self.solves_per_s, "cycles": self.cycles,
-                "table": self.table}
+        return {"nu1": self.nu1, "nu2": self.nu2, "blocks": self.blocks, "solves_per_s": self.solves_per_s,
+                "cycles": self.cycles, "table": self.table}
+
+    @staticmethod
+    def from_dict(d: dict) -> "Choice":
+        return Choice(d["nu1"], d["nu2"], d.get("blocks", 16), d["solves_per_s"], d["cycles"], d.get("table", []))
+
+    def apply(self, E: Elliptic) -> None:
+        """Sets this choice on a mixed-precision solver."""
+        E.set_smoother_blocks(self.blocks)
+        E.set_inner_sweeps(self.nu1, self.nu2)
 
 
 def shape_key(p: Problem, concurrency: int) -> str:
@@ -55,7 +71,7 @@ def _load(path: Optional[str]) -> dict:
     return {}
 
 
-def tune(p: Problem, concurrency: int = 8, candidates: Sequence[Tuple[int, int]] = CANDIDATES,
+def tune(p: Problem, concurrency: int = 8, candidates: Sequence[Tuple[int, int, int]] = CANDIDATES,
          tol: Optional[float] = None, max_cycles: int = 200, cache_path: Optional[str] = None,
          device: int = 0, repeats: int = 1) -> Choice:
     """Fastest inner schedule for `concurrency` concurrent mixed solves of p."""
@@ -65,8 +81,7 @@ def tune(p: Problem, concurrency: int = 8, candidates: Sequence[Tuple[int, int]]
             return _memo[key]
         disk = _load(cache_path)
         if key in disk:
-            d = disk[key]
-            _memo[key] = Choice(d["nu1"], d["nu2"], d["solves_per_s"], d["cycles"], d.get("table", []))
+            _memo[key] = Choice.from_dict(disk[key])
             return _memo[key]
     tol = p.tol if tol is None else tol
     sol = [Elliptic(p, device=device) for _ in range(concurrency)]
@@ -74,8 +89,9 @@ def tune(p: Problem, concurrency: int = 8, candidates: Sequence[Tuple[int, int]]
     try:
         for E in sol:
             E.set_precision(True)
-        for nu1, nu2 in candidates:
+        for nu1, nu2, blocks in candidates:
             for E in sol:
+                E.set_smoother_blocks(blocks)
                 E.set_inner_sweeps(nu1, nu2)
             for E in sol:                      # warm-up (first launches of the new graph)
                 E.reset()
@@ -90,13 +106,13 @@ def tune(p: Problem, concurrency: int = 8, candidates: Sequence[Tuple[int, int]]
                 ok = all(r.final_res <= tol for r in reps)
                 rate = concurrency / dt if ok else 0.0
                 best = rate if best is None else max(best, rate)
-            table.append({"nu1": nu1, "nu2": nu2, "solves_per_s": best, "cycles": int(reps[0].cycles),
+            table.append({"nu1": nu1, "nu2": nu2, "blocks": blocks, "solves_per_s": best, "cycles": int(reps[0].cycles),
                           "reached_tol": ok})
     finally:
         for E in sol:
             E.close()
     top = max(table, key=lambda r: r["solves_per_s"])
-    choice = Choice(top["nu1"], top["nu2"], top["solves_per_s"], top["cycles"], table)
+    choice = Choice(top["nu1"], top["nu2"], top["blocks"], top["solves_per_s"], top["cycles"], table)
     with _lock:
         _memo[key] = choice
         if cache_path:
@@ -116,4 +132,4 @@ def cached(p: Problem, concurrency: int = 8, cache_path: Optional[str] = None) -
         if key in _memo:
             return _memo[key]
     d = _load(cache_path).get(key)
-    return Choice(d["nu1"], d["nu2"], d["solves_per_s"], d["cycles"], d.get("table", [])) if d else None
+    return Choice.from_dict(d) if d else None

@@ -127,6 +127,7 @@ struct olgpu_hierarchy {
   std::vector<size_t> sc_smem;
   // pre-/post-smoothing sweeps of the FP32 correction cycle (-1: nu1/nu2)
   int inner_nu1 = -1, inner_nu2 = -1;
+  int sc_max = 16;   // largest cluster for the FP32 smoother (0: per-colour launches)
 };
 
 namespace {
@@ -728,13 +729,13 @@ void choose_smooth_clusters(olgpu_hierarchy *h)
   const int L = h->G.levels;
   h->sc_ncta.assign(L, 0);
   h->sc_smem.assign(L, 0);
-  if (std::getenv("OLGPU_SMOOTH32_LAUNCHES")) return;
+  if (std::getenv("OLGPU_SMOOTH32_LAUNCHES") || h->sc_max < 8) return;
   for (int l = 0; l < L; l++) {
     const int ord = level_order(h, l);
     const void *kern = smooth32_cluster_kernel(ord, h->equation);
     int best = 0, best_share = 1 << 30;
     size_t best_smem = 0;
-    for (int ncta = 16; ncta >= 8; ncta--) {
+    for (int ncta = std::min(h->sc_max, 16); ncta >= 8; ncta--) {
       size_t smem = 0;
       int share = 0;
       bool ok = true;
@@ -1644,6 +1645,18 @@ olgpu_status olgpu_set_inner_sweeps(olgpu_hierarchy *h, int nu1, int nu2)
   olgpu_status st = capture_mixed(h);
   if (st != OLGPU_OK) return st;
   return reset_anderson(h);
+}
+
+olgpu_status olgpu_set_smoother_blocks(olgpu_hierarchy *h, int max_blocks)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (max_blocks != 0 && (max_blocks < 8 || max_blocks > 16))
+    return fail(OLGPU_ERR_INVALID_ARG, "smoother blocks must be 0 or 8..16");
+  CUDA_TRY(cudaSetDevice(h->device));
+  h->sc_max = max_blocks;
+  if (!h->graph_mixed) return OLGPU_OK;   // used when the mixed cycle is built
+  choose_smooth_clusters(h);
+  return capture_mixed(h);
 }
 
 int olgpu_last_coarse_iters(const olgpu_hierarchy *h) { return h && h->h_stats ? h->h_stats->coarse_iters : 0; }

@@ -80,9 +80,10 @@ class _Track:
 class Server:
     def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
                  tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
-                 inner_sweeps: Optional[Tuple[int, int]] = None):
-        """inner_sweeps: (nu1, nu2) of every mixed solve's FP32 cycle (for
-        example an autotune choice); None keeps each problem's own nu1/nu2."""
+                 inner_sweeps: Optional[Tuple[int, ...]] = None):
+        """inner_sweeps: (nu1, nu2[, smoother cluster blocks]) of every mixed
+        solve's FP32 cycle (for example an autotune choice); None keeps each
+        problem's own nu1/nu2 and the default smoother layout."""
         self.device, self.mem_budget, self.max_active = device, mem_budget, max_active
         self.mixed, self.tol, self.max_cycles, self.keep_u = mixed, tol, max_cycles, keep_u
         self.inner_sweeps = inner_sweeps
@@ -92,7 +93,9 @@ class Server:
         E = Elliptic(problem, device=self.device)
         E.set_precision(self.mixed)
         if self.mixed and self.inner_sweeps:
-            E.set_inner_sweeps(*self.inner_sweeps)
+            if len(self.inner_sweeps) > 2:
+                E.set_smoother_blocks(self.inner_sweeps[2])
+            E.set_inner_sweeps(*self.inner_sweeps[:2])
         return E
 
     def run(self, stream: Sequence[Tuple[float, Problem]]) -> dict:

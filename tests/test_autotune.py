@@ -18,7 +18,7 @@ def test_shape_key_and_cache(tmp_path):
     assert autotune.cached(P, 8, str(path)) is None
     path.write_text(json.dumps({k: {"nu1": 2, "nu2": 6, "solves_per_s": 1.0, "cycles": 9, "table": []}}))
     c = autotune.cached(P, 8, str(path))
-    assert (c.nu1, c.nu2, c.cycles) == (2, 6, 9)
+    assert (c.nu1, c.nu2, c.blocks, c.cycles) == (2, 6, 16, 9)
 
 
 @pytest.mark.gpu
@@ -27,15 +27,15 @@ def test_tuned_schedule_solves_to_tolerance(tmp_path, oracle_mod):
     from ollipticid_gb300 import _abi, autotune
     P = problem("o4_binary_merge")
     path = str(tmp_path / "tuned.json")
-    choice = autotune.tune(P, concurrency=2, candidates=((3, 20), (2, 4)), tol=1e-11, cache_path=path)
-    assert (choice.nu1, choice.nu2) in ((3, 20), (2, 4))
+    choice = autotune.tune(P, concurrency=2, candidates=((3, 20, 16), (2, 4, 0)), tol=1e-11, cache_path=path)
+    assert (choice.nu1, choice.nu2, choice.blocks) in ((3, 20, 16), (2, 4, 0))
     assert len(choice.table) == 2 and all(r["reached_tol"] for r in choice.table)
     assert autotune.cached(P, 2, path).nu2 == choice.nu2
     orc = oracle_mod.Oracle(P.oracle_dict())
     orc.fixed_point(tol=1e-14)
     with og.Elliptic(P) as E:
         E.set_precision(True)
-        E.set_inner_sweeps(choice.nu1, choice.nu2)
+        choice.apply(E)
         rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-11)
         assert rep.final_res <= 1e-11
         for g, (a, b) in enumerate(zip([E.get_field(g) for g in range(len(E.boxes))], orc.all_u())):
