@@ -89,6 +89,7 @@ struct olgpu_hierarchy {
   AxisEntry *d_tab = nullptr;
   // per level k >= 1
   std::vector<Transfer> restrict_u, xfer_w, set_in, prolong_v, ghost_u;
+  std::vector<Transfer> ghost_lo;   // cubic ghost fills (the FP32 cycle's correction may use them)
   std::vector<AdmJob> hadm;
   AdmJob *d_adm = nullptr;
   Stats *d_stats = nullptr;
@@ -961,7 +962,8 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
     h->xfer_w32[k] = remap(h->xfer_w[k], G_T, G_W);
     h->set_in32[k] = remap(h->set_in[k], G_W, G_S);
     h->prolong_v32[k] = remap(h->prolong_v[k], G_V, G_V);
-    h->ghost_e[k] = remap(h->ghost_u[k], G_E, G_E);
+    // the correction's ghosts: cubic Lagrange (the FP64 ghosts of u keep order+1)
+    h->ghost_e[k] = remap(h->ghost_lo[k], G_E, G_E);
   }
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) {
@@ -1195,6 +1197,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   h->set_in.resize(L);
   h->prolong_v.resize(L);
   h->ghost_u.resize(L);
+  h->ghost_lo.resize(L);
   for (int k = 1; k < L; k++) {
     h->restrict_u[k] = make_transfer(h, k, F_U, k - 1, F_U, IT_INSIDE, XM_LAGRANGE, 3, false, false);
     h->xfer_w[k] = make_transfer(h, k, F_T, k - 1, F_W, IT_ALL, XM_LAGRANGE, 2, k - 1 <= mg, false);
@@ -1204,6 +1207,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     else
       h->prolong_v[k] = make_transfer(h, k - 1, F_V, k, F_V, IT_INSIDE, XM_LINEAR, 1, true, false);
     if (k > mg) h->ghost_u[k] = make_transfer(h, k - 1, F_U, k, F_U, IT_BOUNDARY, XM_LAGRANGE, order + 1, true, false);
+    if (k > mg) h->ghost_lo[k] = make_transfer(h, k - 1, F_U, k, F_U, IT_BOUNDARY, XM_LAGRANGE, 3, true, false);
   }
   // ADM: 4th-order Lagrange at each puncture on finest box i (box 0 if absent)
   {
@@ -1253,7 +1257,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
             up((void **)&h->d_coords, h->hcoords.data(), sizeof(double) * h->hcoords.size()) &&
             up((void **)&h->d_tab, h->htab.data(), sizeof(AxisEntry) * h->htab.size()) &&
             up((void **)&h->d_adm, h->hadm.data(), sizeof(AdmJob) * h->hadm.size());
-  for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
+  for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
     for (auto &X : *vec)
       ok = ok && up((void **)&X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size());
   ok = ok && cudaMalloc(&h->d_stats, sizeof(Stats)) == cudaSuccess &&
@@ -1324,7 +1328,7 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   cudaFree(h->d_pinned);
   cudaFree(h->d_and_state);
   cudaFree(h->d_and_part);
-  for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u})
+  for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   cudaFree(h->d_arena);
   cudaFree(h->d_boxes);
