@@ -54,7 +54,10 @@ struct AxisEntry {
   double w[kMaxInterpPoints];
 };
 
-enum XferMethod { XM_LINEAR = 0, XM_LAGRANGE = 1, XM_COPY = 2 };
+// XM_STRIDED: a job whose every target coincides with a source node that
+// moves by a fixed step per target index (restriction and tau transfer at
+// coinciding points, Set_In): a strided copy, found when the plan is built.
+enum XferMethod { XM_LINEAR = 0, XM_LAGRANGE = 1, XM_COPY = 2, XM_STRIDED = 3 };
 enum IterKind { IT_ALL = 0, IT_INSIDE = 1, IT_BOUNDARY = 2 };
 
 // One (target box, source box, target sub-region) piece of a transfer.
@@ -68,6 +71,7 @@ struct XferJob {
   int row_axis;         // row kernel: rows run along x (0) or y (1)
   int pad_;
   long long rblk0;      // row kernel: first block of this job
+  int sstart[3], sstep[3];   // XM_STRIDED: source node of target r0 and its step
 };
 
 struct PunctureParams {

@@ -570,6 +570,13 @@ __global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, 
   }
   V *dst = F.f[J.tfield] + T.off;
   const long long tp = pidx(T, i, j, k);
+  if (J.method == XM_STRIDED) {   // every target coincides with a node: no table lookups
+    const DevBox &S = boxes[J.sbox];
+    dst[tp] = F.f[J.sfield][S.off + pidx(S, J.sstart[0] + J.sstep[0] * (i - J.r0[0]),
+                                          J.sstart[1] + J.sstep[1] * (j - J.r0[1]),
+                                          J.sstart[2] + J.sstep[2] * (k - J.r0[2]))];
+    return;
+  }
   const AxisEntry &ax = tab[J.tab[0] + i];
   const AxisEntry &ay = tab[J.tab[1] + j];
   const AxisEntry &az = tab[J.tab[2] + k];

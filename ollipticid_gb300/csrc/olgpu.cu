@@ -273,6 +273,27 @@ void add_region_jobs(Transfer &X, XferJob base, const domain &T, const int sel_l
   }
 }
 
+// Marks the jobs of X whose every target is selected and coincides with a
+// source node that moves by a constant step along each axis (the exact-copy
+// branch of the transfer for all of them) as strided copies.
+void stride_jobs(const olgpu_hierarchy *h, Transfer &X)
+{
+  for (XferJob &J : X.jobs) {
+    if (J.method != XM_LAGRANGE && J.method != XM_COPY) continue;
+    bool ok = true;
+    for (int a = 0; a < 3 && ok; a++) {
+      const AxisEntry *e = h->htab.data() + J.tab[a];
+      const int r0 = J.r0[a], r1 = J.r1[a];
+      const int step = r1 - r0 > 1 ? e[r0 + 1].node - e[r0].node : 1;
+      for (int t = r0; t < r1 && ok; t++)
+        ok = e[t].sel && (J.method == XM_COPY || e[t].exact) && e[t].node == e[r0].node + step * (t - r0);
+      J.sstart[a] = e[r0].node;
+      J.sstep[a] = step;
+    }
+    if (ok) J.method = XM_STRIDED;
+  }
+}
+
 // Transferir(from, sfield, to, tfield, iter, method, ord, all, to_zero):
 // every (source box, target box) pair of the two levels.
 Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfield, int iter, int method, int ord,
@@ -306,6 +327,7 @@ Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfi
       }
       add_region_jobs(X, J, T, lo, hi);
     }
+  if (!std::getenv("OLGPU_XFER_POINTS")) stride_jobs(h, X);
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
   X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
   return X;
@@ -342,6 +364,7 @@ Transfer make_set_in(olgpu_hierarchy *h, int k)
       add_region_jobs(X, J, C, lo, hi);
     }
   }
+  if (!std::getenv("OLGPU_XFER_POINTS")) stride_jobs(h, X);
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
   X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
   return X;
