@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(64) k_robin32_edges_corners(BoxList L, const D
 }
 
 enum Ew32Op { EW32_W_EQ_S_MINUS_R = 0, EW32_S_EQ_W_PLUS_R, EW32_W_PLUS_EQ_R, EW32_WW_EQ_E, EW32_V_EQ_E_MINUS_WW,
-              EW32_E_PLUS_EQ_V };
+              EW32_E_PLUS_EQ_V, EW32_S_EQ_W_PLUS_R_WW_EQ_E, EW32_W_PLUS_EQ_R_WW_EQ_E };
 
 __global__ void __launch_bounds__(256) k_elementwise32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
                                                        int op)
@@ -457,10 +457,19 @@ __global__ void __launch_bounds__(256) k_elementwise32(BoxList L, const DevBox *
   case EW32_WW_EQ_E: G.f[G_WW][p] = G.f[G_E][p]; break;
   case EW32_V_EQ_E_MINUS_WW: G.f[G_V][p] = G.f[G_E][p] - G.f[G_WW][p]; break;
   case EW32_E_PLUS_EQ_V: G.f[G_E][p] = G.f[G_E][p] + G.f[G_V][p]; break;
+  case EW32_S_EQ_W_PLUS_R_WW_EQ_E:   // two steps of one level in one pass
+    G.f[G_S][p] = G.f[G_W][p] + G.f[G_R][p];
+    G.f[G_WW][p] = G.f[G_E][p];
+    break;
+  case EW32_W_PLUS_EQ_R_WW_EQ_E:
+    G.f[G_W][p] = G.f[G_W][p] + G.f[G_R][p];
+    G.f[G_WW][p] = G.f[G_E][p];
+    break;
   }
 }
 
-// T = (1,2,1)^3/64 average of W on INSIDE points (see k_full_weight)
+// T = (1,2,1)^3/64 average of W = S - R on INSIDE points (see k_full_weight),
+// W formed where it is read (it is needed for nothing else)
 __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G)
 {
   long long lb;
@@ -472,8 +481,9 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
   const int i = (int)(t % B.n[0]);
   const long long r = t / B.n[0];
   const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
-  const float *w = G.f[G_W] + B.off;
-  const float c = w[t];
+  const float *gs = G.f[G_S] + B.off, *gr = G.f[G_R] + B.off;
+  auto w = [&](long long q) { return gs[q] - gr[q]; };
+  const float c = w(t);
   const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
   if (!inside) {
     G.f[G_T][B.off + t] = c;
@@ -486,9 +496,64 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
         const int ii = i + di, jj = j + dj, kk = k + dk;
         const float wt = (float)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (1.0f / 64.0f);
         const bool in = ii >= b && ii < B.n[0] - b && jj >= b && jj < B.n[1] - b && kk >= b && kk < B.n[2] - b;
-        acc += wt * (in ? w[pidx(B, ii, jj, kk)] : c);
+        acc += wt * (in ? w(pidx(B, ii, jj, kk)) : c);
       }
   G.f[G_T][B.off + t] = acc;
+}
+
+// The coarse-to-fine correction of one level in one pass: for every target
+// of the (trilinear) prolongation plan, E_fine += P(E_coarse - WW_coarse),
+// the difference formed at each source node as it is read.  The same terms
+// in the same order as V = E - WW, V_fine = P V, E += V_fine; targets the plan
+// zeroes get a zero correction and are left as they are.
+__global__ void __launch_bounds__(256) k_prolong_correct32(const XferJob *__restrict__ jobs, int njobs,
+                                                           const DevBox *__restrict__ boxes, DevFields32 G,
+                                                           const AxisEntry *__restrict__ tab)
+{
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox T = boxes[J.tbox];
+  if (J.iter != IT_ALL) {
+    const int b = T.buf;
+    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+    if ((J.iter == IT_INSIDE) != inside) return;
+  }
+  const AxisEntry &ax = tab[J.tab[0] + i];
+  const AxisEntry &ay = tab[J.tab[1] + j];
+  const AxisEntry &az = tab[J.tab[2] + k];
+  if (!(ax.sel && ay.sel && az.sel)) return;
+  const DevBox S = boxes[J.sbox];
+  const float *ec = G.f[G_E] + S.off, *wc = G.f[G_WW] + S.off;
+  auto v = [&](long long q) { return ec[q] - wc[q]; };
+  float vf;
+  if (ax.exact && ay.exact && az.exact) {
+    vf = v(pidx(S, ax.node, ay.node, az.node));
+  } else {
+    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
+    const float dxi = (float)ax.w[0], dxf = (float)ax.w[1], dyi = (float)ay.w[0], dyf = (float)ay.w[1],
+                dzi = (float)az.w[0], dzf = (float)az.w[1];
+    const float v000 = v(pidx(S, i0, j0, k0)), v100 = v(pidx(S, i0 + 1, j0, k0));
+    const float v010 = v(pidx(S, i0, j0 + 1, k0)), v110 = v(pidx(S, i0 + 1, j0 + 1, k0));
+    const float v001 = v(pidx(S, i0, j0, k0 + 1)), v101 = v(pidx(S, i0 + 1, j0, k0 + 1));
+    const float v011 = v(pidx(S, i0, j0 + 1, k0 + 1)), v111 = v(pidx(S, i0 + 1, j0 + 1, k0 + 1));
+    vf = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
+         ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
+  }
+  float *ef = G.f[G_E] + T.off;
+  const long long tp = pidx(T, i, j, k);
+  ef[tp] = ef[tp] + vf;
 }
 
 // Coarsest correction problem in one CTA: repeat { Robin; one red-black SOR

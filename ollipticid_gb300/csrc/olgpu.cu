@@ -843,7 +843,6 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   if (k <= mg) dispatch_robin32(h, k - 1, 1);
   dispatch_apply_op32<EQ>(h, k);
   if (k <= mg) dispatch_robin32(h, k, 1);
-  launch_ew32(h, k, EW32_W_EQ_S_MINUS_R);
   {
     const BoxList L = level_list(h, k, blocks_all);
     k_full_weight32<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32);
@@ -851,12 +850,11 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   }
   launch_transfer32(h, h->xfer_w32[k]);
   if (k <= mg) {
-    launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R);
+    launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R_WW_EQ_E);
   } else {
-    launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R);
+    launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R_WW_EQ_E);   // WW = E: nothing writes E before set_in
     launch_transfer32(h, h->set_in32[k]);
   }
-  launch_ew32(h, k - 1, EW32_WW_EQ_E);
   if (k == 1) {
     const DevBox &B = h->hboxes[h->G.first_box[0]];
     const size_t np = (size_t)B.n[0] * B.n[1] * B.n[2];
@@ -873,9 +871,14 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   } else {
     emit_fasn32<EQ>(h, k - 1);
   }
-  launch_ew32(h, k - 1, EW32_V_EQ_E_MINUS_WW);
-  launch_transfer32(h, h->prolong_v32[k]);
-  launch_ew32(h, k, EW32_E_PLUS_EQ_V);
+  {
+    const Transfer &X = h->prolong_v32[k];
+    if (!X.jobs.empty()) {
+      k_prolong_correct32<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes,
+                                                                         h->F32, h->d_tab);
+      h->launches_mixed++;
+    }
+  }
   if (k > mg) launch_transfer32(h, h->ghost_e[k]);
   if (k <= mg) dispatch_robin32(h, k, 0);
   dispatch_smooth32<EQ>(h, k, h->inner_nu2 >= 0 ? h->inner_nu2 : h->P.nu2);
@@ -911,7 +914,7 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     h->launches_mixed++;
   }
   const size_t n32 = sizeof(float) * (size_t)h->total_pts;
-  for (int f : {G_E, G_R, G_V}) cudaMemsetAsync(h->F32.f[f], 0, n32, h->stream);
+  for (int f : {G_E, G_R}) cudaMemsetAsync(h->F32.f[f], 0, n32, h->stream);
   // FP32 correction V-cycle
   emit_fasn32<EQ>(h, top);
   // FP64 update and the FP64 defect of the finest level as the cycle's norm
