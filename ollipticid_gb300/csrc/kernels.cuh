@@ -773,6 +773,60 @@ inline bool xfer_rows(const XferJob *jobs, size_t n, int width)
   return true;
 }
 
+// The tau transfer with the full weighting folded in: every job of the plan
+// is a strided copy from the fine level, so the (1,2,1)^3/64 average of W is
+// formed only at the fine nodes that are read (one in eight), with
+// k_full_weight's terms and order.  DIFF: W = f[fa] - f[fb] (the FP32 cycle
+// forms S - R where it is read), else W = f[fa].
+template <class V, class Fields, bool DIFF>
+__global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ jobs, int njobs,
+                                                 const DevBox *__restrict__ boxes, Fields F, int fa, int fb)
+{
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox &T = boxes[J.tbox];
+  if (J.iter != IT_ALL) {
+    const int b = T.buf;
+    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+    if ((J.iter == IT_INSIDE) != inside) return;
+  }
+  const DevBox &S = boxes[J.sbox];
+  const int si = J.sstart[0] + J.sstep[0] * (i - J.r0[0]);
+  const int sj = J.sstart[1] + J.sstep[1] * (j - J.r0[1]);
+  const int sk = J.sstart[2] + J.sstep[2] * (k - J.r0[2]);
+  const V *wa = F.f[fa] + S.off;
+  const V *wb = DIFF ? F.f[fb] + S.off : nullptr;
+  auto w = [&](long long q) -> V { return DIFF ? wa[q] - wb[q] : wa[q]; };
+  const V c = w(pidx(S, si, sj, sk));
+  const int b = S.buf;
+  V val = c;
+  if (si >= b && si < S.n[0] - b && sj >= b && sj < S.n[1] - b && sk >= b && sk < S.n[2] - b) {
+    V acc = V(0);
+    for (int dk = -1; dk <= 1; dk++)
+      for (int dj = -1; dj <= 1; dj++)
+        for (int di = -1; di <= 1; di++) {
+          const int ii = si + di, jj = sj + dj, kk = sk + dk;
+          const V wt = (V)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (V(1) / V(64));
+          const bool in = ii >= b && ii < S.n[0] - b && jj >= b && jj < S.n[1] - b && kk >= b && kk < S.n[2] - b;
+          acc += wt * (in ? w(pidx(S, ii, jj, kk)) : c);
+        }
+    val = acc;
+  }
+  F.f[J.tfield][T.off + pidx(T, i, j, k)] = val;
+}
+
 // ----------------------------------------------------------------------------
 // K5: coarsest-grid solve in one CTA: repeat { Robin; one red-black sweep }
 // until the sweep norm <= eps or stops changing (src/elliptic.cc:1782-1816),

@@ -60,6 +60,7 @@ struct Transfer {
   long long row_blocks = 0;         // blocks of the row kernel (k_xfer_rows)
   int width = 0;                    // kernel variant (xfer_width of the jobs)
   bool rows = false;                // run on k_xfer_rows
+  bool strided = false;             // every job is a strided copy
   XferJob *d_jobs = nullptr;
 };
 
@@ -330,6 +331,8 @@ Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfi
   if (!std::getenv("OLGPU_XFER_POINTS")) stride_jobs(h, X);
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
   X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
+  X.strided = !X.jobs.empty() && std::all_of(X.jobs.begin(), X.jobs.end(),
+                                             [](const XferJob &J) { return J.method == XM_STRIDED; });
   return X;
 }
 
@@ -367,6 +370,8 @@ Transfer make_set_in(olgpu_hierarchy *h, int k)
   if (!std::getenv("OLGPU_XFER_POINTS")) stride_jobs(h, X);
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
   X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
+  X.strided = !X.jobs.empty() && std::all_of(X.jobs.begin(), X.jobs.end(),
+                                             [](const XferJob &J) { return J.method == XM_STRIDED; });
   return X;
 }
 
@@ -577,12 +582,17 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   dispatch_apply_op<EQ>(h, k);
   if (k <= mg) dispatch_robin(h, k, 1);
   launch_ew(h, k, EW_W_EQ_S_MINUS_R);
-  {
+  if (h->xfer_w[k].strided) {   // full weighting folded into the transfer
+    const Transfer &X = h->xfer_w[k];
+    k_xfer_fw<double, DevFields, false><<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(
+        X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F, F_W, F_W);
+    h->launches++;
+  } else {
     const BoxList L = level_list(h, k, blocks_all);
     k_full_weight<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F);
     h->launches++;
+    launch_transfer(h, h->xfer_w[k]);
   }
-  launch_transfer(h, h->xfer_w[k]);
   if (k <= mg) {
     launch_ew(h, k - 1, EW_S_EQ_W_PLUS_R);
   } else {
@@ -843,12 +853,17 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   if (k <= mg) dispatch_robin32(h, k - 1, 1);
   dispatch_apply_op32<EQ>(h, k);
   if (k <= mg) dispatch_robin32(h, k, 1);
-  {
+  if (h->xfer_w32[k].strided) {   // full weighting of S - R folded into the transfer
+    const Transfer &X = h->xfer_w32[k];
+    k_xfer_fw<float, DevFields32, true><<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(
+        X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32, G_S, G_R);
+    h->launches_mixed++;
+  } else {
     const BoxList L = level_list(h, k, blocks_all);
     k_full_weight32<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32);
     h->launches_mixed++;
+    launch_transfer32(h, h->xfer_w32[k]);
   }
-  launch_transfer32(h, h->xfer_w32[k]);
   if (k <= mg) {
     launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R_WW_EQ_E);
   } else {
@@ -949,6 +964,7 @@ Transfer remap(const Transfer &X, int sfield, int tfield)
   Y.blocks = X.blocks;
   Y.width = X.width;
   Y.rows = X.rows;
+  Y.strided = X.strided;
   Y.row_blocks = X.row_blocks;
   for (auto &J : Y.jobs) {
     J.sfield = sfield;
