@@ -501,6 +501,45 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
   G.f[G_T][B.off + t] = acc;
 }
 
+// Set_In of a refinement level with the coarse operator folded in: at every
+// target of the (strided, same-box) Set_In plan S = W + N(e), N evaluated as
+// k_apply_op32 does on INSIDE points and 0 on the ghosts (where R is 0 on a
+// refinement level).  The coarse R is needed nowhere else, so it is formed
+// only where Set_In copies, not on the whole level.
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_set_in_op32(const XferJob *__restrict__ jobs, int njobs,
+                                                     const DevBox *__restrict__ boxes, DevFields32 G)
+{
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox T = boxes[J.tbox];
+  const DevBox &S = boxes[J.sbox];
+  const long long sp = pidx(S, J.sstart[0] + J.sstep[0] * (i - J.r0[0]), J.sstart[1] + J.sstep[1] * (j - J.r0[1]),
+                            J.sstart[2] + J.sstep[2] * (k - J.r0[2]));
+  const long long tp = pidx(T, i, j, k);
+  const int b = T.buf;
+  float rr = 0.0f;
+  if (i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b) {
+    const float lv = lapf<ORD>(G.f[G_E] + T.off, tp, T.n[0], (long long)T.n[0] * T.n[1], T);
+    float op, dop;
+    corr_at<EQ>(T, G, tp, lv, op, dop);
+    rr = op;
+  }
+  G.f[G_S][T.off + tp] = G.f[G_W][S.off + sp] + rr;
+}
+
 // The coarse-to-fine correction of one level in one pass: for every target
 // of the (trilinear) prolongation plan, E_fine += P(E_coarse - WW_coarse),
 // the difference formed at each source node as it is read.  The same terms

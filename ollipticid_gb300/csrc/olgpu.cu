@@ -849,7 +849,10 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   if (k <= mg) dispatch_robin32(h, k, 0);
   dispatch_smooth32<EQ>(h, k, h->inner_nu1 >= 0 ? h->inner_nu1 : h->P.nu1);
   launch_transfer32(h, h->restrict_e[k]);
-  dispatch_apply_op32<EQ>(h, k - 1);
+  // on a refinement level the coarse operator is only needed where Set_In
+  // copies (k_set_in_op32 forms it there)
+  const bool fold_set_in = k > mg && h->set_in32[k].strided;
+  if (!fold_set_in) dispatch_apply_op32<EQ>(h, k - 1);
   if (k <= mg) dispatch_robin32(h, k - 1, 1);
   dispatch_apply_op32<EQ>(h, k);
   if (k <= mg) dispatch_robin32(h, k, 1);
@@ -866,6 +869,18 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   }
   if (k <= mg) {
     launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R_WW_EQ_E);
+  } else if (fold_set_in) {
+    launch_ew32(h, k - 1, EW32_WW_EQ_E);
+    const Transfer &X = h->set_in32[k];
+    const unsigned nb = (unsigned)X.blocks;
+    const int nj = (int)X.jobs.size();
+    switch (level_order(h, k - 1)) {
+    case 2: k_set_in_op32<2, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F32); break;
+    case 4: k_set_in_op32<4, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F32); break;
+    case 6: k_set_in_op32<6, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F32); break;
+    default: k_set_in_op32<8, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F32); break;
+    }
+    h->launches_mixed++;
   } else {
     launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R_WW_EQ_E);   // WW = E: nothing writes E before set_in
     launch_transfer32(h, h->set_in32[k]);
