@@ -827,6 +827,104 @@ __global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ job
   F.f[J.tfield][T.off + pidx(T, i, j, k)] = val;
 }
 
+// The coarse-to-fine correction of one level in one pass: for every target
+// of the (trilinear) prolongation plan, E_fine += P(E_coarse - WW_coarse),
+// the difference formed at each source node as it is read (fe, fww: the
+// solution / correction field and its copy from before the coarse solve).
+// The same terms in the same order as V = E - WW, V_fine = P V,
+// E += V_fine; targets the plan zeroes get a zero correction and are left
+// as they are.
+template <class V, class Fields>
+__global__ void __launch_bounds__(256) k_prolong_correct(const XferJob *__restrict__ jobs, int njobs,
+                                                         const DevBox *__restrict__ boxes, Fields F,
+                                                         const AxisEntry *__restrict__ tab, int fe, int fww)
+{
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox T = boxes[J.tbox];
+  if (J.iter != IT_ALL) {
+    const int b = T.buf;
+    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+    if ((J.iter == IT_INSIDE) != inside) return;
+  }
+  const AxisEntry &ax = tab[J.tab[0] + i];
+  const AxisEntry &ay = tab[J.tab[1] + j];
+  const AxisEntry &az = tab[J.tab[2] + k];
+  if (!(ax.sel && ay.sel && az.sel)) return;
+  const DevBox S = boxes[J.sbox];
+  const V *ec = F.f[fe] + S.off, *wc = F.f[fww] + S.off;
+  auto v = [&](long long q) -> V { return ec[q] - wc[q]; };
+  V vf;
+  if (ax.exact && ay.exact && az.exact) {
+    vf = v(pidx(S, ax.node, ay.node, az.node));
+  } else {
+    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
+    const V dxi = (V)ax.w[0], dxf = (V)ax.w[1], dyi = (V)ay.w[0], dyf = (V)ay.w[1], dzi = (V)az.w[0],
+            dzf = (V)az.w[1];
+    const V v000 = v(pidx(S, i0, j0, k0)), v100 = v(pidx(S, i0 + 1, j0, k0));
+    const V v010 = v(pidx(S, i0, j0 + 1, k0)), v110 = v(pidx(S, i0 + 1, j0 + 1, k0));
+    const V v001 = v(pidx(S, i0, j0, k0 + 1)), v101 = v(pidx(S, i0 + 1, j0, k0 + 1));
+    const V v011 = v(pidx(S, i0, j0 + 1, k0 + 1)), v111 = v(pidx(S, i0 + 1, j0 + 1, k0 + 1));
+    vf = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
+         ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
+  }
+  V *ef = F.f[fe] + T.off;
+  const long long tp = pidx(T, i, j, k);
+  ef[tp] = ef[tp] + vf;
+}
+
+// Set_In of a refinement level with the coarse FP64 operator folded in:
+// RHO = W + OP(u) at every target of the (strided, same-box) Set_In plan, OP
+// evaluated as k_apply_op does on INSIDE points and 0 on the ghosts (R is 0
+// there on a refinement level).  The coarse R is needed nowhere else.
+template <int ORD, int EQ>
+__global__ void __launch_bounds__(256) k_set_in_op(const XferJob *__restrict__ jobs, int njobs,
+                                                   const DevBox *__restrict__ boxes, DevFields F)
+{
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    else hi = mid - 1;
+  }
+  const XferJob J = jobs[lo];
+  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
+  if (t >= (long long)e0 * e1 * e2) return;
+  const int i = J.r0[0] + (int)(t % e0);
+  const long long r = t / e0;
+  const int j = J.r0[1] + (int)(r % e1);
+  const int k = J.r0[2] + (int)(r / e1);
+  const DevBox T = boxes[J.tbox];
+  const DevBox &S = boxes[J.sbox];
+  const long long sp = pidx(S, J.sstart[0] + J.sstep[0] * (i - J.r0[0]), J.sstart[1] + J.sstep[1] * (j - J.r0[1]),
+                            J.sstart[2] + J.sstep[2] * (k - J.r0[2]));
+  const long long tp = pidx(T, i, j, k);
+  const int b = T.buf;
+  double rr = 0.0;
+  if (i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b) {
+    const double *u = F.f[F_U] + T.off;
+    const double lv = lap<ORD>(u, tp, T.n[0], (long long)T.n[0] * T.n[1], T);
+    double op, dop;
+    point_op<EQ>(lv, T.dulap, u[tp], F.f[F_B][T.off + tp], F.f[F_C][T.off + tp],
+                 EQ ? F.f[F_D][T.off + tp] : 0.0, EQ ? F.f[F_E][T.off + tp] : 0.0, op, dop);
+    rr = op;
+  }
+  F.f[F_RHO][T.off + tp] = F.f[F_W][S.off + sp] + rr;
+}
+
 // ----------------------------------------------------------------------------
 // K5: coarsest-grid solve in one CTA: repeat { Robin; one red-black sweep }
 // until the sweep norm <= eps or stops changing (src/elliptic.cc:1782-1816),

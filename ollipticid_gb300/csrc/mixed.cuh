@@ -540,61 +540,6 @@ __global__ void __launch_bounds__(256) k_set_in_op32(const XferJob *__restrict__
   G.f[G_S][T.off + tp] = G.f[G_W][S.off + sp] + rr;
 }
 
-// The coarse-to-fine correction of one level in one pass: for every target
-// of the (trilinear) prolongation plan, E_fine += P(E_coarse - WW_coarse),
-// the difference formed at each source node as it is read.  The same terms
-// in the same order as V = E - WW, V_fine = P V, E += V_fine; targets the plan
-// zeroes get a zero correction and are left as they are.
-__global__ void __launch_bounds__(256) k_prolong_correct32(const XferJob *__restrict__ jobs, int njobs,
-                                                           const DevBox *__restrict__ boxes, DevFields32 G,
-                                                           const AxisEntry *__restrict__ tab)
-{
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
-    else hi = mid - 1;
-  }
-  const XferJob J = jobs[lo];
-  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
-  const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
-  if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
-  const DevBox T = boxes[J.tbox];
-  if (J.iter != IT_ALL) {
-    const int b = T.buf;
-    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
-    if ((J.iter == IT_INSIDE) != inside) return;
-  }
-  const AxisEntry &ax = tab[J.tab[0] + i];
-  const AxisEntry &ay = tab[J.tab[1] + j];
-  const AxisEntry &az = tab[J.tab[2] + k];
-  if (!(ax.sel && ay.sel && az.sel)) return;
-  const DevBox S = boxes[J.sbox];
-  const float *ec = G.f[G_E] + S.off, *wc = G.f[G_WW] + S.off;
-  auto v = [&](long long q) { return ec[q] - wc[q]; };
-  float vf;
-  if (ax.exact && ay.exact && az.exact) {
-    vf = v(pidx(S, ax.node, ay.node, az.node));
-  } else {
-    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
-    const float dxi = (float)ax.w[0], dxf = (float)ax.w[1], dyi = (float)ay.w[0], dyf = (float)ay.w[1],
-                dzi = (float)az.w[0], dzf = (float)az.w[1];
-    const float v000 = v(pidx(S, i0, j0, k0)), v100 = v(pidx(S, i0 + 1, j0, k0));
-    const float v010 = v(pidx(S, i0, j0 + 1, k0)), v110 = v(pidx(S, i0 + 1, j0 + 1, k0));
-    const float v001 = v(pidx(S, i0, j0, k0 + 1)), v101 = v(pidx(S, i0 + 1, j0, k0 + 1));
-    const float v011 = v(pidx(S, i0, j0 + 1, k0 + 1)), v111 = v(pidx(S, i0 + 1, j0 + 1, k0 + 1));
-    vf = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
-         ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
-  }
-  float *ef = G.f[G_E] + T.off;
-  const long long tp = pidx(T, i, j, k);
-  ef[tp] = ef[tp] + vf;
-}
-
 // Coarsest correction problem in one CTA: repeat { Robin; one red-black SOR
 // sweep } until the sweep norm <= rtol * first, stops changing, or max_it.
 // e lives in shared memory; with SMEM the read-only coefficients (A, 1/(c+u),

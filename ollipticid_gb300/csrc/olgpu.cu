@@ -130,6 +130,10 @@ struct olgpu_hierarchy {
   // pre-/post-smoothing sweeps of the FP32 correction cycle (-1: nu1/nu2)
   int inner_nu1 = -1, inner_nu2 = -1;
   int sc_max = 16;   // largest cluster for the FP32 smoother (0: per-colour launches)
+  // structural fast paths of the transfers (strided copies, folded full
+  // weighting / Set_In operator, fused prolong-and-correct); off only to test
+  // them against the plain steps
+  bool fast_paths = !std::getenv("OLGPU_XFER_POINTS");
 };
 
 namespace {
@@ -577,7 +581,10 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   if (k <= mg) dispatch_robin(h, k, 0);
   dispatch_smooth<EQ>(h, k, h->P.nu1, 2 * k);
   launch_transfer(h, h->restrict_u[k]);
-  dispatch_apply_op<EQ>(h, k - 1);
+  // on a refinement level the coarse operator is only needed where Set_In
+  // copies (k_set_in_op forms it there)
+  const bool fold_set_in = k > mg && h->set_in[k].strided;
+  if (!fold_set_in) dispatch_apply_op<EQ>(h, k - 1);
   if (k <= mg) dispatch_robin(h, k - 1, 1);
   dispatch_apply_op<EQ>(h, k);
   if (k <= mg) dispatch_robin(h, k, 1);
@@ -595,6 +602,17 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   }
   if (k <= mg) {
     launch_ew(h, k - 1, EW_S_EQ_W_PLUS_R);
+  } else if (fold_set_in) {
+    const Transfer &X = h->set_in[k];
+    const unsigned nb = (unsigned)X.blocks;
+    const int nj = (int)X.jobs.size();
+    switch (level_order(h, k - 1)) {
+    case 2: k_set_in_op<2, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F); break;
+    case 4: k_set_in_op<4, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F); break;
+    case 6: k_set_in_op<6, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F); break;
+    default: k_set_in_op<8, EQ><<<nb, kThreads, 0, h->stream>>>(X.d_jobs, nj, h->d_boxes, h->F); break;
+    }
+    h->launches++;
   } else {
     launch_ew(h, k - 1, EW_W_PLUS_EQ_R);
     launch_transfer(h, h->set_in[k]);
@@ -614,9 +632,18 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   } else {
     emit_fasn<EQ>(h, k - 1, top);
   }
-  launch_ew(h, k - 1, EW_V_EQ_U_MINUS_WW);
-  launch_transfer(h, h->prolong_v[k]);
-  launch_ew(h, k, EW_U_PLUS_EQ_V);
+  if (h->fast_paths) {   // u_fine += P(u - ww) in one pass
+    const Transfer &X = h->prolong_v[k];
+    if (!X.jobs.empty()) {
+      k_prolong_correct<double, DevFields><<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(
+          X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F, h->d_tab, F_U, F_WW);
+      h->launches++;
+    }
+  } else {
+    launch_ew(h, k - 1, EW_V_EQ_U_MINUS_WW);
+    launch_transfer(h, h->prolong_v[k]);
+    launch_ew(h, k, EW_U_PLUS_EQ_V);
+  }
   if (k > mg) launch_transfer(h, h->ghost_u[k]);
   if (k <= mg) dispatch_robin(h, k, 0);
   dispatch_smooth<EQ>(h, k, h->P.nu2, 2 * k + 1);
@@ -901,13 +928,17 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   } else {
     emit_fasn32<EQ>(h, k - 1);
   }
-  {
+  if (h->fast_paths) {   // e_fine += P(e - ww) in one pass
     const Transfer &X = h->prolong_v32[k];
     if (!X.jobs.empty()) {
-      k_prolong_correct32<<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(X.d_jobs, (int)X.jobs.size(), h->d_boxes,
-                                                                         h->F32, h->d_tab);
+      k_prolong_correct<float, DevFields32><<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(
+          X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32, h->d_tab, G_E, G_WW);
       h->launches_mixed++;
     }
+  } else {
+    launch_ew32(h, k - 1, EW32_V_EQ_E_MINUS_WW);
+    launch_transfer32(h, h->prolong_v32[k]);
+    launch_ew32(h, k, EW32_E_PLUS_EQ_V);
   }
   if (k > mg) launch_transfer32(h, h->ghost_e[k]);
   if (k <= mg) dispatch_robin32(h, k, 0);
@@ -944,7 +975,8 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     h->launches_mixed++;
   }
   const size_t n32 = sizeof(float) * (size_t)h->total_pts;
-  for (int f : {G_E, G_R}) cudaMemsetAsync(h->F32.f[f], 0, n32, h->stream);
+  for (int f : {G_E, G_R, G_V})
+    if (f != G_V || !h->fast_paths) cudaMemsetAsync(h->F32.f[f], 0, n32, h->stream);
   // FP32 correction V-cycle
   emit_fasn32<EQ>(h, top);
   // FP64 update and the FP64 defect of the finest level as the cycle's norm
