@@ -41,6 +41,12 @@ UNIT = "solves/s"
 # the oracle, which reproduces the reference's iterates bit for bit).
 CPU_CYCLES_PER_SOLVE = 17
 SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
+# DRAM bytes (read + write) and FP64-pipe occupancy of one finest-level
+# launch of k_smooth_color<4,0> on this workload, from an ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum; sm__inst_executed_pipe_fp64
+# .avg.pct_of_peak_sustained_active)
+SMOOTH_TRAFFIC_PER_LAUNCH = 17_600_768
+SMOOTH_FP64_PIPE_PCT = 70.4
 
 
 def _peaks():
@@ -402,19 +408,27 @@ def run_gpu(args, rank: int, world: int, local: int):
         batched = run_batched(args)
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]) + (concurrent["smoother_blocks"],))
 
-    # ---- roofline of the dominant kernel (multicolour smoother), all levels
+    # ---- roofline of the dominant kernel: one colour pass of the FP64
+    # multicolour smoother (k_smooth_color) on the finest level, timed with
+    # CUDA events on the solver's stream over 10 sweeps of that level
     peak, peak_kind = _peaks()
-    tot_bytes, tot_ms, tot_launch = 0.0, 0.0, 0
-    for lev in range(1, E.levels):
-        E.time_smoother(lev, 2)                      # warm
-        ms, nl = E.time_smoother(lev, 10)
-        tot_bytes += E.interior_points(lev) * SMOOTH_BYTES_PER_POINT * 10
-        tot_ms += ms
-        tot_launch += nl
-    achieved = tot_bytes / (tot_ms / 1000.0) / 1e9
+    top = E.levels - 1
+    colours = P.order // 2 + 1
+    E.time_smoother(top, 2)                               # warm
+    ms, nl = E.time_smoother(top, 10)
+    pts = E.interior_points(top)
+    launch_s = ms / 1000.0 / nl
+    bytes_per_launch = SMOOTH_BYTES_PER_POINT * pts / colours
+    achieved = bytes_per_launch / launch_s / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "peak_kind": peak_kind, "traffic": None, "kernel": "k_smooth_color (all levels)",
-            "launches_timed": tot_launch}
+            "peak_kind": peak_kind, "traffic": SMOOTH_TRAFFIC_PER_LAUNCH,
+            "kernel": f"k_smooth_color<{P.order},0>: one colour pass of the finest level "
+                      f"({pts} interior points, {colours} colours)",
+            "algorithmic_bytes_per_launch": bytes_per_launch, "launch_us": launch_s * 1e6, "launches_timed": nl,
+            "fp64_pipe_active_pct": SMOOTH_FP64_PIPE_PCT,
+            "note": "FP64-issue bound on GB300 (about 2 FP64 FMA per clock per SM): the HBM fraction is low by "
+                    "design; traffic and FP64 pipe occupancy are from one ncu capture of this launch (ncu flushes "
+                    "L2 first, so traffic is the level's fields read once; in the timed sweeps they stay in L2)"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
