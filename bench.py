@@ -274,7 +274,40 @@ def run_concurrent(E_ref, P, u_fix, adm_fix, plain_value, n: int = 16):
             E.close()
 
 
-def run_batched(args, count: int = 16, group: int = 8):
+CONFIG3_ARGS = WORKLOAD_ARGS.replace("-N 65", "-N 129").replace("-O 4", "-O 8").replace("-s 1e-11", "-s 1e-10")
+
+
+def run_config3():
+    """The same binary at 8th order on boxes of 129^3 points: plain FP64 and
+    mixed precision, each solved from u = 0 to a residual of 1e-10, against
+    the FP64 fixed point (max |u - u_FP64| on every fixed point, ADM)."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    P = og.parse_olliptic_args(CONFIG3_ARGS.split())
+    E = og.Elliptic(P)
+    try:
+        out = {"workload": "binary O8 N129 l9 L1000, tol 1e-10", "boxes": len(E.boxes),
+               "points": sum(b.n[0] * b.n[1] * b.n[2] for b in E.boxes)}
+        res = {}
+        for mixed in (False, True):
+            E.set_precision(mixed)
+            E.reset()
+            rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+            res[mixed] = (rep, E.last_device_ms, [E.get_field(g) for g in range(len(E.boxes))])
+        u_fix = fixed_point(E)
+        adm_fix = E.ADM_mass
+        for mixed, key in ((False, "plain_fp64"), (True, "mixed")):
+            rep, ms, u = res[mixed]
+            out[key] = {"solves_per_s": 1000.0 / ms, "ms_per_solve": ms, "cycles": rep.cycles,
+                        "final_res": rep.final_res, "max_abs_u_minus_fp64_fixed_point": pinned_max_diff(E, u, u_fix),
+                        "adm_minus_fp64_fixed_point": [a - b for a, b in zip(rep.adm[:2], adm_fix)]}
+        out["adm_fp64_fixed_point"] = list(adm_fix)
+        return out
+    finally:
+        E.close()
+
+
+def run_batched(args, count: int = 16, group: int = 16, tuned=None):
     """Seeded batched binaries (mixed precision, tol 1e-10): solves/s when
     `group` solves run concurrently, and the same instances one at a time."""
     import ollipticid_gb300 as og
@@ -285,6 +318,8 @@ def run_batched(args, count: int = 16, group: int = 8):
         sol = [og.Elliptic(p) for p in probs[g0:g0 + group]]
         for E in sol:
             E.set_precision(True)
+            if tuned is not None:
+                tuned.apply(E)
         for E in sol:                                   # warm-up
             E.reset()
         og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
@@ -303,6 +338,7 @@ def run_batched(args, count: int = 16, group: int = 8):
             E.close()
     return {"workload": f"first {count} of 256 seeded binaries (N in {{33,49,65,97}}, 6-10 levels, O4), "
                         f"mixed precision to 1e-10", "concurrent_solves": group,
+            "inner_sweeps": None if tuned is None else [tuned.nu1, tuned.nu2, tuned.blocks],
             "value": count / con_s, "unit": UNIT, "one_at_a_time": count / seq_s,
             "cycles_mean": sum(cycles) / len(cycles), "timing": "host wall clock around the solves"}
 
@@ -402,10 +438,12 @@ def run_gpu(args, rank: int, world: int, local: int):
     # ---- the same workload with the mixed-precision cycle
     mixed = run_mixed(E, P, args, dev, u_fix, adm_fix)
 
-    concurrent = batched = served = None
+    concurrent = batched = served = config3 = None
     if rank == 0 and world == 1 and not args.no_extra:
+        from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, u_fix, adm_fix, value / world)
-        batched = run_batched(args)
+        batched = run_batched(args, tuned=autotune.tune(P, concurrency=16))
+        config3 = run_config3()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]) + (concurrent["smoother_blocks"],))
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
@@ -449,7 +487,7 @@ def run_gpu(args, rank: int, world: int, local: int):
                        "points": total_pts, "wall_s": wall},
             "accuracy": {"max_abs_u_minus_fixed_point": err_fp64,
                          "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
-            "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served,
+            "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served, "config3": config3,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
         }
