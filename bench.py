@@ -358,6 +358,23 @@ def run_served(rates=(4.0, 16.0), count: int = 24, inner_sweeps=None):
     return out
 
 
+def slowest_rank_ms(ms: float, world: int, device) -> float:
+    """The timed region's length: the maximum over ranks (replicas run the
+    same work; the job is done when the slowest one is)."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.barrier()
+    return float(t.item())
+
+
+def replica_throughput(steps: int, slowest_ms: float, world: int) -> float:
+    """Whole-job solves/s: every rank solves `steps` problems of its own."""
+    return world * steps / (slowest_ms / 1000.0)
+
+
 def run_gpu(args, rank: int, world: int, local: int):
     import numpy as np
     import torch
@@ -397,14 +414,10 @@ def run_gpu(args, rank: int, world: int, local: int):
         reps.append(rep)
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall0
-    if world > 1:
-        t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
-        torch.distributed.barrier()
+    dev_ms = slowest_rank_ms(dev_ms, world, dev)
     clk = clocks.stop()
     ms_per_step = dev_ms / args.steps
-    value = world * args.steps / (dev_ms / 1000.0)
+    value = replica_throughput(args.steps, dev_ms, world)
     launches = E.kernels_per_cycle * cycles
 
     # ---- end to end through the C ABI with host buffers

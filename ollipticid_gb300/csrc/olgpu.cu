@@ -104,8 +104,8 @@ struct olgpu_hierarchy {
   int coarse_max_iters = 2000;
   int coarse_ncta = 0;            // blocks of the coarse-solve cluster (0: one block)
   size_t coarse_cluster_smem = 0;
-  double coarse_omega = 1.85;
-  double coarse_rtol = 1e-5;
+  double coarse_omega = 1.9;
+  double coarse_rtol = 1e-4;
   double eps_solv = 0, eps_coarse = 0;
   int launches = 0;               // kernels emitted while capturing the V-cycle
   // mixed precision (FP32 correction cycle around the FP64 state)
@@ -1366,6 +1366,11 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     if (e1 != cudaSuccess || e2 != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, "shared memory opt-in failed"));
   }
   if (!std::getenv("OLGPU_COARSE_ONE_BLOCK")) choose_coarse_cluster(h);
+  // coarsest-solve tuning knobs (over-relaxation, relative stop): they change
+  // the work per cycle and how well the coarse problem is solved, not the
+  // fixed point of the cycle
+  if (const char *v = std::getenv("OLGPU_COARSE_OMEGA")) h->coarse_omega = std::atof(v);
+  if (const char *v = std::getenv("OLGPU_COARSE_RTOL")) h->coarse_rtol = std::atof(v);
   st = olgpu_reset(h);
   if (st != OLGPU_OK) return cleanup(st);
   // coefficients on the device
