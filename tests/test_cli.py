@@ -1,0 +1,63 @@
+"""Olliptic_gpu.x: the reference's command line on the C ABI.  The plan and
+the refusal of other equations need no GPU; the solve's printed ADM masses
+equal the Python API's solve of the same command line."""
+import os
+import re
+import subprocess
+
+import pytest
+
+from tests.cases import CASES, CONFIG2, problem
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "ollipticid_gb300", "_build", "Olliptic_gpu.x")
+
+
+@pytest.fixture(scope="module")
+def cli():
+    from ollipticid_gb300 import build
+    build.build()
+    assert os.path.exists(CLI)
+    return CLI
+
+
+def run(cli, args, check=True):
+    r = subprocess.run([cli] + args.split(), capture_output=True, text=True, timeout=600)
+    if check:
+        assert r.returncode == 0, r.stderr
+    return r
+
+
+def test_plan_matches_the_library(cli):
+    import ctypes as C
+    from ollipticid_gb300 import _abi
+    r = run(cli, CONFIG2 + " -plan yes")
+    m = re.search(r"(\d+) levels \((\d+) multigrid\), (\d+) boxes", r.stdout)
+    assert m, r.stdout
+    lib = _abi.load()
+    cp = problem(CONFIG2).to_c()
+    out = (_abi.BoxInfo * 512)()
+    nb, nl, mg = C.c_int(), C.c_int(), C.c_int()
+    _abi.check(lib.olgpu_plan_boxes(C.byref(cp), out, 512, C.byref(nb), C.byref(nl), C.byref(mg)))
+    assert (int(m.group(1)), int(m.group(2)), int(m.group(3))) == (nl.value, mg.value, nb.value)
+    sizes = re.findall(r"box +\d+ level +\d+ +(\d+) x (\d+) x (\d+)", r.stdout)
+    assert [tuple(map(int, s)) for s in sizes] == [(out[g].nx, out[g].ny, out[g].nz) for g in range(nb.value)]
+
+
+def test_other_equations_are_refused(cli):
+    r = run(cli, "-eq Poisson -N 33", check=False)
+    assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["o4_binary_merge", "sf_binary"])
+def test_cli_solve_matches_the_api(cli, case):
+    import ollipticid_gb300 as og
+    r = run(cli, CASES[case])
+    adm = [float(x) for x in re.findall(r"ADM mass\[\d+\] = (\S+)", r.stdout)]
+    with og.Elliptic(problem(case)) as E:
+        rep = E.Solve()
+        assert len(adm) == len(E.ADM_mass)
+        for a, b in zip(adm, E.ADM_mass):
+            assert a == b
+        assert f"Solved in {rep.cycles} V-cycles" in r.stdout
