@@ -28,9 +28,10 @@ from typing import Dict, List, Optional, Sequence, Tuple
 from . import Elliptic, Problem, _abi, solve_many
 
 # (nu1, nu2, smoother cluster blocks) candidates: the reference's own (3, 20)
-# and lighter schedules, cluster-resident or per-colour smoothing
-CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((3, 20, 16), (3, 12, 16), (3, 8, 16), (2, 4, 16), (3, 8, 0),
-                                                (2, 4, 0))
+# and lighter schedules (more pre- than post-smoothing pays: fewer outer
+# cycles), cluster-resident or per-colour smoothing
+CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((3, 20, 16), (3, 8, 16), (4, 6, 16), (4, 4, 16), (5, 4, 16),
+                                                (5, 6, 16), (6, 4, 16), (4, 6, 0), (3, 8, 0), (2, 4, 0))
 
 _lock = threading.Lock()
 _memo: Dict[str, "Choice"] = {}
