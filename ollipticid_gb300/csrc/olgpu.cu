@@ -1152,7 +1152,7 @@ double elapsed_ms(cudaEvent_t a, cudaEvent_t b)
 extern "C" {
 
 const char *olgpu_last_error(void) { return g_last_error.c_str(); }
-const char *olgpu_version(void) { return "olgpu 0.1 (sm_103a, FP64 FAS)"; }
+const char *olgpu_version(void) { return "olgpu 0.2 (sm_103a, FP64 FAS; FP32/FP64 mixed precision)"; }
 
 void olgpu_problem_defaults(olgpu_problem *p)
 {
