@@ -721,7 +721,8 @@ namespace olgpu {
 // on the coarse levels under the refinement boxes) is damped much faster.
 // Differences are stored in FP32 (they are correction-sized); sums in FP64.
 // ---------------------------------------------------------------------------
-constexpr int kAndMax = 4;
+constexpr int kAndMax = 4;   // largest history depth (deeper histories did not cut cycles)
+constexpr int kAndDefault = 4;
 
 struct AndersonState {
   int k;            // outer iterations done since the last reset
@@ -806,15 +807,17 @@ __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__
 }
 
 // Solves the regularised normal equations for gamma.  Launched with
-// kAndPart warps: warp v adds partial v of every block (lane l takes blocks
-// l, l + 32, ...; then a fixed butterfly), so the sums do not depend on
-// scheduling; thread 0 then eliminates.
-__global__ void __launch_bounds__(32 * kAndPart) k_and_solve(AndersonState *st, const double *__restrict__ part,
-                                                             int nblocks)
+// kAndSolveWarps warps: warp w adds partials w, w + kAndSolveWarps, ... of
+// every block (lane l takes blocks l, l + 32, ...; then a fixed butterfly),
+// so the sums do not depend on scheduling; thread 0 then eliminates.
+constexpr int kAndSolveWarps = kAndPart < 32 ? kAndPart : 32;
+
+__global__ void __launch_bounds__(32 * kAndSolveWarps) k_and_solve(AndersonState *st, const double *__restrict__ part,
+                                                                   int nblocks)
 {
   __shared__ double tot[kAndPart];
-  const int v = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (v < kAndPart) {
+  const int lane = threadIdx.x & 31;
+  for (int v = threadIdx.x >> 5; v < kAndPart; v += kAndSolveWarps) {
     double s = 0.0;
     for (int blk = lane; blk < nblocks; blk += 32) s += part[(long long)blk * kAndPart + v];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

@@ -117,7 +117,7 @@ struct olgpu_hierarchy {
   int launches_mixed = 0;
   double last_defect = 0, last_correction = 0;   // parts of the last mixed cycle's norm
   // Anderson acceleration of the mixed outer iteration
-  int anderson_m = kAndMax;
+  int anderson_m = kAndDefault;
   float *d_and = nullptr;               // DU[m], DF[m], fprev (FP32, total_pts each)
   unsigned char *d_pinned = nullptr;    // points the discrete system fixes
   AndersonState *d_and_state = nullptr;
@@ -986,7 +986,7 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     const int nblk = 152 * 4;
     k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E], fprev, DF, h->d_pinned, h->d_and_state,
                                                     h->d_and_part, &h->d_stats->slots[126]);
-    k_and_solve<<<1, 32 * kAndPart, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
+    k_and_solve<<<1, 32 * kAndSolveWarps, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
     k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U], h->F32.f[G_E], DU, DF, h->d_and_state);
     h->launches_mixed += 3;
   } else {
