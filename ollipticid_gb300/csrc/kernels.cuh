@@ -232,6 +232,20 @@ __device__ __forceinline__ void robin_point(const DevBox &B, const DevFields &F,
 }
 
 // ----------------------------------------------------------------------------
+// programmatic dependent launch: a kernel launched with
+// cudaLaunchAttributeProgrammaticStreamSerialization may be scheduled while
+// its predecessor in the stream is still running; it must not read anything
+// the predecessor writes before griddep_wait() returns (then all of the
+// predecessor's memory operations are complete and visible).
+// griddep_launch_dependents() lets the next such kernel be scheduled early.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents()
+{
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// ----------------------------------------------------------------------------
 // reductions
 // ----------------------------------------------------------------------------
 // v >= 0: a non-negative double orders like its bit pattern read as an
@@ -288,6 +302,7 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
                                                       unsigned long long *norm_slot, int *nan_flag)
 {
   constexpr int NC = num_colors<ORD>();
+  griddep_wait();                 // launched as a programmatic dependent
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
   const int b = B.buf;

@@ -265,6 +265,7 @@ __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__res
                                                   int color, int *nan_flag)
 {
   constexpr int NC = num_colors<ORD>();
+  griddep_wait();                 // launched as a programmatic dependent
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
   const int b = B.buf;

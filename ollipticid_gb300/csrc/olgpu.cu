@@ -134,6 +134,9 @@ struct olgpu_hierarchy {
   // weighting / Set_In operator, fused prolong-and-correct); off only to test
   // them against the plain steps
   bool fast_paths = !std::getenv("OLGPU_XFER_POINTS");
+  // smoother launches as programmatic dependents (overlap launch with the
+  // previous kernel's tail); off with OLGPU_NO_PDL
+  bool pdl = !std::getenv("OLGPU_NO_PDL");
 };
 
 namespace {
@@ -379,16 +382,34 @@ Transfer make_set_in(olgpu_hierarchy *h, int k)
   return X;
 }
 
+// Launches a kernel as a programmatic dependent of the previous work in the
+// stream (the kernel waits on griddep_wait() before reading anything).
+template <class... KArgs, class... Args>
+void launch_pdl(olgpu_hierarchy *h, void (*kern)(KArgs...), unsigned grid, unsigned block, Args... args)
+{
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(block, 1, 1);
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = h->pdl ? 1 : 0;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 template <int ORD, int EQ>
 void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
 {
   const BoxList L = level_list(h, level, blocks_color);
   const int nb = L.blk[L.count];
   for (int s = 0; s < nu; s++)
-    for (int color = 0; color < num_colors<ORD>(); color++)
-      k_smooth_color<ORD, EQ><<<nb, kSmoothThreads, 0, h->stream>>>(L, h->d_boxes, h->F, color,
-                                                              &h->d_stats->slots[slot], &h->d_stats->nan_flag),
-          h->launches++;
+    for (int color = 0; color < num_colors<ORD>(); color++) {
+      launch_pdl(h, k_smooth_color<ORD, EQ>, (unsigned)nb, (unsigned)kSmoothThreads, L,
+                 (const DevBox *)h->d_boxes, h->F, color, &h->d_stats->slots[slot], &h->d_stats->nan_flag);
+      h->launches++;
+    }
 }
 
 template <int ORD, int EQ>
@@ -696,8 +717,8 @@ void launch_smooth32(olgpu_hierarchy *h, int level, int nu)
   const BoxList L = level_list(h, level, blocks_color);
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
-      k_smooth32<ORD, EQ><<<L.blk[L.count], kSmoothThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, color,
-                                                                       &h->d_stats->nan_flag);
+      launch_pdl(h, k_smooth32<ORD, EQ>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
+                 (const DevBox *)h->d_boxes, h->F32, color, &h->d_stats->nan_flag);
       h->launches_mixed++;
     }
 }
