@@ -72,6 +72,12 @@ struct XferJob {
   int pad_;
   long long rblk0;      // row kernel: first block of this job
   int sstart[3], sstep[3];   // XM_STRIDED: source node of target r0 and its step
+  // periodic linear jobs (lin2 = 1): along each axis the table entries of the
+  // targets r0 + 2m + q are those of r0 + q with window start and node moved
+  // by m; these are the entries of r0 and r0 + 1
+  int lin2;
+  int lstart[3][2], lnode[3][2], lexact[3][2];
+  double lw0[3][2], lw1[3][2];
 };
 
 struct PunctureParams {

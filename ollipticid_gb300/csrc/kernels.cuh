@@ -312,10 +312,10 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
   const long long total = (long long)H * m1 * m2;
   double rabs = 0.0;
   if (t < total) {
-    const int ih = (int)(t % H);
-    const long long r = t / H;
-    const int j = b + (int)(r % m1);
-    const int k = b + (int)(r / m1);
+    const int ih = ((int)t % H);
+    const int r = (int)t / H;
+    const int j = b + (r % m1);
+    const int k = b + (r / m1);
     const int delta = (((color - b - j - k) % NC) + NC) % NC;
     const int i = b + delta + NC * ih;
     if (i < B.n[0] - b) {
@@ -346,10 +346,10 @@ __global__ void __launch_bounds__(256) k_apply_op(BoxList L, const DevBox *__res
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const long long t = lb * blockDim.x + threadIdx.x;
   if (t >= (long long)m0 * m1 * m2) return;
-  const int i = b + (int)(t % m0);
-  const long long r = t / m0;
-  const int j = b + (int)(r % m1);
-  const int k = b + (int)(r / m1);
+  const int i = b + ((int)t % m0);
+  const int r = (int)t / m0;
+  const int j = b + (r % m1);
+  const int k = b + (r / m1);
   const double *u = F.f[F_U] + B.off;
   const long long p = pidx(B, i, j, k);
   const double lv = lap<ORD>(u, p, B.n[0], (long long)B.n[0] * B.n[1], B);
@@ -377,8 +377,8 @@ __global__ void __launch_bounds__(256) k_robin_faces(BoxList L, const DevBox *__
     const long long cols = (long long)m1 * m2;
     if (t < cols) {
       int ijk[3];
-      ijk[a1] = b + (int)(t % m1);
-      ijk[a2] = b + (int)(t / m1);
+      ijk[a1] = b + ((int)t % m1);
+      ijk[a2] = b + (int)t / m1;
       for (int l = 0; l < b; l++) {
         ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
         robin_point<ORD>(B, F, crd, mode, 1 << a, ijk[0], ijk[1], ijk[2]);
@@ -471,9 +471,9 @@ __global__ void __launch_bounds__(256) k_full_weight(BoxList L, const DevBox *__
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
   const int b = B.buf;
-  const int i = (int)(t % B.n[0]);
-  const long long r = t / B.n[0];
-  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
   const double *w = F.f[F_W] + B.off;
   const double c = w[t];
   const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
@@ -569,14 +569,14 @@ __global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, 
     }
     jb = lo;
   }
-  const XferJob J = jobs[jb];
+  const XferJob &J = jobs[jb];
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
+  const int i = J.r0[0] + ((int)t % e0);
+  const int r = (int)t / e0;
+  const int j = J.r0[1] + (r % e1);
+  const int k = J.r0[2] + (r / e1);
   const DevBox T = boxes[J.tbox];
   if (J.iter != IT_ALL) {
     const int b = T.buf;
@@ -655,14 +655,14 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_xfer_rows(const XferJob *__r
     if (jobs[mid].rblk0 <= (long long)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
-  const XferJob J = jobs[lo];
+  const XferJob &J = jobs[lo];
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1];
   const int ra = J.row_axis;
   const long long row = ((long long)blockIdx.x - J.rblk0) * kRowWarps + warp;
   const int across = ra == 0 ? e1 : e0;   // rows per plane
   if (row >= (long long)across * (J.r1[2] - J.r0[2])) return;   // the whole warp leaves together
-  const int k = J.r0[2] + (int)(row / across);
-  const int fixed = (ra == 0 ? J.r0[1] : J.r0[0]) + (int)(row % across);
+  const int k = J.r0[2] + (int)row / across;
+  const int fixed = (ra == 0 ? J.r0[1] : J.r0[0]) + (int)row % across;
   const int len = ra == 0 ? e0 : e1, first = ra == 0 ? J.r0[0] : J.r0[1];
   const DevBox T = boxes[J.tbox], S = boxes[J.sbox];
   V *dst = F.f[J.tfield] + T.off;
@@ -803,14 +803,14 @@ __global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ job
     if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
-  const XferJob J = jobs[lo];
+  const XferJob &J = jobs[lo];
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
+  const int i = J.r0[0] + ((int)t % e0);
+  const int r = (int)t / e0;
+  const int j = J.r0[1] + (r % e1);
+  const int k = J.r0[2] + (r / e1);
   const DevBox &T = boxes[J.tbox];
   if (J.iter != IT_ALL) {
     const int b = T.buf;
@@ -860,34 +860,50 @@ __global__ void __launch_bounds__(256) k_prolong_correct(const XferJob *__restri
     if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
-  const XferJob J = jobs[lo];
+  const XferJob &J = jobs[lo];
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
+  const int i = J.r0[0] + ((int)t % e0);
+  const int r = (int)t / e0;
+  const int j = J.r0[1] + (r % e1);
+  const int k = J.r0[2] + (r / e1);
   const DevBox T = boxes[J.tbox];
   if (J.iter != IT_ALL) {
     const int b = T.buf;
     const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
     if ((J.iter == IT_INSIDE) != inside) return;
   }
-  const AxisEntry &ax = tab[J.tab[0] + i];
-  const AxisEntry &ay = tab[J.tab[1] + j];
-  const AxisEntry &az = tab[J.tab[2] + k];
-  if (!(ax.sel && ay.sel && az.sel)) return;
+  // the axis entries: formed from the job's two per-parity entries on a
+  // periodic job, else read from the tables
+  int sx, sy_, sz_, nx, ny, nz, ex, ey, ez;
+  double wx0, wx1, wy0, wy1, wz0, wz1;
+  if (J.lin2) {
+    const int qi = (i - J.r0[0]) & 1, qj = (j - J.r0[1]) & 1, qk = (k - J.r0[2]) & 1;
+    const int mi = (i - J.r0[0]) >> 1, mj = (j - J.r0[1]) >> 1, mk = (k - J.r0[2]) >> 1;
+    sx = J.lstart[0][qi] + mi, sy_ = J.lstart[1][qj] + mj, sz_ = J.lstart[2][qk] + mk;
+    nx = J.lnode[0][qi] + mi, ny = J.lnode[1][qj] + mj, nz = J.lnode[2][qk] + mk;
+    ex = J.lexact[0][qi], ey = J.lexact[1][qj], ez = J.lexact[2][qk];
+    wx0 = J.lw0[0][qi], wx1 = J.lw1[0][qi], wy0 = J.lw0[1][qj], wy1 = J.lw1[1][qj];
+    wz0 = J.lw0[2][qk], wz1 = J.lw1[2][qk];
+  } else {
+    const AxisEntry &ax = tab[J.tab[0] + i];
+    const AxisEntry &ay = tab[J.tab[1] + j];
+    const AxisEntry &az = tab[J.tab[2] + k];
+    if (!(ax.sel && ay.sel && az.sel)) return;
+    sx = ax.start, sy_ = ay.start, sz_ = az.start, nx = ax.node, ny = ay.node, nz = az.node;
+    ex = ax.exact, ey = ay.exact, ez = az.exact;
+    wx0 = ax.w[0], wx1 = ax.w[1], wy0 = ay.w[0], wy1 = ay.w[1], wz0 = az.w[0], wz1 = az.w[1];
+  }
   const DevBox S = boxes[J.sbox];
   const V *ec = F.f[fe] + S.off, *wc = F.f[fww] + S.off;
   auto v = [&](long long q) -> V { return ec[q] - wc[q]; };
   V vf;
-  if (ax.exact && ay.exact && az.exact) {
-    vf = v(pidx(S, ax.node, ay.node, az.node));
+  if (ex && ey && ez) {
+    vf = v(pidx(S, nx, ny, nz));
   } else {
-    const int i0 = ax.start, j0 = ay.start, k0 = az.start;
-    const V dxi = (V)ax.w[0], dxf = (V)ax.w[1], dyi = (V)ay.w[0], dyf = (V)ay.w[1], dzi = (V)az.w[0],
-            dzf = (V)az.w[1];
+    const int i0 = sx, j0 = sy_, k0 = sz_;
+    const V dxi = (V)wx0, dxf = (V)wx1, dyi = (V)wy0, dyf = (V)wy1, dzi = (V)wz0, dzf = (V)wz1;
     const V v000 = v(pidx(S, i0, j0, k0)), v100 = v(pidx(S, i0 + 1, j0, k0));
     const V v010 = v(pidx(S, i0, j0 + 1, k0)), v110 = v(pidx(S, i0 + 1, j0 + 1, k0));
     const V v001 = v(pidx(S, i0, j0, k0 + 1)), v101 = v(pidx(S, i0 + 1, j0, k0 + 1));
@@ -914,14 +930,14 @@ __global__ void __launch_bounds__(256) k_set_in_op(const XferJob *__restrict__ j
     if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
-  const XferJob J = jobs[lo];
+  const XferJob &J = jobs[lo];
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
+  const int i = J.r0[0] + ((int)t % e0);
+  const int r = (int)t / e0;
+  const int j = J.r0[1] + (r % e1);
+  const int k = J.r0[2] + (r / e1);
   const DevBox T = boxes[J.tbox];
   const DevBox &S = boxes[J.sbox];
   const long long sp = pidx(S, J.sstart[0] + J.sstep[0] * (i - J.r0[0]), J.sstart[1] + J.sstep[1] * (j - J.r0[1]),
@@ -1167,9 +1183,9 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
-  const int i = (int)(t % B.n[0]);
-  const long long r = t / B.n[0];
-  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
   const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
   F.f[F_B][B.off + t] = dev_punctures_b(P, x, y, z);

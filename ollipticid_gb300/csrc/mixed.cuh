@@ -123,9 +123,9 @@ __global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__re
   double rabs = 0.0;
   if (t < n) {
     const int b = B.buf;
-    const int i = (int)(t % B.n[0]);
-    const long long r = t / B.n[0];
-    const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+    const int i = ((int)t % B.n[0]);
+    const int r = (int)t / B.n[0];
+    const int j = (r % B.n[1]), k = (r / B.n[1]);
     const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
     const double *u = F.f[F_U] + B.off;
     double d = F.f[F_RHO][B.off + t];
@@ -172,9 +172,9 @@ __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__rest
     G.f[G_E5][p] = (float)(F.f[F_E][p] * (q4 * q));
   }
   const int b = B.buf;
-  const int i = (int)(t % B.n[0]);
-  const long long r = t / B.n[0];
-  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
   const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
   double d = F.f[F_RHO][p];
   if (inside) {
@@ -209,9 +209,9 @@ __global__ void __launch_bounds__(256) k_mx_robin_defect(BoxList L, const DevBox
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
-  const int i = (int)(t % B.n[0]);
-  const long long r = t / B.n[0];
-  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
   const int ijk[3] = {i, j, k};
   int mask = 0;
   for (int a = 0; a < 3; a++)
@@ -237,9 +237,9 @@ __global__ void __launch_bounds__(256) k_mx_update(BoxList L, const DevBox *__re
     bool pinned = B.level >= mg;
     if (!pinned) {
       const int b = B.buf;
-      const int i = (int)(t % B.n[0]);
-      const long long r = t / B.n[0];
-      const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+      const int i = ((int)t % B.n[0]);
+      const int r = (int)t / B.n[0];
+      const int j = (r % B.n[1]), k = (r / B.n[1]);
       pinned = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
     }
     if (pinned) eabs = fabs(e);
@@ -273,10 +273,10 @@ __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__res
   const int H = (m0 + NC - 1) / NC;
   const long long t = lb * blockDim.x + threadIdx.x;
   if (t >= (long long)H * m1 * m2) return;
-  const int ih = (int)(t % H);
-  const long long r = t / H;
-  const int j = b + (int)(r % m1);
-  const int k = b + (int)(r / m1);
+  const int ih = ((int)t % H);
+  const int r = (int)t / H;
+  const int j = b + (r % m1);
+  const int k = b + (r / m1);
   const int delta = (((color - b - j - k) % NC) + NC) % NC;
   const int i = b + delta + NC * ih;
   if (i >= B.n[0] - b) return;
@@ -301,10 +301,10 @@ __global__ void __launch_bounds__(256) k_apply_op32(BoxList L, const DevBox *__r
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const long long t = lb * blockDim.x + threadIdx.x;
   if (t >= (long long)m0 * m1 * m2) return;
-  const int i = b + (int)(t % m0);
-  const long long r = t / m0;
-  const int j = b + (int)(r % m1);
-  const int k = b + (int)(r / m1);
+  const int i = b + ((int)t % m0);
+  const int r = (int)t / m0;
+  const int j = b + (r % m1);
+  const int k = b + (r / m1);
   const long long p = pidx(B, i, j, k);
   const float lv = lapf<ORD>(G.f[G_E] + B.off, p, B.n[0], (long long)B.n[0] * B.n[1], B);
   float op, dop;
@@ -388,8 +388,8 @@ __global__ void __launch_bounds__(256) k_robin32_faces(BoxList L, const DevBox *
     const long long cols = (long long)m1 * m2;
     if (t < cols) {
       int ijk[3];
-      ijk[a1] = b + (int)(t % m1);
-      ijk[a2] = b + (int)(t / m1);
+      ijk[a1] = b + ((int)t % m1);
+      ijk[a2] = b + (int)t / m1;
       for (int l = 0; l < b; l++) {
         ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
         robin32_point<ORD>(B, G, crd, mode, 1 << a, ijk[0], ijk[1], ijk[2]);
@@ -479,9 +479,9 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
   const int b = B.buf;
-  const int i = (int)(t % B.n[0]);
-  const long long r = t / B.n[0];
-  const int j = (int)(r % B.n[1]), k = (int)(r / B.n[1]);
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
   const float *gs = G.f[G_S] + B.off, *gr = G.f[G_R] + B.off;
   auto w = [&](long long q) { return gs[q] - gr[q]; };
   const float c = w(t);
@@ -517,14 +517,14 @@ __global__ void __launch_bounds__(256) k_set_in_op32(const XferJob *__restrict__
     if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
-  const XferJob J = jobs[lo];
+  const XferJob &J = jobs[lo];
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + (int)(t % e0);
-  const long long r = t / e0;
-  const int j = J.r0[1] + (int)(r % e1);
-  const int k = J.r0[2] + (int)(r / e1);
+  const int i = J.r0[0] + ((int)t % e0);
+  const int r = (int)t / e0;
+  const int j = J.r0[1] + (r % e1);
+  const int k = J.r0[2] + (r / e1);
   const DevBox T = boxes[J.tbox];
   const DevBox &S = boxes[J.sbox];
   const long long sp = pidx(S, J.sstart[0] + J.sstep[0] * (i - J.r0[0]), J.sstart[1] + J.sstep[1] * (j - J.r0[1]),

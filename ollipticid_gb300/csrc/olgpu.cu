@@ -302,6 +302,37 @@ void stride_jobs(const olgpu_hierarchy *h, Transfer &X)
   }
 }
 
+// Marks the linear jobs of X whose axis tables repeat with period two (2:1
+// prolongation): every target selected and, along each axis, the entry of
+// r0 + 2m + q equal to that of r0 + q with start and node moved by m.  The
+// prolong-and-correct kernel then forms the entries instead of loading them.
+void periodic_linear_jobs(const olgpu_hierarchy *h, Transfer &X)
+{
+  for (XferJob &J : X.jobs) {
+    if (J.method != XM_LINEAR) continue;
+    bool ok = true;
+    for (int a = 0; a < 3 && ok; a++) {
+      const AxisEntry *e = h->htab.data() + J.tab[a];
+      const int r0 = J.r0[a], r1 = J.r1[a];
+      for (int q = 0; q < 2; q++) {
+        const AxisEntry &b = e[std::min(r0 + q, r1 - 1)];
+        J.lstart[a][q] = b.start;
+        J.lnode[a][q] = b.node;
+        J.lexact[a][q] = b.exact;
+        J.lw0[a][q] = b.w[0];
+        J.lw1[a][q] = b.w[1];
+      }
+      for (int t = r0; t < r1 && ok; t++) {
+        const int q = (t - r0) & 1, m = (t - r0) >> 1;
+        const AxisEntry &b = e[r0 + q];
+        ok = e[t].sel && e[t].exact == b.exact && e[t].start == b.start + m && e[t].node == b.node + m &&
+             e[t].w[0] == b.w[0] && e[t].w[1] == b.w[1];
+      }
+    }
+    J.lin2 = ok ? 1 : 0;
+  }
+}
+
 // Transferir(from, sfield, to, tfield, iter, method, ord, all, to_zero):
 // every (source box, target box) pair of the two levels.
 Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfield, int iter, int method, int ord,
@@ -335,7 +366,10 @@ Transfer make_transfer(olgpu_hierarchy *h, int from, int sfield, int to, int tfi
       }
       add_region_jobs(X, J, T, lo, hi);
     }
-  if (!std::getenv("OLGPU_XFER_POINTS")) stride_jobs(h, X);
+  if (!std::getenv("OLGPU_XFER_POINTS")) {
+    stride_jobs(h, X);
+    periodic_linear_jobs(h, X);
+  }
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
   X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
   X.strided = !X.jobs.empty() && std::all_of(X.jobs.begin(), X.jobs.end(),
@@ -374,7 +408,10 @@ Transfer make_set_in(olgpu_hierarchy *h, int k)
       add_region_jobs(X, J, C, lo, hi);
     }
   }
-  if (!std::getenv("OLGPU_XFER_POINTS")) stride_jobs(h, X);
+  if (!std::getenv("OLGPU_XFER_POINTS")) {
+    stride_jobs(h, X);
+    periodic_linear_jobs(h, X);
+  }
   X.width = xfer_width(X.jobs.data(), X.jobs.size());
   X.rows = xfer_rows(X.jobs.data(), X.jobs.size(), X.width) && !std::getenv("OLGPU_XFER_POINTS");
   X.strided = !X.jobs.empty() && std::all_of(X.jobs.begin(), X.jobs.end(),
