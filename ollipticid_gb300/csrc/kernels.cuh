@@ -180,19 +180,22 @@ __device__ __forceinline__ double deriv(const double *__restrict__ u, long long 
 
 // Robin term r^2/n * sum_a (du/dx_a)/x_a for the axes in mask (n = 1), grouped
 // like Boundary_Face (one axis) and Boundary_Edge/Corner (two/three axes).
+// A box's coordinate table holds x, y, z and then 1/x, 1/y, 1/z: the
+// divisions by the coordinate are products with its reciprocal (within an
+// ulp of the quotient; an FP64 division costs GB300 about ten FP64
+// instructions).
 template <int ORD>
 __device__ __forceinline__ double robin_term(const double *__restrict__ u, const DevBox &B,
                                              const double *__restrict__ crd, int mask, int i, int j,
                                              int k, double &dF)
 {
-  const double x = crd[B.coord_off + i];
-  const double y = crd[B.coord_off + B.n[0] + j];
-  const double z = crd[B.coord_off + B.n[0] + B.n[1] + k];
+  const double *c = crd + B.coord_off, *ic = c + (B.n[0] + B.n[1] + B.n[2]);
+  const double x = c[i], y = c[B.n[0] + j], z = c[B.n[0] + B.n[1] + k];
   const double r2 = x * x + y * y + z * z;
   const long long p = pidx(B, i, j, k);
   const long long st[3] = {1, (long long)B.n[0], (long long)B.n[0] * B.n[1]};
   const int ijk[3] = {i, j, k};
-  const double xyz[3] = {x, y, z};
+  const double ixyz[3] = {ic[i], ic[B.n[0] + j], ic[B.n[0] + B.n[1] + k]};
   double t = 0.0, dt = 0.0;
   int na = 0;
 #pragma unroll
@@ -201,11 +204,11 @@ __device__ __forceinline__ double robin_term(const double *__restrict__ u, const
     double du;
     const double dv = deriv<ORD>(u, p, st[a], ijk[a], B.n[a], B.idx[a], du);
     if (na == 0 && mask == (1 << a)) {          // face
-      dF = r2 * du / xyz[a] + 1.0;
-      return r2 * dv / xyz[a];
+      dF = r2 * du * ixyz[a] + 1.0;
+      return r2 * dv * ixyz[a];
     }
-    t = na == 0 ? dv / xyz[a] : t + dv / xyz[a];
-    dt = na == 0 ? du / xyz[a] : dt + du / xyz[a];
+    t = na == 0 ? dv * ixyz[a] : t + dv * ixyz[a];
+    dt = na == 0 ? du * ixyz[a] : dt + du * ixyz[a];
     na++;
   }
   dF = r2 * dt + 1.0;
@@ -223,9 +226,9 @@ __device__ __forceinline__ void robin_point(const DevBox &B, const DevFields &F,
   const long long p = pidx(B, i, j, k);
   double dF;
   const double t = robin_term<ORD>(u, B, crd, mask, i, j, k, dF);
-  if (mode == 0) {
+  if (mode == 0) {   // the step's divisor only sizes the step: F = 0 stays the solution
     const double Fv = t + u[p] - F.f[F_RHO][B.off + p];
-    u[p] = u[p] - Fv / dF;
+    u[p] = u[p] - Fv * rcp_approx64(dF);
   } else {
     F.f[F_R][B.off + p] = t + u[p];
   }
@@ -971,7 +974,7 @@ __device__ __forceinline__ void cs_robin_point(const DevBox &B, double *u, const
   double dF;
   const double t = robin_term<2>(u, B, crd, mask, i, j, k, dF);
   const double Fv = t + u[p] - rho[p];
-  u[p] = u[p] - Fv / dF;
+  u[p] = u[p] - Fv * rcp_approx64(dF);   // the divisor only sizes the step
 }
 
 template <int EQ>

@@ -348,26 +348,27 @@ __device__ __forceinline__ void robin32_point(const DevBox &B, const DevFields32
                                               int mode, int mask, int i, int j, int k)
 {
   float *e = G.f[G_E] + B.off;
-  const float x = (float)crd[B.coord_off + i];
-  const float y = (float)crd[B.coord_off + B.n[0] + j];
-  const float z = (float)crd[B.coord_off + B.n[0] + B.n[1] + k];
+  const double *c = crd + B.coord_off, *ic = c + (B.n[0] + B.n[1] + B.n[2]);   // coordinates, reciprocals
+  const float x = (float)c[i];
+  const float y = (float)c[B.n[0] + j];
+  const float z = (float)c[B.n[0] + B.n[1] + k];
   const float r2 = x * x + y * y + z * z;
   const long long p = pidx(B, i, j, k);
   const long long st[3] = {1, (long long)B.n[0], (long long)B.n[0] * B.n[1]};
   const int ijk[3] = {i, j, k};
-  const float xyz[3] = {x, y, z};
+  const float ixyz[3] = {(float)ic[i], (float)ic[B.n[0] + j], (float)ic[B.n[0] + B.n[1] + k]};
   float t = 0.0f, dt = 0.0f;
 #pragma unroll
   for (int a = 0; a < 3; a++) {
     if (!(mask & (1 << a))) continue;
     float du;
     const float dv = derivf<ORD>(e, p, st[a], ijk[a], B.n[a], (float)B.idx[a], du);
-    t += dv / xyz[a];
-    dt += du / xyz[a];
+    t += dv * ixyz[a];
+    dt += du * ixyz[a];
   }
   if (mode == 0) {
     const float Fv = r2 * t + e[p] - G.f[G_S][B.off + p];
-    e[p] = e[p] - Fv / (r2 * dt + 1.0f);
+    e[p] = e[p] - Fv * rcp_fast(r2 * dt + 1.0f);
   } else {
     G.f[G_R][B.off + p] = r2 * t + e[p];
   }

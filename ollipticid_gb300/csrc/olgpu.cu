@@ -1330,9 +1330,16 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     case 6: B.dulap = -490 * s * (1.0 / 180); break;
     default: B.dulap = -205 * s / 72.0; break;
     }
+    // x, y, z of the box's nodes, then their reciprocals (ghost nodes lie on
+    // the outer faces; a node at 0 gets 0, it is never a Robin point)
     for (int a = 0; a < 3; a++)
       for (int i = 0; i < D.n[a]; i++) h->hcoords.push_back(D.coord(a, i));
-    coff += D.n[0] + D.n[1] + D.n[2];
+    for (int a = 0; a < 3; a++)
+      for (int i = 0; i < D.n[a]; i++) {
+        const double x = D.coord(a, i);
+        h->hcoords.push_back(x != 0.0 ? 1.0 / x : 0.0);
+      }
+    coff += 2 * (D.n[0] + D.n[1] + D.n[2]);
     off += D.npts();
     h->hboxes.push_back(B);
   }
