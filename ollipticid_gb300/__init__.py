@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
-from typing import List, Sequence
+from typing import Optional, List, Sequence
 
 import numpy as np
 
@@ -175,9 +175,14 @@ class Elliptic:
         return [g for g, b in enumerate(self.boxes) if b.level == level][ibox]
 
     # -- fields -------------------------------------------------------------
-    def get_field(self, box: int, name: str = "u") -> np.ndarray:
+    def get_field(self, box: int, name: str = "u", out: Optional[np.ndarray] = None) -> np.ndarray:
+        """A box's field as a (nz, ny, nx) array; `out` (C-contiguous float64
+        of that shape, e.g. in pinned memory) receives it if given."""
         nx, ny, nz = self.boxes[box].n
-        out = np.empty((nz, ny, nx), dtype=np.float64)
+        if out is None:
+            out = np.empty((nz, ny, nx), dtype=np.float64)
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.size != nx * ny * nz:
+            raise ValueError("out must be a C-contiguous float64 array of the box's size")
         check(self.lib.olgpu_download(self._h, box, name.encode(), out.ctypes.data_as(C.c_void_p)))
         return out
 
