@@ -85,28 +85,9 @@ __device__ __forceinline__ void corr_op(float lapv, float dl, float e, float A, 
 }
 
 // ---------------------------------------------------------------------------
-// FP64 preparation: coefficients of the correction operator on ALL points
+// FP64 preparation (coefficients and defect: k_mx_prep below) and the FP64
+// defect of the finest level after the update (the cycle's norm)
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_mx_coeffs(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                   DevFields32 G, int eq)
-{
-  long long lb;
-  const DevBox B = boxes[list_box(L, lb)];
-  const long long t = lb * blockDim.x + threadIdx.x;
-  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
-  if (t >= n) return;
-  const long long p = B.off + t;
-  const double q = F.f[F_C][p] + F.f[F_U][p];
-  const double iq = rcp_newton(q);
-  const double iq2 = iq * iq, iq4 = iq2 * iq2;
-  G.f[G_A][p] = (float)(F.f[F_B][p] * (iq4 * iq2 * iq));
-  G.f[G_IQ][p] = (float)iq;
-  if (eq == 1) {
-    const double q2 = q * q;
-    G.f[G_D][p] = (float)F.f[F_D][p];
-    G.f[G_E5][p] = (float)(F.f[F_E][p] * (q2 * q2 * q));
-  }
-}
 
 // FP64 defect S - OP(u) on INSIDE points into the FP32 source; the other
 // points get S (the operator value there is written by the Robin kernels in
