@@ -481,7 +481,7 @@ def run_gpu(args, rank: int, world: int, local: int):
         concurrent = run_concurrent(E, P, u_fix, adm_fix, value / world)
         batched = run_batched(args, tuned=autotune.tune(P, concurrency=16))
         config3 = run_config3()
-        served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]) + (concurrent["smoother_blocks"],))
+        served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
     # multicolour smoother (k_smooth_color) on the finest level, timed with

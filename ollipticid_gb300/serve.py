@@ -80,22 +80,28 @@ class _Track:
 class Server:
     def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
                  tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
-                 inner_sweeps: Optional[Tuple[int, ...]] = None):
+                 inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4):
         """inner_sweeps: (nu1, nu2[, smoother cluster blocks]) of every mixed
         solve's FP32 cycle (for example an autotune choice); None keeps each
-        problem's own nu1/nu2 and the default smoother layout."""
+        problem's own nu1/nu2 and the default smoother layout.  Without a
+        layout in inner_sweeps the layout follows the load when a request is
+        admitted: per-colour launches while fewer than `busy` solves are on
+        the GPU (a solve alone is bound by its chain of launches), the
+        cluster-resident smoother beyond (it holds fewer SMs per solve).  The
+        two layouts give the same result bit for bit."""
         self.device, self.mem_budget, self.max_active = device, mem_budget, max_active
         self.mixed, self.tol, self.max_cycles, self.keep_u = mixed, tol, max_cycles, keep_u
-        self.inner_sweeps = inner_sweeps
+        self.inner_sweeps, self.busy = inner_sweeps, busy
         self.pool = ThreadPoolExecutor(max_workers=builders)
 
-    def _build(self, problem: Problem) -> Elliptic:
+    def _build(self, problem: Problem, blocks: int) -> Elliptic:
         E = Elliptic(problem, device=self.device)
+        if self.mixed:
+            # the schedule first: set before the mixed cycle is captured, once
+            E.set_smoother_blocks(blocks)
+            if self.inner_sweeps:
+                E.set_inner_sweeps(*self.inner_sweeps[:2])
         E.set_precision(self.mixed)
-        if self.mixed and self.inner_sweeps:
-            if len(self.inner_sweeps) > 2:
-                E.set_smoother_blocks(self.inner_sweeps[2])
-            E.set_inner_sweeps(*self.inner_sweeps[:2])
         return E
 
     def run(self, stream: Sequence[Tuple[float, Problem]]) -> dict:
@@ -126,7 +132,11 @@ class Server:
                 rid, arr, prob, nbytes = waiting.popleft()
                 used += nbytes
                 results[rid].admitted = now()
-                building.append((self.pool.submit(self._build, prob), rid, prob, nbytes))
+                if self.inner_sweeps and len(self.inner_sweeps) > 2:
+                    blocks = self.inner_sweeps[2]
+                else:
+                    blocks = 0 if len(active) + len(building) < self.busy else 16
+                building.append((self.pool.submit(self._build, prob, blocks), rid, prob, nbytes))
             for item in list(building):
                 fut, rid, prob, nbytes = item
                 if fut.done():
