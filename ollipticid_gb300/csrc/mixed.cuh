@@ -123,10 +123,11 @@ __global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__re
   if (norm_slot) block_max_atomic(rabs, norm_slot);
 }
 
-// The FP64 preparation of one level in one pass: on ALL points the
+// The FP64 preparation of one level in one pass: on INSIDE points the
 // coefficients of the correction operator, A = b/(c+u)^7 and 1/(c+u) (and d,
-// E5 = e (c+u)^5 for the scalar field), and the source S32 = S - OP(u) on
-// INSIDE points, S elsewhere (as k_mx_defect), sharing 1/(c+u) between them.
+// E5 = e (c+u)^5 for the scalar field; nothing reads them on the ghosts) and
+// the source S32 = S - OP(u), sharing 1/(c+u); S on the other points (as
+// k_mx_defect).
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
                                                  DevFields32 G)
@@ -137,6 +138,15 @@ __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__rest
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
   const long long p = B.off + t;
+  const int b = B.buf;
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
+  const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
+  if (!inside) {   // the FP32 cycle reads the coefficients on INSIDE points only
+    G.f[G_S][p] = (float)F.f[F_RHO][p];
+    return;
+  }
   const double *u = F.f[F_U] + B.off;
   const double uu = u[t], bb = F.f[F_B][p];
   const double q = F.f[F_C][p] + uu;
@@ -152,19 +162,10 @@ __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__rest
     G.f[G_D][p] = (float)F.f[F_D][p];
     G.f[G_E5][p] = (float)(F.f[F_E][p] * (q4 * q));
   }
-  const int b = B.buf;
-  const int i = ((int)t % B.n[0]);
-  const int r = (int)t / B.n[0];
-  const int j = (r % B.n[1]), k = (r / B.n[1]);
-  const bool inside = i >= b && i < B.n[0] - b && j >= b && j < B.n[1] - b && k >= b && k < B.n[2] - b;
-  double d = F.f[F_RHO][p];
-  if (inside) {
-    const double lv = lap<ORD>(u, t, B.n[0], (long long)B.n[0] * B.n[1], B);
-    double op = lv + t7;
-    if (EQ == 1) op = op + F.f[F_D][p] * q + F.f[F_E][p] * (q4 * q);
-    d = d - op;
-  }
-  G.f[G_S][p] = (float)d;
+  const double lv = lap<ORD>(u, t, B.n[0], (long long)B.n[0] * B.n[1], B);
+  double op = lv + t7;
+  if (EQ == 1) op = op + F.f[F_D][p] * q + F.f[F_E][p] * (q4 * q);
+  G.f[G_S][p] = (float)(F.f[F_RHO][p] - op);
 }
 
 // Robin defect on the physical boundary: S32 = S - (term(u) + u) (FP64).
