@@ -543,10 +543,16 @@ def main():
     ap.add_argument("--profile-cycle", action="store_true",
                     help="run two V-cycles of the workload and exit (for the ncu launch list)")
     ap.add_argument("--mixed", action="store_true", help="with --profile-cycle: the mixed-precision cycle")
+    ap.add_argument("--inner", default=None,
+                    help="with --profile-cycle --mixed: inner schedule nu1,nu2,blocks (e.g. 4,6,16)")
     args = ap.parse_args()
     if args.profile_cycle:
         import ollipticid_gb300 as og
         E = og.Elliptic(og.parse_olliptic_args(WORKLOAD_ARGS.split()))
+        if args.inner:
+            nu1, nu2, blocks = (int(v) for v in args.inner.split(","))
+            E.set_inner_sweeps(nu1, nu2)
+            E.set_smoother_blocks(blocks)
         E.set_precision(args.mixed)
         r = [E.FASN() for _ in range(2)]
         print(json.dumps({"profile_cycles": 2, "res": r, "kernels_per_cycle": E.kernels_per_cycle}))
