@@ -72,6 +72,7 @@ typedef struct {
   double xi, yi, zi;            /* coordinate of point (0,0,0)            */
   double dx, dy, dz;
   double cx, cy, cz;            /* box centre                             */
+  double xf, yf, zf;            /* coordinate of the last point (domain xf) */
 } olgpu_box_info;
 
 /* Stop rules for olgpu_solve. */
@@ -128,6 +129,32 @@ olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res);
 /* Repeated V-cycles under a stop rule; rule NULL = the reference's rule. */
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out);
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
+
+/* Smoother norms of one cycle of the current solve (0 = its first cycle;
+ * olgpu_solve / olgpu_solve_many start a new history): pre[l] and post[l],
+ * l = 0 .. olgpu_num_levels - 1, the L-infinity norms the smoother of level
+ * l reported before and after the cycle's correction (the reference's
+ * "Loo[l]" lines, elliptic::Print_Pre_Cycle / Print_Post_Cycle,
+ * src/output.cc:1355-1605); level 0
+ * holds the coarsest solve's norm.  In mixed precision they are the norms
+ * of the FP32 correction cycle. */
+olgpu_status olgpu_level_norms(const olgpu_hierarchy *h, int cycle, double *pre, double *post);
+
+/* u at arbitrary points, as the reference prints and exports it
+ * (multigrid::Print_Interpol_1D / _2D, src/multigrid.cc:151-261 and 555-880;
+ * ffunction::Print_1D, src/ffunction.cc:819-960; the Lagrange sum of
+ * ffunction::Lagrange_Interpol_In, src/interpolation.cc:188-375).
+ * box < 0: each point is read from the last box, in level order, whose
+ * interior (no ghost layers) holds it, from the largest box when none does,
+ * and is NaN outside the largest box (the reference prints no line there);
+ * box >= 0: every point is read from that box.  The value is the node value
+ * where the point coincides with a node, else the Lagrange sum over ord+1
+ * nodes per axis (the reference prints with ord = order + 1), window clamped
+ * to the box.  xyz holds npts (x, y, z) triples and out npts values, both
+ * host memory; the gather runs on the device, ordered after the cycles
+ * already enqueued. */
+olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, long long npts, int ord,
+                               double *out);
 
 /* Asynchronous stepping, for hosts that drive several solves at once (each
  * hierarchy has its own CUDA stream, so cycles of different hierarchies run

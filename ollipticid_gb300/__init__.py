@@ -245,6 +245,28 @@ class Elliptic:
         check(self.lib.olgpu_adm_mass(self._h, out))
         return [out[i] for i in range(self.problem.numbh)]
 
+    def level_norms(self, cycle: int):
+        """(pre, post) smoother norms per level of one cycle of the last solve
+        (the reference's Loo[l] lines; level 0: the coarsest solve)."""
+        pre = np.empty(self.levels, dtype=np.float64)
+        post = np.empty(self.levels, dtype=np.float64)
+        check(self.lib.olgpu_level_norms(self._h, int(cycle), pre.ctypes.data_as(C.POINTER(C.c_double)),
+                                         post.ctypes.data_as(C.POINTER(C.c_double))))
+        return pre, post
+
+    def interpolate(self, points, ord: Optional[int] = None, box: int = -1) -> np.ndarray:
+        """u at (npts, 3) points, as the reference prints it (Print_Interpol_1D
+        / _2D with box=-1: the finest box whose interior holds each point, NaN
+        outside the largest box; ffunction::Print_1D with box >= 0).  ord+1
+        Lagrange nodes per axis, default order + 1 like the reference's
+        printout."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        out = np.empty(len(pts), dtype=np.float64)
+        k = self.problem.order + 1 if ord is None else int(ord)
+        check(self.lib.olgpu_interpolate(self._h, int(box), pts.ctypes.data_as(C.c_void_p), len(pts), k,
+                                         out.ctypes.data_as(C.c_void_p)))
+        return out
+
     @property
     def last_device_ms(self) -> float:
         return self.lib.olgpu_last_device_ms(self._h)

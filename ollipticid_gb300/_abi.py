@@ -33,6 +33,7 @@ class BoxInfo(C.Structure):
         ("xi", C.c_double), ("yi", C.c_double), ("zi", C.c_double),
         ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
         ("cx", C.c_double), ("cy", C.c_double), ("cz", C.c_double),
+        ("xf", C.c_double), ("yf", C.c_double), ("zf", C.c_double),
     ]
 
 
@@ -74,6 +75,8 @@ SIGNATURES = {
     "olgpu_vcycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(StopRule), C.POINTER(Report)]),
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "olgpu_level_norms": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "olgpu_interpolate": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
     "olgpu_cycle_launch": (C.c_int, [C.c_void_p]),
     "olgpu_cycle_poll": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "olgpu_solve_many": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(StopRule), C.POINTER(Report)]),

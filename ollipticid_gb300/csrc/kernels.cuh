@@ -24,6 +24,8 @@
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
+#include <cfloat>
+
 namespace olgpu {
 
 __device__ __forceinline__ long long pidx(const DevBox &B, int i, int j, int k)
@@ -1231,6 +1233,145 @@ __global__ void k_adm(const AdmJob *__restrict__ jobs, int n, const DevBox *__re
       uy += uz * J.w[1][Jj];
     }
     fx += uy * J.w[0][I];
+  }
+  out[q] = fx;
+}
+
+// ----------------------------------------------------------------------------
+// u at arbitrary points: the reference's printed cuts and exports.
+// multigrid::Print_Interpol_1D / _2D (src/multigrid.cc:151-261, 555-880) read
+// each point from the last box, in level order, whose interior holds it
+// (domain::is_in_nb, include/domain.h:839-850), the largest box when none
+// does, and print nothing for a point outside the largest box (domain::is_in);
+// ffunction::Print_1D (src/ffunction.cc:819-960) reads one given box.  The
+// value is ffunction::Lagrange_Interpol_In (src/interpolation.cc:188-375):
+// the node value where the point coincides with a node on every axis (the
+// 3-epsilon test), else the tensor Lagrange sum over ord+1 nodes per axis,
+// the window clamped to the box, summed over z, then y, then x.  Every
+// product, quotient and sum is rounded on its own (no fused multiply-add), in
+// the reference's order, so the result is the host's bit for bit.
+// ----------------------------------------------------------------------------
+struct InterpBox {
+  double lo[3], hi[3], d[3];
+  int n[3];
+  int buf;
+  long long off;
+};
+
+constexpr int kMaxInterpOrd = 15;
+
+__device__ __forceinline__ double ib_coord(const InterpBox &B, int a, int i)
+{
+  return __dadd_rn(B.lo[a], __dmul_rn((double)i, B.d[a]));   // domain::Get_x: xi + i dx
+}
+
+__device__ __forceinline__ bool ib_dcomp(double x, double y) { return fabs(__dsub_rn(x, y)) <= 3 * DBL_EPSILON; }
+
+// domain::Get_i: the first node at or after x (binary search)
+__device__ int ib_locate(const InterpBox &B, int a, double x)
+{
+  const int np = B.n[a];
+  int lo_i = 0, hi_i = np, i;
+  if (__dsub_rn(B.lo[a], x) < 0.0 && __dsub_rn(x, B.hi[a]) < 0.0) {
+    i = np % 2 == 0 ? np / 2 : (np - 1) / 2;
+    do {
+      const double xi = ib_coord(B, a, i);
+      if (xi > x || ib_dcomp(xi, x))
+        hi_i = i;
+      else
+        lo_i = i;
+      i = (hi_i + lo_i) / 2;
+    } while (lo_i + 1 < hi_i);
+  } else {
+    i = (B.lo[a] >= x) ? 0 : np - 2;
+  }
+  return i + 1;
+}
+
+__device__ __forceinline__ bool ib_is_in(const InterpBox &B, const double p[3])
+{
+  for (int a = 0; a < 3; a++) {
+    const double m = __dmul_rn(B.d[a], 0.1);
+    if (!(__dsub_rn(B.lo[a], m) <= p[a] && p[a] <= __dadd_rn(B.hi[a], m))) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ bool ib_is_in_nb(const InterpBox &B, const double p[3])
+{
+  for (int a = 0; a < 3; a++) {
+    const double m = __dmul_rn(B.d[a], __dsub_rn((double)B.buf, 0.1));
+    if (!(__dadd_rn(B.lo[a], m) < p[a] && p[a] < __dsub_rn(B.hi[a], m))) return false;
+  }
+  return true;
+}
+
+// LagrangePoly (src/interpolation.cc:308-375)
+__device__ double ib_lagrange(const InterpBox &B, int a, double t, int i, int ni, int nf)
+{
+  double lp = 1.0;
+  const double ti = ib_coord(B, a, i);
+  for (int j = ni; j < i; j++) {
+    const double cj = ib_coord(B, a, j);
+    lp = __dmul_rn(lp, __ddiv_rn(__dsub_rn(t, cj), __dsub_rn(ti, cj)));
+  }
+  for (int j = i + 1; j <= nf; j++) {
+    const double cj = ib_coord(B, a, j);
+    lp = __dmul_rn(lp, __ddiv_rn(__dsub_rn(t, cj), __dsub_rn(ti, cj)));
+  }
+  return lp;
+}
+
+// One thread per point.  box >= 0: that box; box < 0: the printed-cut rule
+// with `base` the largest box (NaN outside it).
+__global__ void __launch_bounds__(128) k_interp_points(const InterpBox *__restrict__ boxes, int nboxes, int base,
+                                                       int box, const double *__restrict__ u,
+                                                       const double *__restrict__ xyz, long long npts, int ord,
+                                                       double *__restrict__ out)
+{
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= npts) return;
+  const double p[3] = {xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]};
+  int g = box;
+  if (g < 0) {
+    if (!ib_is_in(boxes[base], p)) {
+      out[q] = __longlong_as_double(0x7ff8000000000000LL);
+      return;
+    }
+    g = base;
+    for (int b = 0; b < nboxes; b++)
+      if (ib_is_in_nb(boxes[b], p)) g = b;
+  }
+  const InterpBox B = boxes[g];
+  const double *f = u + B.off;
+  const long long sy = B.n[0], sz = (long long)B.n[0] * B.n[1];
+  int node[3], st[3];
+  bool exact = true;
+  for (int a = 0; a < 3; a++) {
+    node[a] = ib_locate(B, a, p[a]);
+    exact = exact && node[a] < B.n[a] && ib_dcomp(p[a], ib_coord(B, a, node[a]));
+    int s = ord % 2 == 0 ? node[a] - ord / 2 : node[a] - (ord + 1) / 2;
+    if (s < 0) s = 0;
+    else if (s + ord >= B.n[a]) s = B.n[a] - ord - 1;
+    st[a] = s;
+  }
+  if (exact) {
+    out[q] = f[node[0] + node[1] * sy + node[2] * sz];
+    return;
+  }
+  double wy[kMaxInterpOrd + 1], wz[kMaxInterpOrd + 1];
+  for (int J = 0; J <= ord; J++) wy[J] = ib_lagrange(B, 1, p[1], st[1] + J, st[1], st[1] + ord);
+  for (int K = 0; K <= ord; K++) wz[K] = ib_lagrange(B, 2, p[2], st[2] + K, st[2], st[2] + ord);
+  double fx = 0.0;
+  for (int I = 0; I <= ord; I++) {
+    double uy = 0.0;
+    for (int J = 0; J <= ord; J++) {
+      const double *col = f + (st[0] + I) + (st[1] + J) * sy + st[2] * sz;
+      double uz = 0.0;
+      for (int K = 0; K <= ord; K++) uz = __dadd_rn(uz, __dmul_rn(col[K * sz], wz[K]));
+      uy = __dadd_rn(uy, __dmul_rn(uz, wy[J]));
+    }
+    fx = __dadd_rn(fx, __dmul_rn(uy, ib_lagrange(B, 0, p[0], st[0] + I, st[0], st[0] + ord)));
   }
   out[q] = fx;
 }

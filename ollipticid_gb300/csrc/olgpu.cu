@@ -116,6 +116,10 @@ struct olgpu_hierarchy {
   cudaGraphExec_t graph_mixed = nullptr;
   int launches_mixed = 0;
   double last_defect = 0, last_correction = 0;   // parts of the last mixed cycle's norm
+  // smoother norms of every cycle since the solve began: per cycle, levels
+  // pre-smoothing norms then levels post-smoothing norms (level 0: the
+  // coarsest solve's)
+  std::vector<double> norm_hist;
   // Anderson acceleration of the mixed outer iteration
   int anderson_m = kAndDefault;
   float *d_and = nullptr;               // DU[m], DF[m], fprev (FP32, total_pts each)
@@ -1249,6 +1253,9 @@ static void fill_box_info(const domain &D, olgpu_box_info *o)
   o->cx = D.c[0];
   o->cy = D.c[1];
   o->cz = D.c[2];
+  o->xf = D.hi[0];
+  o->yf = D.hi[1];
+  o->zf = D.hi[2];
 }
 
 olgpu_status olgpu_plan_boxes(const olgpu_problem *p, olgpu_box_info *out, int cap, int *nboxes, int *nlevels,
@@ -1578,6 +1585,12 @@ static olgpu_status cycle_finish(olgpu_hierarchy *h, double *res)
     h->last_correction = corr;
     if (corr > *res) *res = corr;
   }
+  for (int post = 0; post < 2; post++)
+    for (int l = 0; l <= top; l++) {
+      double v = h->h_stats->coarse_norm;
+      if (l > 0) std::memcpy(&v, &h->h_stats->slots[2 * l + post], sizeof(double));
+      h->norm_hist.push_back(v);
+    }
   const olgpu_problem &P = h->P;
   for (int i = 0; i < P.numbh; i++) {
     double bhmj = 0;
@@ -1643,6 +1656,7 @@ static olgpu_status make_track(olgpu_hierarchy *h, const olgpu_stop_rule *rule, 
   if (rule) T.R = *rule;
   if (T.R.max_cycles <= 0) return fail(OLGPU_ERR_INVALID_ARG, "max_cycles must be > 0");
   T.tol = T.R.tol > 0 ? T.R.tol : h->eps_solv;
+  h->norm_hist.clear();
   return OLGPU_OK;
 }
 
@@ -1745,6 +1759,87 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
 {
   if (!h || !out) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
   for (int i = 0; i < h->P.numbh; i++) out[i] = h->adm[i];
+  return OLGPU_OK;
+}
+
+// u at arbitrary points (the printed cuts and exports; k_interp_points).
+olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, long long npts, int ord,
+                               double *out)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (npts < 0 || (npts > 0 && (!xyz || !out))) return fail(OLGPU_ERR_INVALID_ARG, "null or negative point array");
+  if (ord < 1 || ord > kMaxInterpOrd) return fail(OLGPU_ERR_INVALID_ARG, "interpolation order must be 1..15");
+  const int nb = (int)h->G.boxes.size();
+  if (box >= nb) return fail(OLGPU_ERR_INVALID_ARG, "box index out of range");
+  if (npts == 0) return OLGPU_OK;
+  if (npts > 128LL * 0x7fffffffLL) return fail(OLGPU_ERR_INVALID_ARG, "too many points for one call");
+  if (box >= 0) {
+    for (int a = 0; a < 3; a++)
+      if (h->G.boxes[box].n[a] < ord + 1) return fail(OLGPU_ERR_INVALID_ARG, "box smaller than the window");
+  } else {
+    for (const domain &D : h->G.boxes)
+      for (int a = 0; a < 3; a++)
+        if (D.n[a] < ord + 1) return fail(OLGPU_ERR_INVALID_ARG, "a box is smaller than the window");
+  }
+  std::vector<InterpBox> ib(nb);
+  int base = 0;   // multigrid::multigrid: the box that strictly holds every box scanned before it
+  for (int g = 0; g < nb; g++) {
+    const domain &D = h->G.boxes[g];
+    InterpBox &B = ib[g];
+    for (int a = 0; a < 3; a++) {
+      B.lo[a] = D.lo[a];
+      B.hi[a] = D.hi[a];
+      B.d[a] = D.d[a];
+      B.n[a] = D.n[a];
+    }
+    B.buf = D.buf;
+    B.off = h->hboxes[g].off;
+    const domain &C = h->G.boxes[base];
+    bool holds = true;   // domain::operator< (src/domain.cc:1947-1954): C strictly inside D
+    for (int a = 0; a < 3; a++) holds = holds && D.lo[a] < C.lo[a] && C.hi[a] < D.hi[a];
+    if (g > 0 && holds) base = g;
+  }
+  CUDA_TRY(cudaSetDevice(h->device));
+  InterpBox *d_b = nullptr;
+  double *d_xyz = nullptr, *d_out = nullptr;
+  auto release = [&]() {
+    cudaFree(d_b);
+    cudaFree(d_xyz);
+    cudaFree(d_out);
+  };
+  cudaError_t e = cudaMalloc((void **)&d_b, sizeof(InterpBox) * nb);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_xyz, sizeof(double) * 3 * (size_t)npts);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&d_out, sizeof(double) * (size_t)npts);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_b, ib.data(), sizeof(InterpBox) * nb, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * (size_t)npts, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) {
+    const long long blocks = cdiv(npts, 128);
+    k_interp_points<<<(unsigned)blocks, 128, 0, h->stream>>>(d_b, nb, base, box, h->F.f[F_U], d_xyz, npts, ord,
+                                                             d_out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d_out, sizeof(double) * (size_t)npts, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  release();
+  if (e != cudaSuccess)
+    return fail(e == cudaErrorMemoryAllocation ? OLGPU_ERR_OOM : OLGPU_ERR_CUDA,
+                std::string("olgpu_interpolate: ") + cudaGetErrorString(e));
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_level_norms(const olgpu_hierarchy *h, int cycle, double *pre, double *post)
+{
+  if (!h || !pre || !post) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  const int L = h->G.levels;
+  const int cycles = (int)(h->norm_hist.size() / (2 * (size_t)L));
+  if (cycle < 0 || cycle >= cycles) return fail(OLGPU_ERR_INVALID_ARG, "no such cycle in this solve");
+  const double *v = h->norm_hist.data() + (size_t)cycle * 2 * L;
+  for (int l = 0; l < L; l++) {
+    pre[l] = v[l];
+    post[l] = v[L + l];
+  }
   return OLGPU_OK;
 }
 

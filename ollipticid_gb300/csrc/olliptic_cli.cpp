@@ -16,15 +16,29 @@
 //
 // Output: the hierarchy, one line per V-cycle with its norm, and the ADM
 // masses in the reference's "ADM mass[i] = ..." form (src/elliptic.cc:2466-
-// 2469).  Exit status 0 on success; otherwise the C ABI's status with its
-// message on stderr.
+// 2469) on stdout; in the output directory (-o, default Output) the files of
+// elliptic::Print_Solution (src/output.cc:624-700) for the puncture path:
+// the per-box cuts u-l<l>b<i>-0.{x,y,z} (-p1d, ffunction::Print_1D,
+// src/ffunction.cc:819-960) and the interpolated cuts u.X, u.Y, u.Z and the
+// plane u.XY (-pint, multigrid::Print_Interpol_1D / _2D, src/multigrid.cc:
+// 151-880), with the reference's number formats, each cycle's
+// pre-smoothing norms per level as Loo.gp (-so yes, elliptic::Print_Pre_Cycle,
+// src/output.cc:1355-1460), and the command line as <dir>.run.  stdout0.out
+// (the banner and log) is not written.  The directory is rotated like the reference's
+// (interface.cc:1470-1538): an existing <dir> becomes <dir>_prev, replacing
+// an older <dir>_prev.  2-D and 3-D dumps (-p2d, -p3d) are not written.
+// Exit status 0 on success; otherwise the C ABI's status with its message on
+// stderr.
 #include "olgpu.h"
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <map>
 #include <string>
+#include <system_error>
 #include <vector>
 
 namespace {
@@ -60,7 +74,176 @@ struct Args {
     const char *v = find(names);
     return v && (!std::strcmp(v, "yes") || !std::strcmp(v, "YES") || !std::strcmp(v, "true"));
   }
+  // a logic parameter with the reference's default when absent
+  bool logic(std::initializer_list<const char *> names, bool def) const
+  {
+    return find(names) ? yes(names) : def;
+  }
 };
+
+// The geometry of one box as the output needs it (domain::Get_x, is_in).
+struct BoxGeom {
+  olgpu_box_info b;
+  double lo(int a) const { return a == 0 ? b.xi : a == 1 ? b.yi : b.zi; }
+  double hi(int a) const { return a == 0 ? b.xf : a == 1 ? b.yf : b.zf; }
+  double d(int a) const { return a == 0 ? b.dx : a == 1 ? b.dy : b.dz; }
+  int n(int a) const { return a == 0 ? b.nx : a == 1 ? b.ny : b.nz; }
+  double coord(int a, int i) const { return lo(a) + (double)i * d(a); }
+  bool is_in_axis(int a, double x) const { return lo(a) - d(a) * 0.1 <= x && x <= hi(a) + d(a) * 0.1; }
+  // domain::Get_i: the first node at or after x
+  int locate(int a, double x) const
+  {
+    const int np = n(a);
+    int lo_i = 0, hi_i = np, i;
+    if (lo(a) - x < 0.0 && x - hi(a) < 0.0) {
+      i = np % 2 == 0 ? np / 2 : (np - 1) / 2;
+      do {
+        const double xi = coord(a, i);
+        if (xi > x || std::fabs(xi - x) <= 3 * 2.220446049250313080847e-16)
+          hi_i = i;
+        else
+          lo_i = i;
+        i = (hi_i + lo_i) / 2;
+      } while (lo_i + 1 < hi_i);
+    } else {
+      i = (lo(a) >= x) ? 0 : np - 2;
+    }
+    return i + 1;
+  }
+};
+
+// interface.cc:1470-1538: <dir>_prev is removed, <dir> moved to it, <dir>
+// made afresh, and the command line written to <dir>/<dir>.run.
+bool prepare_output_dir(const std::string &name, int argc, char **argv)
+{
+  namespace fs = std::filesystem;
+  std::error_code ec;
+  const fs::path dir(name), prev(name + "_prev");
+  if (fs::exists(dir, ec)) {
+    fs::remove_all(prev, ec);
+    fs::rename(dir, prev, ec);
+  }
+  fs::create_directories(dir, ec);
+  if (!fs::is_directory(dir, ec)) return false;
+  const std::string run = name + "/" + fs::path(name).filename().string() + ".run";
+  FILE *f = std::fopen(run.c_str(), "w");
+  if (!f) return false;
+  for (int i = 0; i < argc; i++) std::fprintf(f, "%s%s", i ? " " : "", argv[i]);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+  fs::permissions(run, fs::perms::owner_exec | fs::perms::group_exec | fs::perms::others_exec,
+                  fs::perm_options::add, ec);
+  return true;
+}
+
+// ffunction::Print_1D of one box and one axis: at every node along `axis`
+// (ghosts included) through the other coordinates 0 when the box holds them,
+// else through its middle node; the value is interpolated (Lagrange, order+1)
+// when `interpolate`, else the node value.  "%.12e\t%.12e\t" lines, then a
+// blank line.
+olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis, bool interpolate, int ord,
+                           const std::string &file)
+{
+  int node[3];
+  double at[3];
+  for (int a = 0; a < 3; a++) {
+    const int m = B.n(a) % 2 == 0 ? B.n(a) / 2 : (B.n(a) - 1) / 2;
+    node[a] = m;
+    at[a] = B.coord(a, m);
+    if (a == axis) continue;
+    if (B.is_in_axis(a, 0.0)) {
+      if (interpolate)
+        at[a] = 0.0;
+      else {
+        node[a] = B.locate(a, 0.0);
+        at[a] = B.coord(a, node[a]);
+      }
+    }
+  }
+  const int np = B.n(axis);
+  std::vector<double> pts(3 * (size_t)np), val(np);
+  for (int i = 0; i < np; i++) {
+    for (int a = 0; a < 3; a++) pts[3 * i + a] = at[a];
+    pts[3 * i + axis] = B.coord(axis, i);
+  }
+  if (interpolate) {
+    const olgpu_status st = olgpu_interpolate(h, g, pts.data(), np, ord, val.data());
+    if (st != OLGPU_OK) return st;
+  } else {
+    std::vector<double> u((size_t)B.b.nx * B.b.ny * B.b.nz);
+    const olgpu_status st = olgpu_download(h, g, "u", u.data());
+    if (st != OLGPU_OK) return st;
+    for (int i = 0; i < np; i++) {
+      int ijk[3] = {node[0], node[1], node[2]};
+      ijk[axis] = i;
+      val[i] = u[((size_t)ijk[2] * B.b.ny + ijk[1]) * B.b.nx + ijk[0]];
+    }
+  }
+  FILE *f = std::fopen(file.c_str(), "a");
+  if (!f) return OLGPU_ERR_INVALID_ARG;
+  for (int i = 0; i < np; i++) std::fprintf(f, "%.12e\t%.12e\t\n", B.coord(axis, i), val[i]);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+  return OLGPU_OK;
+}
+
+// multigrid::Print_Interpol_1D along one axis: from -LD/2 by D (LD/1000 when
+// D <= 0) while <= LD/2, the other coordinates 0, points outside the largest
+// box skipped; "%.18e\t%.18e" lines, then a blank line.
+olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D, int ord, const std::string &file)
+{
+  const double xi = -0.5 * LD, xf = 0.5 * LD, Dx = D > 0.0 ? D : LD / 1000;
+  std::vector<double> pts, xs;
+  for (double x = xi; x <= xf; x += Dx) {
+    double p[3] = {0.0, 0.0, 0.0};
+    p[axis] = x;
+    pts.insert(pts.end(), p, p + 3);
+    xs.push_back(x);
+  }
+  std::vector<double> val(xs.size());
+  const olgpu_status st = olgpu_interpolate(h, -1, pts.data(), (long long)xs.size(), ord, val.data());
+  if (st != OLGPU_OK) return st;
+  FILE *f = std::fopen(file.c_str(), "a");
+  if (!f) return OLGPU_ERR_INVALID_ARG;
+  for (size_t i = 0; i < xs.size(); i++)
+    if (!std::isnan(val[i])) std::fprintf(f, "%.18e\t%.18e\n", xs[i], val[i]);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+  return OLGPU_OK;
+}
+
+// multigrid::Print_Interpol_2D, the z = 0 plane: x and y from -L/4 by L/200
+// while <= L/4; "%.18e\t%.18e\t%.18e" lines, a blank line after each x and
+// one more at the end.
+olgpu_status print_interpol_xy(olgpu_hierarchy *h, double LD1, double LD2, int ord, const std::string &file)
+{
+  const double x1i = -0.25 * LD1, x2i = -0.25 * LD2, x1f = 0.25 * LD1, x2f = 0.25 * LD2;
+  const double Dx1 = LD1 / 200, Dx2 = LD2 / 200;
+  std::vector<double> pts, xs, ys;
+  std::vector<int> row_end;
+  for (double x = x1i; x <= x1f; x += Dx1) {
+    for (double y = x2i; y <= x2f; y += Dx2) {
+      const double p[3] = {x, y, 0.0};
+      pts.insert(pts.end(), p, p + 3);
+      xs.push_back(x);
+      ys.push_back(y);
+    }
+    row_end.push_back((int)xs.size());
+  }
+  std::vector<double> val(xs.size());
+  const olgpu_status st = olgpu_interpolate(h, -1, pts.data(), (long long)xs.size(), ord, val.data());
+  if (st != OLGPU_OK) return st;
+  FILE *f = std::fopen(file.c_str(), "a");
+  if (!f) return OLGPU_ERR_INVALID_ARG;
+  size_t q = 0;
+  for (int e : row_end) {
+    for (; q < (size_t)e; q++) std::fprintf(f, "%.18e\t%.18e\t%.18e\n", xs[q], ys[q], val[q]);
+    std::fprintf(f, "\n");
+  }
+  std::fprintf(f, "\n");
+  std::fclose(f);
+  return OLGPU_OK;
+}
 
 int fail(olgpu_status st, const char *what)
 {
@@ -140,6 +323,17 @@ int main(int argc, char **argv)
                 boxes[g].ny, boxes[g].nz, boxes[g].xi, boxes[g].yi, boxes[g].zi, boxes[g].dx);
   if (A.yes({"-plan"})) return 0;
 
+  // the output directory exists from start-up on, as the reference's
+  const char *o = A.find({"-o", "--out-dir"});
+  const std::string out = o ? o : "Output";
+  if (!prepare_output_dir(out, argc, argv)) {
+    std::fprintf(stderr, "Olliptic_gpu.x: cannot create the output directory %s\n", out.c_str());
+    return (int)OLGPU_ERR_INVALID_ARG;
+  }
+  const std::string dir = out + "/";
+  const char *so = A.find({"-so", "--std-output"});
+  const bool std_output = !so || !std::strcmp(so, "yes");
+
   olgpu_hierarchy *h = nullptr;
   st = olgpu_hierarchy_create(&p, A.integer({"-gpu-device"}, -1), &h);
   if (st != OLGPU_OK) return fail(st, "hierarchy");
@@ -159,10 +353,55 @@ int main(int argc, char **argv)
   }
   std::printf("Solved in %d V-cycles, norm %.6e, %.3f ms on the device\n", rep.cycles, rep.final_res,
               olgpu_last_device_ms(h));
+  if (std_output) {   // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
+    FILE *f = std::fopen((dir + "Loo.gp").c_str(), "a");
+    std::vector<double> pre(nl), post(nl);
+    for (int c = 0; f && c < rep.cycles; c++) {
+      if (olgpu_level_norms(h, c, pre.data(), post.data()) != OLGPU_OK) break;
+      for (int k = nl - 1; k >= 0; k--) std::fprintf(f, "%d\t%.18e\n", c, pre[k]);
+    }
+    if (f) std::fclose(f);
+  }
   std::printf("Puncure method: \n");
   double adm[OLGPU_MAX_BH];
   olgpu_adm_mass(h, adm);
   for (int i = 0; i < p.numbh; i++) std::printf("ADM mass[%d] = %.17g\n", i, adm[i]);
+
+  // elliptic::Print_Solution (src/output.cc:624-700), variable "u"
+  const bool print_1d = A.logic({"-p1d", "--print-1d"}, true);
+  const bool print_interpol = A.logic({"-pint", "--print-interpol"}, true);
+  const bool interpol_output = A.logic({"-int", "--interpol-output"}, true);
+  if (print_1d || print_interpol) {
+    const int ord = p.order + 1;
+    std::printf("Printing...\n");
+    olgpu_status ps = OLGPU_OK;
+    if (print_1d) {
+      std::vector<int> in_level(nl, 0);
+      static const char *ext[3] = {".x", ".y", ".z"};
+      for (int l = 0; l < nl && ps == OLGPU_OK; l++)
+        for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
+          if (boxes[g].level != l) continue;
+          const BoxGeom B{boxes[g]};
+          const std::string stem = dir + "u-l" + std::to_string(l) + "b" + std::to_string(in_level[l]++) + "-0";
+          for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
+            ps = print_box_cut(h, B, g, a, interpol_output, ord, stem + ext[a]);
+        }
+    }
+    if (print_interpol && ps == OLGPU_OK) {
+      const double Dp = A.num({"-Dp", "--d-print"}, -1.0);
+      const double Lx = A.num({"-Lx", "--length-x"}, p.L), Ly = A.num({"-Ly", "--length-y"}, p.L),
+                   Lz = A.num({"-Lz", "--length-z"}, p.L);
+      static const char *ext[3] = {"u.X", "u.Y", "u.Z"};
+      const double LD[3] = {Lx, Ly, Lz};
+      for (int a = 0; a < 3 && ps == OLGPU_OK; a++) ps = print_interpol_1d(h, a, LD[a], Dp, ord, dir + ext[a]);
+      if (ps == OLGPU_OK) ps = print_interpol_xy(h, Lx, Ly, ord, dir + "u.XY");
+    }
+    if (ps != OLGPU_OK) {
+      olgpu_hierarchy_destroy(h);
+      return fail(ps, "output");
+    }
+    std::printf("done\n");
+  }
   olgpu_hierarchy_destroy(h);
   return 0;
 }

@@ -1129,6 +1129,41 @@ int orc_set_field(orc_solver *S, int g, const char *name, const double *in)
   return 0;
 }
 
+/* u at arbitrary points as the reference prints it.  box < 0: the rule of
+ * multigrid::Print_Interpol_1D / _2D (src/multigrid.cc:151-261, 555-880):
+ * the largest box l0 (multigrid::multigrid, src/multigrid.cc:40-48, with
+ * domain::operator<, src/domain.cc:1947-1954), a point outside it is not
+ * printed (NaN here), otherwise the last box in level order whose interior
+ * holds it (is_in_nb), l0 when none does.  box >= 0: that box, as
+ * ffunction::Print_1D (src/ffunction.cc:819-960).  The value is
+ * Lagrange_Interpol_In with ord+1 nodes per axis. */
+int orc_interpolate(const orc_solver *S, int box, const double *xyz, long npts, int ord, double *out)
+{
+  if (box >= S->nboxes || ord < 1 || ord > 15) return -1;
+  int l0 = 0;
+  for (int g = 1; g < S->nboxes; g++) {
+    const odom *A = &S->box[l0].D, *B = &S->box[g].D;
+    int inside = 1;
+    for (int a = 0; a < 3; a++) inside = inside && B->lo[a] < A->lo[a] && A->hi[a] < B->hi[a];
+    if (inside) l0 = g;
+  }
+  for (long q = 0; q < npts; q++) {
+    const double x = xyz[3 * q], y = xyz[3 * q + 1], z = xyz[3 * q + 2];
+    int g = box;
+    if (g < 0) {
+      if (!dom_is_in(&S->box[l0].D, x, y, z)) {
+        out[q] = NAN;
+        continue;
+      }
+      g = l0;
+      for (int b = 0; b < S->nboxes; b++)
+        if (dom_is_in_nb(&S->box[b].D, x, y, z)) g = b;
+    }
+    out[q] = interp_lagrange(&S->box[g], S->box[g].f[F_U], ord, x, y, z);
+  }
+  return 0;
+}
+
 double orc_vcycle(orc_solver *S)
 {
   return fasn(S, S->levels - 1, S->levels - 1);

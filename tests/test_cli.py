@@ -4,7 +4,9 @@ equal the Python API's solve of the same command line."""
 import os
 import re
 import subprocess
+import tempfile
 
+import numpy as np
 import pytest
 
 from tests.cases import CASES, CONFIG2, problem
@@ -21,8 +23,11 @@ def cli():
     return CLI
 
 
-def run(cli, args, check=True):
-    r = subprocess.run([cli] + args.split(), capture_output=True, text=True, timeout=600)
+def run(cli, args, check=True, cwd=None):
+    """Runs the command line in `cwd` (a fresh temporary directory when None:
+    it writes its output directory where it runs)."""
+    with tempfile.TemporaryDirectory() as tmp:
+        r = subprocess.run([cli] + args.split(), capture_output=True, text=True, timeout=600, cwd=cwd or tmp)
     if check:
         assert r.returncode == 0, r.stderr
     return r
@@ -42,6 +47,22 @@ def test_plan_matches_the_library(cli):
     assert (int(m.group(1)), int(m.group(2)), int(m.group(3))) == (nl.value, mg.value, nb.value)
     sizes = re.findall(r"box +\d+ level +\d+ +(\d+) x (\d+) x (\d+)", r.stdout)
     assert [tuple(map(int, s)) for s in sizes] == [(out[g].nx, out[g].ny, out[g].nz) for g in range(nb.value)]
+
+
+def test_output_directory_is_rotated_like_the_reference(cli, tmp_path):
+    """interface.cc:1470-1538: <dir> is made at start-up with <dir>.run (the
+    command line); a second run moves it to <dir>_prev.  No GPU is needed:
+    the directory exists before the device is touched (the run then fails
+    here, or solves where a GPU is present)."""
+    args = "-eq Punctures -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 -o Res -p1d no -pint no -gpu-device 9999"
+    run(cli, args, check=False, cwd=str(tmp_path))
+    assert (tmp_path / "Res" / "Res.run").exists()
+    recorded = (tmp_path / "Res" / "Res.run").read_text().split()
+    assert recorded[1:] == args.split() and os.access(tmp_path / "Res" / "Res.run", os.X_OK)
+    (tmp_path / "Res" / "marker").write_text("first")
+    run(cli, args, check=False, cwd=str(tmp_path))
+    assert (tmp_path / "Res_prev" / "marker").read_text() == "first"
+    assert not (tmp_path / "Res" / "marker").exists()
 
 
 def test_other_equations_are_refused(cli):
