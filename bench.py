@@ -325,6 +325,38 @@ def run_config3():
         E.close()
 
 
+def run_convergence():
+    """The reference's self-convergence study (utils/run_conv.sh): one
+    spinning puncture at N = 25, 49, 97 (4th order, 4 levels, L = 100),
+    solved on the GPU in FP64 and in mixed precision to 1e-11, u read on the
+    reference's u.X points; the order p of |u_h - u_h/2| ~ h^p away from the
+    puncture beside the order of the reference's own runs (the committed
+    fixture made by its Olliptic.x)."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "convergence",
+                        "o4_spin_l4.npz")
+    g = np.load(path)
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from tests.golden.make_convergence_golden import orders
+    args = g["args"].item().decode()
+    x = g["x_25"]
+    pts = np.stack([x, np.zeros_like(x), np.zeros_like(x)], axis=1)
+    out = {"workload": "run_conv.sh study: " + args + ", N = 25/49/97",
+           "reference": {"p_inf": float(g["p_inf"]), "p_l2": float(g["p_l2"])}}
+    for mixed, key in ((False, "plain_fp64"), (True, "mixed")):
+        cuts, dev = [], []
+        for N in g["resolutions"]:
+            with og.Elliptic(og.parse_olliptic_args((args + f" -N {int(N)}").split())) as E:
+                E.set_precision(mixed)
+                E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=300, tol=1e-11)
+                cuts.append(E.interpolate(pts))
+                dev.append(float(np.max(np.abs(cuts[-1] - g[f"u_{int(N)}"]))))
+        p_inf, p_l2 = orders(x, *cuts)
+        out[key] = {"p_inf": p_inf, "p_l2": p_l2, "max_abs_u_minus_reference_cut": dev}
+    return out
+
+
 def run_batched(args, count: int = 16, group: int = 16, tuned=None):
     """Seeded batched binaries (mixed precision, tol 1e-10): solves/s when
     `group` solves run concurrently, and the same instances one at a time."""
@@ -475,12 +507,13 @@ def run_gpu(args, rank: int, world: int, local: int):
     # ---- the same workload with the mixed-precision cycle
     mixed = run_mixed(E, P, args, dev, u_fix, adm_fix)
 
-    concurrent = batched = served = config3 = None
+    concurrent = batched = served = config3 = convergence = None
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, u_fix, adm_fix, value / world)
         batched = run_batched(args, tuned=autotune.tune(P, concurrency=16))
         config3 = run_config3()
+        convergence = run_convergence()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
@@ -525,6 +558,7 @@ def run_gpu(args, rank: int, world: int, local: int):
             "accuracy": {"max_abs_u_minus_fixed_point": err_fp64,
                          "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served, "config3": config3,
+            "convergence": convergence,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
         }

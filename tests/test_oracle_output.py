@@ -36,3 +36,17 @@ def test_oracle_reprints_the_reference_cuts(path):
         got = orc.interpolate(pts, P.order + 1)
         assert not np.isnan(got).any()
         assert np.array_equal(got, vals[rows]), name
+
+
+@pytest.mark.parametrize("case", ["o2_spin_l4", "o4_spin_l4"])
+def test_oracle_reprints_the_reference_convergence_run(case):
+    """The coarsest run of the convergence study (N = 25): the oracle's
+    solve under the reference's stop rule and its u.X cut are the
+    reference's, digit for digit."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "convergence", case + ".npz"))
+    P = problem(g["args"].item().decode() + " -N 25")
+    orc = oracle_mod.Oracle(P.oracle_dict())
+    orc.solve()
+    x = g["x_25"]
+    got = orc.interpolate(np.stack([x, 0 * x, 0 * x], axis=1), P.order + 1)
+    assert np.array_equal(got, g["u_25"])
