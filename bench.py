@@ -332,6 +332,7 @@ def run_convergence():
     reference's u.X points; the order p of |u_h - u_h/2| ~ h^p away from the
     puncture beside the order of the reference's own runs (the committed
     fixture made by its Olliptic.x)."""
+    import numpy as np
     import ollipticid_gb300 as og
     from ollipticid_gb300 import _abi
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "convergence",
