@@ -394,16 +394,22 @@ def run_batched(args, count: int = 16, group: int = 16, tuned=None):
             "cycles_mean": sum(cycles) / len(cycles), "timing": "host wall clock around the solves"}
 
 
-def run_served(rates=(4.0, 16.0), count: int = 24, inner_sweeps=None):
+def run_served(rates=(4.0, 16.0, 64.0), count: int = 24, inner_sweeps=None, native: bool = False):
     """Poisson request streams (NumBH 1-4, N 33-129, orders 2-8, 6-10
-    levels, 10% scalar field) served with memory admission."""
+    levels, 10% scalar field) served with memory admission, by the Python
+    loop (serve.Server) or by the library's C++ server (native)."""
     from ollipticid_gb300 import workloads
-    from ollipticid_gb300.serve import Server
+    from ollipticid_gb300.serve import NativeServer, Server
     out = []
     for rate in rates:
-        rep = Server(mem_budget=120 << 30, max_active=16, inner_sweeps=inner_sweeps).run(
-            workloads.served_stream(count, rate))
+        if native:
+            with NativeServer(mem_budget=120 << 30, max_active=16, inner_sweeps=inner_sweeps) as S:
+                rep = S.run(workloads.served_stream(count, rate))
+        else:
+            rep = Server(mem_budget=120 << 30, max_active=16, inner_sweeps=inner_sweeps).run(
+                workloads.served_stream(count, rate))
         out.append({"rate_hz": rate, "requests": count, "inner_sweeps": inner_sweeps,
+                    "server": "C++ (olgpu_server_*)" if native else "Python loop",
                     **{k: rep[k] for k in ("throughput_solves_per_s", "latency_p50_s", "latency_p99_s",
                                            "latency_max_s", "cycles_mean", "peak_concurrent_solves", "makespan_s")}})
     return out
@@ -516,6 +522,7 @@ def run_gpu(args, rank: int, world: int, local: int):
         config3 = run_config3()
         convergence = run_convergence()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
+        served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
     # multicolour smoother (k_smooth_color) on the finest level, timed with

@@ -207,6 +207,61 @@ olgpu_status olgpu_set_smoother_blocks(olgpu_hierarchy *h, int max_blocks);
  * and coefficients, so that one hierarchy can serve repeated solves. */
 olgpu_status olgpu_reset(olgpu_hierarchy *h);
 
+/* Serving: continuous batching of puncture solves on one GPU (no reference
+ * counterpart; the reference runs one solve per process).  Requests are
+ * admitted in arrival order while a slot (max_active) and their device
+ * footprint (from the host-only plan) fit in mem_budget; builder threads
+ * make their hierarchies while a scheduler thread keeps every admitted solve's
+ * next cycle queued on its own stream (olgpu_cycle_launch / _poll), so the
+ * work of different requests overlaps on the device; a finished solve frees
+ * its memory at once and the next request takes its place.  A request whose
+ * footprint exceeds mem_budget is refused with OLGPU_ERR_OOM.  Each result is
+ * the one the same problem gives solved alone, bit for bit.
+ * olgpu_server_submit and olgpu_server_poll may be called from any thread. */
+typedef struct olgpu_server olgpu_server;
+
+typedef struct {
+  int device;                   /* CUDA device (-1: the current one)          */
+  long long mem_budget;         /* device bytes the admitted solves may hold   */
+  int max_active;               /* solves on the GPU (or being built) at once  */
+  int precision;                /* olgpu_precision of every solve              */
+  int stop;                     /* olgpu_stop_kind of every solve              */
+  int max_cycles;               /* cap on V-cycles per solve (> 0)             */
+  double tol;                   /* <= 0: each problem's -s tolerance           */
+  int builders;                 /* host threads building hierarchies (>= 1)    */
+  int nu1, nu2;                 /* FP32 cycle sweeps (mixed); nu1 < 0: the problem's */
+  int blocks;                   /* FP32 smoother cluster blocks; < 0: follow the load */
+  int busy;                     /* with blocks < 0: per-colour launches while fewer
+                                   solves are on the GPU, clusters of 16 beyond */
+  int keep_solutions;           /* != 0: a finished solve's hierarchy is handed
+                                   to the caller in olgpu_server_result.h      */
+} olgpu_server_config;
+
+typedef struct {
+  long long id;                 /* the request                                */
+  int status;                   /* olgpu_status of the request                */
+  int cycles;                   /* V-cycles run                               */
+  double final_res;             /* norm of the last cycle                     */
+  double adm[OLGPU_MAX_BH];     /* ADM masses after the last cycle            */
+  double queue_s;               /* arrival (submit) to admission              */
+  double latency_s;             /* arrival to the end of the last cycle       */
+  olgpu_hierarchy *h;           /* keep_solutions: the solved hierarchy, now the
+                                   caller's (destroy it); else NULL            */
+} olgpu_server_result;
+
+void olgpu_server_config_defaults(olgpu_server_config *c);
+olgpu_status olgpu_server_create(const olgpu_server_config *c, olgpu_server **out);
+/* Queues one problem; *id identifies its result. */
+olgpu_status olgpu_server_submit(olgpu_server *s, const olgpu_problem *p, long long *id);
+/* *done = 1 and *out filled once request id has finished (its result is then
+ * released; a second poll of the same id is an error); wait != 0 blocks until
+ * it has.  Returns the call's status; the request's own is out->status. */
+olgpu_status olgpu_server_poll(olgpu_server *s, long long id, int wait, int *done, olgpu_server_result *out);
+/* Solves on the GPU, being built or waiting, and the peak of the first. */
+olgpu_status olgpu_server_stats(olgpu_server *s, int *active, int *building, int *waiting, int *peak_active);
+/* Stops the threads, finishes nothing more and frees every hierarchy it holds. */
+olgpu_status olgpu_server_destroy(olgpu_server *s);
+
 /* Timing aids. */
 /* device time of the last olgpu_solve / olgpu_vcycle in ms */
 double olgpu_last_device_ms(const olgpu_hierarchy *h);

@@ -48,6 +48,21 @@ class Report(C.Structure):
     ]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [
+        ("device", C.c_int), ("mem_budget", C.c_longlong), ("max_active", C.c_int), ("precision", C.c_int),
+        ("stop", C.c_int), ("max_cycles", C.c_int), ("tol", C.c_double), ("builders", C.c_int),
+        ("nu1", C.c_int), ("nu2", C.c_int), ("blocks", C.c_int), ("busy", C.c_int), ("keep_solutions", C.c_int),
+    ]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [
+        ("id", C.c_longlong), ("status", C.c_int), ("cycles", C.c_int), ("final_res", C.c_double),
+        ("adm", _D16), ("queue_s", C.c_double), ("latency_s", C.c_double), ("h", C.c_void_p),
+    ]
+
+
 class BoxFields(C.Structure):
     _fields_ = [
         ("u", C.c_void_p), ("b", C.c_void_p), ("c", C.c_void_p), ("s", C.c_void_p),
@@ -91,6 +106,14 @@ SIGNATURES = {
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),
     "olgpu_time_smoother": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "olgpu_smooth_box_noalloc": (C.c_int, [C.POINTER(BoxFields), C.c_int, C.POINTER(C.c_double), C.c_void_p]),
+    "olgpu_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
+    "olgpu_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),
+    "olgpu_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Problem), C.POINTER(C.c_longlong)]),
+    "olgpu_server_poll": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(C.c_int),
+                                    C.POINTER(ServerResult)]),
+    "olgpu_server_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]),
+    "olgpu_server_destroy": (C.c_int, [C.c_void_p]),
     "olgpu_last_error": (C.c_char_p, []),
     "olgpu_version": (C.c_char_p, []),
 }

@@ -24,7 +24,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
 CU_SOURCES = ["olgpu.cu"]
-CPP_SOURCES = ["grid.cpp"]
+CPP_SOURCES = ["grid.cpp", "server.cpp"]
 HEADERS = ["device.cuh", "kernels.cuh", "coarse_cluster.cuh", "mixed.cuh", "smooth_cluster.cuh", "grid.h", "../../include/olgpu.h"]
 
 
@@ -59,13 +59,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for s in CPP_SOURCES:
         o = os.path.join(BUILD, s + ".o")
         objs.append(o)
-        jobs.append([CXX, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-c", os.path.join(CSRC, s), "-o", o])
+        jobs.append([CXX, "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-I", INCLUDE, "-c",
+                     os.path.join(CSRC, s), "-o", o])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:
             sys.stdout.write(o)
-    _run([NVCC, "-shared", *ARCH, *objs, "-o", LIB, "-lcudart"])
+    _run([NVCC, "-shared", *ARCH, *objs, "-o", LIB, "-lcudart", "-lpthread"])
     if os.path.exists(cli_src):
         _run([CXX, "-O2", "-std=c++17", "-ffp-contract=off", "-I", INCLUDE, cli_src, "-o", CLI,
               "-L", BUILD, "-lolgpu", "-Wl,-rpath,$ORIGIN"])

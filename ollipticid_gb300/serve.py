@@ -186,3 +186,114 @@ class Server:
             "peak_concurrent_solves": peak_active,
             "results": [results[i] for i in sorted(results)],
         }
+
+
+class NativeServer:
+    """The library's own continuous-batching server (olgpu_server_*, server.cpp):
+    C++ builder threads make the hierarchies and a C++ scheduler thread admits
+    requests and keeps their cycles queued; Python only submits and polls.
+    Same admission rule, smoother layout policy and stop rule as `Server`."""
+
+    def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
+                 tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
+                 inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4, stop: int = _abi.STOP_TOLERANCE):
+        self.lib = _abi.load()
+        c = _abi.ServerConfig()
+        self.lib.olgpu_server_config_defaults(C.byref(c))
+        c.device, c.mem_budget, c.max_active = device, mem_budget, max_active
+        c.precision = _abi.PREC_MIXED if mixed else _abi.PREC_FP64
+        c.stop, c.max_cycles, c.tol, c.builders, c.busy = stop, max_cycles, tol or 0.0, builders, busy
+        if inner_sweeps:
+            c.nu1, c.nu2 = inner_sweeps[0], inner_sweeps[1]
+            c.blocks = inner_sweeps[2] if len(inner_sweeps) > 2 else -1
+        c.keep_solutions = 1 if keep_u else 0
+        self.keep_u = keep_u
+        s = C.c_void_p()
+        check(self.lib.olgpu_server_create(C.byref(c), C.byref(s)))
+        self._s = s
+        self._problems = {}
+
+    def submit(self, problem: Problem) -> int:
+        cp = problem.to_c()
+        rid = C.c_longlong()
+        check(self.lib.olgpu_server_submit(self._s, C.byref(cp), C.byref(rid)))
+        self._problems[rid.value] = problem
+        return rid.value
+
+    def poll(self, rid: int, wait: bool = True) -> Optional[Result]:
+        out = _abi.ServerResult()
+        done = C.c_int()
+        check(self.lib.olgpu_server_poll(self._s, rid, 1 if wait else 0, C.byref(done), C.byref(out)))
+        if not done.value:
+            return None
+        r = Result(rid, 0.0, cycles=out.cycles, final_res=out.final_res, status=out.status)
+        r.admitted = out.queue_s
+        r.finished = out.latency_s          # relative to arrival
+        nbh = self._problems.pop(rid).numbh
+        r.adm = [out.adm[i] for i in range(nbh)]
+        if out.h:
+            h = C.c_void_p(out.h)
+            if self.keep_u:
+                r.u = []
+                for g in range(self.lib.olgpu_num_boxes(h)):
+                    bi = _abi.BoxInfo()
+                    check(self.lib.olgpu_box(h, g, C.byref(bi)))
+                    a = np.empty((bi.nz, bi.ny, bi.nx))
+                    check(self.lib.olgpu_download(h, g, b"u", a.ctypes.data_as(C.c_void_p)))
+                    r.u.append(a)
+            self.lib.olgpu_hierarchy_destroy(h)
+        return r
+
+    def stats(self) -> dict:
+        v = [C.c_int() for _ in range(4)]
+        check(self.lib.olgpu_server_stats(self._s, *(C.byref(x) for x in v)))
+        return dict(zip(("active", "building", "waiting", "peak_active"), (x.value for x in v)))
+
+    def run(self, stream: Sequence[Tuple[float, Problem]]) -> dict:
+        """Submits (arrival time, problem) pairs in real time, then collects
+        every result; the report has the keys of `Server.run`."""
+        reqs = sorted(enumerate(stream), key=lambda r: r[1][0])
+        t0 = time.perf_counter()
+        ids = {}
+        for i, (arr, prob) in reqs:
+            delay = arr - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            ids[i] = (self.submit(prob), time.perf_counter() - t0)
+        results = {}
+        for i, (rid, arrival) in ids.items():
+            r = self.poll(rid, wait=True)
+            r.rid, r.arrival = i, arrival
+            r.admitted += arrival
+            r.finished += arrival
+            results[i] = r
+        makespan = max(r.finished for r in results.values()) - min(r.arrival for r in results.values())
+        lat = np.array([results[i].latency for i in sorted(results)])
+        return {
+            "completed": len(results),
+            "makespan_s": makespan,
+            "throughput_solves_per_s": len(results) / makespan if makespan > 0 else float("nan"),
+            "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99)),
+            "latency_max_s": float(lat.max()),
+            "cycles_mean": float(np.mean([r.cycles for r in results.values()])),
+            "peak_concurrent_solves": self.stats()["peak_active"],
+            "results": [results[i] for i in sorted(results)],
+        }
+
+    def close(self):
+        if getattr(self, "_s", None):
+            self.lib.olgpu_server_destroy(self._s)
+            self._s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

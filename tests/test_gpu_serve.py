@@ -37,3 +37,40 @@ def test_request_larger_than_the_budget_is_refused():
     from ollipticid_gb300.serve import Server
     rep = Server(mem_budget=1 << 20).run([(0.0, problem("o4_spin"))])
     assert rep["results"][0].status == _abi.ERR_OOM
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [True, False], ids=["mixed", "fp64"])
+def test_native_server_results_match_solo_solves(mixed):
+    """The C++ server behind the C ABI (olgpu_server_*): uneven requests
+    overlap on the GPU and each result is the solo solve's bit for bit."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    from ollipticid_gb300.serve import NativeServer
+    probs = [problem(n) for n in NAMES]
+    stream = [(0.002 * i, p) for i, p in enumerate(probs)]
+    with NativeServer(max_active=3, keep_u=True, tol=1e-11, mixed=mixed) as S:
+        rep = S.run(stream)
+    assert rep["completed"] == len(probs)
+    assert rep["peak_concurrent_solves"] >= 2
+    for p, r in zip(probs, rep["results"]):
+        with og.Elliptic(p) as E:
+            E.set_precision(mixed)
+            solo = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-11)
+            u = [E.get_field(g) for g in range(len(E.boxes))]
+            adm = E.ADM_mass
+        assert r.status == 0 and r.cycles == solo.cycles and r.final_res == solo.final_res
+        assert r.adm == adm
+        err = max(float(np.max(np.abs(a - b))) for a, b in zip(u, r.u))
+        assert err == 0.0, err
+
+
+@pytest.mark.gpu
+def test_native_server_admits_by_memory():
+    """A budget that holds one solve at a time runs them one after another."""
+    from ollipticid_gb300.serve import NativeServer, footprint
+    probs = [problem("o4_spin") for _ in range(3)]
+    with NativeServer(mem_budget=footprint(probs[0]) + 1024, max_active=8, tol=1e-10) as S:
+        rep = S.run([(0.0, p) for p in probs])
+    assert [r.status for r in rep["results"]] == [0, 0, 0]
+    assert rep["peak_concurrent_solves"] == 1
