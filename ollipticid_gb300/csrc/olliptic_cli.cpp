@@ -31,6 +31,7 @@
 // stderr.
 #include "olgpu.h"
 
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -251,6 +252,193 @@ int fail(olgpu_status st, const char *what)
   return (int)st;
 }
 
+bool file_exists(const std::string &name)
+{
+  FILE *f = std::fopen(name.c_str(), "r");
+  if (f) std::fclose(f);
+  return f != nullptr;
+}
+
+bool read_file(const std::string &name, std::string &text)
+{
+  FILE *f = std::fopen(name.c_str(), "rb");
+  if (!f) return false;
+  char buf[1 << 16];
+  size_t n;
+  text.clear();
+  while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+  std::fclose(f);
+  return true;
+}
+
+// Reads the next number the way `stream >> double` does (leading white space
+// skipped); false at the end of the text or on a token that is no number.
+bool next_number(const std::string &t, size_t &pos, double &v)
+{
+  while (pos < t.size() && std::isspace((unsigned char)t[pos])) pos++;
+  if (pos >= t.size()) return false;
+  char *end = nullptr;
+  v = std::strtod(t.c_str() + pos, &end);
+  if (end == t.c_str() + pos) return false;
+  pos = (size_t)(end - t.c_str());
+  return true;
+}
+
+// u at the points, each point checked against the largest box as the
+// exporters do ("bam grid bigger than Olliptic grid": exit status 1).
+int export_values(olgpu_hierarchy *h, int ord, const std::vector<double> &xyz, std::vector<double> &val)
+{
+  val.assign(xyz.size() / 3, 0.0);
+  if (val.empty()) return 0;
+  const olgpu_status st = olgpu_interpolate(h, -1, xyz.data(), (long long)val.size(), ord, val.data());
+  if (st != OLGPU_OK) return fail(st, "export");
+  for (size_t q = 0; q < val.size(); q++)
+    if (std::isnan(val[q])) {
+      std::printf("X: %e\tY: %e\tZ: %e\n", xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]);
+      std::printf("Error: bam grid bigger than Olliptic grid\n");
+      return 1;
+    }
+  return 0;
+}
+
+// elliptic::IO_bam (src/output.cc:377-410) and multigrid::Print_IO_BAM
+// (src/multigrid.cc:990-1120): the files <prefix><level><"", a..e> that exist,
+// level by level until a level has none; in each, every record "x y z val" is
+// rewritten in place, from the record's first byte, as x, y, z (%16.9e,
+// %17.9e, %17.9e) and u there (%24.15e), and reading resumes one byte after
+// the old value.  A file with a point outside the largest box is left as it
+// was (the reference has rewritten the records before that point when it
+// stops).
+int export_bam(olgpu_hierarchy *h, int ord, const std::string &prefix)
+{
+  static const char *ending[6] = {"", "a", "b", "c", "d", "e"};
+  std::vector<std::string> files;
+  for (int level = 0;; level++) {
+    int found = 0;
+    for (const char *e : ending) {
+      const std::string f = prefix + std::to_string(level) + e;
+      if (file_exists(f)) {
+        std::printf("File found: %s\n", f.c_str());
+        files.push_back(f);
+        found++;
+      }
+    }
+    if (!found) break;
+  }
+  for (const std::string &name : files) {
+    std::string t;
+    if (!read_file(name, t)) continue;
+    std::printf("reading from: %s\n", name.c_str());
+    // the records and where each starts and ends, read as the exporter does:
+    // the positions do not move when a rewrite has another length
+    std::vector<size_t> start, after;
+    std::vector<double> xyz;
+    size_t pos = 0;
+    for (;;) {
+      const size_t r1 = pos;
+      double x, y, z, v;
+      size_t q = pos;
+      if (!next_number(t, q, x) || !next_number(t, q, y) || !next_number(t, q, z) || !next_number(t, q, v)) break;
+      start.push_back(r1);
+      after.push_back(q);
+      xyz.insert(xyz.end(), {x, y, z});
+      pos = q + 1;
+      if (pos > t.size()) break;
+    }
+    std::vector<double> val;
+    const int rc = export_values(h, ord, xyz, val);
+    if (rc) return rc;
+    // rewrite record by record; a later record is read from the text as the
+    // earlier rewrites left it, as the reference's in-place stream does
+    std::string out = t;
+    pos = 0;
+    for (size_t rrec = 0;; rrec++) {
+      const size_t r1 = pos;
+      double x, y, z, v;
+      size_t q = pos;
+      if (!next_number(out, q, x) || !next_number(out, q, y) || !next_number(out, q, z) || !next_number(out, q, v))
+        break;
+      double u = rrec < val.size() && x == xyz[3 * rrec] && y == xyz[3 * rrec + 1] && z == xyz[3 * rrec + 2]
+                     ? val[rrec]
+                     : std::nan("");
+      if (std::isnan(u)) {   // the text changed under the rewrite: read this point afresh
+        std::vector<double> p1 = {x, y, z}, v1;
+        const int rc1 = export_values(h, ord, p1, v1);
+        if (rc1) return rc1;
+        u = v1[0];
+      }
+      char rec[160];
+      const int n = std::snprintf(rec, sizeof rec, "%16.9e%17.9e%17.9e%24.15e", x, y, z, u);
+      if (r1 + n > out.size()) out.resize(r1 + n, ' ');
+      out.replace(r1, n, rec, n);
+      pos = q + 1;
+      if (pos > out.size()) break;
+    }
+    FILE *f = std::fopen(name.c_str(), "wb");
+    if (!f) return (int)OLGPU_ERR_INVALID_ARG;
+    std::fwrite(out.data(), 1, out.size(), f);
+    std::fclose(f);
+  }
+  return 0;
+}
+
+// elliptic::IO_Zcode (src/output.cc:412-618) and multigrid::Print_IO_Zcode
+// (src/multigrid.cc:1123-1180): the files <prefix><LL>-0<b>.mgid (two-digit
+// level, b = 0..5) level by level until a level has none, then the shells
+// <prefix>SH-{xm,xp,ym,yp,zm,zp}.mgid; each record "x y z val" becomes the
+// line "x y z u" (%.16e) of <file>_m.  The reference's read loop ends on the
+// end-of-file flag, so when the last record is followed by white space it
+// is written twice; that is kept.
+int export_zcode(olgpu_hierarchy *h, int ord, const std::string &prefix)
+{
+  std::vector<std::string> files;
+  for (int level = 0;; level++) {
+    int found = 0;
+    for (int b = 0; b < 6; b++) {
+      char f[32];
+      std::snprintf(f, sizeof f, "%s%d-0%d.mgid", level < 10 ? "0" : "", level, b);
+      const std::string name = prefix + f;
+      if (file_exists(name)) {
+        std::printf("File found: %s\n", name.c_str());
+        files.push_back(name);
+        found++;
+      }
+    }
+    if (!found) break;
+  }
+  for (const char *sh : {"SH-xm.mgid", "SH-xp.mgid", "SH-ym.mgid", "SH-yp.mgid", "SH-zm.mgid", "SH-zp.mgid"})
+    if (file_exists(prefix + sh)) {
+      std::printf("File found: %s\n", (prefix + sh).c_str());
+      files.push_back(prefix + sh);
+    }
+  for (const std::string &name : files) {
+    std::string t;
+    if (!read_file(name, t)) continue;
+    std::printf("reading from: %s\n", name.c_str());
+    std::vector<double> xyz;
+    size_t pos = 0;
+    bool trailing = false;   // white space after the last record
+    for (;;) {
+      double x, y, z, v;
+      size_t q = pos;
+      if (!next_number(t, q, x) || !next_number(t, q, y) || !next_number(t, q, z) || !next_number(t, q, v)) break;
+      xyz.insert(xyz.end(), {x, y, z});
+      pos = q;
+      trailing = pos < t.size();
+    }
+    if (!xyz.empty() && trailing) xyz.insert(xyz.end(), xyz.end() - 3, xyz.end());
+    std::vector<double> val;
+    const int rc = export_values(h, ord, xyz, val);
+    if (rc) return rc;
+    FILE *f = std::fopen((name + "_m").c_str(), "w");
+    if (!f) return (int)OLGPU_ERR_INVALID_ARG;
+    for (size_t q = 0; q < val.size(); q++)
+      std::fprintf(f, "%.16e %.16e %.16e %.16e\n", xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2], val[q]);
+    std::fclose(f);
+  }
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
@@ -323,6 +511,13 @@ int main(int argc, char **argv)
                 boxes[g].ny, boxes[g].nz, boxes[g].xi, boxes[g].yi, boxes[g].zi, boxes[g].dx);
   if (A.yes({"-plan"})) return 0;
 
+  {   // interface.cc:1168-1176: -iob needs -iof
+    const char *iof = A.find({"-iof", "--io-bam-file"});
+    if (A.yes({"-iob", "--io-bam"}) && (!iof || !std::strcmp(iof, "none"))) {
+      std::printf("\n\n*** Error: Missing file.\n");
+      return 1;
+    }
+  }
   // the output directory exists from start-up on, as the reference's
   const char *o = A.find({"-o", "--out-dir"});
   const std::string out = o ? o : "Output";
@@ -402,6 +597,11 @@ int main(int argc, char **argv)
     }
     std::printf("done\n");
   }
+  // initial data for other codes (main.cc:133-141): u at their grid points
+  const char *iof = A.find({"-iof", "--io-bam-file"});
+  int rc = 0;
+  if (A.yes({"-iob", "--io-bam"})) rc = export_bam(h, p.order + 1, iof);
+  if (!rc && A.yes({"-ioZ", "--io-Zcode"})) rc = export_zcode(h, p.order + 1, iof ? iof : "none");
   olgpu_hierarchy_destroy(h);
-  return 0;
+  return rc;
 }

@@ -65,6 +65,14 @@ def test_output_directory_is_rotated_like_the_reference(cli, tmp_path):
     assert not (tmp_path / "Res" / "marker").exists()
 
 
+def test_bam_export_needs_a_file(cli, tmp_path):
+    """interface.cc:1168-1176: -iob yes without -iof is refused before any work."""
+    r = run(cli, "-eq Punctures -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 -iob yes", check=False,
+            cwd=str(tmp_path))
+    assert r.returncode == 1 and "Missing file" in r.stdout
+    assert not (tmp_path / "Output").exists()
+
+
 def test_other_equations_are_refused(cli):
     r = run(cli, "-eq Poisson -N 33", check=False)
     assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
