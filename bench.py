@@ -358,6 +358,34 @@ def run_convergence():
     return out
 
 
+def run_approx_start():
+    """The benchmark binary solved from the reference's analytic puncture
+    approximation (elliptic::ApproximateID, olgpu_approximate_id) instead of
+    u = 0, plain FP64 and mixed precision, each to the same residual by the
+    reference's stop rule; cycles and solves/s beside the zero start."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
+    out = {"workload": "binary_O4_N65_l9_L1000_tol1e-11, FP64 and mixed, zero and approximate start"}
+    with og.Elliptic(P) as E:
+        for mixed, key in ((False, "plain_fp64"), (True, "mixed")):
+            E.set_precision(mixed)
+            row = {}
+            for start in ("zero", "approx"):
+                best = None
+                for _ in range(3):
+                    if start == "approx":
+                        E.ApproximateID()
+                    else:
+                        E.reset()
+                    rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=300)
+                    best = E.last_device_ms if best is None else min(best, E.last_device_ms)
+                row[start] = {"cycles": rep.cycles, "final_res": rep.final_res, "ms_per_solve": best,
+                              "solves_per_s": 1000.0 / best}
+            out[key] = row
+    return out
+
+
 def run_batched(args, count: int = 16, group: int = 16, tuned=None):
     """Seeded batched binaries (mixed precision, tol 1e-10): solves/s when
     `group` solves run concurrently, and the same instances one at a time."""
@@ -514,13 +542,14 @@ def run_gpu(args, rank: int, world: int, local: int):
     # ---- the same workload with the mixed-precision cycle
     mixed = run_mixed(E, P, args, dev, u_fix, adm_fix)
 
-    concurrent = batched = served = config3 = convergence = None
+    concurrent = batched = served = config3 = convergence = approx_start = None
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, u_fix, adm_fix, value / world)
         batched = run_batched(args, tuned=autotune.tune(P, concurrency=16))
         config3 = run_config3()
         convergence = run_convergence()
+        approx_start = run_approx_start()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
 
@@ -566,7 +595,7 @@ def run_gpu(args, rank: int, world: int, local: int):
             "accuracy": {"max_abs_u_minus_fixed_point": err_fp64,
                          "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served, "config3": config3,
-            "convergence": convergence,
+            "convergence": convergence, "approx_start": approx_start,
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk,
         }

@@ -147,14 +147,17 @@ olgpu_status olgpu_level_norms(const olgpu_hierarchy *h, int cycle, double *pre,
  * box < 0: each point is read from the last box, in level order, whose
  * interior (no ghost layers) holds it, from the largest box when none does,
  * and is NaN outside the largest box (the reference prints no line there);
- * box >= 0: every point is read from that box.  The value is the node value
+ * box >= 0: every point is read from that box.  With box < 0 only the boxes
+ * of levels >= first_level take part: 0 as the V-cycle's hierarchy prints;
+ * olgpu_mgrid_levels() for the analytic method's (elliptic::ApproximateID),
+ * whose hierarchy has no multigrid coarse grids.  The value is the node value
  * where the point coincides with a node, else the Lagrange sum over ord+1
  * nodes per axis (the reference prints with ord = order + 1), window clamped
  * to the box.  xyz holds npts (x, y, z) triples and out npts values, both
  * host memory; the gather runs on the device, ordered after the cycles
  * already enqueued. */
-olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, long long npts, int ord,
-                               double *out);
+olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, const double *xyz, long long npts,
+                               int ord, double *out);
 
 /* Asynchronous stepping, for hosts that drive several solves at once (each
  * hierarchy has its own CUDA stream, so cycles of different hierarchies run
@@ -261,6 +264,17 @@ olgpu_status olgpu_server_poll(olgpu_server *s, long long id, int wait, int *don
 olgpu_status olgpu_server_stats(olgpu_server *s, int *active, int *building, int *waiting, int *peak_active);
 /* Stops the threads, finishes nothing more and frees every hierarchy it holds. */
 olgpu_status olgpu_server_destroy(olgpu_server *s);
+
+/* elliptic::ApproximateID (src/elliptic.cc:1977-2226, the reference's
+ * "-m AppPuncture" method): u on every point of every box becomes the
+ * perturbative puncture solution (spin, momentum and cross terms summed over
+ * the punctures), the work fields are reset as by olgpu_reset.  as_guess = 0
+ * evaluates the formula as the reference writes it (what -m AppPuncture
+ * prints); as_guess != 0 takes the momentum term's small-distance limit from
+ * its series (the formula cancels to rounding noise of order 1e10 on a
+ * puncture that sits on a grid node).  As a start for olgpu_solve it leaves
+ * the fixed point unchanged and takes cycles off. */
+olgpu_status olgpu_approximate_id(olgpu_hierarchy *h, int as_guess);
 
 /* Timing aids. */
 /* device time of the last olgpu_solve / olgpu_vcycle in ms */

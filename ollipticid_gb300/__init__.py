@@ -239,6 +239,12 @@ class Elliptic:
     def reset(self):
         check(self.lib.olgpu_reset(self._h))
 
+    def ApproximateID(self, as_guess: bool = True):
+        """u = the perturbative puncture solution everywhere (elliptic::
+        ApproximateID); a starting guess that leaves the fixed point as it is
+        (as_guess=False: the formula exactly as the reference evaluates it)."""
+        check(self.lib.olgpu_approximate_id(self._h, 1 if as_guess else 0))
+
     @property
     def ADM_mass(self) -> List[float]:
         out = (C.c_double * _abi.MAX_BH)()
@@ -254,16 +260,17 @@ class Elliptic:
                                          post.ctypes.data_as(C.POINTER(C.c_double))))
         return pre, post
 
-    def interpolate(self, points, ord: Optional[int] = None, box: int = -1) -> np.ndarray:
+    def interpolate(self, points, ord: Optional[int] = None, box: int = -1, first_level: int = 0) -> np.ndarray:
         """u at (npts, 3) points, as the reference prints it (Print_Interpol_1D
         / _2D with box=-1: the finest box whose interior holds each point, NaN
         outside the largest box; ffunction::Print_1D with box >= 0).  ord+1
         Lagrange nodes per axis, default order + 1 like the reference's
-        printout."""
+        printout.  first_level: with box=-1, only boxes of that level and
+        finer take part (mgrid_levels for the analytic method's printout)."""
         pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
         out = np.empty(len(pts), dtype=np.float64)
         k = self.problem.order + 1 if ord is None else int(ord)
-        check(self.lib.olgpu_interpolate(self._h, int(box), pts.ctypes.data_as(C.c_void_p), len(pts), k,
+        check(self.lib.olgpu_interpolate(self._h, int(box), int(first_level), pts.ctypes.data_as(C.c_void_p), len(pts), k,
                                          out.ctypes.data_as(C.c_void_p)))
         return out
 

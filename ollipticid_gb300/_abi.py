@@ -90,8 +90,9 @@ SIGNATURES = {
     "olgpu_vcycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(StopRule), C.POINTER(Report)]),
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "olgpu_approximate_id": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_level_norms": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
-    "olgpu_interpolate": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "olgpu_interpolate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
     "olgpu_cycle_launch": (C.c_int, [C.c_void_p]),
     "olgpu_cycle_poll": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "olgpu_solve_many": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(StopRule), C.POINTER(Report)]),

@@ -1202,6 +1202,105 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
 }
 
 // ----------------------------------------------------------------------------
+// elliptic::ApproximateID (src/elliptic.cc:1977-2226): the perturbative
+// puncture solution, summed over the punctures on every point of every box:
+// with R = 2 r / m and l = 1 / (1 + R), the spin part
+//   J^2 (u0j + u2j R^2 P2(mu_S)),  u0j = (l + l^2 + l^3 - 4 l^4 + 2 l^5) / 40,
+//   u2j = -l^5 / 20,  J = 4 S / m^2,
+// the momentum part
+//   P^2 (u0p + u2p P2(mu_P)),  P = 2 p / m,
+//   u0p = (5/32) (l - 2 l^2 + 2 l^3 - l^4 + l^5 / 5),
+//   u2p = (15 l + 132 l^2 + 53 l^3 + 96 l^4 + 82 l^5 + 84 (l^5 + ln(l) / R) / R) / (80 R),
+// and the cross term (P x J) . (2 x / m) (1 + 5 R + 10 R^2) l^5 / 80; P2 is
+// the Legendre polynomial of the cosine between the point's direction and
+// the spin (momentum), 0 where that vector vanishes; r below 1e-11 is taken
+// as 1e-10.  Products, quotients and sums are rounded one by one in the
+// reference's order; near a puncture the u2p bracket cancels (about 1/R^2
+// amplification of rounding), so its value there is only as good as that.
+// With `stable` (a starting guess rather than the reference's printout) u2p
+// below R = 1e-3 takes the leading term of its series instead: the bracket
+// is R^3 / 5 + O(R^4), so u2p = R^2 / 400 + O(R^3), where the formula as
+// written returns rounding noise of order 1e10 on a puncture that sits on
+// a grid node (r clamped to 1e-10).
+// ----------------------------------------------------------------------------
+__device__ double dev_approx_u(const PunctureParams &P, double x, double y, double z, bool stable)
+{
+  double u = 0.0;
+  for (int i = 0; i < P.numbh && P.mp[i] != 0.0; i++) {
+    const double sbl = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(P.sx[i], P.sx[i]), __dmul_rn(P.sy[i], P.sy[i])),
+                                            __dmul_rn(P.sz[i], P.sz[i])));
+    const double imass = __ddiv_rn(1.0, P.mp[i]);
+    const double imass2 = __dmul_rn(imass, imass);
+    const double Jx = __dmul_rn(__dmul_rn(4.0, P.sx[i]), imass2);
+    const double Jy = __dmul_rn(__dmul_rn(4.0, P.sy[i]), imass2);
+    const double Jz = __dmul_rn(__dmul_rn(4.0, P.sz[i]), imass2);
+    const double J2 = __dadd_rn(__dadd_rn(__dmul_rn(Jx, Jx), __dmul_rn(Jy, Jy)), __dmul_rn(Jz, Jz));
+    const double pbl = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(P.px[i], P.px[i]), __dmul_rn(P.py[i], P.py[i])),
+                                            __dmul_rn(P.pz[i], P.pz[i])));
+    const double Px = __dmul_rn(__dmul_rn(2.0, P.px[i]), imass);
+    const double Py = __dmul_rn(__dmul_rn(2.0, P.py[i]), imass);
+    const double Pz = __dmul_rn(__dmul_rn(2.0, P.pz[i]), imass);
+    const double P2 = __dadd_rn(__dadd_rn(__dmul_rn(Px, Px), __dmul_rn(Py, Py)), __dmul_rn(Pz, Pz));
+    const double xi = __dsub_rn(x, P.x[i]), yi = __dsub_rn(y, P.y[i]), zi = __dsub_rn(z, P.z[i]);
+    double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(xi, xi), __dmul_rn(yi, yi)), __dmul_rn(zi, zi)));
+    if (fabs(r) <= 0.00000000001) r = 0.0000000001;
+    const double Rx = __dmul_rn(__dmul_rn(2.0, xi), imass);
+    const double Ry = __dmul_rn(__dmul_rn(2.0, yi), imass);
+    const double Rz = __dmul_rn(__dmul_rn(2.0, zi), imass);
+    const double R = __dmul_rn(__dmul_rn(2.0, r), imass);
+    const double l1 = __ddiv_rn(1.0, __dadd_rn(1.0, R));
+    const double l2 = __dmul_rn(l1, l1), l3 = __dmul_rn(l2, l1), l4 = __dmul_rn(l3, l1), l5 = __dmul_rn(l4, l1);
+    const double u0j = __dmul_rn(
+        0.025, __dadd_rn(__dsub_rn(__dadd_rn(__dadd_rn(l1, l2), l3), __dmul_rn(4.0, l4)), __dmul_rn(2.0, l5)));
+    const double u2j = __dmul_rn(-0.05, l5);
+    double muj = 0.0;
+    if (sbl != 0.0 && r != 0.0)
+      muj = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(P.sx[i], xi), __dmul_rn(P.sy[i], yi)), __dmul_rn(P.sz[i], zi)),
+                      __dmul_rn(r, sbl));
+    const double PL2j = __dmul_rn(0.5, __dsub_rn(__dmul_rn(__dmul_rn(3.0, muj), muj), 1.0));
+    const double uj = __dmul_rn(J2, __dadd_rn(u0j, __dmul_rn(__dmul_rn(__dmul_rn(u2j, R), R), PL2j)));
+    const double u0p = __dmul_rn(
+        0.15625, __dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(l1, __dmul_rn(2.0, l2)), __dmul_rn(2.0, l3)), l4),
+                           __dmul_rn(0.2, l5)));
+    double br = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(15.0, l1), __dmul_rn(132.0, l2)),
+                                              __dmul_rn(53.0, l3)), __dmul_rn(96.0, l4)), __dmul_rn(82.0, l5));
+    br = __dadd_rn(br, __ddiv_rn(__dmul_rn(84.0, __dadd_rn(l5, __ddiv_rn(log(l1), R))), R));
+    double u2p = __ddiv_rn(__dmul_rn(0.0125, br), R);
+    if (stable && R < 1e-3) u2p = __dmul_rn(0.0025, __dmul_rn(R, R));
+    double mup = 0.0;
+    if (pbl != 0.0 && r != 0.0)
+      mup = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(P.px[i], xi), __dmul_rn(P.py[i], yi)), __dmul_rn(P.pz[i], zi)),
+                      __dmul_rn(r, pbl));
+    const double PL2p = __dmul_rn(0.5, __dsub_rn(__dmul_rn(__dmul_rn(3.0, mup), mup), 1.0));
+    const double up = __dmul_rn(P2, __dadd_rn(u0p, __dmul_rn(u2p, PL2p)));
+    const double X0 = __dsub_rn(__dmul_rn(Py, Jz), __dmul_rn(Pz, Jy));
+    const double X1 = __dsub_rn(__dmul_rn(Pz, Jx), __dmul_rn(Px, Jz));
+    const double X2 = __dsub_rn(__dmul_rn(Px, Jy), __dmul_rn(Py, Jx));
+    const double dotr = __dadd_rn(__dadd_rn(__dmul_rn(X0, Rx), __dmul_rn(X1, Ry)), __dmul_rn(X2, Rz));
+    const double poly = __dadd_rn(__dadd_rn(1.0, __dmul_rn(5.0, R)), __dmul_rn(__dmul_rn(10.0, R), R));
+    const double uc = __dmul_rn(__dmul_rn(__dmul_rn(0.0125, dotr), poly), l5);
+    u = __dadd_rn(u, __dadd_rn(__dadd_rn(uj, up), uc));
+  }
+  return u;
+}
+
+__global__ void __launch_bounds__(256) k_approx_id(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                   const double *__restrict__ crd, PunctureParams P, int stable)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
+  const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
+               z = crd[B.coord_off + B.n[0] + B.n[1] + k];
+  F.f[F_U][B.off + t] = dev_approx_u(P, x, y, z, stable != 0);
+}
+
+// ----------------------------------------------------------------------------
 // K7: u at each puncture by 4th-order Lagrange on the finest box (ADM mass)
 // ----------------------------------------------------------------------------
 struct AdmJob {
@@ -1323,9 +1422,9 @@ __device__ double ib_lagrange(const InterpBox &B, int a, double t, int i, int ni
 }
 
 // One thread per point.  box >= 0: that box; box < 0: the printed-cut rule
-// with `base` the largest box (NaN outside it).
-__global__ void __launch_bounds__(128) k_interp_points(const InterpBox *__restrict__ boxes, int nboxes, int base,
-                                                       int box, const double *__restrict__ u,
+// over boxes first .. nboxes-1 with `base` the largest (NaN outside it).
+__global__ void __launch_bounds__(128) k_interp_points(const InterpBox *__restrict__ boxes, int first, int nboxes,
+                                                       int base, int box, const double *__restrict__ u,
                                                        const double *__restrict__ xyz, long long npts, int ord,
                                                        double *__restrict__ out)
 {
@@ -1339,7 +1438,7 @@ __global__ void __launch_bounds__(128) k_interp_points(const InterpBox *__restri
       return;
     }
     g = base;
-    for (int b = 0; b < nboxes; b++)
+    for (int b = first; b < nboxes; b++)
       if (ib_is_in_nb(boxes[b], p)) g = b;
   }
   const InterpBox B = boxes[g];

@@ -185,6 +185,29 @@ long long blocks_faces(const DevBox &B)
   return cdiv(cols, kThreads);   // one thread per normal column of each face
 }
 
+PunctureParams puncture_params(const olgpu_problem *p)
+{
+  PunctureParams PP{};
+  PP.numbh = p->numbh;
+  PP.equation = p->equation;
+  PP.ps_case = p->ps_case;
+  for (int i = 0; i < p->numbh; i++) {
+    PP.mp[i] = p->mp[i]; PP.x[i] = p->x[i]; PP.y[i] = p->y[i]; PP.z[i] = p->z[i];
+    PP.px[i] = p->px[i]; PP.py[i] = p->py[i]; PP.pz[i] = p->pz[i];
+    PP.sx[i] = p->sx[i]; PP.sy[i] = p->sy[i]; PP.sz[i] = p->sz[i];
+  }
+  // scalar-field constants (src/elliptic.cc:71-81)
+  PP.ps_r0 = p->ps_r0;
+  PP.ps_isigma = 1 / p->ps_sigma;
+  const double a2 = p->ps_a2;
+  PP.ps_phi0 = (a2 * a2 / (1 + a2 * a2)) * p->ps_phi0;
+  PP.ps_d1 = M_PI * PP.ps_phi0 * PP.ps_phi0 * PP.ps_isigma * PP.ps_isigma;
+  PP.ps_e1 = 1 / (16 * p->ps_a2);
+  PP.ps_e2 = 4 * std::sqrt(M_PI / 3);
+  PP.ps_de1 = 4 * M_PI * PP.ps_phi0 * PP.ps_phi0 * PP.ps_isigma * PP.ps_isigma;
+  return PP;
+}
+
 // LagrangePoly (src/interpolation.cc:308-375)
 double lagrange_poly(const domain &D, int a, double t, int i, int ni, int nf)
 {
@@ -1447,24 +1470,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   if (st != OLGPU_OK) return cleanup(st);
   // coefficients on the device
   {
-    PunctureParams PP{};
-    PP.numbh = p->numbh;
-    PP.equation = p->equation;
-    PP.ps_case = p->ps_case;
-    for (int i = 0; i < p->numbh; i++) {
-      PP.mp[i] = p->mp[i]; PP.x[i] = p->x[i]; PP.y[i] = p->y[i]; PP.z[i] = p->z[i];
-      PP.px[i] = p->px[i]; PP.py[i] = p->py[i]; PP.pz[i] = p->pz[i];
-      PP.sx[i] = p->sx[i]; PP.sy[i] = p->sy[i]; PP.sz[i] = p->sz[i];
-    }
-    // scalar-field constants (src/elliptic.cc:71-81)
-    PP.ps_r0 = p->ps_r0;
-    PP.ps_isigma = 1 / p->ps_sigma;
-    const double a2 = p->ps_a2;
-    PP.ps_phi0 = (a2 * a2 / (1 + a2 * a2)) * p->ps_phi0;
-    PP.ps_d1 = M_PI * PP.ps_phi0 * PP.ps_phi0 * PP.ps_isigma * PP.ps_isigma;
-    PP.ps_e1 = 1 / (16 * p->ps_a2);
-    PP.ps_e2 = 4 * std::sqrt(M_PI / 3);
-    PP.ps_de1 = 4 * M_PI * PP.ps_phi0 * PP.ps_phi0 * PP.ps_isigma * PP.ps_isigma;
+    const PunctureParams PP = puncture_params(p);
     for (int l = 0; l < L; l++) {
       const BoxList BL = level_list(h, l, blocks_all);
       k_coefficients<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords, PP);
@@ -1763,14 +1769,16 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
 }
 
 // u at arbitrary points (the printed cuts and exports; k_interp_points).
-olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, long long npts, int ord,
-                               double *out)
+olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, const double *xyz, long long npts,
+                               int ord, double *out)
 {
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
   if (npts < 0 || (npts > 0 && (!xyz || !out))) return fail(OLGPU_ERR_INVALID_ARG, "null or negative point array");
   if (ord < 1 || ord > kMaxInterpOrd) return fail(OLGPU_ERR_INVALID_ARG, "interpolation order must be 1..15");
   const int nb = (int)h->G.boxes.size();
   if (box >= nb) return fail(OLGPU_ERR_INVALID_ARG, "box index out of range");
+  if (first_level < 0 || first_level >= h->G.levels) return fail(OLGPU_ERR_INVALID_ARG, "no such level");
+  const int first = h->G.first_box[first_level];   // boxes are level-major
   if (npts == 0) return OLGPU_OK;
   if (npts > 128LL * 0x7fffffffLL) return fail(OLGPU_ERR_INVALID_ARG, "too many points for one call");
   if (box >= 0) {
@@ -1782,7 +1790,7 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, l
         if (D.n[a] < ord + 1) return fail(OLGPU_ERR_INVALID_ARG, "a box is smaller than the window");
   }
   std::vector<InterpBox> ib(nb);
-  int base = 0;   // multigrid::multigrid: the box that strictly holds every box scanned before it
+  int base = first;   // multigrid::multigrid: the box that strictly holds every box scanned before it
   for (int g = 0; g < nb; g++) {
     const domain &D = h->G.boxes[g];
     InterpBox &B = ib[g];
@@ -1797,7 +1805,7 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, l
     const domain &C = h->G.boxes[base];
     bool holds = true;   // domain::operator< (src/domain.cc:1947-1954): C strictly inside D
     for (int a = 0; a < 3; a++) holds = holds && D.lo[a] < C.lo[a] && C.hi[a] < D.hi[a];
-    if (g > 0 && holds) base = g;
+    if (g > first && holds) base = g;
   }
   CUDA_TRY(cudaSetDevice(h->device));
   InterpBox *d_b = nullptr;
@@ -1815,8 +1823,8 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, l
     e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * (size_t)npts, cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) {
     const long long blocks = cdiv(npts, 128);
-    k_interp_points<<<(unsigned)blocks, 128, 0, h->stream>>>(d_b, nb, base, box, h->F.f[F_U], d_xyz, npts, ord,
-                                                             d_out);
+    k_interp_points<<<(unsigned)blocks, 128, 0, h->stream>>>(d_b, first, nb, base, box, h->F.f[F_U], d_xyz, npts,
+                                                             ord, d_out);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)
@@ -1826,6 +1834,25 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, const double *xyz, l
   if (e != cudaSuccess)
     return fail(e == cudaErrorMemoryAllocation ? OLGPU_ERR_OOM : OLGPU_ERR_CUDA,
                 std::string("olgpu_interpolate: ") + cudaGetErrorString(e));
+  return OLGPU_OK;
+}
+
+// elliptic::ApproximateID: u = the perturbative puncture solution on every
+// point of every box, the work fields and the acceleration history reset
+// (k_approx_id).
+olgpu_status olgpu_approximate_id(olgpu_hierarchy *h, int as_guess)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  olgpu_status st = olgpu_reset(h);
+  if (st != OLGPU_OK) return st;
+  const PunctureParams PP = puncture_params(&h->P);
+  for (int l = 0; l < h->G.levels; l++) {
+    const BoxList BL = level_list(h, l, blocks_all);
+    k_approx_id<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords, PP,
+                                                              as_guess ? 1 : 0);
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   return OLGPU_OK;
 }
 

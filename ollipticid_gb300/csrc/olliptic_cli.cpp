@@ -9,8 +9,13 @@
 // and ignored, as the reference ignores unknown flags.  Equations other than
 // Punctures / Punctures_scalar_field are refused.
 //
+// Methods (-m): Vcycle (the default) and AppPuncture (the analytic
+// approximation alone, elliptic::ApproximateID); the others are refused.
+//
 // Extra flags of this program (no reference counterpart):
 //   -gpu-mixed yes|no   mixed-precision cycles (FP32 correction around FP64)
+//   -gpu-guess approx   start the V-cycles from the analytic approximation
+//                       (the same fixed point, fewer cycles) instead of u = 0
 //   -gpu-device N       CUDA device (default: the current one)
 //   -plan yes           print the box hierarchy (no GPU needed) and exit
 //
@@ -168,7 +173,7 @@ olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis
     pts[3 * i + axis] = B.coord(axis, i);
   }
   if (interpolate) {
-    const olgpu_status st = olgpu_interpolate(h, g, pts.data(), np, ord, val.data());
+    const olgpu_status st = olgpu_interpolate(h, g, 0, pts.data(), np, ord, val.data());
     if (st != OLGPU_OK) return st;
   } else {
     std::vector<double> u((size_t)B.b.nx * B.b.ny * B.b.nz);
@@ -191,7 +196,8 @@ olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis
 // multigrid::Print_Interpol_1D along one axis: from -LD/2 by D (LD/1000 when
 // D <= 0) while <= LD/2, the other coordinates 0, points outside the largest
 // box skipped; "%.18e\t%.18e" lines, then a blank line.
-olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D, int ord, const std::string &file)
+olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D, int ord, int first_level,
+                               const std::string &file)
 {
   const double xi = -0.5 * LD, xf = 0.5 * LD, Dx = D > 0.0 ? D : LD / 1000;
   std::vector<double> pts, xs;
@@ -202,7 +208,7 @@ olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D
     xs.push_back(x);
   }
   std::vector<double> val(xs.size());
-  const olgpu_status st = olgpu_interpolate(h, -1, pts.data(), (long long)xs.size(), ord, val.data());
+  const olgpu_status st = olgpu_interpolate(h, -1, first_level, pts.data(), (long long)xs.size(), ord, val.data());
   if (st != OLGPU_OK) return st;
   FILE *f = std::fopen(file.c_str(), "a");
   if (!f) return OLGPU_ERR_INVALID_ARG;
@@ -216,7 +222,8 @@ olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D
 // multigrid::Print_Interpol_2D, the z = 0 plane: x and y from -L/4 by L/200
 // while <= L/4; "%.18e\t%.18e\t%.18e" lines, a blank line after each x and
 // one more at the end.
-olgpu_status print_interpol_xy(olgpu_hierarchy *h, double LD1, double LD2, int ord, const std::string &file)
+olgpu_status print_interpol_xy(olgpu_hierarchy *h, double LD1, double LD2, int ord, int first_level,
+                               const std::string &file)
 {
   const double x1i = -0.25 * LD1, x2i = -0.25 * LD2, x1f = 0.25 * LD1, x2f = 0.25 * LD2;
   const double Dx1 = LD1 / 200, Dx2 = LD2 / 200;
@@ -232,7 +239,7 @@ olgpu_status print_interpol_xy(olgpu_hierarchy *h, double LD1, double LD2, int o
     row_end.push_back((int)xs.size());
   }
   std::vector<double> val(xs.size());
-  const olgpu_status st = olgpu_interpolate(h, -1, pts.data(), (long long)xs.size(), ord, val.data());
+  const olgpu_status st = olgpu_interpolate(h, -1, first_level, pts.data(), (long long)xs.size(), ord, val.data());
   if (st != OLGPU_OK) return st;
   FILE *f = std::fopen(file.c_str(), "a");
   if (!f) return OLGPU_ERR_INVALID_ARG;
@@ -290,7 +297,7 @@ int export_values(olgpu_hierarchy *h, int ord, const std::vector<double> &xyz, s
 {
   val.assign(xyz.size() / 3, 0.0);
   if (val.empty()) return 0;
-  const olgpu_status st = olgpu_interpolate(h, -1, xyz.data(), (long long)val.size(), ord, val.data());
+  const olgpu_status st = olgpu_interpolate(h, -1, 0, xyz.data(), (long long)val.size(), ord, val.data());
   if (st != OLGPU_OK) return fail(st, "export");
   for (size_t q = 0; q < val.size(); q++)
     if (std::isnan(val[q])) {
@@ -463,6 +470,15 @@ int main(int argc, char **argv)
     std::fprintf(stderr, "Olliptic_gpu.x: equation %s is not on the puncture FAS path\n", equation.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
   }
+  // elliptic::Set_Method (src/elliptic.cc:229-294): V-cycles, or the
+  // analytic approximation alone (AppPuncture, elliptic::ApproximateID)
+  const char *me = A.find({"-m", "--method"});
+  const std::string method = me ? me : "Vcycle";
+  const bool approx_only = method == "AppPuncture";
+  if (method != "Vcycle" && !approx_only) {
+    std::fprintf(stderr, "Olliptic_gpu.x: method %s is not on the puncture FAS path\n", method.c_str());
+    return (int)OLGPU_ERR_INVALID_ARG;
+  }
   p.numbh = A.integer({"-NumBH", "--num-bh"}, 1);
   if (p.numbh < 1 || p.numbh > OLGPU_MAX_BH) {
     std::fprintf(stderr, "Olliptic_gpu.x: NumBH must be 1..%d\n", OLGPU_MAX_BH);
@@ -539,7 +555,39 @@ int main(int argc, char **argv)
       return fail(st, "mixed precision");
     }
   }
-  olgpu_report rep;
+  if (approx_only || A.find({"-gpu-guess"}) && !std::strcmp(A.find({"-gpu-guess"}), "approx")) {
+    st = olgpu_approximate_id(h, approx_only ? 0 : 1);
+    if (st != OLGPU_OK) {
+      olgpu_hierarchy_destroy(h);
+      return fail(st, "approximate initial data");
+    }
+  }
+  if (approx_only) {
+    // elliptic::Get_Puncture_App (src/elliptic.cc:2232-2444): u at the node
+    // at or after each puncture, added over the finest boxes that hold it
+    std::vector<double> up(p.numbh, 0.0);
+    for (int g = 0; g < nb; g++) {
+      if (boxes[g].level != nl - 1) continue;
+      const BoxGeom B{boxes[g]};
+      for (int j = 0; j < p.numbh; j++) {
+        const double q[3] = {p.x[j], p.y[j], p.z[j]};
+        if (!(B.is_in_axis(0, q[0]) && B.is_in_axis(1, q[1]) && B.is_in_axis(2, q[2]))) continue;
+        double node[3], v = 0;
+        for (int a = 0; a < 3; a++) node[a] = B.coord(a, B.locate(a, q[a]));
+        st = olgpu_interpolate(h, g, 0, node, 1, 1, &v);
+        if (st != OLGPU_OK) {
+          olgpu_hierarchy_destroy(h);
+          return fail(st, "approximate initial data");
+        }
+        up[j] += v;
+      }
+    }
+    for (int i = 0; i < p.numbh; i++)
+      std::printf(" == Approximate ID: puncture %d\n x : %.7e\t y : %.7e\t z : %.7e\t u : %.7e\n", i, p.x[i], p.y[i],
+                  p.z[i], up[i]);
+  }
+  olgpu_report rep{};
+  if (!approx_only) {
   st = olgpu_solve(h, nullptr, &rep);   // the reference stop rule
   for (int c = 0; c < rep.cycles && c < 256; c++) std::printf("  V-cycle %3d  norm %.6e\n", c + 1, rep.res[c]);
   if (st != OLGPU_OK) {
@@ -548,7 +596,8 @@ int main(int argc, char **argv)
   }
   std::printf("Solved in %d V-cycles, norm %.6e, %.3f ms on the device\n", rep.cycles, rep.final_res,
               olgpu_last_device_ms(h));
-  if (std_output) {   // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
+  }
+  if (std_output && !approx_only) {   // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
     FILE *f = std::fopen((dir + "Loo.gp").c_str(), "a");
     std::vector<double> pre(nl), post(nl);
     for (int c = 0; f && c < rep.cycles; c++) {
@@ -557,10 +606,12 @@ int main(int argc, char **argv)
     }
     if (f) std::fclose(f);
   }
-  std::printf("Puncure method: \n");
-  double adm[OLGPU_MAX_BH];
-  olgpu_adm_mass(h, adm);
-  for (int i = 0; i < p.numbh; i++) std::printf("ADM mass[%d] = %.17g\n", i, adm[i]);
+  if (!approx_only) {
+    std::printf("Puncure method: \n");
+    double adm[OLGPU_MAX_BH];
+    olgpu_adm_mass(h, adm);
+    for (int i = 0; i < p.numbh; i++) std::printf("ADM mass[%d] = %.17g\n", i, adm[i]);
+  }
 
   // elliptic::Print_Solution (src/output.cc:624-700), variable "u"
   const bool print_1d = A.logic({"-p1d", "--print-1d"}, true);
@@ -570,14 +621,18 @@ int main(int argc, char **argv)
     const int ord = p.order + 1;
     std::printf("Printing...\n");
     olgpu_status ps = OLGPU_OK;
+    // the analytic method's hierarchy has no multigrid coarse grids: its
+    // levels are the refinement levels, numbered from the base
+    const int l0 = approx_only ? mg : 0;
     if (print_1d) {
       std::vector<int> in_level(nl, 0);
       static const char *ext[3] = {".x", ".y", ".z"};
-      for (int l = 0; l < nl && ps == OLGPU_OK; l++)
+      for (int l = l0; l < nl && ps == OLGPU_OK; l++)
         for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
           if (boxes[g].level != l) continue;
           const BoxGeom B{boxes[g]};
-          const std::string stem = dir + "u-l" + std::to_string(l) + "b" + std::to_string(in_level[l]++) + "-0";
+          const std::string stem =
+              dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
           for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
             ps = print_box_cut(h, B, g, a, interpol_output, ord, stem + ext[a]);
         }
@@ -588,8 +643,8 @@ int main(int argc, char **argv)
                    Lz = A.num({"-Lz", "--length-z"}, p.L);
       static const char *ext[3] = {"u.X", "u.Y", "u.Z"};
       const double LD[3] = {Lx, Ly, Lz};
-      for (int a = 0; a < 3 && ps == OLGPU_OK; a++) ps = print_interpol_1d(h, a, LD[a], Dp, ord, dir + ext[a]);
-      if (ps == OLGPU_OK) ps = print_interpol_xy(h, Lx, Ly, ord, dir + "u.XY");
+      for (int a = 0; a < 3 && ps == OLGPU_OK; a++) ps = print_interpol_1d(h, a, LD[a], Dp, ord, l0, dir + ext[a]);
+      if (ps == OLGPU_OK) ps = print_interpol_xy(h, Lx, Ly, ord, l0, dir + "u.XY");
     }
     if (ps != OLGPU_OK) {
       olgpu_hierarchy_destroy(h);

@@ -1077,6 +1077,56 @@ static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
   return S;
 }
 
+/* elliptic::ApproximateID, src/elliptic.cc:1977-2226: u on every point of
+ * every box := the sum over the punctures of the perturbative spin,
+ * momentum and cross terms, in the reference's operation order. */
+static double approx_u(const orc_problem *p, double x, double y, double z)
+{
+  double u = 0.0;
+  for (int i = 0; i < p->numbh && p->mp[i] != 0.0; i++) {
+    double sbl = sqrt(p->sx[i] * p->sx[i] + p->sy[i] * p->sy[i] + p->sz[i] * p->sz[i]);
+    double imass = 1.0 / p->mp[i];
+    double imass2 = imass * imass;
+    double Jx = 4.0 * p->sx[i] * imass2, Jy = 4.0 * p->sy[i] * imass2, Jz = 4.0 * p->sz[i] * imass2;
+    double J2 = Jx * Jx + Jy * Jy + Jz * Jz;
+    double pbl = sqrt(p->px[i] * p->px[i] + p->py[i] * p->py[i] + p->pz[i] * p->pz[i]);
+    double Px = 2.0 * p->px[i] * imass, Py = 2.0 * p->py[i] * imass, Pz = 2.0 * p->pz[i] * imass;
+    double P2 = Px * Px + Py * Py + Pz * Pz;
+    double xi = x - p->x[i], yi = y - p->y[i], zi = z - p->z[i];
+    double r = sqrt(xi * xi + yi * yi + zi * zi);
+    if (fabs(r) <= 0.00000000001) r = 0.0000000001;
+    double Rx = 2.0 * xi * imass, Ry = 2.0 * yi * imass, Rz = 2.0 * zi * imass;
+    double R = 2.0 * r * imass;
+    double l1 = 1.0 / (1.0 + R), l2 = l1 * l1, l3 = l2 * l1, l4 = l3 * l1, l5 = l4 * l1;
+    double u0j = 0.025 * (l1 + l2 + l3 - 4.0 * l4 + 2.0 * l5);
+    double u2j = -0.05 * l5;
+    double muj = (sbl != 0.0 && r != 0.0) ? (p->sx[i] * xi + p->sy[i] * yi + p->sz[i] * zi) / (r * sbl) : 0.0;
+    double PL2j = 0.5 * (3.0 * muj * muj - 1.0);
+    double uj = J2 * (u0j + u2j * R * R * PL2j);
+    double u0p = 0.15625 * (l1 - 2.0 * l2 + 2.0 * l3 - l4 + 0.2 * l5);
+    double u2p = 0.0125 * (15.0 * l1 + 132.0 * l2 + 53.0 * l3 + 96.0 * l4 + 82 * l5 + 84.0 * (l5 + log(l1) / R) / R) / R;
+    double mup = (pbl != 0.0 && r != 0.0) ? (p->px[i] * xi + p->py[i] * yi + p->pz[i] * zi) / (r * pbl) : 0.0;
+    double PL2p = 0.5 * (3.0 * mup * mup - 1.0);
+    double up = P2 * (u0p + u2p * PL2p);
+    double X0 = Py * Jz - Pz * Jy, X1 = Pz * Jx - Px * Jz, X2 = Px * Jy - Py * Jx;
+    double uc = 0.0125 * (X0 * Rx + X1 * Ry + X2 * Rz) * (1.0 + 5.0 * R + 10.0 * R * R) * l5;
+    u += uj + up + uc;
+  }
+  return u;
+}
+
+void orc_approximate_id(orc_solver *S)
+{
+  for (int g = 0; g < S->nboxes; g++) {
+    obox *B = &S->box[g];
+    for (int k = 0; k < B->D.n[2]; k++)
+      for (int j = 0; j < B->D.n[1]; j++)
+        for (int i = 0; i < B->D.n[0]; i++)
+          B->f[F_U][IDX(B, i, j, k)] =
+              approx_u(&S->P, dom_coord(&B->D, 0, i), dom_coord(&B->D, 1, j), dom_coord(&B->D, 2, k));
+  }
+}
+
 void orc_destroy(orc_solver *S)
 {
   if (!S) return;
@@ -1137,11 +1187,13 @@ int orc_set_field(orc_solver *S, int g, const char *name, const double *in)
  * holds it (is_in_nb), l0 when none does.  box >= 0: that box, as
  * ffunction::Print_1D (src/ffunction.cc:819-960).  The value is
  * Lagrange_Interpol_In with ord+1 nodes per axis. */
-int orc_interpolate(const orc_solver *S, int box, const double *xyz, long npts, int ord, double *out)
+int orc_interpolate(const orc_solver *S, int box, int first_level, const double *xyz, long npts, int ord,
+                    double *out)
 {
-  if (box >= S->nboxes || ord < 1 || ord > 15) return -1;
-  int l0 = 0;
-  for (int g = 1; g < S->nboxes; g++) {
+  if (box >= S->nboxes || ord < 1 || ord > 15 || first_level < 0 || first_level >= S->levels) return -1;
+  const int first = S->first[first_level];
+  int l0 = first;
+  for (int g = first + 1; g < S->nboxes; g++) {
     const odom *A = &S->box[l0].D, *B = &S->box[g].D;
     int inside = 1;
     for (int a = 0; a < 3; a++) inside = inside && B->lo[a] < A->lo[a] && A->hi[a] < B->hi[a];
@@ -1156,7 +1208,7 @@ int orc_interpolate(const orc_solver *S, int box, const double *xyz, long npts, 
         continue;
       }
       g = l0;
-      for (int b = 0; b < S->nboxes; b++)
+      for (int b = first; b < S->nboxes; b++)
         if (dom_is_in_nb(&S->box[b].D, x, y, z)) g = b;
     }
     out[q] = interp_lagrange(&S->box[g], S->box[g].f[F_U], ord, x, y, z);

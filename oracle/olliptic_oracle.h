@@ -58,9 +58,13 @@ int orc_get_field(const orc_solver *s, int box, const char *name, double *out);
 int orc_set_field(orc_solver *s, int box, const char *name, const double *in);
 /* u at npts (x, y, z) points (xyz, 3*npts doubles): box < 0 follows the
  * reference's printed-cut rule (finest box whose interior holds the point,
- * NaN outside the largest box), box >= 0 reads that box; ord+1 Lagrange
- * nodes per axis.  Returns 0, or -1 on a bad argument. */
-int orc_interpolate(const orc_solver *s, int box, const double *xyz, long npts, int ord, double *out);
+ * NaN outside the largest box) over the boxes of levels >= first_level
+ * (the analytic method's hierarchy has no multigrid grids), box >= 0 reads
+ * that box; ord+1 Lagrange nodes per axis.  Returns 0, or -1 on a bad argument. */
+int orc_interpolate(const orc_solver *s, int box, int first_level, const double *xyz, long npts, int ord,
+                    double *out);
+/* elliptic::ApproximateID: u := the perturbative puncture solution on every box */
+void orc_approximate_id(orc_solver *s);
 /* one FAS V-cycle from the top level (elliptic::FASN); returns the top-level norm */
 double orc_vcycle(orc_solver *s);
 /* elliptic::Vcycle: cycles while res > eps && res < res_prev; returns cycles run */

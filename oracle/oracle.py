@@ -71,7 +71,8 @@ def load():
         L.orc_solve.restype = C.c_int
         L.orc_solve.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
         L.orc_adm.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
-        L.orc_interpolate.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p]
+        L.orc_approximate_id.argtypes = [C.c_void_p]
+        L.orc_interpolate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p]
         L.orc_set_multicolor.argtypes = [C.c_void_p, C.c_int]
         L.orc_set_coarse_cap.argtypes = [C.c_void_p, C.c_long]
         L.orc_set_wsmooth.argtypes = [C.c_void_p, C.c_int]
@@ -180,10 +181,13 @@ class Oracle:
         self.L.orc_adm(self._s, out)
         return [out[i] for i in range(self.numbh)]
 
-    def interpolate(self, points, ord: int, box: int = -1) -> np.ndarray:
+    def approximate_id(self):
+        self.L.orc_approximate_id(self._s)
+
+    def interpolate(self, points, ord: int, box: int = -1, first_level: int = 0) -> np.ndarray:
         pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
         out = np.empty(len(pts), dtype=np.float64)
-        rc = self.L.orc_interpolate(self._s, int(box), pts.ctypes.data_as(C.c_void_p), len(pts), int(ord),
+        rc = self.L.orc_interpolate(self._s, int(box), int(first_level), pts.ctypes.data_as(C.c_void_p), len(pts), int(ord),
                                     out.ctypes.data_as(C.c_void_p))
         if rc != 0:
             raise ValueError("orc_interpolate: bad argument")
