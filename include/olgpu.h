@@ -44,7 +44,11 @@ typedef enum {
   OLGPU_ERR_NO_DEVICE = 8
 } olgpu_status;
 
-typedef enum { OLGPU_EQ_PUNCTURES = 0, OLGPU_EQ_PUNCTURES_SCALAR = 1 } olgpu_equation;
+/* OLGPU_EQ_POISSON is the reference's Gaussian test (-eq Poisson,
+ * src/operator.cc:640-655, 1865-1887): Lap u + u^2 = a e^{-r^2}(a + e^{r^2/2}
+ * (r^2 - 3)), whose solution u = a e^{-r^2/2} (a = 0.004) is known; it runs
+ * on the same FAS path in FP64 and serves as a known-answer test. */
+typedef enum { OLGPU_EQ_PUNCTURES = 0, OLGPU_EQ_PUNCTURES_SCALAR = 1, OLGPU_EQ_POISSON = 2 } olgpu_equation;
 
 /* The Olliptic.x parameters of the puncture problem (src/interface.cc:73-273,
  * 748-856); -L is the full domain length and dx = L/(N-1). */

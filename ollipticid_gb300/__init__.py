@@ -24,10 +24,15 @@ __all__ = ["Problem", "Elliptic", "parse_olliptic_args", "OlgpuError", "FIELDS",
 FIELDS = ("u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v")
 
 
+# the equations on the FAS path: the puncture constraint, with a scalar
+# field, and the reference's Gaussian test (a known answer)
+EQUATIONS = {"Punctures": 0, "Punctures_scalar_field": 1, "Poisson": 2}
+
+
 @dataclass
 class Problem:
     """The Olliptic.x parameters of a puncture problem (src/interface.cc:73-273)."""
-    equation: str = "Punctures"          # or "Punctures_scalar_field"
+    equation: str = "Punctures"          # or "Punctures_scalar_field", "Poisson" (the Gaussian test)
     mp: List[float] = field(default_factory=lambda: [0.0])
     x: List[float] = field(default_factory=lambda: [0.0])
     y: List[float] = field(default_factory=lambda: [0.0])
@@ -57,7 +62,7 @@ class Problem:
 
     def to_c(self) -> _abi.Problem:
         p = _abi.Problem()
-        p.equation = 0 if self.equation == "Punctures" else 1
+        p.equation = EQUATIONS[self.equation]
         p.numbh = self.numbh
         if not 1 <= p.numbh <= _abi.MAX_BH:
             raise ValueError("NumBH must be in 1..16")
@@ -76,7 +81,7 @@ class Problem:
         d = {k: getattr(self, k) for k in ("mp", "x", "y", "z", "px", "py", "pz", "sx", "sy", "sz", "n", "L",
                                            "order", "levels", "nu1", "nu2", "tol", "ps_case", "ps_phi0", "ps_r0",
                                            "ps_sigma", "ps_a2")}
-        d["equation"] = 0 if self.equation == "Punctures" else 1
+        d["equation"] = EQUATIONS[self.equation]
         return d
 
 
@@ -95,7 +100,7 @@ def parse_olliptic_args(argv: Sequence[str]) -> Problem:
         return default
 
     eq = get(["-eq", "--equation"], str, "Punctures")
-    if eq not in ("Punctures", "Punctures_scalar_field"):
+    if eq not in EQUATIONS:
         raise ValueError(f"equation {eq!r} is not on the puncture FAS path")
     nb = get(["-NumBH", "--num-bh"], int, 1)
     P = Problem(equation=eq)

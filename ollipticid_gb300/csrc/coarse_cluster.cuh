@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
   }
   double *gu = F.f[F_U] + B.off;
   const double *gb = F.f[F_B] + B.off, *gc = F.f[F_C] + B.off, *gs = F.f[F_RHO] + B.off;
-  const double *gd = EQ ? F.f[F_D] + B.off : nullptr, *ge = EQ ? F.f[F_E] + B.off : nullptr;
+  const double *gd = EQ == 1 ? F.f[F_D] + B.off : nullptr, *ge = EQ == 1 ? F.f[F_E] + B.off : nullptr;
   for (int p = threadIdx.x; p < (kz1 - kz0) * n01; p += blockDim.x) su[p] = gu[(long long)kz0 * n01 + p];
   for (int t = threadIdx.x; t < n0 + n1 + n2; t += blockDim.x) {
     const int a = t < n0 ? 0 : t < n0 + n1 ? 1 : 2;
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
                             (U(i, j, k + 1) - 2.0 * c0 + U(i, j, k - 1)) * B.idx2[2];
         const long long p = ((long long)k * n1 + j) * n0 + i;
         double op, dop;
-        point_op<EQ>(lapv, B.dulap, c0, gb[p], gc[p], EQ ? gd[p] : 0.0, EQ ? ge[p] : 0.0, op, dop);
+        point_op<EQ>(lapv, B.dulap, c0, gb[p], gc[p], EQ == 1 ? gd[p] : 0.0, EQ == 1 ? ge[p] : 0.0, op, dop);
         const double R = op - gs[p];
         const double un = c0 - omega * (R * step_inverse(dop));
         U(i, j, k) = un;

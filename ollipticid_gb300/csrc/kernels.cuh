@@ -143,6 +143,11 @@ __device__ __forceinline__ void point_op(double lapv, double dl, double uu, doub
   const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
   op = lapv + t7;
   dop = dl - 7.0 * t7 * iq;                  // -7 b / (c+u)^8
+  if (EQ == 2) {   // the Gaussian test: poisson_OP / _duOP, include/elliptic.h:359-366
+    op = lapv + uu * uu;
+    dop = dl + 2.0 * uu;
+    return;
+  }
   if (EQ == 1) {
     const double q2 = q * q;
     const double q4 = q2 * q2;
@@ -330,7 +335,7 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
       const double lv = lap<ORD>(u, p, sy, sz, B);
       double op, dop;
       point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
-                   EQ ? F.f[F_D][B.off + p] : 0.0, EQ ? F.f[F_E][B.off + p] : 0.0, op, dop);
+                   EQ == 1 ? F.f[F_D][B.off + p] : 0.0, EQ == 1 ? F.f[F_E][B.off + p] : 0.0, op, dop);
       const double R = op - F.f[F_RHO][B.off + p];
       const double un = u[p] - R * step_inverse(dop);
       u[p] = un;
@@ -360,7 +365,7 @@ __global__ void __launch_bounds__(256) k_apply_op(BoxList L, const DevBox *__res
   const double lv = lap<ORD>(u, p, B.n[0], (long long)B.n[0] * B.n[1], B);
   double op, dop;
   point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
-               EQ ? F.f[F_D][B.off + p] : 0.0, EQ ? F.f[F_E][B.off + p] : 0.0, op, dop);
+               EQ == 1 ? F.f[F_D][B.off + p] : 0.0, EQ == 1 ? F.f[F_E][B.off + p] : 0.0, op, dop);
   F.f[F_R][B.off + p] = op;
 }
 
@@ -955,7 +960,7 @@ __global__ void __launch_bounds__(256) k_set_in_op(const XferJob *__restrict__ j
     const double lv = lap<ORD>(u, tp, T.n[0], (long long)T.n[0] * T.n[1], T);
     double op, dop;
     point_op<EQ>(lv, T.dulap, u[tp], F.f[F_B][T.off + tp], F.f[F_C][T.off + tp],
-                 EQ ? F.f[F_D][T.off + tp] : 0.0, EQ ? F.f[F_E][T.off + tp] : 0.0, op, dop);
+                 EQ == 1 ? F.f[F_D][T.off + tp] : 0.0, EQ == 1 ? F.f[F_E][T.off + tp] : 0.0, op, dop);
     rr = op;
   }
   F.f[F_RHO][T.off + tp] = F.f[F_W][S.off + sp] + rr;
@@ -993,7 +998,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
   const long long np = (long long)B.n[0] * B.n[1] * B.n[2];
   double *gu = F.f[F_U] + B.off;
   const double *gb = F.f[F_B] + B.off, *gc = F.f[F_C] + B.off, *gs = F.f[F_RHO] + B.off;
-  const double *gd = EQ ? F.f[F_D] + B.off : nullptr, *ge = EQ ? F.f[F_E] + B.off : nullptr;
+  const double *gd = EQ == 1 ? F.f[F_D] + B.off : nullptr, *ge = EQ == 1 ? F.f[F_E] + B.off : nullptr;
   for (long long p = threadIdx.x; p < np; p += blockDim.x) su[p] = gu[p];
   __syncthreads();
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
@@ -1051,7 +1056,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
         const long long p = pidx(B, i, j, k);
         const double lv = lap<2>(su, p, sy, sz, B);
         double op, dop;
-        point_op<EQ>(lv, B.dulap, su[p], gb[p], gc[p], EQ ? gd[p] : 0.0, EQ ? ge[p] : 0.0, op, dop);
+        point_op<EQ>(lv, B.dulap, su[p], gb[p], gc[p], EQ == 1 ? gd[p] : 0.0, EQ == 1 ? ge[p] : 0.0, op, dop);
         const double R = op - gs[p];
         su[p] = su[p] - omega * (R * step_inverse(dop));
         rmax = fmax(rmax, fabs(R));
@@ -1193,12 +1198,57 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
   const int j = (r % B.n[1]), k = (r / B.n[1]);
   const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
+  if (P.equation == 2) {   // the Gaussian test has no puncture coefficients
+    F.f[F_B][B.off + t] = 0.0;
+    F.f[F_C][B.off + t] = 0.0;
+    return;
+  }
   F.f[F_B][B.off + t] = dev_punctures_b(P, x, y, z);
   F.f[F_C][B.off + t] = dev_punctures_c(P, x, y, z);
   if (P.equation == 1) {
     F.f[F_D][B.off + t] = dev_scalar_d(P, x, y, z);
     F.f[F_E][B.off + t] = dev_scalar_e(P, x, y, z);
   }
+}
+
+// ----------------------------------------------------------------------------
+// The Gaussian test (equation Poisson, src/operator.cc:640-655, 1865-1887):
+// u = a exp(-r^2/2), a = 0.004, solves Lap u + u^2 = a exp(-r^2) (a +
+// exp(r^2/2) (r^2 - 3)).  Initial state (Set_Coefficients, Set_Boundary,
+// src/boundary.cc:8-78): rho0 = that source on every point and then the Robin
+// boundary value 0 on the BOUNDARY (ghost) points of every box, u = the
+// Gaussian on every point.
+// ----------------------------------------------------------------------------
+__device__ double dev_gaussian_source(double x, double y, double z)
+{
+  const double r2 = x * x + y * y + z * z;
+  const double a = 0.004;
+  return a * exp(-r2) * (a + exp(0.5 * r2) * (r2 - 3.0));
+}
+
+__device__ double dev_gaussian(double x, double y, double z)
+{
+  const double r2 = x * x + y * y + z * z;
+  return 0.004 * exp(-0.5 * r2);
+}
+
+__global__ void __launch_bounds__(256) k_gaussian_init(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                       const double *__restrict__ crd)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
+  const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
+               z = crd[B.coord_off + B.n[0] + B.n[1] + k];
+  const int b = B.buf;
+  const bool ghost = i < b || j < b || k < b || i >= B.n[0] - b || j >= B.n[1] - b || k >= B.n[2] - b;
+  F.f[F_RHO][B.off + t] = ghost ? 0.0 : dev_gaussian_source(x, y, z);
+  F.f[F_U][B.off + t] = dev_gaussian(x, y, z);
 }
 
 // ----------------------------------------------------------------------------

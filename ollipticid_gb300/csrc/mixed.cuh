@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__re
       const double lv = lap<ORD>(u, t, B.n[0], (long long)B.n[0] * B.n[1], B);
       double op, dop;
       point_op<EQ>(lv, B.dulap, u[t], F.f[F_B][B.off + t], F.f[F_C][B.off + t],
-                   EQ ? F.f[F_D][B.off + t] : 0.0, EQ ? F.f[F_E][B.off + t] : 0.0, op, dop);
+                   EQ == 1 ? F.f[F_D][B.off + t] : 0.0, EQ == 1 ? F.f[F_E][B.off + t] : 0.0, op, dop);
       d = d - op;
       rabs = fabs(d);
     }
@@ -237,8 +237,8 @@ __device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, l
                                         float &dop)
 {
   const long long q = B.off + p;
-  corr_op<EQ>(lv, (float)B.dulap, G.f[G_E][q], G.f[G_A][q], G.f[G_IQ][q], EQ ? G.f[G_D][q] : 0.0f,
-              EQ ? G.f[G_E5][q] : 0.0f, op, dop);
+  corr_op<EQ>(lv, (float)B.dulap, G.f[G_E][q], G.f[G_A][q], G.f[G_IQ][q], EQ == 1 ? G.f[G_D][q] : 0.0f,
+              EQ == 1 ? G.f[G_E5][q] : 0.0f, op, dop);
 }
 
 // One multicolour pass on e (colour (i+j+k) mod (order/2+1)).
@@ -545,7 +545,7 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
   const int np = n0 * n1 * n2;
   float *ge = G.f[G_E] + B.off;
   const float *gs = G.f[G_S] + B.off, *ga = G.f[G_A] + B.off, *giq = G.f[G_IQ] + B.off;
-  const float *gd = EQ ? G.f[G_D] + B.off : nullptr, *ge5 = EQ ? G.f[G_E5] + B.off : nullptr;
+  const float *gd = EQ == 1 ? G.f[G_D] + B.off : nullptr, *ge5 = EQ == 1 ? G.f[G_E5] + B.off : nullptr;
   float *cs = se + np, *ca = se + 2 * np, *ciq = se + 3 * np, *cd = se + 4 * np, *ce5 = se + 5 * np;
   for (int p = threadIdx.x; p < np; p += blockDim.x) {
     se[p] = ge[p];
@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
         const float lv = (se[p + 1] - 2.0f * c0 + se[p - 1]) * ix2 + (se[p + sy] - 2.0f * c0 + se[p - sy]) * iy2 +
                          (se[p + sz] - 2.0f * c0 + se[p - sz]) * iz2;
         float op, dop;
-        corr_op<EQ>(lv, dl, c0, A_[p], IQ_[p], EQ ? D_[p] : 0.0f, EQ ? E5_[p] : 0.0f, op, dop);
+        corr_op<EQ>(lv, dl, c0, A_[p], IQ_[p], EQ == 1 ? D_[p] : 0.0f, EQ == 1 ? E5_[p] : 0.0f, op, dop);
         const float R = op - S_[p];
         const float en = c0 - omega * (R * rcp_fast(dop));
         se[p] = en;

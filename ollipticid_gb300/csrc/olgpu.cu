@@ -649,8 +649,10 @@ void choose_coarse_cluster(olgpu_hierarchy *h)
     for (int r = 0; r < ncta; r++)
       planes = std::max(planes, cslab_begin(r + 1, B.n[2], ncta) - cslab_begin(r, B.n[2], ncta));
     const size_t smem = sizeof(double) * (size_t)planes * B.n[0] * B.n[1];
-    const bool ok = ncta == 16 ? (cluster_fits<0, 16>(h, smem) && cluster_fits<1, 16>(h, smem))
-                               : (cluster_fits<0, 8>(h, smem) && cluster_fits<1, 8>(h, smem));
+    const bool ok = ncta == 16 ? (cluster_fits<0, 16>(h, smem) && cluster_fits<1, 16>(h, smem) &&
+                                  cluster_fits<2, 16>(h, smem))
+                               : (cluster_fits<0, 8>(h, smem) && cluster_fits<1, 8>(h, smem) &&
+                                  cluster_fits<2, 8>(h, smem));
     if (ok) {
       h->coarse_ncta = ncta;
       h->coarse_cluster_smem = smem;
@@ -1000,7 +1002,7 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   if (k == 1) {
     const DevBox &B = h->hboxes[h->G.first_box[0]];
     const size_t np = (size_t)B.n[0] * B.n[1] * B.n[2];
-    const size_t staged = sizeof(float) * np * (EQ ? 6 : 4);
+    const size_t staged = sizeof(float) * np * (EQ == 1 ? 6 : 4);
     if (staged <= kCoarseSmemMax)
       k_coarse32<EQ, true><<<1, 1024, staged, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F32, h->d_coords,
                                                             h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
@@ -1204,6 +1206,7 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
   h->launches = 0;
   if (h->equation == 1) emit_fasn<1>(h, top, top);
+  else if (h->equation == 2) emit_fasn<2>(h, top, top);
   else emit_fasn<0>(h, top, top);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -1310,7 +1313,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
   if (p->levels < 1) return fail(OLGPU_ERR_INVALID_ARG, "levels must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0) return fail(OLGPU_ERR_INVALID_ARG, "negative sweep count");
-  if (p->equation != 0 && p->equation != 1) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
+  if (p->equation < 0 || p->equation > 2) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
   if (p->equation == 1 && !(p->ps_case >= 1 && p->ps_case <= 4))
     return fail(OLGPU_ERR_INVALID_ARG, "ps_case must be 1..4");
   int ndev = 0;
@@ -1431,7 +1434,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   cudaError_t e = cudaMalloc(&h->d_arena, arena);
   if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_OOM, "device arena allocation failed"));
   for (int f = 0; f < F_NUM; f++) h->F.f[f] = h->d_arena + (size_t)f * h->total_pts;
-  if (h->equation == 0) h->F.f[F_D] = h->F.f[F_E] = nullptr;
+  if (h->equation != 1) h->F.f[F_D] = h->F.f[F_E] = nullptr;
   auto up = [&](void **dst, const void *src, size_t bytes) -> bool {
     if (bytes == 0) return true;
     if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
@@ -1458,7 +1461,9 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     const int lim = (int)kCoarseSmemMax;
     cudaError_t e1 = cudaFuncSetAttribute(k_coarse_solve<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     cudaError_t e2 = cudaFuncSetAttribute(k_coarse_solve<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    if (e1 != cudaSuccess || e2 != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, "shared memory opt-in failed"));
+    cudaError_t e3 = cudaFuncSetAttribute(k_coarse_solve<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+      return cleanup(fail(OLGPU_ERR_CUDA, "shared memory opt-in failed"));
   }
   if (!std::getenv("OLGPU_COARSE_ONE_BLOCK")) choose_coarse_cluster(h);
   // coarsest-solve tuning knobs (over-relaxation, relative stop): they change
@@ -1564,6 +1569,14 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h)
   for (int f : {F_U, F_RHO, F_R, F_W, F_WW, F_V, F_T}) CUDA_TRY(cudaMemsetAsync(h->F.f[f], 0, n, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   std::fill(h->adm, h->adm + OLGPU_MAX_BH, 0.0);
+  if (h->equation == OLGPU_EQ_POISSON) {   // the Gaussian test's initial u and source
+    for (int l = 0; l < h->G.levels; l++) {
+      const BoxList BL = level_list(h, l, blocks_all);
+      k_gaussian_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords);
+    }
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+  }
   return reset_anderson(h);
 }
 
@@ -1843,6 +1856,7 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, con
 olgpu_status olgpu_approximate_id(olgpu_hierarchy *h, int as_guess)
 {
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (h->equation == OLGPU_EQ_POISSON) return fail(OLGPU_ERR_INVALID_ARG, "the approximation is for punctures");
   olgpu_status st = olgpu_reset(h);
   if (st != OLGPU_OK) return st;
   const PunctureParams PP = puncture_params(&h->P);
@@ -1911,6 +1925,8 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
     return fail(OLGPU_ERR_INVALID_ARG, "precision must be OLGPU_PREC_FP64 or OLGPU_PREC_MIXED");
   CUDA_TRY(cudaSetDevice(h->device));
   if (precision == OLGPU_PREC_MIXED) {
+    if (h->equation == OLGPU_EQ_POISSON)
+      return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the puncture equations");
     olgpu_status st = build_mixed(h);
     if (st != OLGPU_OK) return st;
   }
@@ -1971,6 +1987,7 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
     else dispatch_smooth32<0>(h, level, sweeps);
   } else {
     if (h->equation == 1) dispatch_smooth<1>(h, level, sweeps, 0);
+    else if (h->equation == 2) dispatch_smooth<2>(h, level, sweeps, 0);
     else dispatch_smooth<0>(h, level, sweeps, 0);
   }
   CUDA_TRY(cudaEventRecord(h->ev1, h->stream));

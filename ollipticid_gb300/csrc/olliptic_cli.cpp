@@ -7,7 +7,8 @@
 // program.  Flags of the puncture FAS path are read with the reference's names
 // and defaults; flags outside it (output, printing, symmetry, MPI) are accepted
 // and ignored, as the reference ignores unknown flags.  Equations other than
-// Punctures / Punctures_scalar_field are refused.
+// Punctures / Punctures_scalar_field / Poisson (the reference's Gaussian
+// test) are refused, and so are boundary conditions other than Robin.
 //
 // Methods (-m): Vcycle (the default) and AppPuncture (the analytic
 // approximation alone, elliptic::ApproximateID); the others are refused.
@@ -466,6 +467,7 @@ int main(int argc, char **argv)
   const std::string equation = eq ? eq : "Punctures";
   if (equation == "Punctures") p.equation = OLGPU_EQ_PUNCTURES;
   else if (equation == "Punctures_scalar_field") p.equation = OLGPU_EQ_PUNCTURES_SCALAR;
+  else if (equation == "Poisson") p.equation = OLGPU_EQ_POISSON;
   else {
     std::fprintf(stderr, "Olliptic_gpu.x: equation %s is not on the puncture FAS path\n", equation.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
@@ -477,6 +479,15 @@ int main(int argc, char **argv)
   const bool approx_only = method == "AppPuncture";
   if (method != "Vcycle" && !approx_only) {
     std::fprintf(stderr, "Olliptic_gpu.x: method %s is not on the puncture FAS path\n", method.c_str());
+    return (int)OLGPU_ERR_INVALID_ARG;
+  }
+  // the boundary condition (interface.cc:272, default Dirichlet): the GPU
+  // path has the Robin condition of the puncture runs (every pars/ file
+  // passes -B Robin); another is refused rather than replaced
+  const char *bc = A.find({"-B", "--boundary"});
+  if (!bc || std::strcmp(bc, "Robin")) {
+    std::fprintf(stderr, "Olliptic_gpu.x: boundary %s is not on the GPU path (pass -B Robin)\n",
+                 bc ? bc : "Dirichlet (the default)");
     return (int)OLGPU_ERR_INVALID_ARG;
   }
   p.numbh = A.integer({"-NumBH", "--num-bh"}, 1);
@@ -606,7 +617,7 @@ int main(int argc, char **argv)
     }
     if (f) std::fclose(f);
   }
-  if (!approx_only) {
+  if (!approx_only && p.equation != OLGPU_EQ_POISSON) {   // Vcycle prints ADM for punctures only
     std::printf("Puncure method: \n");
     double adm[OLGPU_MAX_BH];
     olgpu_adm_mass(h, adm);

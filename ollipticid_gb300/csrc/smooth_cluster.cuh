@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
   const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
   const float dl = (float)B.dulap;
   const float *gs = G.f[G_S] + B.off, *ga = G.f[G_A] + B.off, *giq = G.f[G_IQ] + B.off;
-  const float *gd = EQ ? G.f[G_D] + B.off : nullptr, *ge5 = EQ ? G.f[G_E5] + B.off : nullptr;
+  const float *gd = EQ == 1 ? G.f[G_D] + B.off : nullptr, *ge5 = EQ == 1 ? G.f[G_E5] + B.off : nullptr;
   const int m0 = n0 - 2 * b, m1 = n1 - 2 * b;
   const int ka = z0 > b ? z0 : b, kb = z1 < n2 - b ? z1 : n2 - b;
   const int nk = kb > ka ? kb - ka : 0;
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
               ix2, iy2, iz2);
           const int p = k * n01 + q;
           float op, dop;
-          corr_op<EQ>(lv, dl, c, __ldg(ga + p), __ldg(giq + p), EQ ? __ldg(gd + p) : 0.0f, EQ ? __ldg(ge5 + p) : 0.0f,
+          corr_op<EQ>(lv, dl, c, __ldg(ga + p), __ldg(giq + p), EQ == 1 ? __ldg(gd + p) : 0.0f, EQ == 1 ? __ldg(ge5 + p) : 0.0f,
                       op, dop);
           const float R = op - __ldg(gs + p);
           en[u] = c - R * rcp_fast(dop);

@@ -552,12 +552,29 @@ static inline double du_deriv(const obox *B, int a, int i, int j, int k)
   return 25 * id / 12.0;
 }
 
+/* The Gaussian test, src/operator.cc:1865-1887: u = a exp(-r^2 / 2) solves
+ * Lap u + u^2 = a exp(-r^2) (a + exp(r^2 / 2) (r^2 - 3)), a = 0.004. */
+static double gaussian_source(double x, double y, double z)
+{
+  double r2 = x * x + y * y + z * z;
+  double a = 0.004;
+  return (a * exp(-r2) * (a + exp(0.5 * r2) * (r2 - 3.0)));
+}
+
+static double gaussian(double x, double y, double z)
+{
+  double r2 = x * x + y * y + z * z;
+  double a = 0.004;
+  return (a * exp(-0.5 * r2));
+}
+
 /* ------------------------------------------------------------------------ */
 /* pointwise operator: include/elliptic.h:405-445                            */
 /* ------------------------------------------------------------------------ */
 static inline double op_at(const orc_solver *S, const obox *B, long p, double lap)
 {
   const double *u = B->f[F_U], *b = B->f[F_B], *c = B->f[F_C];
+  if (S->P.equation == 2) return lap + u[p] * u[p];   /* poisson_OP, include/elliptic.h:359-362 */
   if (S->P.equation == 0) return lap + b[p] / pow(c[p] + u[p], 7);
   const double *d = B->f[F_D], *e = B->f[F_E];
   return lap + b[p] / pow(c[p] + u[p], 7) + d[p] * (c[p] + u[p]) + e[p] * pow(c[p] + u[p], 5);
@@ -566,6 +583,7 @@ static inline double op_at(const orc_solver *S, const obox *B, long p, double la
 static inline double duop_at(const orc_solver *S, const obox *B, long p, double dl)
 {
   const double *u = B->f[F_U], *b = B->f[F_B], *c = B->f[F_C];
+  if (S->P.equation == 2) return dl + 2.0 * u[p];   /* poisson_duOP */
   if (S->P.equation == 0) return dl - 7.0 * b[p] / pow(c[p] + u[p], 8);
   const double *d = B->f[F_D], *e = B->f[F_E];
   return dl - 7.0 * b[p] / pow(c[p] + u[p], 8) + d[p] + 5 * e[p] * pow(c[p] + u[p], 4);
@@ -1065,6 +1083,18 @@ static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
         for (int i = 0; i < B->D.n[0]; i++) {
           double x = dom_coord(&B->D, 0, i), y = dom_coord(&B->D, 1, j), z = dom_coord(&B->D, 2, k);
           long q = IDX(B, i, j, k);
+          if (p->equation == 2) {
+            /* the Gaussian test (src/operator.cc:640-655, 1865-1887): rho0 =
+             * Gaussian_source on every point, then the Robin boundary value
+             * 0 on the BOUNDARY points (Set_Boundary, src/boundary.cc:8-78),
+             * and u = Gaussian on every point as the initial guess */
+            const int bb = B->D.buf;
+            const int ghost = i < bb || j < bb || k < bb || i >= B->D.n[0] - bb || j >= B->D.n[1] - bb ||
+                              k >= B->D.n[2] - bb;
+            B->f[F_RHO][q] = ghost ? 0.0 : gaussian_source(x, y, z);
+            B->f[F_U][q] = gaussian(x, y, z);
+            continue;
+          }
           B->f[F_B][q] = punctures_b(p, x, y, z);
           B->f[F_C][q] = punctures_c(p, x, y, z);
           if (p->equation == 1) {

@@ -54,7 +54,7 @@ def test_output_directory_is_rotated_like_the_reference(cli, tmp_path):
     command line); a second run moves it to <dir>_prev.  No GPU is needed:
     the directory exists before the device is touched (the run then fails
     here, or solves where a GPU is present)."""
-    args = "-eq Punctures -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 -o Res -p1d no -pint no -gpu-device 9999"
+    args = "-eq Punctures -B Robin -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 -o Res -p1d no -pint no -gpu-device 9999"
     run(cli, args, check=False, cwd=str(tmp_path))
     assert (tmp_path / "Res" / "Res.run").exists()
     recorded = (tmp_path / "Res" / "Res.run").read_text().split()
@@ -67,15 +67,27 @@ def test_output_directory_is_rotated_like_the_reference(cli, tmp_path):
 
 def test_bam_export_needs_a_file(cli, tmp_path):
     """interface.cc:1168-1176: -iob yes without -iof is refused before any work."""
-    r = run(cli, "-eq Punctures -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 -iob yes", check=False,
+    r = run(cli, "-eq Punctures -B Robin -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 -iob yes", check=False,
             cwd=str(tmp_path))
     assert r.returncode == 1 and "Missing file" in r.stdout
     assert not (tmp_path / "Output").exists()
 
 
 def test_other_equations_are_refused(cli):
-    r = run(cli, "-eq Poisson -N 33", check=False)
+    r = run(cli, "-eq Bowen_York -B Robin -N 33", check=False)
     assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
+    r = run(cli, "-eq Punctures -B Robin -N 33 -m Full-Multigrid", check=False)
+    assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
+
+
+@pytest.mark.parametrize("flag", ["", "-B Dirichlet", "-B Asymptotic"])
+def test_boundaries_other_than_robin_are_refused(cli, flag, tmp_path):
+    """The reference's default boundary is Dirichlet; only Robin (what every
+    pars/ file passes) is on the GPU path, and another is refused before any
+    work rather than replaced."""
+    r = run(cli, "-eq Punctures -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 " + flag, check=False, cwd=str(tmp_path))
+    assert r.returncode != 0 and "is not on the GPU path" in r.stderr
+    assert not (tmp_path / "Output").exists()
 
 
 @pytest.mark.gpu

@@ -61,4 +61,5 @@ def test_parse_ignores_unknown_flags():
                             "-o Out -pc yes -N 65 -L 100 -O 6 -l 5".split())
     assert P.mp == [0.4, 0.6] and (P.n, P.L, P.order, P.levels) == (65, 100.0, 6, 5)
     with pytest.raises(ValueError):
-        parse_olliptic_args("-eq Poisson".split())
+        parse_olliptic_args("-eq Bowen_York".split())
+    assert parse_olliptic_args("-eq Poisson".split()).equation == "Poisson"   # the Gaussian test

@@ -1,0 +1,61 @@
+"""The Gaussian test (-eq Poisson) on the GPU: Olliptic_gpu.x prints the
+reference's cuts, and the distance from the exact solution a e^{-r^2/2} at
+each resolution is the reference's (a known answer: both are the
+discretisation error of the same discrete problem)."""
+import glob
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.test_gpu_output import box_levels
+from tests.test_oracle_poisson import cut
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "ollipticid_gb300", "_build", "Olliptic_gpu.x")
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "poisson", "*.npz")))
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=lambda p: os.path.basename(p)[:-4])
+def test_gaussian_test_matches_the_reference(path, tmp_path):
+    g = np.load(path)
+    for N in g["resolutions"]:
+        args = g["args"].item().decode() + f" -N {int(N)}"
+        run = tmp_path / f"N{int(N)}"
+        run.mkdir()
+        r = subprocess.run([CLI] + args.split() + ["-o", "Output"], cwd=str(run), capture_output=True, text=True,
+                           timeout=600)
+        assert r.returncode == 0, r.stderr
+        assert "ADM mass" not in r.stdout
+        mg = int(re.search(r"\((\d+) multigrid\)", r.stdout).group(1))
+        level_of = box_levels(args)
+        for name in ("u.X", "u.Y", "u.Z"):
+            ours = np.loadtxt(run / "Output" / name)
+            pts, want = cut(g, name, int(N))
+            assert np.array_equal(ours[:, 0], pts[:, "XYZ".index(name[-1])])
+            tol = np.where(level_of(pts) < mg, 1e-6, 1e-9)
+            assert (np.abs(ours[:, 1] - want) <= tol).all(), name
+        # the distance from the exact solution, over the points read from
+        # the solution levels (a multigrid coarse grid holds the last
+        # coarse-grid approximation there, in the reference as here)
+        a = np.loadtxt(run / "Output" / "u.X")
+        pts, want = cut(g, "u.X", int(N))
+        sol = level_of(pts) >= mg
+        exact = 0.004 * np.exp(-0.5 * a[:, 0] ** 2)
+        err, ref_err = np.max(np.abs(a[sol, 1] - exact[sol])), np.max(np.abs(want[sol] - exact[sol]))
+        assert abs(err - ref_err) <= 1e-9, (err, ref_err)
+
+
+def test_mixed_precision_is_refused_for_the_gaussian_test():
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    g = np.load(GOLDEN[0])
+    with og.Elliptic(og.parse_olliptic_args((g["args"].item().decode() + " -N 25").split())) as E:
+        with pytest.raises(_abi.OlgpuError):
+            E.set_precision(True)
+        rep = E.Solve()
+        assert rep.status == 0
