@@ -50,6 +50,12 @@ typedef enum {
  * on the same FAS path in FP64 and serves as a known-answer test. */
 typedef enum { OLGPU_EQ_PUNCTURES = 0, OLGPU_EQ_PUNCTURES_SCALAR = 1, OLGPU_EQ_POISSON = 2 } olgpu_equation;
 
+/* The outer boundary condition (-B, src/boundary.cc:447-1535): Robin, u ~
+ * u_inf + C / r^n (what the puncture pars/ files use), or Dirichlet, u fixed
+ * to the boundary function on the outer ghost layers (the reference's
+ * default without -B).  olgpu_problem_defaults picks Robin. */
+typedef enum { OLGPU_BC_ROBIN = 0, OLGPU_BC_DIRICHLET = 1 } olgpu_boundary;
+
 /* The Olliptic.x parameters of the puncture problem (src/interface.cc:73-273,
  * 748-856); -L is the full domain length and dx = L/(N-1). */
 typedef struct {
@@ -67,6 +73,7 @@ typedef struct {
   double tol;                   /* -s                                   */
   int ps_case;                  /* -psc                                 */
   double ps_phi0, ps_r0, ps_sigma, ps_a2;   /* -phi0 -r0 -sigma -a2     */
+  int boundary;                 /* -B: olgpu_boundary                   */
 } olgpu_problem;
 
 typedef struct {

@@ -27,6 +27,9 @@ FIELDS = ("u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v")
 # the equations on the FAS path: the puncture constraint, with a scalar
 # field, and the reference's Gaussian test (a known answer)
 EQUATIONS = {"Punctures": 0, "Punctures_scalar_field": 1, "Poisson": 2}
+# the outer boundary conditions (-B): Robin, and Dirichlet, the reference's
+# default when -B is not given
+BOUNDARIES = {"Robin": 0, "Dirichlet": 1}
 
 
 @dataclass
@@ -55,6 +58,7 @@ class Problem:
     ps_r0: float = 120.0
     ps_sigma: float = 8.0
     ps_a2: float = 1.0
+    boundary: str = "Robin"              # or "Dirichlet" (the reference's default without -B)
 
     @property
     def numbh(self) -> int:
@@ -75,6 +79,7 @@ class Problem:
             setattr(p, name, int(getattr(self, name)))
         for name in ("L", "tol", "ps_phi0", "ps_r0", "ps_sigma", "ps_a2"):
             setattr(p, name, float(getattr(self, name)))
+        p.boundary = BOUNDARIES[self.boundary]
         return p
 
     def oracle_dict(self) -> dict:
@@ -82,6 +87,7 @@ class Problem:
                                            "order", "levels", "nu1", "nu2", "tol", "ps_case", "ps_phi0", "ps_r0",
                                            "ps_sigma", "ps_a2")}
         d["equation"] = EQUATIONS[self.equation]
+        d["boundary"] = BOUNDARIES[self.boundary]
         return d
 
 
@@ -102,8 +108,11 @@ def parse_olliptic_args(argv: Sequence[str]) -> Problem:
     eq = get(["-eq", "--equation"], str, "Punctures")
     if eq not in EQUATIONS:
         raise ValueError(f"equation {eq!r} is not on the puncture FAS path")
+    bc = get(["-B", "--boundary"], str, "Dirichlet")   # interface.cc:272
+    if bc not in BOUNDARIES:
+        raise ValueError(f"boundary {bc!r} is not on the GPU path")
     nb = get(["-NumBH", "--num-bh"], int, 1)
-    P = Problem(equation=eq)
+    P = Problem(equation=eq, boundary=bc)
     for name, flag in (("mp", "-bhmp"), ("x", "-bhx"), ("y", "-bhy"), ("z", "-bhz"), ("px", "-bhpx"),
                        ("py", "-bhpy"), ("pz", "-bhpz"), ("sx", "-bhsx"), ("sy", "-bhsy"), ("sz", "-bhsz")):
         setattr(P, name, [get([f"{flag}{i + 1}"], float, 0.0) for i in range(nb)])

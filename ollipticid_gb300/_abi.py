@@ -22,7 +22,7 @@ class Problem(C.Structure):
         ("n", C.c_int), ("L", C.c_double), ("order", C.c_int), ("levels", C.c_int),
         ("nu1", C.c_int), ("nu2", C.c_int), ("tol", C.c_double),
         ("ps_case", C.c_int), ("ps_phi0", C.c_double), ("ps_r0", C.c_double),
-        ("ps_sigma", C.c_double), ("ps_a2", C.c_double),
+        ("ps_sigma", C.c_double), ("ps_a2", C.c_double), ("boundary", C.c_int),
     ]
 
 

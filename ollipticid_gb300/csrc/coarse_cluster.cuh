@@ -45,7 +45,7 @@ template <int EQ, int NCTA>
 __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict__ boxes, int box, DevFields F,
                                                         const double *__restrict__ crd, double eps, int max_it,
                                                         double omega, double rtol, double *norm_out,
-                                                        int *iters_out, int *nan_flag)
+                                                        int *iters_out, int *nan_flag, int dirichlet)
 {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -101,6 +101,10 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
   // an ulp); the Newton step divides by an approximate reciprocal of the
   // derivative, which only sizes the step (F = 0 stays the solution).
   auto robin = [&](int mask, int i, int j, int k) {
+    if (dirichlet) {   // u = S on the boundary points
+      U(i, j, k) = gs[((long long)k * n1 + j) * n0 + i];
+      return;
+    }
     const double r2 = s_x[0][i] * s_x[0][i] + s_x[1][j] * s_x[1][j] + s_x[2][k] * s_x[2][k];
     const int ijk[3] = {i, j, k};
     double tF = 0.0, dF = 1.0, t = 0.0, dt = 0.0;

@@ -231,6 +231,11 @@ __device__ __forceinline__ void robin_point(const DevBox &B, const DevFields &F,
 {
   double *u = F.f[F_U] + B.off;
   const long long p = pidx(B, i, j, k);
+  if (mode >= 2) {   // Dirichlet (src/boundary.cc:800-812, 1481-1490): u = S, and R = u
+    if (mode == 2) u[p] = F.f[F_RHO][B.off + p];
+    else F.f[F_R][B.off + p] = u[p];
+    return;
+  }
   double dF;
   const double t = robin_term<ORD>(u, B, crd, mask, i, j, k, dF);
   if (mode == 0) {   // the step's divisor only sizes the step: F = 0 stays the solution
@@ -975,9 +980,14 @@ __global__ void __launch_bounds__(256) k_set_in_op(const XferJob *__restrict__ j
 // u lives in shared memory; b, c, S (and d, e) are read through L1.
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ void cs_robin_point(const DevBox &B, double *u, const double *rho,
-                                               const double *crd, int mask, int i, int j, int k)
+                                               const double *crd, int mask, int i, int j, int k,
+                                               bool dirichlet)
 {
   const long long p = pidx(B, i, j, k);
+  if (dirichlet) {   // u = S on the boundary points
+    u[p] = rho[p];
+    return;
+  }
   double dF;
   const double t = robin_term<2>(u, B, crd, mask, i, j, k, dF);
   const double Fv = t + u[p] - rho[p];
@@ -988,7 +998,7 @@ template <int EQ>
 __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict__ boxes, int box, DevFields F,
                                                        const double *__restrict__ crd, double eps, int max_it,
                                                        double omega, double rtol, double *norm_out,
-                                                       int *iters_out, int *nan_flag)
+                                                       int *iters_out, int *nan_flag, int dirichlet)
 {
   extern __shared__ double su[];
   __shared__ double red[32];
@@ -1017,7 +1027,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
         ijk[a] = hi ? B.n[a] - 1 : 0;
         ijk[a1] = 1 + t % c1;
         ijk[a2] = 1 + t / c1;
-        cs_robin_point(B, su, gs, crd, 1 << a, ijk[0], ijk[1], ijk[2]);
+        cs_robin_point(B, su, gs, crd, 1 << a, ijk[0], ijk[1], ijk[2], dirichlet);
       }
     }
     __syncthreads();
@@ -1032,7 +1042,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
           ijk[fa] = 1 + q;
           ijk[a] = (e >> 1) ? B.n[a] - 1 : 0;
           ijk[c] = (e & 1) ? B.n[c] - 1 : 0;
-          cs_robin_point(B, su, gs, crd, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+          cs_robin_point(B, su, gs, crd, (1 << a) | (1 << c), ijk[0], ijk[1], ijk[2], dirichlet);
         }
       }
     }
@@ -1041,7 +1051,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
       const int i = (threadIdx.x & 1) ? n0 - 1 : 0;
       const int j = ((threadIdx.x >> 1) & 1) ? n1 - 1 : 0;
       const int k = (threadIdx.x >> 2) ? n2 - 1 : 0;
-      cs_robin_point(B, su, gs, crd, 7, i, j, k);
+      cs_robin_point(B, su, gs, crd, 7, i, j, k, dirichlet);
     }
     __syncthreads();
     // one red-black sweep
@@ -1215,9 +1225,9 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
 // The Gaussian test (equation Poisson, src/operator.cc:640-655, 1865-1887):
 // u = a exp(-r^2/2), a = 0.004, solves Lap u + u^2 = a exp(-r^2) (a +
 // exp(r^2/2) (r^2 - 3)).  Initial state (Set_Coefficients, Set_Boundary,
-// src/boundary.cc:8-78): rho0 = that source on every point and then the Robin
-// boundary value 0 on the BOUNDARY (ghost) points of every box, u = the
-// Gaussian on every point.
+// src/boundary.cc:8-78): rho0 = that source on every point and then the
+// boundary value on the BOUNDARY (ghost) points of every box (0 for Robin,
+// the Gaussian for Dirichlet), u = the Gaussian on every point.
 // ----------------------------------------------------------------------------
 __device__ double dev_gaussian_source(double x, double y, double z)
 {
@@ -1233,7 +1243,7 @@ __device__ double dev_gaussian(double x, double y, double z)
 }
 
 __global__ void __launch_bounds__(256) k_gaussian_init(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                       const double *__restrict__ crd)
+                                                       const double *__restrict__ crd, int dirichlet)
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
@@ -1247,7 +1257,9 @@ __global__ void __launch_bounds__(256) k_gaussian_init(BoxList L, const DevBox *
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
   const int b = B.buf;
   const bool ghost = i < b || j < b || k < b || i >= B.n[0] - b || j >= B.n[1] - b || k >= B.n[2] - b;
-  F.f[F_RHO][B.off + t] = ghost ? 0.0 : dev_gaussian_source(x, y, z);
+  // the boundary value: Robin's coefficient 0, or Dirichlet's boundary
+  // function (the Gaussian itself)
+  F.f[F_RHO][B.off + t] = ghost ? (dirichlet ? dev_gaussian(x, y, z) : 0.0) : dev_gaussian_source(x, y, z);
   F.f[F_U][B.off + t] = dev_gaussian(x, y, z);
 }
 

@@ -563,6 +563,8 @@ void dispatch_apply_op(olgpu_hierarchy *h, int level)
 
 void dispatch_robin(olgpu_hierarchy *h, int level, int mode)
 {
+  // the Dirichlet condition runs through the same boundary walk: modes 2, 3
+  if (h->P.boundary == OLGPU_BC_DIRICHLET) mode += 2;
   if (level_order(h, level) == 2) launch_robin<2>(h, level, mode);
   else launch_robin<4>(h, level, mode);   // orders 4, 6, 8 share dx4 (src/ffunction.cc:197-282)
 }
@@ -585,7 +587,7 @@ cudaError_t launch_coarse_cluster_n(olgpu_hierarchy *h)
   return cudaLaunchKernelEx(&cfg, k_coarse_cluster<EQ, NCTA>, (const DevBox *)h->d_boxes, h->G.first_box[0], h->F,
                             (const double *)h->d_coords, h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
                             h->coarse_rtol, &h->d_stats->coarse_norm, &h->d_stats->coarse_iters,
-                            &h->d_stats->nan_flag);
+                            &h->d_stats->nan_flag, h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
 }
 
 template <int EQ>
@@ -714,7 +716,8 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
       k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
                                                        h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
                                                        h->coarse_rtol, &h->d_stats->coarse_norm,
-                                                       &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+                                                       &h->d_stats->coarse_iters, &h->d_stats->nan_flag,
+                                                       h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
     h->launches++;
   } else {
     emit_fasn<EQ>(h, k - 1, top);
@@ -1314,6 +1317,8 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   if (p->levels < 1) return fail(OLGPU_ERR_INVALID_ARG, "levels must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0) return fail(OLGPU_ERR_INVALID_ARG, "negative sweep count");
   if (p->equation < 0 || p->equation > 2) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
+  if (p->boundary != OLGPU_BC_ROBIN && p->boundary != OLGPU_BC_DIRICHLET)
+    return fail(OLGPU_ERR_INVALID_ARG, "boundary must be Robin or Dirichlet");
   if (p->equation == 1 && !(p->ps_case >= 1 && p->ps_case <= 4))
     return fail(OLGPU_ERR_INVALID_ARG, "ps_case must be 1..4");
   int ndev = 0;
@@ -1572,7 +1577,8 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h)
   if (h->equation == OLGPU_EQ_POISSON) {   // the Gaussian test's initial u and source
     for (int l = 0; l < h->G.levels; l++) {
       const BoxList BL = level_list(h, l, blocks_all);
-      k_gaussian_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords);
+      k_gaussian_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords,
+                                                                    h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
     }
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1927,6 +1933,8 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
   if (precision == OLGPU_PREC_MIXED) {
     if (h->equation == OLGPU_EQ_POISSON)
       return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the puncture equations");
+    if (h->P.boundary != OLGPU_BC_ROBIN)
+      return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the Robin boundary");
     olgpu_status st = build_mixed(h);
     if (st != OLGPU_OK) return st;
   }

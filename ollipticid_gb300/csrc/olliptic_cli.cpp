@@ -8,7 +8,8 @@
 // and defaults; flags outside it (output, printing, symmetry, MPI) are accepted
 // and ignored, as the reference ignores unknown flags.  Equations other than
 // Punctures / Punctures_scalar_field / Poisson (the reference's Gaussian
-// test) are refused, and so are boundary conditions other than Robin.
+// test) are refused, and so are boundary conditions other than Robin and
+// Dirichlet (the reference's default).
 //
 // Methods (-m): Vcycle (the default) and AppPuncture (the analytic
 // approximation alone, elliptic::ApproximateID); the others are refused.
@@ -481,13 +482,15 @@ int main(int argc, char **argv)
     std::fprintf(stderr, "Olliptic_gpu.x: method %s is not on the puncture FAS path\n", method.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
   }
-  // the boundary condition (interface.cc:272, default Dirichlet): the GPU
-  // path has the Robin condition of the puncture runs (every pars/ file
-  // passes -B Robin); another is refused rather than replaced
+  // the boundary condition (interface.cc:272, Dirichlet without -B): Robin
+  // (what every pars/ file passes) or Dirichlet; another is refused rather
+  // than replaced
   const char *bc = A.find({"-B", "--boundary"});
-  if (!bc || std::strcmp(bc, "Robin")) {
-    std::fprintf(stderr, "Olliptic_gpu.x: boundary %s is not on the GPU path (pass -B Robin)\n",
-                 bc ? bc : "Dirichlet (the default)");
+  const std::string boundary = bc ? bc : "Dirichlet";
+  if (boundary == "Robin") p.boundary = OLGPU_BC_ROBIN;
+  else if (boundary == "Dirichlet") p.boundary = OLGPU_BC_DIRICHLET;
+  else {
+    std::fprintf(stderr, "Olliptic_gpu.x: boundary %s is not on the GPU path\n", boundary.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
   }
   p.numbh = A.integer({"-NumBH", "--num-bh"}, 1);

@@ -666,10 +666,13 @@ typedef void (*robin_pt_fn)(orc_solver *, obox *, int mask, int i, int j, int k)
 
 static void robin_update_pt(orc_solver *S, obox *B, int mask, int i, int j, int k)
 {
-  (void)S;
   double *u = B->f[F_U];
   const double *rho = B->f[F_RHO];
   long p = IDX(B, i, j, k);
+  if (S->P.boundary == 1) {   /* Dirichlet: u = S on the BOUNDARY points, src/boundary.cc:800-812 */
+    u[p] = rho[p];
+    return;
+  }
   double dF;
   double t = robin_F(B, u, mask, i, j, k, &dF);
   double F = t + u[p] - rho[p];
@@ -678,9 +681,12 @@ static void robin_update_pt(orc_solver *S, obox *B, int mask, int i, int j, int 
 
 static void robin_operator_pt(orc_solver *S, obox *B, int mask, int i, int j, int k)
 {
-  (void)S;
   const double *u = B->f[F_U];
   long p = IDX(B, i, j, k);
+  if (S->P.boundary == 1) {   /* Dirichlet: R = u on the BOUNDARY points, src/boundary.cc:1481-1490 */
+    B->f[F_R][p] = u[p];
+    return;
+  }
   double dF;
   double t = robin_F(B, u, mask, i, j, k, &dF);
   B->f[F_R][p] = t + u[p];
@@ -1091,7 +1097,9 @@ static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
             const int bb = B->D.buf;
             const int ghost = i < bb || j < bb || k < bb || i >= B->D.n[0] - bb || j >= B->D.n[1] - bb ||
                               k >= B->D.n[2] - bb;
-            B->f[F_RHO][q] = ghost ? 0.0 : gaussian_source(x, y, z);
+            /* the boundary value: Robin's coefficient 0, or Dirichlet's
+             * boundary function (the Gaussian itself) */
+            B->f[F_RHO][q] = ghost ? (p->boundary == 1 ? gaussian(x, y, z) : 0.0) : gaussian_source(x, y, z);
             B->f[F_U][q] = gaussian(x, y, z);
             continue;
           }

@@ -34,6 +34,7 @@ typedef struct {
   /* scalar field (-psc -phi0 -r0 -sigma -a2) */
   int ps_case;
   double ps_phi0, ps_r0, ps_sigma, ps_a2;
+  int boundary;            /* -B: 0 Robin, 1 Dirichlet (the reference's default) */
 } orc_problem;
 
 typedef struct orc_solver orc_solver;

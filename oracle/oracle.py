@@ -28,7 +28,7 @@ class OrcProblem(C.Structure):
         ("n", C.c_int), ("L", C.c_double), ("order", C.c_int), ("levels", C.c_int),
         ("nu1", C.c_int), ("nu2", C.c_int), ("tol", C.c_double),
         ("ps_case", C.c_int), ("ps_phi0", C.c_double), ("ps_r0", C.c_double),
-        ("ps_sigma", C.c_double), ("ps_a2", C.c_double),
+        ("ps_sigma", C.c_double), ("ps_a2", C.c_double), ("boundary", C.c_int),
     ]
 
 
@@ -107,6 +107,7 @@ class Oracle:
         p.tol = float(params.get("tol", 1e-8)); p.ps_case = int(params.get("ps_case", 1))
         p.ps_phi0 = float(params.get("ps_phi0", 0.025)); p.ps_r0 = float(params.get("ps_r0", 120.0))
         p.ps_sigma = float(params.get("ps_sigma", 8.0)); p.ps_a2 = float(params.get("ps_a2", 1.0))
+        p.boundary = int(params.get("boundary", 0))
         self.numbh = p.numbh
         self._p = p
         self._s = (L.orc_create_extra_coarse if extra_coarse else L.orc_create)(C.byref(p))

@@ -80,11 +80,11 @@ def test_other_equations_are_refused(cli):
     assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
 
 
-@pytest.mark.parametrize("flag", ["", "-B Dirichlet", "-B Asymptotic"])
-def test_boundaries_other_than_robin_are_refused(cli, flag, tmp_path):
-    """The reference's default boundary is Dirichlet; only Robin (what every
-    pars/ file passes) is on the GPU path, and another is refused before any
-    work rather than replaced."""
+@pytest.mark.parametrize("flag", ["-B Asymptotic", "-B Neumann"])
+def test_boundaries_other_than_robin_and_dirichlet_are_refused(cli, flag, tmp_path):
+    """Robin (what every pars/ file passes) and Dirichlet (the reference's
+    default without -B) are on the GPU path; another condition is refused
+    before any work rather than replaced."""
     r = run(cli, "-eq Punctures -NumBH 1 -bhmp1 0.5 -N 25 -L 40 -O 2 -l 3 " + flag, check=False, cwd=str(tmp_path))
     assert r.returncode != 0 and "is not on the GPU path" in r.stderr
     assert not (tmp_path / "Output").exists()
