@@ -33,7 +33,9 @@
 // src/output.cc:1355-1460), and the command line as <dir>.run.  stdout0.out
 // (the banner and log) is not written.  The directory is rotated like the reference's
 // (interface.cc:1470-1538): an existing <dir> becomes <dir>_prev, replacing
-// an older <dir>_prev.  2-D and 3-D dumps (-p2d, -p3d) are not written.
+// an older <dir>_prev.  -p2d yes adds the per-box planes u-l<l>b<i>-0.{yz,xz,xy}
+// (ffunction::Print_2D); the 3-D dumps (-p3d) are not written (they list the
+// points in the reference's permuted storage order).
 // Exit status 0 on success; otherwise the C ABI's status with its message on
 // stderr.
 #include "olgpu.h"
@@ -190,6 +192,58 @@ olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis
   FILE *f = std::fopen(file.c_str(), "a");
   if (!f) return OLGPU_ERR_INVALID_ARG;
   for (int i = 0; i < np; i++) std::fprintf(f, "%.12e\t%.12e\t\n", B.coord(axis, i), val[i]);
+  std::fprintf(f, "\n");
+  std::fclose(f);
+  return OLGPU_OK;
+}
+
+// ffunction::Print_2D of one box (src/ffunction.cc:477-735, called by
+// multigrid::Print_2D with the Lagrange order 2): the plane through the
+// normal coordinate 0 when the box holds it and the values are interpolated,
+// else through the box's middle node; every node of the other two axes, the
+// lower axis outer; "%.12e\t%.12e\t%.12e\t" lines, a blank line after each
+// outer index and one more at the end.
+olgpu_status print_box_plane(olgpu_hierarchy *h, const BoxGeom &B, int g, int normal, bool interpolate,
+                             const std::string &file)
+{
+  const int a1 = normal == 0 ? 1 : 0, a2 = normal == 2 ? 1 : 2;   // in-plane axes, a1 < a2
+  const int nm = B.n(normal) % 2 == 0 ? B.n(normal) / 2 : (B.n(normal) - 1) / 2;
+  double at = B.coord(normal, nm);
+  if (interpolate && B.is_in_axis(normal, 0.0)) at = 0.0;
+  const int n1 = B.n(a1), n2 = B.n(a2);
+  std::vector<double> pts(3 * (size_t)n1 * n2), val((size_t)n1 * n2);
+  for (int p = 0; p < n1; p++)
+    for (int q = 0; q < n2; q++) {
+      double *x = &pts[3 * ((size_t)p * n2 + q)];
+      x[normal] = at;
+      x[a1] = B.coord(a1, p);
+      x[a2] = B.coord(a2, q);
+    }
+  if (interpolate) {
+    const olgpu_status st = olgpu_interpolate(h, g, 0, pts.data(), (long long)val.size(), 2, val.data());
+    if (st != OLGPU_OK) return st;
+  } else {
+    std::vector<double> u((size_t)B.b.nx * B.b.ny * B.b.nz);
+    const olgpu_status st = olgpu_download(h, g, "u", u.data());
+    if (st != OLGPU_OK) return st;
+    for (int p = 0; p < n1; p++)
+      for (int q = 0; q < n2; q++) {
+        int ijk[3];
+        ijk[normal] = nm;
+        ijk[a1] = p;
+        ijk[a2] = q;
+        val[(size_t)p * n2 + q] = u[((size_t)ijk[2] * B.b.ny + ijk[1]) * B.b.nx + ijk[0]];
+      }
+  }
+  FILE *f = std::fopen(file.c_str(), "a");
+  if (!f) return OLGPU_ERR_INVALID_ARG;
+  for (int p = 0; p < n1; p++) {
+    for (int q = 0; q < n2; q++) {
+      const size_t r = (size_t)p * n2 + q;
+      std::fprintf(f, "%.12e\t%.12e\t%.12e\t\n", pts[3 * r + a1], pts[3 * r + a2], val[r]);
+    }
+    std::fprintf(f, "\n");
+  }
   std::fprintf(f, "\n");
   std::fclose(f);
   return OLGPU_OK;
@@ -629,9 +683,10 @@ int main(int argc, char **argv)
 
   // elliptic::Print_Solution (src/output.cc:624-700), variable "u"
   const bool print_1d = A.logic({"-p1d", "--print-1d"}, true);
+  const bool print_2d = A.logic({"-p2d", "--print-2d"}, false);
   const bool print_interpol = A.logic({"-pint", "--print-interpol"}, true);
   const bool interpol_output = A.logic({"-int", "--interpol-output"}, true);
-  if (print_1d || print_interpol) {
+  if (print_1d || print_2d || print_interpol) {
     const int ord = p.order + 1;
     std::printf("Printing...\n");
     olgpu_status ps = OLGPU_OK;
@@ -649,6 +704,19 @@ int main(int argc, char **argv)
               dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
           for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
             ps = print_box_cut(h, B, g, a, interpol_output, ord, stem + ext[a]);
+        }
+    }
+    if (print_2d) {   // the planes .yz, .xz, .xy of every box, level by level
+      std::vector<int> in_level(nl, 0);
+      static const char *ext[3] = {".yz", ".xz", ".xy"};
+      for (int l = l0; l < nl && ps == OLGPU_OK; l++)
+        for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
+          if (boxes[g].level != l) continue;
+          const BoxGeom B{boxes[g]};
+          const std::string stem =
+              dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
+          for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
+            ps = print_box_plane(h, B, g, a, interpol_output, stem + ext[a]);
         }
     }
     if (print_interpol && ps == OLGPU_OK) {

@@ -43,6 +43,8 @@ OUTPUT_CASES = {   # name: (command line, value_tol, mg_tol)
     "o2_binary": (BIN + " -Dp 0.5", 1e-9, 1e-6),
     # per-box cuts as node values, no interpolated files
     "o2_binary_nodes": (BIN + " -int no -pint no", 1e-9, 1e-6),
+    # per-box planes (-p2d), interpolated through 0 where the box holds it
+    "o2_binary_planes": (BIN + " -p2d yes -p1d no -pint no", 1e-9, 1e-6),
 }
 
 
