@@ -656,16 +656,17 @@ int main(int argc, char **argv)
   }
   olgpu_report rep{};
   if (!approx_only) {
-  st = olgpu_solve(h, nullptr, &rep);   // the reference stop rule
-  for (int c = 0; c < rep.cycles && c < 256; c++) std::printf("  V-cycle %3d  norm %.6e\n", c + 1, rep.res[c]);
-  if (st != OLGPU_OK) {
-    olgpu_hierarchy_destroy(h);
-    return fail(st, "solve");
+    st = olgpu_solve(h, nullptr, &rep);   // the reference stop rule
+    for (int c = 0; c < rep.cycles && c < 256; c++) std::printf("  V-cycle %3d  norm %.6e\n", c + 1, rep.res[c]);
+    if (st != OLGPU_OK) {
+      olgpu_hierarchy_destroy(h);
+      return fail(st, "solve");
+    }
+    std::printf("Solved in %d V-cycles, norm %.6e, %.3f ms on the device\n", rep.cycles, rep.final_res,
+                olgpu_last_device_ms(h));
   }
-  std::printf("Solved in %d V-cycles, norm %.6e, %.3f ms on the device\n", rep.cycles, rep.final_res,
-              olgpu_last_device_ms(h));
-  }
-  if (std_output && !approx_only) {   // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
+  // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
+  if (std_output && !approx_only) {
     FILE *f = std::fopen((dir + "Loo.gp").c_str(), "a");
     std::vector<double> pre(nl), post(nl);
     for (int c = 0; f && c < rep.cycles; c++) {
