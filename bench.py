@@ -386,6 +386,37 @@ def run_approx_start():
     return out
 
 
+def fp32_smoother_roofline(peak: float, peak_kind: str):
+    """The mixed cycle's dominant kernel, the cluster-resident FP32 smoother
+    (k_smooth32_cluster), on the finest level of the benchmark binary: 12
+    sweeps timed with CUDA events on the solver's stream (olgpu_time_smoother),
+    20 algorithmic bytes per interior point and sweep (read S, A, 1/(c+u) and
+    e, write e).  One 16-block cluster per box holds e in distributed shared
+    memory through the sweeps, so the kernel runs on 16 SMs per box: the rate
+    per SM, scaled to all 152, is what bounds many solves sharing the GPU."""
+    import ollipticid_gb300 as og
+    P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
+    with og.Elliptic(P) as E:
+        E.set_smoother_blocks(16)
+        E.set_inner_sweeps(4, 6)
+        E.set_precision(True)
+        top = E.levels - 1
+        pts = E.interior_points(top)
+        boxes = sum(1 for b in E.boxes if b.level == top)
+        E.time_smoother(top, 3)                               # warm
+        sweeps = 12
+        ms, nl = E.time_smoother(top, sweeps)
+    achieved = 20.0 * pts * sweeps / (ms / 1e3) / 1e9
+    sms = 16 * boxes
+    return {"bound": "hbm", "kernel": f"k_smooth32_cluster<{P.order},0>: {sweeps} sweeps of the finest level "
+                                      f"({pts} interior points, {boxes} boxes, one 16-block cluster each)",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+            "sms": sms, "achieved_scaled_to_152_sms": achieved * 152 / sms,
+            "frac_scaled_to_152_sms": achieved * 152 / sms / peak, "ms": ms, "launches": nl,
+            "note": "the level stays in shared and L2 memory through the sweeps; the algorithmic rate is per "
+                    "the SMs the clusters hold"}
+
+
 def run_batched(args, count: int = 16, group: int = 16, tuned=None):
     """Seeded batched binaries (mixed precision, tol 1e-10): solves/s when
     `group` solves run concurrently, and the same instances one at a time."""
@@ -575,6 +606,8 @@ def run_gpu(args, rank: int, world: int, local: int):
                     "design; traffic and FP64 pipe occupancy are from one ncu capture of this launch (ncu flushes "
                     "L2 first, so traffic is the level's fields read once; in the timed sweeps they stay in L2)"}
 
+    roof32 = fp32_smoother_roofline(peak, peak_kind) if rank == 0 and world == 1 and not args.no_extra else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         n_cycles = 2
@@ -596,7 +629,8 @@ def run_gpu(args, rank: int, world: int, local: int):
                          "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served, "config3": config3,
             "convergence": convergence, "approx_start": approx_start,
-            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "roofline": roof, "roofline_fp32_smoother": roof32, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": launches,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
