@@ -273,7 +273,9 @@ olgpu_status olgpu_server_submit(olgpu_server *s, const olgpu_problem *p, long l
 olgpu_status olgpu_server_poll(olgpu_server *s, long long id, int wait, int *done, olgpu_server_result *out);
 /* Solves on the GPU, being built or waiting, and the peak of the first. */
 olgpu_status olgpu_server_stats(olgpu_server *s, int *active, int *building, int *waiting, int *peak_active);
-/* Stops the threads, finishes nothing more and frees every hierarchy it holds. */
+/* Stops the threads, finishes nothing more and frees every hierarchy it holds
+ * (results not yet polled included).  No other call on s may be running or
+ * waiting when it is called. */
 olgpu_status olgpu_server_destroy(olgpu_server *s);
 
 /* elliptic::ApproximateID (src/elliptic.cc:1977-2226, the reference's
