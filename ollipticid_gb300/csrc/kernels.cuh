@@ -478,6 +478,39 @@ __global__ void __launch_bounds__(256) k_elementwise(BoxList L, const DevBox *__
 // injection would hand the coarse level a single colour.  W vanishes at the
 // fixed point, so the averaging changes the path, not the solution.
 // ----------------------------------------------------------------------------
+// The (1,2,1)^3/64 average of w around (i, j, k), a neighbour outside the
+// INSIDE range taking the centre value c: summed separably, rows along x
+// first ((v[-1] + 2 v[0]) + v[+1]), then those rows along y, then the
+// planes along z, and scaled by 1/64 once.  The factors are powers of two,
+// so only the additions round; every kernel that forms the weighting uses
+// this one order, so the fused and the plain steps agree bit for bit.  The
+// INSIDE test of a neighbour is the product of three per-axis tests.
+template <class V, class W>
+__device__ __forceinline__ V fw_sum(const W &w, V c, const DevBox &B, int i, int j, int k, long long p)
+{
+  const int b = B.buf;
+  const long long sy = B.n[0], sz = (long long)B.n[0] * B.n[1];
+  const bool xin[3] = {i - 1 >= b, true, i + 1 < B.n[0] - b};
+  const bool yin[3] = {j - 1 >= b, true, j + 1 < B.n[1] - b};
+  const bool zin[3] = {k - 1 >= b, true, k + 1 < B.n[2] - b};
+  V plane[3];
+#pragma unroll
+  for (int dk = 0; dk < 3; dk++) {
+    V row[3];
+#pragma unroll
+    for (int dj = 0; dj < 3; dj++) {
+      const long long q = p + (long long)(dk - 1) * sz + (long long)(dj - 1) * sy;
+      const bool yz = yin[dj] && zin[dk];
+      const V vm = (yz && xin[0]) ? w(q - 1) : c;
+      const V v0 = yz ? w(q) : c;
+      const V vp = (yz && xin[2]) ? w(q + 1) : c;
+      row[dj] = (vm + V(2) * v0) + vp;
+    }
+    plane[dk] = (row[0] + V(2) * row[1]) + row[2];
+  }
+  return ((plane[0] + V(2) * plane[1]) + plane[2]) * (V(1) / V(64));
+}
+
 __global__ void __launch_bounds__(256) k_full_weight(BoxList L, const DevBox *__restrict__ boxes, DevFields F)
 {
   long long lb;
@@ -496,16 +529,7 @@ __global__ void __launch_bounds__(256) k_full_weight(BoxList L, const DevBox *__
     F.f[F_T][B.off + t] = c;
     return;
   }
-  double acc = 0.0;
-  for (int dk = -1; dk <= 1; dk++)
-    for (int dj = -1; dj <= 1; dj++)
-      for (int di = -1; di <= 1; di++) {
-        const int ii = i + di, jj = j + dj, kk = k + dk;
-        const double wt = (double)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (1.0 / 64.0);
-        const bool in = ii >= b && ii < B.n[0] - b && jj >= b && jj < B.n[1] - b && kk >= b && kk < B.n[2] - b;
-        acc += wt * (in ? w[pidx(B, ii, jj, kk)] : c);
-      }
-  F.f[F_T][B.off + t] = acc;
+  F.f[F_T][B.off + t] = fw_sum<double>([&](long long q) { return w[q]; }, c, B, i, j, k, t);
 }
 
 // ----------------------------------------------------------------------------
@@ -806,7 +830,7 @@ inline bool xfer_rows(const XferJob *jobs, size_t n, int width)
 // The tau transfer with the full weighting folded in: every job of the plan
 // is a strided copy from the fine level, so the (1,2,1)^3/64 average of W is
 // formed only at the fine nodes that are read (one in eight), with
-// k_full_weight's terms and order.  DIFF: W = f[fa] - f[fb] (the FP32 cycle
+// k_full_weight's terms and order (fw_sum).  DIFF: W = f[fa] - f[fb] (the FP32 cycle
 // forms S - R where it is read), else W = f[fa].
 template <class V, class Fields, bool DIFF>
 __global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ jobs, int njobs,
@@ -839,21 +863,12 @@ __global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ job
   const V *wa = F.f[fa] + S.off;
   const V *wb = DIFF ? F.f[fb] + S.off : nullptr;
   auto w = [&](long long q) -> V { return DIFF ? wa[q] - wb[q] : wa[q]; };
-  const V c = w(pidx(S, si, sj, sk));
+  const long long sp = pidx(S, si, sj, sk);
+  const V c = w(sp);
   const int b = S.buf;
   V val = c;
-  if (si >= b && si < S.n[0] - b && sj >= b && sj < S.n[1] - b && sk >= b && sk < S.n[2] - b) {
-    V acc = V(0);
-    for (int dk = -1; dk <= 1; dk++)
-      for (int dj = -1; dj <= 1; dj++)
-        for (int di = -1; di <= 1; di++) {
-          const int ii = si + di, jj = sj + dj, kk = sk + dk;
-          const V wt = (V)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (V(1) / V(64));
-          const bool in = ii >= b && ii < S.n[0] - b && jj >= b && jj < S.n[1] - b && kk >= b && kk < S.n[2] - b;
-          acc += wt * (in ? w(pidx(S, ii, jj, kk)) : c);
-        }
-    val = acc;
-  }
+  if (si >= b && si < S.n[0] - b && sj >= b && sj < S.n[1] - b && sk >= b && sk < S.n[2] - b)
+    val = fw_sum<V>(w, c, S, si, sj, sk, sp);
   F.f[J.tfield][T.off + pidx(T, i, j, k)] = val;
 }
 

@@ -473,16 +473,7 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
     G.f[G_T][B.off + t] = c;
     return;
   }
-  float acc = 0.0f;
-  for (int dk = -1; dk <= 1; dk++)
-    for (int dj = -1; dj <= 1; dj++)
-      for (int di = -1; di <= 1; di++) {
-        const int ii = i + di, jj = j + dj, kk = k + dk;
-        const float wt = (float)((2 - di * di) * (2 - dj * dj) * (2 - dk * dk)) * (1.0f / 64.0f);
-        const bool in = ii >= b && ii < B.n[0] - b && jj >= b && jj < B.n[1] - b && kk >= b && kk < B.n[2] - b;
-        acc += wt * (in ? w(pidx(B, ii, jj, kk)) : c);
-      }
-  G.f[G_T][B.off + t] = acc;
+  G.f[G_T][B.off + t] = fw_sum<float>(w, c, B, i, j, k, t);
 }
 
 // Set_In of a refinement level with the coarse operator folded in: at every
