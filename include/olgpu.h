@@ -44,11 +44,22 @@ typedef enum {
   OLGPU_ERR_NO_DEVICE = 8
 } olgpu_status;
 
-/* OLGPU_EQ_POISSON is the reference's Gaussian test (-eq Poisson,
- * src/operator.cc:640-655, 1865-1887): Lap u + u^2 = a e^{-r^2}(a + e^{r^2/2}
- * (r^2 - 3)), whose solution u = a e^{-r^2/2} (a = 0.004) is known; it runs
- * on the same FAS path in FP64 and serves as a known-answer test. */
-typedef enum { OLGPU_EQ_PUNCTURES = 0, OLGPU_EQ_PUNCTURES_SCALAR = 1, OLGPU_EQ_POISSON = 2 } olgpu_equation;
+/* The reference's test equations, Lap u + u^2 = source (poisson_OP,
+ * include/elliptic.h:359-366), run on the same FAS path in FP64:
+ * OLGPU_EQ_POISSON, the Gaussian test (-eq Poisson, src/operator.cc:640-655,
+ * 1865-1887): source a e^{-r^2}(a + e^{r^2/2}(r^2 - 3)), whose solution
+ * u = a e^{-r^2/2} (a = 0.004) is known (a known-answer test);
+ * OLGPU_EQ_BOUNDARY_TEST (-eq Boundary-test, 661-673, 1772-1816): source
+ * -2a tanh(r) / (r cosh^2 r), boundary function a tanh(r) / r;
+ * OLGPU_EQ_MULTIBOX_TEST (-eq Multibox-test, 1145-1175, 1820-1857): two
+ * Gaussians e^{-0.05 r_i^2} centred at x = bhx1, bhx2 (NumBH >= 2). */
+typedef enum {
+  OLGPU_EQ_PUNCTURES = 0,
+  OLGPU_EQ_PUNCTURES_SCALAR = 1,
+  OLGPU_EQ_POISSON = 2,
+  OLGPU_EQ_BOUNDARY_TEST = 3,
+  OLGPU_EQ_MULTIBOX_TEST = 4
+} olgpu_equation;
 
 /* The outer boundary condition (-B, src/boundary.cc:447-1535): Robin, u ~
  * u_inf + C / r^n (what the puncture pars/ files use), or Dirichlet, u fixed

@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
   const int j = (r % B.n[1]), k = (r / B.n[1]);
   const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
-  if (P.equation == 2) {   // the Gaussian test has no puncture coefficients
+  if (P.equation >= 2) {   // the test equations have no puncture coefficients
     F.f[F_B][B.off + t] = 0.0;
     F.f[F_C][B.off + t] = 0.0;
     return;
@@ -1237,28 +1237,52 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
 }
 
 // ----------------------------------------------------------------------------
-// The Gaussian test (equation Poisson, src/operator.cc:640-655, 1865-1887):
-// u = a exp(-r^2/2), a = 0.004, solves Lap u + u^2 = a exp(-r^2) (a +
-// exp(r^2/2) (r^2 - 3)).  Initial state (Set_Coefficients, Set_Boundary,
-// src/boundary.cc:8-78): rho0 = that source on every point and then the
-// boundary value on the BOUNDARY (ghost) points of every box (0 for Robin,
-// the Gaussian for Dirichlet), u = the Gaussian on every point.
+// The reference's test equations (Lap u + u^2 = source) and their boundary
+// functions, src/operator.cc:1772-1887: the Gaussian test (Poisson: u = a
+// e^{-r^2/2}, which solves it), Boundary-test (a tanh(r)/r) and
+// Multibox-test (two Gaussians centred at x = bhx1, bhx2).  Initial state
+// (Set_Coefficients, Set_Boundary, src/boundary.cc:8-78): rho0 = the source
+// on every point, then the boundary value on the BOUNDARY (ghost) points of
+// every box (0 for Robin, the boundary function for Dirichlet); u = the
+// boundary function on every point.
 // ----------------------------------------------------------------------------
-__device__ double dev_gaussian_source(double x, double y, double z)
+__device__ __forceinline__ bool dev_dcomp0(double r) { return fabs(r) <= 3 * DBL_EPSILON; }
+
+__device__ double dev_test_function(const PunctureParams &P, double x, double y, double z)
 {
-  const double r2 = x * x + y * y + z * z;
+  if (P.equation == 3) {   // test_boundary
+    const double r = sqrt(x * x + y * y + z * z);
+    return !dev_dcomp0(r) ? 0.004 * tanh(r) / r : 0.004;
+  }
+  if (P.equation == 4) {   // test_mfunct
+    const double r2_1 = (x - P.x[0]) * (x - P.x[0]) + y * y + z * z;
+    const double r2_2 = (x - P.x[1]) * (x - P.x[1]) + y * y + z * z;
+    const double a = 0.05;
+    return exp(-a * r2_1) + exp(-a * r2_2);
+  }
+  const double r2 = x * x + y * y + z * z;   // Gaussian
+  return 0.004 * exp(-0.5 * r2);
+}
+
+__device__ double dev_test_source(const PunctureParams &P, double x, double y, double z)
+{
+  if (P.equation == 3) {   // test_boundary_source
+    const double r = sqrt(x * x + y * y + z * z);
+    return !dev_dcomp0(r) ? -2.0 * 0.004 * tanh(r) / (r * cosh(r) * cosh(r)) : -2.0 * 0.004;
+  }
+  if (P.equation == 4) {   // test_mfunct_source
+    const double r2_1 = (x - P.x[0]) * (x - P.x[0]) + y * y + z * z;
+    const double r2_2 = (x - P.x[1]) * (x - P.x[1]) + y * y + z * z;
+    const double a = 0.05;
+    return 2.0 * a * exp(-a * r2_1) * ((2 * a * r2_1 - 3)) + 2.0 * a * exp(-a * r2_2) * ((2 * a * r2_2 - 3));
+  }
+  const double r2 = x * x + y * y + z * z;   // Gaussian_source
   const double a = 0.004;
   return a * exp(-r2) * (a + exp(0.5 * r2) * (r2 - 3.0));
 }
 
-__device__ double dev_gaussian(double x, double y, double z)
-{
-  const double r2 = x * x + y * y + z * z;
-  return 0.004 * exp(-0.5 * r2);
-}
-
-__global__ void __launch_bounds__(256) k_gaussian_init(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                       const double *__restrict__ crd, int dirichlet)
+__global__ void __launch_bounds__(256) k_test_init(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                   const double *__restrict__ crd, PunctureParams P, int dirichlet)
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
@@ -1272,10 +1296,9 @@ __global__ void __launch_bounds__(256) k_gaussian_init(BoxList L, const DevBox *
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
   const int b = B.buf;
   const bool ghost = i < b || j < b || k < b || i >= B.n[0] - b || j >= B.n[1] - b || k >= B.n[2] - b;
-  // the boundary value: Robin's coefficient 0, or Dirichlet's boundary
-  // function (the Gaussian itself)
-  F.f[F_RHO][B.off + t] = ghost ? (dirichlet ? dev_gaussian(x, y, z) : 0.0) : dev_gaussian_source(x, y, z);
-  F.f[F_U][B.off + t] = dev_gaussian(x, y, z);
+  const double g = dev_test_function(P, x, y, z);
+  F.f[F_RHO][B.off + t] = ghost ? (dirichlet ? g : 0.0) : dev_test_source(P, x, y, z);
+  F.f[F_U][B.off + t] = g;
 }
 
 // ----------------------------------------------------------------------------

@@ -1209,7 +1209,7 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
   h->launches = 0;
   if (h->equation == 1) emit_fasn<1>(h, top, top);
-  else if (h->equation == 2) emit_fasn<2>(h, top, top);
+  else if (h->equation >= 2) emit_fasn<2>(h, top, top);   // the test equations share one operator
   else emit_fasn<0>(h, top, top);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -1316,7 +1316,9 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
   if (p->levels < 1) return fail(OLGPU_ERR_INVALID_ARG, "levels must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0) return fail(OLGPU_ERR_INVALID_ARG, "negative sweep count");
-  if (p->equation < 0 || p->equation > 2) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
+  if (p->equation < 0 || p->equation > 4) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
+  if (p->equation == OLGPU_EQ_MULTIBOX_TEST && p->numbh < 2)
+    return fail(OLGPU_ERR_INVALID_ARG, "the multibox test takes its two centres from bhx1 and bhx2");
   if (p->boundary != OLGPU_BC_ROBIN && p->boundary != OLGPU_BC_DIRICHLET)
     return fail(OLGPU_ERR_INVALID_ARG, "boundary must be Robin or Dirichlet");
   if (p->equation == 1 && !(p->ps_case >= 1 && p->ps_case <= 4))
@@ -1574,11 +1576,12 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h)
   for (int f : {F_U, F_RHO, F_R, F_W, F_WW, F_V, F_T}) CUDA_TRY(cudaMemsetAsync(h->F.f[f], 0, n, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   std::fill(h->adm, h->adm + OLGPU_MAX_BH, 0.0);
-  if (h->equation == OLGPU_EQ_POISSON) {   // the Gaussian test's initial u and source
+  if (h->equation >= OLGPU_EQ_POISSON) {   // a test equation's initial u and source
     for (int l = 0; l < h->G.levels; l++) {
       const BoxList BL = level_list(h, l, blocks_all);
-      k_gaussian_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords,
-                                                                    h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
+      k_test_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords,
+                                                                puncture_params(&h->P),
+                                                                h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
     }
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1862,7 +1865,7 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, con
 olgpu_status olgpu_approximate_id(olgpu_hierarchy *h, int as_guess)
 {
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
-  if (h->equation == OLGPU_EQ_POISSON) return fail(OLGPU_ERR_INVALID_ARG, "the approximation is for punctures");
+  if (h->equation >= OLGPU_EQ_POISSON) return fail(OLGPU_ERR_INVALID_ARG, "the approximation is for punctures");
   olgpu_status st = olgpu_reset(h);
   if (st != OLGPU_OK) return st;
   const PunctureParams PP = puncture_params(&h->P);
@@ -1931,7 +1934,7 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
     return fail(OLGPU_ERR_INVALID_ARG, "precision must be OLGPU_PREC_FP64 or OLGPU_PREC_MIXED");
   CUDA_TRY(cudaSetDevice(h->device));
   if (precision == OLGPU_PREC_MIXED) {
-    if (h->equation == OLGPU_EQ_POISSON)
+    if (h->equation >= OLGPU_EQ_POISSON)
       return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the puncture equations");
     if (h->P.boundary != OLGPU_BC_ROBIN)
       return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the Robin boundary");
@@ -1995,7 +1998,7 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
     else dispatch_smooth32<0>(h, level, sweeps);
   } else {
     if (h->equation == 1) dispatch_smooth<1>(h, level, sweeps, 0);
-    else if (h->equation == 2) dispatch_smooth<2>(h, level, sweeps, 0);
+    else if (h->equation >= 2) dispatch_smooth<2>(h, level, sweeps, 0);
     else dispatch_smooth<0>(h, level, sweeps, 0);
   }
   CUDA_TRY(cudaEventRecord(h->ev1, h->stream));

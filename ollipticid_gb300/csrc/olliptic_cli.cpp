@@ -7,8 +7,8 @@
 // program.  Flags of the puncture FAS path are read with the reference's names
 // and defaults; flags outside it (output, printing, symmetry, MPI) are accepted
 // and ignored, as the reference ignores unknown flags.  Equations other than
-// Punctures / Punctures_scalar_field / Poisson (the reference's Gaussian
-// test) are refused, and so are boundary conditions other than Robin and
+// Punctures / Punctures_scalar_field and the reference's test equations
+// Poisson (the Gaussian test), Boundary-test and Multibox-test are refused, and so are boundary conditions other than Robin and
 // Dirichlet (the reference's default).
 //
 // Methods (-m): Vcycle (the default) and AppPuncture (the analytic
@@ -523,6 +523,8 @@ int main(int argc, char **argv)
   if (equation == "Punctures") p.equation = OLGPU_EQ_PUNCTURES;
   else if (equation == "Punctures_scalar_field") p.equation = OLGPU_EQ_PUNCTURES_SCALAR;
   else if (equation == "Poisson") p.equation = OLGPU_EQ_POISSON;
+  else if (equation == "Boundary-test") p.equation = OLGPU_EQ_BOUNDARY_TEST;
+  else if (equation == "Multibox-test") p.equation = OLGPU_EQ_MULTIBOX_TEST;
   else {
     std::fprintf(stderr, "Olliptic_gpu.x: equation %s is not on the puncture FAS path\n", equation.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
@@ -675,7 +677,7 @@ int main(int argc, char **argv)
     }
     if (f) std::fclose(f);
   }
-  if (!approx_only && p.equation != OLGPU_EQ_POISSON) {   // Vcycle prints ADM for punctures only
+  if (!approx_only && p.equation < OLGPU_EQ_POISSON) {   // Vcycle prints ADM for punctures only
     std::printf("Puncure method: \n");
     double adm[OLGPU_MAX_BH];
     olgpu_adm_mass(h, adm);

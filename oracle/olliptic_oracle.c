@@ -568,13 +568,45 @@ static double gaussian(double x, double y, double z)
   return (a * exp(-0.5 * r2));
 }
 
+/* Boundary-test and Multibox-test, src/operator.cc:1772-1857 (the source is
+ * of the Laplacian alone, as the reference writes it) */
+static int dcomp0(double r) { return fabs(r) <= 3 * DBL_EPSILON; }
+
+static double test_boundary(double x, double y, double z)
+{
+  double r = sqrt(x * x + y * y + z * z);
+  return !dcomp0(r) ? (0.004 * tanh(r) / r) : (0.004);
+}
+
+static double test_boundary_source(double x, double y, double z)
+{
+  double r = sqrt(x * x + y * y + z * z);
+  return !dcomp0(r) ? (-2.0 * 0.004 * tanh(r) / (r * cosh(r) * cosh(r))) : (-2.0 * 0.004);
+}
+
+static double test_mfunct(const orc_problem *p, double x, double y, double z)
+{
+  double r2_1 = (x - p->x[0]) * (x - p->x[0]) + y * y + z * z;
+  double r2_2 = (x - p->x[1]) * (x - p->x[1]) + y * y + z * z;
+  double a = 0.05;
+  return (exp(-a * r2_1) + exp(-a * r2_2));
+}
+
+static double test_mfunct_source(const orc_problem *p, double x, double y, double z)
+{
+  double r2_1 = (x - p->x[0]) * (x - p->x[0]) + y * y + z * z;
+  double r2_2 = (x - p->x[1]) * (x - p->x[1]) + y * y + z * z;
+  double a = 0.05;
+  return (2.0 * a * exp(-a * r2_1) * ((2 * a * r2_1 - 3)) + 2.0 * a * exp(-a * r2_2) * ((2 * a * r2_2 - 3)));
+}
+
 /* ------------------------------------------------------------------------ */
 /* pointwise operator: include/elliptic.h:405-445                            */
 /* ------------------------------------------------------------------------ */
 static inline double op_at(const orc_solver *S, const obox *B, long p, double lap)
 {
   const double *u = B->f[F_U], *b = B->f[F_B], *c = B->f[F_C];
-  if (S->P.equation == 2) return lap + u[p] * u[p];   /* poisson_OP, include/elliptic.h:359-362 */
+  if (S->P.equation >= 2) return lap + u[p] * u[p];   /* poisson_OP, include/elliptic.h:359-362 */
   if (S->P.equation == 0) return lap + b[p] / pow(c[p] + u[p], 7);
   const double *d = B->f[F_D], *e = B->f[F_E];
   return lap + b[p] / pow(c[p] + u[p], 7) + d[p] * (c[p] + u[p]) + e[p] * pow(c[p] + u[p], 5);
@@ -583,7 +615,7 @@ static inline double op_at(const orc_solver *S, const obox *B, long p, double la
 static inline double duop_at(const orc_solver *S, const obox *B, long p, double dl)
 {
   const double *u = B->f[F_U], *b = B->f[F_B], *c = B->f[F_C];
-  if (S->P.equation == 2) return dl + 2.0 * u[p];   /* poisson_duOP */
+  if (S->P.equation >= 2) return dl + 2.0 * u[p];   /* poisson_duOP */
   if (S->P.equation == 0) return dl - 7.0 * b[p] / pow(c[p] + u[p], 8);
   const double *d = B->f[F_D], *e = B->f[F_E];
   return dl - 7.0 * b[p] / pow(c[p] + u[p], 8) + d[p] + 5 * e[p] * pow(c[p] + u[p], 4);
@@ -1089,18 +1121,28 @@ static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
         for (int i = 0; i < B->D.n[0]; i++) {
           double x = dom_coord(&B->D, 0, i), y = dom_coord(&B->D, 1, j), z = dom_coord(&B->D, 2, k);
           long q = IDX(B, i, j, k);
-          if (p->equation == 2) {
-            /* the Gaussian test (src/operator.cc:640-655, 1865-1887): rho0 =
-             * Gaussian_source on every point, then the Robin boundary value
-             * 0 on the BOUNDARY points (Set_Boundary, src/boundary.cc:8-78),
-             * and u = Gaussian on every point as the initial guess */
+          if (p->equation >= 2) {
+            /* the test equations (src/operator.cc:640-673, 1145-1175): rho0
+             * = the source on every point, then the boundary value on the
+             * BOUNDARY points (Set_Boundary, src/boundary.cc:8-78: Robin's
+             * coefficient 0, or Dirichlet's boundary function), and u = the
+             * boundary function on every point as the initial guess */
             const int bb = B->D.buf;
             const int ghost = i < bb || j < bb || k < bb || i >= B->D.n[0] - bb || j >= B->D.n[1] - bb ||
                               k >= B->D.n[2] - bb;
-            /* the boundary value: Robin's coefficient 0, or Dirichlet's
-             * boundary function (the Gaussian itself) */
-            B->f[F_RHO][q] = ghost ? (p->boundary == 1 ? gaussian(x, y, z) : 0.0) : gaussian_source(x, y, z);
-            B->f[F_U][q] = gaussian(x, y, z);
+            double g, src;
+            if (p->equation == 3) {
+              g = test_boundary(x, y, z);
+              src = test_boundary_source(x, y, z);
+            } else if (p->equation == 4) {
+              g = test_mfunct(p, x, y, z);
+              src = test_mfunct_source(p, x, y, z);
+            } else {
+              g = gaussian(x, y, z);
+              src = gaussian_source(x, y, z);
+            }
+            B->f[F_RHO][q] = ghost ? (p->boundary == 1 ? g : 0.0) : src;
+            B->f[F_U][q] = g;
             continue;
           }
           B->f[F_B][q] = punctures_b(p, x, y, z);

@@ -19,7 +19,8 @@ extern "C" {
 #define ORC_MAX_BH 16
 
 typedef struct {
-  int equation;            /* 0 Punctures, 1 Punctures_scalar_field, 2 Poisson (Gaussian test) */
+  int equation;            /* 0 Punctures, 1 Punctures_scalar_field, 2 Poisson (Gaussian test),
+                              3 Boundary-test, 4 Multibox-test */
   int numbh;
   double mp[ORC_MAX_BH];
   double x[ORC_MAX_BH], y[ORC_MAX_BH], z[ORC_MAX_BH];

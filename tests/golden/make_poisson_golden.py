@@ -1,14 +1,16 @@
-"""Regenerates tests/golden/poisson/*.npz: the reference's Gaussian test
-(-eq Poisson: Lap u + u^2 = a e^{-r^2}(a + e^{r^2/2}(r^2 - 3)), solution
-u = a e^{-r^2/2}, a = 0.004) from its own Olliptic.x (oracle/_ref, built
-from its unmodified sources by `make -C oracle ref`).
+"""Regenerates tests/golden/poisson/*.npz: the reference's test equations
+(Lap u + u^2 = source) from its own Olliptic.x (oracle/_ref, built from its
+unmodified sources by `make -C oracle ref`): the Gaussian test (-eq Poisson,
+solution u = a e^{-r^2/2}, a = 0.004) at 2nd and 4th order and
+Boundary-test.
 
     make -C oracle ref && python tests/golden/make_poisson_golden.py
 
-Each case (2nd and 4th order, L = 10, 3 levels, Robin boundary) is run at
-N = 25 and 49; the fixture holds, per N, the printed u.X, u.Y, u.Z (first
-column as text, values as floats), the cycles the reference ran, and its
-largest distance from the exact Gaussian on the u.X points.
+Each case (L = 10 or 20, 3 levels, Robin boundary) is run at N = 25 and 49;
+the fixture holds, per N, the printed u.X, u.Y, u.Z (first column as text,
+values as floats), the cycles the reference ran, and for the Gaussian test
+its largest distance from the exact solution on the u.X points (NaN for the
+others, whose exact solutions are not known).
 """
 import os
 import shutil
@@ -24,7 +26,15 @@ from tests.golden.make_output_golden import parse_data_file  # noqa: E402
 
 REF_CLI = os.path.join(ROOT, "oracle", "_ref", "Olliptic.x")
 BASE = "-eq Poisson -B Robin -L 10 -l 3 -s 1e-12 -Dp 0.1 -p1d no"
-POISSON_CASES = {"o2": BASE + " -O 2", "o4": BASE + " -O 4"}
+POISSON_CASES = {
+    "o2": BASE + " -O 2",
+    "o4": BASE + " -O 4",
+    "boundary_test_o4": "-eq Boundary-test -B Robin -L 10 -l 3 -s 1e-12 -Dp 0.1 -p1d no -O 4",
+}
+# Multibox-test has no fixture: the reference's own runs of it (two unit
+# Gaussians at x = -3, 3, L = 20, N = 25, 2nd order, Robin or Dirichlet)
+# diverge on the coarsest grid (norm 1e10 in the first cycle) and did not
+# finish in ten minutes; the test checks its initial state instead.
 RESOLUTIONS = (25, 49)
 
 
@@ -45,7 +55,8 @@ def main():
             cyc = [int(line.split()[0]) for line in open(os.path.join(run, "Output", "Loo.gp")) if line.strip()]
             rec[f"cycles_{N}"] = np.array(max(cyc) + 1)
             a = np.loadtxt(os.path.join(run, "Output", "u.X"))
-            rec[f"max_error_{N}"] = np.array(np.max(np.abs(a[:, 1] - 0.004 * np.exp(-0.5 * a[:, 0] ** 2))))
+            exact = 0.004 * np.exp(-0.5 * a[:, 0] ** 2) if "-eq Poisson" in args else np.nan
+            rec[f"max_error_{N}"] = np.array(np.max(np.abs(a[:, 1] - exact)))
         np.savez_compressed(os.path.join(HERE, "poisson", name + ".npz"), **rec)
         print(name, {k: float(v) for k, v in rec.items() if k.startswith(("cycles", "max_error"))})
 

@@ -37,11 +37,17 @@ def test_gaussian_test_matches_the_reference(path, tmp_path):
             ours = np.loadtxt(run / "Output" / name)
             pts, want = cut(g, name, int(N))
             assert np.array_equal(ours[:, 0], pts[:, "XYZ".index(name[-1])])
-            tol = np.where(level_of(pts) < mg, 1e-6, 1e-9)
+            # both runs stop at residual 1e-12; Boundary-test converges so
+            # slowly (the reference needs 244 cycles at N = 49) that its stop
+            # lies about 1e-8 from the fixed point
+            sol_tol = 1e-9 if "-eq Poisson" in args else 1e-7
+            tol = np.where(level_of(pts) < mg, 1e-6, sol_tol)
             assert (np.abs(ours[:, 1] - want) <= tol).all(), name
-        # the distance from the exact solution, over the points read from
-        # the solution levels (a multigrid coarse grid holds the last
-        # coarse-grid approximation there, in the reference as here)
+        # the distance from the exact solution (the Gaussian test's), over
+        # the points read from the solution levels (a multigrid coarse grid
+        # holds the last coarse-grid approximation there, as in the reference)
+        if np.isnan(float(g[f"max_error_{int(N)}"])):
+            continue
         a = np.loadtxt(run / "Output" / "u.X")
         pts, want = cut(g, "u.X", int(N))
         sol = level_of(pts) >= mg
@@ -59,3 +65,20 @@ def test_mixed_precision_is_refused_for_the_gaussian_test():
             E.set_precision(True)
         rep = E.Solve()
         assert rep.status == 0
+
+
+def test_multibox_initial_state_is_the_oracles():
+    """Multibox-test (two Gaussians at x = bhx1, bhx2): its source and initial
+    u on every box, Robin and Dirichlet (the reference's runs of it diverge,
+    so the state it starts from is what is compared)."""
+    import ollipticid_gb300 as og
+    from oracle import oracle as oracle_mod
+    for bc in ("Robin", "Dirichlet"):
+        P = og.parse_olliptic_args(("-eq Multibox-test -B " + bc + " -NumBH 2 -bhx1 -3 -bhx2 3 -L 20 -N 25 -l 3 "
+                                    "-O 2").split())
+        orc = oracle_mod.Oracle(P.oracle_dict())
+        with og.Elliptic(P) as E:
+            for b in range(len(E.boxes)):
+                for name in ("u", "rho"):
+                    got, want = E.get_field(b, name).ravel(), orc.field(b, name).ravel()
+                    assert np.max(np.abs(got - want)) <= 1e-15 * max(1.0, np.max(np.abs(want))), (bc, b, name)
