@@ -71,6 +71,7 @@ struct XferJob {
   int row_axis;         // row kernel: rows run along x (0) or y (1)
   int pad_;
   long long rblk0;      // row kernel: first block of this job
+  long long pblk0;      // pair kernel (two x-neighbour targets a thread): first block of this job
   int sstart[3], sstep[3];   // XM_STRIDED: source node of target r0 and its step
   // periodic linear jobs (lin2 = 1): along each axis the table entries of the
   // targets r0 + 2m + q are those of r0 + q with window start and node moved

@@ -884,66 +884,87 @@ __global__ void __launch_bounds__(256) k_prolong_correct(const XferJob *__restri
                                                          const DevBox *__restrict__ boxes, Fields F,
                                                          const AxisEntry *__restrict__ tab, int fe, int fww)
 {
+  // two x-neighbour targets per thread: the job search, the index split, the
+  // y and z axis entries and the boxes are shared by both
   int lo = 0, hi = njobs - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].blk0 <= (long long)blockIdx.x) lo = mid;
+    if (jobs[mid].pblk0 <= (long long)blockIdx.x) lo = mid;
     else hi = mid - 1;
   }
   const XferJob &J = jobs[lo];
-  const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
+  const long long t = ((long long)blockIdx.x - J.pblk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
-  if (t >= (long long)e0 * e1 * e2) return;
-  const int i = J.r0[0] + ((int)t % e0);
-  const int r = (int)t / e0;
+  const int h0 = (e0 + 1) >> 1;
+  if (t >= (long long)h0 * e1 * e2) return;
+  const int ih = (int)t % h0;
+  const int r = (int)t / h0;
   const int j = J.r0[1] + (r % e1);
   const int k = J.r0[2] + (r / e1);
   const DevBox T = boxes[J.tbox];
-  if (J.iter != IT_ALL) {
-    const int b = T.buf;
-    const bool inside = i >= b && i < T.n[0] - b && j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
-    if ((J.iter == IT_INSIDE) != inside) return;
-  }
-  // the axis entries: formed from the job's two per-parity entries on a
-  // periodic job, else read from the tables
-  int sx, sy_, sz_, nx, ny, nz, ex, ey, ez;
-  double wx0, wx1, wy0, wy1, wz0, wz1;
+  const DevBox S = boxes[J.sbox];
+  const int b = T.buf;
+  const bool yz_inside = j >= b && j < T.n[1] - b && k >= b && k < T.n[2] - b;
+  // y and z entries: from the job's per-parity entries on a periodic job,
+  // else from the tables
+  int sy_, sz_, ny, nz, ey, ez;
+  double wy0, wy1, wz0, wz1;
+  bool yz_sel = true;
   if (J.lin2) {
-    const int qi = (i - J.r0[0]) & 1, qj = (j - J.r0[1]) & 1, qk = (k - J.r0[2]) & 1;
-    const int mi = (i - J.r0[0]) >> 1, mj = (j - J.r0[1]) >> 1, mk = (k - J.r0[2]) >> 1;
-    sx = J.lstart[0][qi] + mi, sy_ = J.lstart[1][qj] + mj, sz_ = J.lstart[2][qk] + mk;
-    nx = J.lnode[0][qi] + mi, ny = J.lnode[1][qj] + mj, nz = J.lnode[2][qk] + mk;
-    ex = J.lexact[0][qi], ey = J.lexact[1][qj], ez = J.lexact[2][qk];
-    wx0 = J.lw0[0][qi], wx1 = J.lw1[0][qi], wy0 = J.lw0[1][qj], wy1 = J.lw1[1][qj];
-    wz0 = J.lw0[2][qk], wz1 = J.lw1[2][qk];
+    const int qj = (j - J.r0[1]) & 1, qk = (k - J.r0[2]) & 1;
+    const int mj = (j - J.r0[1]) >> 1, mk = (k - J.r0[2]) >> 1;
+    sy_ = J.lstart[1][qj] + mj, sz_ = J.lstart[2][qk] + mk;
+    ny = J.lnode[1][qj] + mj, nz = J.lnode[2][qk] + mk;
+    ey = J.lexact[1][qj], ez = J.lexact[2][qk];
+    wy0 = J.lw0[1][qj], wy1 = J.lw1[1][qj], wz0 = J.lw0[2][qk], wz1 = J.lw1[2][qk];
   } else {
-    const AxisEntry &ax = tab[J.tab[0] + i];
     const AxisEntry &ay = tab[J.tab[1] + j];
     const AxisEntry &az = tab[J.tab[2] + k];
-    if (!(ax.sel && ay.sel && az.sel)) return;
-    sx = ax.start, sy_ = ay.start, sz_ = az.start, nx = ax.node, ny = ay.node, nz = az.node;
-    ex = ax.exact, ey = ay.exact, ez = az.exact;
-    wx0 = ax.w[0], wx1 = ax.w[1], wy0 = ay.w[0], wy1 = ay.w[1], wz0 = az.w[0], wz1 = az.w[1];
+    yz_sel = ay.sel && az.sel;
+    sy_ = ay.start, sz_ = az.start, ny = ay.node, nz = az.node;
+    ey = ay.exact, ez = az.exact;
+    wy0 = ay.w[0], wy1 = ay.w[1], wz0 = az.w[0], wz1 = az.w[1];
   }
-  const DevBox S = boxes[J.sbox];
+  if (!yz_sel) return;
   const V *ec = F.f[fe] + S.off, *wc = F.f[fww] + S.off;
-  auto v = [&](long long q) -> V { return ec[q] - wc[q]; };
-  V vf;
-  if (ex && ey && ez) {
-    vf = v(pidx(S, nx, ny, nz));
-  } else {
-    const int i0 = sx, j0 = sy_, k0 = sz_;
-    const V dxi = (V)wx0, dxf = (V)wx1, dyi = (V)wy0, dyf = (V)wy1, dzi = (V)wz0, dzf = (V)wz1;
-    const V v000 = v(pidx(S, i0, j0, k0)), v100 = v(pidx(S, i0 + 1, j0, k0));
-    const V v010 = v(pidx(S, i0, j0 + 1, k0)), v110 = v(pidx(S, i0 + 1, j0 + 1, k0));
-    const V v001 = v(pidx(S, i0, j0, k0 + 1)), v101 = v(pidx(S, i0 + 1, j0, k0 + 1));
-    const V v011 = v(pidx(S, i0, j0 + 1, k0 + 1)), v111 = v(pidx(S, i0 + 1, j0 + 1, k0 + 1));
-    vf = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
-         ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
-  }
   V *ef = F.f[fe] + T.off;
-  const long long tp = pidx(T, i, j, k);
-  ef[tp] = ef[tp] + vf;
+  auto v = [&](long long q) -> V { return ec[q] - wc[q]; };
+#pragma unroll
+  for (int d = 0; d < 2; d++) {
+    const int i = J.r0[0] + 2 * ih + d;
+    if (i >= J.r1[0]) break;
+    if (J.iter != IT_ALL) {
+      const bool inside = yz_inside && i >= b && i < T.n[0] - b;
+      if ((J.iter == IT_INSIDE) != inside) continue;
+    }
+    int sx, nx, ex;
+    double wx0, wx1;
+    if (J.lin2) {
+      const int qi = (i - J.r0[0]) & 1, mi = (i - J.r0[0]) >> 1;
+      sx = J.lstart[0][qi] + mi, nx = J.lnode[0][qi] + mi, ex = J.lexact[0][qi];
+      wx0 = J.lw0[0][qi], wx1 = J.lw1[0][qi];
+    } else {
+      const AxisEntry &ax = tab[J.tab[0] + i];
+      if (!ax.sel) continue;
+      sx = ax.start, nx = ax.node, ex = ax.exact;
+      wx0 = ax.w[0], wx1 = ax.w[1];
+    }
+    V vf;
+    if (ex && ey && ez) {
+      vf = v(pidx(S, nx, ny, nz));
+    } else {
+      const int i0 = sx, j0 = sy_, k0 = sz_;
+      const V dxi = (V)wx0, dxf = (V)wx1, dyi = (V)wy0, dyf = (V)wy1, dzi = (V)wz0, dzf = (V)wz1;
+      const V v000 = v(pidx(S, i0, j0, k0)), v100 = v(pidx(S, i0 + 1, j0, k0));
+      const V v010 = v(pidx(S, i0, j0 + 1, k0)), v110 = v(pidx(S, i0 + 1, j0 + 1, k0));
+      const V v001 = v(pidx(S, i0, j0, k0 + 1)), v101 = v(pidx(S, i0 + 1, j0, k0 + 1));
+      const V v011 = v(pidx(S, i0, j0 + 1, k0 + 1)), v111 = v(pidx(S, i0 + 1, j0 + 1, k0 + 1));
+      vf = ((v000 * dxi + v100 * dxf) * dyi + (v010 * dxi + v110 * dxf) * dyf) * dzi +
+           ((v001 * dxi + v101 * dxf) * dyi + (v011 * dxi + v111 * dxf) * dyf) * dzf;
+    }
+    const long long tp = pidx(T, i, j, k);
+    ef[tp] = ef[tp] + vf;
+  }
 }
 
 // Set_In of a refinement level with the coarse FP64 operator folded in:

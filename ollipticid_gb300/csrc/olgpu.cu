@@ -58,6 +58,7 @@ struct Transfer {
   std::vector<XferJob> jobs;
   long long blocks = 0;
   long long row_blocks = 0;         // blocks of the row kernel (k_xfer_rows)
+  long long pair_blocks = 0;        // blocks of the pair kernel (k_prolong_correct)
   int width = 0;                    // kernel variant (xfer_width of the jobs)
   bool rows = false;                // run on k_xfer_rows
   bool strided = false;             // every job is a strided copy
@@ -304,6 +305,8 @@ void add_region_jobs(Transfer &X, XferJob base, const domain &T, const int sel_l
     J.row_axis = e0 >= e1 ? 0 : 1;
     J.rblk0 = X.row_blocks;
     X.row_blocks += cdiv((J.row_axis == 0 ? e1 : e0) * e2, kRowWarps);
+    J.pblk0 = X.pair_blocks;
+    X.pair_blocks += cdiv(cdiv(e0, 2) * e1 * e2, kThreads);
     X.jobs.push_back(J);
   }
 }
@@ -725,7 +728,7 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   if (h->fast_paths) {   // u_fine += P(u - ww) in one pass
     const Transfer &X = h->prolong_v[k];
     if (!X.jobs.empty()) {
-      k_prolong_correct<double, DevFields><<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(
+      k_prolong_correct<double, DevFields><<<(unsigned)X.pair_blocks, kThreads, 0, h->stream>>>(
           X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F, h->d_tab, F_U, F_WW);
       h->launches++;
     }
@@ -1021,7 +1024,7 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   if (h->fast_paths) {   // e_fine += P(e - ww) in one pass
     const Transfer &X = h->prolong_v32[k];
     if (!X.jobs.empty()) {
-      k_prolong_correct<float, DevFields32><<<(unsigned)X.blocks, kThreads, 0, h->stream>>>(
+      k_prolong_correct<float, DevFields32><<<(unsigned)X.pair_blocks, kThreads, 0, h->stream>>>(
           X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32, h->d_tab, G_E, G_WW);
       h->launches_mixed++;
     }
@@ -1103,6 +1106,7 @@ Transfer remap(const Transfer &X, int sfield, int tfield)
   Y.rows = X.rows;
   Y.strided = X.strided;
   Y.row_blocks = X.row_blocks;
+  Y.pair_blocks = X.pair_blocks;
   for (auto &J : Y.jobs) {
     J.sfield = sfield;
     J.tfield = tfield;
