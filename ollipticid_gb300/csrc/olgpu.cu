@@ -1247,7 +1247,11 @@ double elapsed_ms(cudaEvent_t a, cudaEvent_t b)
 extern "C" {
 
 const char *olgpu_last_error(void) { return g_last_error.c_str(); }
-const char *olgpu_version(void) { return "olgpu 0.2 (sm_103a, FP64 FAS; FP32/FP64 mixed precision)"; }
+const char *olgpu_version(void)
+{
+  return "olgpu 0.3 (sm_103a, FP64 FAS; FP32/FP64 mixed precision; Robin and Dirichlet boundaries; point gather; "
+         "continuous-batching server)";
+}
 
 void olgpu_problem_defaults(olgpu_problem *p)
 {
