@@ -625,7 +625,8 @@ int main(int argc, char **argv)
       return fail(st, "mixed precision");
     }
   }
-  if (approx_only || A.find({"-gpu-guess"}) && !std::strcmp(A.find({"-gpu-guess"}), "approx")) {
+  const char *guess = A.find({"-gpu-guess"});
+  if (approx_only || (guess && !std::strcmp(guess, "approx"))) {
     st = olgpu_approximate_id(h, approx_only ? 0 : 1);
     if (st != OLGPU_OK) {
       olgpu_hierarchy_destroy(h);
