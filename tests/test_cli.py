@@ -102,3 +102,16 @@ def test_cli_solve_matches_the_api(cli, case):
         for a, b in zip(adm, E.ADM_mass):
             assert a == b
         assert f"Solved in {rep.cycles} V-cycles" in r.stdout
+
+
+@pytest.mark.parametrize("args", [
+    "-eq Poisson -B Robin -L 10 -N 25 -O 4 -l 3",
+    "-eq Boundary-test -L 10 -N 25 -O 4 -l 3",
+    "-eq Multibox-test -B Dirichlet -NumBH 2 -bhx1 -3 -bhx2 3 -L 20 -N 25 -O 2 -l 3",
+    "-eq Punctures -NumBH 1 -bhmp1 0.5 -L 40 -N 25 -O 4 -l 3 -m AppPuncture",
+])
+def test_test_equations_methods_and_boundaries_are_accepted(cli, args):
+    """The test equations, the Dirichlet default and the analytic method parse
+    and plan without a GPU (the plan is the same host geometry as the solve)."""
+    r = run(cli, args + " -plan yes")
+    assert re.search(r"(\d+) levels \((\d+) multigrid\), (\d+) boxes", r.stdout), r.stdout
