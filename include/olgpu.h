@@ -140,6 +140,12 @@ int olgpu_num_levels(const olgpu_hierarchy *h);
 int olgpu_mgrid_levels(const olgpu_hierarchy *h);
 olgpu_status olgpu_box(const olgpu_hierarchy *h, int box, olgpu_box_info *out);
 
+/* The reference's storage order of a box's points (domain::Fix_Points,
+ * src/domain.cc:574-1388: corners, edges, faces, interior), the order its
+ * iterators and its 3-D dumps visit them: out receives nx*ny*nz indices
+ * into the lexicographic layout of the box (i fastest).  Host only. */
+olgpu_status olgpu_storage_order(const olgpu_box_info *box, long long *out);
+
 /* Field access by reference name: "u" "b" "c" "d" "e" "rho" (the source
  * rho0), "r", "w", "ww", "v".  Host arrays hold nx*ny*nz doubles in
  * lexicographic order, i fastest. */

@@ -85,6 +85,7 @@ SIGNATURES = {
     "olgpu_num_levels": (C.c_int, [C.c_void_p]),
     "olgpu_mgrid_levels": (C.c_int, [C.c_void_p]),
     "olgpu_box": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(BoxInfo)]),
+    "olgpu_storage_order": (C.c_int, [C.POINTER(BoxInfo), C.c_void_p]),
     "olgpu_upload": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_void_p]),
     "olgpu_download": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_void_p]),
     "olgpu_vcycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),

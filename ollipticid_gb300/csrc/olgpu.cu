@@ -1295,6 +1295,60 @@ static void fill_box_info(const domain &D, olgpu_box_info *o)
   o->zf = D.hi[2];
 }
 
+// domain::Fix_Points (src/domain.cc:574-1388): the 8 corner blocks, the 12
+// edge blocks, the 6 face blocks and the interior, each a triple loop whose
+// axes run over the low ghost band inward-out (b-1 .. 0), the high band
+// (n-b .. n-1) or the interior (b .. n-b-1).  One row per block: the
+// outer, middle and inner axis, and the band of x, y, z (L, H, I).
+olgpu_status olgpu_storage_order(const olgpu_box_info *box, long long *out)
+{
+  if (!box || !out) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  struct Block {
+    int axis[3];    // loop axes, outer to inner (0 = x, 1 = y, 2 = z)
+    char band[4];   // band of x, y, z
+  };
+  static const Block blocks[27] = {
+      {{2, 1, 0}, "LLL"}, {{2, 1, 0}, "LLH"}, {{2, 1, 0}, "HLL"}, {{2, 1, 0}, "HLH"},   // corners
+      {{2, 1, 0}, "LHL"}, {{2, 1, 0}, "LHH"}, {{2, 1, 0}, "HHL"}, {{2, 1, 0}, "HHH"},
+      {{0, 1, 2}, "LLI"}, {{0, 1, 2}, "LHI"}, {{0, 1, 2}, "HLI"}, {{0, 1, 2}, "HHI"},   // edges along z
+      {{0, 2, 1}, "LIL"}, {{0, 2, 1}, "LIH"}, {{0, 2, 1}, "HIL"}, {{0, 2, 1}, "HIH"},   // edges along y
+      {{2, 1, 0}, "ILL"}, {{2, 1, 0}, "ILH"}, {{2, 1, 0}, "IHL"}, {{2, 1, 0}, "IHH"},   // edges along x
+      {{0, 2, 1}, "LII"}, {{0, 2, 1}, "HII"}, {{1, 2, 0}, "ILI"}, {{1, 2, 0}, "IHI"},   // faces
+      {{2, 1, 0}, "IIL"}, {{2, 1, 0}, "IIH"},
+      {{2, 1, 0}, "III"}};                                                               // interior
+  const int n[3] = {box->nx, box->ny, box->nz}, b = box->buf;
+  for (int a = 0; a < 3; a++)
+    if (n[a] < 2 * b + 1 || b < 1) return fail(OLGPU_ERR_INVALID_ARG, "box smaller than its ghost bands");
+  // the values an axis takes in a band, in loop order
+  auto band = [&](int a, char c, std::vector<int> &v) {
+    v.clear();
+    if (c == 'L')
+      for (int t = b - 1; t >= 0; t--) v.push_back(t);
+    else if (c == 'H')
+      for (int t = n[a] - b; t < n[a]; t++) v.push_back(t);
+    else
+      for (int t = b; t < n[a] - b; t++) v.push_back(t);
+  };
+  long long q = 0;
+  std::vector<int> r[3];
+  for (const Block &B : blocks) {
+    for (int a = 0; a < 3; a++) band(a, B.band[a], r[a]);
+    const int A0 = B.axis[0], A1 = B.axis[1], A2 = B.axis[2];
+    int ijk[3];
+    for (int v0 : r[A0]) {
+      ijk[A0] = v0;
+      for (int v1 : r[A1]) {
+        ijk[A1] = v1;
+        for (int v2 : r[A2]) {
+          ijk[A2] = v2;
+          out[q++] = ((long long)ijk[2] * n[1] + ijk[1]) * n[0] + ijk[0];
+        }
+      }
+    }
+  }
+  return OLGPU_OK;
+}
+
 olgpu_status olgpu_plan_boxes(const olgpu_problem *p, olgpu_box_info *out, int cap, int *nboxes, int *nlevels,
                               int *mgrid_levels)
 {

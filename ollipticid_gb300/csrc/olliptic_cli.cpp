@@ -34,8 +34,8 @@
 // (the banner and log) is not written.  The directory is rotated like the reference's
 // (interface.cc:1470-1538): an existing <dir> becomes <dir>_prev, replacing
 // an older <dir>_prev.  -p2d yes adds the per-box planes u-l<l>b<i>-0.{yz,xz,xy}
-// (ffunction::Print_2D); the 3-D dumps (-p3d) are not written (they list the
-// points in the reference's permuted storage order).
+// (ffunction::Print_2D) and -p3d yes the dumps u-l<l>b<i>-0.xyz of every point
+// in the reference's storage order (ffunction::Print_3D).
 // Exit status 0 on success; otherwise the C ABI's status with its message on
 // stderr.
 #include "olgpu.h"
@@ -245,6 +245,27 @@ olgpu_status print_box_plane(olgpu_hierarchy *h, const BoxGeom &B, int g, int no
     std::fprintf(f, "\n");
   }
   std::fprintf(f, "\n");
+  std::fclose(f);
+  return OLGPU_OK;
+}
+
+// ffunction::Print_3D of one box (src/ffunction.cc:412-475): every point in
+// the reference's storage order (olgpu_storage_order), "%.12e\t" x, y, z and
+// the node value of u, then a line end; no blank line at the end.
+olgpu_status print_box_3d(olgpu_hierarchy *h, const BoxGeom &B, int g, const std::string &file)
+{
+  const size_t np = (size_t)B.b.nx * B.b.ny * B.b.nz;
+  std::vector<double> u(np);
+  std::vector<long long> order(np);
+  olgpu_status st = olgpu_download(h, g, "u", u.data());
+  if (st == OLGPU_OK) st = olgpu_storage_order(&B.b, order.data());
+  if (st != OLGPU_OK) return st;
+  FILE *f = std::fopen(file.c_str(), "a");
+  if (!f) return OLGPU_ERR_INVALID_ARG;
+  for (long long q : order) {
+    const int i = (int)(q % B.b.nx), j = (int)((q / B.b.nx) % B.b.ny), k = (int)(q / ((long long)B.b.nx * B.b.ny));
+    std::fprintf(f, "%.12e\t%.12e\t%.12e\t%.12e\t\n", B.coord(0, i), B.coord(1, j), B.coord(2, k), u[(size_t)q]);
+  }
   std::fclose(f);
   return OLGPU_OK;
 }
@@ -688,9 +709,10 @@ int main(int argc, char **argv)
   // elliptic::Print_Solution (src/output.cc:624-700), variable "u"
   const bool print_1d = A.logic({"-p1d", "--print-1d"}, true);
   const bool print_2d = A.logic({"-p2d", "--print-2d"}, false);
+  const bool print_3d = A.logic({"-p3d", "--print-3d"}, false);
   const bool print_interpol = A.logic({"-pint", "--print-interpol"}, true);
   const bool interpol_output = A.logic({"-int", "--interpol-output"}, true);
-  if (print_1d || print_2d || print_interpol) {
+  if (print_1d || print_2d || print_3d || print_interpol) {
     const int ord = p.order + 1;
     std::printf("Printing...\n");
     olgpu_status ps = OLGPU_OK;
@@ -721,6 +743,16 @@ int main(int argc, char **argv)
               dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
           for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
             ps = print_box_plane(h, B, g, a, interpol_output, stem + ext[a]);
+        }
+    }
+    if (print_3d) {   // every point of every box, level by level
+      std::vector<int> in_level(nl, 0);
+      for (int l = l0; l < nl && ps == OLGPU_OK; l++)
+        for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
+          if (boxes[g].level != l) continue;
+          const BoxGeom B{boxes[g]};
+          ps = print_box_3d(h, B, g,
+                            dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0.xyz");
         }
     }
     if (print_interpol && ps == OLGPU_OK) {

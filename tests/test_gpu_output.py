@@ -137,3 +137,28 @@ def test_interpolation_is_the_oracles_bit_for_bit(case, ord):
             gb = E.interpolate(inside, ord=min(ord, min(E.boxes[b].n) - 1), box=b)
             wb = orc.interpolate(inside, min(ord, min(E.boxes[b].n) - 1), box=b)
             assert np.array_equal(gb.view(np.int64), wb.view(np.int64)), b
+
+
+STORAGE = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "storage", "*.npz")))
+
+
+@pytest.mark.parametrize("path", STORAGE, ids=lambda p: os.path.basename(p)[:-4])
+def test_3d_dumps_match_the_reference(path, tmp_path):
+    """Olliptic_gpu.x -p3d: every point of every box in the reference's
+    storage order (the order of the printed coordinates is compared exactly)
+    with u within the solve-to-solve difference (both stop at residual 1e-10;
+    the fixture keeps the reference's u in float32)."""
+    from tests.golden.make_storage_golden import order_of
+    g = np.load(path)
+    args = g["args"].item().decode()
+    r = subprocess.run([CLI] + args.split() + ["-o", "Output"], cwd=str(tmp_path), capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    mg = int(re.search(r"\((\d+) multigrid\)", r.stdout).group(1))
+    for f in g["files"]:
+        name = f.decode()
+        order, n, u = order_of(str(tmp_path / "Output" / name))
+        assert list(n) == list(g[name + "__n"]) and np.array_equal(order, g[name + "__order"]), name
+        if name + "__u" in g.files:
+            tol = 1e-6 if int(name[3:name.index("b")]) < mg else 5e-9
+            assert np.max(np.abs(u - g[name + "__u"].astype(np.float64))) <= tol, name
