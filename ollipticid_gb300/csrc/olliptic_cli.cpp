@@ -30,8 +30,9 @@
 // plane u.XY (-pint, multigrid::Print_Interpol_1D / _2D, src/multigrid.cc:
 // 151-880), with the reference's number formats, each cycle's
 // pre-smoothing norms per level as Loo.gp (-so yes, elliptic::Print_Pre_Cycle,
-// src/output.cc:1355-1460), and the command line as <dir>.run.  stdout0.out
-// (the banner and log) is not written.  The directory is rotated like the reference's
+// src/output.cc:1355-1460), the banner and the per-cycle norms as
+// stdout0.out (Print_Info, Print_Pre_Cycle / Print_Post_Cycle) and the
+// command line as <dir>.run.  The directory is rotated like the reference's
 // (interface.cc:1470-1538): an existing <dir> becomes <dir>_prev, replacing
 // an older <dir>_prev.  -p2d yes adds the per-box planes u-l<l>b<i>-0.{yz,xz,xy}
 // (ffunction::Print_2D) and -p3d yes the dumps u-l<l>b<i>-0.xyz of every point
@@ -144,6 +145,67 @@ bool prepare_output_dir(const std::string &name, int argc, char **argv)
   fs::permissions(run, fs::perms::owner_exec | fs::perms::group_exec | fs::perms::others_exec,
                   fs::perm_options::add, ec);
   return true;
+}
+
+// elliptic::Print_Info (src/output.cc:1030-1345) into <dir>stdout0.out: the
+// run's parameters and every box (ffunction::Print_Info with the domain's
+// stream form, src/domain.cc:1759-1790), then "Init Multigrid iteration".
+// `levels` and `mg` are the hierarchy's; the analytic method's hierarchy has
+// no multigrid grids, so its listing starts at the base.
+void write_banner(FILE *f, const olgpu_problem &p, const char *equation_str, const char *method_str,
+                  const char *boundary_str, const std::string &dir, const std::vector<olgpu_box_info> &boxes, int nb,
+                  int nl, int mg, bool skip_mg)
+{
+  const double eps_coarse = 2 * 2.220446049250313080847e-16;
+  const double eps_solv = p.tol < eps_coarse ? eps_coarse : p.tol;
+  static const char *orders[5] = {"", "2nd", "4th", "6th", "8th"};
+  std::fprintf(f, " ---------------------------- Olliptic -----------------------------\n");
+  std::fprintf(f, "Equation\t:\t%s\nMethod\t\t:\t%s\n", equation_str, method_str);
+  std::fprintf(f, "Tolerance \n Fine grid\t:\t%g\n Coarse grid\t:\t%g\n", eps_solv, eps_coarse);
+  std::fprintf(f, "Smooth sweeps \n Pre\t\t:\t%d\n Post\t\t:\t%d\n", p.nu1, p.nu2);
+  std::fprintf(f, "Levels\t\t:\t%d\nBoxes\t\t:\t%d\nOrder\t\t:\t%s\n\n", nl - mg, p.numbh,
+               p.order >= 2 && p.order <= 8 ? orders[p.order / 2] : "");
+  std::fprintf(f, "Boundary\t:\t%s\nSymmetry\t:\tFull domain\n\nOutput to\t:\t%s*\n", boundary_str, dir.c_str());
+  std::vector<int> in_level(nl, 0);
+  for (int l = skip_mg ? mg : 0; l < nl; l++)
+    for (int g = 0; g < nb; g++) {
+      if (boxes[g].level != l) continue;
+      const olgpu_box_info &b = boxes[g];
+      std::fprintf(f, "\n  __________________________________________________________________\n");
+      std::fprintf(f, "  level: %d | box: %d | Interpolation: %d\n", l - (skip_mg ? mg : 0), in_level[l]++, b.order);
+      std::fprintf(f, "  ------------------------------------------------------------------\n");
+      std::fprintf(f, "  nx = %d, \t\tny = %d, \t\tnz = %d\n", b.nx, b.ny, b.nz);
+      std::fprintf(f, "  dx = %.3e, \tdy = %.3e, \tdz = %.3e\n", b.dx, b.dy, b.dz);
+      std::fprintf(f, "  lx = %.2f, \t\tly = %.2f, \t\tlz = %.2f\n", b.xf - b.xi, b.yf - b.yi, b.zf - b.zi);
+      std::fprintf(f, "  x-->[%.2f,%.2f]\ty-->[%.2f,%.2f]\tz-->[%.2f,%.2f]\n", b.xi, b.xf, b.yi, b.yf, b.zi, b.zf);
+    }
+  std::fprintf(f, "--------------------------------------------------------------------\n  Init Multigrid iteration\n");
+}
+
+// One V-cycle's lines of <dir>stdout0.out (elliptic::Print_Pre_Cycle /
+// Print_Post_Cycle, src/output.cc:1355-1605): the cycle header, the
+// pre-smoothing norms from the finest level down, the coarsest solve's, the
+// post-smoothing norms back up, and the cycle's norm against the tolerance.
+void write_cycle(FILE *f, int c, int nl, const std::vector<double> &pre, const std::vector<double> &post,
+                 double eps_solv)
+{
+  const int top = nl - 1;
+  auto line = [&](int k, double v) {
+    for (int j = 0; j < k; j++) std::fprintf(f, "|\t\t\t");
+    std::fprintf(f, "|Loo[%d] : %.8e", k, v);
+    for (int j = k + 1; j <= top + 1; j++) std::fprintf(f, "|\t\t\t");
+    std::fprintf(f, "\n");
+  };
+  auto rule = [&]() {
+    for (int j = 0; j <= top; j++) std::fprintf(f, "========================");
+    std::fprintf(f, "\n");
+  };
+  std::fprintf(f, "\n\nCycle: %d\n", c);
+  rule();
+  for (int k = top; k >= 0; k--) line(k, pre[k]);
+  for (int k = 1; k <= top; k++) line(k, post[k]);
+  rule();
+  std::fprintf(f, "%.8e  -->  %.8e\n", post[top], eps_solv);
 }
 
 // ffunction::Print_1D of one box and one axis: at every node along `axis`
@@ -635,6 +697,20 @@ int main(int argc, char **argv)
   const std::string dir = out + "/";
   const char *so = A.find({"-so", "--std-output"});
   const bool std_output = !so || !std::strcmp(so, "yes");
+  const bool std_partial = so && !std::strcmp(so, "partial");
+  {   // stdout0.out: the banner now (main.cc:111), the cycles after the solve
+    FILE *f = std::fopen((dir + "stdout0.out").c_str(), "a");
+    if (f && (std_output || std_partial)) {
+      const char *eq_str = p.equation == OLGPU_EQ_PUNCTURES        ? "Punctures ID"
+                           : p.equation == OLGPU_EQ_POISSON        ? "Poisson"
+                           : p.equation == OLGPU_EQ_BOUNDARY_TEST  ? "Robin boundary test"
+                           : p.equation == OLGPU_EQ_MULTIBOX_TEST  ? "Multibox test"
+                                                                   : "";   // the scalar field has no name there
+      write_banner(f, p, eq_str, approx_only ? "Analitical Approximate" : "Multigrid V-Cycles",
+                   p.boundary == OLGPU_BC_ROBIN ? "Robin" : "Dirichlet", dir, boxes, nb, nl, mg, approx_only);
+    }
+    if (f) std::fclose(f);
+  }
 
   olgpu_hierarchy *h = nullptr;
   st = olgpu_hierarchy_create(&p, A.integer({"-gpu-device"}, -1), &h);
@@ -688,6 +764,16 @@ int main(int argc, char **argv)
     }
     std::printf("Solved in %d V-cycles, norm %.6e, %.3f ms on the device\n", rep.cycles, rep.final_res,
                 olgpu_last_device_ms(h));
+  }
+  if (std_output && !approx_only) {   // stdout0.out: each cycle's norms
+    FILE *f = std::fopen((dir + "stdout0.out").c_str(), "a");
+    std::vector<double> pre(nl), post(nl);
+    const double eps_coarse = 2 * 2.220446049250313080847e-16;
+    for (int c = 0; f && c < rep.cycles; c++) {
+      if (olgpu_level_norms(h, c, pre.data(), post.data()) != OLGPU_OK) break;
+      write_cycle(f, c, nl, pre, post, p.tol < eps_coarse ? eps_coarse : p.tol);
+    }
+    if (f) std::fclose(f);
   }
   // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
   if (std_output && !approx_only) {

@@ -69,7 +69,7 @@ def test_output_files_match_the_reference(path, tmp_path):
     mg = int(re.search(r"\((\d+) multigrid\)", r.stdout).group(1))
     level_of = box_levels(args)
     out = tmp_path / "Output"
-    ours = sorted(os.listdir(out))
+    ours = sorted(f for f in os.listdir(out) if f != "stdout0.out")   # the fixtures leave the log out
     assert ours == [f.decode() for f in g["files"]]
     for name in ours:
         p = str(out / name)
@@ -83,6 +83,14 @@ def test_output_files_match_the_reference(path, tmp_path):
             assert cyc.count(0) == levels and len(rows) % levels == 0
             assert cyc == [c for c in range(len(rows) // levels) for _ in range(levels)]
             assert all(float(v) >= 0.0 for _, v in rows)
+            # stdout0.out: one block a cycle, the levels' pre-smoothing norms
+            # down, the coarsest solve's, the post-smoothing norms back up
+            log = (out / "stdout0.out").read_text()
+            blocks = log.split("\n\nCycle: ")[1:]
+            assert len(blocks) == len(rows) // levels
+            for c, blk in enumerate(blocks):
+                assert blk.startswith(f"{c}\n") and blk.count("|Loo[") == 2 * levels - 1
+                assert "  -->  " in blk
             continue
         text, vals = parse_data_file(p)
         ref_text, ref_vals = g[name + "__text"], g[name + "__vals"]
