@@ -226,7 +226,28 @@ struct orc_solver {
   int extra_coarse;    /* checker option: keep coarsening below 12 points (down to >= 5) */
   double lnorm[64][2]; /* last cycle: smoother norms per level (pre, post) */
   double coarse_norm;
+  long ncycles;        /* top-level cycles run (the cycle count each starts from) */
+  /* every Print_Pre_Cycle / Print_Post_Cycle call of the solve, in order */
+  orc_event *ev;
+  long nev, cap_ev;
+  long w_cap;          /* checker guard: iterations of one level's W loop (the reference has none) */
 };
+
+static void log_event(orc_solver *S, int level, int post, long cycle, double norm)
+{
+  if (S->nev == S->cap_ev) {
+    const long cap = S->cap_ev ? 2 * S->cap_ev : 256;
+    orc_event *ev = (orc_event *)realloc(S->ev, sizeof(orc_event) * cap);
+    if (!ev) return;
+    S->ev = ev;
+    S->cap_ev = cap;
+  }
+  S->ev[S->nev].level = level;
+  S->ev[S->nev].post = post;
+  S->ev[S->nev].cycle = cycle;
+  S->ev[S->nev].norm = norm;
+  S->nev++;
+}
 
 static inline long IDX(const obox *B, int i, int j, int k)
 {
@@ -968,88 +989,101 @@ static void full_weight_w(obox *B)
   free(t);
 }
 
-/* elliptic::FASN with Wcycle = false, src/elliptic.cc:1468-1968 */
-static double fasn(orc_solver *S, int k, int k_top)
+/* elliptic::FASN, src/elliptic.cc:1468-1968.  With wcycle the level repeats
+ * its body (and so every coarser level its own loop) while its
+ * post-smoothing norm is above eps_solv (1956); `cycle` counts the
+ * iterations from the caller's count and is what Print_Pre_Cycle /
+ * Print_Post_Cycle print (1499, 1535, 1818, 1936, 1948). */
+static double fasn(orc_solver *S, int k, int k_top, int wcycle, long icycle)
 {
   const int mg = S->mgrid_levels;
   const int order = S->P.order;
-  double norm_k = 0, norm_km1;
+  double norm_k = 0, norm_km1 = 0;
   obox *Bk = &S->box[S->first[k]];
   obox *Bc = &S->box[S->first[k - 1]];
   const int nk = S->ndl[k], nc = S->ndl[k - 1];
+  long cycle = icycle, iters = 0;
 
-  for (int i = 0; i < nk; i++) {                                  /* 1518-1533 */
-    if (k <= mg) robin_walk(S, &Bk[i], robin_update_pt);
-    double n = smooth_box(S, &Bk[i], S->P.nu1);
-    norm_k = n > norm_k ? n : norm_k;
-  }
-  if (k < 64) S->lnorm[k][0] = norm_k;
-  transferir(S, k, F_U, k - 1, F_U, IT_INSIDE, M_LAGRANGE, 3, 0, 0);   /* 1543-1546 */
-  for (int j = 0; j < nc; j++) {                                  /* 1582-1594 */
-    app_ell_operator(S, &Bc[j]);
-    if (k <= mg) robin_walk(S, &Bc[j], robin_operator_pt);
-  }
-  for (int i = 0; i < nk; i++) {                                  /* 1603-1614 */
-    app_ell_operator(S, &Bk[i]);
-    if (k <= mg) robin_walk(S, &Bk[i], robin_operator_pt);
-  }
-  for (int i = 0; i < nk; i++)                                    /* 1625-1649 */
-    for (long p = 0; p < Bk[i].npts; p++) Bk[i].f[F_W][p] = Bk[i].f[F_RHO][p] - Bk[i].f[F_R][p];
-  if (S->wsmooth)
-    for (int i = 0; i < nk; i++) full_weight_w(&Bk[i]);
-  if (k - 1 <= mg)                                                /* 1660-1676 */
-    transferir(S, k, F_W, k - 1, F_W, IT_ALL, M_LAGRANGE, 2, 1, 0);
-  else
-    transferir(S, k, F_W, k - 1, F_W, IT_ALL, M_LAGRANGE, 2, 0, 0);
-  for (int j = 0; j < nc; j++) {                                  /* 1692-1747 */
-    if (k <= mg)
-      axpy_all(&Bc[j], F_RHO, F_W, 1.0, F_R);
-    else {
-      for (long p = 0; p < Bc[j].npts; p++) Bc[j].f[F_W][p] = Bc[j].f[F_W][p] + Bc[j].f[F_R][p];
-      for (int i = 0; i < nk; i++) set_in(&Bc[j], &Bc[j], &Bk[i].D);
+  do {
+    norm_k = 0;
+    for (int i = 0; i < nk; i++) {                                  /* 1518-1533 */
+      if (k <= mg) robin_walk(S, &Bk[i], robin_update_pt);
+      double n = smooth_box(S, &Bk[i], S->P.nu1);
+      norm_k = n > norm_k ? n : norm_k;
     }
-  }
-  for (int j = 0; j < nc; j++)                                    /* 1756-1775 */
-    memcpy(Bc[j].f[F_WW], Bc[j].f[F_U], sizeof(double) * Bc[j].npts);
-  if (k == 1) {                                                   /* 1782-1816 */
-    for (int j = 0; j < nc; j++) {
-      double norm_prev;
-      norm_km1 = 1;
-      long guard = 0;
-      double first = -1.0;
-      do {
-        norm_prev = norm_km1;
-        robin_walk(S, &Bc[j], robin_update_pt);
-        norm_km1 = smooth_box_w(S, &Bc[j], 1, S->coarse_omega);
-        if (first < 0) first = norm_km1;
-        ++guard;
-        if (S->nan_flag) break;
-        if (S->coarse_rtol > 0 && norm_km1 <= S->coarse_rtol * first) break;
-      } while (norm_km1 > S->eps_coarse && norm_prev != norm_km1 && guard < S->coarse_cap);
-      S->coarse_iters = guard;
-      S->coarse_norm = norm_km1;
+    if (k < 64) S->lnorm[k][0] = norm_k;
+    log_event(S, k, 0, cycle, norm_k);                              /* 1535 */
+    transferir(S, k, F_U, k - 1, F_U, IT_INSIDE, M_LAGRANGE, 3, 0, 0);   /* 1543-1546 */
+    for (int j = 0; j < nc; j++) {                                  /* 1582-1594 */
+      app_ell_operator(S, &Bc[j]);
+      if (k <= mg) robin_walk(S, &Bc[j], robin_operator_pt);
     }
-  } else {
-    norm_km1 = fasn(S, k - 1, k_top);
-  }
-  (void)norm_km1;
-  for (int j = 0; j < nc; j++) axpy_all(&Bc[j], F_V, F_U, -1.0, F_WW);   /* 1827-1850 */
-  if (k <= mg)                                                    /* 1857-1885 */
-    transferir(S, k - 1, F_V, k, F_V, IT_ALL, M_LINEAR, 3, 1, 1);
-  else
-    transferir(S, k - 1, F_V, k, F_V, IT_INSIDE, M_LINEAR, order + 1, 1, 0);
-  for (int i = 0; i < nk; i++)                                    /* 1890-1903 */
-    for (long p = 0; p < Bk[i].npts; p++) Bk[i].f[F_U][p] = Bk[i].f[F_U][p] + Bk[i].f[F_V][p];
-  if (k > mg)                                                     /* 1905-1908 */
-    transferir(S, k - 1, F_U, k, F_U, IT_BOUNDARY, M_LAGRANGE, order + 1, 1, 0);
-  norm_k = 0;                                                     /* 1917-1932 */
-  for (int i = 0; i < nk; i++) {
-    if (k <= mg) robin_walk(S, &Bk[i], robin_update_pt);
-    double n = smooth_box(S, &Bk[i], S->P.nu2);
-    norm_k = n > norm_k ? n : norm_k;
-  }
-  if (k < 64) S->lnorm[k][1] = norm_k;
-  if (k == k_top) compute_adm(S);                                 /* 1939-1941 */
+    for (int i = 0; i < nk; i++) {                                  /* 1603-1614 */
+      app_ell_operator(S, &Bk[i]);
+      if (k <= mg) robin_walk(S, &Bk[i], robin_operator_pt);
+    }
+    for (int i = 0; i < nk; i++)                                    /* 1625-1649 */
+      for (long p = 0; p < Bk[i].npts; p++) Bk[i].f[F_W][p] = Bk[i].f[F_RHO][p] - Bk[i].f[F_R][p];
+    if (S->wsmooth)
+      for (int i = 0; i < nk; i++) full_weight_w(&Bk[i]);
+    if (k - 1 <= mg)                                                /* 1660-1676 */
+      transferir(S, k, F_W, k - 1, F_W, IT_ALL, M_LAGRANGE, 2, 1, 0);
+    else
+      transferir(S, k, F_W, k - 1, F_W, IT_ALL, M_LAGRANGE, 2, 0, 0);
+    for (int j = 0; j < nc; j++) {                                  /* 1692-1747 */
+      if (k <= mg)
+        axpy_all(&Bc[j], F_RHO, F_W, 1.0, F_R);
+      else {
+        for (long p = 0; p < Bc[j].npts; p++) Bc[j].f[F_W][p] = Bc[j].f[F_W][p] + Bc[j].f[F_R][p];
+        for (int i = 0; i < nk; i++) set_in(&Bc[j], &Bc[j], &Bk[i].D);
+      }
+    }
+    for (int j = 0; j < nc; j++)                                    /* 1756-1775 */
+      memcpy(Bc[j].f[F_WW], Bc[j].f[F_U], sizeof(double) * Bc[j].npts);
+    if (k == 1) {                                                   /* 1782-1816 */
+      for (int j = 0; j < nc; j++) {
+        double norm_prev;
+        norm_km1 = 1;
+        long guard = 0;
+        double first = -1.0;
+        do {
+          norm_prev = norm_km1;
+          robin_walk(S, &Bc[j], robin_update_pt);
+          norm_km1 = smooth_box_w(S, &Bc[j], 1, S->coarse_omega);
+          if (first < 0) first = norm_km1;
+          ++guard;
+          if (S->nan_flag) break;
+          if (S->coarse_rtol > 0 && norm_km1 <= S->coarse_rtol * first) break;
+        } while (norm_km1 > S->eps_coarse && norm_prev != norm_km1 && guard < S->coarse_cap);
+        S->coarse_iters = guard;
+        S->coarse_norm = norm_km1;
+      }
+      log_event(S, 0, 0, cycle, norm_km1);                          /* 1818 */
+    } else {
+      norm_km1 = fasn(S, k - 1, k_top, wcycle, cycle);
+    }
+    (void)norm_km1;
+    for (int j = 0; j < nc; j++) axpy_all(&Bc[j], F_V, F_U, -1.0, F_WW);   /* 1827-1850 */
+    if (k <= mg)                                                    /* 1857-1885 */
+      transferir(S, k - 1, F_V, k, F_V, IT_ALL, M_LINEAR, 3, 1, 1);
+    else
+      transferir(S, k - 1, F_V, k, F_V, IT_INSIDE, M_LINEAR, order + 1, 1, 0);
+    for (int i = 0; i < nk; i++)                                    /* 1890-1903 */
+      for (long p = 0; p < Bk[i].npts; p++) Bk[i].f[F_U][p] = Bk[i].f[F_U][p] + Bk[i].f[F_V][p];
+    if (k > mg)                                                     /* 1905-1908 */
+      transferir(S, k - 1, F_U, k, F_U, IT_BOUNDARY, M_LAGRANGE, order + 1, 1, 0);
+    norm_k = 0;                                                     /* 1917-1932 */
+    for (int i = 0; i < nk; i++) {
+      if (k <= mg) robin_walk(S, &Bk[i], robin_update_pt);
+      double n = smooth_box(S, &Bk[i], S->P.nu2);
+      norm_k = n > norm_k ? n : norm_k;
+    }
+    if (k < 64) S->lnorm[k][1] = norm_k;
+    log_event(S, k, 1, cycle, norm_k);                              /* 1936 */
+    if (k == k_top) compute_adm(S);                                 /* 1939-1941 */
+    cycle++;
+    iters++;
+  } while (wcycle && norm_k > S->eps_solv && !S->nan_flag && iters < S->w_cap);   /* 1956 */
   return norm_k;
 }
 
@@ -1087,6 +1121,7 @@ static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
   S->extra_coarse = extra_coarse;
   S->eps_coarse = 2 * EPS;                          /* src/elliptic.cc:62 */
   S->coarse_cap = 1000000000L;
+  S->w_cap = 1000000000L;
   S->coarse_omega = 1.0;
   S->eps_solv = p->tol < S->eps_coarse ? S->eps_coarse : p->tol;
   S->ps_isigma = 1 / p->ps_sigma;                   /* src/elliptic.cc:71-81 */
@@ -1215,6 +1250,7 @@ void orc_destroy(orc_solver *S)
   free(S->box);
   free(S->ndl);
   free(S->first);
+  free(S->ev);
   free(S);
 }
 
@@ -1298,7 +1334,7 @@ int orc_interpolate(const orc_solver *S, int box, int first_level, const double 
 
 double orc_vcycle(orc_solver *S)
 {
-  return fasn(S, S->levels - 1, S->levels - 1);
+  return fasn(S, S->levels - 1, S->levels - 1, 0, S->ncycles++);
 }
 
 /* elliptic::Vcycle, src/elliptic.cc:1251-1342 */
@@ -1315,6 +1351,31 @@ int orc_solve(orc_solver *S, int max_cycles, double *final_res)
   if (final_res) *final_res = res;
   return S->nan_flag ? -c : c;
 }
+
+/* elliptic::Wcycle, src/elliptic.cc:1348-1380: W-cycles from the top level
+ * while res > eps && res < res_prev; each one repeats every level until its
+ * norm is <= eps_solv */
+int orc_solve_wcycle(orc_solver *S, int max_cycles, double *final_res)
+{
+  double res = 1e12, res_prev;
+  int c = 0;
+  do {
+    res_prev = res;
+    res = fasn(S, S->levels - 1, S->levels - 1, 1, S->ncycles++);
+    c++;
+    if (S->nan_flag) break;
+  } while (res > S->eps_solv && res < res_prev && c < max_cycles);
+  if (final_res) *final_res = res;
+  return S->nan_flag ? -c : c;
+}
+
+long orc_events(const orc_solver *S, long first, long cap, orc_event *out)
+{
+  for (long i = 0; i < cap && first + i < S->nev; i++) out[i] = S->ev[first + i];
+  return S->nev;
+}
+
+void orc_set_wcycle_cap(orc_solver *S, long cap) { S->w_cap = cap > 0 ? cap : 1000000000L; }
 
 void orc_adm(const orc_solver *S, double *out)
 {

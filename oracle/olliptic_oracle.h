@@ -71,6 +71,22 @@ void orc_approximate_id(orc_solver *s);
 double orc_vcycle(orc_solver *s);
 /* elliptic::Vcycle: cycles while res > eps && res < res_prev; returns cycles run */
 int orc_solve(orc_solver *s, int max_cycles, double *final_res);
+/* elliptic::Wcycle: W-cycles (every level repeated until its norm <= eps)
+ * while res > eps && res < res_prev; returns top-level cycles run */
+int orc_solve_wcycle(orc_solver *s, int max_cycles, double *final_res);
+/* One elliptic::Print_Pre_Cycle (post = 0) or Print_Post_Cycle (post = 1)
+ * call: the level (0: the coarsest solve), the cycle number it prints and
+ * the norm.  orc_events copies events [first, first+cap) and returns how many
+ * the solver has logged since it was created. */
+typedef struct {
+  int level;
+  int post;
+  long cycle;
+  double norm;
+} orc_event;
+long orc_events(const orc_solver *s, long first, long cap, orc_event *out);
+/* checker guard on one level's W loop (the reference has none) */
+void orc_set_wcycle_cap(orc_solver *s, long cap);
 /* ADM masses computed at the end of every top-level cycle */
 void orc_adm(const orc_solver *s, double *out);
 /* Single-box building blocks, exposed for unit tests. */

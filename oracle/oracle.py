@@ -39,6 +39,10 @@ class OrcBox(C.Structure):
                     "gxi", "gyi", "gzi", "gxf", "gyf", "gzf")]
 
 
+class OrcEvent(C.Structure):
+    _fields_ = [("level", C.c_int), ("post", C.c_int), ("cycle", C.c_long), ("norm", C.c_double)]
+
+
 _lib = None
 
 
@@ -70,6 +74,11 @@ def load():
         L.orc_vcycle.argtypes = [C.c_void_p]
         L.orc_solve.restype = C.c_int
         L.orc_solve.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        L.orc_solve_wcycle.restype = C.c_int
+        L.orc_solve_wcycle.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        L.orc_events.restype = C.c_long
+        L.orc_events.argtypes = [C.c_void_p, C.c_long, C.c_long, C.POINTER(OrcEvent)]
+        L.orc_set_wcycle_cap.argtypes = [C.c_void_p, C.c_long]
         L.orc_adm.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_approximate_id.argtypes = [C.c_void_p]
         L.orc_interpolate.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_void_p]
@@ -176,6 +185,19 @@ class Oracle:
         r = C.c_double()
         c = self.L.orc_solve(self._s, max_cycles, C.byref(r))
         return c, r.value
+
+    def solve_wcycle(self, max_cycles: int = 100000):
+        r = C.c_double()
+        c = self.L.orc_solve_wcycle(self._s, max_cycles, C.byref(r))
+        return c, r.value
+
+    def events(self):
+        """Every Print_Pre_Cycle / Print_Post_Cycle call so far as
+        (level, post, cycle, norm) tuples."""
+        n = self.L.orc_events(self._s, 0, 0, None)
+        buf = (OrcEvent * max(n, 1))()
+        self.L.orc_events(self._s, 0, n, buf)
+        return [(e.level, e.post, e.cycle, e.norm) for e in buf[:n]]
 
     def adm(self):
         out = (C.c_double * MAX_BH)()
