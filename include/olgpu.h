@@ -67,6 +67,15 @@ typedef enum {
  * default without -B).  olgpu_problem_defaults picks Robin. */
 typedef enum { OLGPU_BC_ROBIN = 0, OLGPU_BC_DIRICHLET = 1 } olgpu_boundary;
 
+/* The cycle olgpu_solve runs (-m, elliptic::Set_Method, src/elliptic.cc:229-294):
+ * V-cycles (elliptic::Vcycle, 1251-1342), or W-cycles (elliptic::Wcycle,
+ * 1348-1380), where FASN repeats every level, each time through its own
+ * coarser levels, until that level's post-smoothing norm is <= tol
+ * (src/elliptic.cc:1956).  A W-cycle runs in FP64, from olgpu_solve only;
+ * the mixed-precision cycle, olgpu_cycle_launch, olgpu_solve_many and the
+ * server take V-cycles. */
+typedef enum { OLGPU_METHOD_VCYCLE = 0, OLGPU_METHOD_WCYCLE = 1 } olgpu_method;
+
 /* The Olliptic.x parameters of the puncture problem (src/interface.cc:73-273,
  * 748-856); -L is the full domain length and dx = L/(N-1). */
 typedef struct {
@@ -85,6 +94,7 @@ typedef struct {
   int ps_case;                  /* -psc                                 */
   double ps_phi0, ps_r0, ps_sigma, ps_a2;   /* -phi0 -r0 -sigma -a2     */
   int boundary;                 /* -B: olgpu_boundary                   */
+  int method;                   /* -m: olgpu_method                     */
 } olgpu_problem;
 
 typedef struct {
@@ -111,7 +121,7 @@ typedef struct {
 } olgpu_stop_rule;
 
 typedef struct {
-  int cycles;                   /* V-cycles run                           */
+  int cycles;                   /* top-level cycles run                   */
   int status;                   /* olgpu_status of the solve              */
   double final_res;             /* top-level residual norm of the last cycle */
   double adm[OLGPU_MAX_BH];     /* ADM masses after the last cycle        */
@@ -154,7 +164,12 @@ olgpu_status olgpu_download(olgpu_hierarchy *h, int box, const char *field, doub
 
 /* One FAS V-cycle from the finest level; *res receives the top-level norm. */
 olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res);
-/* Repeated V-cycles under a stop rule; rule NULL = the reference's rule. */
+/* Repeated cycles of the problem's method under a stop rule; rule NULL =
+ * the reference's rule.  For W-cycles the rule stops the top-level calls
+ * (normally one: its own loop meets tol) and max_cycles also caps the
+ * iterations of each level's loop in one call (the reference has no cap);
+ * a level that reaches the cap without meeting tol ends the solve with
+ * OLGPU_ERR_DIVERGED. */
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out);
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
 
@@ -167,6 +182,24 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
  * holds the coarsest solve's norm.  In mixed precision they are the norms
  * of the FP32 correction cycle. */
 olgpu_status olgpu_level_norms(const olgpu_hierarchy *h, int cycle, double *pre, double *post);
+
+/* Every elliptic::Print_Pre_Cycle (post = 0) and Print_Post_Cycle (post = 1)
+ * call of the current solve, in the reference's order: the level (0: the
+ * coarsest solve, logged as a pre call), the cycle number it prints (the
+ * per-level count of FASN, src/elliptic.cc:1499, 1935) and the norm.  Loo.gp
+ * holds the pre calls' (cycle, norm); stdout0.out's tables all of them.  A
+ * V-cycle logs levels-1 .. 1 pre, 0, 1 .. levels-1 post, all with the cycle's
+ * number; a W-cycle logs each level iteration as it runs.  Copies calls
+ * [first, first + cap) into out (NULL when cap is 0) and writes how many the
+ * solve has logged into *total. */
+typedef struct {
+  int level;
+  int post;
+  long long cycle;
+  double norm;
+} olgpu_cycle_event;
+olgpu_status olgpu_cycle_events(const olgpu_hierarchy *h, long long first, int cap, olgpu_cycle_event *out,
+                                long long *total);
 
 /* u at arbitrary points, as the reference prints and exports it
  * (multigrid::Print_Interpol_1D / _2D, src/multigrid.cc:151-261 and 555-880;

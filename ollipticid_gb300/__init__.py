@@ -31,6 +31,9 @@ EQUATIONS = {"Punctures": 0, "Punctures_scalar_field": 1, "Poisson": 2, "Boundar
 # the outer boundary conditions (-B): Robin, and Dirichlet, the reference's
 # default when -B is not given
 BOUNDARIES = {"Robin": 0, "Dirichlet": 1}
+# the cycles of -m (elliptic::Set_Method): V-cycles, and W-cycles, where every
+# level repeats until its own norm meets the tolerance
+METHODS = {"Vcycle": 0, "Wcycle": 1}
 
 
 @dataclass
@@ -60,6 +63,7 @@ class Problem:
     ps_sigma: float = 8.0
     ps_a2: float = 1.0
     boundary: str = "Robin"              # or "Dirichlet" (the reference's default without -B)
+    method: str = "Vcycle"               # or "Wcycle"
 
     @property
     def numbh(self) -> int:
@@ -81,6 +85,7 @@ class Problem:
         for name in ("L", "tol", "ps_phi0", "ps_r0", "ps_sigma", "ps_a2"):
             setattr(p, name, float(getattr(self, name)))
         p.boundary = BOUNDARIES[self.boundary]
+        p.method = METHODS[self.method]
         return p
 
     def oracle_dict(self) -> dict:
@@ -112,8 +117,12 @@ def parse_olliptic_args(argv: Sequence[str]) -> Problem:
     bc = get(["-B", "--boundary"], str, "Dirichlet")   # interface.cc:272
     if bc not in BOUNDARIES:
         raise ValueError(f"boundary {bc!r} is not on the GPU path")
+    me = get(["-m", "--method"], str, "Vcycle")        # interface.cc:259
+    if me not in METHODS and me != "AppPuncture":
+        raise ValueError(f"method {me!r} is not on the GPU path")
     nb = get(["-NumBH", "--num-bh"], int, 1)
-    P = Problem(equation=eq, boundary=bc)
+    # AppPuncture's hierarchy is the V-cycle's; Elliptic.ApproximateID runs it
+    P = Problem(equation=eq, boundary=bc, method="Wcycle" if me == "Wcycle" else "Vcycle")
     for name, flag in (("mp", "-bhmp"), ("x", "-bhx"), ("y", "-bhy"), ("z", "-bhz"), ("px", "-bhpx"),
                        ("py", "-bhpy"), ("pz", "-bhpz"), ("sx", "-bhsx"), ("sy", "-bhsy"), ("sz", "-bhsz")):
         setattr(P, name, [get([f"{flag}{i + 1}"], float, 0.0) for i in range(nb)])
@@ -217,7 +226,8 @@ class Elliptic:
         return r.value
 
     def Solve(self, stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000, tol: float = 0.0) -> "_abi.Report":
-        """elliptic::Solve -> Vcycle with the reference stop rule by default."""
+        """elliptic::Solve -> Vcycle or Wcycle (the problem's method) with the
+        reference stop rule by default."""
         rule = _abi.StopRule(stop, max_cycles, tol)
         rep = _abi.Report()
         st = self.lib.olgpu_solve(self._h, C.byref(rule), C.byref(rep))
@@ -274,6 +284,17 @@ class Elliptic:
         check(self.lib.olgpu_level_norms(self._h, int(cycle), pre.ctypes.data_as(C.POINTER(C.c_double)),
                                          post.ctypes.data_as(C.POINTER(C.c_double))))
         return pre, post
+
+    def cycle_events(self):
+        """Every Print_Pre_Cycle / Print_Post_Cycle call of the last solve as
+        (level, post, cycle, norm) tuples, in the reference's order (level 0:
+        the coarsest solve; Loo.gp holds the (cycle, norm) of the post = 0
+        calls)."""
+        total = C.c_longlong()
+        check(self.lib.olgpu_cycle_events(self._h, 0, 0, None, C.byref(total)))
+        buf = (_abi.CycleEvent * max(total.value, 1))()
+        check(self.lib.olgpu_cycle_events(self._h, 0, total.value, buf, C.byref(total)))
+        return [(e.level, e.post, e.cycle, e.norm) for e in buf[:total.value]]
 
     def interpolate(self, points, ord: Optional[int] = None, box: int = -1, first_level: int = 0) -> np.ndarray:
         """u at (npts, 3) points, as the reference prints it (Print_Interpol_1D

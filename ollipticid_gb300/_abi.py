@@ -22,7 +22,7 @@ class Problem(C.Structure):
         ("n", C.c_int), ("L", C.c_double), ("order", C.c_int), ("levels", C.c_int),
         ("nu1", C.c_int), ("nu2", C.c_int), ("tol", C.c_double),
         ("ps_case", C.c_int), ("ps_phi0", C.c_double), ("ps_r0", C.c_double),
-        ("ps_sigma", C.c_double), ("ps_a2", C.c_double), ("boundary", C.c_int),
+        ("ps_sigma", C.c_double), ("ps_a2", C.c_double), ("boundary", C.c_int), ("method", C.c_int),
     ]
 
 
@@ -35,6 +35,10 @@ class BoxInfo(C.Structure):
         ("cx", C.c_double), ("cy", C.c_double), ("cz", C.c_double),
         ("xf", C.c_double), ("yf", C.c_double), ("zf", C.c_double),
     ]
+
+
+class CycleEvent(C.Structure):
+    _fields_ = [("level", C.c_int), ("post", C.c_int), ("cycle", C.c_longlong), ("norm", C.c_double)]
 
 
 class StopRule(C.Structure):
@@ -93,6 +97,8 @@ SIGNATURES = {
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_approximate_id": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_level_norms": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "olgpu_cycle_events": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(CycleEvent),
+                                     C.POINTER(C.c_longlong)]),
     "olgpu_interpolate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
     "olgpu_cycle_launch": (C.c_int, [C.c_void_p]),
     "olgpu_cycle_poll": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),

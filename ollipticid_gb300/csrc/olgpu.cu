@@ -121,6 +121,14 @@ struct olgpu_hierarchy {
   // pre-smoothing norms then levels post-smoothing norms (level 0: the
   // coarsest solve's)
   std::vector<double> norm_hist;
+  // every Print_Pre_Cycle / Print_Post_Cycle call of the current solve
+  std::vector<olgpu_cycle_event> events;
+  // W-cycle: per level k >= 1 FASN's descent (smoothing down to the saved
+  // coarse u) and ascent (correction and smoothing), and the coarsest solve,
+  // each captured alone so that the host can repeat every level (built on
+  // the first W-cycle solve)
+  std::vector<cudaGraphExec_t> graph_down, graph_up;
+  cudaGraphExec_t graph_coarse = nullptr;
   // Anderson acceleration of the mixed outer iteration
   int anderson_m = kAndDefault;
   float *d_and = nullptr;               // DU[m], DF[m], fprev (FP32, total_pts each)
@@ -666,8 +674,11 @@ void choose_coarse_cluster(olgpu_hierarchy *h)
   }
 }
 
+// FASN's descent on level k (src/elliptic.cc:1518-1775): boundary and
+// pre-smoothing, u restricted, the coarse level's source with tau, the
+// coarse u saved in ww
 template <int EQ>
-void emit_fasn(olgpu_hierarchy *h, int k, int top)
+void emit_fasn_down(olgpu_hierarchy *h, int k)
 {
   const int mg = h->G.mgrid_levels;
   if (k <= mg) dispatch_robin(h, k, 0);
@@ -710,21 +721,32 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
     launch_transfer(h, h->set_in[k]);
   }
   launch_ew(h, k - 1, EW_WW_EQ_U);
-  if (k == 1) {
-    const DevBox &B = h->hboxes[h->G.first_box[0]];
-    const size_t smem = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
-    if (h->coarse_ncta > 0)
-      launch_coarse_cluster<EQ>(h);
-    else
-      k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
-                                                       h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
-                                                       h->coarse_rtol, &h->d_stats->coarse_norm,
-                                                       &h->d_stats->coarse_iters, &h->d_stats->nan_flag,
-                                                       h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
-    h->launches++;
-  } else {
-    emit_fasn<EQ>(h, k - 1, top);
-  }
+}
+
+// the coarsest solve (src/elliptic.cc:1782-1816)
+template <int EQ>
+void emit_coarse(olgpu_hierarchy *h)
+{
+  const DevBox &B = h->hboxes[h->G.first_box[0]];
+  const size_t smem = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
+  if (h->coarse_ncta > 0)
+    launch_coarse_cluster<EQ>(h);
+  else
+    k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
+                                                     h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
+                                                     h->coarse_rtol, &h->d_stats->coarse_norm,
+                                                     &h->d_stats->coarse_iters, &h->d_stats->nan_flag,
+                                                     h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
+  h->launches++;
+}
+
+// FASN's ascent on level k (src/elliptic.cc:1827-1941): the coarse
+// correction prolonged and added, ghosts refilled, boundary and
+// post-smoothing, the ADM integrand on the top level
+template <int EQ>
+void emit_fasn_up(olgpu_hierarchy *h, int k, int top)
+{
+  const int mg = h->G.mgrid_levels;
   if (h->fast_paths) {   // u_fine += P(u - ww) in one pass
     const Transfer &X = h->prolong_v[k];
     if (!X.jobs.empty()) {
@@ -745,6 +767,16 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
     k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
     h->launches++;
   }
+}
+
+// elliptic::FASN with Wcycle = false (src/elliptic.cc:1468-1968)
+template <int EQ>
+void emit_fasn(olgpu_hierarchy *h, int k, int top)
+{
+  emit_fasn_down<EQ>(h, k);
+  if (k == 1) emit_coarse<EQ>(h);
+  else emit_fasn<EQ>(h, k - 1, top);
+  emit_fasn_up<EQ>(h, k, top);
 }
 
 // ---------------------------------------------------------------------------
@@ -1223,6 +1255,57 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   return OLGPU_OK;
 }
 
+// Captures what emit() enqueues on the hierarchy's stream as one graph.
+template <class Emit>
+olgpu_status capture_piece(olgpu_hierarchy *h, Emit emit, cudaGraphExec_t *out, const char *what)
+{
+  cudaGraph_t g;
+  CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  emit();
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string(what) + " capture: " + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string(what) + " instantiate: " + cudaGetErrorString(e));
+  return OLGPU_OK;
+}
+
+template <int EQ>
+olgpu_status build_wgraphs_eq(olgpu_hierarchy *h)
+{
+  const int top = h->G.levels - 1;
+  const int saved = h->launches;   // the V-cycle's kernel count stays the reported one
+  for (auto *vec : {&h->graph_down, &h->graph_up})   // pieces of an earlier attempt that failed
+    for (cudaGraphExec_t g : *vec)
+      if (g) cudaGraphExecDestroy(g);
+  h->graph_down.assign(top + 1, nullptr);
+  h->graph_up.assign(top + 1, nullptr);
+  olgpu_status st = OLGPU_OK;
+  for (int k = 1; k <= top && st == OLGPU_OK; k++) {
+    unsigned long long *pre = &h->d_stats->slots[2 * k], *post = &h->d_stats->slots[2 * k + 1];
+    st = capture_piece(h, [&] {
+      cudaMemsetAsync(pre, 0, sizeof(*pre), h->stream);   // the smoother max-reduces into its slot
+      emit_fasn_down<EQ>(h, k);
+    }, &h->graph_down[k], "W-cycle descent");
+    if (st != OLGPU_OK) break;
+    st = capture_piece(h, [&] {
+      cudaMemsetAsync(post, 0, sizeof(*post), h->stream);
+      emit_fasn_up<EQ>(h, k, top);
+    }, &h->graph_up[k], "W-cycle ascent");
+  }
+  if (st == OLGPU_OK) st = capture_piece(h, [&] { emit_coarse<EQ>(h); }, &h->graph_coarse, "W-cycle coarse solve");
+  h->launches = saved;
+  return st;
+}
+
+olgpu_status build_wgraphs(olgpu_hierarchy *h)
+{
+  if (h->graph_coarse) return OLGPU_OK;
+  if (h->equation == 1) return build_wgraphs_eq<1>(h);
+  if (h->equation >= 2) return build_wgraphs_eq<2>(h);
+  return build_wgraphs_eq<0>(h);
+}
+
 int field_id(const char *name)
 {
   static const char *names[F_NUM] = {"u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v", "t"};
@@ -1383,6 +1466,8 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     return fail(OLGPU_ERR_INVALID_ARG, "the multibox test takes its two centres from bhx1 and bhx2");
   if (p->boundary != OLGPU_BC_ROBIN && p->boundary != OLGPU_BC_DIRICHLET)
     return fail(OLGPU_ERR_INVALID_ARG, "boundary must be Robin or Dirichlet");
+  if (p->method != OLGPU_METHOD_VCYCLE && p->method != OLGPU_METHOD_WCYCLE)
+    return fail(OLGPU_ERR_INVALID_ARG, "method must be Vcycle or Wcycle");
   if (p->equation == 1 && !(p->ps_case >= 1 && p->ps_case <= 4))
     return fail(OLGPU_ERR_INVALID_ARG, "ps_case must be 1..4");
   int ndev = 0;
@@ -1567,6 +1652,10 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->graph_mixed) cudaGraphExecDestroy(h->graph_mixed);
+  for (auto *vec : {&h->graph_down, &h->graph_up})
+    for (cudaGraphExec_t g : *vec)
+      if (g) cudaGraphExecDestroy(g);
+  if (h->graph_coarse) cudaGraphExecDestroy(h->graph_coarse);
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   cudaFree(h->d_arena32);
@@ -1662,6 +1751,8 @@ static olgpu_status cycle_enqueue(olgpu_hierarchy *h)
   return OLGPU_OK;
 }
 
+static olgpu_status finish_adm(olgpu_hierarchy *h);
+
 // Reads a finished cycle's norms: the cycle's norm, the ADM masses, NaN.
 static olgpu_status cycle_finish(olgpu_hierarchy *h, double *res)
 {
@@ -1675,12 +1766,25 @@ static olgpu_status cycle_finish(olgpu_hierarchy *h, double *res)
     h->last_correction = corr;
     if (corr > *res) *res = corr;
   }
+  const long long c = (long long)(h->norm_hist.size() / (2 * (top + 1)));
   for (int post = 0; post < 2; post++)
     for (int l = 0; l <= top; l++) {
       double v = h->h_stats->coarse_norm;
       if (l > 0) std::memcpy(&v, &h->h_stats->slots[2 * l + post], sizeof(double));
       h->norm_hist.push_back(v);
     }
+  // the cycle's print calls: pre-smoothing from the top down, the coarsest
+  // solve, post-smoothing back up
+  const double *pre = &h->norm_hist[h->norm_hist.size() - 2 * (top + 1)], *post = pre + top + 1;
+  for (int l = top; l >= 0; l--) h->events.push_back(olgpu_cycle_event{l, 0, c, pre[l]});
+  for (int l = 1; l <= top; l++) h->events.push_back(olgpu_cycle_event{l, 1, c, post[l]});
+  return finish_adm(h);
+}
+
+// The ADM masses from the last cycle's integrals (elliptic::Compute_ADM_Mass,
+// src/elliptic.cc:2447-2611) and the NaN check.
+static olgpu_status finish_adm(olgpu_hierarchy *h)
+{
   const olgpu_problem &P = h->P;
   for (int i = 0; i < P.numbh; i++) {
     double bhmj = 0;
@@ -1747,6 +1851,7 @@ static olgpu_status make_track(olgpu_hierarchy *h, const olgpu_stop_rule *rule, 
   if (T.R.max_cycles <= 0) return fail(OLGPU_ERR_INVALID_ARG, "max_cycles must be > 0");
   T.tol = T.R.tol > 0 ? T.R.tol : h->eps_solv;
   h->norm_hist.clear();
+  h->events.clear();
   return OLGPU_OK;
 }
 
@@ -1759,6 +1864,73 @@ static void close_track(olgpu_hierarchy *h, SolveTrack &T, olgpu_report *out)
   if (out) *out = T.rep;
 }
 
+// elliptic::FASN with Wcycle = true (src/elliptic.cc:1468-1968): level k
+// repeats its descent, the coarser levels' own loop (the coarsest solve
+// below level 1) and its ascent while its post-smoothing norm is above tol,
+// at most `cap` times.  One host sync per iteration reads the level's norms
+// (and the coarsest solve's): the loop's test needs them.
+static olgpu_status wcycle_level(olgpu_hierarchy *h, int k, long long icycle, double tol, int cap, double *norm_k)
+{
+  long long cycle = icycle;
+  int iters = 0;
+  do {
+    const size_t pre = h->events.size();
+    h->events.push_back(olgpu_cycle_event{k, 0, cycle, 0.0});   // its norm is read after the sync below
+    CUDA_TRY(cudaGraphLaunch(h->graph_down[k], h->stream));
+    if (k == 1) {
+      h->events.push_back(olgpu_cycle_event{0, 0, cycle, 0.0});
+      CUDA_TRY(cudaGraphLaunch(h->graph_coarse, h->stream));
+    } else {
+      double inner = 0;
+      olgpu_status st = wcycle_level(h, k - 1, cycle, tol, cap, &inner);
+      if (st != OLGPU_OK) return st;
+    }
+    CUDA_TRY(cudaGraphLaunch(h->graph_up[k], h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->h_stats, h->d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    std::memcpy(&h->events[pre].norm, &h->h_stats->slots[2 * k], sizeof(double));
+    if (k == 1) h->events[pre + 1].norm = h->h_stats->coarse_norm;
+    std::memcpy(norm_k, &h->h_stats->slots[2 * k + 1], sizeof(double));
+    h->events.push_back(olgpu_cycle_event{k, 1, cycle, *norm_k});
+    if (h->h_stats->nan_flag) return fail(OLGPU_ERR_NAN, "NaN in the smoother");
+    cycle++;
+    iters++;
+  } while (*norm_k > tol && iters < cap);
+  if (*norm_k > tol)
+    return fail(OLGPU_ERR_DIVERGED, "W-cycle: level " + std::to_string(k) + " did not reach the tolerance in " +
+                                        std::to_string(cap) + " iterations");
+  return OLGPU_OK;
+}
+
+// elliptic::Wcycle (src/elliptic.cc:1348-1380) under the stop rule: each
+// top-level call runs the top level's own loop.
+static void solve_wcycle(olgpu_hierarchy *h, SolveTrack &T)
+{
+  const int top = h->G.levels - 1;
+  olgpu_status st = build_wgraphs(h);
+  if (st == OLGPU_OK && cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream) != cudaSuccess)
+    st = fail(OLGPU_ERR_CUDA, "W-cycle: clearing the norms");
+  if (st != OLGPU_OK) {
+    T.step(st, 0.0);
+    return;
+  }
+  for (;;) {
+    double r = 0;
+    olgpu_status s = wcycle_level(h, top, T.cycles, T.tol, T.R.max_cycles, &r);
+    if (s == OLGPU_OK || s == OLGPU_ERR_DIVERGED) {
+      for (int post = 0; post < 2; post++)   // the latest norms of every level, as a V-cycle's
+        for (int l = 0; l <= top; l++) {
+          double v = h->h_stats->coarse_norm;
+          if (l > 0) std::memcpy(&v, &h->h_stats->slots[2 * l + post], sizeof(double));
+          h->norm_hist.push_back(v);
+        }
+      const olgpu_status a = finish_adm(h);
+      if (s == OLGPU_OK) s = a;
+    }
+    if (T.step(s, r)) break;
+  }
+}
+
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out)
 {
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
@@ -1767,10 +1939,14 @@ olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_
   if (st != OLGPU_OK) return st;
   CUDA_TRY(cudaSetDevice(h->device));
   CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
-  for (;;) {
-    double r = 0;
-    olgpu_status s = run_cycle(h, &r);
-    if (T.step(s, r)) break;
+  if (h->P.method == OLGPU_METHOD_WCYCLE) {
+    solve_wcycle(h, T);
+  } else {
+    for (;;) {
+      double r = 0;
+      olgpu_status s = run_cycle(h, &r);
+      if (T.step(s, r)) break;
+    }
   }
   cudaEventRecord(h->ev1, h->stream);
   cudaEventSynchronize(h->ev1);
@@ -1782,6 +1958,7 @@ olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_
 olgpu_status olgpu_cycle_launch(olgpu_hierarchy *h)
 {
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (h->P.method != OLGPU_METHOD_VCYCLE) return fail(OLGPU_ERR_INVALID_ARG, "W-cycles run from olgpu_solve only");
   CUDA_TRY(cudaSetDevice(h->device));
   return cycle_enqueue(h);
 }
@@ -1808,6 +1985,7 @@ olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule
   std::vector<SolveTrack> T(n);
   for (int i = 0; i < n; i++) {
     if (!hs[i]) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy in the set");
+    if (hs[i]->P.method != OLGPU_METHOD_VCYCLE) return fail(OLGPU_ERR_INVALID_ARG, "W-cycles run from olgpu_solve only");
     olgpu_status st = make_track(hs[i], rule, T[i]);
     if (st != OLGPU_OK) return st;
   }
@@ -1941,6 +2119,16 @@ olgpu_status olgpu_approximate_id(olgpu_hierarchy *h, int as_guess)
   return OLGPU_OK;
 }
 
+olgpu_status olgpu_cycle_events(const olgpu_hierarchy *h, long long first, int cap, olgpu_cycle_event *out,
+                                long long *total)
+{
+  if (!h || first < 0 || cap < 0 || (cap > 0 && !out)) return fail(OLGPU_ERR_INVALID_ARG, "bad argument");
+  const long long n = (long long)h->events.size();
+  for (long long i = 0; i < cap && first + i < n; i++) out[i] = h->events[first + i];
+  if (total) *total = n;
+  return OLGPU_OK;
+}
+
 olgpu_status olgpu_level_norms(const olgpu_hierarchy *h, int cycle, double *pre, double *post)
 {
   if (!h || !pre || !post) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
@@ -2000,6 +2188,8 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)
       return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the puncture equations");
     if (h->P.boundary != OLGPU_BC_ROBIN)
       return fail(OLGPU_ERR_INVALID_ARG, "mixed precision is built for the Robin boundary");
+    if (h->P.method != OLGPU_METHOD_VCYCLE)
+      return fail(OLGPU_ERR_INVALID_ARG, "the W-cycle runs in FP64");
     olgpu_status st = build_mixed(h);
     if (st != OLGPU_OK) return st;
   }

@@ -11,8 +11,10 @@
 // Poisson (the Gaussian test), Boundary-test and Multibox-test are refused, and so are boundary conditions other than Robin and
 // Dirichlet (the reference's default).
 //
-// Methods (-m): Vcycle (the default) and AppPuncture (the analytic
-// approximation alone, elliptic::ApproximateID); the others are refused.
+// Methods (-m): Vcycle (the default), Wcycle (every level repeated until its
+// own norm meets the tolerance, elliptic::Wcycle; FP64) and AppPuncture (the
+// analytic approximation alone, elliptic::ApproximateID); the others are
+// refused.
 //
 // Extra flags of this program (no reference counterpart):
 //   -gpu-mixed yes|no   mixed-precision cycles (FP32 correction around FP64)
@@ -21,15 +23,15 @@
 //   -gpu-device N       CUDA device (default: the current one)
 //   -plan yes           print the box hierarchy (no GPU needed) and exit
 //
-// Output: the hierarchy, one line per V-cycle with its norm, and the ADM
+// Output: the hierarchy, one line per top-level cycle with its norm, and the ADM
 // masses in the reference's "ADM mass[i] = ..." form (src/elliptic.cc:2466-
 // 2469) on stdout; in the output directory (-o, default Output) the files of
 // elliptic::Print_Solution (src/output.cc:624-700) for the puncture path:
 // the per-box cuts u-l<l>b<i>-0.{x,y,z} (-p1d, ffunction::Print_1D,
 // src/ffunction.cc:819-960) and the interpolated cuts u.X, u.Y, u.Z and the
 // plane u.XY (-pint, multigrid::Print_Interpol_1D / _2D, src/multigrid.cc:
-// 151-880), with the reference's number formats, each cycle's
-// pre-smoothing norms per level as Loo.gp (-so yes, elliptic::Print_Pre_Cycle,
+// 151-880), with the reference's number formats, the cycle number and norm
+// of every pre-smoothing step as Loo.gp (-so yes, elliptic::Print_Pre_Cycle,
 // src/output.cc:1355-1460), the banner and the per-cycle norms as
 // stdout0.out (Print_Info, Print_Pre_Cycle / Print_Post_Cycle) and the
 // command line as <dir>.run.  The directory is rotated like the reference's
@@ -182,30 +184,32 @@ void write_banner(FILE *f, const olgpu_problem &p, const char *equation_str, con
   std::fprintf(f, "--------------------------------------------------------------------\n  Init Multigrid iteration\n");
 }
 
-// One V-cycle's lines of <dir>stdout0.out (elliptic::Print_Pre_Cycle /
-// Print_Post_Cycle, src/output.cc:1355-1605): the cycle header, the
-// pre-smoothing norms from the finest level down, the coarsest solve's, the
-// post-smoothing norms back up, and the cycle's norm against the tolerance.
-void write_cycle(FILE *f, int c, int nl, const std::vector<double> &pre, const std::vector<double> &post,
-                 double eps_solv)
+// The cycle tables of <dir>stdout0.out (elliptic::Print_Pre_Cycle /
+// Print_Post_Cycle, src/output.cc:1355-1605), one indented "|Loo[k] : norm"
+// line per call of the solve: a cycle header and a rule before the top
+// level's pre-smoothing line, a rule and the norm against the tolerance
+// after its post-smoothing line.
+void write_cycle_tables(FILE *f, const std::vector<olgpu_cycle_event> &ev, int nl, double eps_solv)
 {
   const int top = nl - 1;
-  auto line = [&](int k, double v) {
-    for (int j = 0; j < k; j++) std::fprintf(f, "|\t\t\t");
-    std::fprintf(f, "|Loo[%d] : %.8e", k, v);
-    for (int j = k + 1; j <= top + 1; j++) std::fprintf(f, "|\t\t\t");
-    std::fprintf(f, "\n");
-  };
   auto rule = [&]() {
     for (int j = 0; j <= top; j++) std::fprintf(f, "========================");
     std::fprintf(f, "\n");
   };
-  std::fprintf(f, "\n\nCycle: %d\n", c);
-  rule();
-  for (int k = top; k >= 0; k--) line(k, pre[k]);
-  for (int k = 1; k <= top; k++) line(k, post[k]);
-  rule();
-  std::fprintf(f, "%.8e  -->  %.8e\n", post[top], eps_solv);
+  for (const olgpu_cycle_event &e : ev) {
+    if (!e.post && e.level == top) {
+      std::fprintf(f, "\n\nCycle: %lld\n", e.cycle);
+      rule();
+    }
+    for (int j = 0; j < e.level; j++) std::fprintf(f, "|\t\t\t");
+    std::fprintf(f, "|Loo[%d] : %.8e", e.level, e.norm);
+    for (int j = e.level + 1; j <= top + 1; j++) std::fprintf(f, "|\t\t\t");
+    std::fprintf(f, "\n");
+    if (e.post && e.level == top) {
+      rule();
+      std::fprintf(f, "%.8e  -->  %.8e\n", e.norm, eps_solv);
+    }
+  }
 }
 
 // ffunction::Print_1D of one box and one axis: at every node along `axis`
@@ -612,12 +616,13 @@ int main(int argc, char **argv)
     std::fprintf(stderr, "Olliptic_gpu.x: equation %s is not on the puncture FAS path\n", equation.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
   }
-  // elliptic::Set_Method (src/elliptic.cc:229-294): V-cycles, or the
-  // analytic approximation alone (AppPuncture, elliptic::ApproximateID)
+  // elliptic::Set_Method (src/elliptic.cc:229-294): V-cycles, W-cycles, or
+  // the analytic approximation alone (AppPuncture, elliptic::ApproximateID)
   const char *me = A.find({"-m", "--method"});
   const std::string method = me ? me : "Vcycle";
   const bool approx_only = method == "AppPuncture";
-  if (method != "Vcycle" && !approx_only) {
+  if (method == "Wcycle") p.method = OLGPU_METHOD_WCYCLE;
+  else if (method != "Vcycle" && !approx_only) {
     std::fprintf(stderr, "Olliptic_gpu.x: method %s is not on the puncture FAS path\n", method.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
   }
@@ -706,7 +711,10 @@ int main(int argc, char **argv)
                            : p.equation == OLGPU_EQ_BOUNDARY_TEST  ? "Robin boundary test"
                            : p.equation == OLGPU_EQ_MULTIBOX_TEST  ? "Multibox test"
                                                                    : "";   // the scalar field has no name there
-      write_banner(f, p, eq_str, approx_only ? "Analitical Approximate" : "Multigrid V-Cycles",
+      write_banner(f, p, eq_str,
+                   approx_only                          ? "Analitical Approximate"
+                   : p.method == OLGPU_METHOD_WCYCLE    ? "Multigrid W-Cycle"
+                                                        : "Multigrid V-Cycles",
                    p.boundary == OLGPU_BC_ROBIN ? "Robin" : "Dirichlet", dir, boxes, nb, nl, mg, approx_only);
     }
     if (f) std::fclose(f);
@@ -757,32 +765,36 @@ int main(int argc, char **argv)
   olgpu_report rep{};
   if (!approx_only) {
     st = olgpu_solve(h, nullptr, &rep);   // the reference stop rule
-    for (int c = 0; c < rep.cycles && c < 256; c++) std::printf("  V-cycle %3d  norm %.6e\n", c + 1, rep.res[c]);
+    const char *cyc = p.method == OLGPU_METHOD_WCYCLE ? "W-cycle" : "V-cycle";
+    for (int c = 0; c < rep.cycles && c < 256; c++) std::printf("  %s %3d  norm %.6e\n", cyc, c + 1, rep.res[c]);
     if (st != OLGPU_OK) {
       olgpu_hierarchy_destroy(h);
       return fail(st, "solve");
     }
-    std::printf("Solved in %d V-cycles, norm %.6e, %.3f ms on the device\n", rep.cycles, rep.final_res,
+    std::printf("Solved in %d %ss, norm %.6e, %.3f ms on the device\n", rep.cycles, cyc, rep.final_res,
                 olgpu_last_device_ms(h));
   }
-  if (std_output && !approx_only) {   // stdout0.out: each cycle's norms
-    FILE *f = std::fopen((dir + "stdout0.out").c_str(), "a");
-    std::vector<double> pre(nl), post(nl);
-    const double eps_coarse = 2 * 2.220446049250313080847e-16;
-    for (int c = 0; f && c < rep.cycles; c++) {
-      if (olgpu_level_norms(h, c, pre.data(), post.data()) != OLGPU_OK) break;
-      write_cycle(f, c, nl, pre, post, p.tol < eps_coarse ? eps_coarse : p.tol);
+  // every Print_Pre_Cycle / Print_Post_Cycle call of the solve
+  std::vector<olgpu_cycle_event> events;
+  if (std_output && !approx_only) {
+    long long total = 0;
+    if (olgpu_cycle_events(h, 0, 0, nullptr, &total) == OLGPU_OK && total > 0) {
+      events.resize((size_t)total);
+      if (olgpu_cycle_events(h, 0, (int)total, events.data(), &total) != OLGPU_OK) events.clear();
     }
+  }
+  if (std_output && !approx_only) {   // stdout0.out: the cycle tables
+    FILE *f = std::fopen((dir + "stdout0.out").c_str(), "a");
+    const double eps_coarse = 2 * 2.220446049250313080847e-16;
+    if (f) write_cycle_tables(f, events, nl, p.tol < eps_coarse ? eps_coarse : p.tol);
     if (f) std::fclose(f);
   }
-  // Loo.gp: each cycle's pre-smoothing norms, finest level first (Print_Pre_Cycle)
+  // Loo.gp: the cycle number and norm of every pre-smoothing step and
+  // coarsest solve (Print_Pre_Cycle)
   if (std_output && !approx_only) {
     FILE *f = std::fopen((dir + "Loo.gp").c_str(), "a");
-    std::vector<double> pre(nl), post(nl);
-    for (int c = 0; f && c < rep.cycles; c++) {
-      if (olgpu_level_norms(h, c, pre.data(), post.data()) != OLGPU_OK) break;
-      for (int k = nl - 1; k >= 0; k--) std::fprintf(f, "%d\t%.18e\n", c, pre[k]);
-    }
+    for (const olgpu_cycle_event &e : events)
+      if (f && !e.post) std::fprintf(f, "%lld\t%.18e\n", e.cycle, e.norm);
     if (f) std::fclose(f);
   }
   if (!approx_only && p.equation < OLGPU_EQ_POISSON) {   // Vcycle prints ADM for punctures only

@@ -286,6 +286,7 @@ olgpu_status olgpu_server_create(const olgpu_server_config *c, olgpu_server **ou
 olgpu_status olgpu_server_submit(olgpu_server *s, const olgpu_problem *p, long long *id)
 {
   if (!s || !p || !id) return OLGPU_ERR_INVALID_ARG;
+  if (p->method != OLGPU_METHOD_VCYCLE) return OLGPU_ERR_INVALID_ARG;   // the scheduler steps V-cycles
   static const int kMaxBoxes = 1024;
   std::vector<olgpu_box_info> boxes(kMaxBoxes);
   int nb = 0;

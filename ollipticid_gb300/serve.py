@@ -121,6 +121,10 @@ class Server:
             while pending and pending[0][1][0] <= t:
                 rid, (arr, prob) = pending.popleft()
                 results[rid] = Result(rid, arr)
+                if prob.method != "Vcycle":           # the scheduler steps V-cycles
+                    results[rid].status = _abi.ERR_INVALID_ARG
+                    results[rid].finished = now()
+                    continue
                 nbytes = footprint(prob, self.mixed)
                 if nbytes > self.mem_budget:          # can never fit: refuse now
                     results[rid].status = _abi.ERR_OOM

@@ -24,6 +24,7 @@ BANNER_CASES = {
     "gaussian_dirichlet": "-eq Poisson -L 10 -N 25 -O 6 -l 2 -s 1e-10",
     "boundary_test_tol": "-eq Boundary-test -B Robin -L 10 -N 25 -O 8 -l 2 -s 1e-20 -nu1 2",
     "approx": BIN + " -m AppPuncture",
+    "wcycle": BIN + " -m Wcycle",
 }
 END = "  Init Multigrid iteration\n"
 

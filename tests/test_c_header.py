@@ -1,7 +1,8 @@
 """include/olgpu.h is a C header (the drop-in boundary is a C ABI): a C11
 program that includes it builds with warnings as errors, links against
 libolgpu.so and calls the entry points that need no GPU (version, defaults,
-the host-only box plan, the server's configuration check)."""
+the host-only box plan, the server's configuration check, the argument check
+of the cycle-event accessor)."""
 import os
 import shutil
 import subprocess
@@ -28,6 +29,7 @@ int main(void)
   olgpu_problem_defaults(&p);
   p.equation = OLGPU_EQ_PUNCTURES;
   p.boundary = OLGPU_BC_ROBIN;
+  p.method = OLGPU_METHOD_VCYCLE;
   p.numbh = 1;
   p.mp[0] = 0.5;
   p.n = 25;
@@ -39,6 +41,7 @@ int main(void)
   olgpu_server_config_defaults(&cfg);
   cfg.max_active = 0;
   if (olgpu_server_create(&cfg, &s) != OLGPU_ERR_INVALID_ARG) return 2;
+  if (olgpu_cycle_events(NULL, 0, 0, NULL, NULL) != OLGPU_ERR_INVALID_ARG) return 4;
   p.order = 3;
   if (olgpu_plan_boxes(&p, boxes, 64, &nb, &nl, &mg) == OLGPU_OK) return 3;
   printf("refused: %s\n", olgpu_last_error());

@@ -50,3 +50,19 @@ def test_wcycle_and_vcycle_share_the_fixed_point(oracle_mod):
     for g_ in range(ow.nboxes):
         if ow.boxes[g_].level >= ow.mgrid_levels:
             assert np.max(np.abs(ow.field(g_, "u") - ov.field(g_, "u"))) < 1e-11
+
+
+def test_wcycle_call_checker_accepts_the_reference_and_rejects_a_v_cycle(oracle_mod):
+    """The call checker the GPU tests use, on the oracle's (reference-pinned)
+    W-cycle calls, and on a V-cycle's, which it must reject."""
+    from tests.wcycle_log import check_wcycle_calls
+    g = np.load(GOLDEN[0])
+    P = problem(g["args"].item().decode())
+    orc = oracle_mod.Oracle(P.oracle_dict())
+    orc.solve_wcycle()
+    iters = check_wcycle_calls(orc.events(), orc.levels, P.tol)
+    assert iters[-1] == g["stdout_cycles"].item().decode().count("Cycle:")
+    ov = oracle_mod.Oracle(P.oracle_dict())
+    ov.solve()
+    with pytest.raises(AssertionError):
+        check_wcycle_calls(ov.events(), ov.levels, P.tol)

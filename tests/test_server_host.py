@@ -1,7 +1,8 @@
 """The C++ server's host side without a GPU: its threads start and stop, a
 request that can never fit is refused at once with OLGPU_ERR_OOM, a request
-whose build fails reports the failure as its status (no fallback), and a
-result can be collected once."""
+whose build fails reports the failure as its status (no fallback), a
+W-cycle request (the scheduler steps V-cycles) is refused at submission, and
+a result can be collected once."""
 import ctypes as C
 
 import pytest
@@ -35,6 +36,10 @@ def test_server_refuses_and_reports_without_a_device():
         assert done.value == 1 and out.status not in (_abi.OK, _abi.ERR_OOM) and not out.h
         assert lib.olgpu_server_poll(s, ids[1], 0, C.byref(done), C.byref(out)) == _abi.OK and done.value == 0
         assert lib.olgpu_server_poll(s, 12345, 0, C.byref(done), C.byref(out)) == _abi.ERR_INVALID_ARG
+        w = problem("o4_spin")
+        w.method = "Wcycle"
+        wp, rid = w.to_c(), C.c_longlong()
+        assert lib.olgpu_server_submit(s, C.byref(wp), C.byref(rid)) == _abi.ERR_INVALID_ARG
         v = [C.c_int() for _ in range(4)]
         assert lib.olgpu_server_stats(s, *(C.byref(x) for x in v)) == _abi.OK
         assert [x.value for x in v[:3]] == [0, 0, 0]
