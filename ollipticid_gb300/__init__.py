@@ -117,8 +117,8 @@ def parse_olliptic_args(argv: Sequence[str]) -> Problem:
     bc = get(["-B", "--boundary"], str, "Dirichlet")   # interface.cc:272
     if bc not in BOUNDARIES:
         raise ValueError(f"boundary {bc!r} is not on the GPU path")
-    me = get(["-m", "--method"], str, "Vcycle")        # interface.cc:259
-    if me not in METHODS and me != "AppPuncture":
+    me = get(["-m", "--method"], str, "Vcycle")        # interface.cc:259, 1333-1354: unknown = Vcycle
+    if me in ("Gauss-Seidel", "Full-Multigrid"):
         raise ValueError(f"method {me!r} is not on the GPU path")
     nb = get(["-NumBH", "--num-bh"], int, 1)
     # AppPuncture's hierarchy is the V-cycle's; Elliptic.ApproximateID runs it

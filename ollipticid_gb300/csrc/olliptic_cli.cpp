@@ -11,10 +11,11 @@
 // Poisson (the Gaussian test), Boundary-test and Multibox-test are refused, and so are boundary conditions other than Robin and
 // Dirichlet (the reference's default).
 //
-// Methods (-m): Vcycle (the default), Wcycle (every level repeated until its
-// own norm meets the tolerance, elliptic::Wcycle; FP64) and AppPuncture (the
-// analytic approximation alone, elliptic::ApproximateID); the others are
-// refused.
+// Methods (-m): Vcycle (the default, and, as in the reference, what a name it
+// does not know means), Wcycle (every level repeated until its own norm
+// meets the tolerance, elliptic::Wcycle; FP64) and AppPuncture (the analytic
+// approximation alone, elliptic::ApproximateID); Gauss-Seidel and
+// Full-Multigrid are refused.
 //
 // Extra flags of this program (no reference counterpart):
 //   -gpu-mixed yes|no   mixed-precision cycles (FP32 correction around FP64)
@@ -617,12 +618,17 @@ int main(int argc, char **argv)
     return (int)OLGPU_ERR_INVALID_ARG;
   }
   // elliptic::Set_Method (src/elliptic.cc:229-294): V-cycles, W-cycles, or
-  // the analytic approximation alone (AppPuncture, elliptic::ApproximateID)
+  // the analytic approximation alone (AppPuncture, elliptic::ApproximateID).
+  // Like interface.cc:1333-1354 a name it does not know means Vcycle;
+  // Gauss-Seidel (elliptic::Gauss_Seidel, src/elliptic.cc:1389-1454) is not
+  // built, and Full-Multigrid is an empty member in the reference
+  // (include/elliptic.h:323-325: it leaves u at the initial guess), so both
+  // are refused rather than replaced.
   const char *me = A.find({"-m", "--method"});
   const std::string method = me ? me : "Vcycle";
   const bool approx_only = method == "AppPuncture";
   if (method == "Wcycle") p.method = OLGPU_METHOD_WCYCLE;
-  else if (method != "Vcycle" && !approx_only) {
+  else if (method == "Gauss-Seidel" || method == "Full-Multigrid") {
     std::fprintf(stderr, "Olliptic_gpu.x: method %s is not on the puncture FAS path\n", method.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
   }

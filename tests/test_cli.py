@@ -76,8 +76,9 @@ def test_bam_export_needs_a_file(cli, tmp_path):
 def test_other_equations_are_refused(cli):
     r = run(cli, "-eq Bowen_York -B Robin -N 33", check=False)
     assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
-    r = run(cli, "-eq Punctures -B Robin -N 33 -m Full-Multigrid", check=False)
-    assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
+    for m in ("Full-Multigrid", "Gauss-Seidel"):
+        r = run(cli, "-eq Punctures -B Robin -N 33 -m " + m, check=False)
+        assert r.returncode != 0 and "not on the puncture FAS path" in r.stderr
 
 
 @pytest.mark.parametrize("flag", ["-B Asymptotic", "-B Neumann"])
@@ -109,6 +110,8 @@ def test_cli_solve_matches_the_api(cli, case):
     "-eq Boundary-test -L 10 -N 25 -O 4 -l 3",
     "-eq Multibox-test -B Dirichlet -NumBH 2 -bhx1 -3 -bhx2 3 -L 20 -N 25 -O 2 -l 3",
     "-eq Punctures -NumBH 1 -bhmp1 0.5 -L 40 -N 25 -O 4 -l 3 -m AppPuncture",
+    "-eq Punctures -NumBH 1 -bhmp1 0.5 -L 40 -N 25 -O 4 -l 3 -m Wcycle",
+    "-eq Punctures -NumBH 1 -bhmp1 0.5 -L 40 -N 25 -O 4 -l 3 -m Multigrid",   # an unknown name is Vcycle
 ])
 def test_test_equations_methods_and_boundaries_are_accepted(cli, args):
     """The test equations, the Dirichlet default and the analytic method parse

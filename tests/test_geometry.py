@@ -63,3 +63,7 @@ def test_parse_ignores_unknown_flags():
     with pytest.raises(ValueError):
         parse_olliptic_args("-eq Bowen_York".split())
     assert parse_olliptic_args("-eq Poisson".split()).equation == "Poisson"   # the Gaussian test
+    assert parse_olliptic_args("-m Wcycle".split()).method == "Wcycle"
+    assert parse_olliptic_args("-m Multigrid".split()).method == "Vcycle"      # interface.cc: unknown = Vcycle
+    with pytest.raises(ValueError):
+        parse_olliptic_args("-m Gauss-Seidel".split())
