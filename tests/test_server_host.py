@@ -54,3 +54,14 @@ def test_server_config_is_checked():
     cfg.max_active = 0
     s = C.c_void_p()
     assert lib.olgpu_server_create(C.byref(cfg), C.byref(s)) == _abi.ERR_INVALID_ARG
+
+
+def test_python_scheduler_refuses_a_wcycle_request():
+    """The Python scheduler steps V-cycles too: a W-cycle request is refused
+    on arrival, before any device work."""
+    from ollipticid_gb300.serve import Server
+    w = problem("o4_spin")
+    w.method = "Wcycle"
+    S = Server(device=9999)
+    rep = S.run([(0.0, w)])
+    assert rep["completed"] == 1 and rep["results"][0].status == _abi.ERR_INVALID_ARG
