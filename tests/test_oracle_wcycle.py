@@ -66,3 +66,22 @@ def test_wcycle_call_checker_accepts_the_reference_and_rejects_a_v_cycle(oracle_
     ov.solve()
     with pytest.raises(AssertionError):
         check_wcycle_calls(ov.events(), ov.levels, P.tol)
+
+
+def test_oracle_vcycle_calls_reprint_the_reference(oracle_mod):
+    """The V-cycle's print calls (pre-smoothing from the top down, the
+    coarsest solve, post-smoothing back up, all with the cycle's number), the
+    order the library logs for its V-cycles, give the reference's own Loo.gp
+    and stdout0.out tables bit for bit (tests/golden/vcycle)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "vcycle", "o2_single.npz"))
+    P = problem(g["args"].item().decode())
+    orc = oracle_mod.Oracle(P.oracle_dict())
+    orc.solve()
+    ev = orc.events()
+    top = orc.levels - 1
+    assert [(e[0], e[1]) for e in ev[:2 * top + 1]] == [(k, 0) for k in range(top, -1, -1)] + \
+        [(k, 1) for k in range(1, top + 1)]
+    pre = [(c, v) for _, post, c, v in ev if not post]
+    assert [c for c, _ in pre] == list(g["loo_cycle"])
+    assert np.array_equal(np.array([v for _, v in pre]), g["loo_norm"])
+    assert render_cycle_tables(ev, orc.levels, P.tol) == g["stdout_cycles"].item().decode()
