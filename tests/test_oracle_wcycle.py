@@ -3,7 +3,8 @@ level repeated until its norm meets the tolerance) in the oracle, pinned
 against the reference's own runs (tests/golden/wcycle, from its Olliptic.x
 with -m Wcycle): the same sequence of level iterations with the same cycle
 numbers and bit-identical norms (Loo.gp), the same cycle tables
-(stdout0.out) and u.X, u.Y, u.Z digit for digit."""
+(stdout0.out) and u.X, u.Y, u.Z digit for digit; the V-cycle's calls are
+pinned the same way (tests/golden/vcycle)."""
 import glob
 import os
 
