@@ -1907,7 +1907,7 @@ static olgpu_status wcycle_level(olgpu_hierarchy *h, int k, long long icycle, do
 static void solve_wcycle(olgpu_hierarchy *h, SolveTrack &T)
 {
   const int top = h->G.levels - 1;
-  olgpu_status st = build_wgraphs(h);
+  olgpu_status st = top >= 1 ? build_wgraphs(h) : fail(OLGPU_ERR_GEOMETRY, "W-cycle: no coarser level");
   if (st == OLGPU_OK && cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream) != cudaSuccess)
     st = fail(OLGPU_ERR_CUDA, "W-cycle: clearing the norms");
   if (st != OLGPU_OK) {
