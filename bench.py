@@ -1,18 +1,20 @@
-"""Benchmark: puncture FAS solves/s on one GB300 (BASELINE configs[1]).
+"""Benchmark: puncture FAS solves/s on one GB300, plain FP64.
 
 Workload (one step = one full solve): the equal-mass binary of the reference's
 pars/Punctures/TestBH.run at 4th order -- two punctures m=0.487209 at
 y=+-5.5 with momenta (-+0.0901099, -+0.000703975, 0), Robin boundary, N=65,
 9 refinement levels, L=1000, 20 post-smoothing sweeps, solved from u = 0
-until the top-level residual is <= 1e-11.  Plain FP64 on the GPU.  Inputs are
-synthetic (the reference ships no data set; the problem is defined by its
-command line).
+until the top-level residual is <= 1e-11 and the cycle's largest change of u
+is <= 5e-11 (so that u ends within 1e-10 of the fixed point on every level,
+which the accuracy keys check against the reference's own fixed point).
+Inputs are synthetic (the reference ships no data set; the problem is
+defined by its command line).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
---impl reference times the reference algorithm on the host CPU cores (the
-oracle port, a bit-exact restatement of the reference's CPU solver) on the
-same workload.  With torchrun (N > 1) every rank solves its own copies of the
+--impl reference times complete solves of the same workload on the host CPU
+cores by the oracle port (a bit-exact restatement of the reference's CPU
+solver) under the reference's own stop rule.  With torchrun (N > 1) every rank solves its own copies of the
 workload on its own GPU (replicas: one solve never spans GPUs) and rank 0
 prints one JSON line.
 """
@@ -36,10 +38,12 @@ WORKLOAD_ARGS = ("-eq Punctures -B Robin -BA 0.0 -Bn 1 -NumBH 2 -bhmp1 0.487209 
 WORKLOAD_NAME = "binary_O4_N65_l9_L1000_tol1e-11"
 METRIC = "puncture solves/s to 1e-10 (served FP32/FP64 vs plain FP64); p99 latency; GB/s"
 UNIT = "solves/s"
-# The reference's own stop rule (src/elliptic.cc:1330) ends this workload
-# after 17 V-cycles at 9.95e-12 (lexicographic CPU solver, measured here with
-# the oracle, which reproduces the reference's iterates bit for bit).
-CPU_CYCLES_PER_SOLVE = 17
+# The timed stop (OLGPU_STOP_ERROR): top-level residual <= the problem's
+# tolerance (1e-11) and the cycle's largest change of u on every fixed point
+# <= half the metric's 1e-10 accuracy bar, so that u ends within 1e-10 of the
+# fixed point on every level (the reference's own rule, residual only, ends
+# this workload 1e-9 away).
+DU_TOL = 5e-11
 SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
 # DRAM bytes (read + write) and FP64-pipe occupancy of one finest-level
 # launch of k_smooth_color<4,0> on this workload, from an ncu capture
@@ -47,6 +51,15 @@ SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
 # .avg.pct_of_peak_sustained_active)
 SMOOTH_TRAFFIC_PER_LAUNCH = 17_600_768
 SMOOTH_FP64_PIPE_PCT = 70.4
+GOLDEN = os.path.join(ROOT, "tests", "golden", "configs")
+
+
+def bench_config():
+    """The workload as both arms name it (static: no measured values)."""
+    return {"workload": WORKLOAD_NAME, "args": WORKLOAD_ARGS,
+            "stop": f"top-level residual <= 1e-11 and the cycle's largest change of u <= {DU_TOL:g}",
+            "l2": "256 MiB buffer written before every timed solve (the 339 MB arena also exceeds L2)",
+            "boxes": 13, "points": 3852011}
 
 
 def _peaks():
@@ -59,60 +72,89 @@ def _peaks():
 
 
 # ----------------------------------------------------------------------------
-# CPU side (oracle port of the reference solver)
+# CPU side (oracle port of the reference solver): complete solves
 # ----------------------------------------------------------------------------
-def _cpu_worker(args):
-    n_warm, n_cycles, q = args
+def _cpu_solver(args):
+    """One process: `n` complete solves of the workload by the oracle port
+    under the reference's own stop rule (src/elliptic.cc:1330), each timed
+    from u = 0 to the stop; the hierarchy is built once, outside the timing
+    (the GPU arm's hierarchy is also resident)."""
+    n, q = args
     from oracle import oracle as O
     import ollipticid_gb300 as og
     P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
-    orc = O.Oracle(P.oracle_dict())
-    for _ in range(n_warm):
-        orc.vcycle()
-    times = []
-    for _ in range(n_cycles):
+    out = []
+    for _ in range(n):
+        orc = O.Oracle(P.oracle_dict())
         t0 = time.perf_counter()
-        orc.vcycle()
-        times.append(time.perf_counter() - t0)
-    q.put(times)
+        cycles, res = orc.solve()
+        out.append((time.perf_counter() - t0, cycles, res))
+        orc.close()
+    q.put(out)
 
 
-def cpu_throughput(n_warm: int, n_cycles: int, procs: int):
-    """Solves/s of `procs` concurrent single-threaded oracle solvers, from
-    timed V-cycles scaled by the cycles a full CPU solve needs."""
+def cpu_solves(total: int, procs: int):
+    """`total` complete CPU solves spread over `procs` single-threaded
+    processes (spawned); returns (aggregate solves/s of the busy processes,
+    wall seconds, per-solve records)."""
     from oracle import oracle as O
     O.build()
+    procs = max(1, min(procs, total))
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    ps = [ctx.Process(target=_cpu_worker, args=((n_warm, n_cycles, q),)) for _ in range(procs)]
+    share = [total // procs + (1 if i < total % procs else 0) for i in range(procs)]
+    ps = [ctx.Process(target=_cpu_solver, args=((n, q),)) for n in share]
+    t0 = time.perf_counter()
     for p in ps:
         p.start()
-    res = [q.get() for _ in ps]
+    recs = [q.get() for _ in ps]
+    wall = time.perf_counter() - t0
     for p in ps:
         p.join()
-    per_proc = [sum(t) / len(t) for t in res]                  # s per V-cycle
-    solves_per_s = sum(1.0 / (t * CPU_CYCLES_PER_SOLVE) for t in per_proc)
-    return solves_per_s, per_proc
+    rate = sum(len(r) / sum(t for t, _, _ in r) for r in recs)
+    return rate, wall, [x for r in recs for x in r]
+
+
+class CpuBaseline:
+    """One complete single-core solve, run in a spawned process beside the
+    GPU work (one host core of the GPU machine's 16)."""
+
+    def __init__(self):
+        from oracle import oracle as O
+        O.build()
+        ctx = mp.get_context("spawn")
+        self.q = ctx.Queue()
+        self.p = ctx.Process(target=_cpu_solver, args=((1, self.q),))
+        self.p.start()
+
+    def result(self):
+        (t, cycles, res), = self.q.get()
+        self.p.join()
+        return {"value": 1.0 / t, "unit": UNIT, "cores": 1, "kind": "port",
+                "sample": f"one complete single-threaded solve of this workload by the oracle port under the "
+                          f"reference's stop rule: {cycles} V-cycles to residual {res:.3g} in {t:.1f} s"}
 
 
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
-    procs = os.cpu_count() or 1
-    n_cycles = max(1, min(args.steps, 4))
-    n_warm = 0 if args.warmup <= 0 else 1
-    sps, per_proc = cpu_throughput(n_warm, n_cycles, procs)
+    procs = min(os.cpu_count() or 1, max(1, args.steps))
+    rate, wall, recs = cpu_solves(args.steps, procs)
+    cyc = sorted({c for _, c, _ in recs})
     line = {
         "impl": "reference",
-        "metric": METRIC, "value": sps, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1000.0 * procs / sps if sps > 0 else None,
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * wall / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD_NAME, "args": WORKLOAD_ARGS},
-        "cpu_baseline": {"value": sps, "unit": UNIT, "cores": procs, "kind": "port",
-                         "sample": f"{procs} concurrent single-threaded oracle solvers, {n_warm} warm-up + "
-                                   f"{n_cycles} timed V-cycles each, scaled by {CPU_CYCLES_PER_SOLVE} cycles/solve; "
-                                   f"mean s/cycle per process {sum(per_proc) / len(per_proc):.3f}"},
-        "e2e": {"value": sps, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": bench_config(),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": f"{args.steps} complete solves of the workload (the reference's stop rule, "
+                                   f"{'/'.join(map(str, cyc))} V-cycles each) by the oracle port in {procs} "
+                                   f"single-threaded processes; value = the sum of the processes' solve rates, "
+                                   f"ms_per_step = wall / steps ({wall:.1f} s); the hierarchy is built before each "
+                                   f"solve's timing; no warm-up (a CPU solve has nothing to warm)"},
+        "solves": [{"s": t, "cycles": c, "final_res": r} for t, c, r in recs],
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
@@ -189,63 +231,93 @@ def pinned_max_diff(E, a, b):
     return worst
 
 
-def fixed_point(E, tol=1e-14, max_cycles=120):
-    """Drive the FP64 cycle until u stops changing (untimed reference state)."""
+def load_fixture(name):
+    """The reference's fixed point of a benchmark problem, sampled
+    (tests/golden/configs, made by tests/golden/make_config_golden.py)."""
+    import numpy as np
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    return np.load(path) if os.path.exists(path) else None
+
+
+def reference_error(E, fx, u=None, adm=None):
+    """max |u - u_reference| at the fixture's sample points the discrete
+    system fixes, and the ADM masses' differences; u: per-box arrays (default:
+    the hierarchy's current u)."""
+    import numpy as np
+    if fx is None:
+        return None
+    worst, count = 0.0, 0
+    for g, box in enumerate(E.boxes):
+        x = (E.get_field(g) if u is None else u[g]).ravel()
+        idx = fx[f"idx_b{g}"].astype(np.int64)
+        want = fx[f"fixed_u_b{g}"]
+        if box.level < E.mgrid_levels:
+            nx, ny, nz = box.n
+            k, rem = np.divmod(idx, nx * ny)
+            j, i = np.divmod(rem, nx)
+            w = box.buf
+            keep = (i >= w) & (i < nx - w) & (j >= w) & (j < ny - w) & (k >= w) & (k < nz - w)
+            idx, want = idx[keep], want[keep]
+        worst = max(worst, float(np.max(np.abs(x[idx] - want))))
+        count += len(idx)
+    adm = E.ADM_mass if adm is None else adm
+    return {"max_abs_u_minus_reference": worst,
+            "adm_minus_reference": [float(a - b) for a, b in zip(adm, fx["fixed_adm"])],
+            "reference_points": count, "reference_source": str(fx["fixed_source"])}
+
+
+def fixed_point(E, du_tol=1e-13, max_cycles=300):
+    """The GPU's own FP64 fixed point (untimed): cycles until the largest
+    change of u is <= du_tol; returns u per box."""
     from ollipticid_gb300 import _abi
     E.set_precision(False)
     E.reset()
-    E.Solve(stop=_abi.STOP_FIXED, max_cycles=20)
-    prev = [E.get_field(g) for g in range(len(E.boxes))]
-    for _ in range(max_cycles):
-        E.FASN()
-        cur = [E.get_field(g) for g in range(len(E.boxes))]
-        d = max(float(abs(x - y).max()) for x, y in zip(cur, prev))
-        prev = cur
-        if d <= tol:
-            break
-    return prev
+    E.Solve(stop=_abi.STOP_ERROR, max_cycles=max_cycles, tol=E.problem.tol, du_tol=du_tol)
+    return [E.get_field(g) for g in range(len(E.boxes))]
 
 
-def run_mixed(E, P, args, dev, u_fix, adm_fix):
-    """Solves/s of the mixed-precision cycle on the same workload, stopped at
-    the same tolerance on the FP64 defect of the finest level, with its
-    deviation from the FP64 fixed point."""
-    import torch
+def timed_solves(E, steps, dev, tol, du_tol=DU_TOL):
+    """`steps` solves from u = 0 under the timed stop, L2 flushed before each;
+    (device ms, reports)."""
     from ollipticid_gb300 import _abi
-    E.set_precision(True)
-    for _ in range(args.warmup):
-        E.reset()
-        E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
-    ms, cycles = 0.0, 0
-    for _ in range(args.steps):
+    ms, reps = 0.0, []
+    for _ in range(steps):
         _flush_l2(dev)
         E.reset()
-        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
+        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=tol, du_tol=du_tol)
+        if not (rep.final_res <= tol and rep.final_du <= du_tol):
+            raise RuntimeError(f"solve stopped at residual {rep.final_res:.3g}, change {rep.final_du:.3g}")
         ms += E.last_device_ms
-        cycles += rep.cycles
+        reps.append(rep)
+    return ms, reps
+
+
+def run_mixed(E, P, args, dev, u_fix, fx):
+    """Solves/s of the mixed-precision cycle on the same workload under the
+    same stop (finest FP64 defect <= tol, change of u <= DU_TOL), with its
+    deviation from the reference's fixed point and from the GPU's FP64 one."""
+    E.set_precision(True)
+    timed_solves(E, args.warmup, dev, P.tol)
+    ms, reps = timed_solves(E, args.steps, dev, P.tol)
     u = [E.get_field(g) for g in range(len(E.boxes))]
+    ref = reference_error(E, fx, u, reps[-1].adm[:2])
     # the same solve alone with the schedule the autotuner picks for one solve
     from ollipticid_gb300 import autotune
     choice = autotune.tune(P, concurrency=1)
     choice.apply(E)
-    tms, tcyc = 0.0, 0
-    for _ in range(args.steps):
-        _flush_l2(dev)
-        E.reset()
-        trep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
-        tms += E.last_device_ms
-        tcyc += trep.cycles
+    tms, treps = timed_solves(E, args.steps, dev, P.tol)
+    tu = [E.get_field(g) for g in range(len(E.boxes))]
     tuned = {"value": args.steps / (tms / 1000.0), "ms_per_step": tms / args.steps,
              "inner_sweeps": [choice.nu1, choice.nu2], "smoother_blocks": choice.blocks,
-             "cycles_per_solve": tcyc / args.steps, "final_fp64_defect": trep.final_res,
-             "max_abs_u_minus_fp64_fixed_point": pinned_max_diff(E, [E.get_field(g) for g in range(len(E.boxes))],
-                                                                 u_fix)}
+             "cycles_per_solve": sum(r.cycles for r in treps) / args.steps, "final_fp64_defect": treps[-1].final_res,
+             "final_du": treps[-1].final_du, "accuracy": reference_error(E, fx, tu, treps[-1].adm[:2]),
+             "max_abs_u_minus_gpu_fp64_fixed_point": pinned_max_diff(E, tu, u_fix)}
     E.set_smoother_blocks(16)
     E.set_inner_sweeps(P.nu1, P.nu2)
     out = {"value": args.steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / args.steps,
-           "cycles_per_solve": cycles / args.steps, "final_fp64_defect": rep.final_res,
-           "max_abs_u_minus_fp64_fixed_point": pinned_max_diff(E, u, u_fix),
-           "adm_minus_fp64_fixed_point": [a - b for a, b in zip(rep.adm[:2], adm_fix)],
+           "cycles_per_solve": sum(r.cycles for r in reps) / args.steps, "final_fp64_defect": reps[-1].final_res,
+           "final_du": reps[-1].final_du, "accuracy": ref,
+           "max_abs_u_minus_gpu_fp64_fixed_point": pinned_max_diff(E, u, u_fix),
            "kernels_per_cycle": E.kernels_per_cycle, "tuned_alone": tuned,
            "dtype": "FP32 inner V-cycle (smoothing, Robin, transfers, coarse solve) on a correction; "
                     "FP64 defect, singular terms, update and norm"}
@@ -253,9 +325,11 @@ def run_mixed(E, P, args, dev, u_fix, adm_fix):
     return out
 
 
-def run_concurrent(E_ref, P, u_fix, adm_fix, plain_value, n: int = 16):
+def run_concurrent(E_ref, P, fx, plain_value, n: int = 16):
     """n copies of the workload solved at once (solve_many), mixed precision,
-    inner sweep schedule chosen by the autotuner at this concurrency."""
+    inner sweep schedule chosen by the autotuner at this concurrency, every
+    copy under the timed stop and checked against the reference's fixed
+    point."""
     import ollipticid_gb300 as og
     from ollipticid_gb300 import _abi, autotune
     choice = autotune.tune(P, concurrency=n)
@@ -266,25 +340,26 @@ def run_concurrent(E_ref, P, u_fix, adm_fix, plain_value, n: int = 16):
             choice.apply(E)
         for E in sol:
             E.reset()
-        og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200)           # warm-up
+        og.solve_many(sol, stop=_abi.STOP_ERROR, max_cycles=300, du_tol=DU_TOL)           # warm-up
         best = None
         for _ in range(3):
             for E in sol:
                 E.reset()
             t = time.perf_counter()
-            reps = og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200)
+            reps = og.solve_many(sol, stop=_abi.STOP_ERROR, max_cycles=300, du_tol=DU_TOL)
             dt = time.perf_counter() - t
             best = dt if best is None else min(best, dt)
-        worst_err = max(pinned_max_diff(E_ref, [E.get_field(g) for g in range(len(E.boxes))], u_fix)
-                        for E in sol[:2])
+        errs = [reference_error(E, fx) for E in sol]
         value = n / best
         return {"workload": f"{n} copies of {WORKLOAD_NAME} at once (solve_many), mixed precision",
                 "concurrent_solves": n, "value": value, "unit": UNIT,
                 "inner_sweeps": [choice.nu1, choice.nu2], "smoother_blocks": choice.blocks,
                 "autotune_table": choice.table,
                 "cycles_per_solve": reps[0].cycles, "final_fp64_defect": max(r.final_res for r in reps),
-                "max_abs_u_minus_fp64_fixed_point": worst_err,
-                "adm_minus_fp64_fixed_point": [a - b for a, b in zip(reps[0].adm[:2], adm_fix)],
+                "final_du": max(r.final_du for r in reps),
+                "max_abs_u_minus_reference": max(e["max_abs_u_minus_reference"] for e in errs) if fx else None,
+                "max_abs_adm_minus_reference": max(abs(a) for e in errs for a in e["adm_minus_reference"]) if fx
+                else None,
                 "vs_plain_fp64": value / plain_value,
                 "timing": "host wall clock around solve_many (best of 3), inputs resident in HBM"}
     finally:
@@ -297,29 +372,27 @@ CONFIG3_ARGS = WORKLOAD_ARGS.replace("-N 65", "-N 129").replace("-O 4", "-O 8").
 
 def run_config3():
     """The same binary at 8th order on boxes of 129^3 points: plain FP64 and
-    mixed precision, each solved from u = 0 to a residual of 1e-10, against
-    the FP64 fixed point (max |u - u_FP64| on every fixed point, ADM)."""
+    mixed precision, each solved from u = 0 under the timed stop (residual
+    <= 1e-10, change of u <= DU_TOL), against the reference's fixed point."""
     import ollipticid_gb300 as og
     from ollipticid_gb300 import _abi
     P = og.parse_olliptic_args(CONFIG3_ARGS.split())
+    fx = load_fixture("config3")
     E = og.Elliptic(P)
     try:
         out = {"workload": "binary O8 N129 l9 L1000, tol 1e-10", "boxes": len(E.boxes),
                "points": sum(b.n[0] * b.n[1] * b.n[2] for b in E.boxes)}
-        res = {}
-        for mixed in (False, True):
-            E.set_precision(mixed)
-            E.reset()
-            rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
-            res[mixed] = (rep, E.last_device_ms, [E.get_field(g) for g in range(len(E.boxes))])
-        u_fix = fixed_point(E)
-        adm_fix = E.ADM_mass
         for mixed, key in ((False, "plain_fp64"), (True, "mixed")):
-            rep, ms, u = res[mixed]
-            out[key] = {"solves_per_s": 1000.0 / ms, "ms_per_solve": ms, "cycles": rep.cycles,
-                        "final_res": rep.final_res, "max_abs_u_minus_fp64_fixed_point": pinned_max_diff(E, u, u_fix),
-                        "adm_minus_fp64_fixed_point": [a - b for a, b in zip(rep.adm[:2], adm_fix)]}
-        out["adm_fp64_fixed_point"] = list(adm_fix)
+            E.set_precision(mixed)
+            best = None
+            for _ in range(2):
+                E.reset()
+                rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)
+                best = E.last_device_ms if best is None else min(best, E.last_device_ms)
+            out[key] = {"solves_per_s": 1000.0 / best, "ms_per_solve": best, "cycles": rep.cycles,
+                        "final_res": rep.final_res, "final_du": rep.final_du,
+                        "accuracy": reference_error(E, fx, None, rep.adm[:2])}
+        E.set_precision(False)
         return out
     finally:
         E.close()
@@ -361,8 +434,8 @@ def run_convergence():
 def run_approx_start():
     """The benchmark binary solved from the reference's analytic puncture
     approximation (elliptic::ApproximateID, olgpu_approximate_id) instead of
-    u = 0, plain FP64 and mixed precision, each to the same residual by the
-    reference's stop rule; cycles and solves/s beside the zero start."""
+    u = 0, plain FP64 and mixed precision, each under the timed stop; cycles
+    and solves/s beside the zero start."""
     import ollipticid_gb300 as og
     from ollipticid_gb300 import _abi
     P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
@@ -378,7 +451,7 @@ def run_approx_start():
                         E.ApproximateID()
                     else:
                         E.reset()
-                    rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=300)
+                    rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=DU_TOL)
                     best = E.last_device_ms if best is None else min(best, E.last_device_ms)
                 row[start] = {"cycles": rep.cycles, "final_res": rep.final_res, "ms_per_solve": best,
                               "solves_per_s": 1000.0 / best}
@@ -418,12 +491,15 @@ def fp32_smoother_roofline(peak: float, peak_kind: str):
 
 
 def run_batched(args, count: int = 16, group: int = 16, tuned=None):
-    """Seeded batched binaries (mixed precision, tol 1e-10): solves/s when
-    `group` solves run concurrently, and the same instances one at a time."""
+    """Seeded batched binaries (mixed precision, residual <= 1e-10, change of
+    u <= DU_TOL): solves/s when `group` solves run concurrently, and the same
+    instances one at a time; each result against that problem's own FP64
+    fixed point on every point it fixes."""
     import ollipticid_gb300 as og
     from ollipticid_gb300 import _abi, workloads
     probs = workloads.batched_binaries(256)[:count]
-    seq_s, con_s, cycles = 0.0, 0.0, []
+    seq_s, con_s, cycles, errs = 0.0, 0.0, [], []
+    rule = dict(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)
     for g0 in range(0, count, group):
         sol = [og.Elliptic(p) for p in probs[g0:g0 + group]]
         for E in sol:
@@ -432,25 +508,33 @@ def run_batched(args, count: int = 16, group: int = 16, tuned=None):
                 tuned.apply(E)
         for E in sol:                                   # warm-up
             E.reset()
-        og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+        og.solve_many(sol, **rule)
         t = time.perf_counter()
         for E in sol:
             E.reset()
-            E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+            E.Solve(**rule)
         seq_s += time.perf_counter() - t
         for E in sol:
             E.reset()
         t = time.perf_counter()
-        reps = og.solve_many(sol, stop=_abi.STOP_TOLERANCE, max_cycles=200, tol=1e-10)
+        reps = og.solve_many(sol, **rule)
         con_s += time.perf_counter() - t
         cycles += [r.cycles for r in reps]
-        for E in sol:
+        for E, r in zip(sol, reps):
+            u = [E.get_field(g) for g in range(len(E.boxes))]
+            ufix = fixed_point(E)
+            errs.append((pinned_max_diff(E, u, ufix), max(abs(a - b) for a, b in zip(r.adm[:2], E.ADM_mass))))
             E.close()
     return {"workload": f"first {count} of 256 seeded binaries (N in {{33,49,65,97}}, 6-10 levels, O4), "
-                        f"mixed precision to 1e-10", "concurrent_solves": group,
+                        f"mixed precision, residual <= 1e-10 and change of u <= {DU_TOL:g}",
+            "concurrent_solves": group,
             "inner_sweeps": None if tuned is None else [tuned.nu1, tuned.nu2, tuned.blocks],
             "value": count / con_s, "unit": UNIT, "one_at_a_time": count / seq_s,
-            "cycles_mean": sum(cycles) / len(cycles), "timing": "host wall clock around the solves"}
+            "cycles_mean": sum(cycles) / len(cycles),
+            "max_abs_u_minus_fp64_fixed_point": max(e for e, _ in errs),
+            "max_abs_adm_minus_fp64_fixed_point": max(a for _, a in errs),
+            "accuracy_reference": "each problem's own FP64 fixed point on the GPU, every fixed point compared",
+            "timing": "host wall clock around the solves"}
 
 
 def run_served(rates=(4.0, 16.0, 64.0), count: int = 24, inner_sweeps=None, native: bool = False):
@@ -497,22 +581,17 @@ def run_gpu(args, rank: int, world: int, local: int):
     import ollipticid_gb300 as og
     from ollipticid_gb300 import _abi
 
+    # the single-core CPU solve runs in a spawned process beside the GPU work
+    cpu_job = CpuBaseline() if rank == 0 and world == 1 and not args.no_cpu_baseline else None
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
     E = og.Elliptic(P, device=local)
     nboxes = len(E.boxes)
     total_pts = sum(b.n[0] * b.n[1] * b.n[2] for b in E.boxes)
+    fx = load_fixture("config2")
 
-    def solve():
-        E.reset()
-        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
-        if rep.final_res > P.tol:
-            raise RuntimeError(f"solve did not reach {P.tol}: {rep.final_res}")
-        return rep
-
-    for _ in range(args.warmup):
-        solve()
+    timed_solves(E, args.warmup, dev, P.tol)
     # ---- timed region: K solves (device time from CUDA events on the solver's stream)
     clocks = ClockSampler(local)
     clocks.start()
@@ -520,14 +599,8 @@ def run_gpu(args, rank: int, world: int, local: int):
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     t_wall0 = time.perf_counter()
-    dev_ms, cycles = 0.0, 0
-    reps = []
-    for _ in range(args.steps):
-        _flush_l2(dev)
-        rep = solve()
-        dev_ms += E.last_device_ms
-        cycles += rep.cycles
-        reps.append(rep)
+    dev_ms, reps = timed_solves(E, args.steps, dev, P.tol)
+    cycles = sum(r.cycles for r in reps)
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall0
     dev_ms = slowest_rank_ms(dev_ms, world, dev)
@@ -535,6 +608,8 @@ def run_gpu(args, rank: int, world: int, local: int):
     ms_per_step = dev_ms / args.steps
     value = replica_throughput(args.steps, dev_ms, world)
     launches = E.kernels_per_cycle * cycles
+    u_stop = [E.get_field(g) for g in range(nboxes)]
+    accuracy = reference_error(E, fx, u_stop, reps[-1].adm[:2])
 
     # ---- end to end through the C ABI with host buffers (pinned host memory)
     def pinned_like(x):
@@ -556,27 +631,25 @@ def run_gpu(args, rank: int, world: int, local: int):
         E.reset()
         for g in range(nboxes):
             E.set_field(g, "u", hu0[g])
-        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=200)
+        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=DU_TOL)
         for g in range(nboxes):
             E.get_field(g, "u", out=hu[g])
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e = {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 3 * 8 * total_pts,
            "d2h_bytes_per_step": 8 * total_pts, "host_buffers": "pinned"}
 
-    # ---- accuracy of the timed solve against the converged FP64 fixed point
-    u_stop = [E.get_field(g) for g in range(nboxes)]
-    adm_stop = list(reps[-1].adm[:2])
+    # ---- the GPU's own FP64 fixed point (every point, beside the reference's samples)
     u_fix = fixed_point(E)
-    adm_fix = E.ADM_mass
-    err_fp64 = pinned_max_diff(E, u_stop, u_fix)
+    accuracy["max_abs_u_minus_gpu_fp64_fixed_point"] = pinned_max_diff(E, u_stop, u_fix)
+    accuracy["gpu_fp64_fixed_point_vs_reference"] = reference_error(E, fx, u_fix)
 
     # ---- the same workload with the mixed-precision cycle
-    mixed = run_mixed(E, P, args, dev, u_fix, adm_fix)
+    mixed = run_mixed(E, P, args, dev, u_fix, fx)
 
     concurrent = batched = served = config3 = convergence = approx_start = None
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
-        concurrent = run_concurrent(E, P, u_fix, adm_fix, value / world)
+        concurrent = run_concurrent(E, P, fx, value / world)
         batched = run_batched(args, tuned=autotune.tune(P, concurrency=16))
         config3 = run_config3()
         convergence = run_convergence()
@@ -602,34 +675,32 @@ def run_gpu(args, rank: int, world: int, local: int):
                       f"({pts} interior points, {colours} colours)",
             "algorithmic_bytes_per_launch": bytes_per_launch, "launch_us": launch_s * 1e6, "launches_timed": nl,
             "fp64_pipe_active_pct": SMOOTH_FP64_PIPE_PCT,
-            "note": "FP64-issue bound on GB300 (about 2 FP64 FMA per clock per SM): the HBM fraction is low by "
-                    "design; traffic and FP64 pipe occupancy are from one ncu capture of this launch (ncu flushes "
-                    "L2 first, so traffic is the level's fields read once; in the timed sweeps they stay in L2)"}
+            "note": "FP64-issue bound on GB300 (fp64_fma_peak_tflops, measured in this run): the HBM fraction is "
+                    "low by design; traffic and FP64 pipe occupancy are from one ncu capture of this launch (ncu "
+                    "flushes L2 first, so traffic is the level's fields read once; in the timed sweeps they stay "
+                    "in L2)"}
 
     roof32 = fp32_smoother_roofline(peak, peak_kind) if rank == 0 and world == 1 and not args.no_extra else None
+    # FMA issue rates of this GPU (the stencils' instruction roofline)
+    fma = {"fp64_tflops": og.fma_peak(True), "fp32_tflops": og.fma_peak(False),
+           "how": "olgpu_fma_peak: 8 blocks of 256 threads per SM, 8 independent FMA chains a thread, CUDA events, "
+                  "best of 3 after a warm-up launch; 2 flops per FMA"}
+    roof["fp64_fma_peak_tflops"] = fma["fp64_tflops"]
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        n_cycles = 2
-        sps, per_proc = cpu_throughput(0, n_cycles, 1)
-        cpu = {"value": sps, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"one single-threaded oracle solver, {n_cycles} timed V-cycles of this workload "
-                         f"({per_proc[0]:.2f} s/cycle) scaled by {CPU_CYCLES_PER_SOLVE} cycles/solve"}
+    cpu = cpu_job.result() if cpu_job is not None else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "args": WORKLOAD_ARGS, "precision": "plain FP64",
-                       "stop": "top-level residual <= 1e-11", "cycles_per_solve": cycles / args.steps,
-                       "final_res": reps[-1].final_res, "adm": [reps[-1].adm[0], reps[-1].adm[1]],
-                       "l2": "256 MiB buffer written before every timed solve", "boxes": nboxes,
-                       "points": total_pts, "wall_s": wall},
-            "accuracy": {"max_abs_u_minus_fixed_point": err_fp64,
-                         "adm_minus_fixed_point": [a - b for a, b in zip(adm_stop, adm_fix)]},
+            "config": bench_config(),
+            "solve": {"precision": "plain FP64", "cycles_per_solve": cycles / args.steps,
+                      "final_res": reps[-1].final_res, "final_du": reps[-1].final_du,
+                      "adm": [reps[-1].adm[0], reps[-1].adm[1]], "wall_s": wall},
+            "accuracy": accuracy,
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served, "config3": config3,
             "convergence": convergence, "approx_start": approx_start,
-            "roofline": roof, "roofline_fp32_smoother": roof32, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roof, "roofline_fp32_smoother": roof32, "fma_peaks": fma, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
         }

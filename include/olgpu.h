@@ -107,17 +107,27 @@ typedef struct {
   double xf, yf, zf;            /* coordinate of the last point (domain xf) */
 } olgpu_box_info;
 
-/* Stop rules for olgpu_solve. */
+/* Stop rules for olgpu_solve.  The reference stops on the top level's
+ * residual alone; on nested boxes the coarser levels can still be moving
+ * then (u 1e-9 from the fixed point at a 1e-11 residual), so
+ * OLGPU_STOP_ERROR also bounds the cycle's largest change of u on every
+ * point the discrete system fixes: with the cycle's contraction rate below
+ * one half that change bounds the distance of u from the fixed point.  For
+ * mixed precision the residual part is the finest FP64 defect.  V-cycles
+ * only. */
 typedef enum {
   OLGPU_STOP_REFERENCE = 0,     /* while res > tol && res < res_prev (src/elliptic.cc:1330) */
   OLGPU_STOP_TOLERANCE = 1,     /* while res > tol                                          */
-  OLGPU_STOP_FIXED = 2          /* exactly max_cycles cycles                                */
+  OLGPU_STOP_FIXED = 2,         /* exactly max_cycles cycles                                */
+  OLGPU_STOP_ERROR = 3          /* while res > tol || max |du| > du_tol                     */
 } olgpu_stop_kind;
 
 typedef struct {
   int stop;                     /* olgpu_stop_kind                        */
   int max_cycles;               /* hard cap on V-cycles (> 0)             */
   double tol;                   /* <= 0: the problem's -s tolerance       */
+  double du_tol;                /* OLGPU_STOP_ERROR's bound on the cycle's
+                                   largest change of u; <= 0: tol         */
 } olgpu_stop_rule;
 
 typedef struct {
@@ -126,6 +136,8 @@ typedef struct {
   double final_res;             /* top-level residual norm of the last cycle */
   double adm[OLGPU_MAX_BH];     /* ADM masses after the last cycle        */
   double res[256];              /* per-cycle top-level norms (first 256)  */
+  double final_du;              /* the last cycle's largest change of u on
+                                   the points the discrete system fixes   */
 } olgpu_report;
 
 typedef struct olgpu_hierarchy olgpu_hierarchy;
@@ -157,8 +169,9 @@ olgpu_status olgpu_box(const olgpu_hierarchy *h, int box, olgpu_box_info *out);
 olgpu_status olgpu_storage_order(const olgpu_box_info *box, long long *out);
 
 /* Field access by reference name: "u" "b" "c" "d" "e" "rho" (the source
- * rho0), "r", "w", "ww", "v".  Host arrays hold nx*ny*nz doubles in
- * lexicographic order, i fastest. */
+ * rho0), "r", "w", "ww", "v", and the solver's work fields "t" (the
+ * full-weighted W) and "up" (u as the last cycle found it).  Host arrays
+ * hold nx*ny*nz doubles in lexicographic order, i fastest. */
 olgpu_status olgpu_upload(olgpu_hierarchy *h, int box, const char *field, const double *host);
 olgpu_status olgpu_download(olgpu_hierarchy *h, int box, const char *field, double *host);
 
@@ -166,12 +179,21 @@ olgpu_status olgpu_download(olgpu_hierarchy *h, int box, const char *field, doub
 olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res);
 /* Repeated cycles of the problem's method under a stop rule; rule NULL =
  * the reference's rule.  For W-cycles the rule stops the top-level calls
- * (normally one: its own loop meets tol) and max_cycles also caps the
- * iterations of each level's loop in one call (the reference has no cap);
- * a level that reaches the cap without meeting tol ends the solve with
- * OLGPU_ERR_DIVERGED. */
+ * (normally one: its own loop meets tol), and the iterations of each level's
+ * loop in one call are capped at min(max_cycles, OLGPU_WCYCLE_LEVEL_CAP)
+ * (the reference has no cap and repeats forever where a level's norm levels
+ * off above tol); a level that reaches the cap without meeting tol ends the
+ * solve with OLGPU_ERR_DIVERGED. */
+#define OLGPU_WCYCLE_LEVEL_CAP 500
 olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out);
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out);
+/* The parts of the last finished cycle's norm (either pointer may be NULL):
+ * *res its residual (FP64: the top level's post-smoothing norm, the
+ * reference's; mixed: the finest FP64 defect) and *du its largest change of
+ * u on the points the discrete system fixes (every point of the solution
+ * levels, the INSIDE points of the multigrid coarse levels).  No reference
+ * counterpart. */
+olgpu_status olgpu_last_cycle(const olgpu_hierarchy *h, double *res, double *du);
 
 /* Smoother norms of one cycle of the current solve (0 = its first cycle;
  * olgpu_solve / olgpu_solve_many start a new history): pre[l] and post[l],
@@ -299,6 +321,8 @@ typedef struct {
                                    solves are on the GPU, clusters of 16 beyond */
   int keep_solutions;           /* != 0: a finished solve's hierarchy is handed
                                    to the caller in olgpu_server_result.h      */
+  double du_tol;                /* OLGPU_STOP_ERROR's bound on a cycle's change
+                                   of u; <= 0: the tolerance                   */
 } olgpu_server_config;
 
 typedef struct {
@@ -311,6 +335,7 @@ typedef struct {
   double latency_s;             /* arrival to the end of the last cycle       */
   olgpu_hierarchy *h;           /* keep_solutions: the solved hierarchy, now the
                                    caller's (destroy it); else NULL            */
+  double final_du;              /* the last cycle's largest change of u       */
 } olgpu_server_result;
 
 void olgpu_server_config_defaults(olgpu_server_config *c);
@@ -354,6 +379,13 @@ long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level);
  * *launches the number of smoother kernels it launched.  Changes u (FP64
  * precision) or the FP32 correction e (mixed precision: its smoother). */
 olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, double *ms, int *launches);
+/* Measured issue rate of dependent-free fused multiply-adds on the current
+ * device (no reference counterpart): every SM runs eight 256-thread blocks,
+ * each thread eight independent FMA chains of `iters` steps, timed with CUDA
+ * events; *tflops = 2 * FMAs / time.  precision: OLGPU_PREC_FP64 (double
+ * FMA) or OLGPU_PREC_MIXED (float FMA).  The stencil kernels' instruction
+ * roofline is taken against it. */
+olgpu_status olgpu_fma_peak(int precision, int iters, double *tflops);
 
 /* One box whose fields the caller already holds in device memory (all
  * nx*ny*nz doubles, lexicographic, i fastest, ghost layers included). */
@@ -386,6 +418,9 @@ typedef struct {
  *           returns after that stream has finished the sweeps.
  * The first call on a device looks up the scratch array's device address
  * (set-up once per device); make that first call before any stream capture.
+ * A device reset (cudaDeviceReset) makes that address stale: a call that
+ * meets a CUDA error forgets it and the next call looks it up again, so
+ * after a reset call once outside any capture before relying on it.
  * Every call on a device shares the one scratch array, and the call clears
  * the parts that must start at zero: calls that overlap on the GPU (from
  * several host threads or streams) race on it and must be serialised by the

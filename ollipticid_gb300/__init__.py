@@ -225,10 +225,12 @@ class Elliptic:
         check(self.lib.olgpu_vcycle(self._h, C.byref(r)))
         return r.value
 
-    def Solve(self, stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000, tol: float = 0.0) -> "_abi.Report":
+    def Solve(self, stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000, tol: float = 0.0,
+              du_tol: float = 0.0) -> "_abi.Report":
         """elliptic::Solve -> Vcycle or Wcycle (the problem's method) with the
-        reference stop rule by default."""
-        rule = _abi.StopRule(stop, max_cycles, tol)
+        reference stop rule by default.  STOP_ERROR also waits for the
+        cycle's largest change of u to be <= du_tol (0: tol)."""
+        rule = _abi.StopRule(stop, max_cycles, tol, du_tol)
         rep = _abi.Report()
         st = self.lib.olgpu_solve(self._h, C.byref(rule), C.byref(rep))
         self.last_report = rep
@@ -254,6 +256,13 @@ class Elliptic:
     def cycle_launch(self):
         """Enqueue one V-cycle without waiting (see cycle_poll)."""
         check(self.lib.olgpu_cycle_launch(self._h))
+
+    def last_cycle(self):
+        """(residual part, largest change of u on the fixed points) of the
+        last finished cycle (olgpu_last_cycle)."""
+        r, d = C.c_double(), C.c_double()
+        check(self.lib.olgpu_last_cycle(self._h, C.byref(r), C.byref(d)))
+        return r.value, d.value
 
     def cycle_poll(self, wait: bool = False):
         """(done, norm) of the last launched cycle."""
@@ -349,15 +358,30 @@ def smooth_box_noalloc(u: int, b: int, c: int, s: int, n, order: int, d, sweeps:
     return [norms[i] for i in range(int(sweeps))]
 
 
+def fma_peak(fp64: bool = True, iters: int = 0) -> float:
+    """Measured FMA throughput of the current device in TFLOP/s (FP64 or
+    FP32), the instruction roofline of the stencil kernels
+    (olgpu_fma_peak)."""
+    lib = _abi.load()
+    out = C.c_double()
+    n = iters or (4096 if fp64 else 65536)
+    check(lib.olgpu_fma_peak(_abi.PREC_FP64 if fp64 else _abi.PREC_MIXED, int(n), C.byref(out)))
+    return out.value
+
+
 def solve_many(solvers: Sequence["Elliptic"], stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000,
-               tol: float = 0.0) -> List["_abi.Report"]:
-    """Solve several problems concurrently on the GPU (olgpu_solve_many)."""
+               tol: float = 0.0, du_tol: float = 0.0, raise_on_error: bool = True) -> List["_abi.Report"]:
+    """Solve several problems concurrently on the GPU (olgpu_solve_many).
+    With raise_on_error False a failed solve does not raise: each report's
+    `status` tells how its problem ended."""
     lib = _abi.load()
     n = len(solvers)
     hs = (C.c_void_p * n)(*[s._h.value if isinstance(s._h, C.c_void_p) else s._h for s in solvers])
     reps = (_abi.Report * n)()
-    rule = _abi.StopRule(stop, max_cycles, tol)
-    check(lib.olgpu_solve_many(hs, n, C.byref(rule), reps))
+    rule = _abi.StopRule(stop, max_cycles, tol, du_tol)
+    st = lib.olgpu_solve_many(hs, n, C.byref(rule), reps)
     for s, r in zip(solvers, reps):
         s.last_report = r
+    if raise_on_error or st not in (_abi.OK, _abi.ERR_NAN, _abi.ERR_DIVERGED):
+        check(st)
     return list(reps)

@@ -7,7 +7,7 @@ import os
 MAX_BH = 16
 
 OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_NAN, ERR_DIVERGED, ERR_TIMEOUT, ERR_GEOMETRY, ERR_NO_DEVICE = range(9)
-STOP_REFERENCE, STOP_TOLERANCE, STOP_FIXED = range(3)
+STOP_REFERENCE, STOP_TOLERANCE, STOP_FIXED, STOP_ERROR = range(4)
 PREC_FP64, PREC_MIXED = range(2)
 
 _D16 = C.c_double * MAX_BH
@@ -42,13 +42,13 @@ class CycleEvent(C.Structure):
 
 
 class StopRule(C.Structure):
-    _fields_ = [("stop", C.c_int), ("max_cycles", C.c_int), ("tol", C.c_double)]
+    _fields_ = [("stop", C.c_int), ("max_cycles", C.c_int), ("tol", C.c_double), ("du_tol", C.c_double)]
 
 
 class Report(C.Structure):
     _fields_ = [
         ("cycles", C.c_int), ("status", C.c_int), ("final_res", C.c_double),
-        ("adm", _D16), ("res", C.c_double * 256),
+        ("adm", _D16), ("res", C.c_double * 256), ("final_du", C.c_double),
     ]
 
 
@@ -57,6 +57,7 @@ class ServerConfig(C.Structure):
         ("device", C.c_int), ("mem_budget", C.c_longlong), ("max_active", C.c_int), ("precision", C.c_int),
         ("stop", C.c_int), ("max_cycles", C.c_int), ("tol", C.c_double), ("builders", C.c_int),
         ("nu1", C.c_int), ("nu2", C.c_int), ("blocks", C.c_int), ("busy", C.c_int), ("keep_solutions", C.c_int),
+        ("du_tol", C.c_double),
     ]
 
 
@@ -64,6 +65,7 @@ class ServerResult(C.Structure):
     _fields_ = [
         ("id", C.c_longlong), ("status", C.c_int), ("cycles", C.c_int), ("final_res", C.c_double),
         ("adm", _D16), ("queue_s", C.c_double), ("latency_s", C.c_double), ("h", C.c_void_p),
+        ("final_du", C.c_double),
     ]
 
 
@@ -95,6 +97,7 @@ SIGNATURES = {
     "olgpu_vcycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "olgpu_solve": (C.c_int, [C.c_void_p, C.POINTER(StopRule), C.POINTER(Report)]),
     "olgpu_adm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "olgpu_last_cycle": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "olgpu_approximate_id": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_level_norms": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "olgpu_cycle_events": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(CycleEvent),
@@ -113,6 +116,7 @@ SIGNATURES = {
     "olgpu_kernels_per_cycle": (C.c_int, [C.c_void_p]),
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),
     "olgpu_time_smoother": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "olgpu_fma_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),
     "olgpu_smooth_box_noalloc": (C.c_int, [C.POINTER(BoxFields), C.c_int, C.POINTER(C.c_double), C.c_void_p]),
     "olgpu_server_config_defaults": (None, [C.POINTER(ServerConfig)]),
     "olgpu_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(C.c_void_p)]),

@@ -10,9 +10,10 @@
 
 namespace olgpu {
 
-// F_T is a work field of the device solver (full-weighted W), not a
-// reference field.
-enum Field { F_U = 0, F_B, F_C, F_D, F_E, F_RHO, F_R, F_W, F_WW, F_V, F_T, F_NUM };
+// F_T and F_UP are work fields of the device solver, not reference fields:
+// F_T holds the full-weighted W, F_UP u as the current cycle found it (the
+// cycle's largest change of u is measured against it).
+enum Field { F_U = 0, F_B, F_C, F_D, F_E, F_RHO, F_R, F_W, F_WW, F_V, F_T, F_UP, F_NUM };
 
 constexpr int kMaxBoxesPerLevel = 32;
 constexpr int kMaxInterpPoints = 10;   // Lagrange order 9 (order 8 ghosts)

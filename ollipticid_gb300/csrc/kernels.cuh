@@ -292,6 +292,49 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long *s
 }
 
 
+// Largest change of u over one cycle, max |u - up| over the points the
+// discrete system fixes (pinned[p] != 0: every point of the solution levels,
+// the INSIDE points of the multigrid coarse levels), into *slot as a bit
+// pattern.  A NaN difference wins the maximum.  n = all points of the arena.
+__global__ void __launch_bounds__(256) k_du_max(long long n, const double *__restrict__ u,
+                                                const double *__restrict__ up,
+                                                const unsigned char *__restrict__ pinned,
+                                                unsigned long long *slot)
+{
+  double m = 0.0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
+    if (pinned[p]) {
+      const double d = fabs(u[p] - up[p]);
+      if (d > m || is_nan_bits(d)) m = d;
+      if (is_nan_bits(m)) break;
+    }
+  block_max_atomic(m, slot);
+}
+
+// FMA issue-rate probe (olgpu_fma_peak): kFmaChains independent chains per
+// thread, x <- x * a + c, which stays near c / (1 - a) = 1 (no overflow, no
+// subnormals).  The result is stored only if it is impossible (x > 1e30), so
+// the loop is kept and nothing is written.
+constexpr int kFmaChains = 8;
+
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_peak(int iters, T *sink)
+{
+  T x[kFmaChains];
+#pragma unroll
+  for (int c = 0; c < kFmaChains; c++) x[c] = T(threadIdx.x + c) * T(1e-3);
+  const T a = T(0.999), k = T(1e-3);
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int c = 0; c < kFmaChains; c++) x[c] = fma(x[c], a, k);
+  }
+  T s = 0;
+#pragma unroll
+  for (int c = 0; c < kFmaChains; c++) s += x[c];
+  if (s > T(1e30)) *sink = s;
+}
+
 // Inverse of the Newton diagonal dOP/du for the smoother's step.  The step
 // u -= R / dOP only needs the diagonal approximately: a relative error of
 // about 1e-6 in it scales the step by 1 +- 1e-6 and leaves the fixed point

@@ -52,6 +52,8 @@ constexpr int kThreads = 256;
 // wave of 256-thread blocks, so smaller blocks spread it more evenly
 constexpr int kSmoothThreads = 128;
 constexpr size_t kCoarseSmemMax = 200 * 1024;   // dynamic shared memory of the coarse solves
+// iterations of one W-cycle level's loop in one call (OLGPU_WCYCLE_LEVEL_CAP)
+constexpr int kWcycleLevelCap = OLGPU_WCYCLE_LEVEL_CAP;
 
 // Host copy of one transfer: its jobs, their block prefix and the device copy.
 struct Transfer {
@@ -65,8 +67,13 @@ struct Transfer {
   XferJob *d_jobs = nullptr;
 };
 
+// Norm slots of a cycle beside the smoothers' (2 a level, pre/post): the
+// cycle's largest change of u on the fixed points, the mixed cycle's largest
+// correction and its finest FP64 defect.
+constexpr int kSlotDu = 125, kSlotCorr = 126, kSlotDefect = 127;
+
 struct Stats {                      // device scalars read back after a cycle
-  unsigned long long slots[128];    // smoother norms, 2 per level (pre/post)
+  unsigned long long slots[128];    // smoother norms, 2 per level (pre/post), then kSlot*
   double coarse_norm;
   int coarse_iters;
   int nan_flag;
@@ -117,6 +124,10 @@ struct olgpu_hierarchy {
   cudaGraphExec_t graph_mixed = nullptr;
   int launches_mixed = 0;
   double last_defect = 0, last_correction = 0;   // parts of the last mixed cycle's norm
+  // the last finished cycle: its residual (FP64: the top level's post-
+  // smoothing norm; mixed: the finest FP64 defect) and its largest change of
+  // u on the fixed points
+  double last_res = 0, last_du = 0;
   // smoother norms of every cycle since the solve began: per cycle, levels
   // pre-smoothing norms then levels post-smoothing norms (level 0: the
   // coarsest solve's)
@@ -192,6 +203,28 @@ long long blocks_faces(const DevBox &B)
   long long cols = 0;
   for (int a = 0; a < 3; a++) cols += 2LL * (B.n[(a + 1) % 3] - 2 * b) * (B.n[(a + 2) % 3] - 2 * b);
   return cdiv(cols, kThreads);   // one thread per normal column of each face
+}
+
+// The stencil terms of a box descriptor, shared by the hierarchy's boxes and
+// the single caller-owned box of olgpu_smooth_box_noalloc: 1/dx and 1/dx^2
+// per axis, whether every axis has the same spacing, and the diagonal of the
+// order's Laplacian (duLapc2/4/6/8, include/ffunction.h:1310-1313,
+// 1382-1385, 1466-1469, 1521-1524).
+void set_box_stencil(DevBox &B, int order, const double d[3])
+{
+  B.order = order;
+  for (int a = 0; a < 3; a++) {
+    B.idx[a] = 1.0 / d[a];
+    B.idx2[a] = B.idx[a] * B.idx[a];
+  }
+  B.iso = B.idx2[0] == B.idx2[1] && B.idx2[1] == B.idx2[2];
+  const double s = B.idx2[0] + B.idx2[1] + B.idx2[2];
+  switch (order) {
+  case 2: B.dulap = -2.0 * s; break;
+  case 4: B.dulap = -2.5 * s; break;
+  case 6: B.dulap = -490 * s * (1.0 / 180); break;
+  default: B.dulap = -205 * s / 72.0; break;
+  }
 }
 
 PunctureParams puncture_params(const olgpu_problem *p)
@@ -779,6 +812,23 @@ void emit_fasn(olgpu_hierarchy *h, int k, int top)
   emit_fasn_up<EQ>(h, k, top);
 }
 
+// The cycle's largest change of u on the points the discrete system fixes:
+// u as the cycle finds it is copied to F_UP first, max |u - up| ends the
+// cycle.  With the residual it bounds how far u still is from the fixed
+// point (OLGPU_STOP_ERROR).
+void emit_du_begin(olgpu_hierarchy *h)
+{
+  cudaMemcpyAsync(h->F.f[F_UP], h->F.f[F_U], sizeof(double) * (size_t)h->total_pts, cudaMemcpyDeviceToDevice,
+                  h->stream);
+}
+
+int emit_du_end(olgpu_hierarchy *h)
+{
+  k_du_max<<<152 * 4, kThreads, 0, h->stream>>>(h->total_pts, h->F.f[F_U], h->F.f[F_UP], h->d_pinned,
+                                                  &h->d_stats->slots[kSlotDu]);
+  return 1;
+}
+
 // ---------------------------------------------------------------------------
 // mixed precision: FP64 preparation, FP32 correction cycle, FP64 update
 // ---------------------------------------------------------------------------
@@ -1110,7 +1160,7 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     float *DU = h->d_and, *DF = h->d_and + (size_t)kAndMax * n, *fprev = h->d_and + (size_t)2 * kAndMax * n;
     const int nblk = 152 * 4;
     k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E], fprev, DF, h->d_pinned, h->d_and_state,
-                                                    h->d_and_part, &h->d_stats->slots[126]);
+                                                    h->d_and_part, &h->d_stats->slots[kSlotCorr]);
     k_and_solve<<<1, 32 * kAndSolveWarps, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
     k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U], h->F32.f[G_E], DU, DF, h->d_and_state);
     h->launches_mixed += 3;
@@ -1118,11 +1168,11 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
     for (int l = 0; l < L; l++) {
       const BoxList BL = level_list(h, l, blocks_all);
       k_mx_update<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, mg,
-                                                                &h->d_stats->slots[126]);
+                                                                &h->d_stats->slots[kSlotCorr]);
       h->launches_mixed++;
     }
   }
-  dispatch_mx_defect<EQ>(h, top, &h->d_stats->slots[127]);
+  dispatch_mx_defect<EQ>(h, top, &h->d_stats->slots[kSlotDefect]);
   if (!h->hadm.empty()) {
     k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
     h->launches_mixed++;
@@ -1190,21 +1240,9 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
   {
     const size_t n = (size_t)h->total_pts;
     if (cudaMalloc(&h->d_and, sizeof(float) * n * (2 * kAndMax + 1)) != cudaSuccess ||
-        cudaMalloc(&h->d_pinned, n) != cudaSuccess || cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess ||
+        cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess ||
         cudaMalloc(&h->d_and_part, sizeof(double) * 152 * 4 * kAndPart) != cudaSuccess)
       return fail(OLGPU_ERR_OOM, "Anderson history allocation failed");
-    std::vector<unsigned char> pin(n, 1);
-    for (const DevBox &B : h->hboxes) {
-      if (B.level >= h->G.mgrid_levels) continue;
-      for (int k = 0; k < B.n[2]; k++)
-        for (int j = 0; j < B.n[1]; j++)
-          for (int i = 0; i < B.n[0]; i++) {
-            const bool in = i >= B.buf && i < B.n[0] - B.buf && j >= B.buf && j < B.n[1] - B.buf && k >= B.buf &&
-                            k < B.n[2] - B.buf;
-            if (!in) pin[B.off + ((size_t)k * B.n[1] + j) * B.n[0] + i] = 0;
-          }
-    }
-    CUDA_TRY(cudaMemcpy(h->d_pinned, pin.data(), n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(h->d_and, 0, sizeof(float) * n * (2 * kAndMax + 1)));
     olgpu_status st = reset_anderson(h);
     if (st != OLGPU_OK) return st;
@@ -1227,8 +1265,10 @@ olgpu_status capture_mixed(olgpu_hierarchy *h)
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
   h->launches_mixed = 0;
+  emit_du_begin(h);
   if (h->equation == 1) emit_mixed_cycle<1>(h);
   else emit_mixed_cycle<0>(h);
+  h->launches_mixed += emit_du_end(h);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("mixed graph capture: ") + cudaGetErrorString(e));
   e = cudaGraphInstantiate(&h->graph_mixed, g, 0);
@@ -1244,9 +1284,11 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
   h->launches = 0;
+  emit_du_begin(h);
   if (h->equation == 1) emit_fasn<1>(h, top, top);
   else if (h->equation >= 2) emit_fasn<2>(h, top, top);   // the test equations share one operator
   else emit_fasn<0>(h, top, top);
+  h->launches += emit_du_end(h);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
   e = cudaGraphInstantiate(&h->graph, g, 0);
@@ -1308,7 +1350,7 @@ olgpu_status build_wgraphs(olgpu_hierarchy *h)
 
 int field_id(const char *name)
 {
-  static const char *names[F_NUM] = {"u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v", "t"};
+  static const char *names[F_NUM] = {"u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v", "t", "up"};
   if (!name) return -1;
   for (int f = 0; f < F_NUM; f++)
     if (!std::strcmp(name, names[f])) return f;
@@ -1485,7 +1527,7 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     delete h;
     return fail(OLGPU_ERR_GEOMETRY, "not enough grid points for multigrid");
   }
-  if (h->G.levels > 64) {
+  if (h->G.levels > 60) {   // norm slots 0..119 (2 a level); 120..127 hold the cycle's other norms
     delete h;
     return fail(OLGPU_ERR_INVALID_ARG, "too many levels");
   }
@@ -1499,24 +1541,12 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   int coff = 0;
   for (const domain &D : h->G.boxes) {
     DevBox B{};
-    for (int a = 0; a < 3; a++) {
-      B.n[a] = D.n[a];
-      B.idx[a] = 1.0 / D.d[a];
-      B.idx2[a] = B.idx[a] * B.idx[a];
-    }
+    for (int a = 0; a < 3; a++) B.n[a] = D.n[a];
     B.buf = D.buf;
-    B.order = D.order;
     B.level = D.level;
     B.off = off;
     B.coord_off = coff;
-    B.iso = B.idx2[0] == B.idx2[1] && B.idx2[1] == B.idx2[2];
-    const double s = B.idx2[0] + B.idx2[1] + B.idx2[2];
-    switch (D.order) {   // duLapc2/4/6/8
-    case 2: B.dulap = -2.0 * s; break;
-    case 4: B.dulap = -2.5 * s; break;
-    case 6: B.dulap = -490 * s * (1.0 / 180); break;
-    default: B.dulap = -205 * s / 72.0; break;
-    }
+    set_box_stencil(B, D.order, D.d);
     // x, y, z of the box's nodes, then their reciprocals (ghost nodes lie on
     // the outer faces; a node at 0 gets 0, it is never a Robin point)
     for (int a = 0; a < 3; a++)
@@ -1604,6 +1634,24 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   ok = ok && cudaMalloc(&h->d_stats, sizeof(Stats)) == cudaSuccess &&
        cudaMallocHost(&h->h_stats, sizeof(Stats)) == cudaSuccess;
   if (!ok) return cleanup(fail(OLGPU_ERR_OOM, "device allocation failed"));
+  // the points the discrete system fixes: every point of the solution levels,
+  // the INSIDE points of the multigrid coarse levels (their ghost layers keep
+  // whatever the iteration leaves there once W vanishes)
+  {
+    std::vector<unsigned char> pin((size_t)h->total_pts, 1);
+    for (const DevBox &B : h->hboxes) {
+      if (B.level >= h->G.mgrid_levels) continue;
+      for (int k = 0; k < B.n[2]; k++)
+        for (int j = 0; j < B.n[1]; j++)
+          for (int i = 0; i < B.n[0]; i++) {
+            const bool in = i >= B.buf && i < B.n[0] - B.buf && j >= B.buf && j < B.n[1] - B.buf && k >= B.buf &&
+                            k < B.n[2] - B.buf;
+            if (!in) pin[B.off + ((size_t)k * B.n[1] + j) * B.n[0] + i] = 0;
+          }
+    }
+    if (!up((void **)&h->d_pinned, pin.data(), pin.size()))
+      return cleanup(fail(OLGPU_ERR_OOM, "device allocation failed"));
+  }
   // coarsest box must fit in shared memory
   {
     const DevBox &B0 = h->hboxes[h->G.first_box[0]];
@@ -1758,10 +1806,12 @@ static olgpu_status cycle_finish(olgpu_hierarchy *h, double *res)
 {
   const bool mixed = h->precision == OLGPU_PREC_MIXED;
   const int top = h->G.levels - 1;
-  std::memcpy(res, &h->h_stats->slots[mixed ? 127 : 2 * top + 1], sizeof(double));
+  std::memcpy(res, &h->h_stats->slots[mixed ? kSlotDefect : 2 * top + 1], sizeof(double));
+  h->last_res = *res;
+  std::memcpy(&h->last_du, &h->h_stats->slots[kSlotDu], sizeof(double));
   if (mixed) {   // norm of a mixed cycle: max(finest FP64 defect, max |correction|)
     double corr;
-    std::memcpy(&corr, &h->h_stats->slots[126], sizeof(double));
+    std::memcpy(&corr, &h->h_stats->slots[kSlotCorr], sizeof(double));
     h->last_defect = *res;
     h->last_correction = corr;
     if (corr > *res) *res = corr;
@@ -1809,27 +1859,33 @@ static olgpu_status run_cycle(olgpu_hierarchy *h, double *res)
 // Stop-rule bookkeeping shared by olgpu_solve and olgpu_solve_many.
 struct SolveTrack {
   olgpu_stop_rule R;
-  double tol;
+  double tol, du_tol;
   double res = 1e12, res_prev = 1e12;
+  double du = 0;
   int cycles = 0;
   bool done = false;
   olgpu_status status = OLGPU_OK;
   olgpu_report rep{};
 
-  // Records one finished cycle; returns true once the rule stops the solve.
-  bool step(olgpu_status s, double r)
+  // Records one finished cycle (r: its norm; part: its residual part;
+  // change: its largest change of u); returns true once the rule stops the
+  // solve.
+  bool step(olgpu_status s, double r, double part, double change)
   {
     res_prev = res;
     res = r;
+    du = change;
     if (cycles < 256) rep.res[cycles] = r;
     cycles++;
     status = s;
     if (s != OLGPU_OK || cycles >= R.max_cycles) return true;
     if (R.stop == OLGPU_STOP_FIXED) return false;
+    if (R.stop == OLGPU_STOP_ERROR) return part <= tol && change <= du_tol;   // a NaN never stops it
     if (!(res > tol)) return true;
     if (R.stop == OLGPU_STOP_REFERENCE && !(res < res_prev)) return true;
     return false;
   }
+  bool step(olgpu_hierarchy *h, olgpu_status s, double r) { return step(s, r, h->last_res, h->last_du); }
 };
 
 olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res)
@@ -1846,10 +1902,14 @@ olgpu_status olgpu_vcycle(olgpu_hierarchy *h, double *res)
 
 static olgpu_status make_track(olgpu_hierarchy *h, const olgpu_stop_rule *rule, SolveTrack &T)
 {
-  T.R = olgpu_stop_rule{OLGPU_STOP_REFERENCE, 100000, 0.0};
+  T.R = olgpu_stop_rule{OLGPU_STOP_REFERENCE, 100000, 0.0, 0.0};
   if (rule) T.R = *rule;
   if (T.R.max_cycles <= 0) return fail(OLGPU_ERR_INVALID_ARG, "max_cycles must be > 0");
+  if (T.R.stop < OLGPU_STOP_REFERENCE || T.R.stop > OLGPU_STOP_ERROR) return fail(OLGPU_ERR_INVALID_ARG, "unknown stop rule");
+  if (T.R.stop == OLGPU_STOP_ERROR && h->P.method != OLGPU_METHOD_VCYCLE)
+    return fail(OLGPU_ERR_INVALID_ARG, "OLGPU_STOP_ERROR is a V-cycle rule");
   T.tol = T.R.tol > 0 ? T.R.tol : h->eps_solv;
+  T.du_tol = T.R.du_tol > 0 ? T.R.du_tol : T.tol;
   h->norm_hist.clear();
   h->events.clear();
   return OLGPU_OK;
@@ -1860,6 +1920,7 @@ static void close_track(olgpu_hierarchy *h, SolveTrack &T, olgpu_report *out)
   T.rep.cycles = T.cycles;
   T.rep.status = T.status;
   T.rep.final_res = T.res;
+  T.rep.final_du = T.du;
   for (int i = 0; i < h->P.numbh; i++) T.rep.adm[i] = h->adm[i];
   if (out) *out = T.rep;
 }
@@ -1911,12 +1972,16 @@ static void solve_wcycle(olgpu_hierarchy *h, SolveTrack &T)
   if (st == OLGPU_OK && cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream) != cudaSuccess)
     st = fail(OLGPU_ERR_CUDA, "W-cycle: clearing the norms");
   if (st != OLGPU_OK) {
-    T.step(st, 0.0);
+    T.step(st, 0.0, 0.0, 0.0);
     return;
   }
+  // each level's own loop is capped separately (the reference has no cap):
+  // a coarse level whose norm levels off above tol would otherwise repeat
+  // max_cycles times inside every iteration of the levels above it
+  const int level_cap = std::min(T.R.max_cycles, kWcycleLevelCap);
   for (;;) {
     double r = 0;
-    olgpu_status s = wcycle_level(h, top, T.cycles, T.tol, T.R.max_cycles, &r);
+    olgpu_status s = wcycle_level(h, top, T.cycles, T.tol, level_cap, &r);
     if (s == OLGPU_OK || s == OLGPU_ERR_DIVERGED) {
       for (int post = 0; post < 2; post++)   // the latest norms of every level, as a V-cycle's
         for (int l = 0; l <= top; l++) {
@@ -1927,7 +1992,7 @@ static void solve_wcycle(olgpu_hierarchy *h, SolveTrack &T)
       const olgpu_status a = finish_adm(h);
       if (s == OLGPU_OK) s = a;
     }
-    if (T.step(s, r)) break;
+    if (T.step(s, r, r, 0.0)) break;
   }
 }
 
@@ -1945,7 +2010,7 @@ olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_
     for (;;) {
       double r = 0;
       olgpu_status s = run_cycle(h, &r);
-      if (T.step(s, r)) break;
+      if (T.step(h, s, r)) break;
     }
   }
   cudaEventRecord(h->ev1, h->stream);
@@ -2008,7 +2073,7 @@ olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule
       olgpu_status s = olgpu_cycle_poll(hs[i], 0, &done, &r);
       if (!done && s == OLGPU_OK) continue;
       progressed = true;
-      if (T[i].step(s, r)) {
+      if (T[i].step(hs[i], s, r)) {
         T[i].done = true;
         active--;
         if (s != OLGPU_OK) worst = s;
@@ -2021,6 +2086,14 @@ olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule
   }
   for (int i = 0; i < n; i++) close_track(hs[i], T[i], reports ? &reports[i] : nullptr);
   return worst;
+}
+
+olgpu_status olgpu_last_cycle(const olgpu_hierarchy *h, double *res, double *du)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (res) *res = h->last_res;
+  if (du) *du = h->last_du;
+  return OLGPU_OK;
 }
 
 olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
@@ -2164,7 +2237,6 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
       for (auto &X : *vec) { cudaFree(X.d_jobs); X.d_jobs = nullptr; }
     cudaFree(h->d_arena32); h->d_arena32 = nullptr;
     cudaFree(h->d_and); h->d_and = nullptr;
-    cudaFree(h->d_pinned); h->d_pinned = nullptr;
     cudaFree(h->d_and_state); h->d_and_state = nullptr;
     cudaFree(h->d_and_part); h->d_and_part = nullptr;
     if (h->precision == OLGPU_PREC_MIXED) {
@@ -2262,6 +2334,43 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
   return OLGPU_OK;
 }
 
+olgpu_status olgpu_fma_peak(int precision, int iters, double *tflops)
+{
+  if (!tflops || iters < 1 || (precision != OLGPU_PREC_FP64 && precision != OLGPU_PREC_MIXED))
+    return fail(OLGPU_ERR_INVALID_ARG, "olgpu_fma_peak: bad argument");
+  int dev = 0, sms = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  cudaStream_t st;
+  CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t a, b;
+  CUDA_TRY(cudaEventCreate(&a));
+  CUDA_TRY(cudaEventCreate(&b));
+  const int blocks = 8 * sms, threads = 256;
+  double *sink = nullptr;
+  cudaError_t e = cudaMalloc(&sink, sizeof(double));
+  double best = 0.0;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+    cudaEventRecord(a, st);
+    if (precision == OLGPU_PREC_FP64) k_fma_peak<double><<<blocks, threads, 0, st>>>(iters, sink);
+    else k_fma_peak<float><<<blocks, threads, 0, st>>>(iters, reinterpret_cast<float *>(sink));
+    cudaEventRecord(b, st);
+    e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (rep == 0) continue;   // warm-up launch
+    const double ms = elapsed_ms(a, b);
+    const double fmas = (double)blocks * threads * kFmaChains * (double)iters;
+    if (ms > 0) best = std::max(best, 2.0 * fmas / (ms * 1e-3) / 1e12);
+  }
+  cudaFree(sink);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaStreamDestroy(st);
+  if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("olgpu_fma_peak: ") + cudaGetErrorString(e));
+  *tflops = best;
+  return OLGPU_OK;
+}
+
 }  // extern "C"
 
 // ============================================================================
@@ -2288,7 +2397,9 @@ constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 unsigned long long *g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
 
-// Device address of the scratch array on the current device (set-up once).
+// Device address of the scratch array on the current device (set-up once;
+// dropped again by noalloc_forget after a CUDA error, so that a call after a
+// device reset looks it up anew).
 olgpu_status noalloc_scratch(unsigned long long **out)
 {
   int dev = 0;
@@ -2305,6 +2416,25 @@ olgpu_status noalloc_scratch(unsigned long long **out)
   *out = g_noalloc_addr[dev];
   return OLGPU_OK;
 }
+
+void noalloc_forget()
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  g_noalloc_addr[dev] = nullptr;
+}
+
+// CUDA_TRY for the non-allocating entry point: a failed CUDA call also drops
+// the cached scratch address of the current device.
+#define NOALLOC_TRY(expr)                                                                    \
+  do {                                                                                       \
+    cudaError_t e_ = (expr);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      noalloc_forget();                                                                      \
+      return fail(OLGPU_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_));       \
+    }                                                                                        \
+  } while (0)
 
 template <int ORD, int EQ>
 void noalloc_sweeps(const BoxList &L, const DevBox *box, const DevFields &F, int sweeps, unsigned long long *scr,
@@ -2354,24 +2484,12 @@ extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int 
   B.n[1] = f->ny;
   B.n[2] = f->nz;
   B.buf = buf;
-  B.order = f->order;
   B.off = 0;
   const double d[3] = {f->dx, f->dy, f->dz};
-  for (int a = 0; a < 3; a++) {
-    B.idx[a] = 1.0 / d[a];
-    B.idx2[a] = B.idx[a] * B.idx[a];
-  }
-  B.iso = B.idx2[0] == B.idx2[1] && B.idx2[1] == B.idx2[2];
-  const double sum = B.idx2[0] + B.idx2[1] + B.idx2[2];
-  switch (f->order) {
-  case 2: B.dulap = -2.0 * sum; break;
-  case 4: B.dulap = -2.5 * sum; break;
-  case 6: B.dulap = -490 * sum * (1.0 / 180); break;
-  default: B.dulap = -205 * sum / 72.0; break;
-  }
+  set_box_stencil(B, f->order, d);
   // the descriptor and the zeroed accumulators go into the fixed scratch
-  CUDA_TRY(cudaMemcpyAsync(scr, &B, sizeof(DevBox), cudaMemcpyHostToDevice, cs));
-  CUDA_TRY(cudaMemsetAsync(scr + kNoAllocNormOff, 0,
+  NOALLOC_TRY(cudaMemcpyAsync(scr, &B, sizeof(DevBox), cudaMemcpyHostToDevice, cs));
+  NOALLOC_TRY(cudaMemsetAsync(scr + kNoAllocNormOff, 0,
                            sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1), cs));
   DevFields F{};
   F.f[F_U] = f->u;
@@ -2388,11 +2506,11 @@ extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int 
   const DevBox *dbox = reinterpret_cast<const DevBox *>(scr);
   if (f->d) noalloc_dispatch<1>(f->order, L, dbox, F, sweeps, scr, cs);
   else noalloc_dispatch<0>(f->order, L, dbox, F, sweeps, scr, cs);
-  CUDA_TRY(cudaGetLastError());
+  NOALLOC_TRY(cudaGetLastError());
   unsigned long long host[OLGPU_NOALLOC_MAX_SWEEPS + 1];
-  CUDA_TRY(cudaMemcpyAsync(host, scr + kNoAllocNormOff, sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1),
+  NOALLOC_TRY(cudaMemcpyAsync(host, scr + kNoAllocNormOff, sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1),
                            cudaMemcpyDeviceToHost, cs));
-  CUDA_TRY(cudaStreamSynchronize(cs));
+  NOALLOC_TRY(cudaStreamSynchronize(cs));
   if (norms)
     for (int s = 0; s < sweeps; s++) std::memcpy(&norms[s], &host[s], sizeof(double));
   int nan_flag = 0;

@@ -23,11 +23,11 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-// device bytes per point: 11 FP64 fields; mixed precision adds 11 FP32
-// fields, 9 FP32 Anderson vectors and a mask byte; plus a fixed allowance
+// device bytes per point: 12 FP64 fields and a mask byte; mixed precision
+// adds 11 FP32 fields and 9 FP32 Anderson vectors; plus a fixed allowance
 // for plans, tables and graphs
-constexpr long long kBytesPerPointFP64 = 11 * 8;
-constexpr long long kBytesPerPointMixed = 11 * 8 + 11 * 4 + 9 * 4 + 1;
+constexpr long long kBytesPerPointFP64 = 12 * 8 + 1;
+constexpr long long kBytesPerPointMixed = 12 * 8 + 11 * 4 + 9 * 4 + 1;
 constexpr long long kFixedBytes = 64LL << 20;
 
 struct Request {
@@ -47,15 +47,19 @@ struct Built {
 // olgpu_solve's stop rule for one served solve
 struct Track {
   int stop = OLGPU_STOP_TOLERANCE, max_cycles = 200;
-  double tol = 0, res = 1e12, res_prev = 1e12;
+  double tol = 0, du_tol = 0, res = 1e12, res_prev = 1e12, du = 0;
   int cycles = 0;
-  bool step(olgpu_status s, double r)
+  // r: the cycle's norm; part, change: its residual part and its largest
+  // change of u (olgpu_last_cycle)
+  bool step(olgpu_status s, double r, double part, double change)
   {
     res_prev = res;
     res = r;
+    du = change;
     cycles++;
     if (s != OLGPU_OK || cycles >= max_cycles) return true;
     if (stop == OLGPU_STOP_FIXED) return false;
+    if (stop == OLGPU_STOP_ERROR) return part <= tol && change <= du_tol;
     if (!(res > tol)) return true;
     if (stop == OLGPU_STOP_REFERENCE && !(res < res_prev)) return true;
     return false;
@@ -90,17 +94,19 @@ struct olgpu_server {
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
   void builder_loop();
   void scheduler_loop();
-  void finish(const Request &r, olgpu_status st, int cycles, double res, const double *adm, olgpu_hierarchy *keep);
+  void finish(const Request &r, olgpu_status st, int cycles, double res, const double *adm, olgpu_hierarchy *keep,
+              double du = 0.0);
 };
 
 void olgpu_server::finish(const Request &r, olgpu_status st, int cycles, double res, const double *adm,
-                          olgpu_hierarchy *keep)
+                          olgpu_hierarchy *keep, double du)
 {
   olgpu_server_result out{};
   out.id = r.id;
   out.status = st;
   out.cycles = cycles;
   out.final_res = res;
+  out.final_du = du;
   if (adm)
     for (int i = 0; i < OLGPU_MAX_BH; i++) out.adm[i] = adm[i];
   out.queue_s = r.admitted > 0 ? r.admitted - r.arrival : 0.0;
@@ -186,6 +192,7 @@ void olgpu_server::scheduler_loop()
       a.T.stop = cfg.stop;
       a.T.max_cycles = cfg.max_cycles;
       a.T.tol = cfg.tol > 0 ? cfg.tol : b.r.p.tol;
+      a.T.du_tol = cfg.du_tol > 0 ? cfg.du_tol : a.T.tol;
       const olgpu_status st = olgpu_cycle_launch(a.h);
       {
         std::lock_guard<std::mutex> g(mu);
@@ -215,7 +222,9 @@ void olgpu_server::scheduler_loop()
         continue;
       }
       progressed = true;
-      if (!a.T.step(st, res)) {
+      double part = res, change = 0;
+      olgpu_last_cycle(a.h, &part, &change);
+      if (!a.T.step(st, res, part, change)) {
         st = olgpu_cycle_launch(a.h);   // the next cycle; a failure ends the solve
         if (st == OLGPU_OK) {
           i++;
@@ -232,7 +241,7 @@ void olgpu_server::scheduler_loop()
         used -= a.r.bytes;
         n_active--;
       }
-      finish(a.r, rs, a.T.cycles, a.T.res, adm, keep);
+      finish(a.r, rs, a.T.cycles, a.T.res, adm, keep, a.T.du);
       active[i] = active.back();
       active.pop_back();
     }
@@ -266,6 +275,7 @@ void olgpu_server_config_defaults(olgpu_server_config *c)
   c->blocks = -1;
   c->busy = 4;
   c->keep_solutions = 0;
+  c->du_tol = 0.0;
 }
 
 olgpu_status olgpu_server_create(const olgpu_server_config *c, olgpu_server **out)
@@ -273,7 +283,7 @@ olgpu_status olgpu_server_create(const olgpu_server_config *c, olgpu_server **ou
   if (!c || !out) return OLGPU_ERR_INVALID_ARG;
   if (c->max_active < 1 || c->builders < 1 || c->max_cycles < 1 || c->mem_budget <= 0 ||
       (c->precision != OLGPU_PREC_FP64 && c->precision != OLGPU_PREC_MIXED) || c->stop < OLGPU_STOP_REFERENCE ||
-      c->stop > OLGPU_STOP_FIXED)
+      c->stop > OLGPU_STOP_ERROR)
     return OLGPU_ERR_INVALID_ARG;
   olgpu_server *s = new olgpu_server();
   s->cfg = *c;

@@ -28,10 +28,11 @@ import numpy as np
 from . import Elliptic, Problem, _abi
 from ._abi import check
 
-# device bytes per point: 11 FP64 fields, 11 FP32 fields, 9 FP32 Anderson
-# vectors, one mask byte (mixed precision); 11 FP64 fields in plain FP64
-BYTES_PER_POINT_MIXED = 11 * 8 + 11 * 4 + 9 * 4 + 1
-BYTES_PER_POINT_FP64 = 11 * 8
+# device bytes per point: 12 FP64 fields and one mask byte (the points the
+# discrete system fixes); mixed precision adds 11 FP32 fields and 9 FP32
+# Anderson vectors
+BYTES_PER_POINT_MIXED = 12 * 8 + 11 * 4 + 9 * 4 + 1
+BYTES_PER_POINT_FP64 = 12 * 8 + 1
 
 
 def footprint(problem: Problem, mixed: bool = True) -> int:
@@ -54,6 +55,7 @@ class Result:
     finished: float = 0.0
     cycles: int = 0
     final_res: float = 0.0
+    final_du: float = 0.0
     status: int = 0
     adm: List[float] = field(default_factory=list)
     u: Optional[list] = None
@@ -64,24 +66,34 @@ class Result:
 
 
 class _Track:
-    """The stop rule of olgpu_solve (tolerance on the cycle norm)."""
+    """The stop rule of olgpu_solve: STOP_TOLERANCE (the cycle norm <= tol)
+    or STOP_ERROR (its residual part <= tol and its largest change of u <=
+    du_tol)."""
 
-    def __init__(self, tol: float, max_cycles: int):
-        self.tol, self.max_cycles = tol, max_cycles
+    def __init__(self, tol: float, max_cycles: int, stop: int = _abi.STOP_TOLERANCE, du_tol: float = 0.0):
+        self.tol, self.max_cycles, self.stop = tol, max_cycles, stop
+        self.du_tol = du_tol if du_tol > 0 else tol
         self.cycles = 0
         self.res = 1e12
+        self.du = 0.0
 
-    def step(self, res: float) -> bool:
+    def step(self, res: float, part: float = None, du: float = 0.0) -> bool:
         self.cycles += 1
-        self.res = res
-        return not (res > self.tol) or self.cycles >= self.max_cycles
+        self.res, self.du = res, du
+        if self.cycles >= self.max_cycles:
+            return True
+        if self.stop == _abi.STOP_ERROR:
+            return (res if part is None else part) <= self.tol and du <= self.du_tol
+        return not (res > self.tol)
 
 
 class Server:
     def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
                  tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
-                 inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4):
-        """inner_sweeps: (nu1, nu2[, smoother cluster blocks]) of every mixed
+                 inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4, stop: int = _abi.STOP_TOLERANCE,
+                 du_tol: float = 0.0):
+        """stop: STOP_TOLERANCE or STOP_ERROR (with du_tol, 0: the
+        tolerance), the rule of every solve.  inner_sweeps: (nu1, nu2[, smoother cluster blocks]) of every mixed
         solve's FP32 cycle (for example an autotune choice); None keeps each
         problem's own nu1/nu2 and the default smoother layout.  Without a
         layout in inner_sweeps the layout follows the load when a request is
@@ -92,6 +104,7 @@ class Server:
         self.device, self.mem_budget, self.max_active = device, mem_budget, max_active
         self.mixed, self.tol, self.max_cycles, self.keep_u = mixed, tol, max_cycles, keep_u
         self.inner_sweeps, self.busy = inner_sweeps, busy
+        self.stop, self.du_tol = stop, du_tol
         self.pool = ThreadPoolExecutor(max_workers=builders)
 
     def _build(self, problem: Problem, blocks: int) -> Elliptic:
@@ -155,20 +168,27 @@ class Server:
                     tol = self.tol if self.tol is not None else prob.tol
                     E.cycle_launch()
                     results[rid].started = now()
-                    active.append({"rid": rid, "E": E, "track": _Track(tol, self.max_cycles), "bytes": nbytes})
+                    active.append({"rid": rid, "E": E, "bytes": nbytes,
+                                   "track": _Track(tol, self.max_cycles, self.stop, self.du_tol)})
             peak_active = max(peak_active, len(active))
             progressed = False
             for a in list(active):
-                done, res = a["E"].cycle_poll(False)
+                status = _abi.OK
+                try:
+                    done, res = a["E"].cycle_poll(False)
+                except _abi.OlgpuError as exc:      # e.g. NaN: this request ends, the others go on
+                    done, res, status = True, float("nan"), exc.status
                 if not done:
                     continue
                 progressed = True
-                if a["track"].step(res):
+                part, du = a["E"].last_cycle()
+                if status != _abi.OK or a["track"].step(res, part, du):
                     r = results[a["rid"]]
                     r.finished = now()
-                    r.cycles, r.final_res = a["track"].cycles, res
+                    r.status = status
+                    r.cycles, r.final_res, r.final_du = a["track"].cycles + (status != _abi.OK), res, du
                     r.adm = a["E"].ADM_mass
-                    if self.keep_u:
+                    if self.keep_u and status == _abi.OK:
                         r.u = [a["E"].get_field(g) for g in range(len(a["E"].boxes))]
                     a["E"].close()
                     used -= a["bytes"]
@@ -200,7 +220,8 @@ class NativeServer:
 
     def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
                  tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
-                 inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4, stop: int = _abi.STOP_TOLERANCE):
+                 inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4, stop: int = _abi.STOP_TOLERANCE,
+                 du_tol: float = 0.0):
         self.lib = _abi.load()
         c = _abi.ServerConfig()
         self.lib.olgpu_server_config_defaults(C.byref(c))
@@ -211,6 +232,7 @@ class NativeServer:
             c.nu1, c.nu2 = inner_sweeps[0], inner_sweeps[1]
             c.blocks = inner_sweeps[2] if len(inner_sweeps) > 2 else -1
         c.keep_solutions = 1 if keep_u else 0
+        c.du_tol = du_tol
         self.keep_u = keep_u
         s = C.c_void_p()
         check(self.lib.olgpu_server_create(C.byref(c), C.byref(s)))
@@ -230,7 +252,7 @@ class NativeServer:
         check(self.lib.olgpu_server_poll(self._s, rid, 1 if wait else 0, C.byref(done), C.byref(out)))
         if not done.value:
             return None
-        r = Result(rid, 0.0, cycles=out.cycles, final_res=out.final_res, status=out.status)
+        r = Result(rid, 0.0, cycles=out.cycles, final_res=out.final_res, final_du=out.final_du, status=out.status)
         r.admitted = out.queue_s
         r.finished = out.latency_s          # relative to arrival
         nbh = self._problems.pop(rid).numbh

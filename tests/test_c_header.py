@@ -66,3 +66,47 @@ def test_header_is_c_and_the_library_links(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("olgpu ") and "boxes 4 levels 4 multigrid 1" in r.stdout
     assert "refused:" in r.stdout and "order" in r.stdout
+
+
+LAYOUT = r"""
+#include "olgpu.h"
+#include <stddef.h>
+#include <stdio.h>
+#define S(t) printf(#t " %zu\n", sizeof(t))
+#define O(t, f) printf(#t "." #f " %zu\n", offsetof(t, f))
+int main(void)
+{
+  S(olgpu_problem); S(olgpu_box_info); S(olgpu_stop_rule); S(olgpu_report); S(olgpu_cycle_event);
+  S(olgpu_server_config); S(olgpu_server_result); S(olgpu_box_fields);
+  O(olgpu_stop_rule, du_tol); O(olgpu_report, final_du); O(olgpu_server_config, du_tol);
+  O(olgpu_server_result, final_du); O(olgpu_problem, method);
+  return 0;
+}
+"""
+
+
+def test_ctypes_mirror_has_the_header_layout(tmp_path):
+    """Every struct of the ABI has the same size and field offsets in the C
+    header and in the Python mirror (ollipticid_gb300/_abi.py)."""
+    import ctypes as C
+    from ollipticid_gb300 import _abi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(LAYOUT)
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c11", "-I", INCLUDE, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                               check=True).stdout.splitlines())
+    mirror = {"olgpu_problem": _abi.Problem, "olgpu_box_info": _abi.BoxInfo, "olgpu_stop_rule": _abi.StopRule,
+              "olgpu_report": _abi.Report, "olgpu_cycle_event": _abi.CycleEvent,
+              "olgpu_server_config": _abi.ServerConfig, "olgpu_server_result": _abi.ServerResult,
+              "olgpu_box_fields": _abi.BoxFields}
+    for name, cls in mirror.items():
+        assert int(got[name]) == C.sizeof(cls), name
+    for key, val in got.items():
+        if "." in key:
+            t, f = key.split(".")
+            assert int(val) == getattr(mirror[t], f).offset, key

@@ -1,0 +1,149 @@
+"""GPU fixed points of the benchmark problems against the reference's.
+
+The three benchmark problems (tests/cases.py CONFIG1, CONFIG2, CONFIG3: the
+single boosted puncture at 2nd order, the TestBH binary at 4th order on 65^3
+boxes, the same binary at 8th order on 129^3 boxes) are solved on the GPU in
+FP64 under OLGPU_STOP_ERROR to a change of u far below the parity bar; u at
+the fixtures' sample points (tests/golden/configs, made by
+tests/golden/make_config_golden.py from the reference itself, or from the
+oracle where the reference's run is too long: the key `fixed_source`) must
+agree to 1e-10 on every level and the ADM masses to 1e-9, the benchmark spec's
+bar.  The first problem is also compared on every point with the oracle's
+fixed point computed here (the oracle is pinned on this geometry by the same
+fixture, bit for bit, tests/test_oracle_configs.py).
+
+The timed solves of the benchmark (OLGPU_STOP_ERROR with the problem's
+residual tolerance and a change bound of half the 1e-10 bar, plain FP64 and
+mixed precision) must land within 1e-10 of the same fixed point.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from tests.cases import CONFIG1, CONFIG2, CONFIG3
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden", "configs")
+U_TOL = 1e-10        # max |u - u_reference| on every level
+ADM_TOL = 1e-9       # ADM mass
+CONFIGS = {"config1": CONFIG1, "config2": CONFIG2, "config3": CONFIG3}
+# the benchmark's timed stop: residual <= the problem's tolerance and the
+# cycle's largest change of u <= half the 1e-10 parity bar
+BENCH_DU_TOL = 5e-11
+
+
+def load(name):
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip(f"{name} fixture not generated")
+    return np.load(path)
+
+
+def sampled_error(E, g):
+    """max |u_gpu - u_fixture| over the fixture's sample points that the
+    discrete system fixes (coarse multigrid ghosts excluded)."""
+    worst = 0.0
+    for b, box in enumerate(E.boxes):
+        u = E.get_field(b).ravel()
+        idx = g[f"idx_b{b}"].astype(np.int64)
+        want = g[f"fixed_u_b{b}"]
+        if box.level < E.mgrid_levels:
+            nx, ny, nz = box.n
+            k, rem = np.divmod(idx, nx * ny)
+            j, i = np.divmod(rem, nx)
+            w = box.buf
+            keep = (i >= w) & (i < nx - w) & (j >= w) & (j < ny - w) & (k >= w) & (k < nz - w)
+            idx, want = idx[keep], want[keep]
+        worst = max(worst, float(np.max(np.abs(u[idx] - want))))
+    return worst
+
+
+def geometry_matches(E, g):
+    assert len(E.boxes) == len(g["box_n"])
+    for b, box in enumerate(E.boxes):
+        assert tuple(box.n) == tuple(int(v) for v in g["box_n"][b])
+        assert box.level == int(g["box_level"][b])
+        assert np.array_equal(np.array(box.origin), g["box_origin"][b])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["config1", "config2", "config3"])
+def test_fixed_point_matches_reference(name):
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+
+    g = load(name)
+    P = og.parse_olliptic_args(CONFIGS[name].split())
+    with og.Elliptic(P) as E:
+        geometry_matches(E, g)
+        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=400, tol=P.tol, du_tol=1e-13)
+        assert rep.final_du <= 1e-13
+        err = sampled_error(E, g)
+        adm = E.ADM_mass
+    assert err <= U_TOL, f"{name}: max|u_gpu - u_ref| = {err:.3e} ({g['fixed_source']})"
+    for a, b in zip(adm, g["fixed_adm"]):
+        assert abs(a - b) <= ADM_TOL, (name, a, b)
+
+
+@pytest.mark.gpu
+def test_config1_every_point_matches_oracle():
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    from oracle import oracle as O
+
+    P = og.parse_olliptic_args(CONFIG1.split())
+    orc = O.Oracle(P.oracle_dict())
+    orc.fixed_point(tol=1e-14)
+    with og.Elliptic(P) as E:
+        E.Solve(stop=_abi.STOP_ERROR, max_cycles=400, tol=P.tol, du_tol=1e-13)
+        worst = 0.0
+        for b, box in enumerate(E.boxes):
+            a, c = E.get_field(b), orc.field(b)
+            if box.level < E.mgrid_levels:
+                w = box.buf
+                a, c = a[w:-w, w:-w, w:-w], c[w:-w, w:-w, w:-w]
+            worst = max(worst, float(np.max(np.abs(a - c))))
+        adm = E.ADM_mass
+    assert worst <= U_TOL, worst
+    assert abs(adm[0] - orc.adm()[0]) <= ADM_TOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,mixed", [("config1", False), ("config2", False), ("config2", True),
+                                        ("config3", False), ("config3", True)])
+def test_benchmark_stop_lands_within_the_bar(name, mixed):
+    """The benchmark's timed solve from u = 0 under its stop rule ends within
+    1e-10 of the reference's fixed point (the reference's own stop rule ends
+    1e-9 away on the binary: the coarse levels still move at its residual)."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+
+    g = load(name)
+    P = og.parse_olliptic_args(CONFIGS[name].split())
+    with og.Elliptic(P) as E:
+        E.set_precision(mixed)
+        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=BENCH_DU_TOL)
+        assert rep.final_res <= P.tol and rep.final_du <= BENCH_DU_TOL
+        err = sampled_error(E, g)
+        adm = E.ADM_mass
+    assert err <= U_TOL, f"{name} mixed={mixed}: max|u - u_ref| = {err:.3e} after {rep.cycles} cycles"
+    for a, b in zip(adm, g["fixed_adm"]):
+        assert abs(a - b) <= ADM_TOL, (name, a, b)
+
+
+@pytest.mark.gpu
+def test_reference_stop_rule_stops_short_on_the_binary():
+    """What OLGPU_STOP_ERROR is for: the reference's own rule (residual
+    only) ends the binary with u still far from the fixed point, here as in
+    the reference."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+
+    g = load("config2")
+    P = og.parse_olliptic_args(CONFIG2.split())
+    with og.Elliptic(P) as E:
+        rep = E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=300)
+        err = sampled_error(E, g)
+    assert rep.final_res <= P.tol
+    assert err > 1e-10, err

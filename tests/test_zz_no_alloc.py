@@ -20,7 +20,7 @@ U_TOL = 1e-10
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["o4_spin", "sf_binary"])
+@pytest.mark.parametrize("case", ["o2_single", "o4_spin", "o8_offset", "sf_binary"])
 def test_noalloc_smoother_matches_hierarchy(case):
     torch = pytest.importorskip("torch")
     import ollipticid_gb300 as og
