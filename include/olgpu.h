@@ -353,6 +353,51 @@ olgpu_status olgpu_server_stats(olgpu_server *s, int *active, int *building, int
  * waiting when it is called. */
 olgpu_status olgpu_server_destroy(olgpu_server *s);
 
+/* Batching (no reference counterpart; the reference runs one solve per
+ * process): uneven puncture solves stepped together on one GPU, every FASN
+ * step of a level one launch over the boxes of all the solves at that level.
+ * The solves are grouped into unions -- the same equation, order, boundary,
+ * sweep counts and refinement depth (levels above the base grid) -- whose
+ * levels are aligned from the finest down, so that a solve with fewer levels
+ * reaches its coarsest solve earlier while the others descend further; each
+ * union holds its solves' fields in one device arena and steps them with one
+ * captured cycle, a solve that meets its stop rule drops out of every launch
+ * (its boxes are skipped) and the others go on.  A union of several solves
+ * runs each FASN step as one launch where the solves alone would run one
+ * launch each; the arithmetic of every point is the solve's own, so each
+ * result is the same, bit for bit, as the problem solved alone
+ * (olgpu_solve) under the same rule and precision.  V-cycles; mixed precision
+ * for the puncture equations with the Robin boundary. */
+typedef struct olgpu_batch olgpu_batch;
+
+typedef struct {
+  int device;                   /* CUDA device (-1: the current one)            */
+  int precision;                /* olgpu_precision of every solve               */
+  int nu1, nu2;                 /* FP32 cycle sweeps (mixed); < 0: the problems' */
+  int blocks;                   /* FP32 smoother cluster blocks (0: one launch per
+                                   colour and sweep); < 0: the default (16)     */
+} olgpu_batch_config;
+
+void olgpu_batch_config_defaults(olgpu_batch_config *c);
+/* Plans, groups and sets up n problems (initial guess u = 0). */
+olgpu_status olgpu_batch_create(const olgpu_problem *ps, int n, const olgpu_batch_config *c, olgpu_batch **out);
+/* Solves every problem of the batch under the same stop rule (NULL: the
+ * reference's); reports[i] (may be NULL) gets problem i's report.  Returns
+ * the first failure status, if any (each report holds its own). */
+olgpu_status olgpu_batch_solve(olgpu_batch *b, const olgpu_stop_rule *rule, olgpu_report *reports);
+/* u = 0 again for every problem (repeated solves of the same batch). */
+olgpu_status olgpu_batch_reset(olgpu_batch *b);
+/* Problem i's hierarchy, for olgpu_download / olgpu_box / olgpu_adm_mass /
+ * olgpu_level_norms (owned by the batch: do not destroy or solve it). */
+olgpu_hierarchy *olgpu_batch_member(olgpu_batch *b, int i);
+int olgpu_batch_size(const olgpu_batch *b);
+/* Unions the problems were grouped into, and their kernel launches per cycle. */
+int olgpu_batch_unions(const olgpu_batch *b);
+int olgpu_batch_kernels_per_cycle(const olgpu_batch *b);
+/* Host wall-clock time of the last olgpu_batch_solve in ms. */
+double olgpu_batch_last_ms(const olgpu_batch *b);
+olgpu_status olgpu_batch_destroy(olgpu_batch *b);
+
 /* elliptic::ApproximateID (src/elliptic.cc:1977-2226, the reference's
  * "-m AppPuncture" method): u on every point of every box becomes the
  * perturbative puncture solution (spin, momentum and cross terms summed over

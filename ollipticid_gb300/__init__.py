@@ -358,6 +358,107 @@ def smooth_box_noalloc(u: int, b: int, c: int, s: int, n, order: int, d, sweeps:
     return [norms[i] for i in range(int(sweeps))]
 
 
+class Batch:
+    """Uneven puncture solves stepped together (olgpu_batch_*): each FASN
+    step of a level is one launch over the boxes of every solve at that level
+    (solves grouped into unions with their levels aligned from the finest);
+    a solve that meets its stop rule drops out of the launches.  Each result
+    is the problem's solo result bit for bit."""
+
+    def __init__(self, problems: Sequence[Problem], mixed: bool = True, inner_sweeps=None, blocks: int = -1,
+                 device: int = 0):
+        self.lib = _abi.load()
+        self.problems = list(problems)
+        arr = (_abi.Problem * len(self.problems))(*[p.to_c() for p in self.problems])
+        cfg = _abi.BatchConfig()
+        self.lib.olgpu_batch_config_defaults(C.byref(cfg))
+        cfg.device = int(device)
+        cfg.precision = _abi.PREC_MIXED if mixed else _abi.PREC_FP64
+        if inner_sweeps:
+            cfg.nu1, cfg.nu2 = int(inner_sweeps[0]), int(inner_sweeps[1])
+        cfg.blocks = int(blocks)
+        b = C.c_void_p()
+        check(self.lib.olgpu_batch_create(arr, len(self.problems), C.byref(cfg), C.byref(b)))
+        self._b = b
+        self.last_reports = None
+
+    def close(self):
+        if getattr(self, "_b", None):
+            self.lib.olgpu_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.problems)
+
+    def solve(self, stop: int = _abi.STOP_REFERENCE, max_cycles: int = 100000, tol: float = 0.0,
+              du_tol: float = 0.0, raise_on_error: bool = True) -> List["_abi.Report"]:
+        rule = _abi.StopRule(stop, max_cycles, tol, du_tol)
+        reps = (_abi.Report * len(self.problems))()
+        st = self.lib.olgpu_batch_solve(self._b, C.byref(rule), reps)
+        self.last_reports = list(reps)
+        if raise_on_error or st not in (_abi.OK, _abi.ERR_NAN, _abi.ERR_DIVERGED):
+            check(st)
+        return list(reps)
+
+    def reset(self):
+        check(self.lib.olgpu_batch_reset(self._b))
+
+    def _member(self, i: int):
+        h = self.lib.olgpu_batch_member(self._b, int(i))
+        if not h:
+            raise IndexError(i)
+        return C.c_void_p(h)
+
+    def boxes(self, i: int):
+        h = self._member(i)
+        out = []
+        for g in range(self.lib.olgpu_num_boxes(h)):
+            bi = _abi.BoxInfo()
+            check(self.lib.olgpu_box(h, g, C.byref(bi)))
+            out.append(bi)
+        return out
+
+    def get_field(self, i: int, box: int, name: str = "u") -> np.ndarray:
+        h = self._member(i)
+        bi = _abi.BoxInfo()
+        check(self.lib.olgpu_box(h, box, C.byref(bi)))
+        out = np.empty((bi.nz, bi.ny, bi.nx), dtype=np.float64)
+        check(self.lib.olgpu_download(h, box, name.encode(), out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def all_u(self, i: int) -> List[np.ndarray]:
+        return [self.get_field(i, g) for g in range(self.lib.olgpu_num_boxes(self._member(i)))]
+
+    def ADM_mass(self, i: int) -> List[float]:
+        out = (C.c_double * _abi.MAX_BH)()
+        check(self.lib.olgpu_adm_mass(self._member(i), out))
+        return [out[j] for j in range(self.problems[i].numbh)]
+
+    @property
+    def unions(self) -> int:
+        return self.lib.olgpu_batch_unions(self._b)
+
+    @property
+    def kernels_per_cycle(self) -> int:
+        return self.lib.olgpu_batch_kernels_per_cycle(self._b)
+
+    @property
+    def last_ms(self) -> float:
+        return self.lib.olgpu_batch_last_ms(self._b)
+
+
 def fma_peak(fp64: bool = True, iters: int = 0) -> float:
     """Measured FMA throughput of the current device in TFLOP/s (FP64 or
     FP32), the instruction roofline of the stencil kernels

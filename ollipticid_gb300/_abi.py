@@ -69,6 +69,11 @@ class ServerResult(C.Structure):
     ]
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("precision", C.c_int), ("nu1", C.c_int), ("nu2", C.c_int),
+                ("blocks", C.c_int)]
+
+
 class BoxFields(C.Structure):
     _fields_ = [
         ("u", C.c_void_p), ("b", C.c_void_p), ("c", C.c_void_p), ("s", C.c_void_p),
@@ -126,6 +131,16 @@ SIGNATURES = {
     "olgpu_server_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                      C.POINTER(C.c_int)]),
     "olgpu_server_destroy": (C.c_int, [C.c_void_p]),
+    "olgpu_batch_config_defaults": (None, [C.POINTER(BatchConfig)]),
+    "olgpu_batch_create": (C.c_int, [C.POINTER(Problem), C.c_int, C.POINTER(BatchConfig), C.POINTER(C.c_void_p)]),
+    "olgpu_batch_solve": (C.c_int, [C.c_void_p, C.POINTER(StopRule), C.POINTER(Report)]),
+    "olgpu_batch_reset": (C.c_int, [C.c_void_p]),
+    "olgpu_batch_member": (C.c_void_p, [C.c_void_p, C.c_int]),
+    "olgpu_batch_size": (C.c_int, [C.c_void_p]),
+    "olgpu_batch_unions": (C.c_int, [C.c_void_p]),
+    "olgpu_batch_kernels_per_cycle": (C.c_int, [C.c_void_p]),
+    "olgpu_batch_last_ms": (C.c_double, [C.c_void_p]),
+    "olgpu_batch_destroy": (C.c_int, [C.c_void_p]),
     "olgpu_last_error": (C.c_char_p, []),
     "olgpu_version": (C.c_char_p, []),
 }

@@ -58,6 +58,7 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
   __shared__ double s_x[3][64], s_ix[3][64];   // node coordinates and their reciprocals
 
   const DevBox B = boxes[box];
+  if (!B.active) return;   // every block of the cluster reads the same box: all leave
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
   const int n01 = n0 * n1;
   const int kz0 = cslab_begin(rank, n2, NCTA), kz1 = cslab_begin(rank + 1, n2, NCTA);

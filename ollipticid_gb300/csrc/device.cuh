@@ -15,7 +15,9 @@ namespace olgpu {
 // cycle's largest change of u is measured against it).
 enum Field { F_U = 0, F_B, F_C, F_D, F_E, F_RHO, F_R, F_W, F_WW, F_V, F_T, F_UP, F_NUM };
 
-constexpr int kMaxBoxesPerLevel = 32;
+// boxes one launch covers: a level's boxes, or those of the same level of
+// every solve of a batch
+constexpr int kMaxBoxesPerLevel = 64;
 constexpr int kMaxInterpPoints = 10;   // Lagrange order 9 (order 8 ghosts)
 
 struct DevBox {
@@ -29,17 +31,24 @@ struct DevBox {
   double idx[3];        // 1/dx
   double idx2[3];       // 1/dx^2
   double dulap;         // diagonal of the Laplacian stencil
+  int solve;            // the box's solve in a batch (0 alone): its norm slots
+                        // are stats[solve]
+  int active;           // 0: the box's solve has stopped; every kernel leaves it as it is
+  int mg_coarse;        // 1: a multigrid coarse level (level < the solve's
+                        // mgrid levels), whose ghost layers the discrete system
+                        // does not fix
+  int pad_;
 };
 
 struct DevFields {
   double *f[F_NUM];
 };
 
-// Boxes of one level handled by one launch; blocks are split between boxes
-// by the prefix sums in blk.
+// Boxes handled by one launch (indices into the box table); blocks are split
+// between them by the prefix sums in blk.
 struct BoxList {
-  int first;
   int count;
+  int box[kMaxBoxesPerLevel];
   int blk[kMaxBoxesPerLevel + 1];
 };
 
@@ -80,6 +89,22 @@ struct XferJob {
   int lin2;
   int lstart[3][2], lnode[3][2], lexact[3][2];
   double lw0[3][2], lw1[3][2];
+};
+
+// Norm slots of a cycle beside the smoothers' (2 a level, pre/post): the
+// cycle's largest change of u on the fixed points, the mixed cycle's largest
+// correction and its finest FP64 defect.
+constexpr int kSlotDu = 125, kSlotCorr = 126, kSlotDefect = 127;
+
+// Device scalars of one solve, read back after each cycle (a batch holds one
+// per solve, indexed by DevBox::solve).  Norms are kept as the bit patterns
+// of non-negative doubles (atomicMax).
+struct Stats {
+  unsigned long long slots[128];    // smoother norms, 2 per level (pre/post), then kSlot*
+  double coarse_norm;
+  int coarse_iters;
+  int nan_flag;
+  double adm_u[16];
 };
 
 struct PunctureParams {

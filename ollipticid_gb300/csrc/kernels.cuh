@@ -21,6 +21,7 @@
 
 #include "device.cuh"
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -33,13 +34,18 @@ __device__ __forceinline__ long long pidx(const DevBox &B, int i, int j, int k)
   return ((long long)k * B.n[1] + j) * B.n[0] + i;
 }
 
-// Finds the box of this block inside a BoxList launch.
+// Finds the box of this block inside a BoxList launch (the last entry whose
+// first block is <= blockIdx.x).
 __device__ __forceinline__ int list_box(const BoxList &L, long long &local_block)
 {
-  int b = 0;
-  while (b + 1 < L.count && (long long)blockIdx.x >= L.blk[b + 1]) b++;
-  local_block = (long long)blockIdx.x - L.blk[b];
-  return L.first + b;
+  int lo = 0, hi = L.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((long long)blockIdx.x >= L.blk[mid]) lo = mid;
+    else hi = mid - 1;
+  }
+  local_block = (long long)blockIdx.x - L.blk[lo];
+  return L.box[lo];
 }
 
 // ----------------------------------------------------------------------------
@@ -295,12 +301,14 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long *s
 // Largest change of u over one cycle, max |u - up| over the points the
 // discrete system fixes (pinned[p] != 0: every point of the solution levels,
 // the INSIDE points of the multigrid coarse levels), into *slot as a bit
-// pattern.  A NaN difference wins the maximum.  n = all points of the arena.
+// pattern.  A NaN difference wins the maximum.  n = the solve's points (its
+// part of the arena); gate = one of its boxes.
 __global__ void __launch_bounds__(256) k_du_max(long long n, const double *__restrict__ u,
                                                 const double *__restrict__ up,
                                                 const unsigned char *__restrict__ pinned,
-                                                unsigned long long *slot)
+                                                unsigned long long *slot, const DevBox *__restrict__ gate)
 {
+  if (!gate->active) return;   // the solve has stopped (batch); the whole grid leaves
   double m = 0.0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += stride)
@@ -354,15 +362,19 @@ __device__ __forceinline__ double step_inverse(double dop)
 template <int ORD>
 __host__ __device__ constexpr int num_colors() { return ORD / 2 + 1; }
 
+// The pass's residual maximum goes to stats[B.solve].slots[2 * B.level +
+// post] (the level's pre- or post-smoothing norm), a NaN to its nan_flag.
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *__restrict__ boxes,
-                                                      DevFields F, int color,
-                                                      unsigned long long *norm_slot, int *nan_flag)
+                                                      DevFields F, int color, Stats *stats, int post)
 {
   constexpr int NC = num_colors<ORD>();
   griddep_wait();                 // launched as a programmatic dependent
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;          // the whole block leaves (one box a block)
+  unsigned long long *norm_slot = &stats[B.solve].slots[2 * B.level + post];
+  int *nan_flag = &stats[B.solve].nan_flag;
   const int b = B.buf;
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const int H = (m0 + NC - 1) / NC;
@@ -400,6 +412,7 @@ __global__ void __launch_bounds__(256) k_apply_op(BoxList L, const DevBox *__res
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const int b = B.buf;
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const long long t = lb * blockDim.x + threadIdx.x;
@@ -426,6 +439,7 @@ __global__ void __launch_bounds__(256) k_robin_faces(BoxList L, const DevBox *__
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const int b = B.buf;
   long long t = lb * blockDim.x + threadIdx.x;
   for (int f = 0; f < 6; f++) {
@@ -455,7 +469,8 @@ __global__ void __launch_bounds__(64) k_robin_edges_corners(BoxList L, const Dev
 {
   if (part == 0) {
     // one block per (box, edge): 12 edges a box, (a, c) the edge's ghost axes
-    const DevBox B = boxes[L.first + blockIdx.x / 12];
+    const DevBox B = boxes[L.box[blockIdx.x / 12]];
+    if (!B.active) return;
     const int e12 = blockIdx.x % 12, pi = e12 >> 2, e = e12 & 3;
     const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
     const int b = B.buf, m = B.n[fa] - 2 * b;
@@ -473,7 +488,8 @@ __global__ void __launch_bounds__(64) k_robin_edges_corners(BoxList L, const Dev
     return;
   }
   // corners, after every edge (a launch of their own), one block per box
-  const DevBox B = boxes[L.first + blockIdx.x];
+  const DevBox B = boxes[L.box[blockIdx.x]];
+  if (!B.active) return;
   const int b = B.buf;
   if (threadIdx.x < 8) {
     const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
@@ -489,6 +505,103 @@ __global__ void __launch_bounds__(64) k_robin_edges_corners(BoxList L, const Dev
 }
 
 // ----------------------------------------------------------------------------
+// Robin boundary in one launch: one thread-block cluster per box walks every
+// face column (layers inner -> outer), then -- after a cluster barrier --
+// every edge, then -- after another -- the corners, the reference's order
+// (faces, edges, corners; src/boundary.cc:447-907, 1118-1535).  It does the
+// same point updates in the same dependency order as the face launch
+// followed by the edge and corner launches above, so the results are the
+// same bit for bit; the barriers replace two launch boundaries.
+// pt(mask, i, j, k) updates one ghost point.
+// ----------------------------------------------------------------------------
+constexpr int kRobinCluster = 8;
+
+template <class PointFn>
+__device__ __forceinline__ void robin_walk(const DevBox &B, unsigned rank, unsigned ncta, PointFn pt)
+{
+  namespace cg = cooperative_groups;
+  const int b = B.buf;
+  const long long tid = (long long)rank * blockDim.x + threadIdx.x, nth = (long long)ncta * blockDim.x;
+  // faces: the normal columns of the six faces, face by face
+  long long total = 0;
+  for (int f = 0; f < 6; f++) {
+    const int a = f >> 1;
+    total += (long long)(B.n[(a + 1) % 3] - 2 * b) * (B.n[(a + 2) % 3] - 2 * b);
+  }
+  for (long long t0 = tid; t0 < total; t0 += nth) {
+    long long t = t0;
+    for (int f = 0; f < 6; f++) {
+      const int a = f >> 1, hi = f & 1;
+      const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+      const int m1 = B.n[a1] - 2 * b, m2 = B.n[a2] - 2 * b;
+      const long long cols = (long long)m1 * m2;
+      if (t < cols) {
+        int ijk[3];
+        ijk[a1] = b + (int)(t % m1);
+        ijk[a2] = b + (int)(t / m1);
+        for (int l = 0; l < b; l++) {
+          ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
+          pt(1 << a, ijk[0], ijk[1], ijk[2]);
+        }
+        break;
+      }
+      t -= cols;
+    }
+  }
+  cg::this_cluster().sync();   // every face column is done (global writes visible in the cluster)
+  // edges: 12 a box; edge e12 runs along axis fa with ghost axes a and c
+  long long etotal = 0;
+  for (int e12 = 0; e12 < 12; e12++) {
+    const int pi = e12 >> 2, a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2;
+    etotal += B.n[3 - a - c] - 2 * b;
+  }
+  for (long long t0 = tid; t0 < etotal; t0 += nth) {
+    long long t = t0;
+    for (int e12 = 0; e12 < 12; e12++) {
+      const int pi = e12 >> 2, e = e12 & 3;
+      const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
+      const int m = B.n[fa] - 2 * b;
+      if (t < m) {
+        const int ha = e >> 1, hc = e & 1;
+        int ijk[3];
+        ijk[fa] = b + (int)t;
+        for (int ta = 0; ta < b; ta++)
+          for (int tc = 0; tc < b; tc++) {
+            ijk[a] = ha ? B.n[a] - b + ta : b - 1 - ta;
+            ijk[c] = hc ? B.n[c] - b + tc : b - 1 - tc;
+            pt((1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+          }
+        break;
+      }
+      t -= m;
+    }
+  }
+  cg::this_cluster().sync();   // every edge is done
+  if (rank == 0 && threadIdx.x < 8) {
+    const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
+    for (int tk = 0; tk < b; tk++)
+      for (int tj = 0; tj < b; tj++)
+        for (int ti = 0; ti < b; ti++)
+          pt(7, hx ? B.n[0] - b + ti : b - 1 - ti, hy ? B.n[1] - b + tj : b - 1 - tj,
+             hz ? B.n[2] - b + tk : b - 1 - tk);
+  }
+}
+
+// FP64 Robin update (mode 0) / operator (mode 1), Dirichlet (modes 2, 3) of
+// every box of a level: kRobinCluster blocks a box, launched as clusters.
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin_cluster(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                       const double *__restrict__ crd, int mode)
+{
+  namespace cg = cooperative_groups;
+  const unsigned ncta = cg::this_cluster().num_blocks();
+  const DevBox B = boxes[L.box[blockIdx.x / ncta]];
+  if (!B.active) return;   // every block of the cluster reads the same box: all leave
+  robin_walk(B, cg::this_cluster().block_rank(), ncta,
+             [&](int mask, int i, int j, int k) { robin_point<ORD>(B, F, crd, mode, mask, i, j, k); });
+}
+
+// ----------------------------------------------------------------------------
 // element-wise field updates over ALL points of a level
 // ----------------------------------------------------------------------------
 enum EwOp { EW_W_EQ_S_MINUS_R = 0, EW_S_EQ_W_PLUS_R, EW_W_PLUS_EQ_R, EW_WW_EQ_U, EW_V_EQ_U_MINUS_WW,
@@ -499,6 +612,7 @@ __global__ void __launch_bounds__(256) k_elementwise(BoxList L, const DevBox *__
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -558,6 +672,7 @@ __global__ void __launch_bounds__(256) k_full_weight(BoxList L, const DevBox *__
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -652,6 +767,7 @@ __global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, 
     jb = lo;
   }
   const XferJob &J = jobs[jb];
+  if (!boxes[J.tbox].active) return;   // the target's solve has stopped (whole block: one job)
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
@@ -724,23 +840,25 @@ __global__ void __launch_bounds__(256) k_xfer(const XferJob *__restrict__ jobs, 
 constexpr int kRowWarps = 16;    // rows in flight per block
 constexpr int kRowBuf = 320;     // shared partial sums per row (else direct sums)
 
+// The body of k_xfer_rows for block rb of its plan (32 * kRowWarps threads).
 template <class V, class Fields, int P>
-__global__ void __launch_bounds__(32 * kRowWarps) k_xfer_rows(const XferJob *__restrict__ jobs, int njobs,
-                                                              const DevBox *__restrict__ boxes, Fields F,
-                                                              const AxisEntry *__restrict__ tab)
+__device__ __forceinline__ void xfer_rows_body(long long rb, const XferJob *__restrict__ jobs, int njobs,
+                                               const DevBox *__restrict__ boxes, Fields F,
+                                               const AxisEntry *__restrict__ tab)
 {
   __shared__ V sbuf[kRowWarps][kRowBuf];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int lo = 0, hi = njobs - 1;   // last job with rblk0 <= blockIdx.x
+  int lo = 0, hi = njobs - 1;   // last job with rblk0 <= rb
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].rblk0 <= (long long)blockIdx.x) lo = mid;
+    if (jobs[mid].rblk0 <= rb) lo = mid;
     else hi = mid - 1;
   }
   const XferJob &J = jobs[lo];
+  if (!boxes[J.tbox].active) return;   // the target's solve has stopped (whole block: one job)
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1];
   const int ra = J.row_axis;
-  const long long row = ((long long)blockIdx.x - J.rblk0) * kRowWarps + warp;
+  const long long row = (rb - J.rblk0) * kRowWarps + warp;
   const int across = ra == 0 ? e1 : e0;   // rows per plane
   if (row >= (long long)across * (J.r1[2] - J.r0[2])) return;   // the whole warp leaves together
   const int k = J.r0[2] + (int)row / across;
@@ -845,6 +963,14 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_xfer_rows(const XferJob *__r
   }
 }
 
+template <class V, class Fields, int P>
+__global__ void __launch_bounds__(32 * kRowWarps) k_xfer_rows(const XferJob *__restrict__ jobs, int njobs,
+                                                              const DevBox *__restrict__ boxes, Fields F,
+                                                              const AxisEntry *__restrict__ tab)
+{
+  xfer_rows_body<V, Fields, P>(blockIdx.x, jobs, njobs, boxes, F, tab);
+}
+
 // Window width P of a plan's kernel: 0 without Lagrange jobs, the Lagrange
 // order + 1 when it has an instantiation, else -1.
 inline int xfer_width(const XferJob *jobs, size_t n)
@@ -886,6 +1012,7 @@ __global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ job
     else hi = mid - 1;
   }
   const XferJob &J = jobs[lo];
+  if (!boxes[J.tbox].active) return;   // the target's solve has stopped (whole block: one job)
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
@@ -922,21 +1049,24 @@ __global__ void __launch_bounds__(256) k_xfer_fw(const XferJob *__restrict__ job
 // The same terms in the same order as V = E - WW, V_fine = P V,
 // E += V_fine; targets the plan zeroes get a zero correction and are left
 // as they are.
+// The body of k_prolong_correct for virtual block vb of its plan: thread vtid
+// of a block of vdim threads (the plan's pair blocks are 256 threads).
 template <class V, class Fields>
-__global__ void __launch_bounds__(256) k_prolong_correct(const XferJob *__restrict__ jobs, int njobs,
-                                                         const DevBox *__restrict__ boxes, Fields F,
-                                                         const AxisEntry *__restrict__ tab, int fe, int fww)
+__device__ __forceinline__ void prolong_correct_body(long long vb, int vtid, int vdim, const XferJob *__restrict__ jobs,
+                                                     int njobs, const DevBox *__restrict__ boxes, Fields F,
+                                                     const AxisEntry *__restrict__ tab, int fe, int fww)
 {
   // two x-neighbour targets per thread: the job search, the index split, the
   // y and z axis entries and the boxes are shared by both
   int lo = 0, hi = njobs - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].pblk0 <= (long long)blockIdx.x) lo = mid;
+    if (jobs[mid].pblk0 <= vb) lo = mid;
     else hi = mid - 1;
   }
   const XferJob &J = jobs[lo];
-  const long long t = ((long long)blockIdx.x - J.pblk0) * blockDim.x + threadIdx.x;
+  if (!boxes[J.tbox].active) return;   // the target's solve has stopped (whole block: one job)
+  const long long t = (vb - J.pblk0) * vdim + vtid;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   const int h0 = (e0 + 1) >> 1;
   if (t >= (long long)h0 * e1 * e2) return;
@@ -1010,6 +1140,37 @@ __global__ void __launch_bounds__(256) k_prolong_correct(const XferJob *__restri
   }
 }
 
+template <class V, class Fields>
+__global__ void __launch_bounds__(256) k_prolong_correct(const XferJob *__restrict__ jobs, int njobs,
+                                                         const DevBox *__restrict__ boxes, Fields F,
+                                                         const AxisEntry *__restrict__ tab, int fe, int fww)
+{
+  prolong_correct_body<V, Fields>(blockIdx.x, threadIdx.x, blockDim.x, jobs, njobs, boxes, F, tab, fe, fww);
+}
+
+// A refinement level's coarse-to-fine step in one launch: the correction of
+// its INSIDE points (prolong_correct_body, two 256-thread pair blocks per
+// block) and the ghost fill of its BOUNDARY points from the corrected coarse
+// level (xfer_rows_body, the order+1 Lagrange rows).  The two write disjoint
+// points and read only the coarse level, so running them side by side gives
+// the bits of the two launches in a row.
+template <class V, class Fields, int P>
+__global__ void __launch_bounds__(32 * kRowWarps) k_prolong_ghost(const XferJob *__restrict__ pjobs, int npjobs,
+                                                                  long long ppairs, const XferJob *__restrict__ gjobs,
+                                                                  int ngjobs, const DevBox *__restrict__ boxes,
+                                                                  Fields F, const AxisEntry *__restrict__ tab, int fe,
+                                                                  int fww)
+{
+  static_assert(32 * kRowWarps == 512, "two pair blocks of 256 threads per block");
+  const long long pblocks = (ppairs + 1) >> 1;
+  if ((long long)blockIdx.x < pblocks) {
+    const long long vb = 2 * (long long)blockIdx.x + (threadIdx.x >> 8);
+    if (vb < ppairs) prolong_correct_body<V, Fields>(vb, threadIdx.x & 255, 256, pjobs, npjobs, boxes, F, tab, fe, fww);
+    return;
+  }
+  xfer_rows_body<V, Fields, P>((long long)blockIdx.x - pblocks, gjobs, ngjobs, boxes, F, tab);
+}
+
 // Set_In of a refinement level with the coarse FP64 operator folded in:
 // RHO = W + OP(u) at every target of the (strided, same-box) Set_In plan, OP
 // evaluated as k_apply_op does on INSIDE points and 0 on the ghosts (R is 0
@@ -1025,6 +1186,7 @@ __global__ void __launch_bounds__(256) k_set_in_op(const XferJob *__restrict__ j
     else hi = mid - 1;
   }
   const XferJob &J = jobs[lo];
+  if (!boxes[J.tbox].active) return;   // the target's solve has stopped (whole block: one job)
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
@@ -1084,6 +1246,7 @@ __global__ void __launch_bounds__(1024) k_coarse_solve(const DevBox *__restrict_
   __shared__ double s_norm;
   __shared__ int s_nan;
   const DevBox B = boxes[box];
+  if (!B.active) return;   // one block
   const long long np = (long long)B.n[0] * B.n[1] * B.n[2];
   double *gu = F.f[F_U] + B.off;
   const double *gb = F.f[F_B] + B.off, *gc = F.f[F_C] + B.off, *gs = F.f[F_RHO] + B.off;
@@ -1279,6 +1442,7 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -1350,6 +1514,7 @@ __global__ void __launch_bounds__(256) k_test_init(BoxList L, const DevBox *__re
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -1453,6 +1618,7 @@ __global__ void __launch_bounds__(256) k_approx_id(BoxList L, const DevBox *__re
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -1482,6 +1648,7 @@ __global__ void k_adm(const AdmJob *__restrict__ jobs, int n, const DevBox *__re
   if (q >= n) return;
   const AdmJob J = jobs[q];
   const DevBox S = boxes[J.box];
+  if (!S.active) return;
   const double *u = F.f[F_U] + S.off;
   if (J.exact) {
     out[q] = u[pidx(S, J.node[0], J.node[1], J.node[2])];

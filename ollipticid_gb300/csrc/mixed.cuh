@@ -92,13 +92,16 @@ __device__ __forceinline__ void corr_op(float lapv, float dl, float e, float A, 
 // FP64 defect S - OP(u) on INSIDE points into the FP32 source; the other
 // points get S (the operator value there is written by the Robin kernels in
 // mode 2 on boxes with a physical boundary, and stays 0 on refinement ghosts,
-// as the reference's r field does).  Optionally the L-infinity norm.
+// as the reference's r field does).  Optionally (slot >= 0) the L-infinity
+// norm, into stats[B.solve].slots[slot].
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                   DevFields32 G, unsigned long long *norm_slot)
+                                                   DevFields32 G, Stats *stats, int slot)
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;   // the whole block (one box a block)
+  unsigned long long *norm_slot = slot >= 0 ? &stats[B.solve].slots[slot] : nullptr;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   double rabs = 0.0;
@@ -134,6 +137,7 @@ __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__rest
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -186,6 +190,7 @@ __global__ void __launch_bounds__(256) k_mx_robin_defect(BoxList L, const DevBox
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const int b = B.buf;
   // every ghost point of the box: classify by how many axes are in the band
   const long long t = lb * blockDim.x + threadIdx.x;
@@ -202,13 +207,16 @@ __global__ void __launch_bounds__(256) k_mx_robin_defect(BoxList L, const DevBox
 }
 
 // u += e over ALL points (the FP64 outer update), and max |e| over the points
-// the discrete system fixes (every point of levels >= mg, the interior of the
-// coarser multigrid levels, whose ghost values are not fixed).
+// the discrete system fixes (every point of the solution levels, the interior
+// of the multigrid coarse levels, whose ghost values are not fixed), into
+// stats[B.solve].slots[kSlotCorr].
 __global__ void __launch_bounds__(256) k_mx_update(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                   DevFields32 G, int mg, unsigned long long *norm_slot)
+                                                   DevFields32 G, Stats *stats)
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;   // the whole block (one box a block)
+  unsigned long long *norm_slot = &stats[B.solve].slots[kSlotCorr];
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   double eabs = 0.0;
@@ -216,7 +224,7 @@ __global__ void __launch_bounds__(256) k_mx_update(BoxList L, const DevBox *__re
     const long long p = B.off + t;
     const double e = (double)G.f[G_E][p];
     F.f[F_U][p] = F.f[F_U][p] + e;
-    bool pinned = B.level >= mg;
+    bool pinned = !B.mg_coarse;
     if (!pinned) {
       const int b = B.buf;
       const int i = ((int)t % B.n[0]);
@@ -244,12 +252,14 @@ __device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, l
 // One multicolour pass on e (colour (i+j+k) mod (order/2+1)).
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
-                                                  int color, int *nan_flag)
+                                                  int color, Stats *stats)
 {
   constexpr int NC = num_colors<ORD>();
   griddep_wait();                 // launched as a programmatic dependent
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
+  int *nan_flag = &stats[B.solve].nan_flag;
   const int b = B.buf;
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const int H = (m0 + NC - 1) / NC;
@@ -279,6 +289,7 @@ __global__ void __launch_bounds__(256) k_apply_op32(BoxList L, const DevBox *__r
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const int b = B.buf;
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const long long t = lb * blockDim.x + threadIdx.x;
@@ -362,6 +373,7 @@ __global__ void __launch_bounds__(256) k_robin32_faces(BoxList L, const DevBox *
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const int b = B.buf;
   long long t = lb * blockDim.x + threadIdx.x;
   for (int f = 0; f < 6; f++) {
@@ -389,7 +401,8 @@ __global__ void __launch_bounds__(64) k_robin32_edges_corners(BoxList L, const D
 {
   if (part == 0) {
     // one block per (box, edge): 12 edges a box, (a, c) the edge's ghost axes
-    const DevBox B = boxes[L.first + blockIdx.x / 12];
+    const DevBox B = boxes[L.box[blockIdx.x / 12]];
+    if (!B.active) return;
     const int e12 = blockIdx.x % 12, pi = e12 >> 2, e = e12 & 3;
     const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
     const int b = B.buf, m = B.n[fa] - 2 * b;
@@ -407,7 +420,8 @@ __global__ void __launch_bounds__(64) k_robin32_edges_corners(BoxList L, const D
     return;
   }
   // corners, after every edge (a launch of their own), one block per box
-  const DevBox B = boxes[L.first + blockIdx.x];
+  const DevBox B = boxes[L.box[blockIdx.x]];
+  if (!B.active) return;
   const int b = B.buf;
   if (threadIdx.x < 8) {
     const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
@@ -422,6 +436,21 @@ __global__ void __launch_bounds__(64) k_robin32_edges_corners(BoxList L, const D
   }
 }
 
+// FP32 Robin update / operator of the correction, every box of a level in
+// one launch of kRobinCluster-block clusters (robin_walk: faces, edges,
+// corners, in the order of the separate launches above).
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin32_cluster(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
+                                                         const double *__restrict__ crd, int mode)
+{
+  namespace cg = cooperative_groups;
+  const unsigned ncta = cg::this_cluster().num_blocks();
+  const DevBox B = boxes[L.box[blockIdx.x / ncta]];
+  if (!B.active) return;   // every block of the cluster reads the same box: all leave
+  robin_walk(B, cg::this_cluster().block_rank(), ncta,
+             [&](int mask, int i, int j, int k) { robin32_point<ORD>(B, G, crd, mode, mask, i, j, k); });
+}
+
 enum Ew32Op { EW32_W_EQ_S_MINUS_R = 0, EW32_S_EQ_W_PLUS_R, EW32_W_PLUS_EQ_R, EW32_WW_EQ_E, EW32_V_EQ_E_MINUS_WW,
               EW32_E_PLUS_EQ_V, EW32_S_EQ_W_PLUS_R_WW_EQ_E, EW32_W_PLUS_EQ_R_WW_EQ_E };
 
@@ -430,6 +459,7 @@ __global__ void __launch_bounds__(256) k_elementwise32(BoxList L, const DevBox *
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -458,6 +488,7 @@ __global__ void __launch_bounds__(256) k_full_weight32(BoxList L, const DevBox *
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
   if (t >= n) return;
@@ -492,6 +523,7 @@ __global__ void __launch_bounds__(256) k_set_in_op32(const XferJob *__restrict__
     else hi = mid - 1;
   }
   const XferJob &J = jobs[lo];
+  if (!boxes[J.tbox].active) return;   // the target's solve has stopped (whole block: one job)
   const long long t = ((long long)blockIdx.x - J.blk0) * blockDim.x + threadIdx.x;
   const int e0 = J.r1[0] - J.r0[0], e1 = J.r1[1] - J.r0[1], e2 = J.r1[2] - J.r0[2];
   if (t >= (long long)e0 * e1 * e2) return;
@@ -532,6 +564,7 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
   __shared__ int s_nan;
   __shared__ float s_x[3][64], s_ix[3][64];   // node coordinates and their reciprocals
   const DevBox B = boxes[box];
+  if (!B.active) return;   // one block
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
   const int np = n0 * n1 * n2;
   float *ge = G.f[G_E] + B.off;
@@ -718,8 +751,9 @@ constexpr int kAndPart = kAndMax * (kAndMax + 1) / 2 + kAndMax;
 __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__restrict__ f, float *fprev,
                                                     float *DF, const unsigned char *__restrict__ pinned,
                                                     const AndersonState *st, double *part,
-                                                    unsigned long long *fmax_slot)
+                                                    unsigned long long *fmax_slot, const DevBox *__restrict__ gate)
 {
+  if (!gate->active) return;   // the solve has stopped (batch): the whole grid leaves
   const int k = st->k, m = st->m;
   const int nc = k < m ? k : m;
   const int newest = (k + m - 1) % m;   // ring slot of dF_k (k >= 1)
@@ -788,8 +822,9 @@ __global__ void __launch_bounds__(256) k_and_reduce(long long n, const float *__
 constexpr int kAndSolveWarps = kAndPart < 32 ? kAndPart : 32;
 
 __global__ void __launch_bounds__(32 * kAndSolveWarps) k_and_solve(AndersonState *st, const double *__restrict__ part,
-                                                                   int nblocks)
+                                                                   int nblocks, const DevBox *__restrict__ gate)
 {
+  if (!gate->active) return;
   __shared__ double tot[kAndPart];
   const int lane = threadIdx.x & 31;
   for (int v = threadIdx.x >> 5; v < kAndPart; v += kAndSolveWarps) {
@@ -845,8 +880,10 @@ __global__ void __launch_bounds__(32 * kAndSolveWarps) k_and_solve(AndersonState
 
 // u_{k+1} = u_k + f_k - sum gamma_i (dU_i + dF_i); stores dU_{k+1}.
 __global__ void __launch_bounds__(256) k_and_update(long long n, double *u, const float *__restrict__ f, float *DU,
-                                                    const float *__restrict__ DF, const AndersonState *st)
+                                                    const float *__restrict__ DF, const AndersonState *st,
+                                                    const DevBox *__restrict__ gate)
 {
+  if (!gate->active) return;
   const int k = st->k_used, m = st->m;
   const int nc = k < m ? k : m;
   const int newest = (k + m - 1) % m;

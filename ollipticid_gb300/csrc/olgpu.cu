@@ -23,7 +23,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -67,19 +69,6 @@ struct Transfer {
   XferJob *d_jobs = nullptr;
 };
 
-// Norm slots of a cycle beside the smoothers' (2 a level, pre/post): the
-// cycle's largest change of u on the fixed points, the mixed cycle's largest
-// correction and its finest FP64 defect.
-constexpr int kSlotDu = 125, kSlotCorr = 126, kSlotDefect = 127;
-
-struct Stats {                      // device scalars read back after a cycle
-  unsigned long long slots[128];    // smoother norms, 2 per level (pre/post), then kSlot*
-  double coarse_norm;
-  int coarse_iters;
-  int nan_flag;
-  double adm_u[OLGPU_MAX_BH];
-};
-
 }  // namespace
 
 struct olgpu_hierarchy {
@@ -103,6 +92,7 @@ struct olgpu_hierarchy {
   AdmJob *d_adm = nullptr;
   Stats *d_stats = nullptr;
   Stats *h_stats = nullptr;         // pinned
+  Stats *d_stats0 = nullptr;        // what DevBox::solve indexes (d_stats alone)
   cudaStream_t stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -161,22 +151,63 @@ struct olgpu_hierarchy {
   // smoother launches as programmatic dependents (overlap launch with the
   // previous kernel's tail); off with OLGPU_NO_PDL
   bool pdl = !std::getenv("OLGPU_NO_PDL");
+  // the Robin walk as separate face, edge and corner launches (off: one
+  // launch of a cluster per box); the two give the same bits
+  bool robin_split = std::getenv("OLGPU_ROBIN_SPLIT") != nullptr;
+  // The solves this hierarchy steps: alone, one (itself); a union of solves
+  // (olgpu_batch) steps every member's boxes in shared launches, their levels
+  // aligned from the top (a member's level k is the union's level k + off).
+  struct Member {
+    olgpu_hierarchy *h = nullptr;   // the member's own hierarchy (plans, host state)
+    int off = 0;                    // the union level of its level 0
+    int coarse_box = 0;             // its level-0 box in this box table
+    int box_base = 0;               // its first box in this box table
+    long long pt_base = 0;          // its first point in this arena
+    Stats *d_stats = nullptr;       // its stats (this table's stats[solve])
+    AdmJob *d_adm = nullptr;        // its ADM jobs, box indices of this table
+    int nadm = 0;
+    int coarse_ncta = 0;            // its coarsest solve: cluster blocks and shared memory
+    size_t coarse_smem = 0;
+  };
+  std::vector<Member> members;
+  // union: per level the boxes of the members for which it is not the
+  // coarsest level (the fine side of a FASN step); alone, every box
+  std::vector<int> fine_count;
+  bool is_union = false;
+  bool mixed_ready = false;         // FP32 fields, plans and Anderson history are set up
+  bool owns_arena = true, owns_arena32 = true, owns_stats = true;
 };
 
 namespace {
 
-BoxList level_list(const olgpu_hierarchy *h, int level, long long (*blocks_of)(const DevBox &))
+// A launch's box list: the given boxes (indices into the hierarchy's box
+// table) with their block prefix sums.
+BoxList box_list(const std::vector<DevBox> &hboxes, const int *boxes, int count,
+                 long long (*blocks_of)(const DevBox &))
 {
   BoxList L{};
-  L.first = h->G.first_box[level];
-  L.count = h->G.boxes_in_level[level];
+  L.count = count;
   long long acc = 0;
-  for (int b = 0; b < L.count; b++) {
+  for (int b = 0; b < count; b++) {
+    L.box[b] = boxes[b];
     L.blk[b] = (int)acc;
-    acc += blocks_of(h->hboxes[L.first + b]);
+    acc += blocks_of(hboxes[boxes[b]]);
   }
-  L.blk[L.count] = (int)acc;
+  L.blk[count] = (int)acc;
   return L;
+}
+
+// The boxes of a level a launch covers: alone, all of them; in a union of
+// solves, the fine side of a FASN step -- the members for which the level is
+// not their coarsest, which come first in the level's boxes -- or, with
+// whole, every box of the level (the coarse side of a step, per-level
+// passes).
+BoxList level_list(const olgpu_hierarchy *h, int level, long long (*blocks_of)(const DevBox &), bool whole = false)
+{
+  int boxes[kMaxBoxesPerLevel];
+  const int n = whole || h->fine_count.empty() ? h->G.boxes_in_level[level] : h->fine_count[level];
+  for (int b = 0; b < n; b++) boxes[b] = h->G.first_box[level] + b;
+  return box_list(h->hboxes, boxes, n, blocks_of);
 }
 
 long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
@@ -507,6 +538,25 @@ void launch_pdl(olgpu_hierarchy *h, void (*kern)(KArgs...), unsigned grid, unsig
   cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
+// Launches a kernel as clusters of `ncta` blocks on the hierarchy's stream.
+template <class... KArgs, class... Args>
+void launch_clusters(olgpu_hierarchy *h, void (*kern)(KArgs...), unsigned grid, unsigned block, unsigned ncta,
+                     Args... args)
+{
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(grid, 1, 1);
+  cfg.blockDim = dim3(block, 1, 1);
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = ncta;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 template <int ORD, int EQ>
 void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
 {
@@ -515,32 +565,38 @@ void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
       launch_pdl(h, k_smooth_color<ORD, EQ>, (unsigned)nb, (unsigned)kSmoothThreads, L,
-                 (const DevBox *)h->d_boxes, h->F, color, &h->d_stats->slots[slot], &h->d_stats->nan_flag);
+                 (const DevBox *)h->d_boxes, h->F, color, h->d_stats0, slot - 2 * level);
       h->launches++;
     }
 }
 
 template <int ORD, int EQ>
-void launch_apply_op(olgpu_hierarchy *h, int level)
+void launch_apply_op(olgpu_hierarchy *h, int level, bool whole = false)
 {
-  const BoxList L = level_list(h, level, blocks_inside);
+  const BoxList L = level_list(h, level, blocks_inside, whole);
   k_apply_op<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F);
   h->launches++;
 }
 
 template <int ORD>
-void launch_robin(olgpu_hierarchy *h, int level, int mode)
+void launch_robin(olgpu_hierarchy *h, int level, int mode, bool whole = false)
 {
-  const BoxList L = level_list(h, level, blocks_faces);
+  const BoxList L = level_list(h, level, blocks_faces, whole);
+  if (!h->robin_split) {   // faces, edges and corners in one launch, a cluster per box
+    launch_clusters(h, k_robin_cluster<ORD>, (unsigned)(L.count * kRobinCluster), kThreads, kRobinCluster, L,
+                    (const DevBox *)h->d_boxes, h->F, (const double *)h->d_coords, mode);
+    h->launches++;
+    return;
+  }
   k_robin_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
   k_robin_edges_corners<ORD><<<12 * L.count, 64, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode, 0);
   k_robin_edges_corners<ORD><<<L.count, 32, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode, 1);
   h->launches += 3;
 }
 
-void launch_ew(olgpu_hierarchy *h, int level, int op)
+void launch_ew(olgpu_hierarchy *h, int level, int op, bool whole = false)
 {
-  const BoxList L = level_list(h, level, blocks_all);
+  const BoxList L = level_list(h, level, blocks_all, whole);
   k_elementwise<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, op);
   h->launches++;
 }
@@ -595,31 +651,31 @@ void dispatch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
 }
 
 template <int EQ>
-void dispatch_apply_op(olgpu_hierarchy *h, int level)
+void dispatch_apply_op(olgpu_hierarchy *h, int level, bool whole = false)
 {
   switch (level_order(h, level)) {
-  case 2: launch_apply_op<2, EQ>(h, level); break;
-  case 4: launch_apply_op<4, EQ>(h, level); break;
-  case 6: launch_apply_op<6, EQ>(h, level); break;
-  default: launch_apply_op<8, EQ>(h, level); break;
+  case 2: launch_apply_op<2, EQ>(h, level, whole); break;
+  case 4: launch_apply_op<4, EQ>(h, level, whole); break;
+  case 6: launch_apply_op<6, EQ>(h, level, whole); break;
+  default: launch_apply_op<8, EQ>(h, level, whole); break;
   }
 }
 
-void dispatch_robin(olgpu_hierarchy *h, int level, int mode)
+void dispatch_robin(olgpu_hierarchy *h, int level, int mode, bool whole = false)
 {
   // the Dirichlet condition runs through the same boundary walk: modes 2, 3
   if (h->P.boundary == OLGPU_BC_DIRICHLET) mode += 2;
-  if (level_order(h, level) == 2) launch_robin<2>(h, level, mode);
-  else launch_robin<4>(h, level, mode);   // orders 4, 6, 8 share dx4 (src/ffunction.cc:197-282)
+  if (level_order(h, level) == 2) launch_robin<2>(h, level, mode, whole);
+  else launch_robin<4>(h, level, mode, whole);   // orders 4, 6, 8 share dx4 (src/ffunction.cc:197-282)
 }
 
 template <int EQ, int NCTA>
-cudaError_t launch_coarse_cluster_n(olgpu_hierarchy *h)
+cudaError_t launch_coarse_cluster_n(olgpu_hierarchy *h, const olgpu_hierarchy::Member &M)
 {
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(NCTA, 1, 1);
   cfg.blockDim = dim3(256, 1, 1);
-  cfg.dynamicSmemBytes = h->coarse_cluster_smem;
+  cfg.dynamicSmemBytes = M.coarse_smem;
   cfg.stream = h->stream;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -628,17 +684,17 @@ cudaError_t launch_coarse_cluster_n(olgpu_hierarchy *h)
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_coarse_cluster<EQ, NCTA>, (const DevBox *)h->d_boxes, h->G.first_box[0], h->F,
+  return cudaLaunchKernelEx(&cfg, k_coarse_cluster<EQ, NCTA>, (const DevBox *)h->d_boxes, M.coarse_box, h->F,
                             (const double *)h->d_coords, h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
-                            h->coarse_rtol, &h->d_stats->coarse_norm, &h->d_stats->coarse_iters,
-                            &h->d_stats->nan_flag, h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
+                            h->coarse_rtol, &M.d_stats->coarse_norm, &M.d_stats->coarse_iters,
+                            &M.d_stats->nan_flag, h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
 }
 
 template <int EQ>
-void launch_coarse_cluster(olgpu_hierarchy *h)
+void launch_coarse_cluster(olgpu_hierarchy *h, const olgpu_hierarchy::Member &M)
 {
-  if (h->coarse_ncta == 16) launch_coarse_cluster_n<EQ, 16>(h);
-  else launch_coarse_cluster_n<EQ, 8>(h);
+  if (M.coarse_ncta == 16) launch_coarse_cluster_n<EQ, 16>(h, M);
+  else launch_coarse_cluster_n<EQ, 8>(h, M);
 }
 
 // Largest supported cluster for the coarse solve: 16 blocks (non-portable
@@ -720,8 +776,8 @@ void emit_fasn_down(olgpu_hierarchy *h, int k)
   // on a refinement level the coarse operator is only needed where Set_In
   // copies (k_set_in_op forms it there)
   const bool fold_set_in = k > mg && h->set_in[k].strided;
-  if (!fold_set_in) dispatch_apply_op<EQ>(h, k - 1);
-  if (k <= mg) dispatch_robin(h, k - 1, 1);
+  if (!fold_set_in) dispatch_apply_op<EQ>(h, k - 1, true);
+  if (k <= mg) dispatch_robin(h, k - 1, 1, true);
   dispatch_apply_op<EQ>(h, k);
   if (k <= mg) dispatch_robin(h, k, 1);
   launch_ew(h, k, EW_W_EQ_S_MINUS_R);
@@ -737,7 +793,7 @@ void emit_fasn_down(olgpu_hierarchy *h, int k)
     launch_transfer(h, h->xfer_w[k]);
   }
   if (k <= mg) {
-    launch_ew(h, k - 1, EW_S_EQ_W_PLUS_R);
+    launch_ew(h, k - 1, EW_S_EQ_W_PLUS_R, true);
   } else if (fold_set_in) {
     const Transfer &X = h->set_in[k];
     const unsigned nb = (unsigned)X.blocks;
@@ -750,27 +806,50 @@ void emit_fasn_down(olgpu_hierarchy *h, int k)
     }
     h->launches++;
   } else {
-    launch_ew(h, k - 1, EW_W_PLUS_EQ_R);
+    launch_ew(h, k - 1, EW_W_PLUS_EQ_R, true);
     launch_transfer(h, h->set_in[k]);
   }
-  launch_ew(h, k - 1, EW_WW_EQ_U);
+  launch_ew(h, k - 1, EW_WW_EQ_U, true);
 }
 
 // the coarsest solve (src/elliptic.cc:1782-1816)
 template <int EQ>
-void emit_coarse(olgpu_hierarchy *h)
+void emit_coarse(olgpu_hierarchy *h, const olgpu_hierarchy::Member &M)
 {
-  const DevBox &B = h->hboxes[h->G.first_box[0]];
+  const DevBox &B = h->hboxes[M.coarse_box];
   const size_t smem = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
-  if (h->coarse_ncta > 0)
-    launch_coarse_cluster<EQ>(h);
+  if (M.coarse_ncta > 0)
+    launch_coarse_cluster<EQ>(h, M);
   else
-    k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F, h->d_coords,
+    k_coarse_solve<EQ><<<1, 1024, smem, h->stream>>>(h->d_boxes, M.coarse_box, h->F, h->d_coords,
                                                      h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
-                                                     h->coarse_rtol, &h->d_stats->coarse_norm,
-                                                     &h->d_stats->coarse_iters, &h->d_stats->nan_flag,
+                                                     h->coarse_rtol, &M.d_stats->coarse_norm,
+                                                     &M.d_stats->coarse_iters, &M.d_stats->nan_flag,
                                                      h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
   h->launches++;
+}
+
+// The correction of a refinement level's INSIDE points and the ghost fill of
+// its BOUNDARY points in one launch (k_prolong_ghost), when both plans take
+// their fast forms; returns false (nothing launched) otherwise.
+template <class V, class Fields>
+bool launch_prolong_ghost(olgpu_hierarchy *h, const Transfer &Pv, const Transfer &Gh, const Fields &F, int fe, int fww)
+{
+  if (!h->fast_paths || Pv.jobs.empty() || Gh.jobs.empty() || !Gh.rows) return false;
+  const unsigned nb = (unsigned)((Pv.pair_blocks + 1) / 2 + Gh.row_blocks);
+  const int np = (int)Pv.jobs.size(), ng = (int)Gh.jobs.size();
+  const unsigned th = 32 * kRowWarps;
+  switch (Gh.width) {
+  case 4: k_prolong_ghost<V, Fields, 4><<<nb, th, 0, h->stream>>>(Pv.d_jobs, np, Pv.pair_blocks, Gh.d_jobs, ng,
+                                                                  h->d_boxes, F, h->d_tab, fe, fww); break;
+  case 6: k_prolong_ghost<V, Fields, 6><<<nb, th, 0, h->stream>>>(Pv.d_jobs, np, Pv.pair_blocks, Gh.d_jobs, ng,
+                                                                  h->d_boxes, F, h->d_tab, fe, fww); break;
+  case 8: k_prolong_ghost<V, Fields, 8><<<nb, th, 0, h->stream>>>(Pv.d_jobs, np, Pv.pair_blocks, Gh.d_jobs, ng,
+                                                                  h->d_boxes, F, h->d_tab, fe, fww); break;
+  default: k_prolong_ghost<V, Fields, 10><<<nb, th, 0, h->stream>>>(Pv.d_jobs, np, Pv.pair_blocks, Gh.d_jobs, ng,
+                                                                    h->d_boxes, F, h->d_tab, fe, fww); break;
+  }
+  return true;
 }
 
 // FASN's ascent on level k (src/elliptic.cc:1827-1941): the coarse
@@ -780,35 +859,46 @@ template <int EQ>
 void emit_fasn_up(olgpu_hierarchy *h, int k, int top)
 {
   const int mg = h->G.mgrid_levels;
-  if (h->fast_paths) {   // u_fine += P(u - ww) in one pass
-    const Transfer &X = h->prolong_v[k];
-    if (!X.jobs.empty()) {
-      k_prolong_correct<double, DevFields><<<(unsigned)X.pair_blocks, kThreads, 0, h->stream>>>(
-          X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F, h->d_tab, F_U, F_WW);
-      h->launches++;
-    }
+  if (k > mg && launch_prolong_ghost<double>(h, h->prolong_v[k], h->ghost_u[k], h->F, F_U, F_WW)) {
+    h->launches++;   // correction and ghost fill of a refinement level in one launch
   } else {
-    launch_ew(h, k - 1, EW_V_EQ_U_MINUS_WW);
-    launch_transfer(h, h->prolong_v[k]);
-    launch_ew(h, k, EW_U_PLUS_EQ_V);
+    if (h->fast_paths) {   // u_fine += P(u - ww) in one pass
+      const Transfer &X = h->prolong_v[k];
+      if (!X.jobs.empty()) {
+        k_prolong_correct<double, DevFields><<<(unsigned)X.pair_blocks, kThreads, 0, h->stream>>>(
+            X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F, h->d_tab, F_U, F_WW);
+        h->launches++;
+      }
+    } else {
+      launch_ew(h, k - 1, EW_V_EQ_U_MINUS_WW, true);
+      launch_transfer(h, h->prolong_v[k]);
+      launch_ew(h, k, EW_U_PLUS_EQ_V);
+    }
+    if (k > mg) launch_transfer(h, h->ghost_u[k]);
   }
-  if (k > mg) launch_transfer(h, h->ghost_u[k]);
   if (k <= mg) dispatch_robin(h, k, 0);
   dispatch_smooth<EQ>(h, k, h->P.nu2, 2 * k + 1);
-  if (k == top && !h->hadm.empty())
-  {
-    k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
-    h->launches++;
-  }
+  if (k == top)
+    for (const auto &M : h->members)
+      if (M.nadm > 0) {
+        k_adm<<<1, 32, 0, h->stream>>>(M.d_adm, M.nadm, h->d_boxes, h->F, M.d_stats->adm_u);
+        h->launches++;
+      }
 }
 
 // elliptic::FASN with Wcycle = false (src/elliptic.cc:1468-1968)
 template <int EQ>
+// (a union: a member whose coarsest level is k - 1 solves it there, the
+// others descend further)
 void emit_fasn(olgpu_hierarchy *h, int k, int top)
 {
   emit_fasn_down<EQ>(h, k);
-  if (k == 1) emit_coarse<EQ>(h);
-  else emit_fasn<EQ>(h, k - 1, top);
+  bool deeper = false;
+  for (const auto &M : h->members) {
+    if (M.off == k - 1) emit_coarse<EQ>(h, M);
+    else if (M.off < k - 1) deeper = true;
+  }
+  if (deeper) emit_fasn<EQ>(h, k - 1, top);
   emit_fasn_up<EQ>(h, k, top);
 }
 
@@ -824,9 +914,11 @@ void emit_du_begin(olgpu_hierarchy *h)
 
 int emit_du_end(olgpu_hierarchy *h)
 {
-  k_du_max<<<152 * 4, kThreads, 0, h->stream>>>(h->total_pts, h->F.f[F_U], h->F.f[F_UP], h->d_pinned,
-                                                  &h->d_stats->slots[kSlotDu]);
-  return 1;
+  for (const auto &M : h->members)   // each solve's own points and slot
+    k_du_max<<<152 * 4, kThreads, 0, h->stream>>>(M.h->total_pts, h->F.f[F_U] + M.pt_base, h->F.f[F_UP] + M.pt_base,
+                                                  M.h->d_pinned, &M.d_stats->slots[kSlotDu],
+                                                  (const DevBox *)h->d_boxes + M.box_base);
+  return (int)h->members.size();
 }
 
 // ---------------------------------------------------------------------------
@@ -839,23 +931,23 @@ void launch_transfer32(olgpu_hierarchy *h, const Transfer &X)
   h->launches_mixed++;
 }
 
-void launch_ew32(olgpu_hierarchy *h, int level, int op)
+void launch_ew32(olgpu_hierarchy *h, int level, int op, bool whole = false)
 {
-  const BoxList L = level_list(h, level, blocks_all);
+  const BoxList L = level_list(h, level, blocks_all, whole);
   k_elementwise32<<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, op);
   h->launches_mixed++;
 }
 
 template <int ORD, int EQ>
-void launch_mx_defect(olgpu_hierarchy *h, int level, unsigned long long *slot)
+void launch_mx_defect(olgpu_hierarchy *h, int level, int slot)
 {
   const BoxList L = level_list(h, level, blocks_all);
-  k_mx_defect<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->F32, slot);
+  k_mx_defect<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->F32, h->d_stats0, slot);
   h->launches_mixed++;
 }
 
 template <int EQ>
-void dispatch_mx_defect(olgpu_hierarchy *h, int level, unsigned long long *slot)
+void dispatch_mx_defect(olgpu_hierarchy *h, int level, int slot)
 {
   switch (level_order(h, level)) {
   case 2: launch_mx_defect<2, EQ>(h, level, slot); break;
@@ -872,15 +964,15 @@ void launch_smooth32(olgpu_hierarchy *h, int level, int nu)
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
       launch_pdl(h, k_smooth32<ORD, EQ>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
-                 (const DevBox *)h->d_boxes, h->F32, color, &h->d_stats->nan_flag);
+                 (const DevBox *)h->d_boxes, h->F32, color, h->d_stats0);
       h->launches_mixed++;
     }
 }
 
 template <int ORD, int EQ>
-void launch_apply_op32(olgpu_hierarchy *h, int level)
+void launch_apply_op32(olgpu_hierarchy *h, int level, bool whole = false)
 {
-  const BoxList L = level_list(h, level, blocks_inside);
+  const BoxList L = level_list(h, level, blocks_inside, whole);
   k_apply_op32<ORD, EQ><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32);
   h->launches_mixed++;
 }
@@ -901,8 +993,8 @@ void launch_smooth32_cluster(olgpu_hierarchy *h, int level, int nu)
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_smooth32_cluster<ORD, EQ>, (const DevBox *)h->d_boxes, h->G.first_box[level], h->F32,
-                     nu, &h->d_stats->nan_flag);
+  cudaLaunchKernelEx(&cfg, k_smooth32_cluster<ORD, EQ>, (const DevBox *)h->d_boxes, level_list(h, level, blocks_all),
+                     h->F32, nu, h->d_stats0);
   h->launches_mixed++;
 }
 
@@ -975,8 +1067,9 @@ void choose_smooth_clusters(olgpu_hierarchy *h)
       size_t smem = 0;
       int share = 0;
       bool ok = true;
-      for (int g = h->G.first_box[l]; g < h->G.first_box[l] + h->G.boxes_in_level[l]; g++) {
-        const DevBox &B = h->hboxes[g];
+      const BoxList FL = level_list(h, l, blocks_all);   // the boxes the smoother runs on
+      for (int q = 0; q < FL.count; q++) {
+        const DevBox &B = h->hboxes[FL.box[q]];
         const int m2 = B.n[2] - 2 * B.buf;
         if (m2 < ncta || B.n[2] > kMaxClusterPlanes || B.buf < ord / 2 || B.order != ord) ok = false;
         share = std::max(share, (m2 + ncta - 1) / ncta);
@@ -1018,30 +1111,36 @@ void dispatch_smooth32(olgpu_hierarchy *h, int level, int nu)
 }
 
 template <int EQ>
-void dispatch_apply_op32(olgpu_hierarchy *h, int level)
+void dispatch_apply_op32(olgpu_hierarchy *h, int level, bool whole = false)
 {
   switch (level_order(h, level)) {
-  case 2: launch_apply_op32<2, EQ>(h, level); break;
-  case 4: launch_apply_op32<4, EQ>(h, level); break;
-  case 6: launch_apply_op32<6, EQ>(h, level); break;
-  default: launch_apply_op32<8, EQ>(h, level); break;
+  case 2: launch_apply_op32<2, EQ>(h, level, whole); break;
+  case 4: launch_apply_op32<4, EQ>(h, level, whole); break;
+  case 6: launch_apply_op32<6, EQ>(h, level, whole); break;
+  default: launch_apply_op32<8, EQ>(h, level, whole); break;
   }
 }
 
 template <int ORD>
-void launch_robin32(olgpu_hierarchy *h, int level, int mode)
+void launch_robin32(olgpu_hierarchy *h, int level, int mode, bool whole = false)
 {
-  const BoxList L = level_list(h, level, blocks_faces);
+  const BoxList L = level_list(h, level, blocks_faces, whole);
+  if (!h->robin_split) {
+    launch_clusters(h, k_robin32_cluster<ORD>, (unsigned)(L.count * kRobinCluster), kThreads, kRobinCluster, L,
+                    (const DevBox *)h->d_boxes, h->F32, (const double *)h->d_coords, mode);
+    h->launches_mixed++;
+    return;
+  }
   k_robin32_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);
   k_robin32_edges_corners<ORD><<<12 * L.count, 64, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode, 0);
   k_robin32_edges_corners<ORD><<<L.count, 32, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode, 1);
   h->launches_mixed += 3;
 }
 
-void dispatch_robin32(olgpu_hierarchy *h, int level, int mode)
+void dispatch_robin32(olgpu_hierarchy *h, int level, int mode, bool whole = false)
 {
-  if (level_order(h, level) == 2) launch_robin32<2>(h, level, mode);
-  else launch_robin32<4>(h, level, mode);
+  if (level_order(h, level) == 2) launch_robin32<2>(h, level, mode, whole);
+  else launch_robin32<4>(h, level, mode, whole);
 }
 
 template <int EQ>
@@ -1054,8 +1153,8 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   // on a refinement level the coarse operator is only needed where Set_In
   // copies (k_set_in_op32 forms it there)
   const bool fold_set_in = k > mg && h->set_in32[k].strided;
-  if (!fold_set_in) dispatch_apply_op32<EQ>(h, k - 1);
-  if (k <= mg) dispatch_robin32(h, k - 1, 1);
+  if (!fold_set_in) dispatch_apply_op32<EQ>(h, k - 1, true);
+  if (k <= mg) dispatch_robin32(h, k - 1, 1, true);
   dispatch_apply_op32<EQ>(h, k);
   if (k <= mg) dispatch_robin32(h, k, 1);
   if (h->xfer_w32[k].strided) {   // full weighting of S - R folded into the transfer
@@ -1070,9 +1169,9 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
     launch_transfer32(h, h->xfer_w32[k]);
   }
   if (k <= mg) {
-    launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R_WW_EQ_E);
+    launch_ew32(h, k - 1, EW32_S_EQ_W_PLUS_R_WW_EQ_E, true);
   } else if (fold_set_in) {
-    launch_ew32(h, k - 1, EW32_WW_EQ_E);
+    launch_ew32(h, k - 1, EW32_WW_EQ_E, true);
     const Transfer &X = h->set_in32[k];
     const unsigned nb = (unsigned)X.blocks;
     const int nj = (int)X.jobs.size();
@@ -1084,38 +1183,46 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
     }
     h->launches_mixed++;
   } else {
-    launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R_WW_EQ_E);   // WW = E: nothing writes E before set_in
+    launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R_WW_EQ_E, true);   // WW = E: nothing writes E before set_in
     launch_transfer32(h, h->set_in32[k]);
   }
-  if (k == 1) {
-    const DevBox &B = h->hboxes[h->G.first_box[0]];
+  bool deeper = false;   // a union: members whose coarsest level is k - 1 solve it, the others descend
+  for (const auto &M : h->members) {
+    if (M.off != k - 1) {
+      deeper = deeper || M.off < k - 1;
+      continue;
+    }
+    const DevBox &B = h->hboxes[M.coarse_box];
     const size_t np = (size_t)B.n[0] * B.n[1] * B.n[2];
     const size_t staged = sizeof(float) * np * (EQ == 1 ? 6 : 4);
     if (staged <= kCoarseSmemMax)
-      k_coarse32<EQ, true><<<1, 1024, staged, h->stream>>>(h->d_boxes, h->G.first_box[0], h->F32, h->d_coords,
+      k_coarse32<EQ, true><<<1, 1024, staged, h->stream>>>(h->d_boxes, M.coarse_box, h->F32, h->d_coords,
                                                             h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
-                                                            &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+                                                            &M.d_stats->coarse_iters, &M.d_stats->nan_flag);
     else
       k_coarse32<EQ, false><<<1, 1024, sizeof(float) * np, h->stream>>>(
-          h->d_boxes, h->G.first_box[0], h->F32, h->d_coords, h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
-          &h->d_stats->coarse_iters, &h->d_stats->nan_flag);
+          h->d_boxes, M.coarse_box, h->F32, h->d_coords, h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+          &M.d_stats->coarse_iters, &M.d_stats->nan_flag);
+    h->launches_mixed++;
+  }
+  if (deeper) emit_fasn32<EQ>(h, k - 1);
+  if (k > mg && launch_prolong_ghost<float>(h, h->prolong_v32[k], h->ghost_e[k], h->F32, G_E, G_WW)) {
     h->launches_mixed++;
   } else {
-    emit_fasn32<EQ>(h, k - 1);
-  }
-  if (h->fast_paths) {   // e_fine += P(e - ww) in one pass
-    const Transfer &X = h->prolong_v32[k];
-    if (!X.jobs.empty()) {
-      k_prolong_correct<float, DevFields32><<<(unsigned)X.pair_blocks, kThreads, 0, h->stream>>>(
-          X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32, h->d_tab, G_E, G_WW);
-      h->launches_mixed++;
+    if (h->fast_paths) {   // e_fine += P(e - ww) in one pass
+      const Transfer &X = h->prolong_v32[k];
+      if (!X.jobs.empty()) {
+        k_prolong_correct<float, DevFields32><<<(unsigned)X.pair_blocks, kThreads, 0, h->stream>>>(
+            X.d_jobs, (int)X.jobs.size(), h->d_boxes, h->F32, h->d_tab, G_E, G_WW);
+        h->launches_mixed++;
+      }
+    } else {
+      launch_ew32(h, k - 1, EW32_V_EQ_E_MINUS_WW, true);
+      launch_transfer32(h, h->prolong_v32[k]);
+      launch_ew32(h, k, EW32_E_PLUS_EQ_V);
     }
-  } else {
-    launch_ew32(h, k - 1, EW32_V_EQ_E_MINUS_WW);
-    launch_transfer32(h, h->prolong_v32[k]);
-    launch_ew32(h, k, EW32_E_PLUS_EQ_V);
+    if (k > mg) launch_transfer32(h, h->ghost_e[k]);
   }
-  if (k > mg) launch_transfer32(h, h->ghost_e[k]);
   if (k <= mg) dispatch_robin32(h, k, 0);
   dispatch_smooth32<EQ>(h, k, h->inner_nu2 >= 0 ? h->inner_nu2 : h->P.nu2);
 }
@@ -1133,7 +1240,7 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   h->launches = fp64_before;
   // FP64: coefficients of the correction operator and the defect source
   for (int l = 0; l < L; l++) {
-    const BoxList BL = level_list(h, l, blocks_all);
+    const BoxList BL = level_list(h, l, blocks_all, true);
     switch (level_order(h, l)) {
     case 2: k_mx_prep<2, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
     case 4: k_mx_prep<4, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
@@ -1156,27 +1263,33 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   emit_fasn32<EQ>(h, top);
   // FP64 update and the FP64 defect of the finest level as the cycle's norm
   if (h->anderson_m > 0) {
-    const long long n = h->total_pts;
-    float *DU = h->d_and, *DF = h->d_and + (size_t)kAndMax * n, *fprev = h->d_and + (size_t)2 * kAndMax * n;
-    const int nblk = 152 * 4;
-    k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E], fprev, DF, h->d_pinned, h->d_and_state,
-                                                    h->d_and_part, &h->d_stats->slots[kSlotCorr]);
-    k_and_solve<<<1, 32 * kAndSolveWarps, 0, h->stream>>>(h->d_and_state, h->d_and_part, nblk);
-    k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U], h->F32.f[G_E], DU, DF, h->d_and_state);
-    h->launches_mixed += 3;
+    for (const auto &M : h->members) {   // each solve's own history, points and slot
+      const olgpu_hierarchy *m = M.h;
+      const long long n = m->total_pts;
+      float *DU = m->d_and, *DF = m->d_and + (size_t)kAndMax * n, *fprev = m->d_and + (size_t)2 * kAndMax * n;
+      const DevBox *gate = (const DevBox *)h->d_boxes + M.box_base;
+      const int nblk = 152 * 4;
+      k_and_reduce<<<nblk, kThreads, 0, h->stream>>>(n, h->F32.f[G_E] + M.pt_base, fprev, DF, m->d_pinned,
+                                                      m->d_and_state, m->d_and_part, &M.d_stats->slots[kSlotCorr],
+                                                      gate);
+      k_and_solve<<<1, 32 * kAndSolveWarps, 0, h->stream>>>(m->d_and_state, m->d_and_part, nblk, gate);
+      k_and_update<<<nblk, kThreads, 0, h->stream>>>(n, h->F.f[F_U] + M.pt_base, h->F32.f[G_E] + M.pt_base, DU, DF,
+                                                      m->d_and_state, gate);
+      h->launches_mixed += 3;
+    }
   } else {
     for (int l = 0; l < L; l++) {
-      const BoxList BL = level_list(h, l, blocks_all);
-      k_mx_update<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, mg,
-                                                                &h->d_stats->slots[kSlotCorr]);
+      const BoxList BL = level_list(h, l, blocks_all, true);
+      k_mx_update<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, h->d_stats0);
       h->launches_mixed++;
     }
   }
-  dispatch_mx_defect<EQ>(h, top, &h->d_stats->slots[kSlotDefect]);
-  if (!h->hadm.empty()) {
-    k_adm<<<1, 32, 0, h->stream>>>(h->d_adm, (int)h->hadm.size(), h->d_boxes, h->F, h->d_stats->adm_u);
-    h->launches_mixed++;
-  }
+  dispatch_mx_defect<EQ>(h, top, kSlotDefect);
+  for (const auto &M : h->members)
+    if (M.nadm > 0) {
+      k_adm<<<1, 32, 0, h->stream>>>(M.d_adm, M.nadm, h->d_boxes, h->F, M.d_stats->adm_u);
+      h->launches_mixed++;
+    }
 }
 
 Transfer remap(const Transfer &X, int sfield, int tfield)
@@ -1209,13 +1322,25 @@ olgpu_status reset_anderson(olgpu_hierarchy *h)
 olgpu_status capture_mixed(olgpu_hierarchy *h);
 
 // Allocates the FP32 fields and plans and captures the mixed cycle (once).
-olgpu_status build_mixed(olgpu_hierarchy *h)
+// The FP32 fields, plans and Anderson history of the mixed cycle (once).  A
+// union's member gets arena32 (its FP32 field g at arena32 + g * stride +
+// base, inside the union's arena) and keeps only its Anderson history; the
+// union itself has no history of its own (each member's is used).
+olgpu_status prepare_mixed(olgpu_hierarchy *h, float *arena32, long long stride, long long base)
 {
-  if (h->graph_mixed) return OLGPU_OK;
-  const size_t bytes = sizeof(float) * (size_t)h->total_pts * G_NUM;
-  if (cudaMalloc(&h->d_arena32, bytes) != cudaSuccess) return fail(OLGPU_ERR_OOM, "FP32 arena allocation failed");
-  CUDA_TRY(cudaMemset(h->d_arena32, 0, bytes));
-  for (int f = 0; f < G_NUM; f++) h->F32.f[f] = h->d_arena32 + (size_t)f * h->total_pts;
+  if (h->mixed_ready) return OLGPU_OK;
+  const bool member = arena32 != nullptr;
+  if (!member) {
+    const size_t bytes = sizeof(float) * (size_t)h->total_pts * G_NUM;
+    if (cudaMalloc(&h->d_arena32, bytes) != cudaSuccess) return fail(OLGPU_ERR_OOM, "FP32 arena allocation failed");
+    CUDA_TRY(cudaMemset(h->d_arena32, 0, bytes));
+    arena32 = h->d_arena32;
+    stride = h->total_pts;
+    base = 0;
+  } else {
+    h->owns_arena32 = false;
+  }
+  for (int f = 0; f < G_NUM; f++) h->F32.f[f] = arena32 + (size_t)f * stride + base;
   const int L = h->G.levels;
   h->restrict_e.resize(L);
   h->xfer_w32.resize(L);
@@ -1232,12 +1357,12 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
   }
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) {
-      if (X.jobs.empty()) continue;
+      if (X.jobs.empty() || member) continue;   // a member's FP32 steps run in the union's plans
       if (cudaMalloc(&X.d_jobs, sizeof(XferJob) * X.jobs.size()) != cudaSuccess)
         return fail(OLGPU_ERR_OOM, "transfer plan allocation failed");
       CUDA_TRY(cudaMemcpy(X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size(), cudaMemcpyHostToDevice));
     }
-  {
+  if (!h->is_union) {
     const size_t n = (size_t)h->total_pts;
     if (cudaMalloc(&h->d_and, sizeof(float) * n * (2 * kAndMax + 1)) != cudaSuccess ||
         cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess ||
@@ -1250,8 +1375,17 @@ olgpu_status build_mixed(olgpu_hierarchy *h)
   for (const void *kern : {(const void *)k_coarse32<0, true>, (const void *)k_coarse32<1, true>,
                            (const void *)k_coarse32<0, false>, (const void *)k_coarse32<1, false>})
     CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoarseSmemMax));
-  choose_smooth_clusters(h);
-  return capture_mixed(h);
+  if (!member) choose_smooth_clusters(h);
+  h->mixed_ready = true;
+  return OLGPU_OK;
+}
+
+// Prepares and captures the mixed cycle (once).
+olgpu_status build_mixed(olgpu_hierarchy *h)
+{
+  if (h->graph_mixed) return OLGPU_OK;
+  olgpu_status st = prepare_mixed(h, nullptr, 0, 0);
+  return st != OLGPU_OK ? st : capture_mixed(h);
 }
 
 // Captures the mixed cycle into h->graph_mixed (replacing an earlier one).
@@ -1263,7 +1397,7 @@ olgpu_status capture_mixed(olgpu_hierarchy *h)
   }
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
+  cudaMemsetAsync(h->d_stats, 0, sizeof(Stats) * h->members.size(), h->stream);   // a union: every member's
   h->launches_mixed = 0;
   emit_du_begin(h);
   if (h->equation == 1) emit_mixed_cycle<1>(h);
@@ -1282,7 +1416,7 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   const int top = h->G.levels - 1;
   cudaGraph_t g;
   CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(h->d_stats, 0, sizeof(Stats), h->stream);
+  cudaMemsetAsync(h->d_stats, 0, sizeof(Stats) * h->members.size(), h->stream);   // a union: every member's
   h->launches = 0;
   emit_du_begin(h);
   if (h->equation == 1) emit_fasn<1>(h, top, top);
@@ -1335,7 +1469,8 @@ olgpu_status build_wgraphs_eq(olgpu_hierarchy *h)
       emit_fasn_up<EQ>(h, k, top);
     }, &h->graph_up[k], "W-cycle ascent");
   }
-  if (st == OLGPU_OK) st = capture_piece(h, [&] { emit_coarse<EQ>(h); }, &h->graph_coarse, "W-cycle coarse solve");
+  if (st == OLGPU_OK)
+    st = capture_piece(h, [&] { emit_coarse<EQ>(h, h->members[0]); }, &h->graph_coarse, "W-cycle coarse solve");
   h->launches = saved;
   return st;
 }
@@ -1494,10 +1629,9 @@ olgpu_status olgpu_plan_boxes(const olgpu_problem *p, olgpu_box_info *out, int c
   return OLGPU_OK;
 }
 
-olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hierarchy **out)
+// The problem's parameters are ones the solver takes.
+static olgpu_status validate_problem(const olgpu_problem *p)
 {
-  if (!p || !out) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
-  *out = nullptr;
   if (p->numbh < 1 || p->numbh > OLGPU_MAX_BH) return fail(OLGPU_ERR_INVALID_ARG, "numbh out of range 1..16");
   if (!(p->order == 2 || p->order == 4 || p->order == 6 || p->order == 8))
     return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
@@ -1512,11 +1646,14 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     return fail(OLGPU_ERR_INVALID_ARG, "method must be Vcycle or Wcycle");
   if (p->equation == 1 && !(p->ps_case >= 1 && p->ps_case <= 4))
     return fail(OLGPU_ERR_INVALID_ARG, "ps_case must be 1..4");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OLGPU_ERR_NO_DEVICE, "no CUDA device");
-  if (device >= 0) CUDA_TRY(cudaSetDevice(device));
+  return OLGPU_OK;
+}
 
-  auto *h = new olgpu_hierarchy();
+// Host planning of a hierarchy: the geometry (elliptic::Set_Grids), the box
+// table, the coordinate tables, every transfer plan and the ADM jobs.
+// Nothing on the device yet.
+static olgpu_status plan_hierarchy(const olgpu_problem *p, olgpu_hierarchy *h)
+{
   h->P = *p;
   h->equation = p->equation;
   CUDA_TRY(cudaGetDevice(&h->device));
@@ -1524,17 +1661,14 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   h->eps_solv = p->tol < h->eps_coarse ? h->eps_coarse : p->tol;
   puncture_set bh{p->numbh, p->x, p->y, p->z};
   if (!set_grids(p->n, p->L, p->order, p->levels, bh, h->G)) {
-    delete h;
     return fail(OLGPU_ERR_GEOMETRY, "not enough grid points for multigrid");
   }
   if (h->G.levels > 60) {   // norm slots 0..119 (2 a level); 120..127 hold the cycle's other norms
-    delete h;
     return fail(OLGPU_ERR_INVALID_ARG, "too many levels");
   }
   for (int l = 0; l < h->G.levels; l++)
     if (h->G.boxes_in_level[l] > kMaxBoxesPerLevel) {
-      delete h;
-      return fail(OLGPU_ERR_INVALID_ARG, "too many boxes on one level");
+        return fail(OLGPU_ERR_INVALID_ARG, "too many boxes on one level");
     }
   // device box table and coordinate tables
   long long off = 0;
@@ -1546,6 +1680,9 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
     B.level = D.level;
     B.off = off;
     B.coord_off = coff;
+    B.solve = 0;
+    B.active = 1;
+    B.mg_coarse = D.level < h->G.mgrid_levels ? 1 : 0;
     set_box_stencil(B, D.order, D.d);
     // x, y, z of the box's nodes, then their reciprocals (ghost nodes lie on
     // the outer faces; a node at 0 gets 0, it is never a Robin point)
@@ -1604,20 +1741,33 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
       h->hadm.push_back(J);
     }
   }
-  // device memory
+  return OLGPU_OK;
+}
+
+// Device set-up of a planned hierarchy: stream and events, the field arena
+// (its own when arena is NULL, else field f at arena + f * stride + base),
+// the tables and plans, the stats (its own when stats is NULL), the
+// coefficients and initial state, and (capture) its captured V-cycle.
+static olgpu_status setup_device(olgpu_hierarchy *h, double *arena, long long stride, long long base, Stats *stats,
+                                 Stats *hstats, bool capture)
+{
   olgpu_status st = OLGPU_OK;
-  auto cleanup = [&](olgpu_status s) {
-    olgpu_hierarchy_destroy(h);
-    return s;
-  };
+  auto cleanup = [&](olgpu_status s) { return s; };   // the caller destroys h
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_cycle, cudaEventDisableTiming) != cudaSuccess)
     return cleanup(fail(OLGPU_ERR_CUDA, "stream/event creation failed"));
-  const size_t arena = sizeof(double) * (size_t)h->total_pts * F_NUM;
-  cudaError_t e = cudaMalloc(&h->d_arena, arena);
-  if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_OOM, "device arena allocation failed"));
-  for (int f = 0; f < F_NUM; f++) h->F.f[f] = h->d_arena + (size_t)f * h->total_pts;
+  cudaError_t e = cudaSuccess;
+  if (!arena) {   // its own arena
+    e = cudaMalloc(&h->d_arena, sizeof(double) * (size_t)h->total_pts * F_NUM);
+    if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_OOM, "device arena allocation failed"));
+    arena = h->d_arena;
+    stride = h->total_pts;
+    base = 0;
+  } else {
+    h->owns_arena = false;
+  }
+  for (int f = 0; f < F_NUM; f++) h->F.f[f] = arena + (size_t)f * stride + base;
   if (h->equation != 1) h->F.f[F_D] = h->F.f[F_E] = nullptr;
   auto up = [&](void **dst, const void *src, size_t bytes) -> bool {
     if (bytes == 0) return true;
@@ -1631,8 +1781,15 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
     for (auto &X : *vec)
       ok = ok && up((void **)&X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size());
-  ok = ok && cudaMalloc(&h->d_stats, sizeof(Stats)) == cudaSuccess &&
-       cudaMallocHost(&h->h_stats, sizeof(Stats)) == cudaSuccess;
+  if (stats) {   // a member of a union: its stats are the union's
+    h->owns_stats = false;
+    h->d_stats = stats;
+    h->h_stats = hstats;
+  } else {
+    ok = ok && cudaMalloc(&h->d_stats, sizeof(Stats)) == cudaSuccess &&
+         cudaMallocHost(&h->h_stats, sizeof(Stats)) == cudaSuccess;
+  }
+  h->d_stats0 = h->d_stats;
   if (!ok) return cleanup(fail(OLGPU_ERR_OOM, "device allocation failed"));
   // the points the discrete system fixes: every point of the solution levels,
   // the INSIDE points of the multigrid coarse levels (their ghost layers keep
@@ -1677,16 +1834,53 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   if (st != OLGPU_OK) return cleanup(st);
   // coefficients on the device
   {
-    const PunctureParams PP = puncture_params(p);
-    for (int l = 0; l < L; l++) {
-      const BoxList BL = level_list(h, l, blocks_all);
+    const PunctureParams PP = puncture_params(&h->P);
+    for (int l = 0; l < h->G.levels; l++) {
+      const BoxList BL = level_list(h, l, blocks_all, true);
       k_coefficients<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords, PP);
     }
     e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_CUDA, std::string("coefficients: ") + cudaGetErrorString(e)));
   }
-  st = build_graph(h);
-  if (st != OLGPU_OK) return cleanup(st);
+  h->members.assign(1, olgpu_hierarchy::Member{});
+  {
+    olgpu_hierarchy::Member &M = h->members[0];
+    M.h = h;
+    M.off = 0;
+    M.coarse_box = h->G.first_box[0];
+    M.box_base = 0;
+    M.pt_base = 0;
+    M.d_stats = h->d_stats;
+    M.d_adm = h->d_adm;
+    M.nadm = (int)h->hadm.size();
+    M.coarse_ncta = h->coarse_ncta;
+    M.coarse_smem = h->coarse_cluster_smem;
+  }
+  if (capture) {
+    st = build_graph(h);
+    if (st != OLGPU_OK) return cleanup(st);
+  }
+  return OLGPU_OK;
+}
+
+
+olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hierarchy **out)
+{
+  if (!p || !out) return fail(OLGPU_ERR_INVALID_ARG, "null argument");
+  *out = nullptr;
+  olgpu_status st = validate_problem(p);
+  if (st != OLGPU_OK) return st;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OLGPU_ERR_NO_DEVICE, "no CUDA device");
+  if (device >= 0) CUDA_TRY(cudaSetDevice(device));
+
+  auto *h = new olgpu_hierarchy();
+  st = plan_hierarchy(p, h);
+  if (st == OLGPU_OK) st = setup_device(h, nullptr, 0, 0, nullptr, nullptr, true);
+  if (st != OLGPU_OK) {
+    olgpu_hierarchy_destroy(h);
+    return st;
+  }
   *out = h;
   return OLGPU_OK;
 }
@@ -1706,20 +1900,27 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   if (h->graph_coarse) cudaGraphExecDestroy(h->graph_coarse);
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) cudaFree(X.d_jobs);
-  cudaFree(h->d_arena32);
+  if (h->owns_arena32) cudaFree(h->d_arena32);
   cudaFree(h->d_and);
   cudaFree(h->d_pinned);
   cudaFree(h->d_and_state);
   cudaFree(h->d_and_part);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
     for (auto &X : *vec) cudaFree(X.d_jobs);
-  cudaFree(h->d_arena);
+  if (h->owns_arena) cudaFree(h->d_arena);
   cudaFree(h->d_boxes);
   cudaFree(h->d_coords);
   cudaFree(h->d_tab);
   cudaFree(h->d_adm);
-  cudaFree(h->d_stats);
-  if (h->h_stats) cudaFreeHost(h->h_stats);
+  if (h->is_union)   // a union owns its members and their ADM job copies
+    for (auto &M : h->members) {
+      cudaFree(M.d_adm);
+      olgpu_hierarchy_destroy(M.h);
+    }
+  if (h->owns_stats) {
+    cudaFree(h->d_stats);
+    if (h->h_stats) cudaFreeHost(h->h_stats);
+  }
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_cycle) cudaEventDestroy(h->ev_cycle);
@@ -1794,7 +1995,8 @@ static olgpu_status cycle_enqueue(olgpu_hierarchy *h)
 {
   const bool mixed = h->precision == OLGPU_PREC_MIXED;
   CUDA_TRY(cudaGraphLaunch(mixed ? h->graph_mixed : h->graph, h->stream));
-  CUDA_TRY(cudaMemcpyAsync(h->h_stats, h->d_stats, sizeof(Stats), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->h_stats, h->d_stats, sizeof(Stats) * h->members.size(), cudaMemcpyDeviceToHost,
+                           h->stream));   // a union: every member's
   CUDA_TRY(cudaEventRecord(h->ev_cycle, h->stream));
   return OLGPU_OK;
 }
@@ -2236,6 +2438,7 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
     for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
       for (auto &X : *vec) { cudaFree(X.d_jobs); X.d_jobs = nullptr; }
     cudaFree(h->d_arena32); h->d_arena32 = nullptr;
+    h->mixed_ready = false;
     cudaFree(h->d_and); h->d_and = nullptr;
     cudaFree(h->d_and_state); h->d_and_state = nullptr;
     cudaFree(h->d_and_part); h->d_and_part = nullptr;
@@ -2374,10 +2577,424 @@ olgpu_status olgpu_fma_peak(int precision, int iters, double *tflops)
 }  // extern "C"
 
 // ============================================================================
+// Batches of solves (olgpu_batch_*): every FASN step of a level is one launch
+// over the boxes of all the solves at that level
+// ============================================================================
+namespace {
+
+// Appends a member's transfer plan to a union's: box indices through map (the
+// member's box -> the union's), axis-table offsets moved by tab_base, and the
+// plan's block offsets moved past the jobs already there.
+void append_plan(Transfer &U, const Transfer &X, const std::vector<int> &map, int tab_base)
+{
+  for (XferJob J : X.jobs) {
+    J.tbox = map[J.tbox];
+    J.sbox = map[J.sbox];
+    for (int a = 0; a < 3; a++) J.tab[a] += tab_base;
+    J.blk0 += U.blocks;
+    J.rblk0 += U.row_blocks;
+    J.pblk0 += U.pair_blocks;
+    U.jobs.push_back(J);
+  }
+  U.blocks += X.blocks;
+  U.row_blocks += X.row_blocks;
+  U.pair_blocks += X.pair_blocks;
+}
+
+void finish_plan(Transfer &U)
+{
+  U.width = xfer_width(U.jobs.data(), U.jobs.size());
+  U.rows = xfer_rows(U.jobs.data(), U.jobs.size(), U.width) && !std::getenv("OLGPU_XFER_POINTS");
+  U.strided = !U.jobs.empty() && std::all_of(U.jobs.begin(), U.jobs.end(),
+                                             [](const XferJob &J) { return J.method == XM_STRIDED; });
+}
+
+// Members that can share one union: the same equation, order, refinement
+// depth (levels above the base grid: with levels aligned from the top, their
+// multigrid levels then line up), boundary and sweep counts.
+struct UnionKey {
+  int eq, order, depth, boundary, nu1, nu2;
+  bool operator<(const UnionKey &o) const
+  {
+    return std::tie(eq, order, depth, boundary, nu1, nu2) < std::tie(o.eq, o.order, o.depth, o.boundary, o.nu1, o.nu2);
+  }
+};
+
+}  // namespace
+
+struct olgpu_batch {
+  std::vector<olgpu_hierarchy *> members;    // in the caller's order
+  std::vector<olgpu_hierarchy *> unions;
+  std::vector<std::pair<int, int>> where;   // member -> (union, index in the union)
+  int precision = OLGPU_PREC_FP64;
+  double last_ms = 0.0;
+};
+
+// Builds one union of planned members (each with no device state yet),
+// ordered by decreasing levels, and everything it launches.
+static olgpu_status build_union(std::vector<olgpu_hierarchy *> ms, int precision, int nu1, int nu2, int blocks,
+                                olgpu_hierarchy **out)
+{
+  auto *U = new olgpu_hierarchy();
+  U->is_union = true;
+  U->P = ms[0]->P;
+  U->equation = ms[0]->equation;
+  U->device = ms[0]->device;
+  U->eps_coarse = ms[0]->eps_coarse;
+  U->eps_solv = ms[0]->eps_solv;
+  U->inner_nu1 = nu1;
+  U->inner_nu2 = nu2;
+  if (blocks >= 0) U->sc_max = blocks;
+  const int n = (int)ms.size();
+  int Lmax = 0;
+  long long total = 0;
+  for (auto *m : ms) Lmax = std::max(Lmax, m->G.levels);
+  std::vector<int> off(n);
+  std::vector<long long> base(n);
+  for (int i = 0; i < n; i++) {
+    off[i] = Lmax - ms[i]->G.levels;
+    base[i] = total;
+    total += ms[i]->total_pts;
+  }
+  U->total_pts = total;
+  U->G.levels = Lmax;
+  U->G.mgrid_levels = ms[0]->G.mgrid_levels + off[0];
+  auto fail_u = [&](olgpu_status st) {
+    for (auto *m : ms)
+      if (std::find_if(U->members.begin(), U->members.end(),
+                       [&](const olgpu_hierarchy::Member &M) { return M.h == m; }) == U->members.end())
+        olgpu_hierarchy_destroy(m);
+    olgpu_hierarchy_destroy(U);
+    return st;
+  };
+  // device: the union's arena and stats, then each member inside them
+  if (cudaStreamCreateWithFlags(&U->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&U->ev0) != cudaSuccess || cudaEventCreate(&U->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&U->ev_cycle, cudaEventDisableTiming) != cudaSuccess)
+    return fail_u(fail(OLGPU_ERR_CUDA, "batch: stream/event creation failed"));
+  if (cudaMalloc(&U->d_arena, sizeof(double) * (size_t)total * F_NUM) != cudaSuccess ||
+      cudaMalloc(&U->d_stats, sizeof(Stats) * n) != cudaSuccess ||
+      cudaMallocHost(&U->h_stats, sizeof(Stats) * n) != cudaSuccess)
+    return fail_u(fail(OLGPU_ERR_OOM, "batch: device allocation failed"));
+  U->d_stats0 = U->d_stats;
+  for (int f = 0; f < F_NUM; f++) U->F.f[f] = U->d_arena + (size_t)f * total;
+  if (U->equation != 1) U->F.f[F_D] = U->F.f[F_E] = nullptr;
+  U->members.resize(n);
+  for (int i = 0; i < n; i++) {
+    olgpu_status st = setup_device(ms[i], U->d_arena, total, base[i], U->d_stats + i, U->h_stats + i, false);
+    U->members[i].h = ms[i];   // owned by the union from here on
+    if (st != OLGPU_OK) return fail_u(st);
+    ms[i]->precision = precision;
+  }
+  // the union's tables: level-major, members in order inside a level, so that
+  // the members for which a level is not the coarsest come first
+  std::vector<std::vector<int>> map(n);
+  std::vector<int> coord_base(n), tab_base(n);
+  for (int i = 0; i < n; i++) {
+    map[i].assign(ms[i]->hboxes.size(), -1);
+    coord_base[i] = (int)U->hcoords.size();
+    U->hcoords.insert(U->hcoords.end(), ms[i]->hcoords.begin(), ms[i]->hcoords.end());
+    tab_base[i] = (int)U->htab.size();
+    U->htab.insert(U->htab.end(), ms[i]->htab.begin(), ms[i]->htab.end());
+  }
+  U->G.boxes_in_level.assign(Lmax, 0);
+  U->G.first_box.assign(Lmax, 0);
+  U->fine_count.assign(Lmax, 0);
+  for (int A = 0; A < Lmax; A++) {
+    U->G.first_box[A] = (int)U->hboxes.size();
+    for (int i = 0; i < n; i++) {
+      const int k = A - off[i];
+      if (k < 0) continue;
+      const auto &Gm = ms[i]->G;
+      for (int b = 0; b < Gm.boxes_in_level[k]; b++) {
+        const int g = Gm.first_box[k] + b;
+        DevBox B = ms[i]->hboxes[g];
+        B.off += base[i];
+        B.coord_off += coord_base[i];
+        B.solve = i;
+        B.active = 1;
+        map[i][g] = (int)U->hboxes.size();
+        U->hboxes.push_back(B);
+        U->G.boxes.push_back(Gm.boxes[g]);
+        U->G.boxes_in_level[A]++;
+        if (off[i] < A) U->fine_count[A]++;
+      }
+    }
+    if (U->G.boxes_in_level[A] > kMaxBoxesPerLevel)
+      return fail_u(fail(OLGPU_ERR_INVALID_ARG, "batch: too many boxes on one level"));
+  }
+  // the union's plans: each level's members (those for which it is not the
+  // coarsest level) in order
+  const int L = Lmax;
+  for (auto *vec : {&U->restrict_u, &U->xfer_w, &U->set_in, &U->prolong_v, &U->ghost_u, &U->ghost_lo})
+    vec->assign(L, Transfer{});
+  for (int A = 1; A < L; A++) {
+    for (int i = 0; i < n; i++) {
+      const int k = A - off[i];
+      if (k < 1) continue;
+      olgpu_hierarchy *m = ms[i];
+      append_plan(U->restrict_u[A], m->restrict_u[k], map[i], tab_base[i]);
+      append_plan(U->xfer_w[A], m->xfer_w[k], map[i], tab_base[i]);
+      append_plan(U->set_in[A], m->set_in[k], map[i], tab_base[i]);
+      append_plan(U->prolong_v[A], m->prolong_v[k], map[i], tab_base[i]);
+      append_plan(U->ghost_u[A], m->ghost_u[k], map[i], tab_base[i]);
+      append_plan(U->ghost_lo[A], m->ghost_lo[k], map[i], tab_base[i]);
+    }
+    for (auto *vec : {&U->restrict_u, &U->xfer_w, &U->set_in, &U->prolong_v, &U->ghost_u, &U->ghost_lo})
+      finish_plan((*vec)[A]);
+  }
+  auto upload = [&](void **dst, const void *src, size_t bytes) -> bool {
+    if (bytes == 0) return true;
+    if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
+    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+  };
+  bool ok = upload((void **)&U->d_boxes, U->hboxes.data(), sizeof(DevBox) * U->hboxes.size()) &&
+            upload((void **)&U->d_coords, U->hcoords.data(), sizeof(double) * U->hcoords.size()) &&
+            upload((void **)&U->d_tab, U->htab.data(), sizeof(AxisEntry) * U->htab.size());
+  for (auto *vec : {&U->restrict_u, &U->xfer_w, &U->set_in, &U->prolong_v, &U->ghost_u, &U->ghost_lo})
+    for (auto &X : *vec) ok = ok && upload((void **)&X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size());
+  if (!ok) return fail_u(fail(OLGPU_ERR_OOM, "batch: device allocation failed"));
+  // the members' records
+  for (int i = 0; i < n; i++) {
+    olgpu_hierarchy::Member &M = U->members[i];
+    olgpu_hierarchy *m = ms[i];
+    M.off = off[i];
+    M.coarse_box = map[i][m->G.first_box[0]];
+    M.box_base = M.coarse_box;
+    M.pt_base = base[i];
+    M.d_stats = U->d_stats + i;
+    M.coarse_ncta = m->coarse_ncta;
+    M.coarse_smem = m->coarse_cluster_smem;
+    std::vector<AdmJob> adm = m->hadm;
+    for (auto &J : adm) J.box = map[i][J.box];
+    M.nadm = (int)adm.size();
+    if (!upload((void **)&M.d_adm, adm.data(), sizeof(AdmJob) * adm.size()))
+      return fail_u(fail(OLGPU_ERR_OOM, "batch: device allocation failed"));
+  }
+  for (int i = 0; i < n; i++)   // the members' set-up ran on their own streams
+    if (cudaStreamSynchronize(ms[i]->stream) != cudaSuccess)
+      return fail_u(fail(OLGPU_ERR_CUDA, "batch: member set-up failed"));
+  olgpu_status st = OLGPU_OK;
+  if (precision == OLGPU_PREC_MIXED) {
+    st = prepare_mixed(U, nullptr, 0, 0);
+    for (int i = 0; i < n && st == OLGPU_OK; i++) st = prepare_mixed(ms[i], U->d_arena32, total, base[i]);
+    if (st == OLGPU_OK) st = capture_mixed(U);
+  } else {
+    st = build_graph(U);
+  }
+  if (st != OLGPU_OK) return fail_u(st);
+  U->precision = precision;
+  *out = U;
+  return OLGPU_OK;
+}
+
+extern "C" {
+
+void olgpu_batch_config_defaults(olgpu_batch_config *c)
+{
+  if (!c) return;
+  std::memset(c, 0, sizeof(*c));
+  c->device = -1;
+  c->precision = OLGPU_PREC_MIXED;
+  c->nu1 = -1;
+  c->nu2 = -1;
+  c->blocks = -1;
+}
+
+olgpu_status olgpu_batch_create(const olgpu_problem *ps, int n, const olgpu_batch_config *cfg, olgpu_batch **out)
+{
+  if (!ps || n < 1 || !out) return fail(OLGPU_ERR_INVALID_ARG, "batch: no problems");
+  *out = nullptr;
+  olgpu_batch_config c;
+  olgpu_batch_config_defaults(&c);
+  if (cfg) c = *cfg;
+  if (c.precision != OLGPU_PREC_FP64 && c.precision != OLGPU_PREC_MIXED)
+    return fail(OLGPU_ERR_INVALID_ARG, "batch: precision must be OLGPU_PREC_FP64 or OLGPU_PREC_MIXED");
+  if ((c.nu1 >= 0) != (c.nu2 >= 0) || c.nu1 > 64 || c.nu2 > 64 || (c.nu2 >= 0 && c.nu2 < 1))
+    return fail(OLGPU_ERR_INVALID_ARG, "batch: inner sweeps must be 0 <= nu1 <= 64, 1 <= nu2 <= 64 (or both < 0)");
+  for (int i = 0; i < n; i++) {
+    olgpu_status st = validate_problem(&ps[i]);
+    if (st != OLGPU_OK) return st;
+    if (ps[i].method != OLGPU_METHOD_VCYCLE) return fail(OLGPU_ERR_INVALID_ARG, "batch: V-cycles only");
+    if (c.precision == OLGPU_PREC_MIXED &&
+        (ps[i].equation >= OLGPU_EQ_POISSON || ps[i].boundary != OLGPU_BC_ROBIN))
+      return fail(OLGPU_ERR_INVALID_ARG, "batch: mixed precision is built for the puncture equations, Robin");
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(OLGPU_ERR_NO_DEVICE, "no CUDA device");
+  if (c.device >= 0) CUDA_TRY(cudaSetDevice(c.device));
+  auto *b = new olgpu_batch();
+  b->precision = c.precision;
+  // plan every member, then group them into unions
+  std::map<UnionKey, std::vector<int>> groups;
+  for (int i = 0; i < n; i++) {
+    auto *m = new olgpu_hierarchy();
+    olgpu_status st = plan_hierarchy(&ps[i], m);
+    if (st != OLGPU_OK) {
+      olgpu_hierarchy_destroy(m);
+      for (auto *x : b->members) olgpu_hierarchy_destroy(x);
+      delete b;
+      return st;
+    }
+    b->members.push_back(m);
+    const UnionKey key{m->equation >= OLGPU_EQ_POISSON ? 2 : m->equation, m->P.order,
+                       m->G.levels - m->G.mgrid_levels, m->P.boundary, m->P.nu1, m->P.nu2};
+    groups[key].push_back(i);
+  }
+  b->where.assign(n, {-1, -1});
+  olgpu_status st = OLGPU_OK;
+  std::vector<bool> owned(n, false);   // handed to a union (which destroys it)
+  for (auto &kv : groups) {
+    std::vector<int> idx = kv.second;   // deepest first: its boxes open every level
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int x, int y) { return b->members[x]->G.levels > b->members[y]->G.levels; });
+    // chunks whose every level fits one launch's box list
+    size_t at = 0;
+    while (at < idx.size() && st == OLGPU_OK) {
+      std::vector<int> chunk;
+      std::vector<int> per_level;
+      for (; at < idx.size(); at++) {
+        const olgpu_hierarchy *m = b->members[idx[at]];
+        const int Lm = m->G.levels;
+        const int Lmax = chunk.empty() ? Lm : b->members[chunk[0]]->G.levels;
+        std::vector<int> trial = per_level;
+        trial.resize(Lmax, 0);
+        for (int k = 0; k < Lm; k++) trial[k + Lmax - Lm] += m->G.boxes_in_level[k];
+        if (!chunk.empty() && *std::max_element(trial.begin(), trial.end()) > kMaxBoxesPerLevel) break;
+        per_level = trial;
+        chunk.push_back(idx[at]);
+      }
+      std::vector<olgpu_hierarchy *> ms;
+      for (int i : chunk) {
+        ms.push_back(b->members[i]);
+        owned[i] = true;
+      }
+      olgpu_hierarchy *U = nullptr;
+      st = build_union(ms, c.precision, c.nu1, c.nu2, c.blocks, &U);
+      if (st != OLGPU_OK) break;
+      for (size_t q = 0; q < chunk.size(); q++) b->where[chunk[q]] = {(int)b->unions.size(), (int)q};
+      b->unions.push_back(U);
+    }
+    if (st != OLGPU_OK) break;
+  }
+  if (st != OLGPU_OK) {
+    for (int i = 0; i < n; i++)
+      if (!owned[i]) olgpu_hierarchy_destroy(b->members[i]);
+    for (auto *U : b->unions) olgpu_hierarchy_destroy(U);
+    delete b;
+    return st;
+  }
+  *out = b;
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_batch_destroy(olgpu_batch *b)
+{
+  if (!b) return OLGPU_OK;
+  for (auto *U : b->unions) olgpu_hierarchy_destroy(U);
+  delete b;
+  return OLGPU_OK;
+}
+
+int olgpu_batch_size(const olgpu_batch *b) { return b ? (int)b->members.size() : 0; }
+int olgpu_batch_unions(const olgpu_batch *b) { return b ? (int)b->unions.size() : 0; }
+
+int olgpu_batch_kernels_per_cycle(const olgpu_batch *b)
+{
+  if (!b) return 0;
+  int k = 0;
+  for (auto *U : b->unions) k += b->precision == OLGPU_PREC_MIXED ? U->launches_mixed : U->launches;
+  return k;
+}
+
+olgpu_hierarchy *olgpu_batch_member(olgpu_batch *b, int i)
+{
+  return b && i >= 0 && i < (int)b->members.size() ? b->members[i] : nullptr;
+}
+
+olgpu_status olgpu_batch_reset(olgpu_batch *b)
+{
+  if (!b) return fail(OLGPU_ERR_INVALID_ARG, "null batch");
+  for (auto *m : b->members) {
+    olgpu_status st = olgpu_reset(m);
+    if (st != OLGPU_OK) return st;
+  }
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_batch_solve(olgpu_batch *b, const olgpu_stop_rule *rule, olgpu_report *reports)
+{
+  if (!b) return fail(OLGPU_ERR_INVALID_ARG, "null batch");
+  const int n = (int)b->members.size();
+  std::vector<SolveTrack> T(n);
+  for (int i = 0; i < n; i++) {
+    olgpu_status st = make_track(b->members[i], rule, T[i]);
+    if (st != OLGPU_OK) return st;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  olgpu_status worst = OLGPU_OK;
+  std::vector<int> live(b->unions.size(), 0);
+  for (size_t u = 0; u < b->unions.size(); u++) {   // every box active, then the first cycle
+    olgpu_hierarchy *U = b->unions[u];
+    CUDA_TRY(cudaSetDevice(U->device));
+    for (auto &B : U->hboxes) B.active = 1;
+    CUDA_TRY(cudaMemcpyAsync(U->d_boxes, U->hboxes.data(), sizeof(DevBox) * U->hboxes.size(), cudaMemcpyHostToDevice,
+                             U->stream));
+    live[u] = (int)U->members.size();
+    olgpu_status st = cycle_enqueue(U);
+    if (st != OLGPU_OK) return st;
+  }
+  int remaining = n;
+  while (remaining > 0) {
+    bool progressed = false;
+    for (size_t u = 0; u < b->unions.size(); u++) {
+      if (live[u] == 0) continue;
+      olgpu_hierarchy *U = b->unions[u];
+      const cudaError_t e = cudaEventQuery(U->ev_cycle);
+      if (e == cudaErrorNotReady) continue;
+      if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("batch cycle: ") + cudaGetErrorString(e));
+      progressed = true;
+      bool dirty = false;
+      for (int q = 0; q < (int)U->members.size(); q++) {
+        olgpu_hierarchy *m = U->members[q].h;
+        const int i = (int)(std::find(b->members.begin(), b->members.end(), m) - b->members.begin());
+        if (T[i].done) continue;
+        double r = 0;
+        const olgpu_status s = cycle_finish(m, &r);
+        if (!T[i].step(m, s, r)) continue;
+        T[i].done = true;   // this solve stops: its boxes are left as they are from now on
+        if (s != OLGPU_OK) worst = s;
+        for (auto &B : U->hboxes)
+          if (B.solve == q) B.active = 0;
+        dirty = true;
+        live[u]--;
+        remaining--;
+      }
+      if (live[u] == 0) continue;
+      if (dirty)
+        CUDA_TRY(cudaMemcpyAsync(U->d_boxes, U->hboxes.data(), sizeof(DevBox) * U->hboxes.size(),
+                                 cudaMemcpyHostToDevice, U->stream));
+      olgpu_status st = cycle_enqueue(U);
+      if (st != OLGPU_OK) return st;
+    }
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
+  for (auto *U : b->unions) CUDA_TRY(cudaStreamSynchronize(U->stream));
+  b->last_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  for (int i = 0; i < n; i++) close_track(b->members[i], T[i], reports ? &reports[i] : nullptr);
+  return worst;
+}
+
+double olgpu_batch_last_ms(const olgpu_batch *b) { return b ? b->last_ms : 0.0; }
+
+}  // extern "C"
+
+// ============================================================================
 // Non-allocating single-box smoother (olgpu_smooth_box_noalloc)
 //
 // Its scratch is one fixed file-scope device array: the box descriptor the
-// kernel reads, one norm accumulator per sweep and the NaN flag.  In host code
+// kernel reads and a Stats record (the norm accumulator of sweep s in
+// slots[s], the NaN flag).  In host code
 // the symbol is only a stand-in, so each device's address of it is looked up
 // once with cudaGetSymbolAddress (with that device current) and passed to the
 // kernels.
@@ -2386,10 +3003,11 @@ namespace {
 
 constexpr int kNoAllocWords = 256;                    // 2 KiB
 constexpr int kNoAllocBoxWords = 32;                  // DevBox, rounded up
-constexpr int kNoAllocNormOff = kNoAllocBoxWords;     // OLGPU_NOALLOC_MAX_SWEEPS slots
-constexpr int kNoAllocNanOff = kNoAllocNormOff + OLGPU_NOALLOC_MAX_SWEEPS;
+constexpr int kNoAllocStatsOff = kNoAllocBoxWords;    // then one Stats record
 static_assert(sizeof(DevBox) <= kNoAllocBoxWords * sizeof(unsigned long long), "box slot too small");
-static_assert(kNoAllocNanOff + 1 <= kNoAllocWords, "scratch too small");
+static_assert(kNoAllocStatsOff * sizeof(unsigned long long) + sizeof(Stats) <=
+                  kNoAllocWords * sizeof(unsigned long long), "scratch too small");
+static_assert(OLGPU_NOALLOC_MAX_SWEEPS <= kSlotDu, "one norm slot per sweep");
 
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocWords];
 
@@ -2442,8 +3060,8 @@ void noalloc_sweeps(const BoxList &L, const DevBox *box, const DevFields &F, int
 {
   for (int s = 0; s < sweeps; s++)
     for (int color = 0; color < num_colors<ORD>(); color++)
-      k_smooth_color<ORD, EQ><<<L.blk[L.count], kSmoothThreads, 0, st>>>(L, box, F, color, scr + kNoAllocNormOff + s,
-                                                                   reinterpret_cast<int *>(scr + kNoAllocNanOff));
+      k_smooth_color<ORD, EQ><<<L.blk[L.count], kSmoothThreads, 0, st>>>(
+          L, box, F, color, reinterpret_cast<Stats *>(scr + kNoAllocStatsOff), s);   // level 0: slots[s]
 }
 
 template <int EQ>
@@ -2485,12 +3103,14 @@ extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int 
   B.n[2] = f->nz;
   B.buf = buf;
   B.off = 0;
+  B.level = 0;
+  B.solve = 0;
+  B.active = 1;
   const double d[3] = {f->dx, f->dy, f->dz};
   set_box_stencil(B, f->order, d);
   // the descriptor and the zeroed accumulators go into the fixed scratch
   NOALLOC_TRY(cudaMemcpyAsync(scr, &B, sizeof(DevBox), cudaMemcpyHostToDevice, cs));
-  NOALLOC_TRY(cudaMemsetAsync(scr + kNoAllocNormOff, 0,
-                           sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1), cs));
+  NOALLOC_TRY(cudaMemsetAsync(scr + kNoAllocStatsOff, 0, sizeof(Stats), cs));
   DevFields F{};
   F.f[F_U] = f->u;
   F.f[F_B] = const_cast<double *>(f->b);
@@ -2499,22 +3119,20 @@ extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int 
   F.f[F_D] = const_cast<double *>(f->d);
   F.f[F_E] = const_cast<double *>(f->e);
   BoxList L{};
-  L.first = 0;
   L.count = 1;
+  L.box[0] = 0;
   L.blk[0] = 0;
   L.blk[1] = (int)blocks_color(B);
   const DevBox *dbox = reinterpret_cast<const DevBox *>(scr);
   if (f->d) noalloc_dispatch<1>(f->order, L, dbox, F, sweeps, scr, cs);
   else noalloc_dispatch<0>(f->order, L, dbox, F, sweeps, scr, cs);
   NOALLOC_TRY(cudaGetLastError());
-  unsigned long long host[OLGPU_NOALLOC_MAX_SWEEPS + 1];
-  NOALLOC_TRY(cudaMemcpyAsync(host, scr + kNoAllocNormOff, sizeof(unsigned long long) * (OLGPU_NOALLOC_MAX_SWEEPS + 1),
-                           cudaMemcpyDeviceToHost, cs));
+  Stats host;
+  NOALLOC_TRY(cudaMemcpyAsync(&host, scr + kNoAllocStatsOff, sizeof(Stats), cudaMemcpyDeviceToHost, cs));
   NOALLOC_TRY(cudaStreamSynchronize(cs));
   if (norms)
-    for (int s = 0; s < sweeps; s++) std::memcpy(&norms[s], &host[s], sizeof(double));
-  int nan_flag = 0;
-  std::memcpy(&nan_flag, &host[OLGPU_NOALLOC_MAX_SWEEPS], sizeof(int));
+    for (int s = 0; s < sweeps; s++) std::memcpy(&norms[s], &host.slots[s], sizeof(double));
+  const int nan_flag = host.nan_flag;
   if (nan_flag) return fail(OLGPU_ERR_NAN, "NaN in the smoother");
   return OLGPU_OK;
 }

@@ -52,7 +52,7 @@ __host__ __device__ inline int slab_max_planes(int n2, int b, int ncta)
 
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
-    k_smooth32_cluster(const DevBox *__restrict__ boxes, int first_box, DevFields32 G, int sweeps, int *nan_flag)
+    k_smooth32_cluster(const DevBox *__restrict__ boxes, BoxList L, DevFields32 G, int sweeps, Stats *stats)
 {
   namespace cg = cooperative_groups;
   constexpr int NC = num_colors<ORD>();
@@ -62,7 +62,9 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
   float *se = reinterpret_cast<float *>(s_slab4);
   __shared__ const float *plane[kMaxClusterPlanes];
 
-  const DevBox B = boxes[first_box + (int)blockIdx.x / ncta];
+  const DevBox B = boxes[L.box[(int)blockIdx.x / ncta]];
+  if (!B.active) return;   // every block of the cluster reads the same box: all leave
+  int *nan_flag = &stats[B.solve].nan_flag;
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2], b = B.buf;
   const int n01 = n0 * n1;
   const int z0 = slab_begin(rank, n2, b, ncta), z1 = slab_begin(rank + 1, n2, b, ncta);
