@@ -138,6 +138,10 @@ typedef struct {
   double res[256];              /* per-cycle top-level norms (first 256)  */
   double final_du;              /* the last cycle's largest change of u on
                                    the points the discrete system fixes   */
+  double final_part;            /* the last cycle's residual part: FP64, the
+                                   top-level norm (= final_res); mixed, the
+                                   finest FP64 defect (final_res is the larger
+                                   of it and the cycle's largest correction) */
 } olgpu_report;
 
 typedef struct olgpu_hierarchy olgpu_hierarchy;

@@ -430,6 +430,9 @@ class Batch:
             out.append(bi)
         return out
 
+    def mgrid_levels(self, i: int) -> int:
+        return self.lib.olgpu_mgrid_levels(self._member(i))
+
     def get_field(self, i: int, box: int, name: str = "u") -> np.ndarray:
         h = self._member(i)
         bi = _abi.BoxInfo()

@@ -48,7 +48,7 @@ class StopRule(C.Structure):
 class Report(C.Structure):
     _fields_ = [
         ("cycles", C.c_int), ("status", C.c_int), ("final_res", C.c_double),
-        ("adm", _D16), ("res", C.c_double * 256), ("final_du", C.c_double),
+        ("adm", _D16), ("res", C.c_double * 256), ("final_du", C.c_double), ("final_part", C.c_double),
     ]
 
 

@@ -364,7 +364,11 @@ __host__ __device__ constexpr int num_colors() { return ORD / 2 + 1; }
 
 // The pass's residual maximum goes to stats[B.solve].slots[2 * B.level +
 // post] (the level's pre- or post-smoothing norm), a NaN to its nan_flag.
-template <int ORD, int EQ>
+// PTS points of a row per thread (its colour's points ih*PTS .. ih*PTS+PTS-1):
+// every point's loads and arithmetic before any store -- points of one
+// colour do not read each other -- so the latencies of the points overlap;
+// each point's update is the same expression, so any PTS gives the same bits.
+template <int ORD, int EQ, int PTS = 1>
 __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *__restrict__ boxes,
                                                       DevFields F, int color, Stats *stats, int post)
 {
@@ -378,30 +382,42 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
   const int b = B.buf;
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const int H = (m0 + NC - 1) / NC;
+  const int HP = (H + PTS - 1) / PTS;
   const long long t = lb * blockDim.x + threadIdx.x;
-  const long long total = (long long)H * m1 * m2;
+  const long long total = (long long)HP * m1 * m2;
   double rabs = 0.0;
   if (t < total) {
-    const int ih = ((int)t % H);
-    const int r = (int)t / H;
+    const int ihp = ((int)t % HP);
+    const int r = (int)t / HP;
     const int j = b + (r % m1);
     const int k = b + (r / m1);
     const int delta = (((color - b - j - k) % NC) + NC) % NC;
-    const int i = b + delta + NC * ih;
-    if (i < B.n[0] - b) {
-      double *u = F.f[F_U] + B.off;
-      const long long sy = B.n[0], sz = (long long)B.n[0] * B.n[1];
-      const long long p = pidx(B, i, j, k);
+    double *u = F.f[F_U] + B.off;
+    const long long sy = B.n[0], sz = (long long)B.n[0] * B.n[1];
+    double un[PTS];
+    long long pp[PTS];
+    bool ok[PTS];
+#pragma unroll
+    for (int q = 0; q < PTS; q++) {
+      const int i = b + delta + NC * (ihp * PTS + q);
+      ok[q] = i < B.n[0] - b;
+      pp[q] = pidx(B, ok[q] ? i : b + delta, j, k);   // a point past the row's end repeats its first point
+      const long long p = pp[q];
       const double lv = lap<ORD>(u, p, sy, sz, B);
       double op, dop;
       point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
                    EQ == 1 ? F.f[F_D][B.off + p] : 0.0, EQ == 1 ? F.f[F_E][B.off + p] : 0.0, op, dop);
       const double R = op - F.f[F_RHO][B.off + p];
-      const double un = u[p] - R * step_inverse(dop);
-      u[p] = un;
-      rabs = fabs(R);
-      if (is_nan_bits(un)) atomicOr(nan_flag, 1);
+      un[q] = u[p] - R * step_inverse(dop);
+      const double a = fabs(R);
+      if (ok[q] && (a > rabs || is_nan_bits(a))) rabs = a;   // a NaN stays the maximum
     }
+#pragma unroll
+    for (int q = 0; q < PTS; q++)
+      if (ok[q]) {
+        u[pp[q]] = un[q];
+        if (is_nan_bits(un[q])) atomicOr(nan_flag, 1);
+      }
   }
   block_max_atomic(rabs, norm_slot);
 }

@@ -126,6 +126,22 @@ __global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__re
   if (norm_slot) block_max_atomic(rabs, norm_slot);
 }
 
+// Colour-packed position of INSIDE point (i, j, k) of a box: the points of
+// colour c = (i + j + k) mod NC, row by row (plane k, row j), in the order the
+// colour pass visits them (ih = the point's index among its row's colour-c
+// points), so that a colour pass reads its points' coefficients contiguously.
+// Every index is below NC * m2 * m1 * ceil(m0 / NC) <= the box's points.
+template <int ORD>
+__host__ __device__ __forceinline__ long long packed_index(const DevBox &B, int i, int j, int k)
+{
+  constexpr int NC = ORD / 2 + 1;
+  const int b = B.buf;
+  const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
+  const int H = (m0 + NC - 1) / NC;
+  const int c = (i + j + k) % NC;
+  return (((long long)c * m2 + (k - b)) * m1 + (j - b)) * H + (i - b) / NC;
+}
+
 // The FP64 preparation of one level in one pass: on INSIDE points the
 // coefficients of the correction operator, A = b/(c+u)^7 and 1/(c+u) (and d,
 // E5 = e (c+u)^5 for the scalar field; nothing reads them on the ghosts) and
@@ -133,7 +149,7 @@ __global__ void __launch_bounds__(256) k_mx_defect(BoxList L, const DevBox *__re
 // k_mx_defect).
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                 DevFields32 G)
+                                                 DevFields32 G, float2 *__restrict__ aq)
 {
   long long lb;
   const DevBox B = boxes[list_box(L, lb)];
@@ -159,6 +175,7 @@ __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__rest
   const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
   G.f[G_A][p] = (float)t7;
   G.f[G_IQ][p] = (float)iq;
+  if (aq) aq[B.off + packed_index<ORD>(B, i, j, k)] = make_float2((float)t7, (float)iq);
   double q4 = 0.0;
   if (EQ == 1) {
     const double q2 = q * q;

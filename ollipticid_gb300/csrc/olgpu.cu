@@ -110,6 +110,7 @@ struct olgpu_hierarchy {
   int precision = OLGPU_PREC_FP64;
   float *d_arena32 = nullptr;
   DevFields32 F32{};
+  float2 *d_aq = nullptr;           // (A, 1/(c+u)) colour-packed for the cluster smoother
   std::vector<Transfer> restrict_e, xfer_w32, set_in32, prolong_v32, ghost_e;
   cudaGraphExec_t graph_mixed = nullptr;
   int launches_mixed = 0;
@@ -154,6 +155,8 @@ struct olgpu_hierarchy {
   // the Robin walk as separate face, edge and corner launches (off: one
   // launch of a cluster per box); the two give the same bits
   bool robin_split = std::getenv("OLGPU_ROBIN_SPLIT") != nullptr;
+  // FP64 smoother points per thread (1 or 2: OLGPU_SMOOTH_PTS); the same bits
+  int smooth_pts = std::getenv("OLGPU_SMOOTH_PTS") && std::atoi(std::getenv("OLGPU_SMOOTH_PTS")) == 2 ? 2 : 1;
   // The solves this hierarchy steps: alone, one (itself); a union of solves
   // (olgpu_batch) steps every member's boxes in shared launches, their levels
   // aligned from the top (a member's level k is the union's level k + off).
@@ -226,6 +229,14 @@ long long blocks_color(const DevBox &B)
   const int nc = b + 1;   // colours: order/2 + 1 (2 for the order-2 boxes)
   const long long H = (B.n[0] - 2 * b + nc - 1) / nc;
   return cdiv(H * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kSmoothThreads);
+}
+
+long long blocks_color2(const DevBox &B)   // two points of a row per thread
+{
+  const int b = B.buf;
+  const int nc = b + 1;
+  const long long H = (B.n[0] - 2 * b + nc - 1) / nc;
+  return cdiv((H + 1) / 2 * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kSmoothThreads);
 }
 
 long long blocks_faces(const DevBox &B)
@@ -560,12 +571,17 @@ void launch_clusters(olgpu_hierarchy *h, void (*kern)(KArgs...), unsigned grid, 
 template <int ORD, int EQ>
 void launch_smooth(olgpu_hierarchy *h, int level, int nu, int slot)
 {
-  const BoxList L = level_list(h, level, blocks_color);
+  const bool two = h->smooth_pts == 2;   // two points of a row per thread
+  const BoxList L = level_list(h, level, two ? blocks_color2 : blocks_color);
   const int nb = L.blk[L.count];
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
-      launch_pdl(h, k_smooth_color<ORD, EQ>, (unsigned)nb, (unsigned)kSmoothThreads, L,
-                 (const DevBox *)h->d_boxes, h->F, color, h->d_stats0, slot - 2 * level);
+      if (two)
+        launch_pdl(h, k_smooth_color<ORD, EQ, 2>, (unsigned)nb, (unsigned)kSmoothThreads, L,
+                   (const DevBox *)h->d_boxes, h->F, color, h->d_stats0, slot - 2 * level);
+      else
+        launch_pdl(h, k_smooth_color<ORD, EQ, 1>, (unsigned)nb, (unsigned)kSmoothThreads, L,
+                   (const DevBox *)h->d_boxes, h->F, color, h->d_stats0, slot - 2 * level);
       h->launches++;
     }
 }
@@ -707,7 +723,13 @@ bool cluster_fits(olgpu_hierarchy *h, size_t smem)
     cudaGetLastError();
     return false;
   }
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  // the limit is per kernel and process-wide: always the device's maximum,
+  // so that a hierarchy with a smaller coarsest grid never lowers it below
+  // what another one's captured cycle launches with
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) != cudaSuccess ||
+      (size_t)optin < smem ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
@@ -994,7 +1016,7 @@ void launch_smooth32_cluster(olgpu_hierarchy *h, int level, int nu)
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k_smooth32_cluster<ORD, EQ>, (const DevBox *)h->d_boxes, level_list(h, level, blocks_all),
-                     h->F32, nu, h->d_stats0);
+                     h->F32, (const float2 *)h->d_aq, nu, h->d_stats0);
   h->launches_mixed++;
 }
 
@@ -1241,11 +1263,13 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   // FP64: coefficients of the correction operator and the defect source
   for (int l = 0; l < L; l++) {
     const BoxList BL = level_list(h, l, blocks_all, true);
+    // the cluster smoother reads (A, 1/(c+u)) colour-packed
+    float2 *aq = h->sc_ncta.size() > (size_t)l && h->sc_ncta[l] > 0 ? h->d_aq : nullptr;
     switch (level_order(h, l)) {
-    case 2: k_mx_prep<2, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
-    case 4: k_mx_prep<4, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
-    case 6: k_mx_prep<6, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
-    default: k_mx_prep<8, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32); break;
+    case 2: k_mx_prep<2, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, aq); break;
+    case 4: k_mx_prep<4, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, aq); break;
+    case 6: k_mx_prep<6, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, aq); break;
+    default: k_mx_prep<8, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, aq); break;
     }
     if (l <= mg) {
       if (level_order(h, l) == 2)
@@ -1332,7 +1356,9 @@ olgpu_status prepare_mixed(olgpu_hierarchy *h, float *arena32, long long stride,
   const bool member = arena32 != nullptr;
   if (!member) {
     const size_t bytes = sizeof(float) * (size_t)h->total_pts * G_NUM;
-    if (cudaMalloc(&h->d_arena32, bytes) != cudaSuccess) return fail(OLGPU_ERR_OOM, "FP32 arena allocation failed");
+    if (cudaMalloc(&h->d_arena32, bytes) != cudaSuccess ||
+        cudaMalloc(&h->d_aq, sizeof(float2) * (size_t)h->total_pts) != cudaSuccess)
+      return fail(OLGPU_ERR_OOM, "FP32 arena allocation failed");
     CUDA_TRY(cudaMemset(h->d_arena32, 0, bytes));
     arena32 = h->d_arena32;
     stride = h->total_pts;
@@ -1901,6 +1927,7 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   if (h->owns_arena32) cudaFree(h->d_arena32);
+  cudaFree(h->d_aq);
   cudaFree(h->d_and);
   cudaFree(h->d_pinned);
   cudaFree(h->d_and_state);
@@ -2063,7 +2090,7 @@ struct SolveTrack {
   olgpu_stop_rule R;
   double tol, du_tol;
   double res = 1e12, res_prev = 1e12;
-  double du = 0;
+  double du = 0, part = 0;
   int cycles = 0;
   bool done = false;
   olgpu_status status = OLGPU_OK;
@@ -2072,17 +2099,18 @@ struct SolveTrack {
   // Records one finished cycle (r: its norm; part: its residual part;
   // change: its largest change of u); returns true once the rule stops the
   // solve.
-  bool step(olgpu_status s, double r, double part, double change)
+  bool step(olgpu_status s, double r, double part_, double change)
   {
     res_prev = res;
     res = r;
     du = change;
+    part = part_;
     if (cycles < 256) rep.res[cycles] = r;
     cycles++;
     status = s;
     if (s != OLGPU_OK || cycles >= R.max_cycles) return true;
     if (R.stop == OLGPU_STOP_FIXED) return false;
-    if (R.stop == OLGPU_STOP_ERROR) return part <= tol && change <= du_tol;   // a NaN never stops it
+    if (R.stop == OLGPU_STOP_ERROR) return part_ <= tol && change <= du_tol;   // a NaN never stops it
     if (!(res > tol)) return true;
     if (R.stop == OLGPU_STOP_REFERENCE && !(res < res_prev)) return true;
     return false;
@@ -2123,6 +2151,7 @@ static void close_track(olgpu_hierarchy *h, SolveTrack &T, olgpu_report *out)
   T.rep.status = T.status;
   T.rep.final_res = T.res;
   T.rep.final_du = T.du;
+  T.rep.final_part = T.part;
   for (int i = 0; i < h->P.numbh; i++) T.rep.adm[i] = h->adm[i];
   if (out) *out = T.rep;
 }
@@ -2438,6 +2467,7 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
     for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
       for (auto &X : *vec) { cudaFree(X.d_jobs); X.d_jobs = nullptr; }
     cudaFree(h->d_arena32); h->d_arena32 = nullptr;
+    cudaFree(h->d_aq); h->d_aq = nullptr;
     h->mixed_ready = false;
     cudaFree(h->d_and); h->d_and = nullptr;
     cudaFree(h->d_and_state); h->d_and_state = nullptr;
@@ -2742,6 +2772,22 @@ static olgpu_status build_union(std::vector<olgpu_hierarchy *> ms, int precision
     }
     for (auto *vec : {&U->restrict_u, &U->xfer_w, &U->set_in, &U->prolong_v, &U->ghost_u, &U->ghost_lo})
       finish_plan((*vec)[A]);
+    if (std::getenv("OLGPU_VERBOSE")) {
+      auto flags = [](const Transfer &X) {
+        return std::to_string(X.jobs.size()) + (X.strided ? "s" : "") + (X.rows ? "r" : "") + std::to_string(X.width);
+      };
+      std::fprintf(stderr, "olgpu union level %d: restrict %s xfer_w %s set_in %s prolong %s ghost %s |", A,
+                   flags(U->restrict_u[A]).c_str(), flags(U->xfer_w[A]).c_str(), flags(U->set_in[A]).c_str(),
+                   flags(U->prolong_v[A]).c_str(), flags(U->ghost_u[A]).c_str());
+      for (int i = 0; i < n; i++) {
+        const int k = A - off[i];
+        if (k < 1) continue;
+        std::fprintf(stderr, " m%d k%d: %s %s %s %s %s", i, k, flags(ms[i]->restrict_u[k]).c_str(),
+                     flags(ms[i]->xfer_w[k]).c_str(), flags(ms[i]->set_in[k]).c_str(),
+                     flags(ms[i]->prolong_v[k]).c_str(), flags(ms[i]->ghost_u[k]).c_str());
+      }
+      std::fprintf(stderr, "\n");
+    }
   }
   auto upload = [&](void **dst, const void *src, size_t bytes) -> bool {
     if (bytes == 0) return true;

@@ -24,10 +24,11 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 // device bytes per point: 12 FP64 fields and a mask byte; mixed precision
-// adds 11 FP32 fields and 9 FP32 Anderson vectors; plus a fixed allowance
+// adds 11 FP32 fields, the colour-packed (A, 1/(c+u)) pairs and 9 FP32
+// Anderson vectors; plus a fixed allowance
 // for plans, tables and graphs
 constexpr long long kBytesPerPointFP64 = 12 * 8 + 1;
-constexpr long long kBytesPerPointMixed = 12 * 8 + 11 * 4 + 9 * 4 + 1;
+constexpr long long kBytesPerPointMixed = 12 * 8 + 11 * 4 + 2 * 4 + 9 * 4 + 1;
 constexpr long long kFixedBytes = 64LL << 20;
 
 struct Request {

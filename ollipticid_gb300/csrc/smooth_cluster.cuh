@@ -52,7 +52,8 @@ __host__ __device__ inline int slab_max_planes(int n2, int b, int ncta)
 
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
-    k_smooth32_cluster(const DevBox *__restrict__ boxes, BoxList L, DevFields32 G, int sweeps, Stats *stats)
+    k_smooth32_cluster(const DevBox *__restrict__ boxes, BoxList L, DevFields32 G, const float2 *__restrict__ aq,
+                       int sweeps, Stats *stats)
 {
   namespace cg = cooperative_groups;
   constexpr int NC = num_colors<ORD>();
@@ -80,9 +81,10 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
 
   const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
   const float dl = (float)B.dulap;
-  const float *gs = G.f[G_S] + B.off, *ga = G.f[G_A] + B.off, *giq = G.f[G_IQ] + B.off;
+  const float *gs = G.f[G_S] + B.off;
+  const float2 *gaq = aq + B.off;   // (A, 1/(c+u)) colour-packed (packed_index)
   const float *gd = EQ == 1 ? G.f[G_D] + B.off : nullptr, *ge5 = EQ == 1 ? G.f[G_E5] + B.off : nullptr;
-  const int m0 = n0 - 2 * b, m1 = n1 - 2 * b;
+  const int m0 = n0 - 2 * b, m1 = n1 - 2 * b, m2 = n2 - 2 * b;
   const int ka = z0 > b ? z0 : b, kb = z1 < n2 - b ? z1 : n2 - b;
   const int nk = kb > ka ? kb - ka : 0;
   const int H = (m0 + NC - 1) / NC;
@@ -105,6 +107,7 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
       for (int t = t0; t < total; t += U * S) {
         float en[U];
         int qq[U], kk[U];
+        int pk[U];   // the point's colour-packed position
         bool ok[U];
 #pragma unroll
         for (int u = 0; u < U; u++) {
@@ -114,6 +117,7 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
           ok[u] = t + u * S < total && i < n0 - b;
           kk[u] = ok[u] ? k : ka;
           qq[u] = ok[u] ? j * n0 + i : b * n0 + b;
+          pk[u] = ok[u] ? ((color * m2 + (k - b)) * m1 + jr) * H + ih : 0;
           ih += s_ih;
           jr += s_j;
           kr += s_k;
@@ -136,7 +140,8 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
               ix2, iy2, iz2);
           const int p = k * n01 + q;
           float op, dop;
-          corr_op<EQ>(lv, dl, c, __ldg(ga + p), __ldg(giq + p), EQ == 1 ? __ldg(gd + p) : 0.0f, EQ == 1 ? __ldg(ge5 + p) : 0.0f,
+          const float2 aqv = __ldg(gaq + pk[u]);
+          corr_op<EQ>(lv, dl, c, aqv.x, aqv.y, EQ == 1 ? __ldg(gd + p) : 0.0f, EQ == 1 ? __ldg(ge5 + p) : 0.0f,
                       op, dop);
           const float R = op - __ldg(gs + p);
           en[u] = c - R * rcp_fast(dop);

@@ -29,9 +29,9 @@ from . import Elliptic, Problem, _abi
 from ._abi import check
 
 # device bytes per point: 12 FP64 fields and one mask byte (the points the
-# discrete system fixes); mixed precision adds 11 FP32 fields and 9 FP32
-# Anderson vectors
-BYTES_PER_POINT_MIXED = 12 * 8 + 11 * 4 + 9 * 4 + 1
+# discrete system fixes); mixed precision adds 11 FP32 fields, the
+# colour-packed (A, 1/(c+u)) pairs and 9 FP32 Anderson vectors
+BYTES_PER_POINT_MIXED = 12 * 8 + 11 * 4 + 2 * 4 + 9 * 4 + 1
 BYTES_PER_POINT_FP64 = 12 * 8 + 1
 
 

@@ -124,7 +124,7 @@ def test_benchmark_stop_lands_within_the_bar(name, mixed):
     with og.Elliptic(P) as E:
         E.set_precision(mixed)
         rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=BENCH_DU_TOL)
-        assert rep.final_res <= P.tol and rep.final_du <= BENCH_DU_TOL
+        assert rep.final_part <= P.tol and rep.final_du <= BENCH_DU_TOL
         err = sampled_error(E, g)
         adm = E.ADM_mass
     assert err <= U_TOL, f"{name} mixed={mixed}: max|u - u_ref| = {err:.3e} after {rep.cycles} cycles"
