@@ -600,6 +600,76 @@ def run_served(rates=(4.0, 16.0, 64.0), count: int = 24, inner_sweeps=None, nati
     return out
 
 
+def served_binary_error(u, P, inst, fx):
+    """max |u - u_oracle| of a served result of workload instance inst at the
+    fixture's sample points (multigrid coarse ghosts excluded)."""
+    import ctypes as C
+    import numpy as np
+    from ollipticid_gb300 import _abi
+    lib = _abi.load()
+    cp = P.to_c()
+    out = (_abi.BoxInfo * 256)()
+    nb, mg = C.c_int(), C.c_int()
+    lib.olgpu_plan_boxes(C.byref(cp), out, 256, C.byref(nb), None, C.byref(mg))
+    worst = 0.0
+    for g in range(nb.value):
+        bi = out[g]
+        idx = fx[f"inst{inst}_idx_b{g}"].astype(np.int64)
+        want = fx[f"inst{inst}_fixed_u_b{g}"]
+        if bi.level < mg.value:
+            k, rem = np.divmod(idx, bi.nx * bi.ny)
+            j, i = np.divmod(rem, bi.nx)
+            w = bi.buf
+            keep = (i >= w) & (i < bi.nx - w) & (j >= w) & (j < bi.ny - w) & (k >= w) & (k < bi.nz - w)
+            idx, want = idx[keep], want[keep]
+        worst = max(worst, float(np.max(np.abs(u[g].ravel()[idx] - want))))
+    return worst
+
+
+def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None, plain_sample: int = 8):
+    """The batched workload's binaries as a Poisson request stream at a
+    saturating rate through the library's C++ server (continuous batching:
+    requests admitted as slots and memory free up, each on its own stream,
+    their cycles overlapping on the GPU), mixed precision, residual <= 1e-10
+    and change of u <= DU_TOL.  Throughput, p50/p99 latency, the results of
+    the instances with oracle fixtures against them, and the plain FP64
+    solver's rate on the same binaries (a sample solved one at a time)."""
+    import numpy as np
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi, workloads
+    from ollipticid_gb300.serve import NativeServer
+    path = os.path.join(GOLDEN, "batched.npz")
+    fx = np.load(path) if os.path.exists(path) else None
+    with_fx = set(int(i) for i in fx["instances"]) if fx is not None else set()
+    stream = workloads.served_binaries(count, rate)
+    with NativeServer(mem_budget=200 << 30, max_active=32, builders=8, inner_sweeps=inner_sweeps,
+                      stop=_abi.STOP_ERROR, tol=1e-10, du_tol=DU_TOL, keep_u=True, keep_only=with_fx,
+                      max_cycles=300) as S:
+        rep = S.run(stream)
+    errs = [served_binary_error(r.u, stream[i][1], i, fx) for i, r in enumerate(rep["results"])
+            if i in with_fx and r.u is not None]
+    # the plain FP64 solver on a sample of the same binaries, one at a time
+    plain_ms = []
+    for P in workloads.batched_binaries(plain_sample):
+        with og.Elliptic(P) as E:
+            E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)   # warm
+            E.reset()
+            E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)
+            plain_ms.append(E.last_device_ms)
+    plain_rate = len(plain_ms) / (sum(plain_ms) / 1000.0)
+    statuses = [r.status for r in rep["results"]]
+    return {"workload": f"{count} seeded binaries of the batched workload as a Poisson stream at {rate:g} "
+                        f"requests/s, C++ server (olgpu_server_*), mixed precision, residual <= 1e-10 and change "
+                        f"of u <= {DU_TOL:g}",
+            **{k: rep[k] for k in ("throughput_solves_per_s", "latency_p50_s", "latency_p99_s", "latency_max_s",
+                                   "cycles_mean", "peak_concurrent_solves", "makespan_s")},
+            "failed": sum(1 for x in statuses if x != 0),
+            "oracle_checked_results": len(errs), "max_abs_u_minus_oracle": max(errs) if errs else None,
+            "plain_fp64_same_binaries_solves_per_s": plain_rate,
+            "plain_fp64_sample": f"the first {plain_sample} binaries solved alone in FP64, device time",
+            "vs_plain_fp64": rep["throughput_solves_per_s"] / plain_rate}
+
+
 def slowest_rank_ms(ms: float, world: int, device) -> float:
     """The timed region's length: the maximum over ranks (replicas run the
     same work; the job is done when the slowest one is)."""
@@ -688,7 +758,7 @@ def run_gpu(args, rank: int, world: int, local: int):
     # ---- the same workload with the mixed-precision cycle
     mixed = run_mixed(E, P, args, dev, u_fix, fx)
 
-    concurrent = batched = served = config3 = convergence = approx_start = None
+    concurrent = batched = served = served_binaries = config3 = convergence = approx_start = None
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, fx, value / world)
@@ -698,6 +768,7 @@ def run_gpu(args, rank: int, world: int, local: int):
         approx_start = run_approx_start()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
+        served_binaries = run_served_binaries(inner_sweeps=tuple(concurrent["inner_sweeps"]))
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
     # multicolour smoother (k_smooth_color) on the finest level, timed with
@@ -740,7 +811,8 @@ def run_gpu(args, rank: int, world: int, local: int):
                       "final_res": reps[-1].final_res, "final_du": reps[-1].final_du,
                       "adm": [reps[-1].adm[0], reps[-1].adm[1]], "wall_s": wall},
             "accuracy": accuracy,
-            "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served, "config3": config3,
+            "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served,
+            "served_binaries": served_binaries, "config3": config3,
             "convergence": convergence, "approx_start": approx_start,
             "roofline": roof, "roofline_fp32_smoother": roof32, "fma_peaks": fma, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches,

@@ -521,100 +521,138 @@ __global__ void __launch_bounds__(64) k_robin_edges_corners(BoxList L, const Dev
 }
 
 // ----------------------------------------------------------------------------
-// Robin boundary in one launch: one thread-block cluster per box walks every
-// face column (layers inner -> outer), then -- after a cluster barrier --
-// every edge, then -- after another -- the corners, the reference's order
-// (faces, edges, corners; src/boundary.cc:447-907, 1118-1535).  It does the
-// same point updates in the same dependency order as the face launch
-// followed by the edge and corner launches above, so the results are the
-// same bit for bit; the barriers replace two launch boundaries.
+// Robin boundary in fewer launches.  The Newton update (mode 0) must see the
+// faces done before the edges and the edges before the corners (the
+// reference's order: faces, edges, corners; src/boundary.cc:447-907): the
+// faces keep their launch over the whole GPU (k_robin_faces), and the edges
+// and corners of a box follow in one launch of a thread-block cluster per box
+// whose barrier separates them (k_robin_ec_cluster).  The operator value
+// (mode 1, src/boundary.cc:1118-1535) only reads u, so every ghost point of
+// a level -- faces, edges and corners -- is one flat launch (k_robin_all).
+// The point updates and their dependency order are those of the separate
+// face, edge and corner launches above, so the results are the same bits.
 // pt(mask, i, j, k) updates one ghost point.
 // ----------------------------------------------------------------------------
 constexpr int kRobinCluster = 8;
 
-template <class PointFn>
-__device__ __forceinline__ void robin_walk(const DevBox &B, unsigned rank, unsigned ncta, PointFn pt)
+// Ghost points of a box's 12 edges, counted along the edges (each item: the
+// edge's b x b points at one position).
+__host__ __device__ __forceinline__ long long robin_edge_items(const DevBox &B)
 {
-  namespace cg = cooperative_groups;
-  const int b = B.buf;
-  const long long tid = (long long)rank * blockDim.x + threadIdx.x, nth = (long long)ncta * blockDim.x;
-  // faces: the normal columns of the six faces, face by face
-  long long total = 0;
-  for (int f = 0; f < 6; f++) {
-    const int a = f >> 1;
-    total += (long long)(B.n[(a + 1) % 3] - 2 * b) * (B.n[(a + 2) % 3] - 2 * b);
-  }
-  for (long long t0 = tid; t0 < total; t0 += nth) {
-    long long t = t0;
-    for (int f = 0; f < 6; f++) {
-      const int a = f >> 1, hi = f & 1;
-      const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
-      const int m1 = B.n[a1] - 2 * b, m2 = B.n[a2] - 2 * b;
-      const long long cols = (long long)m1 * m2;
-      if (t < cols) {
-        int ijk[3];
-        ijk[a1] = b + (int)(t % m1);
-        ijk[a2] = b + (int)(t / m1);
-        for (int l = 0; l < b; l++) {
-          ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
-          pt(1 << a, ijk[0], ijk[1], ijk[2]);
-        }
-        break;
-      }
-      t -= cols;
-    }
-  }
-  cg::this_cluster().sync();   // every face column is done (global writes visible in the cluster)
-  // edges: 12 a box; edge e12 runs along axis fa with ghost axes a and c
-  long long etotal = 0;
+  long long n = 0;
   for (int e12 = 0; e12 < 12; e12++) {
     const int pi = e12 >> 2, a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2;
-    etotal += B.n[3 - a - c] - 2 * b;
+    n += B.n[3 - a - c] - 2 * B.buf;
   }
-  for (long long t0 = tid; t0 < etotal; t0 += nth) {
-    long long t = t0;
-    for (int e12 = 0; e12 < 12; e12++) {
-      const int pi = e12 >> 2, e = e12 & 3;
-      const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
-      const int m = B.n[fa] - 2 * b;
-      if (t < m) {
-        const int ha = e >> 1, hc = e & 1;
-        int ijk[3];
-        ijk[fa] = b + (int)t;
-        for (int ta = 0; ta < b; ta++)
-          for (int tc = 0; tc < b; tc++) {
-            ijk[a] = ha ? B.n[a] - b + ta : b - 1 - ta;
-            ijk[c] = hc ? B.n[c] - b + tc : b - 1 - tc;
-            pt((1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
-          }
-        break;
+  return n;
+}
+
+// Normal columns of a box's six faces (each item: the column's b points).
+__host__ __device__ __forceinline__ long long robin_face_items(const DevBox &B)
+{
+  const int b = B.buf;
+  long long cols = 0;
+  for (int a = 0; a < 3; a++) cols += 2LL * (B.n[(a + 1) % 3] - 2 * b) * (B.n[(a + 2) % 3] - 2 * b);
+  return cols;
+}
+
+template <class PointFn>
+__device__ __forceinline__ void robin_face_item(const DevBox &B, long long t, PointFn pt)
+{
+  const int b = B.buf;
+  for (int f = 0; f < 6; f++) {
+    const int a = f >> 1, hi = f & 1;
+    const int a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+    const int m1 = B.n[a1] - 2 * b, m2 = B.n[a2] - 2 * b;
+    const long long cols = (long long)m1 * m2;
+    if (t < cols) {
+      int ijk[3];
+      ijk[a1] = b + (int)(t % m1);
+      ijk[a2] = b + (int)(t / m1);
+      for (int l = 0; l < b; l++) {
+        ijk[a] = hi ? B.n[a] - b + l : b - 1 - l;
+        pt(1 << a, ijk[0], ijk[1], ijk[2]);
       }
-      t -= m;
+      return;
     }
-  }
-  cg::this_cluster().sync();   // every edge is done
-  if (rank == 0 && threadIdx.x < 8) {
-    const int hx = threadIdx.x & 1, hy = (threadIdx.x >> 1) & 1, hz = threadIdx.x >> 2;
-    for (int tk = 0; tk < b; tk++)
-      for (int tj = 0; tj < b; tj++)
-        for (int ti = 0; ti < b; ti++)
-          pt(7, hx ? B.n[0] - b + ti : b - 1 - ti, hy ? B.n[1] - b + tj : b - 1 - tj,
-             hz ? B.n[2] - b + tk : b - 1 - tk);
+    t -= cols;
   }
 }
 
-// FP64 Robin update (mode 0) / operator (mode 1), Dirichlet (modes 2, 3) of
-// every box of a level: kRobinCluster blocks a box, launched as clusters.
+template <class PointFn>
+__device__ __forceinline__ void robin_edge_item(const DevBox &B, long long t, PointFn pt)
+{
+  const int b = B.buf;
+  for (int e12 = 0; e12 < 12; e12++) {
+    const int pi = e12 >> 2, e = e12 & 3;
+    const int a = pi == 2 ? 1 : 0, c = pi == 0 ? 1 : 2, fa = 3 - a - c;
+    const int m = B.n[fa] - 2 * b;
+    if (t < m) {
+      const int ha = e >> 1, hc = e & 1;
+      int ijk[3];
+      ijk[fa] = b + (int)t;
+      for (int ta = 0; ta < b; ta++)
+        for (int tc = 0; tc < b; tc++) {
+          ijk[a] = ha ? B.n[a] - b + ta : b - 1 - ta;
+          ijk[c] = hc ? B.n[c] - b + tc : b - 1 - tc;
+          pt((1 << a) | (1 << c), ijk[0], ijk[1], ijk[2]);
+        }
+      return;
+    }
+    t -= m;
+  }
+}
+
+template <class PointFn>
+__device__ __forceinline__ void robin_corner_item(const DevBox &B, int corner, PointFn pt)
+{
+  const int b = B.buf;
+  const int hx = corner & 1, hy = (corner >> 1) & 1, hz = corner >> 2;
+  for (int tk = 0; tk < b; tk++)
+    for (int tj = 0; tj < b; tj++)
+      for (int ti = 0; ti < b; ti++)
+        pt(7, hx ? B.n[0] - b + ti : b - 1 - ti, hy ? B.n[1] - b + tj : b - 1 - tj, hz ? B.n[2] - b + tk : b - 1 - tk);
+}
+
+// Edges, then (cluster barrier) corners of one box by a cluster of ncta blocks.
+template <class PointFn>
+__device__ __forceinline__ void robin_ec_walk(const DevBox &B, unsigned rank, unsigned ncta, PointFn pt)
+{
+  namespace cg = cooperative_groups;
+  const long long tid = (long long)rank * blockDim.x + threadIdx.x, nth = (long long)ncta * blockDim.x;
+  const long long ne = robin_edge_items(B);
+  for (long long t = tid; t < ne; t += nth) robin_edge_item(B, t, pt);
+  cg::this_cluster().sync();   // every edge is done (global writes visible in the cluster)
+  if (tid < 8) robin_corner_item(B, (int)tid, pt);
+}
+
 template <int ORD>
-__global__ void __launch_bounds__(256) k_robin_cluster(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
-                                                       const double *__restrict__ crd, int mode)
+__global__ void __launch_bounds__(256) k_robin_ec_cluster(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                          const double *__restrict__ crd, int mode)
 {
   namespace cg = cooperative_groups;
   const unsigned ncta = cg::this_cluster().num_blocks();
   const DevBox B = boxes[L.box[blockIdx.x / ncta]];
   if (!B.active) return;   // every block of the cluster reads the same box: all leave
-  robin_walk(B, cg::this_cluster().block_rank(), ncta,
-             [&](int mask, int i, int j, int k) { robin_point<ORD>(B, F, crd, mode, mask, i, j, k); });
+  robin_ec_walk(B, cg::this_cluster().block_rank(), ncta,
+                [&](int mask, int i, int j, int k) { robin_point<ORD>(B, F, crd, mode, mask, i, j, k); });
+}
+
+// Every ghost point of the boxes of L in one launch, for the modes that only
+// read u (1: the Robin operator, 3: the Dirichlet one).
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin_all(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                   const double *__restrict__ crd, int mode)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
+  long long t = lb * blockDim.x + threadIdx.x;
+  auto pt = [&](int mask, int i, int j, int k) { robin_point<ORD>(B, F, crd, mode, mask, i, j, k); };
+  const long long nf = robin_face_items(B), ne = robin_edge_items(B);
+  if (t < nf) robin_face_item(B, t, pt);
+  else if ((t -= nf) < ne) robin_edge_item(B, t, pt);
+  else if ((t -= ne) < 8) robin_corner_item(B, (int)t, pt);
 }
 
 // ----------------------------------------------------------------------------

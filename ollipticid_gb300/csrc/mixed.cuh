@@ -453,19 +453,34 @@ __global__ void __launch_bounds__(64) k_robin32_edges_corners(BoxList L, const D
   }
 }
 
-// FP32 Robin update / operator of the correction, every box of a level in
-// one launch of kRobinCluster-block clusters (robin_walk: faces, edges,
-// corners, in the order of the separate launches above).
+// FP32 Robin of the correction in fewer launches (as k_robin_ec_cluster and
+// k_robin_all): the edges and corners of the update in one cluster launch
+// per box after the faces' launch, the operator in one flat launch.
 template <int ORD>
-__global__ void __launch_bounds__(256) k_robin32_cluster(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
-                                                         const double *__restrict__ crd, int mode)
+__global__ void __launch_bounds__(256) k_robin32_ec_cluster(BoxList L, const DevBox *__restrict__ boxes,
+                                                            DevFields32 G, const double *__restrict__ crd, int mode)
 {
   namespace cg = cooperative_groups;
   const unsigned ncta = cg::this_cluster().num_blocks();
   const DevBox B = boxes[L.box[blockIdx.x / ncta]];
   if (!B.active) return;   // every block of the cluster reads the same box: all leave
-  robin_walk(B, cg::this_cluster().block_rank(), ncta,
-             [&](int mask, int i, int j, int k) { robin32_point<ORD>(B, G, crd, mode, mask, i, j, k); });
+  robin_ec_walk(B, cg::this_cluster().block_rank(), ncta,
+                [&](int mask, int i, int j, int k) { robin32_point<ORD>(B, G, crd, mode, mask, i, j, k); });
+}
+
+template <int ORD>
+__global__ void __launch_bounds__(256) k_robin32_all(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
+                                                     const double *__restrict__ crd, int mode)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
+  long long t = lb * blockDim.x + threadIdx.x;
+  auto pt = [&](int mask, int i, int j, int k) { robin32_point<ORD>(B, G, crd, mode, mask, i, j, k); };
+  const long long nf = robin_face_items(B), ne = robin_edge_items(B);
+  if (t < nf) robin_face_item(B, t, pt);
+  else if ((t -= nf) < ne) robin_edge_item(B, t, pt);
+  else if ((t -= ne) < 8) robin_corner_item(B, (int)t, pt);
 }
 
 enum Ew32Op { EW32_W_EQ_S_MINUS_R = 0, EW32_S_EQ_W_PLUS_R, EW32_W_PLUS_EQ_R, EW32_WW_EQ_E, EW32_V_EQ_E_MINUS_WW,

@@ -239,6 +239,11 @@ long long blocks_color2(const DevBox &B)   // two points of a row per thread
   return cdiv((H + 1) / 2 * (B.n[1] - 2 * b) * (B.n[2] - 2 * b), kSmoothThreads);
 }
 
+long long blocks_boundary(const DevBox &B)   // every ghost item: face columns, edge points, corners
+{
+  return cdiv(robin_face_items(B) + robin_edge_items(B) + 8, kThreads);
+}
+
 long long blocks_faces(const DevBox &B)
 {
   const int b = B.buf;
@@ -598,10 +603,18 @@ template <int ORD>
 void launch_robin(olgpu_hierarchy *h, int level, int mode, bool whole = false)
 {
   const BoxList L = level_list(h, level, blocks_faces, whole);
-  if (!h->robin_split) {   // faces, edges and corners in one launch, a cluster per box
-    launch_clusters(h, k_robin_cluster<ORD>, (unsigned)(L.count * kRobinCluster), kThreads, kRobinCluster, L,
+  if (!h->robin_split) {
+    if (mode == 1 || mode == 3) {   // the operator only reads u: every ghost point in one launch
+      const BoxList LA = level_list(h, level, blocks_boundary, whole);
+      k_robin_all<ORD><<<LA.blk[LA.count], kThreads, 0, h->stream>>>(LA, h->d_boxes, h->F, h->d_coords, mode);
+      h->launches++;
+      return;
+    }
+    // the update: the faces over the whole GPU, then edges and corners, a cluster per box
+    k_robin_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
+    launch_clusters(h, k_robin_ec_cluster<ORD>, (unsigned)(L.count * kRobinCluster), kThreads, kRobinCluster, L,
                     (const DevBox *)h->d_boxes, h->F, (const double *)h->d_coords, mode);
-    h->launches++;
+    h->launches += 2;
     return;
   }
   k_robin_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F, h->d_coords, mode);
@@ -1148,9 +1161,16 @@ void launch_robin32(olgpu_hierarchy *h, int level, int mode, bool whole = false)
 {
   const BoxList L = level_list(h, level, blocks_faces, whole);
   if (!h->robin_split) {
-    launch_clusters(h, k_robin32_cluster<ORD>, (unsigned)(L.count * kRobinCluster), kThreads, kRobinCluster, L,
+    if (mode == 1) {   // the operator only reads e: every ghost point in one launch
+      const BoxList LA = level_list(h, level, blocks_boundary, whole);
+      k_robin32_all<ORD><<<LA.blk[LA.count], kThreads, 0, h->stream>>>(LA, h->d_boxes, h->F32, h->d_coords, mode);
+      h->launches_mixed++;
+      return;
+    }
+    k_robin32_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);
+    launch_clusters(h, k_robin32_ec_cluster<ORD>, (unsigned)(L.count * kRobinCluster), kThreads, kRobinCluster, L,
                     (const DevBox *)h->d_boxes, h->F32, (const double *)h->d_coords, mode);
-    h->launches_mixed++;
+    h->launches_mixed += 2;
     return;
   }
   k_robin32_faces<ORD><<<L.blk[L.count], kThreads, 0, h->stream>>>(L, h->d_boxes, h->F32, h->d_coords, mode);

@@ -221,8 +221,13 @@ class NativeServer:
     def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
                  tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
                  inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4, stop: int = _abi.STOP_TOLERANCE,
-                 du_tol: float = 0.0):
+                 du_tol: float = 0.0, keep_only=None):
+        """keep_u: hand every result's u back; keep_only (a set of indices
+        into the stream given to run(), with keep_u) limits that to those
+        requests."""
         self.lib = _abi.load()
+        self.keep_only = keep_only
+        self._keep_rids = None
         c = _abi.ServerConfig()
         self.lib.olgpu_server_config_defaults(C.byref(c))
         c.device, c.mem_budget, c.max_active = device, mem_budget, max_active
@@ -259,7 +264,7 @@ class NativeServer:
         r.adm = [out.adm[i] for i in range(nbh)]
         if out.h:
             h = C.c_void_p(out.h)
-            if self.keep_u:
+            if self.keep_u and (self._keep_rids is None or rid in self._keep_rids):
                 r.u = []
                 for g in range(self.lib.olgpu_num_boxes(h)):
                     bi = _abi.BoxInfo()
@@ -276,23 +281,49 @@ class NativeServer:
         return dict(zip(("active", "building", "waiting", "peak_active"), (x.value for x in v)))
 
     def run(self, stream: Sequence[Tuple[float, Problem]]) -> dict:
-        """Submits (arrival time, problem) pairs in real time, then collects
-        every result; the report has the keys of `Server.run`."""
+        """Submits (arrival time, problem) pairs in real time from a thread
+        while this one collects the results as they finish (so that a
+        finished solve's memory is released at once); the report has the
+        keys of `Server.run`."""
+        import threading
         reqs = sorted(enumerate(stream), key=lambda r: r[1][0])
         t0 = time.perf_counter()
         ids = {}
-        for i, (arr, prob) in reqs:
-            delay = arr - (time.perf_counter() - t0)
-            if delay > 0:
-                time.sleep(delay)
-            ids[i] = (self.submit(prob), time.perf_counter() - t0)
+        lock = threading.Lock()
+        if self.keep_only is not None:
+            self._keep_rids = set()
+
+        def submitter():
+            for i, (arr, prob) in reqs:
+                delay = arr - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                with lock:
+                    rid = self.submit(prob)
+                    ids[i] = (rid, time.perf_counter() - t0)
+                    if self.keep_only is not None and i in self.keep_only:
+                        self._keep_rids.add(rid)
+
+        th = threading.Thread(target=submitter)
+        th.start()
         results = {}
-        for i, (rid, arrival) in ids.items():
-            r = self.poll(rid, wait=True)
-            r.rid, r.arrival = i, arrival
-            r.admitted += arrival
-            r.finished += arrival
-            results[i] = r
+        while len(results) < len(reqs):
+            with lock:
+                pending = [(i, v) for i, v in ids.items() if i not in results]
+            got = False
+            for i, (rid, arrival) in pending:
+                with lock:
+                    r = self.poll(rid, wait=False)
+                if r is None:
+                    continue
+                got = True
+                r.rid, r.arrival = i, arrival
+                r.admitted += arrival
+                r.finished += arrival
+                results[i] = r
+            if not got:
+                time.sleep(0.002)
+        th.join()
         makespan = max(r.finished for r in results.values()) - min(r.arrival for r in results.values())
         lat = np.array([results[i].latency for i in sorted(results)])
         return {

@@ -6,6 +6,8 @@ opposite for the two holes) with |P| ~ U[0, 0.12], spins |S| <= 0.2 m^2 in
 uniformly random directions, N from {33, 49, 65, 97}, 6..10 levels, 4th
 order, Robin boundary.
 
+served_binaries(): those binaries arriving as a Poisson stream.
+
 served_stream(): the served request stream -- 1..4 punctures at positions
 U[-10, 10]^3 with a minimum separation of 2 (rejection sampling), bare masses
 U[0.2, 0.6], |P| <= 0.2, |S| <= 0.3 m^2, N from the allowed sizes in
@@ -54,6 +56,19 @@ def batched_binaries(count: int = 256, seed: int = 1004, L: float = 1000.0,
         P.levels = int(rng.integers(levels[0], levels[1] + 1))
         P.order, P.L, P.nu1, P.nu2, P.tol = 4, L, 3, 20, 1e-10
         out.append(P)
+    return out
+
+
+def served_binaries(count: int, rate_hz: float, seed: int = 1006) -> List[Tuple[float, Problem]]:
+    """The batched workload's binaries (batched_binaries, in order) arriving
+    as a Poisson stream: (arrival time in s, problem) pairs with exponential
+    inter-arrival times of mean 1 / rate_hz."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for P in batched_binaries(count):
+        t += rng.exponential(1.0 / rate_hz)
+        out.append((t, P))
     return out
 
 

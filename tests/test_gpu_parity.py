@@ -94,3 +94,26 @@ def test_row_transfers_equal_point_transfers(case, mixed, monkeypatch):
             out.append([E.get_field(g) for g in range(len(E.boxes))])
     for g, (a, b) in enumerate(zip(*out)):
         assert np.array_equal(a, b), f"box {g}: max diff {float(np.max(np.abs(a - b))):.3e}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["o2_single", "o4_binary_merge", "o8_offset"])
+@pytest.mark.parametrize("mixed", [False, True])
+@pytest.mark.parametrize("variant", ["OLGPU_ROBIN_SPLIT", "OLGPU_SMOOTH_PTS"])
+def test_launch_layouts_give_the_same_bits(case, mixed, variant, monkeypatch):
+    """The Robin walk as separate face, edge and corner launches
+    (OLGPU_ROBIN_SPLIT) and the FP64 smoother with two points a thread
+    (OLGPU_SMOOTH_PTS=2) give the default launches' u bit for bit."""
+    import ollipticid_gb300 as og
+    P = problem(case)
+    out = []
+    for alt in (False, True):
+        if alt:
+            monkeypatch.setenv(variant, "2" if variant == "OLGPU_SMOOTH_PTS" else "1")
+        with og.Elliptic(P) as E:
+            E.set_precision(mixed)
+            for _ in range(3):
+                E.FASN()
+            out.append([E.get_field(g) for g in range(len(E.boxes))])
+    for g, (a, b) in enumerate(zip(*out)):
+        assert np.array_equal(a, b), f"box {g}: max diff {float(np.max(np.abs(a - b))):.3e}"
