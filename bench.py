@@ -44,6 +44,7 @@ UNIT = "solves/s"
 # fixed point on every level (the reference's own rule, residual only, ends
 # this workload 1e-9 away).
 DU_TOL = 5e-11
+ACCEL = 4   # Anderson depth of the plain FP64 iteration (FP64 history and sums)
 SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
 # DRAM bytes (read + write) and FP64-pipe occupancy of one finest-level
 # launch of k_smooth_color<4,0> on this workload, from an ncu capture
@@ -513,7 +514,7 @@ def batched_fixture_error(B, i, inst, fx):
     return worst, adm
 
 
-def run_batched(args, tuned=None, count: int = 256, chunk: int = 64):
+def run_batched(args, tuned=None, count: int = 256, chunk: int = 64, plain_rate=None):
     """The batched workload: all `count` seeded binaries (N in {33, 49, 65,
     97}, 6-10 levels, 4th order), mixed precision, residual <= 1e-10 and
     change of u <= DU_TOL, solved as batches of `chunk` (olgpu_batch: unions
@@ -576,6 +577,8 @@ def run_batched(args, tuned=None, count: int = 256, chunk: int = 64):
             "max_abs_u_minus_oracle": max((e for e, _ in errs), default=None),
             "max_abs_adm_minus_oracle": max((a for _, a in errs), default=None),
             "first16_as_separate_streams": streams,
+            "plain_fp64_same_binaries_solves_per_s": plain_rate,
+            "vs_plain_fp64": (count / solve_s) / plain_rate if plain_rate else None,
             "timing": "host wall clock around olgpu_batch_solve (u = 0 to the stop; hierarchies resident)"}
 
 
@@ -626,7 +629,25 @@ def served_binary_error(u, P, inst, fx):
     return worst
 
 
-def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None, plain_sample: int = 8):
+def plain_binaries_rate(sample: int = 8):
+    """The plain FP64 solver (FP64 cycles with FP64 mixing, the timed stop)
+    on the first `sample` binaries of the batched workload, one at a time:
+    solves/s from device time, after one untimed solve each."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi, workloads
+    ms = []
+    for P in workloads.batched_binaries(sample):
+        with og.Elliptic(P) as E:
+            E.set_fp64_acceleration(ACCEL)
+            E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)
+            E.reset()
+            E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)
+            ms.append(E.last_device_ms)
+    return len(ms) / (sum(ms) / 1000.0)
+
+
+def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None, plain_rate=None,
+                        plain_sample: int = 8):
     """The batched workload's binaries as a Poisson request stream at a
     saturating rate through the library's C++ server (continuous batching:
     requests admitted as slots and memory free up, each on its own stream,
@@ -648,15 +669,8 @@ def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None
         rep = S.run(stream)
     errs = [served_binary_error(r.u, stream[i][1], i, fx) for i, r in enumerate(rep["results"])
             if i in with_fx and r.u is not None]
-    # the plain FP64 solver on a sample of the same binaries, one at a time
-    plain_ms = []
-    for P in workloads.batched_binaries(plain_sample):
-        with og.Elliptic(P) as E:
-            E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)   # warm
-            E.reset()
-            E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=1e-10, du_tol=DU_TOL)
-            plain_ms.append(E.last_device_ms)
-    plain_rate = len(plain_ms) / (sum(plain_ms) / 1000.0)
+    if plain_rate is None:
+        plain_rate = plain_binaries_rate(plain_sample)
     statuses = [r.status for r in rep["results"]]
     return {"workload": f"{count} seeded binaries of the batched workload as a Poisson stream at {rate:g} "
                         f"requests/s, C++ server (olgpu_server_*), mixed precision, residual <= 1e-10 and change "
@@ -666,7 +680,8 @@ def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None
             "failed": sum(1 for x in statuses if x != 0),
             "oracle_checked_results": len(errs), "max_abs_u_minus_oracle": max(errs) if errs else None,
             "plain_fp64_same_binaries_solves_per_s": plain_rate,
-            "plain_fp64_sample": f"the first {plain_sample} binaries solved alone in FP64, device time",
+            "plain_fp64_sample": f"the first {plain_sample} binaries solved alone by the plain FP64 solver, "
+                                 f"device time",
             "vs_plain_fp64": rep["throughput_solves_per_s"] / plain_rate}
 
 
@@ -702,6 +717,10 @@ def run_gpu(args, rank: int, world: int, local: int):
     nboxes = len(E.boxes)
     total_pts = sum(b.n[0] * b.n[1] * b.n[2] for b in E.boxes)
     fx = load_fixture("config2")
+    # the plain FP64 solver: FP64 FAS V-cycles with FP64 Anderson mixing of
+    # depth 4 (the same fixed point, fewer cycles than the reference's
+    # iteration, which is timed below beside it)
+    E.set_fp64_acceleration(ACCEL)
 
     timed_solves(E, args.warmup, dev, P.tol)
     # ---- timed region: K solves (device time from CUDA events on the solver's stream)
@@ -722,6 +741,15 @@ def run_gpu(args, rank: int, world: int, local: int):
     launches = E.kernels_per_cycle * cycles
     u_stop = [E.get_field(g) for g in range(nboxes)]
     accuracy = reference_error(E, fx, u_stop, reps[-1].adm[:2]) or {"reference": "fixture missing"}
+    # the reference's iteration (no mixing) under the same stop, for comparison
+    E.set_fp64_acceleration(0)
+    timed_solves(E, 1, dev, P.tol)
+    ums, ureps = timed_solves(E, args.steps, dev, P.tol)
+    unaccelerated = {"value": args.steps / (ums / 1000.0), "unit": UNIT, "ms_per_step": ums / args.steps,
+                     "cycles_per_solve": sum(r.cycles for r in ureps) / args.steps,
+                     "accuracy": reference_error(E, fx, None, ureps[-1].adm[:2]),
+                     "iteration": "FP64 FAS V-cycles without mixing (the reference's iteration, multicolour)"}
+    E.set_fp64_acceleration(ACCEL)
 
     # ---- end to end through the C ABI with host buffers (pinned host memory)
     def pinned_like(x):
@@ -762,13 +790,14 @@ def run_gpu(args, rank: int, world: int, local: int):
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, fx, value / world)
-        batched = run_batched(args, tuned=autotune.tune(P, concurrency=16))
+        plain_bin = plain_binaries_rate(8)
+        batched = run_batched(args, tuned=autotune.tune(P, concurrency=16), plain_rate=plain_bin)
         config3 = run_config3()
         convergence = run_convergence()
         approx_start = run_approx_start()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
-        served_binaries = run_served_binaries(inner_sweeps=tuple(concurrent["inner_sweeps"]))
+        served_binaries = run_served_binaries(inner_sweeps=tuple(concurrent["inner_sweeps"]), plain_rate=plain_bin)
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
     # multicolour smoother (k_smooth_color) on the finest level, timed with
@@ -807,10 +836,12 @@ def run_gpu(args, rank: int, world: int, local: int):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": bench_config(),
-            "solve": {"precision": "plain FP64", "cycles_per_solve": cycles / args.steps,
+            "solve": {"precision": "plain FP64",
+                      "iteration": f"FP64 FAS V-cycles with FP64 Anderson mixing of depth {ACCEL}",
+                      "cycles_per_solve": cycles / args.steps,
                       "final_res": reps[-1].final_res, "final_du": reps[-1].final_du,
                       "adm": [reps[-1].adm[0], reps[-1].adm[1]], "wall_s": wall},
-            "accuracy": accuracy,
+            "accuracy": accuracy, "plain_fp64_unaccelerated": unaccelerated,
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served,
             "served_binaries": served_binaries, "config3": config3,
             "convergence": convergence, "approx_start": approx_start,

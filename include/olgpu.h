@@ -277,6 +277,14 @@ olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision);
  * the newest correction f by the last `depth` correction differences; the
  * fixed point is unchanged.  Applies to OLGPU_PREC_MIXED only. */
 olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth);
+/* The same Anderson mixing for the plain FP64 V-cycle, with its history and
+ * sums in FP64 (depth 0..4; default 0: the reference's iteration).  Each
+ * cycle's change u - u_before is mixed with the last `depth` changes; the
+ * fixed point is the FP64 cycle's, reached in fewer cycles (the multicolour
+ * FAS cycle's slow smooth mode is damped).  V-cycles of one hierarchy; a
+ * change of depth re-captures the cycle and clears the history.  No
+ * reference counterpart. */
+olgpu_status olgpu_set_fp64_acceleration(olgpu_hierarchy *h, int depth);
 
 /* Pre- and post-smoothing sweeps of the FP32 correction cycle of
  * OLGPU_PREC_MIXED (default: the problem's nu1 / nu2).  No reference

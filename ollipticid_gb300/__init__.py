@@ -253,6 +253,11 @@ class Elliptic:
         """Anderson history depth of the mixed outer iteration (0 = off, 1..4)."""
         check(self.lib.olgpu_set_acceleration(self._h, int(depth)))
 
+    def set_fp64_acceleration(self, depth: int):
+        """Anderson history depth of the plain FP64 cycle (0 = the reference's
+        iteration, 1..4), FP64 throughout; the fixed point is unchanged."""
+        check(self.lib.olgpu_set_fp64_acceleration(self._h, int(depth)))
+
     def cycle_launch(self):
         """Enqueue one V-cycle without waiting (see cycle_poll)."""
         check(self.lib.olgpu_cycle_launch(self._h))

@@ -114,6 +114,7 @@ SIGNATURES = {
     "olgpu_reset": (C.c_int, [C.c_void_p]),
     "olgpu_set_precision": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_set_acceleration": (C.c_int, [C.c_void_p, C.c_int]),
+    "olgpu_set_fp64_acceleration": (C.c_int, [C.c_void_p, C.c_int]),
     "olgpu_last_device_ms": (C.c_double, [C.c_void_p]),
     "olgpu_last_coarse_iters": (C.c_int, [C.c_void_p]),
     "olgpu_set_inner_sweeps": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),

@@ -632,6 +632,7 @@ __global__ void __launch_bounds__(256) k_robin_ec_cluster(BoxList L, const DevBo
 {
   namespace cg = cooperative_groups;
   const unsigned ncta = cg::this_cluster().num_blocks();
+  if ((int)(blockIdx.x / ncta) >= L.count) return;   // the whole cluster: one box a cluster
   const DevBox B = boxes[L.box[blockIdx.x / ncta]];
   if (!B.active) return;   // every block of the cluster reads the same box: all leave
   robin_ec_walk(B, cg::this_cluster().block_rank(), ncta,

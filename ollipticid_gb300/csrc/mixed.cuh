@@ -462,6 +462,7 @@ __global__ void __launch_bounds__(256) k_robin32_ec_cluster(BoxList L, const Dev
 {
   namespace cg = cooperative_groups;
   const unsigned ncta = cg::this_cluster().num_blocks();
+  if ((int)(blockIdx.x / ncta) >= L.count) return;   // the whole cluster: one box a cluster
   const DevBox B = boxes[L.box[blockIdx.x / ncta]];
   if (!B.active) return;   // every block of the cluster reads the same box: all leave
   robin_ec_walk(B, cg::this_cluster().block_rank(), ncta,
@@ -936,6 +937,103 @@ __global__ void __launch_bounds__(256) k_and_update(long long n, double *u, cons
     for (int i = 0; i < kAndMax; i++)
       if (i < nc) step -= gam[i] * (duc[i][p] + dfc[i][p]);
     u[p] = u[p] + (double)step;
+    du_out[p] = step;
+  }
+}
+
+// The same acceleration of the plain FP64 cycle, with its history in FP64:
+// f_k = u - up (up: u as the cycle found it), u_{k+1} = up + f_k - (dU + dF)
+// gamma.  Every stored quantity and every sum is FP64, so the iteration stays
+// FP64 throughout; its fixed point is the FP64 cycle's.
+__global__ void __launch_bounds__(256) k_and_reduce64(long long n, const double *__restrict__ u,
+                                                      const double *__restrict__ up, double *fprev, double *DF,
+                                                      const unsigned char *__restrict__ pinned, const AndersonState *st,
+                                                      double *part, unsigned long long *fmax_slot,
+                                                      const DevBox *__restrict__ gate)
+{
+  if (!gate->active) return;   // the solve has stopped (batch): the whole grid leaves
+  const int k = st->k, m = st->m;
+  const int nc = k < m ? k : m;
+  const int newest = (k + m - 1) % m;
+  const double *dfc[kAndMax];
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) dfc[i] = DF + (long long)((newest - i + 2 * kAndMax * m) % m) * n;
+  double *dfw = DF + (long long)newest * n;
+  double g[kAndMax * (kAndMax + 1) / 2], r[kAndMax];
+#pragma unroll
+  for (int i = 0; i < kAndMax * (kAndMax + 1) / 2; i++) g[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) r[i] = 0.0;
+  double fm = 0.0;
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const double fk = u[p] - up[p];
+    if (k >= 1) dfw[p] = fk - fprev[p];
+    fprev[p] = fk;
+    if (!pinned[p]) continue;
+    fm = fmax(fm, fabs(fk));
+    double c[kAndMax];
+#pragma unroll
+    for (int i = 0; i < kAndMax; i++) {
+      c[i] = i < nc ? dfc[i][p] : 0.0;
+      r[i] += c[i] * fk;
+    }
+    int q = 0;
+#pragma unroll
+    for (int i = 0; i < kAndMax; i++)
+#pragma unroll
+      for (int j = 0; j <= i; j++) g[q++] += c[i] * c[j];
+  }
+  __shared__ double red[32];
+  auto block_sum = [&](double v) -> double {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+    __syncthreads();
+    return s;
+  };
+  double *mine = part + (long long)blockIdx.x * kAndPart;
+  int q = 0;
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) {
+    const double s = block_sum(r[i]);
+    if (threadIdx.x == 0) mine[kAndMax * (kAndMax + 1) / 2 + i] = s;
+#pragma unroll
+    for (int j = 0; j <= i; j++) {
+      const double t = block_sum(g[q]);
+      if (threadIdx.x == 0) mine[q] = t;
+      q++;
+    }
+  }
+  block_max_atomic(fm, fmax_slot);
+}
+
+__global__ void __launch_bounds__(256) k_and_update64(long long n, double *u, const double *__restrict__ up,
+                                                      double *DU, const double *__restrict__ DF,
+                                                      const AndersonState *st, const DevBox *__restrict__ gate)
+{
+  if (!gate->active) return;
+  const int k = st->k_used, m = st->m;
+  const int nc = k < m ? k : m;
+  const int newest = (k + m - 1) % m;
+  double *du_out = DU + (long long)(k % m) * n;
+  const double *duc[kAndMax], *dfc[kAndMax];
+  double gam[kAndMax];
+#pragma unroll
+  for (int i = 0; i < kAndMax; i++) {
+    const long long slot = (newest - i + 2 * kAndMax * m) % m;
+    duc[i] = DU + slot * n;
+    dfc[i] = DF + slot * n;
+    gam[i] = i < nc ? st->gamma[i] : 0.0;
+  }
+  for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    double step = u[p] - up[p];
+#pragma unroll
+    for (int i = 0; i < kAndMax; i++)
+      if (i < nc) step -= gam[i] * (duc[i][p] + dfc[i][p]);
+    u[p] = up[p] + step;
     du_out[p] = step;
   }
 }

@@ -133,6 +133,11 @@ struct olgpu_hierarchy {
   cudaGraphExec_t graph_coarse = nullptr;
   // Anderson acceleration of the mixed outer iteration
   int anderson_m = kAndDefault;
+  // Anderson acceleration of the FP64 cycle (0: the reference's iteration)
+  int anderson64_m = 0;
+  double *d_and64 = nullptr;            // DU[m], DF[m], fprev (FP64, total_pts each)
+  AndersonState *d_and64_state = nullptr;
+  double *d_and64_part = nullptr;
   float *d_and = nullptr;               // DU[m], DF[m], fprev (FP32, total_pts each)
   unsigned char *d_pinned = nullptr;    // points the discrete system fixes
   AndersonState *d_and_state = nullptr;
@@ -913,7 +918,7 @@ void emit_fasn_up(olgpu_hierarchy *h, int k, int top)
   }
   if (k <= mg) dispatch_robin(h, k, 0);
   dispatch_smooth<EQ>(h, k, h->P.nu2, 2 * k + 1);
-  if (k == top)
+  if (k == top && h->anderson64_m == 0)   // with FP64 acceleration: after the update
     for (const auto &M : h->members)
       if (M.nadm > 0) {
         k_adm<<<1, 32, 0, h->stream>>>(M.d_adm, M.nadm, h->d_boxes, h->F, M.d_stats->adm_u);
@@ -1016,8 +1021,10 @@ template <int ORD, int EQ>
 void launch_smooth32_cluster(olgpu_hierarchy *h, int level, int nu)
 {
   const int ncta = h->sc_ncta[level];
+  const BoxList L = level_list(h, level, blocks_all);   // one cluster per box of the list
+  if (L.count == 0) return;
   cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3((unsigned)(ncta * h->G.boxes_in_level[level]), 1, 1);
+  cfg.gridDim = dim3((unsigned)(ncta * L.count), 1, 1);
   cfg.blockDim = dim3(kSmoothClusterThreads, 1, 1);
   cfg.dynamicSmemBytes = h->sc_smem[level];
   cfg.stream = h->stream;
@@ -1028,8 +1035,8 @@ void launch_smooth32_cluster(olgpu_hierarchy *h, int level, int nu)
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_smooth32_cluster<ORD, EQ>, (const DevBox *)h->d_boxes, level_list(h, level, blocks_all),
-                     h->F32, (const float2 *)h->d_aq, nu, h->d_stats0);
+  cudaLaunchKernelEx(&cfg, k_smooth32_cluster<ORD, EQ>, (const DevBox *)h->d_boxes, L, h->F32,
+                     (const float2 *)h->d_aq, nu, h->d_stats0);
   h->launches_mixed++;
 }
 
@@ -1355,12 +1362,42 @@ Transfer remap(const Transfer &X, int sfield, int tfield)
 
 olgpu_status reset_anderson(olgpu_hierarchy *h)
 {
-  if (!h->d_and_state) return OLGPU_OK;
-  AndersonState st{};
-  st.m = h->anderson_m > 0 ? h->anderson_m : 1;
-  CUDA_TRY(cudaMemcpyAsync(h->d_and_state, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  if (h->d_and_state) {
+    AndersonState st{};
+    st.m = h->anderson_m > 0 ? h->anderson_m : 1;
+    CUDA_TRY(cudaMemcpyAsync(h->d_and_state, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  }
+  if (h->d_and64_state) {
+    AndersonState st{};
+    st.m = h->anderson64_m > 0 ? h->anderson64_m : 1;
+    CUDA_TRY(cudaMemcpyAsync(h->d_and64_state, &st, sizeof(st), cudaMemcpyHostToDevice, h->stream));
+  }
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   return OLGPU_OK;
+}
+
+// FP64 acceleration of the FP64 cycle after its last kernel: each solve's
+// mixing over its own points, then its ADM integrand from the mixed u.
+void emit_anderson64(olgpu_hierarchy *h)
+{
+  for (const auto &M : h->members) {
+    const olgpu_hierarchy *m = M.h;
+    const long long n = m->total_pts;
+    double *DU = m->d_and64, *DF = m->d_and64 + (size_t)kAndMax * n, *fprev = m->d_and64 + (size_t)2 * kAndMax * n;
+    const DevBox *gate = (const DevBox *)h->d_boxes + M.box_base;
+    double *u = h->F.f[F_U] + M.pt_base;
+    const double *up = h->F.f[F_UP] + M.pt_base;
+    const int nblk = 152 * 4;
+    k_and_reduce64<<<nblk, kThreads, 0, h->stream>>>(n, u, up, fprev, DF, m->d_pinned, m->d_and64_state,
+                                                      m->d_and64_part, &M.d_stats->slots[kSlotCorr], gate);
+    k_and_solve<<<1, 32 * kAndSolveWarps, 0, h->stream>>>(m->d_and64_state, m->d_and64_part, nblk, gate);
+    k_and_update64<<<nblk, kThreads, 0, h->stream>>>(n, u, up, DU, DF, m->d_and64_state, gate);
+    h->launches += 3;
+    if (M.nadm > 0) {
+      k_adm<<<1, 32, 0, h->stream>>>(M.d_adm, M.nadm, h->d_boxes, h->F, M.d_stats->adm_u);
+      h->launches++;
+    }
+  }
 }
 
 olgpu_status capture_mixed(olgpu_hierarchy *h);
@@ -1468,6 +1505,7 @@ olgpu_status build_graph(olgpu_hierarchy *h)
   if (h->equation == 1) emit_fasn<1>(h, top, top);
   else if (h->equation >= 2) emit_fasn<2>(h, top, top);   // the test equations share one operator
   else emit_fasn<0>(h, top, top);
+  if (h->anderson64_m > 0) emit_anderson64(h);
   h->launches += emit_du_end(h);
   cudaError_t e = cudaStreamEndCapture(h->stream, &g);
   if (e != cudaSuccess) return fail(OLGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -1921,8 +1959,16 @@ olgpu_status olgpu_hierarchy_create(const olgpu_problem *p, int device, olgpu_hi
   if (device >= 0) CUDA_TRY(cudaSetDevice(device));
 
   auto *h = new olgpu_hierarchy();
+  const auto t0 = std::chrono::steady_clock::now();
   st = plan_hierarchy(p, h);
+  const auto t1 = std::chrono::steady_clock::now();
   if (st == OLGPU_OK) st = setup_device(h, nullptr, 0, 0, nullptr, nullptr, true);
+  if (std::getenv("OLGPU_VERBOSE")) {
+    const auto t2 = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "olgpu: hierarchy of %lld points: plan %.1f ms, device set-up and capture %.1f ms\n",
+                 h->total_pts, std::chrono::duration<double, std::milli>(t1 - t0).count(),
+                 std::chrono::duration<double, std::milli>(t2 - t1).count());
+  }
   if (st != OLGPU_OK) {
     olgpu_hierarchy_destroy(h);
     return st;
@@ -1952,6 +1998,9 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   cudaFree(h->d_pinned);
   cudaFree(h->d_and_state);
   cudaFree(h->d_and_part);
+  cudaFree(h->d_and64);
+  cudaFree(h->d_and64_state);
+  cudaFree(h->d_and64_part);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
     for (auto &X : *vec) cudaFree(X.d_jobs);
   if (h->owns_arena) cudaFree(h->d_arena);
@@ -2500,6 +2549,32 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
   }
   h->anderson_m = depth;
   return reset_anderson(h);
+}
+
+olgpu_status olgpu_set_fp64_acceleration(olgpu_hierarchy *h, int depth)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  if (depth < 0 || depth > kAndMax) return fail(OLGPU_ERR_INVALID_ARG, "acceleration depth must be 0..4");
+  if (h->is_union || h->P.method != OLGPU_METHOD_VCYCLE)
+    return fail(OLGPU_ERR_INVALID_ARG, "FP64 acceleration is built for the V-cycle of one hierarchy");
+  CUDA_TRY(cudaSetDevice(h->device));
+  if (depth > 0 && !h->d_and64) {
+    const size_t n = (size_t)h->total_pts;
+    if (cudaMalloc(&h->d_and64, sizeof(double) * n * (2 * kAndMax + 1)) != cudaSuccess ||
+        cudaMalloc(&h->d_and64_state, sizeof(AndersonState)) != cudaSuccess ||
+        cudaMalloc(&h->d_and64_part, sizeof(double) * 152 * 4 * kAndPart) != cudaSuccess)
+      return fail(OLGPU_ERR_OOM, "FP64 Anderson history allocation failed");
+    CUDA_TRY(cudaMemset(h->d_and64, 0, sizeof(double) * n * (2 * kAndMax + 1)));
+  }
+  const bool shape = (depth > 0) != (h->anderson64_m > 0);
+  h->anderson64_m = depth;
+  olgpu_status st = reset_anderson(h);
+  if (st != OLGPU_OK || !shape) return st;
+  if (h->graph) {   // the FP64 cycle's graph gains or loses the mixing
+    CUDA_TRY(cudaGraphExecDestroy(h->graph));
+    h->graph = nullptr;
+  }
+  return build_graph(h);
 }
 
 olgpu_status olgpu_set_precision(olgpu_hierarchy *h, int precision)

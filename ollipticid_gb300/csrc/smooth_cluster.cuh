@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
   float *se = reinterpret_cast<float *>(s_slab4);
   __shared__ const float *plane[kMaxClusterPlanes];
 
+  if ((int)blockIdx.x / ncta >= L.count) return;   // the whole cluster: one box a cluster
   const DevBox B = boxes[L.box[(int)blockIdx.x / ncta]];
   if (!B.active) return;   // every block of the cluster reads the same box: all leave
   int *nan_flag = &stats[B.solve].nan_flag;

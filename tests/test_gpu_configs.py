@@ -147,3 +147,27 @@ def test_reference_stop_rule_stops_short_on_the_binary():
         err = sampled_error(E, g)
     assert rep.final_res <= P.tol
     assert err > 1e-10, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["config1", "config2"])
+def test_fp64_acceleration_keeps_the_fixed_point(name):
+    """Anderson mixing of the plain FP64 cycle (FP64 history and sums) lands
+    within the bar of the reference's fixed point in fewer cycles."""
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+
+    g = load(name)
+    P = og.parse_olliptic_args(CONFIGS[name].split())
+    with og.Elliptic(P) as E:
+        plain = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=BENCH_DU_TOL)
+        E.set_fp64_acceleration(4)
+        E.reset()
+        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=BENCH_DU_TOL)
+        err = sampled_error(E, g)
+        adm = E.ADM_mass
+    assert rep.final_part <= P.tol and rep.final_du <= BENCH_DU_TOL
+    assert rep.cycles < plain.cycles, (rep.cycles, plain.cycles)
+    assert err <= U_TOL, f"{name}: max|u - u_ref| = {err:.3e} after {rep.cycles} cycles"
+    for a, b in zip(adm, g["fixed_adm"]):
+        assert abs(a - b) <= ADM_TOL, (name, a, b)
