@@ -875,6 +875,8 @@ def main():
             E.set_inner_sweeps(nu1, nu2)
             E.set_smoother_blocks(blocks)
         E.set_precision(args.mixed)
+        if not args.mixed:
+            E.set_fp64_acceleration(ACCEL)   # the timed plain FP64 cycle
         r = [E.FASN() for _ in range(2)]
         print(json.dumps({"profile_cycles": 2, "res": r, "kernels_per_cycle": E.kernels_per_cycle}))
         E.close()
