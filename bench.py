@@ -663,7 +663,7 @@ def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None
     fx = np.load(path) if os.path.exists(path) else None
     with_fx = set(int(i) for i in fx["instances"]) if fx is not None else set()
     stream = workloads.served_binaries(count, rate)
-    with NativeServer(mem_budget=200 << 30, max_active=32, builders=8, inner_sweeps=inner_sweeps,
+    with NativeServer(mem_budget=200 << 30, max_active=16, builders=8, inner_sweeps=inner_sweeps,
                       stop=_abi.STOP_ERROR, tol=1e-10, du_tol=DU_TOL, keep_u=True, keep_only=with_fx,
                       max_cycles=300) as S:
         rep = S.run(stream)
@@ -797,7 +797,8 @@ def run_gpu(args, rank: int, world: int, local: int):
         approx_start = run_approx_start()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
-        served_binaries = run_served_binaries(inner_sweeps=tuple(concurrent["inner_sweeps"]), plain_rate=plain_bin)
+        served_binaries = run_served_binaries(
+            inner_sweeps=tuple(concurrent["inner_sweeps"]) + (concurrent["smoother_blocks"],), plain_rate=plain_bin)
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
     # multicolour smoother (k_smooth_color) on the finest level, timed with

@@ -745,9 +745,14 @@ bool cluster_fits(olgpu_hierarchy *h, size_t smem)
   // so that a hierarchy with a smaller coarsest grid never lowers it below
   // what another one's captured cycle launches with
   int optin = 0;
+  cudaFuncAttributes fa{};
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) != cudaSuccess ||
-      (size_t)optin < smem ||
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess) {
+      cudaFuncGetAttributes(&fa, (const void *)kern) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  const int lim = optin - (int)fa.sharedSizeBytes;   // the dynamic part beside the kernel's static arrays
+  if (lim < (int)smem || cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
