@@ -31,6 +31,8 @@ struct DevBox {
   double idx[3];        // 1/dx
   double idx2[3];       // 1/dx^2
   double dulap;         // diagonal of the Laplacian stencil
+  double lscale;        // equal spacing, orders 2 and 4: the factor of the
+                        // Laplacian's neighbour sum (1/dx^2, 1/(12 dx^2))
   int solve;            // the box's solve in a batch (0 alone): its norm slots
                         // are stats[solve]
   int active;           // 0: the box's solve has stopped; every kernel leaves it as it is

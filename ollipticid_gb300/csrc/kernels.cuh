@@ -55,22 +55,27 @@ __device__ __forceinline__ int list_box(const BoxList &L, long long &local_block
 // axis); here those are multiplications by the rounded reciprocal -- a
 // 1-ulp difference, where an FP64 division costs the GB300 FP64 pipe about as
 // much as the rest of the stencil.
+// Equal spacing, orders 2 and 4: the axes share one scale (B.lscale), so the
+// neighbour sums are added first and the centre enters once (fewer FP64
+// instructions; the value differs from the per-axis form by rounding only).
+// This is the sum before that scale.
+template <int ORD>
+__device__ __forceinline__ double lap_sum_iso(const double *__restrict__ u, long long p, long long sy, long long sz)
+{
+  const double c = u[p];
+  if (ORD == 2) return (u[p + 1] + u[p - 1]) + (u[p + sy] + u[p - sy]) + (u[p + sz] + u[p - sz]) - 6.0 * c;
+  const double s1 = (u[p + 1] + u[p - 1]) + (u[p + sy] + u[p - sy]) + (u[p + sz] + u[p - sz]);
+  const double s2 = (u[p + 2] + u[p - 2]) + (u[p + 2 * sy] + u[p - 2 * sy]) + (u[p + 2 * sz] + u[p - 2 * sz]);
+  return 16.0 * s1 - s2 - 90.0 * c;
+}
+
 template <int ORD>
 __device__ __forceinline__ double lap(const double *__restrict__ u, long long p, long long sy,
                                       long long sz, const DevBox &B)
 {
   const double c = u[p];
   const double ix2 = B.idx2[0], iy2 = B.idx2[1], iz2 = B.idx2[2];
-  if (ORD <= 4 && B.iso) {
-    // equal spacing: the axes share one scale, so the neighbour sums are
-    // added first and the centre enters once (fewer FP64 instructions; the
-    // value differs from the per-axis form by rounding only)
-    if (ORD == 2)
-      return ((u[p + 1] + u[p - 1]) + (u[p + sy] + u[p - sy]) + (u[p + sz] + u[p - sz]) - 6.0 * c) * ix2;
-    const double s1 = (u[p + 1] + u[p - 1]) + (u[p + sy] + u[p - sy]) + (u[p + sz] + u[p - sz]);
-    const double s2 = (u[p + 2] + u[p - 2]) + (u[p + 2 * sy] + u[p - 2 * sy]) + (u[p + 2 * sz] + u[p - 2 * sz]);
-    return (16.0 * s1 - s2 - 90.0 * c) * (ix2 * (1.0 / 12.0));
-  }
+  if (ORD <= 4 && B.iso) return lap_sum_iso<ORD>(u, p, sy, sz) * B.lscale;
   if (ORD == 2) {
     return (u[p + 1] - 2.0 * c + u[p - 1]) * ix2 + (u[p + sy] - 2.0 * c + u[p - sy]) * iy2 +
            (u[p + sz] - 2.0 * c + u[p - sz]) * iz2;
@@ -98,6 +103,16 @@ __device__ __forceinline__ double lap(const double *__restrict__ u, long long p,
   }
 }
 
+// Lap u + a, with the scale of the equal-spacing forms and the addition in
+// one multiply-add.
+template <int ORD>
+__device__ __forceinline__ double lap_acc(const double *__restrict__ u, long long p, long long sy, long long sz,
+                                          const DevBox &B, double a)
+{
+  if (ORD <= 4 && B.iso) return fma(lap_sum_iso<ORD>(u, p, sy, sz), B.lscale, a);
+  return lap<ORD>(u, p, sy, sz, B) + a;
+}
+
 // NaN test on the bits (integer pipe).
 __device__ __forceinline__ bool is_nan_bits(double x)
 {
@@ -122,17 +137,16 @@ __device__ __forceinline__ double rcp_approx64(double x)
   return r;
 }
 
-// 1/q in FP64: the approximate reciprocal refined by two Newton steps
-// r <- r + r (1 - q r), each of which squares the relative error (about 1e-6,
-// 1e-12, then the FP64 rounding level).  Four FP64 multiply-adds instead of a
+// 1/q in FP64: the approximate reciprocal r (relative error e = 1 - q r of
+// about 1e-6) refined by one third-order step, 1/q = r / (1 - e) =
+// r (1 + e + e^2 + ...) ~ r + r (e + e^2), whose truncation e^3 (about 1e-18)
+// is below the FP64 rounding level.  Three FP64 multiply-adds instead of a
 // correctly rounded reciprocal; the result is within about an ulp of it.
 __device__ __forceinline__ double rcp_newton(double q)
 {
-  double r = rcp_approx64(q);
-  double e = fma(-q, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-q, r, 1.0);
-  return fma(r, e, r);
+  const double r = rcp_approx64(q);
+  const double e = fma(-q, r, 1.0);
+  return fma(r, fma(e, e, e), r);
 }
 
 // Pointwise operator value and its derivative in u (puncture, optionally with
@@ -158,6 +172,33 @@ __device__ __forceinline__ void point_op(double lapv, double dl, double uu, doub
     const double q2 = q * q;
     const double q4 = q2 * q2;
     op = op + dd * q + ee * (q4 * q);
+    dop = dop + dd + 5.0 * ee * q4;
+  }
+}
+
+// The pointwise part of the operator, nl = OP - Lap u, and duOP, for the
+// smoothers, which add nl - rho to the Laplacian in one multiply-add
+// (lap_acc).  The same terms as point_op.
+template <int EQ>
+__device__ __forceinline__ void point_terms(double dl, double uu, double bb, double cc, double dd, double ee,
+                                            double &nl, double &dop)
+{
+  if (EQ == 2) {
+    nl = uu * uu;
+    dop = dl + 2.0 * uu;
+    return;
+  }
+  const double q = cc + uu;
+  const double iq = rcp_newton(q);
+  const double iq2 = iq * iq;
+  const double iq4 = iq2 * iq2;
+  const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
+  nl = t7;
+  dop = dl - 7.0 * t7 * iq;                  // -7 b / (c+u)^8
+  if (EQ == 1) {
+    const double q2 = q * q;
+    const double q4 = q2 * q2;
+    nl = nl + dd * q + ee * (q4 * q);
     dop = dop + dd + 5.0 * ee * q4;
   }
 }
@@ -273,10 +314,9 @@ __device__ __forceinline__ void griddep_launch_dependents()
 // unsigned integer, so the block maximum is taken on the bits with integer
 // instructions and the FP64 pipe (the smoothers' bottleneck on GB300) stays
 // free.  A NaN compares above every finite value and reaches the slot.
-__device__ __forceinline__ void block_max_atomic(double v, unsigned long long *slot)
+__device__ __forceinline__ void block_max_atomic_bits(unsigned long long m, unsigned long long *slot)
 {
   __shared__ unsigned long long red[32];
-  unsigned long long m = (unsigned long long)__double_as_longlong(v);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
@@ -295,6 +335,11 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long *s
     }
     if (lane == 0 && m > 0ull) atomicMax(slot, m);
   }
+}
+
+__device__ __forceinline__ void block_max_atomic(double v, unsigned long long *slot)
+{
+  block_max_atomic_bits((unsigned long long)__double_as_longlong(v), slot);
 }
 
 
@@ -385,7 +430,7 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
   const int HP = (H + PTS - 1) / PTS;
   const long long t = lb * blockDim.x + threadIdx.x;
   const long long total = (long long)HP * m1 * m2;
-  double rabs = 0.0;
+  unsigned long long rabs = 0ull;   // max |R| as its bit pattern (integer compares)
   if (t < total) {
     const int ihp = ((int)t % HP);
     const int r = (int)t / HP;
@@ -403,14 +448,16 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
       ok[q] = i < B.n[0] - b;
       pp[q] = pidx(B, ok[q] ? i : b + delta, j, k);   // a point past the row's end repeats its first point
       const long long p = pp[q];
-      const double lv = lap<ORD>(u, p, sy, sz, B);
-      double op, dop;
-      point_op<EQ>(lv, B.dulap, u[p], F.f[F_B][B.off + p], F.f[F_C][B.off + p],
-                   EQ == 1 ? F.f[F_D][B.off + p] : 0.0, EQ == 1 ? F.f[F_E][B.off + p] : 0.0, op, dop);
-      const double R = op - F.f[F_RHO][B.off + p];
-      un[q] = u[p] - R * step_inverse(dop);
-      const double a = fabs(R);
-      if (ok[q] && (a > rabs || is_nan_bits(a))) rabs = a;   // a NaN stays the maximum
+      const double up = u[p];
+      double nl, dop;
+      point_terms<EQ>(B.dulap, up, F.f[F_B][B.off + p], F.f[F_C][B.off + p],
+                      EQ == 1 ? F.f[F_D][B.off + p] : 0.0, EQ == 1 ? F.f[F_E][B.off + p] : 0.0, nl, dop);
+      const double R = lap_acc<ORD>(u, p, sy, sz, B, nl - F.f[F_RHO][B.off + p]);
+      un[q] = up - R * step_inverse(dop);
+      // |R| on the bits: non-negative doubles order as their patterns, and a
+      // NaN's pattern is above infinity's, so a NaN stays the maximum
+      const unsigned long long a = (unsigned long long)__double_as_longlong(R) & 0x7fffffffffffffffull;
+      if (ok[q] && a > rabs) rabs = a;
     }
 #pragma unroll
     for (int q = 0; q < PTS; q++)
@@ -419,7 +466,7 @@ __global__ void __launch_bounds__(256) k_smooth_color(BoxList L, const DevBox *_
         if (is_nan_bits(un[q])) atomicOr(nan_flag, 1);
       }
   }
-  block_max_atomic(rabs, norm_slot);
+  block_max_atomic_bits(rabs, norm_slot);
 }
 
 // R = OP(u) on the INSIDE points (App_Ell_Operator).

@@ -183,10 +183,10 @@ __global__ void __launch_bounds__(256) k_mx_prep(BoxList L, const DevBox *__rest
     G.f[G_D][p] = (float)F.f[F_D][p];
     G.f[G_E5][p] = (float)(F.f[F_E][p] * (q4 * q));
   }
-  const double lv = lap<ORD>(u, t, B.n[0], (long long)B.n[0] * B.n[1], B);
-  double op = lv + t7;
-  if (EQ == 1) op = op + F.f[F_D][p] * q + F.f[F_E][p] * (q4 * q);
-  G.f[G_S][p] = (float)(F.f[F_RHO][p] - op);
+  double nl = t7;   // OP - Lap u
+  if (EQ == 1) nl = nl + F.f[F_D][p] * q + F.f[F_E][p] * (q4 * q);
+  // S = rho - OP(u), the Laplacian's scale and the addition in one multiply-add
+  G.f[G_S][p] = (float)-lap_acc<ORD>(u, t, B.n[0], (long long)B.n[0] * B.n[1], B, nl - F.f[F_RHO][p]);
 }
 
 // Robin defect on the physical boundary: S32 = S - (term(u) + u) (FP64).

@@ -57,6 +57,104 @@ constexpr size_t kCoarseSmemMax = 200 * 1024;   // dynamic shared memory of the 
 // iterations of one W-cycle level's loop in one call (OLGPU_WCYCLE_LEVEL_CAP)
 constexpr int kWcycleLevelCap = OLGPU_WCYCLE_LEVEL_CAP;
 
+// ---------------------------------------------------------------------------
+// Device memory of hierarchies and batches: one stream-ordered pool per
+// device.  cudaFree waits for the whole device, so in a server (or under
+// solve_many) every finished solve freed that way would hold up every other
+// solve's queued cycles; cudaFreeAsync on the owner's stream returns at once,
+// the memory goes back to the pool when the stream gets there, and the next
+// hierarchy's allocations are served from it.  The pool keeps what it holds
+// (no release threshold) while any hierarchy of the process is alive and is
+// trimmed when the last one is destroyed.  The pinned host copies of the
+// stats are recycled the same way (cudaFreeHost waits for the device too).
+// ---------------------------------------------------------------------------
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+int g_live[kMaxDevices] = {};
+std::vector<Stats *> g_pinned_stats;
+
+cudaMemPool_t device_pool(int dev)
+{
+  if (dev < 0 || dev >= kMaxDevices) return nullptr;
+  std::lock_guard<std::mutex> g(g_pool_mu);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    g_pools[dev] = pool;
+  }
+  return g_pools[dev];
+}
+
+// bytes of device memory in stream order on s (usable on s at once, on other
+// streams once s has reached this point)
+cudaError_t dev_alloc(void **p, size_t bytes, int dev, cudaStream_t s)
+{
+  *p = nullptr;
+  if (bytes == 0) return cudaSuccess;
+  cudaMemPool_t pool = device_pool(dev);
+  if (!pool) return cudaErrorMemoryAllocation;
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+void dev_free(void *p, cudaStream_t s)
+{
+  if (p) cudaFreeAsync(p, s);
+}
+
+Stats *pinned_stats_get()
+{
+  {
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (!g_pinned_stats.empty()) {
+      Stats *p = g_pinned_stats.back();
+      g_pinned_stats.pop_back();
+      return p;
+    }
+  }
+  Stats *p = nullptr;
+  return cudaMallocHost(&p, sizeof(Stats)) == cudaSuccess ? p : nullptr;
+}
+
+void pinned_stats_put(Stats *p)
+{
+  if (!p) return;
+  std::lock_guard<std::mutex> g(g_pool_mu);
+  g_pinned_stats.push_back(p);
+}
+
+void live_add(int dev)
+{
+  if (dev < 0 || dev >= kMaxDevices) return;
+  std::lock_guard<std::mutex> g(g_pool_mu);
+  g_live[dev]++;
+}
+
+// one hierarchy fewer; true for the device's last one
+bool live_remove(int dev)
+{
+  if (dev < 0 || dev >= kMaxDevices) return false;
+  std::lock_guard<std::mutex> g(g_pool_mu);
+  return --g_live[dev] == 0;
+}
+
+// the pool's unused memory back to the device
+void pool_trim(int dev)
+{
+  cudaMemPool_t pool = device_pool(dev);
+  if (pool) cudaMemPoolTrimTo(pool, 0);
+}
+
 // Host copy of one transfer: its jobs, their block prefix and the device copy.
 struct Transfer {
   std::vector<XferJob> jobs;
@@ -184,6 +282,8 @@ struct olgpu_hierarchy {
   bool is_union = false;
   bool mixed_ready = false;         // FP32 fields, plans and Anderson history are set up
   bool owns_arena = true, owns_arena32 = true, owns_stats = true;
+  bool pooled_hstats = false;   // h_stats from the recycled pinned records (one Stats)
+  bool live = false;            // counted among the device's live hierarchies
 };
 
 namespace {
@@ -270,6 +370,7 @@ void set_box_stencil(DevBox &B, int order, const double d[3])
     B.idx2[a] = B.idx[a] * B.idx[a];
   }
   B.iso = B.idx2[0] == B.idx2[1] && B.idx2[1] == B.idx2[2];
+  B.lscale = order == 2 ? B.idx2[0] : B.idx2[0] * (1.0 / 12.0);
   const double s = B.idx2[0] + B.idx2[1] + B.idx2[2];
   switch (order) {
   case 2: B.dulap = -2.0 * s; break;
@@ -1418,10 +1519,10 @@ olgpu_status prepare_mixed(olgpu_hierarchy *h, float *arena32, long long stride,
   const bool member = arena32 != nullptr;
   if (!member) {
     const size_t bytes = sizeof(float) * (size_t)h->total_pts * G_NUM;
-    if (cudaMalloc(&h->d_arena32, bytes) != cudaSuccess ||
-        cudaMalloc(&h->d_aq, sizeof(float2) * (size_t)h->total_pts) != cudaSuccess)
+    if (dev_alloc((void **)&h->d_arena32, bytes, h->device, h->stream) != cudaSuccess ||
+        dev_alloc((void **)&h->d_aq, sizeof(float2) * (size_t)h->total_pts, h->device, h->stream) != cudaSuccess)
       return fail(OLGPU_ERR_OOM, "FP32 arena allocation failed");
-    CUDA_TRY(cudaMemset(h->d_arena32, 0, bytes));
+    CUDA_TRY(cudaMemsetAsync(h->d_arena32, 0, bytes, h->stream));
     arena32 = h->d_arena32;
     stride = h->total_pts;
     base = 0;
@@ -1446,17 +1547,19 @@ olgpu_status prepare_mixed(olgpu_hierarchy *h, float *arena32, long long stride,
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
     for (auto &X : *vec) {
       if (X.jobs.empty() || member) continue;   // a member's FP32 steps run in the union's plans
-      if (cudaMalloc(&X.d_jobs, sizeof(XferJob) * X.jobs.size()) != cudaSuccess)
+      if (dev_alloc((void **)&X.d_jobs, sizeof(XferJob) * X.jobs.size(), h->device, h->stream) != cudaSuccess)
         return fail(OLGPU_ERR_OOM, "transfer plan allocation failed");
-      CUDA_TRY(cudaMemcpy(X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size(), cudaMemcpyHostToDevice));
+      CUDA_TRY(cudaMemcpyAsync(X.d_jobs, X.jobs.data(), sizeof(XferJob) * X.jobs.size(), cudaMemcpyHostToDevice,
+                               h->stream));
     }
   if (!h->is_union) {
     const size_t n = (size_t)h->total_pts;
-    if (cudaMalloc(&h->d_and, sizeof(float) * n * (2 * kAndMax + 1)) != cudaSuccess ||
-        cudaMalloc(&h->d_and_state, sizeof(AndersonState)) != cudaSuccess ||
-        cudaMalloc(&h->d_and_part, sizeof(double) * 152 * 4 * kAndPart) != cudaSuccess)
+    if (dev_alloc((void **)&h->d_and, sizeof(float) * n * (2 * kAndMax + 1), h->device, h->stream) != cudaSuccess ||
+        dev_alloc((void **)&h->d_and_state, sizeof(AndersonState), h->device, h->stream) != cudaSuccess ||
+        dev_alloc((void **)&h->d_and_part, sizeof(double) * 152 * 4 * kAndPart, h->device, h->stream) !=
+            cudaSuccess)
       return fail(OLGPU_ERR_OOM, "Anderson history allocation failed");
-    CUDA_TRY(cudaMemset(h->d_and, 0, sizeof(float) * n * (2 * kAndMax + 1)));
+    CUDA_TRY(cudaMemsetAsync(h->d_and, 0, sizeof(float) * n * (2 * kAndMax + 1), h->stream));
     olgpu_status st = reset_anderson(h);
     if (st != OLGPU_OK) return st;
   }
@@ -1846,9 +1949,11 @@ static olgpu_status setup_device(olgpu_hierarchy *h, double *arena, long long st
       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->ev_cycle, cudaEventDisableTiming) != cudaSuccess)
     return cleanup(fail(OLGPU_ERR_CUDA, "stream/event creation failed"));
+  live_add(h->device);
+  h->live = true;
   cudaError_t e = cudaSuccess;
   if (!arena) {   // its own arena
-    e = cudaMalloc(&h->d_arena, sizeof(double) * (size_t)h->total_pts * F_NUM);
+    e = dev_alloc((void **)&h->d_arena, sizeof(double) * (size_t)h->total_pts * F_NUM, h->device, h->stream);
     if (e != cudaSuccess) return cleanup(fail(OLGPU_ERR_OOM, "device arena allocation failed"));
     arena = h->d_arena;
     stride = h->total_pts;
@@ -1860,8 +1965,8 @@ static olgpu_status setup_device(olgpu_hierarchy *h, double *arena, long long st
   if (h->equation != 1) h->F.f[F_D] = h->F.f[F_E] = nullptr;
   auto up = [&](void **dst, const void *src, size_t bytes) -> bool {
     if (bytes == 0) return true;
-    if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
-    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (dev_alloc(dst, bytes, h->device, h->stream) != cudaSuccess) return false;
+    return cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, h->stream) == cudaSuccess;
   };
   bool ok = up((void **)&h->d_boxes, h->hboxes.data(), sizeof(DevBox) * h->hboxes.size()) &&
             up((void **)&h->d_coords, h->hcoords.data(), sizeof(double) * h->hcoords.size()) &&
@@ -1875,8 +1980,9 @@ static olgpu_status setup_device(olgpu_hierarchy *h, double *arena, long long st
     h->d_stats = stats;
     h->h_stats = hstats;
   } else {
-    ok = ok && cudaMalloc(&h->d_stats, sizeof(Stats)) == cudaSuccess &&
-         cudaMallocHost(&h->h_stats, sizeof(Stats)) == cudaSuccess;
+    ok = ok && dev_alloc((void **)&h->d_stats, sizeof(Stats), h->device, h->stream) == cudaSuccess &&
+         (h->h_stats = pinned_stats_get()) != nullptr;
+    h->pooled_hstats = true;
   }
   h->d_stats0 = h->d_stats;
   if (!ok) return cleanup(fail(OLGPU_ERR_OOM, "device allocation failed"));
@@ -1995,37 +2101,46 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
     for (cudaGraphExec_t g : *vec)
       if (g) cudaGraphExecDestroy(g);
   if (h->graph_coarse) cudaGraphExecDestroy(h->graph_coarse);
+  // device memory back to the pool in the stream's order (no device-wide wait)
+  cudaStream_t s = h->stream;
   for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
-    for (auto &X : *vec) cudaFree(X.d_jobs);
-  if (h->owns_arena32) cudaFree(h->d_arena32);
-  cudaFree(h->d_aq);
-  cudaFree(h->d_and);
-  cudaFree(h->d_pinned);
-  cudaFree(h->d_and_state);
-  cudaFree(h->d_and_part);
-  cudaFree(h->d_and64);
-  cudaFree(h->d_and64_state);
-  cudaFree(h->d_and64_part);
+    for (auto &X : *vec) dev_free(X.d_jobs, s);
+  if (h->owns_arena32) dev_free(h->d_arena32, s);
+  dev_free(h->d_aq, s);
+  dev_free(h->d_and, s);
+  dev_free(h->d_pinned, s);
+  dev_free(h->d_and_state, s);
+  dev_free(h->d_and_part, s);
+  dev_free(h->d_and64, s);
+  dev_free(h->d_and64_state, s);
+  dev_free(h->d_and64_part, s);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
-    for (auto &X : *vec) cudaFree(X.d_jobs);
-  if (h->owns_arena) cudaFree(h->d_arena);
-  cudaFree(h->d_boxes);
-  cudaFree(h->d_coords);
-  cudaFree(h->d_tab);
-  cudaFree(h->d_adm);
+    for (auto &X : *vec) dev_free(X.d_jobs, s);
+  if (h->owns_arena) dev_free(h->d_arena, s);
+  dev_free(h->d_boxes, s);
+  dev_free(h->d_coords, s);
+  dev_free(h->d_tab, s);
+  dev_free(h->d_adm, s);
   if (h->is_union)   // a union owns its members and their ADM job copies
     for (auto &M : h->members) {
-      cudaFree(M.d_adm);
+      dev_free(M.d_adm, s);
       olgpu_hierarchy_destroy(M.h);
     }
   if (h->owns_stats) {
-    cudaFree(h->d_stats);
-    if (h->h_stats) cudaFreeHost(h->h_stats);
+    dev_free(h->d_stats, s);
+    if (h->pooled_hstats)
+      pinned_stats_put(h->h_stats);
+    else if (h->h_stats)
+      cudaFreeHost(h->h_stats);
   }
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_cycle) cudaEventDestroy(h->ev_cycle);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->live && live_remove(h->device)) {   // the last one: its frees reach the pool, which is trimmed
+    if (s) cudaStreamSynchronize(s);
+    pool_trim(h->device);
+  }
+  if (s) cudaStreamDestroy(s);
   if (prev >= 0) cudaSetDevice(prev);
   delete h;
   return OLGPU_OK;
@@ -2451,13 +2566,13 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, con
   InterpBox *d_b = nullptr;
   double *d_xyz = nullptr, *d_out = nullptr;
   auto release = [&]() {
-    cudaFree(d_b);
-    cudaFree(d_xyz);
-    cudaFree(d_out);
+    dev_free(d_b, h->stream);
+    dev_free(d_xyz, h->stream);
+    dev_free(d_out, h->stream);
   };
-  cudaError_t e = cudaMalloc((void **)&d_b, sizeof(InterpBox) * nb);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d_xyz, sizeof(double) * 3 * (size_t)npts);
-  if (e == cudaSuccess) e = cudaMalloc((void **)&d_out, sizeof(double) * (size_t)npts);
+  cudaError_t e = dev_alloc((void **)&d_b, sizeof(InterpBox) * nb, h->device, h->stream);
+  if (e == cudaSuccess) e = dev_alloc((void **)&d_xyz, sizeof(double) * 3 * (size_t)npts, h->device, h->stream);
+  if (e == cudaSuccess) e = dev_alloc((void **)&d_out, sizeof(double) * (size_t)npts, h->device, h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_b, ib.data(), sizeof(InterpBox) * nb, cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * (size_t)npts, cudaMemcpyHostToDevice, h->stream);
@@ -2539,13 +2654,13 @@ olgpu_status olgpu_set_acceleration(olgpu_hierarchy *h, int depth)
     h->graph_mixed = nullptr;
     h->anderson_m = depth;
     for (auto *vec : {&h->restrict_e, &h->xfer_w32, &h->set_in32, &h->prolong_v32, &h->ghost_e})
-      for (auto &X : *vec) { cudaFree(X.d_jobs); X.d_jobs = nullptr; }
-    cudaFree(h->d_arena32); h->d_arena32 = nullptr;
-    cudaFree(h->d_aq); h->d_aq = nullptr;
+      for (auto &X : *vec) { dev_free(X.d_jobs, h->stream); X.d_jobs = nullptr; }
+    dev_free(h->d_arena32, h->stream); h->d_arena32 = nullptr;
+    dev_free(h->d_aq, h->stream); h->d_aq = nullptr;
     h->mixed_ready = false;
-    cudaFree(h->d_and); h->d_and = nullptr;
-    cudaFree(h->d_and_state); h->d_and_state = nullptr;
-    cudaFree(h->d_and_part); h->d_and_part = nullptr;
+    dev_free(h->d_and, h->stream); h->d_and = nullptr;
+    dev_free(h->d_and_state, h->stream); h->d_and_state = nullptr;
+    dev_free(h->d_and_part, h->stream); h->d_and_part = nullptr;
     if (h->precision == OLGPU_PREC_MIXED) {
       olgpu_status st = build_mixed(h);
       if (st != OLGPU_OK) return st;
@@ -2565,11 +2680,13 @@ olgpu_status olgpu_set_fp64_acceleration(olgpu_hierarchy *h, int depth)
   CUDA_TRY(cudaSetDevice(h->device));
   if (depth > 0 && !h->d_and64) {
     const size_t n = (size_t)h->total_pts;
-    if (cudaMalloc(&h->d_and64, sizeof(double) * n * (2 * kAndMax + 1)) != cudaSuccess ||
-        cudaMalloc(&h->d_and64_state, sizeof(AndersonState)) != cudaSuccess ||
-        cudaMalloc(&h->d_and64_part, sizeof(double) * 152 * 4 * kAndPart) != cudaSuccess)
+    if (dev_alloc((void **)&h->d_and64, sizeof(double) * n * (2 * kAndMax + 1), h->device, h->stream) !=
+            cudaSuccess ||
+        dev_alloc((void **)&h->d_and64_state, sizeof(AndersonState), h->device, h->stream) != cudaSuccess ||
+        dev_alloc((void **)&h->d_and64_part, sizeof(double) * 152 * 4 * kAndPart, h->device, h->stream) !=
+            cudaSuccess)
       return fail(OLGPU_ERR_OOM, "FP64 Anderson history allocation failed");
-    CUDA_TRY(cudaMemset(h->d_and64, 0, sizeof(double) * n * (2 * kAndMax + 1)));
+    CUDA_TRY(cudaMemsetAsync(h->d_and64, 0, sizeof(double) * n * (2 * kAndMax + 1), h->stream));
   }
   const bool shape = (depth > 0) != (h->anderson64_m > 0);
   h->anderson64_m = depth;
@@ -2802,10 +2919,15 @@ static olgpu_status build_union(std::vector<olgpu_hierarchy *> ms, int precision
       cudaEventCreate(&U->ev0) != cudaSuccess || cudaEventCreate(&U->ev1) != cudaSuccess ||
       cudaEventCreateWithFlags(&U->ev_cycle, cudaEventDisableTiming) != cudaSuccess)
     return fail_u(fail(OLGPU_ERR_CUDA, "batch: stream/event creation failed"));
-  if (cudaMalloc(&U->d_arena, sizeof(double) * (size_t)total * F_NUM) != cudaSuccess ||
-      cudaMalloc(&U->d_stats, sizeof(Stats) * n) != cudaSuccess ||
+  live_add(U->device);
+  U->live = true;
+  if (dev_alloc((void **)&U->d_arena, sizeof(double) * (size_t)total * F_NUM, U->device, U->stream) !=
+          cudaSuccess ||
+      dev_alloc((void **)&U->d_stats, sizeof(Stats) * n, U->device, U->stream) != cudaSuccess ||
       cudaMallocHost(&U->h_stats, sizeof(Stats) * n) != cudaSuccess)
     return fail_u(fail(OLGPU_ERR_OOM, "batch: device allocation failed"));
+  // the members set themselves up on their own streams inside this memory
+  if (cudaStreamSynchronize(U->stream) != cudaSuccess) return fail_u(fail(OLGPU_ERR_CUDA, "batch: allocation failed"));
   U->d_stats0 = U->d_stats;
   for (int f = 0; f < F_NUM; f++) U->F.f[f] = U->d_arena + (size_t)f * total;
   if (U->equation != 1) U->F.f[F_D] = U->F.f[F_E] = nullptr;
@@ -2891,8 +3013,8 @@ static olgpu_status build_union(std::vector<olgpu_hierarchy *> ms, int precision
   }
   auto upload = [&](void **dst, const void *src, size_t bytes) -> bool {
     if (bytes == 0) return true;
-    if (cudaMalloc(dst, bytes) != cudaSuccess) return false;
-    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (dev_alloc(dst, bytes, U->device, U->stream) != cudaSuccess) return false;
+    return cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, U->stream) == cudaSuccess;
   };
   bool ok = upload((void **)&U->d_boxes, U->hboxes.data(), sizeof(DevBox) * U->hboxes.size()) &&
             upload((void **)&U->d_coords, U->hcoords.data(), sizeof(double) * U->hcoords.size()) &&
