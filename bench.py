@@ -44,14 +44,17 @@ UNIT = "solves/s"
 # fixed point on every level (the reference's own rule, residual only, ends
 # this workload 1e-9 away).
 DU_TOL = 5e-11
+CONCURRENT_SOLVES = 16   # solves sharing the GPU in the concurrent and smoother-rate measurements
 ACCEL = 4   # Anderson depth of the plain FP64 iteration (FP64 history and sums)
 SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
-# DRAM bytes (read + write) and FP64-pipe occupancy of one finest-level
-# launch of k_smooth_color<4,0> on this workload, from an ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum; sm__inst_executed_pipe_fp64
-# .avg.pct_of_peak_sustained_active)
-SMOOTH_TRAFFIC_PER_LAUNCH = 17_600_768
-SMOOTH_FP64_PIPE_PCT = 70.4
+# DRAM bytes (read + write), FP64-pipe occupancy and FP64 instructions per
+# point-update of one finest-level launch of k_smooth_color<4,0> on this
+# workload, from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum;
+# sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active; that
+# occupancy x sm__cycles_active.avg x 2 per clock x 152 SMs / point-updates)
+SMOOTH_TRAFFIC_PER_LAUNCH = 17_598_208
+SMOOTH_FP64_PIPE_PCT = 64.6
+SMOOTH_FP64_INST_PER_POINT = 28.0
 GOLDEN = os.path.join(ROOT, "tests", "golden", "configs")
 
 
@@ -462,33 +465,45 @@ def run_approx_start():
 
 def fp32_smoother_roofline(peak: float, peak_kind: str):
     """The mixed cycle's dominant kernel, the cluster-resident FP32 smoother
-    (k_smooth32_cluster), on the finest level of the benchmark binary: 12
-    sweeps timed with CUDA events on the solver's stream (olgpu_time_smoother),
-    20 algorithmic bytes per interior point and sweep (read S, A, 1/(c+u) and
-    e, write e).  One 16-block cluster per box holds e in distributed shared
-    memory through the sweeps, so the kernel runs on 16 SMs per box: the rate
-    per SM, scaled to all 152, is what bounds many solves sharing the GPU."""
+    (k_smooth32_cluster), on the finest level of the benchmark binary, 20
+    algorithmic bytes per interior point and sweep (read S, A, 1/(c+u) and e,
+    write e): 12 sweeps of CONCURRENT_SOLVES solves at once, each on its own
+    stream, timed with CUDA events from the common start to the last end
+    (olgpu_time_smoother_many) -- the rate when many solves share the GPU,
+    as in the served and batched forms; beside it one solve alone
+    (olgpu_time_smoother), whose two 16-block clusters hold 32 SMs."""
     import ollipticid_gb300 as og
     P = og.parse_olliptic_args(WORKLOAD_ARGS.split())
-    with og.Elliptic(P) as E:
-        E.set_smoother_blocks(16)
-        E.set_inner_sweeps(4, 6)
-        E.set_precision(True)
+    sols = [og.Elliptic(P) for _ in range(CONCURRENT_SOLVES)]
+    try:
+        for E in sols:
+            E.set_smoother_blocks(16)
+            E.set_inner_sweeps(4, 6)
+            E.set_precision(True)
+        E = sols[0]
         top = E.levels - 1
         pts = E.interior_points(top)
         boxes = sum(1 for b in E.boxes if b.level == top)
         E.time_smoother(top, 3)                               # warm
         sweeps = 12
         ms, nl = E.time_smoother(top, sweeps)
+        og.time_smoother_many(sols, top, 3)                   # warm
+        ms_all = og.time_smoother_many(sols, top, sweeps)
+    finally:
+        for x in sols:
+            x.close()
     achieved = 20.0 * pts * sweeps / (ms / 1e3) / 1e9
+    achieved_all = 20.0 * pts * sweeps * len(sols) / (ms_all / 1e3) / 1e9
     sms = 16 * boxes
     return {"bound": "hbm", "kernel": f"k_smooth32_cluster<{P.order},0>: {sweeps} sweeps of the finest level "
                                       f"({pts} interior points, {boxes} boxes, one 16-block cluster each)",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-            "sms": sms, "achieved_scaled_to_152_sms": achieved * 152 / sms,
-            "frac_scaled_to_152_sms": achieved * 152 / sms / peak, "ms": ms, "launches": nl,
-            "note": "the level stays in shared and L2 memory through the sweeps; the algorithmic rate is per "
-                    "the SMs the clusters hold"}
+            "achieved": achieved_all, "peak": peak, "unit": "GB/s", "frac": achieved_all / peak,
+            "peak_kind": peak_kind, "concurrent_solves": len(sols), "ms": ms_all,
+            "how": f"the level's sweeps of {len(sols)} solves at once, each on its own stream "
+                   f"(olgpu_time_smoother_many), CUDA events from the common start to the last end",
+            "one_solve": {"achieved": achieved, "frac": achieved / peak, "sms": sms, "ms": ms, "launches": nl},
+            "note": "the level stays in shared and L2 memory through the sweeps; alone, one solve's clusters "
+                    "hold 16 SMs per box"}
 
 
 def batched_fixture_error(B, i, inst, fx):
@@ -812,22 +827,27 @@ def run_gpu(args, rank: int, world: int, local: int):
     launch_s = ms / 1000.0 / nl
     bytes_per_launch = SMOOTH_BYTES_PER_POINT * pts / colours
     achieved = bytes_per_launch / launch_s / 1e9
+    # FMA issue rates of this GPU (the stencils' instruction roofline)
+    fma = {"fp64_tflops": og.fma_peak(True), "fp32_tflops": og.fma_peak(False),
+           "how": "olgpu_fma_peak: 8 blocks of 256 threads per SM, 8 independent FMA chains a thread, CUDA events, "
+                  "best of 3 after a warm-up launch; 2 flops per FMA"}
+    fp64_rate = SMOOTH_FP64_INST_PER_POINT * (pts / colours) / launch_s / 1e9   # G FP64 instructions/s
+    fp64_peak = fma["fp64_tflops"] * 1e3 / 2.0                                   # G FP64 FMA/s, measured
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind, "traffic": SMOOTH_TRAFFIC_PER_LAUNCH,
             "kernel": f"k_smooth_color<{P.order},0>: one colour pass of the finest level "
                       f"({pts} interior points, {colours} colours)",
             "algorithmic_bytes_per_launch": bytes_per_launch, "launch_us": launch_s * 1e6, "launches_timed": nl,
             "fp64_pipe_active_pct": SMOOTH_FP64_PIPE_PCT,
+            "fp64_issue": {"instructions_per_point": SMOOTH_FP64_INST_PER_POINT, "achieved_ginst_s": fp64_rate,
+                           "peak_ginst_s": fp64_peak, "frac": fp64_rate / fp64_peak,
+                           "peak_kind": "measured (olgpu_fma_peak, this run)"},
             "note": "FP64-issue bound on GB300 (fp64_fma_peak_tflops, measured in this run): the HBM fraction is "
                     "low by design; traffic and FP64 pipe occupancy are from one ncu capture of this launch (ncu "
                     "flushes L2 first, so traffic is the level's fields read once; in the timed sweeps they stay "
                     "in L2)"}
 
     roof32 = fp32_smoother_roofline(peak, peak_kind) if rank == 0 and world == 1 and not args.no_extra else None
-    # FMA issue rates of this GPU (the stencils' instruction roofline)
-    fma = {"fp64_tflops": og.fma_peak(True), "fp32_tflops": og.fma_peak(False),
-           "how": "olgpu_fma_peak: 8 blocks of 256 threads per SM, 8 independent FMA chains a thread, CUDA events, "
-                  "best of 3 after a warm-up launch; 2 flops per FMA"}
     roof["fp64_fma_peak_tflops"] = fma["fp64_tflops"]
 
     cpu = cpu_job.result() if cpu_job is not None else None
@@ -867,7 +887,19 @@ def main():
     ap.add_argument("--mixed", action="store_true", help="with --profile-cycle: the mixed-precision cycle")
     ap.add_argument("--inner", default=None,
                     help="with --profile-cycle --mixed: inner schedule nu1,nu2,blocks (e.g. 4,6,16)")
+    ap.add_argument("--profile-batch", type=int, default=0, metavar="N",
+                    help="run two cycles of one batch of the first N seeded binaries of the batched workload "
+                         "(mixed precision, schedule 4,6,16) and exit (for the ncu launch list)")
     args = ap.parse_args()
+    if args.profile_batch:
+        import ollipticid_gb300 as og
+        from ollipticid_gb300 import _abi, workloads
+        with og.Batch(workloads.batched_binaries(256)[:args.profile_batch], mixed=True, inner_sweeps=(4, 6),
+                      blocks=16) as B:
+            reps = B.solve(stop=_abi.STOP_ERROR, max_cycles=2, tol=1e-10, du_tol=DU_TOL)
+            print(json.dumps({"profile_batch": args.profile_batch, "cycles": [r.cycles for r in reps],
+                              "unions": B.unions, "kernels_per_cycle": B.kernels_per_cycle}))
+        return
     if args.profile_cycle:
         import ollipticid_gb300 as og
         E = og.Elliptic(og.parse_olliptic_args(WORKLOAD_ARGS.split()))

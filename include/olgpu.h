@@ -436,6 +436,11 @@ long long olgpu_level_interior_points(const olgpu_hierarchy *h, int level);
  * *launches the number of smoother kernels it launched.  Changes u (FP64
  * precision) or the FP32 correction e (mixed precision: its smoother). */
 olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, double *ms, int *launches);
+/* The same for n hierarchies at once (no reference counterpart): each one's
+ * sweeps on its own stream, all started together; *ms is the device time
+ * from the common start to the last one's end.  Measures the smoother's rate
+ * when many solves share the GPU. */
+olgpu_status olgpu_time_smoother_many(olgpu_hierarchy *const *hs, int n, int level, int sweeps, double *ms);
 /* Measured issue rate of dependent-free fused multiply-adds on the current
  * device (no reference counterpart): every SM runs eight 256-thread blocks,
  * each thread eight independent FMA chains of `iters` steps, timed with CUDA

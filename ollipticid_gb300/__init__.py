@@ -467,6 +467,16 @@ class Batch:
         return self.lib.olgpu_batch_last_ms(self._b)
 
 
+def time_smoother_many(solvers: Sequence[Elliptic], level: int, sweeps: int) -> float:
+    """Device ms of `sweeps` smoother sweeps on one level of every solver at
+    once, each on its own stream (olgpu_time_smoother_many)."""
+    lib = _abi.load()
+    hs = (C.c_void_p * len(solvers))(*[E._h.value for E in solvers])
+    ms = C.c_double()
+    check(lib.olgpu_time_smoother_many(hs, len(solvers), level, sweeps, C.byref(ms)))
+    return ms.value
+
+
 def fma_peak(fp64: bool = True, iters: int = 0) -> float:
     """Measured FMA throughput of the current device in TFLOP/s (FP64 or
     FP32), the instruction roofline of the stencil kernels

@@ -580,15 +580,18 @@ __global__ void __launch_bounds__(256) k_set_in_op32(const XferJob *__restrict__
   G.f[G_S][T.off + tp] = G.f[G_W][S.off + sp] + rr;
 }
 
-// Coarsest correction problem in one CTA: repeat { Robin; one red-black SOR
-// sweep } until the sweep norm <= rtol * first, stops changing, or max_it.
-// e lives in shared memory; with SMEM the read-only coefficients (A, 1/(c+u),
-// source, and d, E5 for the scalar field) are staged there too, so an
-// iteration touches no global memory.
+// Coarsest correction problem of one solve in one CTA: repeat { Robin; one
+// red-black SOR sweep } until the sweep norm <= rtol * first, stops
+// changing, or max_it.  e lives in shared memory; with SMEM the read-only
+// coefficients (A, 1/(c+u), source, and d, E5 for the scalar field) are
+// staged there too, so an iteration touches no global memory.  Block b
+// solves box L.box[b], so the coarsest problems of every solve of a batch
+// that ends at this level run side by side in one launch; the iteration
+// count and NaN flag go to that box's solve (stats[B.solve]).
 template <int EQ, bool SMEM>
-__global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ boxes, int box, DevFields32 G,
+__global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ boxes, BoxList L, DevFields32 G,
                                                    const double *__restrict__ crd, int max_it, float omega, float rtol,
-                                                   int *iters_out, int *nan_flag)
+                                                   Stats *stats)
 {
   extern __shared__ float4 s_coarse4[];
   float *se = reinterpret_cast<float *>(s_coarse4);
@@ -596,8 +599,10 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
   __shared__ float s_norm;
   __shared__ int s_nan;
   __shared__ float s_x[3][64], s_ix[3][64];   // node coordinates and their reciprocals
-  const DevBox B = boxes[box];
-  if (!B.active) return;   // one block
+  if ((int)blockIdx.x >= L.count) return;
+  const DevBox B = boxes[L.box[blockIdx.x]];
+  if (!B.active) return;   // the whole block
+  int *iters_out = &stats[B.solve].coarse_iters, *nan_flag = &stats[B.solve].nan_flag;
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
   const int np = n0 * n1 * n2;
   float *ge = G.f[G_E] + B.off;

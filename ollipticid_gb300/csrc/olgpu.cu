@@ -1341,7 +1341,25 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
     launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R_WW_EQ_E, true);   // WW = E: nothing writes E before set_in
     launch_transfer32(h, h->set_in32[k]);
   }
-  bool deeper = false;   // a union: members whose coarsest level is k - 1 solve it, the others descend
+  // a union: members whose coarsest level is k - 1 solve it (one block each,
+  // side by side: one launch for those whose coefficients fit in shared
+  // memory beside e, one for the others), the others descend
+  bool deeper = false;
+  BoxList Ls{}, Lg{};
+  size_t smem_s = 0, smem_g = 0;
+  auto flush = [&](BoxList &BL, size_t smem, bool staged_coeffs) {
+    if (BL.count == 0) return;
+    if (staged_coeffs)
+      k_coarse32<EQ, true><<<BL.count, 1024, smem, h->stream>>>(h->d_boxes, BL, h->F32, h->d_coords,
+                                                                 h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+                                                                 h->d_stats0);
+    else
+      k_coarse32<EQ, false><<<BL.count, 1024, smem, h->stream>>>(h->d_boxes, BL, h->F32, h->d_coords,
+                                                                  h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+                                                                  h->d_stats0);
+    h->launches_mixed++;
+    BL.count = 0;
+  };
   for (const auto &M : h->members) {
     if (M.off != k - 1) {
       deeper = deeper || M.off < k - 1;
@@ -1350,16 +1368,15 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
     const DevBox &B = h->hboxes[M.coarse_box];
     const size_t np = (size_t)B.n[0] * B.n[1] * B.n[2];
     const size_t staged = sizeof(float) * np * (EQ == 1 ? 6 : 4);
-    if (staged <= kCoarseSmemMax)
-      k_coarse32<EQ, true><<<1, 1024, staged, h->stream>>>(h->d_boxes, M.coarse_box, h->F32, h->d_coords,
-                                                            h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
-                                                            &M.d_stats->coarse_iters, &M.d_stats->nan_flag);
-    else
-      k_coarse32<EQ, false><<<1, 1024, sizeof(float) * np, h->stream>>>(
-          h->d_boxes, M.coarse_box, h->F32, h->d_coords, h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
-          &M.d_stats->coarse_iters, &M.d_stats->nan_flag);
-    h->launches_mixed++;
+    const bool st = staged <= kCoarseSmemMax;
+    BoxList &BL = st ? Ls : Lg;
+    size_t &sm = st ? smem_s : smem_g;
+    BL.box[BL.count++] = M.coarse_box;
+    sm = std::max(sm, st ? staged : sizeof(float) * np);
+    if (BL.count == kMaxBoxesPerLevel) flush(BL, sm, st);
   }
+  flush(Ls, smem_s, true);
+  flush(Lg, smem_g, false);
   if (deeper) emit_fasn32<EQ>(h, k - 1);
   if (k > mg && launch_prolong_ghost<float>(h, h->prolong_v32[k], h->ghost_e[k], h->F32, G_E, G_WW)) {
     h->launches_mixed++;
@@ -2781,6 +2798,53 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
   *ms = elapsed_ms(h->ev0, h->ev1);
   if (launches) *launches = count - before;
   count = before;
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_time_smoother_many(olgpu_hierarchy *const *hs, int n, int level, int sweeps, double *ms)
+{
+  if (!hs || n < 1 || !ms || sweeps < 1) return fail(OLGPU_ERR_INVALID_ARG, "bad smoother timing request");
+  for (int i = 0; i < n; i++)
+    if (!hs[i] || hs[i]->is_union || hs[i]->device != hs[0]->device || level < 1 || level >= hs[i]->G.levels)
+      return fail(OLGPU_ERR_INVALID_ARG, "bad smoother timing request");
+  CUDA_TRY(cudaSetDevice(hs[0]->device));
+  std::vector<cudaEvent_t> done(n, nullptr);
+  cudaEvent_t end = nullptr;
+  auto release = [&]() {
+    for (cudaEvent_t e : done)
+      if (e) cudaEventDestroy(e);
+    if (end) cudaEventDestroy(end);
+  };
+  cudaError_t e = cudaEventCreate(&end);
+  for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
+  cudaStream_t s0 = hs[0]->stream;
+  // every stream starts after the start event of the first; the end event
+  // waits for the last smoother of every stream
+  if (e == cudaSuccess) e = cudaEventRecord(hs[0]->ev0, s0);
+  for (int i = 1; i < n && e == cudaSuccess; i++) e = cudaStreamWaitEvent(hs[i]->stream, hs[0]->ev0, 0);
+  for (int i = 0; i < n && e == cudaSuccess; i++) {
+    olgpu_hierarchy *h = hs[i];
+    const bool mixed = h->precision == OLGPU_PREC_MIXED;
+    int &count = mixed ? h->launches_mixed : h->launches;
+    const int before = count;
+    if (mixed) {
+      if (h->equation == 1) dispatch_smooth32<1>(h, level, sweeps);
+      else dispatch_smooth32<0>(h, level, sweeps);
+    } else {
+      if (h->equation == 1) dispatch_smooth<1>(h, level, sweeps, 0);
+      else if (h->equation >= 2) dispatch_smooth<2>(h, level, sweeps, 0);
+      else dispatch_smooth<0>(h, level, sweeps, 0);
+    }
+    count = before;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(done[i], h->stream);
+    if (e == cudaSuccess && i > 0) e = cudaStreamWaitEvent(s0, done[i], 0);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(end, s0);
+  if (e == cudaSuccess) e = cudaEventSynchronize(end);
+  if (e == cudaSuccess) *ms = elapsed_ms(hs[0]->ev0, end);
+  release();
+  CUDA_TRY(e);
   return OLGPU_OK;
 }
 
