@@ -441,6 +441,14 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
  * from the common start to the last one's end.  Measures the smoother's rate
  * when many solves share the GPU. */
 olgpu_status olgpu_time_smoother_many(olgpu_hierarchy *const *hs, int n, int level, int sweeps, double *ms);
+/* Device memory of the library's hierarchies and batches on one device (no
+ * reference counterpart): they allocate from one stream-ordered pool per
+ * device, so that a finished solve frees its memory without waiting for the
+ * GPU and the next one reuses it.  *reserved: bytes the pool holds from the
+ * device; *used: bytes handed out to live hierarchies.  The pool keeps its
+ * memory while any hierarchy is alive and gives it back when the last one
+ * is destroyed. */
+olgpu_status olgpu_device_pool_bytes(int device, long long *reserved, long long *used);
 /* Measured issue rate of dependent-free fused multiply-adds on the current
  * device (no reference counterpart): every SM runs eight 256-thread blocks,
  * each thread eight independent FMA chains of `iters` steps, timed with CUDA

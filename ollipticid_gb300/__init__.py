@@ -467,6 +467,15 @@ class Batch:
         return self.lib.olgpu_batch_last_ms(self._b)
 
 
+def device_pool_bytes(device: int = 0):
+    """(reserved, used) bytes of the library's device-memory pool
+    (olgpu_device_pool_bytes)."""
+    lib = _abi.load()
+    r, u = C.c_longlong(), C.c_longlong()
+    check(lib.olgpu_device_pool_bytes(int(device), C.byref(r), C.byref(u)))
+    return r.value, u.value
+
+
 def time_smoother_many(solvers: Sequence[Elliptic], level: int, sweeps: int) -> float:
     """Device ms of `sweeps` smoother sweeps on one level of every solver at
     once, each on its own stream (olgpu_time_smoother_many)."""

@@ -122,6 +122,7 @@ SIGNATURES = {
     "olgpu_kernels_per_cycle": (C.c_int, [C.c_void_p]),
     "olgpu_level_interior_points": (C.c_longlong, [C.c_void_p, C.c_int]),
     "olgpu_time_smoother": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "olgpu_device_pool_bytes": (C.c_int, [C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "olgpu_time_smoother_many": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
                                            C.POINTER(C.c_double)]),
     "olgpu_fma_peak": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_double)]),

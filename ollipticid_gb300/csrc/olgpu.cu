@@ -245,6 +245,9 @@ struct olgpu_hierarchy {
   // memory per block
   std::vector<int> sc_ncta;
   std::vector<size_t> sc_smem;
+  // per level, bit q: box q of the smoother's box list (level_list order)
+  // runs in the cluster launch; the others take one launch per colour
+  std::vector<unsigned long long> sc_fit;
   // pre-/post-smoothing sweeps of the FP32 correction cycle (-1: nu1/nu2)
   int inner_nu1 = -1, inner_nu2 = -1;
   int sc_max = 16;   // largest cluster for the FP32 smoother (0: per-colour launches)
@@ -315,6 +318,19 @@ BoxList level_list(const olgpu_hierarchy *h, int level, long long (*blocks_of)(c
   int boxes[kMaxBoxesPerLevel];
   const int n = whole || h->fine_count.empty() ? h->G.boxes_in_level[level] : h->fine_count[level];
   for (int b = 0; b < n; b++) boxes[b] = h->G.first_box[level] + b;
+  return box_list(h->hboxes, boxes, n, blocks_of);
+}
+
+// The boxes q of level_list(h, level, ...) whose bit q is (set) / is not
+// (!set) in mask.
+BoxList level_list_mask(const olgpu_hierarchy *h, int level, long long (*blocks_of)(const DevBox &),
+                        unsigned long long mask, bool set)
+{
+  const BoxList A = level_list(h, level, blocks_of);
+  int boxes[kMaxBoxesPerLevel];
+  int n = 0;
+  for (int q = 0; q < A.count; q++)
+    if (((mask >> q) & 1ull) == (set ? 1ull : 0ull)) boxes[n++] = A.box[q];
   return box_list(h->hboxes, boxes, n, blocks_of);
 }
 
@@ -1104,9 +1120,9 @@ void dispatch_mx_defect(olgpu_hierarchy *h, int level, int slot)
 }
 
 template <int ORD, int EQ>
-void launch_smooth32(olgpu_hierarchy *h, int level, int nu)
+void launch_smooth32(olgpu_hierarchy *h, const BoxList &L, int nu)
 {
-  const BoxList L = level_list(h, level, blocks_color);
+  if (L.count == 0) return;
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
       launch_pdl(h, k_smooth32<ORD, EQ>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
@@ -1127,7 +1143,8 @@ template <int ORD, int EQ>
 void launch_smooth32_cluster(olgpu_hierarchy *h, int level, int nu)
 {
   const int ncta = h->sc_ncta[level];
-  const BoxList L = level_list(h, level, blocks_all);   // one cluster per box of the list
+  // one cluster per box of the list that fits one
+  const BoxList L = level_list_mask(h, level, blocks_all, h->sc_fit[level], true);
   if (L.count == 0) return;
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3((unsigned)(ncta * L.count), 1, 1);
@@ -1194,46 +1211,73 @@ const void *smooth32_cluster_kernel(int ord, int eq)
   }
 }
 
-// Per level: the cluster that keeps e resident through the FP32 smoother, or
-// none.  Every box needs its ghost band at least as wide as the stencil's
-// reach, at most kMaxClusterPlanes planes, one interior plane per block and
-// its largest slab in shared memory.  Of the sizes 8..16 whose largest share
-// of interior planes is smallest (the critical path between two barriers),
-// the fewest blocks are taken: the other SMs stay free for other work.
+// Per level: the cluster that keeps e resident through the FP32 smoother, and
+// the boxes that run in it.  A box fits a cluster of ncta blocks when its
+// ghost band is at least as wide as the stencil's reach, it has at most
+// kMaxClusterPlanes planes and one interior plane per block, and its largest
+// slab fits in a block's shared memory; the boxes that do not (in a batch,
+// the largest problems' boxes beside smaller ones) are smoothed by the
+// per-colour launches in the same step (they are other boxes: the two
+// launches touch disjoint points, and both give the same bits).  Of the
+// sizes 8..16 the one that covers the most interior points is taken, then the
+// one whose largest share of interior planes is smallest (the critical path
+// between two barriers), then the fewest blocks: the other SMs stay free.
 void choose_smooth_clusters(olgpu_hierarchy *h)
 {
   const int L = h->G.levels;
   h->sc_ncta.assign(L, 0);
   h->sc_smem.assign(L, 0);
+  h->sc_fit.assign(L, 0ull);
   if (std::getenv("OLGPU_SMOOTH32_LAUNCHES") || h->sc_max < 8) return;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
   for (int l = 0; l < L; l++) {
     const int ord = level_order(h, l);
     const void *kern = smooth32_cluster_kernel(ord, h->equation);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kern) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    const size_t limit = (size_t)optin - fa.sharedSizeBytes;
+    const BoxList FL = level_list(h, l, blocks_all);   // the boxes the smoother runs on
     int best = 0, best_share = 1 << 30;
+    long long best_pts = 0;
     size_t best_smem = 0;
+    unsigned long long best_fit = 0ull;
     for (int ncta = std::min(h->sc_max, 16); ncta >= 8; ncta--) {
       size_t smem = 0;
       int share = 0;
-      bool ok = true;
-      const BoxList FL = level_list(h, l, blocks_all);   // the boxes the smoother runs on
+      long long pts = 0;
+      unsigned long long fit = 0ull;
       for (int q = 0; q < FL.count; q++) {
         const DevBox &B = h->hboxes[FL.box[q]];
         const int m2 = B.n[2] - 2 * B.buf;
-        if (m2 < ncta || B.n[2] > kMaxClusterPlanes || B.buf < ord / 2 || B.order != ord) ok = false;
+        if (m2 < ncta || B.n[2] > kMaxClusterPlanes || B.buf < ord / 2 || B.order != ord) continue;
+        const size_t sb = sizeof(float) * (size_t)slab_max_planes(B.n[2], B.buf, ncta) * B.n[0] * B.n[1];
+        if (sb > limit) continue;
+        fit |= 1ull << q;
         share = std::max(share, (m2 + ncta - 1) / ncta);
-        smem = std::max(smem, sizeof(float) * (size_t)slab_max_planes(B.n[2], B.buf, ncta) * B.n[0] * B.n[1]);
+        smem = std::max(smem, sb);
+        pts += (long long)(B.n[0] - 2 * B.buf) * (B.n[1] - 2 * B.buf) * m2;
       }
-      if (!ok || share > best_share) continue;
+      if (fit == 0ull || pts < best_pts || (pts == best_pts && share > best_share)) continue;
       if (!cluster_launchable(kern, ncta, kSmoothClusterThreads, smem)) continue;
       best = ncta;
       best_share = share;
       best_smem = smem;
+      best_pts = pts;
+      best_fit = fit;
     }
     h->sc_ncta[l] = best;
     h->sc_smem[l] = best_smem;
+    h->sc_fit[l] = best_fit;
     if (std::getenv("OLGPU_VERBOSE"))
-      std::fprintf(stderr, "olgpu: level %d FP32 smoother: %s (%d blocks, %zu B shared memory per block)\n", l,
-                   best ? "cluster-resident" : "one launch per colour", best, best_smem);
+      std::fprintf(stderr, "olgpu: level %d FP32 smoother: %d of %d boxes cluster-resident (%d blocks, %zu B shared "
+                   "memory per block)\n", l, __builtin_popcountll(best_fit), FL.count, best, best_smem);
   }
 }
 
@@ -1241,20 +1285,22 @@ template <int EQ>
 void dispatch_smooth32(olgpu_hierarchy *h, int level, int nu)
 {
   if (nu <= 0) return;
-  if (h->sc_ncta[level] > 0) {
+  const unsigned long long fit = h->sc_ncta[level] > 0 ? h->sc_fit[level] : 0ull;
+  if (fit) {
     switch (level_order(h, level)) {
     case 2: launch_smooth32_cluster<2, EQ>(h, level, nu); break;
     case 4: launch_smooth32_cluster<4, EQ>(h, level, nu); break;
     case 6: launch_smooth32_cluster<6, EQ>(h, level, nu); break;
     default: launch_smooth32_cluster<8, EQ>(h, level, nu); break;
     }
-    return;
   }
+  // the boxes no cluster holds: one launch per colour and sweep
+  const BoxList R = level_list_mask(h, level, blocks_color, fit, false);
   switch (level_order(h, level)) {
-  case 2: launch_smooth32<2, EQ>(h, level, nu); break;
-  case 4: launch_smooth32<4, EQ>(h, level, nu); break;
-  case 6: launch_smooth32<6, EQ>(h, level, nu); break;
-  default: launch_smooth32<8, EQ>(h, level, nu); break;
+  case 2: launch_smooth32<2, EQ>(h, R, nu); break;
+  case 4: launch_smooth32<4, EQ>(h, R, nu); break;
+  case 6: launch_smooth32<6, EQ>(h, R, nu); break;
+  default: launch_smooth32<8, EQ>(h, R, nu); break;
   }
 }
 
@@ -2153,10 +2199,11 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->ev_cycle) cudaEventDestroy(h->ev_cycle);
-  if (h->live && live_remove(h->device)) {   // the last one: its frees reach the pool, which is trimmed
-    if (s) cudaStreamSynchronize(s);
-    pool_trim(h->device);
-  }
+  // the frees complete before the stream goes: a completed free is what the
+  // pool hands to the next allocation on any stream (a pending one on a
+  // destroyed stream would leave the pool growing instead)
+  if (s) cudaStreamSynchronize(s);
+  if (h->live && live_remove(h->device)) pool_trim(h->device);   // the last one: the pool gives its memory back
   if (s) cudaStreamDestroy(s);
   if (prev >= 0) cudaSetDevice(prev);
   delete h;
@@ -2798,6 +2845,24 @@ olgpu_status olgpu_time_smoother(olgpu_hierarchy *h, int level, int sweeps, doub
   *ms = elapsed_ms(h->ev0, h->ev1);
   if (launches) *launches = count - before;
   count = before;
+  return OLGPU_OK;
+}
+
+olgpu_status olgpu_device_pool_bytes(int device, long long *reserved, long long *used)
+{
+  if (!reserved || !used) return fail(OLGPU_ERR_INVALID_ARG, "null output");
+  *reserved = *used = 0;
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (device >= 0 && device < kMaxDevices) pool = g_pools[device];
+  }
+  if (!pool) return OLGPU_OK;   // nothing allocated on this device yet
+  unsigned long long r = 0, u = 0;
+  CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+  CUDA_TRY(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+  *reserved = (long long)r;
+  *used = (long long)u;
   return OLGPU_OK;
 }
 

@@ -34,3 +34,36 @@ def test_same_alone_and_in_the_mix(mixed):
     finally:
         for E in solvers:
             E.close()
+
+
+@pytest.mark.gpu
+def test_device_pool_reuses_freed_memory():
+    """Hierarchies allocate from one stream-ordered pool per device and free
+    into it without a device-wide wait: made and destroyed over and over
+    beside a live one (as a server does), they reuse the same memory -- the
+    pool does not grow -- and the pool gives everything back after the last
+    hierarchy is destroyed."""
+    import gc
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    gc.collect()                                            # hierarchies other tests left to the collector
+    r0, u0 = og.device_pool_bytes(0)
+    keep = og.Elliptic(problem("o4_binary_merge"))
+    try:
+        seen = []
+        for i in range(8):
+            for mixed in (False, True):
+                with og.Elliptic(problem("sf_binary" if i % 2 else "o2_single")) as E:
+                    E.set_precision(mixed)
+                    E.Solve(stop=_abi.STOP_TOLERANCE, max_cycles=2, tol=1e-30)
+            seen.append(og.device_pool_bytes(0))
+        reserved = [r for r, _ in seen]
+        used = [u for _, u in seen]
+        assert used[-1] == used[0] and used[0] > 0          # only the live hierarchy's memory is in use
+        assert reserved[-1] <= reserved[1], reserved       # freed memory is reused, not added to
+    finally:
+        keep.close()
+    r, u = og.device_pool_bytes(0)
+    assert u == u0, (u, u0)
+    if u0 == 0:                                             # no hierarchy left: the pool gave its memory back
+        assert r == 0, r
