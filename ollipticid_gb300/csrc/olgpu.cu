@@ -1211,17 +1211,18 @@ const void *smooth32_cluster_kernel(int ord, int eq)
   }
 }
 
-// Per level: the cluster that keeps e resident through the FP32 smoother, and
-// the boxes that run in it.  A box fits a cluster of ncta blocks when its
-// ghost band is at least as wide as the stencil's reach, it has at most
-// kMaxClusterPlanes planes and one interior plane per block, and its largest
-// slab fits in a block's shared memory; the boxes that do not (in a batch,
-// the largest problems' boxes beside smaller ones) are smoothed by the
-// per-colour launches in the same step (they are other boxes: the two
-// launches touch disjoint points, and both give the same bits).  Of the
-// sizes 8..16 the one that covers the most interior points is taken, then the
-// one whose largest share of interior planes is smallest (the critical path
-// between two barriers), then the fewest blocks: the other SMs stay free.
+// Per level: the cluster that keeps e resident through the FP32 smoother, or
+// none.  A box fits a cluster of ncta blocks when its ghost band is at least
+// as wide as the stencil's reach, it has at most kMaxClusterPlanes planes and
+// one interior plane per block, and its largest slab fits in a block's
+// shared memory.  The cluster is used when every box of the level fits it:
+// splitting a level (the boxes that fit in a cluster launch, the others in
+// per-colour launches after it on the same stream) was measured 4 % slower
+// on the batched binaries, whose union levels put the largest problems'
+// boxes beside smaller ones (the cluster launch, on a few SMs, lengthens
+// the level's chain).  Of the sizes 8..16 whose largest share of interior
+// planes is smallest (the critical path between two barriers), the fewest
+// blocks are taken: the other SMs stay free for other work.
 void choose_smooth_clusters(olgpu_hierarchy *h)
 {
   const int L = h->G.levels;
@@ -1264,7 +1265,8 @@ void choose_smooth_clusters(olgpu_hierarchy *h)
         smem = std::max(smem, sb);
         pts += (long long)(B.n[0] - 2 * B.buf) * (B.n[1] - 2 * B.buf) * m2;
       }
-      if (fit == 0ull || pts < best_pts || (pts == best_pts && share > best_share)) continue;
+      const unsigned long long all = FL.count >= 64 ? ~0ull : (1ull << FL.count) - 1;
+      if (fit != all || FL.count == 0 || pts < best_pts || (pts == best_pts && share > best_share)) continue;
       if (!cluster_launchable(kern, ncta, kSmoothClusterThreads, smem)) continue;
       best = ncta;
       best_share = share;
