@@ -2992,35 +2992,11 @@ void finish_plan(Transfer &U)
 // multigrid levels then line up), boundary and sweep counts.
 struct UnionKey {
   int eq, order, depth, boundary, nu1, nu2;
-  int clusters;   // mixed precision: every box fits the FP32 cluster smoother
   bool operator<(const UnionKey &o) const
   {
-    return std::tie(eq, order, depth, boundary, nu1, nu2, clusters) <
-           std::tie(o.eq, o.order, o.depth, o.boundary, o.nu1, o.nu2, o.clusters);
+    return std::tie(eq, order, depth, boundary, nu1, nu2) < std::tie(o.eq, o.order, o.depth, o.boundary, o.nu1, o.nu2);
   }
 };
-
-// Whether every box of a planned problem fits a 16-block cluster of the FP32
-// smoother (its largest slab in a block's shared memory).  A union level
-// uses the cluster only when all its boxes fit, so problems whose boxes are
-// too large (N = 97 and up at order 4) are kept in unions of their own: the
-// others' levels then keep e in the clusters' shared memory.
-bool fits_smooth_clusters(const olgpu_hierarchy *m)
-{
-  int optin = 0;
-  cudaFuncAttributes fa{};
-  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, m->device) != cudaSuccess ||
-      cudaFuncGetAttributes(&fa, smooth32_cluster_kernel(m->P.order, m->equation)) != cudaSuccess) {
-    cudaGetLastError();
-    return true;
-  }
-  const size_t limit = (size_t)optin - fa.sharedSizeBytes;
-  for (const DevBox &B : m->hboxes)
-    if (B.n[2] > kMaxClusterPlanes ||
-        sizeof(float) * (size_t)slab_max_planes(B.n[2], B.buf, 16) * B.n[0] * B.n[1] > limit)
-      return false;
-  return true;
-}
 
 }  // namespace
 
@@ -3260,13 +3236,8 @@ olgpu_status olgpu_batch_create(const olgpu_problem *ps, int n, const olgpu_batc
       return st;
     }
     b->members.push_back(m);
-    const UnionKey key{m->equation >= OLGPU_EQ_POISSON ? 2 : m->equation,
-                       m->P.order,
-                       m->G.levels - m->G.mgrid_levels,
-                       m->P.boundary,
-                       m->P.nu1,
-                       m->P.nu2,
-                       c.precision == OLGPU_PREC_MIXED && c.blocks != 0 ? (fits_smooth_clusters(m) ? 1 : 0) : 1};
+    const UnionKey key{m->equation >= OLGPU_EQ_POISSON ? 2 : m->equation, m->P.order,
+                       m->G.levels - m->G.mgrid_levels, m->P.boundary, m->P.nu1, m->P.nu2};
     groups[key].push_back(i);
   }
   b->where.assign(n, {-1, -1});
