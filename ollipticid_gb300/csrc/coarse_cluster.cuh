@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         robin(7, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);
     __syncthreads();
     // one red-black SOR sweep over the interior points of this block's planes
-    double rmax = 0.0;
+    unsigned long long rbits = 0ull;
     int nan_seen = 0;
     const int ka = kz0 > 1 ? kz0 : 1, kb = kz1 < n2 - 1 ? kz1 : n2 - 1;
     const int H = (mi0 + 1) / 2;
@@ -185,16 +185,24 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         const int i = 1 + ((color + 1 + j + k) & 1) + 2 * ih;
         if (i >= n0 - 1) continue;
         const double c0 = U(i, j, k);
-        const double lapv = (U(i + 1, j, k) - 2.0 * c0 + U(i - 1, j, k)) * B.idx2[0] +
-                            (U(i, j + 1, k) - 2.0 * c0 + U(i, j - 1, k)) * B.idx2[1] +
-                            (U(i, j, k + 1) - 2.0 * c0 + U(i, j, k - 1)) * B.idx2[2];
         const long long p = ((long long)k * n1 + j) * n0 + i;
-        double op, dop;
-        point_op<EQ>(lapv, B.dulap, c0, gb[p], gc[p], EQ == 1 ? gd[p] : 0.0, EQ == 1 ? ge[p] : 0.0, op, dop);
-        const double R = op - gs[p];
-        const double un = c0 - omega * (R * step_inverse(dop));
+        double nl, dop;
+        point_terms<EQ>(B.dulap, c0, gb[p], gc[p], EQ == 1 ? gd[p] : 0.0, EQ == 1 ? ge[p] : 0.0, nl, dop);
+        double R;
+        if (B.iso) {   // equal spacing: the neighbour sum, its scale and the pointwise terms in one multiply-add
+          const double sum = (U(i + 1, j, k) + U(i - 1, j, k)) + (U(i, j + 1, k) + U(i, j - 1, k)) +
+                             (U(i, j, k + 1) + U(i, j, k - 1)) - 6.0 * c0;
+          R = fma(sum, B.lscale, nl - gs[p]);
+        } else {
+          const double lapv = (U(i + 1, j, k) - 2.0 * c0 + U(i - 1, j, k)) * B.idx2[0] +
+                              (U(i, j + 1, k) - 2.0 * c0 + U(i, j - 1, k)) * B.idx2[1] +
+                              (U(i, j, k + 1) - 2.0 * c0 + U(i, j, k - 1)) * B.idx2[2];
+          R = lapv + (nl - gs[p]);
+        }
+        const double un = c0 - R * (omega * step_inverse(dop));
         U(i, j, k) = un;
-        rmax = fmax(rmax, fabs(R));
+        // |R| on the bits (the integer pipe); a NaN's pattern is above infinity's
+        rbits = max(rbits, (unsigned long long)__double_as_longlong(R) & 0x7fffffffffffffffull);
         if (is_nan_bits(un)) nan_seen = 1;
       }
       if (color == 0) cl.sync();   // colour 1 reads colour 0 of the neighbouring blocks
@@ -202,9 +210,10 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
     // this block's partial norm into the slot of this iteration's parity
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+      rbits = max(rbits, __shfl_xor_sync(0xffffffffu, rbits, o));
       nan_seen |= __shfl_xor_sync(0xffffffffu, nan_seen, o);
     }
+    const double rmax = __longlong_as_double((long long)rbits);
     if ((threadIdx.x & 31) == 0) {
       red[threadIdx.x >> 5] = rmax;
       red_nan[threadIdx.x >> 5] = nan_seen;

@@ -78,6 +78,14 @@ cudaMemPool_t device_pool(int dev)
 {
   if (dev < 0 || dev >= kMaxDevices) return nullptr;
   std::lock_guard<std::mutex> g(g_pool_mu);
+  if (g_pools[dev]) {   // still valid (a device reset by the host destroys it)
+    unsigned long long thr = 0;
+    if (cudaMemPoolGetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &thr) != cudaSuccess) {
+      cudaGetLastError();
+      g_pools[dev] = nullptr;
+      g_live[dev] = 0;
+    }
+  }
   if (!g_pools[dev]) {
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -116,10 +124,14 @@ Stats *pinned_stats_get()
 {
   {
     std::lock_guard<std::mutex> g(g_pool_mu);
-    if (!g_pinned_stats.empty()) {
+    while (!g_pinned_stats.empty()) {
       Stats *p = g_pinned_stats.back();
       g_pinned_stats.pop_back();
-      return p;
+      // a device reset by the host frees pinned memory too: reuse only what
+      // is still registered
+      cudaPointerAttributes pa{};
+      if (cudaPointerGetAttributes(&pa, p) == cudaSuccess && pa.type == cudaMemoryTypeHost) return p;
+      cudaGetLastError();
     }
   }
   Stats *p = nullptr;
