@@ -587,6 +587,7 @@ def run_batched(args, tuned=None, count: int = 256, chunk: int = 64, plain_rate=
             "value": count / solve_s, "unit": UNIT, "solve_s": solve_s, "build_s": build_s,
             "unions": unions, "kernels_per_cycle_all_unions": kpc,
             "inner_sweeps": None if tuned is None else [tuned.nu1, tuned.nu2, tuned.blocks],
+            "autotune_table": None if tuned is None else tuned.table,
             "cycles_mean": sum(cycles) / len(cycles), "cycles_max": max(cycles),
             "oracle_checked_instances": len(errs),
             "max_abs_u_minus_oracle": max((e for e, _ in errs), default=None),
@@ -806,14 +807,17 @@ def run_gpu(args, rank: int, world: int, local: int):
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, fx, value / world)
         plain_bin = plain_binaries_rate(8)
-        batched = run_batched(args, tuned=autotune.tune(P, concurrency=16), plain_rate=plain_bin)
+        # the batched workload's schedule and smoother layout, tuned on its first 64 binaries
+        from ollipticid_gb300 import workloads
+        tuned_batch = autotune.tune_batch(workloads.batched_binaries(256)[:64], du_tol=DU_TOL)
+        batched = run_batched(args, tuned=tuned_batch, plain_rate=plain_bin)
         config3 = run_config3()
         convergence = run_convergence()
         approx_start = run_approx_start()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
         served_binaries = run_served_binaries(
-            inner_sweeps=tuple(concurrent["inner_sweeps"]) + (concurrent["smoother_blocks"],), plain_rate=plain_bin)
+            inner_sweeps=(tuned_batch.nu1, tuned_batch.nu2, tuned_batch.blocks), plain_rate=plain_bin)
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
     # multicolour smoother (k_smooth_color) on the finest level, timed with

@@ -14,7 +14,9 @@ a thread-block cluster per box keeping the correction in shared memory for
 every sweep (blocks = 16), or one launch per colour and sweep (blocks = 0),
 which wins for a solve alone.  Results
 are cached per problem shape (equation, order, N, levels, punctures) and
-concurrency, in memory and optionally in a JSON file.
+concurrency, in memory and optionally in a JSON file.  `tune_batch` makes
+the same choice for a batch of uneven problems (`olgpu_batch_*`) by timing
+one batch solve per candidate on the problems themselves.
 """
 from __future__ import annotations
 
@@ -32,6 +34,10 @@ from . import Elliptic, Problem, _abi, solve_many
 # cycles), cluster-resident or per-colour smoothing
 CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((3, 20, 16), (3, 8, 16), (4, 6, 16), (4, 4, 16), (5, 4, 16),
                                                 (5, 6, 16), (6, 4, 16), (4, 6, 0), (3, 8, 0), (2, 4, 0))
+
+# candidates for batches: the schedules that win for many solves at once,
+# cluster-resident or per-colour smoothing
+BATCH_CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((4, 6, 16), (4, 6, 0), (4, 4, 16), (4, 4, 0))
 
 _lock = threading.Lock()
 _memo: Dict[str, "Choice"] = {}
@@ -134,3 +140,29 @@ def cached(p: Problem, concurrency: int = 8, cache_path: Optional[str] = None) -
             return _memo[key]
     d = _load(cache_path).get(key)
     return Choice.from_dict(d) if d else None
+
+
+def tune_batch(problems: Sequence[Problem], candidates: Sequence[Tuple[int, int, int]] = BATCH_CANDIDATES,
+               tol: float = 1e-10, du_tol: float = 0.0, max_cycles: int = 300) -> Choice:
+    """Fastest (nu1, nu2, blocks) for solving `problems` as one mixed-precision
+    batch: each candidate's batch is built, solved once to warm up and once
+    timed (host wall clock of olgpu_batch_solve), every solve under the same
+    stop rule (OLGPU_STOP_ERROR with tol and du_tol, or the residual alone
+    when du_tol is 0).  Not cached: a batch is a set of problems, not a
+    shape."""
+    from . import Batch
+    rule = dict(stop=_abi.STOP_ERROR if du_tol > 0 else _abi.STOP_TOLERANCE, max_cycles=max_cycles, tol=tol,
+                du_tol=du_tol)
+    table = []
+    for nu1, nu2, blocks in candidates:
+        with Batch(problems, mixed=True, inner_sweeps=(nu1, nu2), blocks=blocks) as B:
+            B.solve(**rule)
+            B.reset()
+            reps = B.solve(**rule)
+            ok = all(r.status == _abi.OK and (r.final_part <= tol and r.final_du <= du_tol if du_tol > 0
+                                              else r.final_res <= tol) for r in reps)
+            rate = len(problems) / (B.last_ms / 1000.0) if ok else 0.0
+        table.append({"nu1": nu1, "nu2": nu2, "blocks": blocks, "solves_per_s": rate,
+                      "cycles": int(max(r.cycles for r in reps)), "reached_tol": ok})
+    top = max(table, key=lambda r: r["solves_per_s"])
+    return Choice(top["nu1"], top["nu2"], top["blocks"], top["solves_per_s"], top["cycles"], table)

@@ -15,10 +15,10 @@
 // The interior planes are split evenly (the ghost planes, which are read but
 // not updated, go with the first and the last block), so every block has the
 // same share of updates between two barriers.  The cluster size is a launch
-// parameter (8..16 blocks).  The kernel is held to 64 registers a thread so
-// that two 512-thread blocks fit an SM: the sweeps wait on shared, distributed
-// shared and L2 loads, and the second block's warps hide that latency when
-// many solves share the GPU.
+// parameter (8..16 blocks).  One 512-thread block per SM: held to 64
+// registers so that two fit, the kernel moved 5 % more bytes with 16 solves
+// sharing the GPU but a solve alone held half the SMs, and 16 copies of the
+// benchmark binary ran 4 % slower (71.7 against 75.1 solves/s).
 #pragma once
 
 #include "mixed.cuh"
@@ -54,7 +54,7 @@ __host__ __device__ inline int slab_max_planes(int n2, int b, int ncta)
 }
 
 template <int ORD, int EQ>
-__global__ void __launch_bounds__(kSmoothClusterThreads, 2)
+__global__ void __launch_bounds__(kSmoothClusterThreads, 1)
     k_smooth32_cluster(const DevBox *__restrict__ boxes, BoxList L, DevFields32 G, const float2 *__restrict__ aq,
                        int sweeps, Stats *stats)
 {

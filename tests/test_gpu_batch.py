@@ -126,3 +126,16 @@ def test_batch_isolates_a_failing_solve():
             want, wrep = solo(probs[i], True)
             assert reps[i].cycles == wrep.cycles
             assert all(np.array_equal(a, b) for a, b in zip(B.all_u(i), want))
+
+
+@pytest.mark.gpu
+def test_batch_autotuner_times_every_candidate():
+    """autotune.tune_batch solves the batch once per candidate layout and
+    returns the fastest of those that all reached the stop rule."""
+    from ollipticid_gb300 import autotune
+    cands = ((2, 3, 16), (2, 3, 0))
+    choice = autotune.tune_batch(uneven_problems(), candidates=cands, tol=1e-9, max_cycles=80)
+    assert [(r["nu1"], r["nu2"], r["blocks"]) for r in choice.table] == list(cands)
+    assert all(r["reached_tol"] and r["solves_per_s"] > 0 for r in choice.table)
+    assert (choice.nu1, choice.nu2, choice.blocks) in cands
+    assert choice.solves_per_s == max(r["solves_per_s"] for r in choice.table)
