@@ -266,10 +266,13 @@ __device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, l
               EQ == 1 ? G.f[G_E5][q] : 0.0f, op, dop);
 }
 
-// One multicolour pass on e (colour (i+j+k) mod (order/2+1)).
+// One multicolour pass on e (colour (i+j+k) mod (order/2+1)).  A and
+// 1/(c+u) come colour-packed from aq (one float2 per point, the pass's points
+// contiguous: packed_index) when the hierarchy keeps that copy, else from the
+// lexicographic fields; the values, and so the bits, are the same.
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
-                                                  int color, Stats *stats)
+                                                  const float2 *__restrict__ aq, int color, Stats *stats)
 {
   constexpr int NC = num_colors<ORD>();
   griddep_wait();                 // launched as a programmatic dependent
@@ -293,7 +296,14 @@ __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__res
   const long long p = pidx(B, i, j, k);
   const float lv = lapf<ORD>(e, p, B.n[0], (long long)B.n[0] * B.n[1], B);
   float op, dop;
-  corr_at<EQ>(B, G, p, lv, op, dop);
+  if (aq) {
+    const float2 a = __ldg(aq + B.off + (((long long)color * m2 + (k - b)) * m1 + (j - b)) * H + ih);
+    const long long q = B.off + p;
+    corr_op<EQ>(lv, (float)B.dulap, e[p], a.x, a.y, EQ == 1 ? G.f[G_D][q] : 0.0f, EQ == 1 ? G.f[G_E5][q] : 0.0f, op,
+                dop);
+  } else {
+    corr_at<EQ>(B, G, p, lv, op, dop);
+  }
   const float R = op - G.f[G_S][B.off + p];
   const float en = e[p] - R * rcp_fast(dop);
   e[p] = en;

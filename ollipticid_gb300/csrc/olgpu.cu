@@ -1138,7 +1138,7 @@ void launch_smooth32(olgpu_hierarchy *h, const BoxList &L, int nu)
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
       launch_pdl(h, k_smooth32<ORD, EQ>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
-                 (const DevBox *)h->d_boxes, h->F32, color, h->d_stats0);
+                 (const DevBox *)h->d_boxes, h->F32, (const float2 *)h->d_aq, color, h->d_stats0);
       h->launches_mixed++;
     }
 }
@@ -1474,7 +1474,7 @@ void emit_mixed_cycle(olgpu_hierarchy *h)
   for (int l = 0; l < L; l++) {
     const BoxList BL = level_list(h, l, blocks_all, true);
     // the cluster smoother reads (A, 1/(c+u)) colour-packed
-    float2 *aq = h->sc_ncta.size() > (size_t)l && h->sc_ncta[l] > 0 ? h->d_aq : nullptr;
+    float2 *aq = h->d_aq;   // both FP32 smoothers read the colour-packed copy
     switch (level_order(h, l)) {
     case 2: k_mx_prep<2, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, aq); break;
     case 4: k_mx_prep<4, EQ><<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->F32, aq); break;
