@@ -27,31 +27,44 @@ struct DevFields32 {
 };
 
 // Laplacian of e on one point from an accessor at(axis, offset) of its
-// neighbours; every FP32 stencil (global or shared-memory resident) evaluates
-// this one expression, so their results agree bit for bit.
+// neighbours.  Every FP32 stencil (global or shared-memory resident, one
+// launch per colour or every sweep in a cluster) evaluates this one
+// expression, and every operation is an explicitly rounded intrinsic: the
+// compiler may not fuse or reorder any of it, so kernels of different shapes
+// get the same bits (plain expressions were seen to differ between two
+// kernels after an unrelated branch was added to one of them).
 template <int ORD, class Acc>
 __device__ __forceinline__ float lapf_acc(float c, Acc at, float ix2, float iy2, float iz2)
 {
   if (ORD == 2) {
-    return (at(0, 1) - 2.0f * c + at(0, -1)) * ix2 + (at(1, 1) - 2.0f * c + at(1, -1)) * iy2 +
-           (at(2, 1) - 2.0f * c + at(2, -1)) * iz2;
+    auto ax = [&](int a) { return __fadd_rn(__fadd_rn(at(a, 1), __fmul_rn(-2.0f, c)), at(a, -1)); };
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2));
   } else if (ORD == 4) {
-    return ((-(at(0, 2) + at(0, -2)) + 16.0f * (at(0, 1) + at(0, -1)) - 30.0f * c) * ix2 +
-            (-(at(1, 2) + at(1, -2)) + 16.0f * (at(1, 1) + at(1, -1)) - 30.0f * c) * iy2 +
-            (-(at(2, 2) + at(2, -2)) + 16.0f * (at(2, 1) + at(2, -1)) - 30.0f * c) * iz2) *
-           (1.0f / 12.0f);
+    auto ax = [&](int a) {
+      return __fadd_rn(__fadd_rn(-__fadd_rn(at(a, 2), at(a, -2)), __fmul_rn(16.0f, __fadd_rn(at(a, 1), at(a, -1)))),
+                       __fmul_rn(-30.0f, c));
+    };
+    return __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2)),
+                     1.0f / 12.0f);
   } else if (ORD == 6) {
     auto ax = [&](int a) {
-      return 2.0f * (at(a, 3) + at(a, -3)) - 27.0f * (at(a, 2) + at(a, -2)) + 270.0f * (at(a, 1) + at(a, -1)) -
-             490.0f * c;
+      float v = __fmul_rn(2.0f, __fadd_rn(at(a, 3), at(a, -3)));
+      v = __fadd_rn(v, __fmul_rn(-27.0f, __fadd_rn(at(a, 2), at(a, -2))));
+      v = __fadd_rn(v, __fmul_rn(270.0f, __fadd_rn(at(a, 1), at(a, -1))));
+      return __fadd_rn(v, __fmul_rn(-490.0f, c));
     };
-    return (ax(0) * ix2 + ax(1) * iy2 + ax(2) * iz2) * (1.0f / 180.0f);
+    return __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2)),
+                     1.0f / 180.0f);
   } else {
     auto ax = [&](int a) {
-      return -9.0f * (at(a, 4) + at(a, -4)) + 128.0f * (at(a, 3) + at(a, -3)) - 1008.0f * (at(a, 2) + at(a, -2)) +
-             8064.0f * (at(a, 1) + at(a, -1)) - 14350.0f * c;
+      float v = __fmul_rn(-9.0f, __fadd_rn(at(a, 4), at(a, -4)));
+      v = __fadd_rn(v, __fmul_rn(128.0f, __fadd_rn(at(a, 3), at(a, -3))));
+      v = __fadd_rn(v, __fmul_rn(-1008.0f, __fadd_rn(at(a, 2), at(a, -2))));
+      v = __fadd_rn(v, __fmul_rn(8064.0f, __fadd_rn(at(a, 1), at(a, -1))));
+      return __fadd_rn(v, __fmul_rn(-14350.0f, c));
     };
-    return (ax(0) * ix2 + ax(1) * iy2 + ax(2) * iz2) * (1.0f / 5040.0f);
+    return __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2)),
+                     1.0f / 5040.0f);
   }
 }
 
@@ -70,18 +83,32 @@ template <int EQ>
 __device__ __forceinline__ void corr_op(float lapv, float dl, float e, float A, float iq, float D, float E5,
                                         float &op, float &dop)
 {
-  const float x = e * iq;
-  const float y = rcp_fast(1.0f + x);
-  const float y2 = y * y, y4 = y2 * y2;
-  const float s = 1.0f + y + y2 + y2 * y + y4 + y4 * y + y4 * y2;   // sum_{k=0..6} y^k
-  op = lapv - A * x * y * s;                                        // A ((1+x)^-7 - 1)
-  dop = dl - 7.0f * A * iq * (y4 * y4);                             // -7 A iq (1+x)^-8
+  // explicitly rounded operations throughout (see lapf_acc)
+  const float x = __fmul_rn(e, iq);
+  const float y = rcp_fast(__fadd_rn(1.0f, x));
+  const float y2 = __fmul_rn(y, y), y4 = __fmul_rn(y2, y2);
+  float s = __fadd_rn(__fadd_rn(1.0f, y), y2);                     // sum_{k=0..6} y^k
+  s = __fadd_rn(__fadd_rn(s, __fmul_rn(y2, y)), y4);
+  s = __fadd_rn(__fadd_rn(s, __fmul_rn(y4, y)), __fmul_rn(y4, y2));
+  op = __fsub_rn(lapv, __fmul_rn(__fmul_rn(__fmul_rn(A, x), y), s));                   // A ((1+x)^-7 - 1)
+  dop = __fsub_rn(dl, __fmul_rn(__fmul_rn(__fmul_rn(7.0f, A), iq), __fmul_rn(y4, y4)));  // -7 A iq (1+x)^-8
   if (EQ == 1) {
     // d e + E5 ((1+x)^5 - 1),  E5 = e_coef (c+u)^5
-    op += D * e + E5 * x * (5.0f + x * (10.0f + x * (10.0f + x * (5.0f + x))));
-    const float x1 = 1.0f + x, x2 = x1 * x1;
-    dop += D + 5.0f * E5 * iq * (x2 * x2);
+    float p = __fadd_rn(5.0f, x);
+    p = __fadd_rn(10.0f, __fmul_rn(x, p));
+    p = __fadd_rn(10.0f, __fmul_rn(x, p));
+    p = __fadd_rn(5.0f, __fmul_rn(x, p));
+    op = __fadd_rn(op, __fadd_rn(__fmul_rn(D, e), __fmul_rn(__fmul_rn(E5, x), p)));
+    const float x1 = __fadd_rn(1.0f, x), x2 = __fmul_rn(x1, x1);
+    dop = __fadd_rn(dop, __fadd_rn(D, __fmul_rn(__fmul_rn(__fmul_rn(5.0f, E5), iq), __fmul_rn(x2, x2))));
   }
+}
+
+// One point's smoother update e - (op - S) / dop, explicitly rounded: every
+// FP32 smoother (per colour, cluster-resident) forms it here.
+__device__ __forceinline__ float corr_update(float e, float op, float dop, float S)
+{
+  return __fsub_rn(e, __fmul_rn(__fsub_rn(op, S), rcp_fast(dop)));
 }
 
 // ---------------------------------------------------------------------------
@@ -272,7 +299,7 @@ __device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, l
 // lexicographic fields; the values, and so the bits, are the same.
 template <int ORD, int EQ>
 __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
-                                                  const float2 *__restrict__ aq, int color, Stats *stats)
+                                                  const float2 *aq, int color, Stats *stats)
 {
   constexpr int NC = num_colors<ORD>();
   griddep_wait();                 // launched as a programmatic dependent
@@ -297,15 +324,18 @@ __global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__res
   const float lv = lapf<ORD>(e, p, B.n[0], (long long)B.n[0] * B.n[1], B);
   float op, dop;
   if (aq) {
-    const float2 a = __ldg(aq + B.off + (((long long)color * m2 + (k - b)) * m1 + (j - b)) * H + ih);
+    // through L2 (ld.global.cg), not the read-only path: this kernel starts
+    // as a programmatic dependent, and a read-only cache line of aq left on
+    // the SM by the previous cycle's passes was seen stale after the next
+    // cycle's k_mx_prep had rewritten aq
+    const float2 a = __ldcg(aq + B.off + (((long long)color * m2 + (k - b)) * m1 + (j - b)) * H + ih);
     const long long q = B.off + p;
     corr_op<EQ>(lv, (float)B.dulap, e[p], a.x, a.y, EQ == 1 ? G.f[G_D][q] : 0.0f, EQ == 1 ? G.f[G_E5][q] : 0.0f, op,
                 dop);
   } else {
     corr_at<EQ>(B, G, p, lv, op, dop);
   }
-  const float R = op - G.f[G_S][B.off + p];
-  const float en = e[p] - R * rcp_fast(dop);
+  const float en = corr_update(e[p], op, dop, G.f[G_S][B.off + p]);
   e[p] = en;
   if (!(en == en)) atomicOr(nan_flag, 1);
 }

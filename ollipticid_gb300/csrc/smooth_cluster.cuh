@@ -9,8 +9,9 @@
 // planes of other blocks).  The colours of a sweep are separated by cluster
 // barriers, so a sweep costs no kernel launch and no HBM round trip of e; the
 // read-only coefficients (A, 1/(c+u), source) come from L2.  The update of a
-// point is the same expression as in k_smooth32 (lapf_acc, corr_op), so the
-// result equals the per-colour launches' bit for bit.
+// point is the same explicitly rounded expression as in k_smooth32 (lapf_acc,
+// corr_op, corr_update), so the result equals the per-colour launches' bit
+// for bit.
 //
 // The interior planes are split evenly (the ghost planes, which are read but
 // not updated, go with the first and the last block), so every block has the
@@ -147,8 +148,7 @@ __global__ void __launch_bounds__(kSmoothClusterThreads, 1)
           const float2 aqv = __ldg(gaq + pk[u]);
           corr_op<EQ>(lv, dl, c, aqv.x, aqv.y, EQ == 1 ? __ldg(gd + p) : 0.0f, EQ == 1 ? __ldg(ge5 + p) : 0.0f,
                       op, dop);
-          const float R = op - __ldg(gs + p);
-          en[u] = c - R * rcp_fast(dop);
+          en[u] = corr_update(c, op, dop, __ldg(gs + p));
         }
 #pragma unroll
         for (int u = 0; u < U; u++)

@@ -30,6 +30,9 @@ Needs the reference sources; run in the build container only:
     make -C oracle ref && python tests/golden/make_config_golden.py [config1 config2 config3]
 
 Reference dumps are kept under /tmp/config_golden/ and reused when present.
+CONFIG_GOLDEN_FIXED_TOL in the environment changes the fixed point's bound
+on max |du| (default 1e-14) and CONFIG_GOLDEN_OUT the output folder; each
+cycle of the oracle's fixed point is logged to stderr.
 """
 import os
 import subprocess
@@ -41,7 +44,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
-OUT = os.path.join(HERE, "configs")
+OUT = os.environ.get("CONFIG_GOLDEN_OUT", os.path.join(HERE, "configs"))
 WORK = "/tmp/config_golden"
 sys.path.insert(0, ROOT)
 
@@ -50,7 +53,7 @@ from tests.golden.make_golden import read_meta  # noqa: E402
 
 CONFIGS = {"config1": CONFIG1, "config2": CONFIG2, "config3": CONFIG3}
 FIXED_FROM = {"config1": "reference", "config2": "reference", "config3": "oracle"}
-FIXED_TOL, FIXED_MAX = 1e-14, 120
+FIXED_TOL, FIXED_MAX = float(os.environ.get("CONFIG_GOLDEN_FIXED_TOL", "1e-14")), 120
 RANDOM_POINTS = 2048
 
 
@@ -115,6 +118,7 @@ def oracle_fixed(args, cyc2_dir):
         orc.vcycle()
         cur = orc.all_u()
         deltas.append(max(float(np.max(np.abs(a - b))) for a, b in zip(cur, prev)))
+        print(f"fixed-point cycle {len(deltas)}: max |du| = {deltas[-1]:.3e}", file=sys.stderr, flush=True)
         prev = cur
         if deltas[-1] <= FIXED_TOL:
             break
