@@ -36,35 +36,31 @@ struct DevFields32 {
 template <int ORD, class Acc>
 __device__ __forceinline__ float lapf_acc(float c, Acc at, float ix2, float iy2, float iz2)
 {
+  // the axes' terms scaled and summed by explicit multiply-adds
+  auto sum3 = [&](float a0, float a1, float a2) {
+    return __fmaf_rn(a2, iz2, __fmaf_rn(a1, iy2, __fmul_rn(a0, ix2)));
+  };
+  auto pair = [&](int a, int d) { return __fadd_rn(at(a, d), at(a, -d)); };
   if (ORD == 2) {
-    auto ax = [&](int a) { return __fadd_rn(__fadd_rn(at(a, 1), __fmul_rn(-2.0f, c)), at(a, -1)); };
-    return __fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2));
+    auto ax = [&](int a) { return __fadd_rn(__fmaf_rn(-2.0f, c, at(a, 1)), at(a, -1)); };
+    return sum3(ax(0), ax(1), ax(2));
   } else if (ORD == 4) {
-    auto ax = [&](int a) {
-      return __fadd_rn(__fadd_rn(-__fadd_rn(at(a, 2), at(a, -2)), __fmul_rn(16.0f, __fadd_rn(at(a, 1), at(a, -1)))),
-                       __fmul_rn(-30.0f, c));
-    };
-    return __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2)),
-                     1.0f / 12.0f);
+    auto ax = [&](int a) { return __fmaf_rn(-30.0f, c, __fmaf_rn(16.0f, pair(a, 1), -pair(a, 2))); };
+    return __fmul_rn(sum3(ax(0), ax(1), ax(2)), 1.0f / 12.0f);
   } else if (ORD == 6) {
     auto ax = [&](int a) {
-      float v = __fmul_rn(2.0f, __fadd_rn(at(a, 3), at(a, -3)));
-      v = __fadd_rn(v, __fmul_rn(-27.0f, __fadd_rn(at(a, 2), at(a, -2))));
-      v = __fadd_rn(v, __fmul_rn(270.0f, __fadd_rn(at(a, 1), at(a, -1))));
-      return __fadd_rn(v, __fmul_rn(-490.0f, c));
+      const float v = __fmaf_rn(-27.0f, pair(a, 2), __fmul_rn(2.0f, pair(a, 3)));
+      return __fmaf_rn(-490.0f, c, __fmaf_rn(270.0f, pair(a, 1), v));
     };
-    return __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2)),
-                     1.0f / 180.0f);
+    return __fmul_rn(sum3(ax(0), ax(1), ax(2)), 1.0f / 180.0f);
   } else {
     auto ax = [&](int a) {
-      float v = __fmul_rn(-9.0f, __fadd_rn(at(a, 4), at(a, -4)));
-      v = __fadd_rn(v, __fmul_rn(128.0f, __fadd_rn(at(a, 3), at(a, -3))));
-      v = __fadd_rn(v, __fmul_rn(-1008.0f, __fadd_rn(at(a, 2), at(a, -2))));
-      v = __fadd_rn(v, __fmul_rn(8064.0f, __fadd_rn(at(a, 1), at(a, -1))));
-      return __fadd_rn(v, __fmul_rn(-14350.0f, c));
+      float v = __fmaf_rn(128.0f, pair(a, 3), __fmul_rn(-9.0f, pair(a, 4)));
+      v = __fmaf_rn(-1008.0f, pair(a, 2), v);
+      v = __fmaf_rn(8064.0f, pair(a, 1), v);
+      return __fmaf_rn(-14350.0f, c, v);
     };
-    return __fmul_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax(0), ix2), __fmul_rn(ax(1), iy2)), __fmul_rn(ax(2), iz2)),
-                     1.0f / 5040.0f);
+    return __fmul_rn(sum3(ax(0), ax(1), ax(2)), 1.0f / 5040.0f);
   }
 }
 
@@ -83,32 +79,32 @@ template <int EQ>
 __device__ __forceinline__ void corr_op(float lapv, float dl, float e, float A, float iq, float D, float E5,
                                         float &op, float &dop)
 {
-  // explicitly rounded operations throughout (see lapf_acc)
+  // explicitly rounded operations and multiply-adds throughout (see lapf_acc)
   const float x = __fmul_rn(e, iq);
   const float y = rcp_fast(__fadd_rn(1.0f, x));
   const float y2 = __fmul_rn(y, y), y4 = __fmul_rn(y2, y2);
   float s = __fadd_rn(__fadd_rn(1.0f, y), y2);                     // sum_{k=0..6} y^k
-  s = __fadd_rn(__fadd_rn(s, __fmul_rn(y2, y)), y4);
-  s = __fadd_rn(__fadd_rn(s, __fmul_rn(y4, y)), __fmul_rn(y4, y2));
-  op = __fsub_rn(lapv, __fmul_rn(__fmul_rn(__fmul_rn(A, x), y), s));                   // A ((1+x)^-7 - 1)
-  dop = __fsub_rn(dl, __fmul_rn(__fmul_rn(__fmul_rn(7.0f, A), iq), __fmul_rn(y4, y4)));  // -7 A iq (1+x)^-8
+  s = __fadd_rn(__fmaf_rn(y2, y, s), y4);
+  s = __fmaf_rn(y4, y2, __fmaf_rn(y4, y, s));
+  op = __fmaf_rn(-__fmul_rn(__fmul_rn(A, x), y), s, lapv);                        // A ((1+x)^-7 - 1)
+  dop = __fmaf_rn(-__fmul_rn(__fmul_rn(7.0f, A), iq), __fmul_rn(y4, y4), dl);    // -7 A iq (1+x)^-8
   if (EQ == 1) {
     // d e + E5 ((1+x)^5 - 1),  E5 = e_coef (c+u)^5
     float p = __fadd_rn(5.0f, x);
-    p = __fadd_rn(10.0f, __fmul_rn(x, p));
-    p = __fadd_rn(10.0f, __fmul_rn(x, p));
-    p = __fadd_rn(5.0f, __fmul_rn(x, p));
-    op = __fadd_rn(op, __fadd_rn(__fmul_rn(D, e), __fmul_rn(__fmul_rn(E5, x), p)));
+    p = __fmaf_rn(x, p, 10.0f);
+    p = __fmaf_rn(x, p, 10.0f);
+    p = __fmaf_rn(x, p, 5.0f);
+    op = __fadd_rn(op, __fmaf_rn(D, e, __fmul_rn(__fmul_rn(E5, x), p)));
     const float x1 = __fadd_rn(1.0f, x), x2 = __fmul_rn(x1, x1);
-    dop = __fadd_rn(dop, __fadd_rn(D, __fmul_rn(__fmul_rn(__fmul_rn(5.0f, E5), iq), __fmul_rn(x2, x2))));
+    dop = __fadd_rn(dop, __fmaf_rn(__fmul_rn(__fmul_rn(5.0f, E5), iq), __fmul_rn(x2, x2), D));
   }
 }
 
-// One point's smoother update e - (op - S) / dop, explicitly rounded: every
+// One point's smoother update e - (op - S) / dop, one explicit multiply-add: every
 // FP32 smoother (per colour, cluster-resident) forms it here.
 __device__ __forceinline__ float corr_update(float e, float op, float dop, float S)
 {
-  return __fsub_rn(e, __fmul_rn(__fsub_rn(op, S), rcp_fast(dop)));
+  return __fmaf_rn(-__fsub_rn(op, S), rcp_fast(dop), e);
 }
 
 // ---------------------------------------------------------------------------
