@@ -289,12 +289,15 @@ __device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, l
               EQ == 1 ? G.f[G_E5][q] : 0.0f, op, dop);
 }
 
-// One multicolour pass on e (colour (i+j+k) mod (order/2+1)).  A and
+// One multicolour pass on e (colour (i+j+k) mod (order/2+1)).  Held to 32
+// registers at orders 4 and 8 (no spills there), so that 16 of its 128-thread
+// blocks fit an SM: the pass waits on loads, and at 40 registers (12 blocks)
+// it ran 4 % slower.  A and
 // 1/(c+u) come colour-packed from aq (one float2 per point, the pass's points
 // contiguous: packed_index) when the hierarchy keeps that copy, else from the
 // lexicographic fields; the values, and so the bits, are the same.
 template <int ORD, int EQ>
-__global__ void __launch_bounds__(256) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
+__global__ void __launch_bounds__(256, ORD == 4 || ORD == 8 ? 8 : 6) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
                                                   const float2 *aq, int color, Stats *stats)
 {
   constexpr int NC = num_colors<ORD>();
