@@ -289,16 +289,20 @@ __device__ __forceinline__ void corr_at(const DevBox &B, const DevFields32 &G, l
               EQ == 1 ? G.f[G_E5][q] : 0.0f, op, dop);
 }
 
-// One multicolour pass on e (colour (i+j+k) mod (order/2+1)).  Held to 32
-// registers at orders 4 and 8 (no spills there), so that 16 of its 128-thread
-// blocks fit an SM: the pass waits on loads, and at 40 registers (12 blocks)
-// it ran 4 % slower.  A and
-// 1/(c+u) come colour-packed from aq (one float2 per point, the pass's points
+// One multicolour pass on e (colour (i+j+k) mod (order/2+1)), PTS points of
+// a row's colour a thread (their loads first, then the updates: points of
+// one colour do not read each other, so any PTS gives the same bits).  Held
+// to 32 registers at order 4 with one point a thread (no spills there), so
+// that 16 of its 128-thread blocks fit an SM: the pass waits on loads, and
+// at 40 registers (12 blocks) it ran 4 % slower; the other forms get the
+// registers they need without spilling.  A and 1/(c+u)
+// come colour-packed from aq (one float2 per point, the pass's points
 // contiguous: packed_index) when the hierarchy keeps that copy, else from the
-// lexicographic fields; the values, and so the bits, are the same.
-template <int ORD, int EQ>
-__global__ void __launch_bounds__(256, ORD == 4 || ORD == 8 ? 8 : 6) k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G,
-                                                  const float2 *aq, int color, Stats *stats)
+// lexicographic fields; the values, and so the bits, are the same.  Each is
+// used once, so aq is read through L2 (ld.global.cg).
+template <int ORD, int EQ, int PTS = 1>
+__global__ void __launch_bounds__(256, PTS == 1 ? (ORD == 4 ? 8 : 6) : 4)
+    k_smooth32(BoxList L, const DevBox *__restrict__ boxes, DevFields32 G, const float2 *aq, int color, Stats *stats)
 {
   constexpr int NC = num_colors<ORD>();
   griddep_wait();                 // launched as a programmatic dependent
@@ -309,34 +313,46 @@ __global__ void __launch_bounds__(256, ORD == 4 || ORD == 8 ? 8 : 6) k_smooth32(
   const int b = B.buf;
   const int m0 = B.n[0] - 2 * b, m1 = B.n[1] - 2 * b, m2 = B.n[2] - 2 * b;
   const int H = (m0 + NC - 1) / NC;
+  const int HP = (H + PTS - 1) / PTS;
   const long long t = lb * blockDim.x + threadIdx.x;
-  if (t >= (long long)H * m1 * m2) return;
-  const int ih = ((int)t % H);
-  const int r = (int)t / H;
+  if (t >= (long long)HP * m1 * m2) return;
+  const int ihp = ((int)t % HP);
+  const int r = (int)t / HP;
   const int j = b + (r % m1);
   const int k = b + (r / m1);
   const int delta = (((color - b - j - k) % NC) + NC) % NC;
-  const int i = b + delta + NC * ih;
-  if (i >= B.n[0] - b) return;
   float *e = G.f[G_E] + B.off;
-  const long long p = pidx(B, i, j, k);
-  const float lv = lapf<ORD>(e, p, B.n[0], (long long)B.n[0] * B.n[1], B);
-  float op, dop;
-  if (aq) {
-    // through L2 (ld.global.cg), not the read-only path: this kernel starts
-    // as a programmatic dependent, and a read-only cache line of aq left on
-    // the SM by the previous cycle's passes was seen stale after the next
-    // cycle's k_mx_prep had rewritten aq
-    const float2 a = __ldcg(aq + B.off + (((long long)color * m2 + (k - b)) * m1 + (j - b)) * H + ih);
-    const long long q = B.off + p;
-    corr_op<EQ>(lv, (float)B.dulap, e[p], a.x, a.y, EQ == 1 ? G.f[G_D][q] : 0.0f, EQ == 1 ? G.f[G_E5][q] : 0.0f, op,
-                dop);
-  } else {
-    corr_at<EQ>(B, G, p, lv, op, dop);
+  const long long sy = B.n[0], sz = (long long)B.n[0] * B.n[1];
+  const long long prow = aq ? B.off + (((long long)color * m2 + (k - b)) * m1 + (j - b)) * H : 0;
+  float en[PTS];
+  long long pp[PTS];
+  bool ok[PTS];
+#pragma unroll
+  for (int q = 0; q < PTS; q++) {
+    const int ih = ihp * PTS + q;
+    const int i = b + delta + NC * ih;
+    ok[q] = i < B.n[0] - b;
+    const int ihq = ok[q] ? ih : 0;   // a point past the row's end repeats the row's first point
+    const long long p = pidx(B, b + delta + NC * ihq, j, k);
+    pp[q] = p;
+    const float lv = lapf<ORD>(e, p, sy, sz, B);
+    float op, dop;
+    if (aq) {
+      const float2 a = __ldcg(aq + prow + ihq);
+      const long long g = B.off + p;
+      corr_op<EQ>(lv, (float)B.dulap, e[p], a.x, a.y, EQ == 1 ? G.f[G_D][g] : 0.0f, EQ == 1 ? G.f[G_E5][g] : 0.0f,
+                  op, dop);
+    } else {
+      corr_at<EQ>(B, G, p, lv, op, dop);
+    }
+    en[q] = corr_update(e[p], op, dop, G.f[G_S][B.off + p]);
   }
-  const float en = corr_update(e[p], op, dop, G.f[G_S][B.off + p]);
-  e[p] = en;
-  if (!(en == en)) atomicOr(nan_flag, 1);
+#pragma unroll
+  for (int q = 0; q < PTS; q++)
+    if (ok[q]) {
+      e[pp[q]] = en[q];
+      if (!(en[q] == en[q])) atomicOr(nan_flag, 1);
+    }
 }
 
 // R = N^u(e) on INSIDE points

@@ -275,6 +275,9 @@ struct olgpu_hierarchy {
   bool robin_split = std::getenv("OLGPU_ROBIN_SPLIT") != nullptr;
   // FP64 smoother points per thread (1 or 2: OLGPU_SMOOTH_PTS); the same bits
   int smooth_pts = std::getenv("OLGPU_SMOOTH_PTS") && std::atoi(std::getenv("OLGPU_SMOOTH_PTS")) == 2 ? 2 : 1;
+  // points of a row a thread in the per-colour FP32 smoother (1, or 2 with
+  // OLGPU_SMOOTH32_PTS=2: the same bits, 2-5 % slower with many solves)
+  int smooth32_pts = std::getenv("OLGPU_SMOOTH32_PTS") && std::atoi(std::getenv("OLGPU_SMOOTH32_PTS")) == 2 ? 2 : 1;
   // The solves this hierarchy steps: alone, one (itself); a union of solves
   // (olgpu_batch) steps every member's boxes in shared launches, their levels
   // aligned from the top (a member's level k is the union's level k + off).
@@ -1137,8 +1140,12 @@ void launch_smooth32(olgpu_hierarchy *h, const BoxList &L, int nu)
   if (L.count == 0) return;
   for (int s = 0; s < nu; s++)
     for (int color = 0; color < num_colors<ORD>(); color++) {
-      launch_pdl(h, k_smooth32<ORD, EQ>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
-                 (const DevBox *)h->d_boxes, h->F32, (const float2 *)h->d_aq, color, h->d_stats0);
+      if (h->smooth32_pts == 2)
+        launch_pdl(h, k_smooth32<ORD, EQ, 2>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
+                   (const DevBox *)h->d_boxes, h->F32, (const float2 *)h->d_aq, color, h->d_stats0);
+      else
+        launch_pdl(h, k_smooth32<ORD, EQ, 1>, (unsigned)L.blk[L.count], (unsigned)kSmoothThreads, L,
+                   (const DevBox *)h->d_boxes, h->F32, (const float2 *)h->d_aq, color, h->d_stats0);
       h->launches_mixed++;
     }
 }
@@ -1309,7 +1316,7 @@ void dispatch_smooth32(olgpu_hierarchy *h, int level, int nu)
     }
   }
   // the boxes no cluster holds: one launch per colour and sweep
-  const BoxList R = level_list_mask(h, level, blocks_color, fit, false);
+  const BoxList R = level_list_mask(h, level, h->smooth32_pts == 2 ? blocks_color2 : blocks_color, fit, false);
   switch (level_order(h, level)) {
   case 2: launch_smooth32<2, EQ>(h, R, nu); break;
   case 4: launch_smooth32<4, EQ>(h, R, nu); break;

@@ -96,23 +96,34 @@ def test_row_transfers_equal_point_transfers(case, mixed, monkeypatch):
         assert np.array_equal(a, b), f"box {g}: max diff {float(np.max(np.abs(a - b))):.3e}"
 
 
+LAYOUTS = {
+    "robin_split": {"OLGPU_ROBIN_SPLIT": "1"},
+    "fp64_two_points": {"OLGPU_SMOOTH_PTS": "2"},
+    "fp32_per_colour": {"OLGPU_SMOOTH32_LAUNCHES": "1"},
+    "fp32_per_colour_two_points": {"OLGPU_SMOOTH32_LAUNCHES": "1", "OLGPU_SMOOTH32_PTS": "2"},
+}
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", ["o2_single", "o4_binary_merge", "o8_offset"])
 @pytest.mark.parametrize("mixed", [False, True])
-@pytest.mark.parametrize("variant", ["OLGPU_ROBIN_SPLIT", "OLGPU_SMOOTH_PTS"])
+@pytest.mark.parametrize("variant", sorted(LAYOUTS))
 def test_launch_layouts_give_the_same_bits(case, mixed, variant, monkeypatch):
-    """The Robin walk as separate face, edge and corner launches
-    (OLGPU_ROBIN_SPLIT) and the FP64 smoother with two points a thread
-    (OLGPU_SMOOTH_PTS=2) give the default launches' u bit for bit."""
+    """The Robin walk as separate face, edge and corner launches, the FP64
+    smoother with two points a thread, and the FP32 smoother as per-colour
+    launches (two points or one a thread) instead of cluster-resident give
+    the default launches' u bit for bit, over five cycles (a difference of
+    the compiler's fusion between two kernels once showed from the third)."""
     import ollipticid_gb300 as og
     P = problem(case)
     out = []
     for alt in (False, True):
         if alt:
-            monkeypatch.setenv(variant, "2" if variant == "OLGPU_SMOOTH_PTS" else "1")
+            for k, v in LAYOUTS[variant].items():
+                monkeypatch.setenv(k, v)
         with og.Elliptic(P) as E:
             E.set_precision(mixed)
-            for _ in range(3):
+            for _ in range(5):
                 E.FASN()
             out.append([E.get_field(g) for g in range(len(E.boxes))])
     for g, (a, b) in enumerate(zip(*out)):
