@@ -141,9 +141,9 @@ def anderson_fixed(orc, m):
     m on the vector of every box's u: x <- x + f - (dX + dF) gamma with
     f = G(x) - x and gamma the least-squares fit of f by the last m changes
     of f (normal equations, slightly regularised).  Near the rounding floor
-    of G the mixing stops helping; when a step makes the change of a plain
-    cycle more than twice the best seen, the history restarts from the best
-    iterate.  Stops when a plain cycle from the current iterate changes u by
+    of G the mixing stops helping; when four cycles in a row have not
+    improved on the smallest change of a plain cycle seen, the history
+    restarts from the best iterate.  Stops when a plain cycle from the current iterate changes u by
     at most FIXED_TOL, or after FIXED_MAX cycles; returns the plain cycle's
     result from the best iterate, and the changes up to it."""
     shapes = [(b.nz, b.ny, b.nx) for b in orc.boxes]
@@ -162,6 +162,7 @@ def anderson_fixed(orc, m):
     dX, dF, deltas = [], [], []
     x_prev = f_prev = None
     best = (np.inf, None, None, 0)   # (change, x, G(x), cycles so far)
+    since = 0                        # cycles since the best
     for _ in range(FIXED_MAX):
         put(x)
         orc.vcycle()
@@ -172,10 +173,14 @@ def anderson_fixed(orc, m):
         print(f"anderson cycle {len(deltas)}: max |du| of a plain cycle = {d:.3e}", file=sys.stderr, flush=True)
         if d < best[0]:
             best = (d, x, gx, len(deltas))
+            since = 0
+        else:
+            since += 1
         if d <= FIXED_TOL:
             break
-        if d > 2.0 * best[0]:   # restart from the best iterate
-            x, dX, dF, x_prev, f_prev = best[1], [], [], None, None
+        if since >= 4:   # no progress: restart from the best iterate's plain step
+            x, dX, dF, x_prev, f_prev = best[2], [], [], None, None
+            since = 0
             continue
         if f_prev is not None:
             dX.append(x - x_prev)

@@ -69,8 +69,8 @@ def geometry_matches(E, g):
 
 # the cycle's change of u at which the GPU's fixed point is taken: far below
 # the bar, and above the rounding floor of the 8th-order cycle on 129^3
-# boxes (about 1e-11 for the oracle's own cycle there)
-FIXED_DU = {"config1": 1e-13, "config2": 1e-13, "config3": 1e-12}
+# boxes (the oracle's own cycle levels off at a few 1e-12 there)
+FIXED_DU = {"config1": 1e-13, "config2": 1e-13, "config3": 5e-12}
 
 
 @pytest.mark.gpu
