@@ -701,6 +701,47 @@ def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None
             "vs_plain_fp64": rep["throughput_solves_per_s"] / plain_rate}
 
 
+def run_served_binaries_batching(count: int = 256, rate: float = 400.0, inner_sweeps=None, plain_rate=None,
+                                 batch_max: int = 16, batch_window: float = 0.05, max_active: int = 64):
+    """The same Poisson stream of the batched workload's binaries through the
+    C++ server with batching: requests admitted together (up to batch_max,
+    after at most batch_window seconds) are solved as one batch
+    (olgpu_batch_*) on a builder thread, several batches at once.  The
+    results carry no u (a batch's hierarchies are not handed out), so each
+    result with an oracle fixture is checked by its ADM masses, and its
+    cycles are reported."""
+    import numpy as np
+    from ollipticid_gb300 import _abi, workloads
+    from ollipticid_gb300.serve import NativeServer
+    path = os.path.join(GOLDEN, "batched.npz")
+    fx = np.load(path) if os.path.exists(path) else None
+    stream = workloads.served_binaries(count, rate)
+    with NativeServer(mem_budget=200 << 30, max_active=max_active, builders=8, inner_sweeps=inner_sweeps,
+                      stop=_abi.STOP_ERROR, tol=1e-10, du_tol=DU_TOL, max_cycles=300, batch_max=batch_max,
+                      batch_window=batch_window) as S:
+        rep = S.run(stream)
+    adm_err = []
+    if fx is not None:
+        for inst in (int(i) for i in fx["instances"]):
+            r = rep["results"][inst]
+            want = fx[f"inst{inst}_adm"]
+            adm_err.append(max(abs(a - b) for a, b in zip(r.adm, want)))
+    statuses = [r.status for r in rep["results"]]
+    out = {"workload": f"{count} seeded binaries of the batched workload as a Poisson stream at {rate:g} "
+                       f"requests/s, C++ server batching up to {batch_max} admitted requests (window "
+                       f"{batch_window:g} s, {max_active} slots), mixed precision, residual <= 1e-10 and change of "
+                       f"u <= {DU_TOL:g}",
+           **{k: rep[k] for k in ("throughput_solves_per_s", "latency_p50_s", "latency_p99_s", "latency_max_s",
+                                  "cycles_mean", "peak_concurrent_solves", "makespan_s")},
+           "failed": sum(1 for x in statuses if x != 0),
+           "oracle_checked_results": len(adm_err), "max_abs_adm_minus_oracle": max(adm_err) if adm_err else None,
+           "inner_sweeps": list(inner_sweeps) if inner_sweeps else None}
+    if plain_rate:
+        out["plain_fp64_same_binaries_solves_per_s"] = plain_rate
+        out["vs_plain_fp64"] = rep["throughput_solves_per_s"] / plain_rate
+    return out
+
+
 def slowest_rank_ms(ms: float, world: int, device) -> float:
     """The timed region's length: the maximum over ranks (replicas run the
     same work; the job is done when the slowest one is)."""
@@ -802,7 +843,8 @@ def run_gpu(args, rank: int, world: int, local: int):
     # ---- the same workload with the mixed-precision cycle
     mixed = run_mixed(E, P, args, dev, u_fix, fx)
 
-    concurrent = batched = served = served_binaries = config3 = convergence = approx_start = None
+    concurrent = batched = served = served_binaries = served_binaries_batching = None
+    config3 = convergence = approx_start = None
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, fx, value / world)
@@ -817,6 +859,8 @@ def run_gpu(args, rank: int, world: int, local: int):
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
         served_binaries = run_served_binaries(
+            inner_sweeps=(tuned_batch.nu1, tuned_batch.nu2, tuned_batch.blocks), plain_rate=plain_bin)
+        served_binaries_batching = run_served_binaries_batching(
             inner_sweeps=(tuned_batch.nu1, tuned_batch.nu2, tuned_batch.blocks), plain_rate=plain_bin)
 
     # ---- roofline of the dominant kernel: one colour pass of the FP64
@@ -868,7 +912,8 @@ def run_gpu(args, rank: int, world: int, local: int):
                       "adm": [reps[-1].adm[0], reps[-1].adm[1]], "wall_s": wall},
             "accuracy": accuracy, "plain_fp64_unaccelerated": unaccelerated,
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served,
-            "served_binaries": served_binaries, "config3": config3,
+            "served_binaries": served_binaries, "served_binaries_batching": served_binaries_batching,
+            "config3": config3,
             "convergence": convergence, "approx_start": approx_start,
             "roofline": roof, "roofline_fp32_smoother": roof32, "fma_peaks": fma, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches,

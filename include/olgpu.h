@@ -314,7 +314,12 @@ olgpu_status olgpu_reset(olgpu_hierarchy *h);
  * work of different requests overlaps on the device; a finished solve frees
  * its memory at once and the next request takes its place.  A request whose
  * footprint exceeds mem_budget is refused with OLGPU_ERR_OOM.  Each result is
- * the one the same problem gives solved alone, bit for bit.
+ * the one the same problem gives solved alone, bit for bit.  With
+ * batch_max >= 2 the requests admitted together (up to batch_max, once as
+ * many wait or the oldest has waited batch_window) are solved as one batch
+ * (olgpu_batch_*: one launch per FASN step over all of them) on a builder
+ * thread, several batches at once; each result is reported when its batch
+ * ends, and keep_solutions is refused.
  * olgpu_server_submit and olgpu_server_poll may be called from any thread. */
 typedef struct olgpu_server olgpu_server;
 
@@ -335,6 +340,12 @@ typedef struct {
                                    to the caller in olgpu_server_result.h      */
   double du_tol;                /* OLGPU_STOP_ERROR's bound on a cycle's change
                                    of u; <= 0: the tolerance                   */
+  int batch_max;                /* >= 2: admitted requests are solved together as
+                                   batches (olgpu_batch_*) of up to batch_max;
+                                   0 or 1: one hierarchy per request           */
+  double batch_window;          /* batching: seconds the oldest waiting request
+                                   waits for a batch to fill before it is
+                                   admitted with those waiting beside it       */
 } olgpu_server_config;
 
 typedef struct {

@@ -57,7 +57,7 @@ class ServerConfig(C.Structure):
         ("device", C.c_int), ("mem_budget", C.c_longlong), ("max_active", C.c_int), ("precision", C.c_int),
         ("stop", C.c_int), ("max_cycles", C.c_int), ("tol", C.c_double), ("builders", C.c_int),
         ("nu1", C.c_int), ("nu2", C.c_int), ("blocks", C.c_int), ("busy", C.c_int), ("keep_solutions", C.c_int),
-        ("du_tol", C.c_double),
+        ("du_tol", C.c_double), ("batch_max", C.c_int), ("batch_window", C.c_double),
     ]
 
 

@@ -7,7 +7,10 @@
 // Threads: `builders` threads make hierarchies (host geometry, plans, device
 // allocation, coefficients, graph capture); one scheduler thread admits
 // requests (arrival order; a slot and the device footprint must fit) and
-// keeps the next cycle of every admitted solve queued on its stream.
+// keeps the next cycle of every admitted solve queued on its stream.  With
+// batch_max >= 2 the scheduler admits requests in groups instead and a
+// builder thread makes and solves each group as one batch (olgpu_batch_*),
+// whose results are the solo solves' bit for bit too.
 #include "olgpu.h"
 
 #include <chrono>
@@ -73,6 +76,12 @@ struct Active {
   Track T;
 };
 
+// requests admitted together, solved as one batch
+struct Group {
+  std::vector<Request> rs;
+  long long bytes = 0;
+};
+
 }  // namespace
 
 struct olgpu_server {
@@ -85,6 +94,7 @@ struct olgpu_server {
   long long used = 0;                 // device bytes of admitted solves
   std::deque<Request> waiting;        // submitted, not yet admitted
   std::deque<Request> to_build;       // admitted, waiting for a builder
+  std::deque<Group> to_solve;         // batching: admitted groups, waiting for a builder
   std::vector<Built> built;           // built, not yet stepping
   int n_building = 0;                 // admitted and not yet stepping
   int n_active = 0, peak_active = 0;  // stepping (scheduler's list size)
@@ -93,8 +103,10 @@ struct olgpu_server {
   std::thread scheduler;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+  bool batching() const { return cfg.batch_max >= 2; }
   void builder_loop();
   void scheduler_loop();
+  void solve_group(Group &G);
   void finish(const Request &r, olgpu_status st, int cycles, double res, const double *adm, olgpu_hierarchy *keep,
               double du = 0.0);
 };
@@ -120,14 +132,79 @@ void olgpu_server::finish(const Request &r, olgpu_status st, int cycles, double 
   cv_done.notify_all();
 }
 
+// One admitted group as one batch: made, solved to the stop rule and
+// destroyed on this builder thread; every member's result is reported when
+// the batch ends.  A group whose batch cannot be made is retried one request
+// at a time, so that one bad request fails alone.
+void olgpu_server::solve_group(Group &G)
+{
+  const int n = (int)G.rs.size();
+  std::vector<olgpu_problem> ps(n);
+  for (int i = 0; i < n; i++) ps[i] = G.rs[i].p;
+  olgpu_batch_config bc;
+  olgpu_batch_config_defaults(&bc);
+  bc.device = cfg.device;
+  bc.precision = cfg.precision;
+  bc.nu1 = cfg.nu1;
+  bc.nu2 = cfg.nu2;
+  bc.blocks = cfg.blocks;
+  olgpu_batch *b = nullptr;
+  const olgpu_status st = olgpu_batch_create(ps.data(), n, &bc, &b);
+  if (st != OLGPU_OK) {
+    if (n > 1) {
+      for (const Request &r : G.rs) {
+        Group one;
+        one.rs.push_back(r);
+        one.bytes = r.bytes;
+        solve_group(one);
+      }
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> g(mu);
+      used -= G.bytes;
+      n_building -= n;
+    }
+    finish(G.rs[0], st, 0, 0.0, nullptr, nullptr);
+    cv_sched.notify_one();
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> g(mu);
+    n_building -= n;
+    n_active += n;
+    if (n_active > peak_active) peak_active = n_active;
+  }
+  const olgpu_stop_rule rule{cfg.stop, cfg.max_cycles, cfg.tol, cfg.du_tol};
+  std::vector<olgpu_report> reps(n);
+  olgpu_batch_solve(b, &rule, reps.data());   // each report holds its own status
+  olgpu_batch_destroy(b);
+  {
+    std::lock_guard<std::mutex> g(mu);
+    used -= G.bytes;
+    n_active -= n;
+  }
+  for (int i = 0; i < n; i++)
+    finish(G.rs[i], (olgpu_status)reps[i].status, reps[i].cycles, reps[i].final_res, reps[i].adm, nullptr,
+           reps[i].final_du);
+  cv_sched.notify_one();
+}
+
 void olgpu_server::builder_loop()
 {
   for (;;) {
     Request r;
     {
       std::unique_lock<std::mutex> g(mu);
-      cv_build.wait(g, [&] { return stopping || !to_build.empty(); });
+      cv_build.wait(g, [&] { return stopping || !to_build.empty() || !to_solve.empty(); });
       if (stopping) return;
+      if (!to_solve.empty()) {
+        Group G = to_solve.front();
+        to_solve.pop_front();
+        g.unlock();
+        solve_group(G);
+        continue;
+      }
       r = to_build.front();
       to_build.pop_front();
     }
@@ -160,8 +237,28 @@ void olgpu_server::scheduler_loop()
     {
       std::unique_lock<std::mutex> g(mu);
       if (stopping) break;
+      // batching: admission in groups, once batch_max requests wait or the
+      // oldest has waited batch_window (arrival order, slots and footprint
+      // as below); a builder thread makes and solves each group
+      while (batching() && !waiting.empty() &&
+             ((int)waiting.size() >= cfg.batch_max || now() - waiting.front().arrival >= cfg.batch_window)) {
+        Group G;
+        while (!waiting.empty() && (int)G.rs.size() < cfg.batch_max && n_active + n_building < cfg.max_active &&
+               used + waiting.front().bytes <= cfg.mem_budget) {
+          Request r = waiting.front();
+          waiting.pop_front();
+          used += r.bytes;
+          G.bytes += r.bytes;
+          r.admitted = now();
+          n_building++;
+          G.rs.push_back(r);
+        }
+        if (G.rs.empty()) break;
+        to_solve.push_back(G);
+        cv_build.notify_one();
+      }
       // admission: arrival order, a slot and the footprint must fit
-      while (!waiting.empty() && n_active + n_building < cfg.max_active &&
+      while (!batching() && !waiting.empty() && n_active + n_building < cfg.max_active &&
              used + waiting.front().bytes <= cfg.mem_budget) {
         Request r = waiting.front();
         waiting.pop_front();
@@ -277,6 +374,8 @@ void olgpu_server_config_defaults(olgpu_server_config *c)
   c->busy = 4;
   c->keep_solutions = 0;
   c->du_tol = 0.0;
+  c->batch_max = 0;
+  c->batch_window = 0.02;
 }
 
 olgpu_status olgpu_server_create(const olgpu_server_config *c, olgpu_server **out)
@@ -284,7 +383,8 @@ olgpu_status olgpu_server_create(const olgpu_server_config *c, olgpu_server **ou
   if (!c || !out) return OLGPU_ERR_INVALID_ARG;
   if (c->max_active < 1 || c->builders < 1 || c->max_cycles < 1 || c->mem_budget <= 0 ||
       (c->precision != OLGPU_PREC_FP64 && c->precision != OLGPU_PREC_MIXED) || c->stop < OLGPU_STOP_REFERENCE ||
-      c->stop > OLGPU_STOP_ERROR)
+      c->stop > OLGPU_STOP_ERROR || c->batch_window < 0.0 ||
+      (c->batch_max >= 2 && c->keep_solutions))   // a batch's hierarchies are not handed out
     return OLGPU_ERR_INVALID_ARG;
   olgpu_server *s = new olgpu_server();
   s->cfg = *c;

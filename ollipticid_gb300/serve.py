@@ -221,10 +221,12 @@ class NativeServer:
     def __init__(self, device: int = 0, mem_budget: int = 64 << 30, max_active: int = 32, mixed: bool = True,
                  tol: Optional[float] = None, max_cycles: int = 200, builders: int = 2, keep_u: bool = False,
                  inner_sweeps: Optional[Tuple[int, ...]] = None, busy: int = 4, stop: int = _abi.STOP_TOLERANCE,
-                 du_tol: float = 0.0, keep_only=None):
+                 du_tol: float = 0.0, keep_only=None, batch_max: int = 0, batch_window: float = 0.02):
         """keep_u: hand every result's u back; keep_only (a set of indices
         into the stream given to run(), with keep_u) limits that to those
-        requests."""
+        requests.  batch_max >= 2: requests admitted together (up to
+        batch_max, after at most batch_window seconds of waiting) are solved
+        as one batch (no keep_u then)."""
         self.lib = _abi.load()
         self.keep_only = keep_only
         self._keep_rids = None
@@ -238,6 +240,7 @@ class NativeServer:
             c.blocks = inner_sweeps[2] if len(inner_sweeps) > 2 else -1
         c.keep_solutions = 1 if keep_u else 0
         c.du_tol = du_tol
+        c.batch_max, c.batch_window = batch_max, batch_window
         self.keep_u = keep_u
         s = C.c_void_p()
         check(self.lib.olgpu_server_create(C.byref(c), C.byref(s)))

@@ -79,7 +79,8 @@ int main(void)
   S(olgpu_problem); S(olgpu_box_info); S(olgpu_stop_rule); S(olgpu_report); S(olgpu_cycle_event);
   S(olgpu_server_config); S(olgpu_server_result); S(olgpu_box_fields);
   O(olgpu_stop_rule, du_tol); O(olgpu_report, final_du); O(olgpu_report, final_part); O(olgpu_server_config, du_tol);
-  O(olgpu_server_result, final_du); O(olgpu_problem, method);
+  O(olgpu_server_result, final_du); O(olgpu_problem, method); O(olgpu_server_config, batch_max);
+  O(olgpu_server_config, batch_window);
   return 0;
 }
 """

@@ -74,3 +74,33 @@ def test_native_server_admits_by_memory():
         rep = S.run([(0.0, p) for p in probs])
     assert [r.status for r in rep["results"]] == [0, 0, 0]
     assert rep["peak_concurrent_solves"] == 1
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mixed", [True, False], ids=["mixed", "fp64"])
+def test_native_server_batching_matches_solo_solves(mixed):
+    """The C++ server with batching (batch_max >= 2): requests admitted
+    together are solved as one batch; every result (status, cycles, final
+    norms, ADM masses) is the solo solve's bit for bit, and a request with a
+    NaN mass fails alone."""
+    import math
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    from ollipticid_gb300.serve import NativeServer
+    probs = [problem(n) for n in NAMES]
+    bad = problem("o4_spin")
+    bad.mp = [math.nan]
+    stream = [(0.0, p) for p in probs[:3]] + [(0.0, bad)] + [(0.01, p) for p in probs[3:]]
+    rule = dict(stop=_abi.STOP_ERROR, max_cycles=100, tol=1e-10)
+    with NativeServer(max_active=16, mixed=mixed, batch_max=4, batch_window=0.005, **rule) as S:
+        rep = S.run(stream)
+    res = rep["results"]
+    assert res[3].status == _abi.ERR_NAN
+    for i, p in enumerate(probs):
+        r = res[i if i < 3 else i + 1]
+        with og.Elliptic(p) as E:
+            E.set_precision(mixed)
+            solo = E.Solve(**rule)
+        assert r.status == _abi.OK and r.cycles == solo.cycles, (i, r.cycles, solo.cycles)
+        assert r.final_res == solo.final_res and r.final_du == solo.final_du
+        assert list(r.adm) == list(solo.adm[:p.numbh])

@@ -56,6 +56,33 @@ def test_server_config_is_checked():
     assert lib.olgpu_server_create(C.byref(cfg), C.byref(s)) == _abi.ERR_INVALID_ARG
 
 
+def test_server_batching_config_and_a_failed_batch():
+    """Batching (batch_max >= 2) refuses keep_solutions (a batch's
+    hierarchies are not handed out); without a device, a group's batch
+    cannot be made and every request of it fails with its own status."""
+    lib = _abi.load()
+    cfg = _abi.ServerConfig()
+    lib.olgpu_server_config_defaults(C.byref(cfg))
+    assert cfg.batch_max == 0 and cfg.batch_window > 0
+    cfg.batch_max, cfg.keep_solutions = 4, 1
+    s = C.c_void_p()
+    assert lib.olgpu_server_create(C.byref(cfg), C.byref(s)) == _abi.ERR_INVALID_ARG
+    cfg.keep_solutions, cfg.device, cfg.batch_window = 0, 9999, 0.0
+    assert lib.olgpu_server_create(C.byref(cfg), C.byref(s)) == _abi.OK
+    try:
+        ids = []
+        for name in ("o4_spin", "o2_single"):
+            p, rid = problem(name).to_c(), C.c_longlong()
+            assert lib.olgpu_server_submit(s, C.byref(p), C.byref(rid)) == _abi.OK
+            ids.append(rid.value)
+        out, done = _abi.ServerResult(), C.c_int()
+        for rid in ids:
+            assert lib.olgpu_server_poll(s, rid, 1, C.byref(done), C.byref(out)) == _abi.OK
+            assert done.value == 1 and out.id == rid and out.status != _abi.OK and not out.h
+    finally:
+        assert lib.olgpu_server_destroy(s) == _abi.OK
+
+
 def test_python_scheduler_refuses_a_wcycle_request():
     """The Python scheduler steps V-cycles too: a W-cycle request is refused
     on arrival, before any device work."""
