@@ -702,7 +702,7 @@ def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None
 
 
 def run_served_binaries_batching(count: int = 256, rate: float = 400.0, inner_sweeps=None, plain_rate=None,
-                                 batch_max: int = 16, batch_window: float = 0.05, max_active: int = 64):
+                                 batch_max: int = 16, batch_window: float = 0.02, max_active: int = 64):
     """The same Poisson stream of the batched workload's binaries through the
     C++ server with batching: requests admitted together (up to batch_max,
     after at most batch_window seconds) are solved as one batch
