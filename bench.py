@@ -45,6 +45,7 @@ UNIT = "solves/s"
 # this workload 1e-9 away).
 DU_TOL = 5e-11
 CONCURRENT_SOLVES = 16   # solves sharing the GPU in the concurrent and smoother-rate measurements
+SERVED_SLOTS = 24        # the C++ server's slots for the served binaries (16, 24, 32 measured: 24 ahead)
 ACCEL = 4   # Anderson depth of the plain FP64 iteration (FP64 history and sums)
 SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
 # DRAM bytes (read + write), FP64-pipe occupancy and FP64 instructions per
@@ -679,7 +680,7 @@ def run_served_binaries(count: int = 256, rate: float = 400.0, inner_sweeps=None
     fx = np.load(path) if os.path.exists(path) else None
     with_fx = set(int(i) for i in fx["instances"]) if fx is not None else set()
     stream = workloads.served_binaries(count, rate)
-    with NativeServer(mem_budget=200 << 30, max_active=16, builders=8, inner_sweeps=inner_sweeps,
+    with NativeServer(mem_budget=200 << 30, max_active=SERVED_SLOTS, builders=8, inner_sweeps=inner_sweeps,
                       stop=_abi.STOP_ERROR, tol=1e-10, du_tol=DU_TOL, keep_u=True, keep_only=with_fx,
                       max_cycles=300) as S:
         rep = S.run(stream)
