@@ -45,7 +45,7 @@ UNIT = "solves/s"
 # this workload 1e-9 away).
 DU_TOL = 5e-11
 CONCURRENT_SOLVES = 16   # solves sharing the GPU in the concurrent and smoother-rate measurements
-SERVED_SLOTS = 24        # the C++ server's slots for the served binaries (16, 24, 32 measured: 24 ahead)
+SERVED_SLOTS = 16        # the C++ server's slots for the served binaries (24 and 32 measured no faster)
 ACCEL = 4   # Anderson depth of the plain FP64 iteration (FP64 history and sums)
 SMOOTH_BYTES_PER_POINT = 40          # read u, b, c, S; write u (FP64)
 # DRAM bytes (read + write), FP64-pipe occupancy and FP64 instructions per
