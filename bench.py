@@ -821,17 +821,22 @@ def run_gpu(args, rank: int, world: int, local: int):
             buf[...] = 0.0 if src is None else src
             lst.append(buf)
     e2e_steps = max(1, min(args.steps, 5))
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+
+    def e2e_step():
         for g in range(nboxes):
             E.set_field(g, "b", hb[g])
             E.set_field(g, "c", hc[g])
         E.reset()
         for g in range(nboxes):
             E.set_field(g, "u", hu0[g])
-        rep = E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=DU_TOL)
+        E.Solve(stop=_abi.STOP_ERROR, max_cycles=300, tol=P.tol, du_tol=DU_TOL)
         for g in range(nboxes):
             E.get_field(g, "u", out=hu[g])
+
+    e2e_step()                    # untimed: the first transfers of the pinned buffers
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     # the hierarchy's set-up, outside the steps above (a resident solver
     # reuses it): host plan, device arena from the pool, tables, coefficients
