@@ -35,9 +35,11 @@ from . import Elliptic, Problem, _abi, solve_many
 CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((3, 20, 16), (3, 8, 16), (4, 6, 16), (4, 4, 16), (5, 4, 16),
                                                 (5, 6, 16), (6, 4, 16), (4, 6, 0), (3, 8, 0), (2, 4, 0))
 
-# candidates for batches: the schedules that win for many solves at once,
-# cluster-resident or per-colour smoothing
-BATCH_CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((4, 6, 16), (4, 6, 0), (4, 4, 16), (4, 4, 0))
+# candidates for batches: the schedules that win for many solves at once
+# (lighter ones win on the batched binaries: (3, 3) and (4, 3) ahead of
+# (4, 4) and (4, 6)), cluster-resident or per-colour smoothing
+BATCH_CANDIDATES: Tuple[Tuple[int, int, int], ...] = ((4, 6, 16), (4, 4, 16), (4, 4, 0), (4, 3, 0), (3, 3, 16),
+                                                      (3, 3, 0))
 
 _lock = threading.Lock()
 _memo: Dict[str, "Choice"] = {}
