@@ -7,7 +7,7 @@ FP64 under OLGPU_STOP_ERROR to a change of u far below the parity bar; u at
 the fixtures' sample points (tests/golden/configs, made by
 tests/golden/make_config_golden.py from the reference itself, or from the
 oracle where the reference's run is too long: the key `fixed_source`) must
-agree to 1e-10 on every level and the ADM masses to 1e-9, the benchmark spec's
+agree to 1e-10 on every level and the ADM masses to 1e-9, the parity
 bar.  The first problem is also compared on every point with the oracle's
 fixed point computed here (the oracle is pinned on this geometry by the same
 fixture, bit for bit, tests/test_oracle_configs.py).
