@@ -25,9 +25,12 @@ FIELDS = ("u", "b", "c", "d", "e", "rho", "r", "w", "ww", "v")
 
 
 # the equations on the FAS path: the puncture constraint, with a scalar
-# field, and the reference's test equations (the Gaussian test, a known
-# answer; Boundary-test; Multibox-test)
-EQUATIONS = {"Punctures": 0, "Punctures_scalar_field": 1, "Poisson": 2, "Boundary-test": 3, "Multibox-test": 4}
+# field, the reference's test equations (the Gaussian test, a known answer;
+# Boundary-test; Multibox-test) and the Bowen-York momentum-constraint test
+# (four unknowns V1, V2, V3, lambda: BY_VARS)
+EQUATIONS = {"Punctures": 0, "Punctures_scalar_field": 1, "Poisson": 2, "Boundary-test": 3, "Multibox-test": 4,
+             "Bowen-York": 5}
+BY_VARS = ("V1", "V2", "V3", "lambda")
 # the outer boundary conditions (-B): Robin, and Dirichlet, the reference's
 # default when -B is not given
 BOUNDARIES = {"Robin": 0, "Dirichlet": 1}

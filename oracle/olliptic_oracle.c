@@ -15,6 +15,14 @@
  * Floating-point expressions are written in the reference's evaluation order
  * (build with -ffp-contract=off) so that the iterates match the reference
  * bit for bit on the same host.
+ *
+ * Bowen-York (four unknowns V1, V2, V3, lambda, include/elliptic.h:772-803)
+ * is restated as its fixed point, not its iterates: the reference smooths
+ * and transfers the four together, this oracle solves V1, V2, V3 (each a
+ * Poisson problem with its own source) and then lambda with the divergence
+ * of the solved V as its source (orc_set_divergence_source).  The discrete
+ * system, and so its fixed point, is the same; it is pinned against the
+ * reference's own fixed point (tests/golden/bowen_york).
  */
 #define _GNU_SOURCE
 #include "olliptic_oracle.h"
@@ -621,12 +629,29 @@ static double test_mfunct_source(const orc_problem *p, double x, double y, doubl
   return (2.0 * a * exp(-a * r2_1) * ((2 * a * r2_1 - 3)) + 2.0 * a * exp(-a * r2_2) * ((2 * a * r2_2 - 3)));
 }
 
+/* Bowen_York_rho0/1/2 (src/operator.cc:3313-3408): the momentum component
+ * `comp` of every puncture within one cell diagonal dr of the point, spread
+ * as 3 p / (4 pi dr^3) (a unit-volume ball of radius dr). */
+static double by_rho(const orc_problem *p, int comp, double X, double Y, double Z, double dx, double dy, double dz)
+{
+  double cval = 0;
+  for (int i = 0; i < p->numbh; i++) {
+    const double x = X - p->x[i], y = Y - p->y[i], z = Z - p->z[i];
+    const double r = sqrt(x * x + y * y + z * z);
+    const double dr = sqrt(dx * dx + dy * dy + dz * dz);
+    const double pc = comp == 0 ? p->px[i] : comp == 1 ? p->py[i] : p->pz[i];
+    if (r <= dr) cval += 3 * pc / (4 * M_PI * dr * dr * dr);
+  }
+  return cval;
+}
+
 /* ------------------------------------------------------------------------ */
 /* pointwise operator: include/elliptic.h:405-445                            */
 /* ------------------------------------------------------------------------ */
 static inline double op_at(const orc_solver *S, const obox *B, long p, double lap)
 {
   const double *u = B->f[F_U], *b = B->f[F_B], *c = B->f[F_C];
+  if (S->P.equation == 5) return lap;                 /* BowenYork_OP_X/Y/Z, include/elliptic.h:772-793 */
   if (S->P.equation >= 2) return lap + u[p] * u[p];   /* poisson_OP, include/elliptic.h:359-362 */
   if (S->P.equation == 0) return lap + b[p] / pow(c[p] + u[p], 7);
   const double *d = B->f[F_D], *e = B->f[F_E];
@@ -636,6 +661,7 @@ static inline double op_at(const orc_solver *S, const obox *B, long p, double la
 static inline double duop_at(const orc_solver *S, const obox *B, long p, double dl)
 {
   const double *u = B->f[F_U], *b = B->f[F_B], *c = B->f[F_C];
+  if (S->P.equation == 5) return dl;                /* BowenYork_duOP_* */
   if (S->P.equation >= 2) return dl + 2.0 * u[p];   /* poisson_duOP */
   if (S->P.equation == 0) return dl - 7.0 * b[p] / pow(c[p] + u[p], 8);
   const double *d = B->f[F_D], *e = B->f[F_E];
@@ -691,12 +717,14 @@ static double smooth_box_w(orc_solver *S, obox *B, int nu, double omega)
  * corner (Boundary_Edge/Corner: F = r2*ipn*(Dx/x + Dy/y [+ Dz/z]) + u - S),
  * with each expression grouped as in src/boundary.cc:947-950, 1011-1016,
  * 1079-1086.  Returns the term without u and S; *dF gets dF/du. */
-static inline double robin_F(const obox *B, const double *u, int mask, int i, int j, int k, double *dF)
+static inline double robin_F(const orc_solver *S, const obox *B, const double *u, int mask, int i, int j, int k,
+                             double *dF)
 {
   const double x = dom_coord(&B->D, 0, i), y = dom_coord(&B->D, 1, j), z = dom_coord(&B->D, 2, k);
   const double x2 = x * x, y2 = y * y, z2 = z * z;
   const double r2 = x2 + y2 + z2;
-  const double ipn = 1.0 / (double)1;  /* falloff n = 1, src/operator.cc:789 */
+  /* falloff n = 1 (src/operator.cc:789), 2 for Bowen-York's variables (1393-1399) */
+  const double ipn = 1.0 / (double)(S->P.equation == 5 ? 2 : 1);
   const double crd[3] = {x, y, z};
   int ax[3], na = 0;
   for (int a = 0; a < 3; a++)
@@ -727,7 +755,7 @@ static void robin_update_pt(orc_solver *S, obox *B, int mask, int i, int j, int 
     return;
   }
   double dF;
-  double t = robin_F(B, u, mask, i, j, k, &dF);
+  double t = robin_F(S, B, u, mask, i, j, k, &dF);
   double F = t + u[p] - rho[p];
   u[p] = u[p] - F / dF;
 }
@@ -741,7 +769,7 @@ static void robin_operator_pt(orc_solver *S, obox *B, int mask, int i, int j, in
     return;
   }
   double dF;
-  double t = robin_F(B, u, mask, i, j, k, &dF);
+  double t = robin_F(S, B, u, mask, i, j, k, &dF);
   B->f[F_R][p] = t + u[p];
 }
 
@@ -1087,6 +1115,26 @@ static double fasn(orc_solver *S, int k, int k_top, int wcycle, long icycle)
   return norm_k;
 }
 
+/* Dx V1 + Dy V2 + Dz V3 into lambda's source on INSIDE points: the
+ * reference's BowenYork_OP_L (include/elliptic.h:796-800) takes the
+ * derivatives with the order's first-derivative stencil (dx2, or dx4 for
+ * orders 4-8: src/ffunction.cc:197-282) and sums them in this order. */
+void orc_set_divergence_source(orc_solver *lam, const orc_solver *v1, const orc_solver *v2, const orc_solver *v3)
+{
+  const orc_solver *V[3] = {v1, v2, v3};
+  for (int g = 0; g < lam->nboxes; g++) {
+    obox *B = &lam->box[g];
+    const int b = B->D.buf;
+    for (int k = b; k < B->D.n[2] - b; k++)
+      for (int j = b; j < B->D.n[1] - b; j++)
+        for (int i = b; i < B->D.n[0] - b; i++) {
+          double d[3];
+          for (int a = 0; a < 3; a++) d[a] = deriv(&V[a]->box[g], V[a]->box[g].f[F_U], a, i, j, k);
+          B->f[F_RHO][IDX(B, i, j, k)] = d[0] + d[1] + d[2];
+        }
+  }
+}
+
 /* ------------------------------------------------------------------------ */
 /* public API                                                                */
 /* ------------------------------------------------------------------------ */
@@ -1166,7 +1214,10 @@ static orc_solver *orc_create_opt(const orc_problem *p, int extra_coarse)
             const int ghost = i < bb || j < bb || k < bb || i >= B->D.n[0] - bb || j >= B->D.n[1] - bb ||
                               k >= B->D.n[2] - bb;
             double g, src;
-            if (p->equation == 3) {
+            if (p->equation == 5) {   /* zero boundary function (src/operator.cc:1380-1386) */
+              g = 0.0;
+              src = p->by_var < 3 ? by_rho(p, p->by_var, x, y, z, B->D.d[0], B->D.d[1], B->D.d[2]) : 0.0;
+            } else if (p->equation == 3) {
               g = test_boundary(x, y, z);
               src = test_boundary_source(x, y, z);
             } else if (p->equation == 4) {

@@ -20,7 +20,8 @@ extern "C" {
 
 typedef struct {
   int equation;            /* 0 Punctures, 1 Punctures_scalar_field, 2 Poisson (Gaussian test),
-                              3 Boundary-test, 4 Multibox-test */
+                              3 Boundary-test, 4 Multibox-test, 5 Bowen-York (one variable of
+                              the system, by_var) */
   int numbh;
   double mp[ORC_MAX_BH];
   double x[ORC_MAX_BH], y[ORC_MAX_BH], z[ORC_MAX_BH];
@@ -36,6 +37,8 @@ typedef struct {
   int ps_case;
   double ps_phi0, ps_r0, ps_sigma, ps_a2;
   int boundary;            /* -B: 0 Robin, 1 Dirichlet (the reference's default) */
+  int by_var;              /* Bowen-York: 0..2 V1..V3 (source rho0..rho2), 3 lambda (source
+                              set by orc_set_divergence_source) */
 } orc_problem;
 
 typedef struct orc_solver orc_solver;
@@ -104,6 +107,14 @@ long orc_coarse_iters(const orc_solver *s);
 /* last cycle's smoother norm on a level (post = 0 pre-, 1 post-smoothing);
  * level 0 gives the coarsest-solve norm */
 double orc_level_norm(const orc_solver *s, int level, int post);
+/* Bowen-York's lambda equation, Lap lambda - (Dx V1 + Dy V2 + Dz V3) = 0
+ * (include/elliptic.h:796-800), with the divergence moved into the source:
+ * rho of every INSIDE point of every box of `lam` := Dx V1 + Dy V2 + Dz V3
+ * of the hierarchies v1, v2, v3 (same problem, by_var 0..2).  The FAS
+ * equations of every level are the same (the divergence of the level's V
+ * enters both sides of the tau correction and cancels), so the fixed point
+ * is the system's. */
+void orc_set_divergence_source(orc_solver *lam, const orc_solver *v1, const orc_solver *v2, const orc_solver *v3);
 /* Valid_N restated (src/interface.cc:883-945) */
 int orc_valid_n(int n);
 

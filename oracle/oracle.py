@@ -28,7 +28,7 @@ class OrcProblem(C.Structure):
         ("n", C.c_int), ("L", C.c_double), ("order", C.c_int), ("levels", C.c_int),
         ("nu1", C.c_int), ("nu2", C.c_int), ("tol", C.c_double),
         ("ps_case", C.c_int), ("ps_phi0", C.c_double), ("ps_r0", C.c_double),
-        ("ps_sigma", C.c_double), ("ps_a2", C.c_double), ("boundary", C.c_int),
+        ("ps_sigma", C.c_double), ("ps_a2", C.c_double), ("boundary", C.c_int), ("by_var", C.c_int),
     ]
 
 
@@ -91,6 +91,7 @@ def load():
         L.orc_coarse_iters.argtypes = [C.c_void_p]
         L.orc_level_norm.restype = C.c_double
         L.orc_level_norm.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.orc_set_divergence_source.argtypes = [C.c_void_p] * 4
         L.orc_valid_n.restype = C.c_int
         L.orc_valid_n.argtypes = [C.c_int]
         _lib = L
@@ -117,6 +118,7 @@ class Oracle:
         p.ps_phi0 = float(params.get("ps_phi0", 0.025)); p.ps_r0 = float(params.get("ps_r0", 120.0))
         p.ps_sigma = float(params.get("ps_sigma", 8.0)); p.ps_a2 = float(params.get("ps_a2", 1.0))
         p.boundary = int(params.get("boundary", 0))
+        p.by_var = int(params.get("by_var", 0))
         self.numbh = p.numbh
         self._p = p
         self._s = (L.orc_create_extra_coarse if extra_coarse else L.orc_create)(C.byref(p))
@@ -233,3 +235,23 @@ class Oracle:
             if d <= tol:
                 break
         return d
+
+
+BOWEN_YORK = 5
+BY_VARS = ("V1", "V2", "V3", "lambda")
+
+
+def bowen_york_fixed_point(params: dict, tol: float = 1e-14, max_cycles: int = 400):
+    """The Bowen-York system's fixed point (include/elliptic.h:772-803): V1,
+    V2, V3 solved one after another, each from its own source (rho0..rho2,
+    src/operator.cc:3313-3408), then lambda with Dx V1 + Dy V2 + Dz V3 as its
+    source.  Returns ({name: [u of every box]}, {name: last max|du|})."""
+    fields, deltas, solved = {}, {}, []
+    for v, name in enumerate(BY_VARS):
+        o = Oracle(dict(params, equation=BOWEN_YORK, by_var=v))
+        if v == 3:
+            o.L.orc_set_divergence_source(o._s, *(s._s for s in solved))
+        deltas[name] = o.fixed_point(tol, max_cycles)
+        fields[name] = o.all_u()
+        solved.append(o)
+    return fields, deltas

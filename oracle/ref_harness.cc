@@ -2,8 +2,10 @@
 //
 // Drives the UNMODIFIED reference solver (WuShichao/OllipticID, compiled from
 // its own sources by oracle/Makefile into oracle/_ref/) and dumps what the
-// parity tests need: per-box geometry, coefficient fields, the solution u on
-// every box, per-cycle residual norms and the ADM masses at 17 digits.
+// parity tests need: per-box geometry, coefficient fields, the solution on
+// every box (u, or every variable of a system: V1, V2, V3, lambda for
+// Bowen-York, b<box>_<name>.f64), per-cycle residual norms and the ADM masses
+// at 17 digits.
 //
 // The reference keeps its solver internals private; this harness opens them
 // (access specifiers only, no behaviour change) so that it can call
@@ -66,18 +68,20 @@ static bool has_field(elliptic &E, size_t l, const std::string &name)
   return false;
 }
 
+// every variable of the equation (elliptic::var_names) on every box
 static void snapshot_u(elliptic &E, std::vector<std::vector<double> > &snap)
 {
   snap.clear();
   for (size_t l = 0; l < E.levels; l++)
-    for (size_t b = 0; b < E.vars.Get_num_dom(l); b++) {
-      ffunction *U = E.vars.Get_ffunction(l, b, "u");
-      domain *D = U->Get_domain();
-      const size_t n = D->Get_Nx() * D->Get_Ny() * D->Get_Nz();
-      std::vector<double> v(n);
-      for (size_t i = 0; i < n; i++) v[i] = U->Get_val((int)i);
-      snap.push_back(v);
-    }
+    for (size_t b = 0; b < E.vars.Get_num_dom(l); b++)
+      for (size_t iv = 0; iv < E.var_names.size(); iv++) {
+        ffunction *U = E.vars.Get_ffunction(l, b, E.var_names[iv]);
+        domain *D = U->Get_domain();
+        const size_t n = D->Get_Nx() * D->Get_Ny() * D->Get_Nz();
+        std::vector<double> v(n);
+        for (size_t i = 0; i < n; i++) v[i] = U->Get_val((int)i);
+        snap.push_back(v);
+      }
 }
 
 static double max_delta(elliptic &E, const std::vector<std::vector<double> > &prev)
@@ -163,7 +167,7 @@ int main(int argc, char **argv)
   size_t gb = 0;
   for (size_t l = 0; l < E.levels; l++)
     for (size_t b = 0; b < E.vars.Get_num_dom(l); b++, gb++) {
-      ffunction *U = E.vars.Get_ffunction(l, b, "u");
+      ffunction *U = E.vars.Get_ffunction(l, b, E.var_names[0]);
       domain *D = U->Get_domain();
       meta << "box " << gb << " level " << l << " ibox " << b
            << " n " << D->Get_Nx() << " " << D->Get_Ny() << " " << D->Get_Nz()
@@ -177,10 +181,11 @@ int main(int argc, char **argv)
            << " bound " << D->Get_Bound_Xi() << "\n";
       std::ostringstream pre;
       pre << outdir << "/b" << gb << "_";
-      dump_field(pre.str() + "u.f64", U);
+      for (size_t iv = 0; iv < E.var_names.size(); iv++)
+        dump_field(pre.str() + E.var_names[iv] + ".f64", E.vars.Get_ffunction(l, b, E.var_names[iv]));
       if (mode == "coeff") {
-        const char *names[] = {"b", "c", "d", "e", "rho0"};
-        for (int f = 0; f < 5; f++)
+        const char *names[] = {"b", "c", "d", "e", "rho0", "rho1", "rho2", "rho3"};
+        for (int f = 0; f < 8; f++)
           if (has_field(E, l, names[f]))
             dump_field(pre.str() + names[f] + ".f64", E.vars.Get_ffunction(l, b, names[f]));
       }

@@ -1,0 +1,68 @@
+"""Regenerates tests/golden/bowen_york/*.npz from the REFERENCE solver itself:
+its Bowen-York momentum-constraint test (-eq Bowen-York, four unknowns V1,
+V2, V3, lambda: include/elliptic.h:772-803, src/operator.cc:370-398,
+1320-1408, 3313-3408), run by oracle/_ref/ref_harness (built from the
+unmodified sources by `make -C oracle ref`).  Build container only:
+
+    make -C oracle ref && python tests/golden/make_bowen_york_golden.py
+
+Each case records the box geometry, the sources rho0..rho2 (sampled, plus
+every point where one is non-zero: the momenta spread over a ball of one
+cell diagonal around each puncture) and the four variables at the
+reference's fixed point (its own stop rule, then V-cycles until the largest
+change of any variable is <= 1e-14), sampled on the three centre lines of
+each box and 256 seeded points.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+sys.path.insert(0, ROOT)
+from tests.golden.make_golden import read_meta, sample_index  # noqa: E402
+
+BY_ARGS = ("-eq Bowen-York -B Robin -NumBH 2 -bhx1 -1.5 -bhx2 1.5 -bhpx1 0.05 -bhpy1 0.1 -bhpy2 -0.1 "
+           "-bhpz2 0.03 -L 20 -N 25 -l 3 -s 1e-10")
+CASES = {"o2": BY_ARGS + " -O 2", "o4": BY_ARGS + " -O 4"}
+VARS = ("V1", "V2", "V3", "lambda")
+
+
+def run(mode, args, out):
+    subprocess.run([HARNESS, mode, out, "--"] + args.split() + ["-o", out + "_run"], check=True,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, cwd="/tmp")
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        raise SystemExit("build the reference harness first: make -C oracle ref")
+    for name, args in CASES.items():
+        tmp = f"/tmp/golden_by_{name}"
+        run("coeff", args, tmp + "_coeff")
+        run("fixed:1e-14:300", args, tmp + "_fixed")
+        boxes, _, _ = read_meta(tmp + "_coeff")
+        _, fixed_norms, _ = read_meta(tmp + "_fixed")
+        rec = {"args": np.array(args), "fixed_norms": fixed_norms}
+        rec["box_level"] = np.array([b[0] for b in boxes])
+        rec["box_n"] = np.array([b[1] for b in boxes])
+        for g, b in enumerate(boxes):
+            idx = sample_index(b[1], 1000 + g)
+            rho = [np.fromfile(f"{tmp}_coeff/b{g}_rho{c}.f64") for c in range(3)]
+            ball = np.flatnonzero(np.any(np.stack(rho) != 0.0, axis=0))
+            rec[f"idx_b{g}"] = idx
+            rec[f"ball_b{g}"] = ball
+            for c in range(3):
+                rec[f"rho{c}_b{g}"] = rho[c][idx]
+                rec[f"rho{c}_ball_b{g}"] = rho[c][ball]
+            for v in VARS:
+                rec[f"{v}_b{g}"] = np.fromfile(f"{tmp}_fixed/b{g}_{v}.f64")[idx]
+        np.savez_compressed(os.path.join(HERE, "bowen_york", name + ".npz"), **rec)
+        print(name, "boxes", len(boxes), "cycles", len(fixed_norms), "ball points",
+              [len(rec[f"ball_b{g}"]) for g in range(len(boxes))])
+
+
+if __name__ == "__main__":
+    main()
