@@ -52,13 +52,24 @@ typedef enum {
  * OLGPU_EQ_BOUNDARY_TEST (-eq Boundary-test, 661-673, 1772-1816): source
  * -2a tanh(r) / (r cosh^2 r), boundary function a tanh(r) / r;
  * OLGPU_EQ_MULTIBOX_TEST (-eq Multibox-test, 1145-1175, 1820-1857): two
- * Gaussians e^{-0.05 r_i^2} centred at x = bhx1, bhx2 (NumBH >= 2). */
+ * Gaussians e^{-0.05 r_i^2} centred at x = bhx1, bhx2 (NumBH >= 2).
+ * OLGPU_EQ_BOWEN_YORK, the momentum-constraint test (-eq Bowen-York,
+ * include/elliptic.h:772-803, src/operator.cc:370-398, 1320-1408, 3313-3408):
+ * four unknowns, Lap V_i = rho_i (the momenta p_i of the punctures spread as
+ * 3 p_i / (4 pi dr^3) over the points within one cell diagonal dr) and
+ * Lap lambda - (Dx V1 + Dy V2 + Dz V3) = 0, each with the Robin falloff
+ * n = 2.  olgpu_solve solves V1, V2, V3 and then lambda (the V equations do
+ * not involve lambda: the same fixed point as the reference's joint
+ * iteration); olgpu_download reads them as "V1", "V2", "V3", "lambda" ("u"
+ * is the one being solved).  FP64, olgpu_solve only (not olgpu_solve_many,
+ * a batch or the server). */
 typedef enum {
   OLGPU_EQ_PUNCTURES = 0,
   OLGPU_EQ_PUNCTURES_SCALAR = 1,
   OLGPU_EQ_POISSON = 2,
   OLGPU_EQ_BOUNDARY_TEST = 3,
-  OLGPU_EQ_MULTIBOX_TEST = 4
+  OLGPU_EQ_MULTIBOX_TEST = 4,
+  OLGPU_EQ_BOWEN_YORK = 5
 } olgpu_equation;
 
 /* The outer boundary condition (-B, src/boundary.cc:447-1535): Robin, u ~
@@ -245,6 +256,11 @@ olgpu_status olgpu_cycle_events(const olgpu_hierarchy *h, long long first, int c
  * already enqueued. */
 olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, const double *xyz, long long npts,
                                int ord, double *out);
+/* The same for any field olgpu_download reads (Bowen-York's "V1", "V2",
+ * "V3", "lambda" among them: the reference prints each variable this way,
+ * src/output.cc:624-730); olgpu_interpolate is this with "u". */
+olgpu_status olgpu_interpolate_field(olgpu_hierarchy *h, const char *field, int box, int first_level,
+                                     const double *xyz, long long npts, int ord, double *out);
 
 /* Asynchronous stepping, for hosts that drive several solves at once (each
  * hierarchy has its own CUDA stream, so cycles of different hierarchies run

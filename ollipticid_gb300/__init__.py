@@ -313,18 +313,21 @@ class Elliptic:
         check(self.lib.olgpu_cycle_events(self._h, 0, total.value, buf, C.byref(total)))
         return [(e.level, e.post, e.cycle, e.norm) for e in buf[:total.value]]
 
-    def interpolate(self, points, ord: Optional[int] = None, box: int = -1, first_level: int = 0) -> np.ndarray:
+    def interpolate(self, points, ord: Optional[int] = None, box: int = -1, first_level: int = 0,
+                    field: str = "u") -> np.ndarray:
         """u at (npts, 3) points, as the reference prints it (Print_Interpol_1D
         / _2D with box=-1: the finest box whose interior holds each point, NaN
         outside the largest box; ffunction::Print_1D with box >= 0).  ord+1
         Lagrange nodes per axis, default order + 1 like the reference's
         printout.  first_level: with box=-1, only boxes of that level and
-        finer take part (mgrid_levels for the analytic method's printout)."""
+        finer take part (mgrid_levels for the analytic method's printout).
+        field: any field get_field reads (Bowen-York's V1, V2, V3, lambda)."""
         pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
         out = np.empty(len(pts), dtype=np.float64)
         k = self.problem.order + 1 if ord is None else int(ord)
-        check(self.lib.olgpu_interpolate(self._h, int(box), int(first_level), pts.ctypes.data_as(C.c_void_p), len(pts), k,
-                                         out.ctypes.data_as(C.c_void_p)))
+        check(self.lib.olgpu_interpolate_field(self._h, field.encode(), int(box), int(first_level),
+                                               pts.ctypes.data_as(C.c_void_p), len(pts), k,
+                                               out.ctypes.data_as(C.c_void_p)))
         return out
 
     @property

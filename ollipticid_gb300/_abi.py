@@ -108,6 +108,8 @@ SIGNATURES = {
     "olgpu_cycle_events": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.POINTER(CycleEvent),
                                      C.POINTER(C.c_longlong)]),
     "olgpu_interpolate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p]),
+    "olgpu_interpolate_field": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_void_p, C.c_longlong, C.c_int,
+                                          C.c_void_p]),
     "olgpu_cycle_launch": (C.c_int, [C.c_void_p]),
     "olgpu_cycle_poll": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "olgpu_solve_many": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(StopRule), C.POINTER(Report)]),

@@ -106,7 +106,8 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
       U(i, j, k) = gs[((long long)k * n1 + j) * n0 + i];
       return;
     }
-    const double r2 = s_x[0][i] * s_x[0][i] + s_x[1][j] * s_x[1][j] + s_x[2][k] * s_x[2][k];
+    const double r2s = s_x[0][i] * s_x[0][i] + s_x[1][j] * s_x[1][j] + s_x[2][k] * s_x[2][k];
+    const double r2 = B.falloff == 2 ? 0.5 * r2s : r2s;   // r^2 / n
     const int ijk[3] = {i, j, k};
     double tF = 0.0, dF = 1.0, t = 0.0, dt = 0.0;
     int na = 0;

@@ -39,7 +39,9 @@ struct DevBox {
   int mg_coarse;        // 1: a multigrid coarse level (level < the solve's
                         // mgrid levels), whose ghost layers the discrete system
                         // does not fix
-  int pad_;
+  int falloff;          // the Robin condition's falloff n (u ~ u_inf + C / r^n):
+                        // 2 for the Bowen-York variables, else 1
+  double d[3];          // spacing dx, dy, dz
 };
 
 struct DevFields {
@@ -113,7 +115,7 @@ struct PunctureParams {
   int numbh;
   int equation;
   int ps_case;
-  int pad;
+  int var;              // Bowen-York: the variable k_test_init sets up (0..2 V1..V3, 3 lambda)
   double mp[16], x[16], y[16], z[16];
   double px[16], py[16], pz[16], sx[16], sy[16], sz[16];
   double ps_phi0, ps_r0, ps_isigma, ps_d1, ps_e1, ps_e2, ps_de1;

@@ -163,9 +163,11 @@ __device__ __forceinline__ void point_op(double lapv, double dl, double uu, doub
   const double t7 = bb * (iq4 * iq2 * iq);   // b / (c+u)^7
   op = lapv + t7;
   dop = dl - 7.0 * t7 * iq;                  // -7 b / (c+u)^8
-  if (EQ == 2) {   // the Gaussian test: poisson_OP / _duOP, include/elliptic.h:359-366
-    op = lapv + uu * uu;
-    dop = dl + 2.0 * uu;
+  if (EQ == 2) {   // the test equations: poisson_OP / _duOP, include/elliptic.h:359-366, with b (1, or 0
+                   // for Bowen-York's Laplacians, 772-803) the factor of u^2
+    const double bu = bb * uu;
+    op = lapv + bu * uu;
+    dop = dl + 2.0 * bu;
     return;
   }
   if (EQ == 1) {
@@ -184,8 +186,9 @@ __device__ __forceinline__ void point_terms(double dl, double uu, double bb, dou
                                             double &nl, double &dop)
 {
   if (EQ == 2) {
-    nl = uu * uu;
-    dop = dl + 2.0 * uu;
+    const double bu = bb * uu;
+    nl = bu * uu;
+    dop = dl + 2.0 * bu;
     return;
   }
   const double q = cc + uu;
@@ -232,7 +235,7 @@ __device__ __forceinline__ double deriv(const double *__restrict__ u, long long 
   }
 }
 
-// Robin term r^2/n * sum_a (du/dx_a)/x_a for the axes in mask (n = 1), grouped
+// Robin term r^2/n * sum_a (du/dx_a)/x_a for the axes in mask (n = B.falloff), grouped
 // like Boundary_Face (one axis) and Boundary_Edge/Corner (two/three axes).
 // A box's coordinate table holds x, y, z and then 1/x, 1/y, 1/z: the
 // divisions by the coordinate are products with its reciprocal (within an
@@ -245,7 +248,9 @@ __device__ __forceinline__ double robin_term(const double *__restrict__ u, const
 {
   const double *c = crd + B.coord_off, *ic = c + (B.n[0] + B.n[1] + B.n[2]);
   const double x = c[i], y = c[B.n[0] + j], z = c[B.n[0] + B.n[1] + k];
-  const double r2 = x * x + y * y + z * z;
+  // r^2 / n (the falloff; the halving is exact, so the grouping of r2 * ipn * D
+  // in src/boundary.cc:947-950 gives the same bits)
+  const double r2 = B.falloff == 2 ? 0.5 * (x * x + y * y + z * z) : x * x + y * y + z * z;
   const long long p = pidx(B, i, j, k);
   const long long st[3] = {1, (long long)B.n[0], (long long)B.n[0] * B.n[1]};
   const int ijk[3] = {i, j, k};
@@ -1553,8 +1558,8 @@ __global__ void __launch_bounds__(256) k_coefficients(BoxList L, const DevBox *_
   const int j = (r % B.n[1]), k = (r / B.n[1]);
   const double x = crd[B.coord_off + i], y = crd[B.coord_off + B.n[0] + j],
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
-  if (P.equation >= 2) {   // the test equations have no puncture coefficients
-    F.f[F_B][B.off + t] = 0.0;
+  if (P.equation >= 2) {   // the test equations: b is the factor of u^2 (none for Bowen-York)
+    F.f[F_B][B.off + t] = P.equation == 5 ? 0.0 : 1.0;
     F.f[F_C][B.off + t] = 0.0;
     return;
   }
@@ -1611,6 +1616,25 @@ __device__ double dev_test_source(const PunctureParams &P, double x, double y, d
   return a * exp(-r2) * (a + exp(0.5 * r2) * (r2 - 3.0));
 }
 
+// Bowen_York_rho0/1/2 (src/operator.cc:3313-3408): momentum component `comp`
+// of every puncture within one cell diagonal dr of the point, spread as
+// 3 p / (4 pi dr^3).  Rounded operation by operation (no contraction): which
+// points lie in a ball is decided by r <= dr, as in the reference.
+__device__ double dev_by_source(const PunctureParams &P, int comp, double X, double Y, double Z, const DevBox &B)
+{
+  double cval = 0.0;
+  const double dr = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(B.d[0], B.d[0]), __dmul_rn(B.d[1], B.d[1])),
+                                         __dmul_rn(B.d[2], B.d[2])));
+  const double vol = __dmul_rn(__dmul_rn(__dmul_rn(4.0 * M_PI, dr), dr), dr);
+  for (int i = 0; i < P.numbh; i++) {
+    const double x = __dsub_rn(X, P.x[i]), y = __dsub_rn(Y, P.y[i]), z = __dsub_rn(Z, P.z[i]);
+    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+    const double pc = comp == 0 ? P.px[i] : comp == 1 ? P.py[i] : P.pz[i];
+    if (r <= dr) cval = __dadd_rn(cval, __ddiv_rn(__dmul_rn(3.0, pc), vol));
+  }
+  return cval;
+}
+
 __global__ void __launch_bounds__(256) k_test_init(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
                                                    const double *__restrict__ crd, PunctureParams P, int dirichlet)
 {
@@ -1627,9 +1651,49 @@ __global__ void __launch_bounds__(256) k_test_init(BoxList L, const DevBox *__re
                z = crd[B.coord_off + B.n[0] + B.n[1] + k];
   const int b = B.buf;
   const bool ghost = i < b || j < b || k < b || i >= B.n[0] - b || j >= B.n[1] - b || k >= B.n[2] - b;
+  if (P.equation == 5) {   // Bowen-York: zero boundary function and initial guess; lambda's source
+                           // is the divergence of V (k_by_divergence)
+    F.f[F_RHO][B.off + t] = ghost || P.var == 3 ? 0.0 : dev_by_source(P, P.var, x, y, z, B);
+    F.f[F_U][B.off + t] = 0.0;
+    return;
+  }
   const double g = dev_test_function(P, x, y, z);
   F.f[F_RHO][B.off + t] = ghost ? (dirichlet ? g : 0.0) : dev_test_source(P, x, y, z);
   F.f[F_U][B.off + t] = g;
+}
+
+// Bowen-York's lambda equation, Lap lambda - (Dx V1 + Dy V2 + Dz V3) = 0
+// (include/elliptic.h:796-800), with the divergence in the source: rho of
+// every INSIDE point := Dx V1 + Dy V2 + Dz V3 of the solved V (v: V1, V2, V3
+// one after another, each laid out like a field of the arena, stride
+// `total`), with the order's first-derivative stencil (dx2, or dx4 for
+// orders 4-8).  The divergence of each level's V enters both sides of that
+// level's FAS tau correction and cancels, so the fixed point is the system's.
+__global__ void __launch_bounds__(256) k_by_divergence(BoxList L, const DevBox *__restrict__ boxes, DevFields F,
+                                                       const double *__restrict__ v, long long total)
+{
+  long long lb;
+  const DevBox B = boxes[list_box(L, lb)];
+  if (!B.active) return;
+  const long long t = lb * blockDim.x + threadIdx.x;
+  const long long n = (long long)B.n[0] * B.n[1] * B.n[2];
+  if (t >= n) return;
+  const int i = ((int)t % B.n[0]);
+  const int r = (int)t / B.n[0];
+  const int j = (r % B.n[1]), k = (r / B.n[1]);
+  const int b = B.buf;
+  if (i < b || j < b || k < b || i >= B.n[0] - b || j >= B.n[1] - b || k >= B.n[2] - b) return;
+  const long long st[3] = {1, (long long)B.n[0], (long long)B.n[0] * B.n[1]};
+  const int ijk[3] = {i, j, k};
+  double d[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double *va = v + a * total + B.off;
+    double du;
+    d[a] = B.order == 2 ? deriv<2>(va, t, st[a], ijk[a], B.n[a], B.idx[a], du)
+                        : deriv<4>(va, t, st[a], ijk[a], B.n[a], B.idx[a], du);
+  }
+  F.f[F_RHO][B.off + t] = d[0] + d[1] + d[2];
 }
 
 // ----------------------------------------------------------------------------

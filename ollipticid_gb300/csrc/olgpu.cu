@@ -186,6 +186,10 @@ struct olgpu_hierarchy {
   hierarchy_geometry G;
   int device = 0;
   int equation = 0;
+  // Bowen-York (four unknowns): the variable u holds now (0..2 V1..V3, 3
+  // lambda) and V1, V2, V3 as solved (3 x total_pts, the arena's layout)
+  int by_var = 0;
+  double *d_by = nullptr;
   std::vector<DevBox> hboxes;
   long long total_pts = 0;
   DevBox *d_boxes = nullptr;
@@ -1913,7 +1917,7 @@ static olgpu_status validate_problem(const olgpu_problem *p)
     return fail(OLGPU_ERR_INVALID_ARG, "order must be 2, 4, 6 or 8");
   if (p->levels < 1) return fail(OLGPU_ERR_INVALID_ARG, "levels must be >= 1");
   if (p->nu1 < 0 || p->nu2 < 0) return fail(OLGPU_ERR_INVALID_ARG, "negative sweep count");
-  if (p->equation < 0 || p->equation > 4) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
+  if (p->equation < 0 || p->equation > OLGPU_EQ_BOWEN_YORK) return fail(OLGPU_ERR_INVALID_ARG, "unknown equation");
   if (p->equation == OLGPU_EQ_MULTIBOX_TEST && p->numbh < 2)
     return fail(OLGPU_ERR_INVALID_ARG, "the multibox test takes its two centres from bhx1 and bhx2");
   if (p->boundary != OLGPU_BC_ROBIN && p->boundary != OLGPU_BC_DIRICHLET)
@@ -1959,6 +1963,8 @@ static olgpu_status plan_hierarchy(const olgpu_problem *p, olgpu_hierarchy *h)
     B.solve = 0;
     B.active = 1;
     B.mg_coarse = D.level < h->G.mgrid_levels ? 1 : 0;
+    B.falloff = h->equation == OLGPU_EQ_BOWEN_YORK ? 2 : 1;   // src/operator.cc:789, 1393-1399
+    for (int a = 0; a < 3; a++) B.d[a] = D.d[a];
     set_box_stencil(B, D.order, D.d);
     // x, y, z of the box's nodes, then their reciprocals (ghost nodes lie on
     // the outer faces; a node at 0 gets 0, it is never a Robin point)
@@ -2109,6 +2115,9 @@ static olgpu_status setup_device(olgpu_hierarchy *h, double *arena, long long st
   // fixed point of the cycle
   if (const char *v = std::getenv("OLGPU_COARSE_OMEGA")) h->coarse_omega = std::atof(v);
   if (const char *v = std::getenv("OLGPU_COARSE_RTOL")) h->coarse_rtol = std::atof(v);
+  if (h->equation == OLGPU_EQ_BOWEN_YORK &&
+      dev_alloc((void **)&h->d_by, sizeof(double) * 3 * (size_t)h->total_pts, h->device, h->stream) != cudaSuccess)
+    return cleanup(fail(OLGPU_ERR_OOM, "Bowen-York variable allocation failed"));
   st = olgpu_reset(h);
   if (st != OLGPU_OK) return cleanup(st);
   // coefficients on the device
@@ -2198,6 +2207,7 @@ olgpu_status olgpu_hierarchy_destroy(olgpu_hierarchy *h)
   dev_free(h->d_and64, s);
   dev_free(h->d_and64_state, s);
   dev_free(h->d_and64_part, s);
+  dev_free(h->d_by, s);
   for (auto *vec : {&h->restrict_u, &h->xfer_w, &h->set_in, &h->prolong_v, &h->ghost_u, &h->ghost_lo})
     for (auto &X : *vec) dev_free(X.d_jobs, s);
   if (h->owns_arena) dev_free(h->d_arena, s);
@@ -2242,14 +2252,42 @@ olgpu_status olgpu_box(const olgpu_hierarchy *h, int box, olgpu_box_info *o)
   return OLGPU_OK;
 }
 
+// Bowen-York's variables by name: the one being solved is u, the V solved
+// before it are in d_by; -1 for any other name
+static int by_var_id(const char *field)
+{
+  static const char *names[4] = {"V1", "V2", "V3", "lambda"};
+  for (int v = 0; v < 4; v++)
+    if (field && std::strcmp(field, names[v]) == 0) return v;
+  return -1;
+}
+
+// The device field of every box (laid out like the arena's) for a field
+// name, or nullptr after fail() for an unknown one or a Bowen-York variable
+// not solved yet.
+static double *field_base(olgpu_hierarchy *h, const char *field)
+{
+  const int bv = h->equation == OLGPU_EQ_BOWEN_YORK ? by_var_id(field) : -1;
+  const int f = bv >= 0 ? F_U : field_id(field);
+  if (f < 0 || !h->F.f[f]) {
+    fail(OLGPU_ERR_INVALID_ARG, std::string("unknown field ") + (field ? field : ""));
+    return nullptr;
+  }
+  if (bv > h->by_var) {
+    fail(OLGPU_ERR_INVALID_ARG, std::string(field) + " is not solved yet");
+    return nullptr;
+  }
+  return bv >= 0 && bv < h->by_var ? h->d_by + (size_t)bv * h->total_pts : h->F.f[f];
+}
+
 static olgpu_status field_copy(olgpu_hierarchy *h, int box, const char *field, void *host, bool upload)
 {
   if (!h || !host || box < 0 || box >= (int)h->G.boxes.size()) return fail(OLGPU_ERR_INVALID_ARG, "bad box");
-  const int f = field_id(field);
-  if (f < 0 || !h->F.f[f]) return fail(OLGPU_ERR_INVALID_ARG, std::string("unknown field ") + (field ? field : ""));
+  double *base = field_base(h, field);
+  if (!base) return OLGPU_ERR_INVALID_ARG;
   CUDA_TRY(cudaSetDevice(h->device));
   const DevBox &B = h->hboxes[box];
-  double *d = h->F.f[f] + B.off;
+  double *d = base + B.off;
   const size_t bytes = sizeof(double) * (size_t)B.n[0] * B.n[1] * B.n[2];
   if (upload)
     CUDA_TRY(cudaMemcpyAsync(d, host, bytes, cudaMemcpyHostToDevice, h->stream));
@@ -2269,25 +2307,38 @@ olgpu_status olgpu_download(olgpu_hierarchy *h, int box, const char *field, doub
   return field_copy(h, box, field, host, false);
 }
 
-olgpu_status olgpu_reset(olgpu_hierarchy *h)
+// The initial state of the solve: u and the FAS work fields cleared, a test
+// equation's initial u and source; for Bowen-York those of variable
+// h->by_var (lambda's source: the divergence of the solved V).
+static olgpu_status init_solve_state(olgpu_hierarchy *h)
 {
-  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
   CUDA_TRY(cudaSetDevice(h->device));
   const size_t n = sizeof(double) * (size_t)h->total_pts;
   for (int f : {F_U, F_RHO, F_R, F_W, F_WW, F_V, F_T}) CUDA_TRY(cudaMemsetAsync(h->F.f[f], 0, n, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   std::fill(h->adm, h->adm + OLGPU_MAX_BH, 0.0);
   if (h->equation >= OLGPU_EQ_POISSON) {   // a test equation's initial u and source
+    PunctureParams PP = puncture_params(&h->P);
+    PP.var = h->by_var;
     for (int l = 0; l < h->G.levels; l++) {
       const BoxList BL = level_list(h, l, blocks_all);
-      k_test_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords,
-                                                                puncture_params(&h->P),
+      k_test_init<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_coords, PP,
                                                                 h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
+      if (h->equation == OLGPU_EQ_BOWEN_YORK && h->by_var == 3)
+        k_by_divergence<<<BL.blk[BL.count], kThreads, 0, h->stream>>>(BL, h->d_boxes, h->F, h->d_by,
+                                                                      h->total_pts);
     }
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(h->stream));
   }
   return reset_anderson(h);
+}
+
+olgpu_status olgpu_reset(olgpu_hierarchy *h)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  h->by_var = 0;
+  return init_solve_state(h);
 }
 
 // Enqueues one cycle (graph + copy of its norms to pinned host memory) and
@@ -2501,14 +2552,8 @@ static void solve_wcycle(olgpu_hierarchy *h, SolveTrack &T)
   }
 }
 
-olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out)
+static void solve_loop(olgpu_hierarchy *h, SolveTrack &T)
 {
-  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
-  SolveTrack T;
-  olgpu_status st = make_track(h, rule, T);
-  if (st != OLGPU_OK) return st;
-  CUDA_TRY(cudaSetDevice(h->device));
-  CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
   if (h->P.method == OLGPU_METHOD_WCYCLE) {
     solve_wcycle(h, T);
   } else {
@@ -2518,6 +2563,59 @@ olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_
       if (T.step(h, s, r)) break;
     }
   }
+}
+
+// Bowen-York (include/elliptic.h:772-803): V1, V2, V3 and then lambda, each
+// solved under the rule from the state it is in (the one in u continues, the
+// later ones start from zero), V kept in d_by as it is solved; lambda's
+// source is the divergence of the solved V.  The reference advances the
+// four together (elliptic::Smooth and every transfer loop over var_names);
+// the equations for V do not involve lambda, so solving them first reaches
+// the same fixed point.  The report: the cycles of all four, the largest
+// final norm and change, the first failure; res[] holds their norms in turn.
+static void solve_bowen_york(olgpu_hierarchy *h, SolveTrack &All)
+{
+  for (;;) {
+    SolveTrack T;
+    T.R = All.R;
+    T.tol = All.tol;
+    T.du_tol = All.du_tol;
+    solve_loop(h, T);
+    for (int c = 0; c < T.cycles && All.cycles + c < 256; c++) All.rep.res[All.cycles + c] = T.rep.res[c];
+    All.cycles += T.cycles;
+    All.res = std::max(All.cycles == T.cycles ? 0.0 : All.res, T.res);
+    All.du = std::max(All.du, T.du);
+    All.part = std::max(All.part, T.part);
+    All.status = T.status;
+    if (T.status != OLGPU_OK || h->by_var == 3) return;
+    const size_t n = sizeof(double) * (size_t)h->total_pts;
+    olgpu_status st = OLGPU_OK;
+    if (cudaMemcpyAsync(h->d_by + (size_t)h->by_var * h->total_pts, h->F.f[F_U], n, cudaMemcpyDeviceToDevice,
+                        h->stream) != cudaSuccess)
+      st = fail(OLGPU_ERR_CUDA, "Bowen-York: keeping a solved V");
+    if (st == OLGPU_OK) {
+      h->by_var++;
+      st = init_solve_state(h);
+    }
+    if (st != OLGPU_OK) {
+      All.status = st;
+      return;
+    }
+  }
+}
+
+olgpu_status olgpu_solve(olgpu_hierarchy *h, const olgpu_stop_rule *rule, olgpu_report *out)
+{
+  if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  SolveTrack T;
+  olgpu_status st = make_track(h, rule, T);
+  if (st != OLGPU_OK) return st;
+  CUDA_TRY(cudaSetDevice(h->device));
+  CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+  if (h->equation == OLGPU_EQ_BOWEN_YORK)
+    solve_bowen_york(h, T);
+  else
+    solve_loop(h, T);
   cudaEventRecord(h->ev1, h->stream);
   cudaEventSynchronize(h->ev1);
   h->last_ms = elapsed_ms(h->ev0, h->ev1);
@@ -2556,6 +2654,8 @@ olgpu_status olgpu_solve_many(olgpu_hierarchy **hs, int n, const olgpu_stop_rule
   for (int i = 0; i < n; i++) {
     if (!hs[i]) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy in the set");
     if (hs[i]->P.method != OLGPU_METHOD_VCYCLE) return fail(OLGPU_ERR_INVALID_ARG, "W-cycles run from olgpu_solve only");
+    if (hs[i]->equation == OLGPU_EQ_BOWEN_YORK)
+      return fail(OLGPU_ERR_INVALID_ARG, "Bowen-York solves its variables in turn: olgpu_solve");
     olgpu_status st = make_track(hs[i], rule, T[i]);
     if (st != OLGPU_OK) return st;
   }
@@ -2612,7 +2712,15 @@ olgpu_status olgpu_adm_mass(olgpu_hierarchy *h, double *out)
 olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, const double *xyz, long long npts,
                                int ord, double *out)
 {
+  return olgpu_interpolate_field(h, "u", box, first_level, xyz, npts, ord, out);
+}
+
+olgpu_status olgpu_interpolate_field(olgpu_hierarchy *h, const char *field, int box, int first_level,
+                                     const double *xyz, long long npts, int ord, double *out)
+{
   if (!h) return fail(OLGPU_ERR_INVALID_ARG, "null hierarchy");
+  const double *src = field_base(h, field);
+  if (!src) return OLGPU_ERR_INVALID_ARG;
   if (npts < 0 || (npts > 0 && (!xyz || !out))) return fail(OLGPU_ERR_INVALID_ARG, "null or negative point array");
   if (ord < 1 || ord > kMaxInterpOrd) return fail(OLGPU_ERR_INVALID_ARG, "interpolation order must be 1..15");
   const int nb = (int)h->G.boxes.size();
@@ -2663,8 +2771,8 @@ olgpu_status olgpu_interpolate(olgpu_hierarchy *h, int box, int first_level, con
     e = cudaMemcpyAsync(d_xyz, xyz, sizeof(double) * 3 * (size_t)npts, cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) {
     const long long blocks = cdiv(npts, 128);
-    k_interp_points<<<(unsigned)blocks, 128, 0, h->stream>>>(d_b, first, nb, base, box, h->F.f[F_U], d_xyz, npts,
-                                                             ord, d_out);
+    k_interp_points<<<(unsigned)blocks, 128, 0, h->stream>>>(d_b, first, nb, base, box, src, d_xyz, npts, ord,
+                                                             d_out);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)

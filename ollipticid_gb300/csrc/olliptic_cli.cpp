@@ -7,9 +7,11 @@
 // program.  Flags of the puncture FAS path are read with the reference's names
 // and defaults; flags outside it (output, printing, symmetry, MPI) are accepted
 // and ignored, as the reference ignores unknown flags.  Equations other than
-// Punctures / Punctures_scalar_field and the reference's test equations
-// Poisson (the Gaussian test), Boundary-test and Multibox-test are refused, and so are boundary conditions other than Robin and
-// Dirichlet (the reference's default).
+// Punctures / Punctures_scalar_field, the reference's test equations Poisson
+// (the Gaussian test), Boundary-test and Multibox-test, and Bowen-York (its
+// variables V1, V2, V3, lambda printed each as the reference prints u) are
+// refused, and so are boundary conditions other than Robin and Dirichlet (the
+// reference's default).
 //
 // Methods (-m): Vcycle (the default, and, as in the reference, what a name it
 // does not know means), Wcycle (every level repeated until its own norm
@@ -218,8 +220,8 @@ void write_cycle_tables(FILE *f, const std::vector<olgpu_cycle_event> &ev, int n
 // else through its middle node; the value is interpolated (Lagrange, order+1)
 // when `interpolate`, else the node value.  "%.12e\t%.12e\t" lines, then a
 // blank line.
-olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis, bool interpolate, int ord,
-                           const std::string &file)
+olgpu_status print_box_cut(olgpu_hierarchy *h, const char *var, const BoxGeom &B, int g, int axis, bool interpolate,
+                           int ord, const std::string &file)
 {
   int node[3];
   double at[3];
@@ -244,11 +246,11 @@ olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis
     pts[3 * i + axis] = B.coord(axis, i);
   }
   if (interpolate) {
-    const olgpu_status st = olgpu_interpolate(h, g, 0, pts.data(), np, ord, val.data());
+    const olgpu_status st = olgpu_interpolate_field(h, var, g, 0, pts.data(), np, ord, val.data());
     if (st != OLGPU_OK) return st;
   } else {
     std::vector<double> u((size_t)B.b.nx * B.b.ny * B.b.nz);
-    const olgpu_status st = olgpu_download(h, g, "u", u.data());
+    const olgpu_status st = olgpu_download(h, g, var, u.data());
     if (st != OLGPU_OK) return st;
     for (int i = 0; i < np; i++) {
       int ijk[3] = {node[0], node[1], node[2]};
@@ -270,8 +272,8 @@ olgpu_status print_box_cut(olgpu_hierarchy *h, const BoxGeom &B, int g, int axis
 // else through the box's middle node; every node of the other two axes, the
 // lower axis outer; "%.12e\t%.12e\t%.12e\t" lines, a blank line after each
 // outer index and one more at the end.
-olgpu_status print_box_plane(olgpu_hierarchy *h, const BoxGeom &B, int g, int normal, bool interpolate,
-                             const std::string &file)
+olgpu_status print_box_plane(olgpu_hierarchy *h, const char *var, const BoxGeom &B, int g, int normal,
+                             bool interpolate, const std::string &file)
 {
   const int a1 = normal == 0 ? 1 : 0, a2 = normal == 2 ? 1 : 2;   // in-plane axes, a1 < a2
   const int nm = B.n(normal) % 2 == 0 ? B.n(normal) / 2 : (B.n(normal) - 1) / 2;
@@ -287,11 +289,11 @@ olgpu_status print_box_plane(olgpu_hierarchy *h, const BoxGeom &B, int g, int no
       x[a2] = B.coord(a2, q);
     }
   if (interpolate) {
-    const olgpu_status st = olgpu_interpolate(h, g, 0, pts.data(), (long long)val.size(), 2, val.data());
+    const olgpu_status st = olgpu_interpolate_field(h, var, g, 0, pts.data(), (long long)val.size(), 2, val.data());
     if (st != OLGPU_OK) return st;
   } else {
     std::vector<double> u((size_t)B.b.nx * B.b.ny * B.b.nz);
-    const olgpu_status st = olgpu_download(h, g, "u", u.data());
+    const olgpu_status st = olgpu_download(h, g, var, u.data());
     if (st != OLGPU_OK) return st;
     for (int p = 0; p < n1; p++)
       for (int q = 0; q < n2; q++) {
@@ -319,12 +321,12 @@ olgpu_status print_box_plane(olgpu_hierarchy *h, const BoxGeom &B, int g, int no
 // ffunction::Print_3D of one box (src/ffunction.cc:412-475): every point in
 // the reference's storage order (olgpu_storage_order), "%.12e\t" x, y, z and
 // the node value of u, then a line end; no blank line at the end.
-olgpu_status print_box_3d(olgpu_hierarchy *h, const BoxGeom &B, int g, const std::string &file)
+olgpu_status print_box_3d(olgpu_hierarchy *h, const char *var, const BoxGeom &B, int g, const std::string &file)
 {
   const size_t np = (size_t)B.b.nx * B.b.ny * B.b.nz;
   std::vector<double> u(np);
   std::vector<long long> order(np);
-  olgpu_status st = olgpu_download(h, g, "u", u.data());
+  olgpu_status st = olgpu_download(h, g, var, u.data());
   if (st == OLGPU_OK) st = olgpu_storage_order(&B.b, order.data());
   if (st != OLGPU_OK) return st;
   FILE *f = std::fopen(file.c_str(), "a");
@@ -340,8 +342,8 @@ olgpu_status print_box_3d(olgpu_hierarchy *h, const BoxGeom &B, int g, const std
 // multigrid::Print_Interpol_1D along one axis: from -LD/2 by D (LD/1000 when
 // D <= 0) while <= LD/2, the other coordinates 0, points outside the largest
 // box skipped; "%.18e\t%.18e" lines, then a blank line.
-olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D, int ord, int first_level,
-                               const std::string &file)
+olgpu_status print_interpol_1d(olgpu_hierarchy *h, const char *var, int axis, double LD, double D, int ord,
+                               int first_level, const std::string &file)
 {
   const double xi = -0.5 * LD, xf = 0.5 * LD, Dx = D > 0.0 ? D : LD / 1000;
   std::vector<double> pts, xs;
@@ -352,7 +354,8 @@ olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D
     xs.push_back(x);
   }
   std::vector<double> val(xs.size());
-  const olgpu_status st = olgpu_interpolate(h, -1, first_level, pts.data(), (long long)xs.size(), ord, val.data());
+  const olgpu_status st =
+      olgpu_interpolate_field(h, var, -1, first_level, pts.data(), (long long)xs.size(), ord, val.data());
   if (st != OLGPU_OK) return st;
   FILE *f = std::fopen(file.c_str(), "a");
   if (!f) return OLGPU_ERR_INVALID_ARG;
@@ -366,8 +369,8 @@ olgpu_status print_interpol_1d(olgpu_hierarchy *h, int axis, double LD, double D
 // multigrid::Print_Interpol_2D, the z = 0 plane: x and y from -L/4 by L/200
 // while <= L/4; "%.18e\t%.18e\t%.18e" lines, a blank line after each x and
 // one more at the end.
-olgpu_status print_interpol_xy(olgpu_hierarchy *h, double LD1, double LD2, int ord, int first_level,
-                               const std::string &file)
+olgpu_status print_interpol_xy(olgpu_hierarchy *h, const char *var, double LD1, double LD2, int ord,
+                               int first_level, const std::string &file)
 {
   const double x1i = -0.25 * LD1, x2i = -0.25 * LD2, x1f = 0.25 * LD1, x2f = 0.25 * LD2;
   const double Dx1 = LD1 / 200, Dx2 = LD2 / 200;
@@ -383,7 +386,8 @@ olgpu_status print_interpol_xy(olgpu_hierarchy *h, double LD1, double LD2, int o
     row_end.push_back((int)xs.size());
   }
   std::vector<double> val(xs.size());
-  const olgpu_status st = olgpu_interpolate(h, -1, first_level, pts.data(), (long long)xs.size(), ord, val.data());
+  const olgpu_status st =
+      olgpu_interpolate_field(h, var, -1, first_level, pts.data(), (long long)xs.size(), ord, val.data());
   if (st != OLGPU_OK) return st;
   FILE *f = std::fopen(file.c_str(), "a");
   if (!f) return OLGPU_ERR_INVALID_ARG;
@@ -613,6 +617,7 @@ int main(int argc, char **argv)
   else if (equation == "Poisson") p.equation = OLGPU_EQ_POISSON;
   else if (equation == "Boundary-test") p.equation = OLGPU_EQ_BOUNDARY_TEST;
   else if (equation == "Multibox-test") p.equation = OLGPU_EQ_MULTIBOX_TEST;
+  else if (equation == "Bowen-York") p.equation = OLGPU_EQ_BOWEN_YORK;
   else {
     std::fprintf(stderr, "Olliptic_gpu.x: equation %s is not on the puncture FAS path\n", equation.c_str());
     return (int)OLGPU_ERR_INVALID_ARG;
@@ -716,6 +721,7 @@ int main(int argc, char **argv)
                            : p.equation == OLGPU_EQ_POISSON        ? "Poisson"
                            : p.equation == OLGPU_EQ_BOUNDARY_TEST  ? "Robin boundary test"
                            : p.equation == OLGPU_EQ_MULTIBOX_TEST  ? "Multibox test"
+                           : p.equation == OLGPU_EQ_BOWEN_YORK     ? "Bowen-York momentum constrain test"
                                                                    : "";   // the scalar field has no name there
       write_banner(f, p, eq_str,
                    approx_only                          ? "Analitical Approximate"
@@ -810,7 +816,8 @@ int main(int argc, char **argv)
     for (int i = 0; i < p.numbh; i++) std::printf("ADM mass[%d] = %.17g\n", i, adm[i]);
   }
 
-  // elliptic::Print_Solution (src/output.cc:624-700), variable "u"
+  // elliptic::Print_Solution (src/output.cc:624-730): each variable (u, or
+  // Bowen-York's V1, V2, V3, lambda) in turn
   const bool print_1d = A.logic({"-p1d", "--print-1d"}, true);
   const bool print_2d = A.logic({"-p2d", "--print-2d"}, false);
   const bool print_3d = A.logic({"-p3d", "--print-3d"}, false);
@@ -823,50 +830,58 @@ int main(int argc, char **argv)
     // the analytic method's hierarchy has no multigrid coarse grids: its
     // levels are the refinement levels, numbered from the base
     const int l0 = approx_only ? mg : 0;
-    if (print_1d) {
-      std::vector<int> in_level(nl, 0);
-      static const char *ext[3] = {".x", ".y", ".z"};
-      for (int l = l0; l < nl && ps == OLGPU_OK; l++)
-        for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
-          if (boxes[g].level != l) continue;
-          const BoxGeom B{boxes[g]};
-          const std::string stem =
-              dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
-          for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
-            ps = print_box_cut(h, B, g, a, interpol_output, ord, stem + ext[a]);
-        }
-    }
-    if (print_2d) {   // the planes .yz, .xz, .xy of every box, level by level
-      std::vector<int> in_level(nl, 0);
-      static const char *ext[3] = {".yz", ".xz", ".xy"};
-      for (int l = l0; l < nl && ps == OLGPU_OK; l++)
-        for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
-          if (boxes[g].level != l) continue;
-          const BoxGeom B{boxes[g]};
-          const std::string stem =
-              dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
-          for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
-            ps = print_box_plane(h, B, g, a, interpol_output, stem + ext[a]);
-        }
-    }
-    if (print_3d) {   // every point of every box, level by level
-      std::vector<int> in_level(nl, 0);
-      for (int l = l0; l < nl && ps == OLGPU_OK; l++)
-        for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
-          if (boxes[g].level != l) continue;
-          const BoxGeom B{boxes[g]};
-          ps = print_box_3d(h, B, g,
-                            dir + "u-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0.xyz");
-        }
-    }
-    if (print_interpol && ps == OLGPU_OK) {
-      const double Dp = A.num({"-Dp", "--d-print"}, -1.0);
-      const double Lx = A.num({"-Lx", "--length-x"}, p.L), Ly = A.num({"-Ly", "--length-y"}, p.L),
-                   Lz = A.num({"-Lz", "--length-z"}, p.L);
-      static const char *ext[3] = {"u.X", "u.Y", "u.Z"};
-      const double LD[3] = {Lx, Ly, Lz};
-      for (int a = 0; a < 3 && ps == OLGPU_OK; a++) ps = print_interpol_1d(h, a, LD[a], Dp, ord, l0, dir + ext[a]);
-      if (ps == OLGPU_OK) ps = print_interpol_xy(h, Lx, Ly, ord, l0, dir + "u.XY");
+    static const char *by_vars[4] = {"V1", "V2", "V3", "lambda"};
+    const bool by = p.equation == OLGPU_EQ_BOWEN_YORK;
+    for (int iv = 0; iv < (by ? 4 : 1) && ps == OLGPU_OK; iv++) {
+      const char *var = by ? by_vars[iv] : "u";
+      const std::string vs = var;
+      if (print_1d) {
+        std::vector<int> in_level(nl, 0);
+        static const char *ext[3] = {".x", ".y", ".z"};
+        for (int l = l0; l < nl && ps == OLGPU_OK; l++)
+          for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
+            if (boxes[g].level != l) continue;
+            const BoxGeom B{boxes[g]};
+            const std::string stem =
+                dir + vs + "-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
+            for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
+              ps = print_box_cut(h, var, B, g, a, interpol_output, ord, stem + ext[a]);
+          }
+      }
+      if (print_2d) {   // the planes .yz, .xz, .xy of every box, level by level
+        std::vector<int> in_level(nl, 0);
+        static const char *ext[3] = {".yz", ".xz", ".xy"};
+        for (int l = l0; l < nl && ps == OLGPU_OK; l++)
+          for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
+            if (boxes[g].level != l) continue;
+            const BoxGeom B{boxes[g]};
+            const std::string stem =
+                dir + vs + "-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0";
+            for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
+              ps = print_box_plane(h, var, B, g, a, interpol_output, stem + ext[a]);
+          }
+      }
+      if (print_3d) {   // every point of every box, level by level
+        std::vector<int> in_level(nl, 0);
+        for (int l = l0; l < nl && ps == OLGPU_OK; l++)
+          for (int g = 0; g < nb && ps == OLGPU_OK; g++) {
+            if (boxes[g].level != l) continue;
+            const BoxGeom B{boxes[g]};
+            const std::string file =
+                dir + vs + "-l" + std::to_string(l - l0) + "b" + std::to_string(in_level[l]++) + "-0.xyz";
+            ps = print_box_3d(h, var, B, g, file);
+          }
+      }
+      if (print_interpol && ps == OLGPU_OK) {
+        const double Dp = A.num({"-Dp", "--d-print"}, -1.0);
+        const double Lx = A.num({"-Lx", "--length-x"}, p.L), Ly = A.num({"-Ly", "--length-y"}, p.L),
+                     Lz = A.num({"-Lz", "--length-z"}, p.L);
+        static const char *ext[3] = {".X", ".Y", ".Z"};
+        const double LD[3] = {Lx, Ly, Lz};
+        for (int a = 0; a < 3 && ps == OLGPU_OK; a++)
+          ps = print_interpol_1d(h, var, a, LD[a], Dp, ord, l0, dir + vs + ext[a]);
+        if (ps == OLGPU_OK) ps = print_interpol_xy(h, var, Lx, Ly, ord, l0, dir + vs + ".XY");
+      }
     }
     if (ps != OLGPU_OK) {
       olgpu_hierarchy_destroy(h);

@@ -398,6 +398,7 @@ olgpu_status olgpu_server_submit(olgpu_server *s, const olgpu_problem *p, long l
 {
   if (!s || !p || !id) return OLGPU_ERR_INVALID_ARG;
   if (p->method != OLGPU_METHOD_VCYCLE) return OLGPU_ERR_INVALID_ARG;   // the scheduler steps V-cycles
+  if (p->equation == OLGPU_EQ_BOWEN_YORK) return OLGPU_ERR_INVALID_ARG;   // four unknowns in turn: olgpu_solve
   static const int kMaxBoxes = 1024;
   std::vector<olgpu_box_info> boxes(kMaxBoxes);
   int nb = 0;

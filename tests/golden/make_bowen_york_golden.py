@@ -11,7 +11,10 @@ every point where one is non-zero: the momenta spread over a ball of one
 cell diagonal around each puncture) and the four variables at the
 reference's fixed point (its own stop rule, then V-cycles until the largest
 change of any variable is <= 1e-14), sampled on the three centre lines of
-each box and 256 seeded points.
+each box and 256 seeded points.  cli_o2.npz holds the reference's own
+printout of the O2 case (Olliptic.x, -s 1e-14 so that its stop lies near the
+fixed point): the interpolated cuts V1.X, V2.Y, V3.Z, lambda.X (first column
+as text, values as floats) and the per-box cut lambda-l3b0-0.x.
 """
 import os
 import subprocess
@@ -24,6 +27,10 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 sys.path.insert(0, ROOT)
 from tests.golden.make_golden import read_meta, sample_index  # noqa: E402
+from tests.golden.make_output_golden import parse_data_file  # noqa: E402
+
+REF_CLI = os.path.join(ROOT, "oracle", "_ref", "Olliptic.x")
+CLI_FILES = ("V1.X", "V2.Y", "V3.Z", "lambda.X", "lambda-l3b0-0.x")
 
 BY_ARGS = ("-eq Bowen-York -B Robin -NumBH 2 -bhx1 -1.5 -bhx2 1.5 -bhpx1 0.05 -bhpy1 0.1 -bhpy2 -0.1 "
            "-bhpz2 0.03 -L 20 -N 25 -l 3 -s 1e-10")
@@ -64,5 +71,20 @@ def main():
               [len(rec[f"ball_b{g}"]) for g in range(len(boxes))])
 
 
+def cli_golden():
+    run = "/tmp/golden_by_cli"
+    subprocess.run(["rm", "-rf", run], check=True)
+    os.makedirs(run)
+    args = CASES["o2"].replace("-s 1e-10", "-s 1e-14")
+    subprocess.run([REF_CLI] + args.split() + ["-o", "Output"], cwd=run, check=True, stdout=subprocess.DEVNULL,
+                   stderr=subprocess.DEVNULL)
+    rec = {"args": np.array(args.encode())}
+    for f in CLI_FILES:
+        rec[f + "__text"], rec[f + "__vals"] = parse_data_file(os.path.join(run, "Output", f))
+    np.savez_compressed(os.path.join(HERE, "bowen_york", "cli_o2.npz"), **rec)
+    print("cli_o2", sorted(os.listdir(os.path.join(run, "Output")))[:6], "...")
+
+
 if __name__ == "__main__":
     main()
+    cli_golden()

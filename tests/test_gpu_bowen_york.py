@@ -1,0 +1,128 @@
+"""Bowen-York's momentum-constraint test on the GPU (olgpu_solve with
+OLGPU_EQ_BOWEN_YORK): the sources bit for bit and the four variables V1, V2,
+V3, lambda at the fixed point against the reference's own run
+(tests/golden/bowen_york) and against the oracle on every point.  The GPU
+solves the V equations and then lambda (the reference advances the four
+together; the discrete system is the same).  Each variable stops once its
+residual is <= 1e-13 and its last cycle moved it by <= 1e-14; the bar is
+1e-12 (both are at the fixed point to rounding).  A multigrid coarse grid's
+ghost layers are not fixed by the system and are left out."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import ollipticid_gb300 as og
+from ollipticid_gb300 import _abi
+from tests.test_oracle_bowen_york import VARS, fixed_mask
+
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bowen_york", "o*.npz")))
+TOL = 1e-12
+
+pytestmark = pytest.mark.gpu
+
+
+def solve(E):
+    return E.Solve(stop=_abi.STOP_ERROR, max_cycles=400, tol=1e-13, du_tol=1e-14)
+
+
+@pytest.mark.parametrize("path", GOLD, ids=lambda p: os.path.basename(p)[:-4])
+def test_fixed_point_matches_the_reference(path, oracle_mod):
+    G = np.load(path)
+    P = og.parse_olliptic_args(str(G["args"]).split())
+    orc = oracle_mod.Oracle(dict(P.oracle_dict(), by_var=0))
+    with og.Elliptic(P) as E:
+        assert [list(b.n) for b in E.boxes] == G["box_n"].tolist()
+        for g in range(len(E.boxes)):   # V1's source, before the solve
+            rho = E.get_field(g, "rho").ravel()
+            np.testing.assert_array_equal(rho[G[f"idx_b{g}"]], G[f"rho0_b{g}"])
+            np.testing.assert_array_equal(rho[G[f"ball_b{g}"]], G[f"rho0_ball_b{g}"])
+        with pytest.raises(_abi.OlgpuError):
+            E.get_field(0, "lambda")   # not solved yet
+        rep = solve(E)
+        assert rep.status == 0 and rep.final_du <= 1e-14, (rep.status, rep.final_du)
+        for g in range(len(E.boxes)):
+            idx = G[f"idx_b{g}"]
+            keep = fixed_mask(orc, g, idx)
+            for v in VARS:
+                got = E.get_field(g, v).ravel()[idx]
+                err = np.max(np.abs(got[keep] - G[f"{v}_b{g}"][keep]))
+                assert err <= TOL, (v, g, err)
+        np.testing.assert_array_equal(E.get_field(1, "u"), E.get_field(1, "lambda"))
+
+
+def test_every_point_matches_the_oracle(oracle_mod):
+    """O2 case: all four variables on every point the system fixes, and
+    lambda's source (the divergence of the solved V) against the oracle's."""
+    G = np.load(GOLD[0])
+    P = og.parse_olliptic_args(str(G["args"]).split())
+    fields, _ = oracle_mod.bowen_york_fixed_point(P.oracle_dict())
+    lam = oracle_mod.Oracle(dict(P.oracle_dict(), by_var=3))
+    with og.Elliptic(P) as E:
+        solve(E)
+        for g, b in enumerate(E.boxes):
+            nx, ny, nz = b.n
+            keep = fixed_mask(lam, g, np.arange(nx * ny * nz)).reshape(nz, ny, nx)
+            for v in VARS:
+                err = np.max(np.abs(E.get_field(g, v) - fields[v][g])[keep])
+                assert err <= TOL, (v, g, err)
+        # the divergence source, from the GPU's V by the GPU and by the oracle,
+        # equal to rounding, on the finest level (on the coarser ones the FAS
+        # correction overwrites the source under the finer boxes)
+        vs = [oracle_mod.Oracle(dict(P.oracle_dict(), by_var=c)) for c in range(3)]
+        for c, o in enumerate(vs):
+            for g in range(o.nboxes):
+                o.set_field(g, "u", E.get_field(g, VARS[c]))
+        lam.L.orc_set_divergence_source(lam._s, *(o._s for o in vs))
+        for g in [g for g, b in enumerate(E.boxes) if b.level == E.levels - 1]:
+            want = lam.field(g, "rho")
+            assert np.max(np.abs(E.get_field(g, "rho") - want)) <= 1e-13 * max(1.0, np.max(np.abs(want)))
+
+
+def test_bowen_york_is_refused_where_it_is_not_built():
+    G = np.load(GOLD[0])
+    P = og.parse_olliptic_args(str(G["args"]).split())
+    with og.Elliptic(P) as E:
+        with pytest.raises(_abi.OlgpuError):
+            E.set_precision(True)
+        with pytest.raises(_abi.OlgpuError):
+            og.solve_many([E])
+
+
+def test_cli_prints_the_reference_cuts(tmp_path):
+    """Olliptic_gpu.x -eq Bowen-York prints each variable as the reference
+    does (V1.X, V2.Y, V3.Z, lambda.X, the per-box cut lambda-l3b0-0.x):
+    the same points, and values equal to the reference's printout, both runs
+    stopped near the fixed point (-s 1e-14), within 1e-10 where the point is
+    read from a solution level.  A point read from a multigrid coarse grid
+    (the ends of a cut) holds the last coarse-grid approximation: within
+    1e-6 for V; lambda's differs more (1e-5), because the reference's
+    coarsest solve updates lambda's ghost layers from a V that is moving in
+    the same sweeps, so those points are not compared for lambda."""
+    import re
+    import subprocess
+    from tests.test_gpu_output import box_levels
+    g = np.load(os.path.join(os.path.dirname(GOLD[0]), "cli_o2.npz"))
+    args = g["args"].item().decode()
+    cli = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "ollipticid_gb300", "_build",
+                       "Olliptic_gpu.x")
+    r = subprocess.run([cli] + args.split() + ["-o", "Output"], cwd=str(tmp_path), capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr
+    mg = int(re.search(r"\((\d+) multigrid\)", r.stdout).group(1))
+    level_of = box_levels(args)
+    for name in ("V1.X", "V2.Y", "V3.Z", "lambda.X", "lambda-l3b0-0.x"):
+        text, want = g[name + "__text"], g[name + "__vals"]
+        rows = [i for i in range(len(text)) if text[i]]
+        ours = np.loadtxt(tmp_path / "Output" / name)
+        x = np.array([float(text[i]) for i in rows])
+        assert np.array_equal(ours[:, 0], x), name
+        pts = np.zeros((len(rows), 3))
+        pts[:, "XYZ".index(name[-1].upper())] = x
+        if name.endswith(".x"):   # a box's own cut: every point is that (finest) box's
+            tol = np.full(len(rows), 1e-10)
+        else:
+            tol = np.where(level_of(pts) < mg, np.inf if name.startswith("lambda") else 1e-6, 1e-10)
+        err = np.abs(ours[:, 1] - want[rows])
+        assert (err <= tol).all(), (name, float(err.max()))

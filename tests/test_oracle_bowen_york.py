@@ -16,7 +16,7 @@ import pytest
 
 from ollipticid_gb300 import parse_olliptic_args
 
-GOLD = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bowen_york", "*.npz")))
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bowen_york", "o*.npz")))
 VARS = ("V1", "V2", "V3", "lambda")
 FIXED_TOL = 1e-13
 
