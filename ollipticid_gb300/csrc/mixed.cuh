@@ -807,6 +807,233 @@ __global__ void __launch_bounds__(1024) k_coarse32(const DevBox *__restrict__ bo
   if (threadIdx.x == 0) *iters_out = it;
 }
 
+// Blocks of k_coarse32_cluster's clusters (portable size).
+constexpr int kCoarse32Ncta = 8;
+
+// Points of the largest slab of k_coarse32_cluster on a box: each of its
+// shared arrays (e and the staged S, A, 1/(c+u), and d, E5) holds that many
+// floats in every block.
+__host__ __device__ inline int coarse32_cluster_slab(int n0, int n1, int n2, int ncta)
+{
+  int smax = 0;
+  for (int r = 0; r < ncta; r++) {
+    const int planes = cslab_begin(r + 1, n2, ncta) - cslab_begin(r, n2, ncta);
+    smax = planes * n0 * n1 > smax ? planes * n0 * n1 : smax;
+  }
+  return smax;
+}
+
+// k_coarse32's iteration with the box spread over a cluster of NCTA blocks,
+// one cluster per box (the coarsest problems of a batch's solves side by
+// side): the z-planes split as in k_coarse_cluster (block 0 owns the low
+// ghost plane and the two interior planes above it, the last block the
+// mirror image, so the Robin update -- faces, edges, corners -- stays inside
+// a block), e in the blocks' shared memory with the other blocks' planes read
+// through distributed shared memory, and each block's S, A, 1/(c+u) (d, E5)
+// staged beside its slab.  A sweep needs a cluster barrier after colour 0
+// (colour 1 reads its z neighbours) and one after colour 1 (the norm, and the
+// next colour 0).  Every block reads every block's partial norm in the same
+// order, so all take the same stop decision.  The updates are k_coarse32's.
+template <int EQ, int NCTA>
+__global__ void __launch_bounds__(256) k_coarse32_cluster(const DevBox *__restrict__ boxes, BoxList L, DevFields32 G,
+                                                          const double *__restrict__ crd, int max_it, float omega,
+                                                          float rtol, Stats *stats)
+{
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  extern __shared__ float4 s_c32[];
+  float *se = reinterpret_cast<float *>(s_c32);
+  __shared__ float *plane[64];
+  __shared__ float red[8];               // one slot per warp (256 threads)
+  __shared__ int red_nan[8];
+  __shared__ float s_part[2][2];         // per iteration parity: max |R| of this block, NaN seen
+  __shared__ float s_x[3][64], s_ix[3][64];
+
+  if ((int)(blockIdx.x / NCTA) >= L.count) return;   // the whole cluster: one box a cluster
+  const DevBox B = boxes[L.box[blockIdx.x / NCTA]];
+  if (!B.active) return;   // every block of the cluster reads the same box: all leave
+  int *iters_out = &stats[B.solve].coarse_iters, *nan_flag = &stats[B.solve].nan_flag;
+  const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
+  const int n01 = n0 * n1;
+  const int kz0 = cslab_begin(rank, n2, NCTA), kz1 = cslab_begin(rank + 1, n2, NCTA);
+  const int slab = (kz1 - kz0) * n01;
+  const int smax = coarse32_cluster_slab(n0, n1, n2, NCTA);
+  float *cs = se + smax, *ca = se + 2 * smax, *ciq = se + 3 * smax;
+  float *cd = se + 4 * smax, *ce5 = se + 5 * smax;   // scalar field only
+  for (int k = threadIdx.x; k < n2; k += blockDim.x) {
+    int r = 0;
+    while (cslab_begin(r + 1, n2, NCTA) <= k) r++;
+    plane[k] = cl.map_shared_rank(se, r) + (k - cslab_begin(r, n2, NCTA)) * n01;
+  }
+  float *ge = G.f[G_E] + B.off;
+  const long long g0 = (long long)kz0 * n01;
+  for (int p = threadIdx.x; p < slab; p += blockDim.x) {
+    se[p] = ge[g0 + p];
+    cs[p] = G.f[G_S][B.off + g0 + p];
+    ca[p] = G.f[G_A][B.off + g0 + p];
+    ciq[p] = G.f[G_IQ][B.off + g0 + p];
+    if (EQ == 1) {
+      cd[p] = G.f[G_D][B.off + g0 + p];
+      ce5[p] = G.f[G_E5][B.off + g0 + p];
+    }
+  }
+  for (int t = threadIdx.x; t < n0 + n1 + n2; t += blockDim.x) {
+    const int a = t < n0 ? 0 : t < n0 + n1 ? 1 : 2;
+    const int i = t - (a == 0 ? 0 : a == 1 ? n0 : n0 + n1);
+    const float x = (float)crd[B.coord_off + t];
+    s_x[a][i] = x;
+    s_ix[a][i] = x != 0.0f ? rcp_fast(x) : 0.0f;
+  }
+  cl.sync();   // every block's slab and plane table are in place
+
+  auto E = [&](int i, int j, int k) -> float & { return plane[k][j * n0 + i]; };
+  auto own = [&](int i, int j, int k) { return (k - kz0) * n01 + j * n0 + i; };   // this block's staged arrays
+  const float dl = (float)B.dulap;
+  const float ix2 = (float)B.idx2[0], iy2 = (float)B.idx2[1], iz2 = (float)B.idx2[2];
+  const float idx[3] = {(float)B.idx[0], (float)B.idx[1], (float)B.idx[2]};
+  // derivf<2> at a ghost position: one-sided, pointing inward
+  auto d1 = [&](int a, int i, int j, int k, float &du) -> float {
+    const int ijk[3] = {i, j, k};
+    const int s = ijk[a] == 0 ? 1 : -1;
+    int p1[3] = {i, j, k}, p2[3] = {i, j, k};
+    p1[a] += s;
+    p2[a] += 2 * s;
+    const float u0 = E(i, j, k), u1 = E(p1[0], p1[1], p1[2]), u2 = E(p2[0], p2[1], p2[2]);
+    if (ijk[a] == 0) {
+      du = -1.5f * idx[a];
+      return (-3.0f * u0 + 4.0f * u1 - u2) * 0.5f * idx[a];
+    }
+    du = 1.5f * idx[a];
+    return (3.0f * u0 - 4.0f * u1 + u2) * 0.5f * idx[a];
+  };
+  auto robin = [&](int mask, int i, int j, int k) {
+    const int ijk[3] = {i, j, k};
+    const float r2 = s_x[0][i] * s_x[0][i] + s_x[1][j] * s_x[1][j] + s_x[2][k] * s_x[2][k];
+    float t = 0.0f, dt = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      if (!(mask & (1 << a))) continue;
+      float du;
+      const float dv = d1(a, i, j, k, du);
+      t += dv * s_ix[a][ijk[a]];
+      dt += du * s_ix[a][ijk[a]];
+    }
+    float &ee = E(i, j, k);
+    const float Fv = r2 * t + ee - cs[own(i, j, k)];
+    ee = ee - Fv * rcp_fast(r2 * dt + 1.0f);
+  };
+
+  float norm = 1.0f, prev, first = -1.0f;
+  int it = 0;
+  const int mi0 = n0 - 2, mi1 = n1 - 2;
+  do {
+    prev = norm;
+    // Robin update of this block's planes: faces, then edges, then corners
+    for (int k = kz0; k < kz1; k++) {
+      if (k == 0 || k == n2 - 1) {
+        for (int t = threadIdx.x; t < mi0 * mi1; t += blockDim.x) robin(4, 1 + t % mi0, 1 + t / mi0, k);
+      } else {
+        for (int t = threadIdx.x; t < 2 * mi1 + 2 * mi0; t += blockDim.x) {
+          if (t < 2 * mi1) robin(1, (t & 1) ? n0 - 1 : 0, 1 + (t >> 1), k);
+          else {
+            const int q = t - 2 * mi1;
+            robin(2, 1 + (q >> 1), (q & 1) ? n1 - 1 : 0, k);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int k = kz0; k < kz1; k++) {
+      if (k == 0 || k == n2 - 1) {
+        for (int t = threadIdx.x; t < 2 * mi1 + 2 * mi0; t += blockDim.x) {
+          if (t < 2 * mi1) robin(5, (t & 1) ? n0 - 1 : 0, 1 + (t >> 1), k);   // x-z edges
+          else {
+            const int q = t - 2 * mi1;
+            robin(6, 1 + (q >> 1), (q & 1) ? n1 - 1 : 0, k);                   // y-z edges
+          }
+        }
+      } else if (threadIdx.x < 4) {
+        robin(3, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);   // x-y edges
+      }
+    }
+    __syncthreads();
+    for (int k = kz0; k < kz1; k++)
+      if ((k == 0 || k == n2 - 1) && threadIdx.x < 4)
+        robin(7, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);
+    __syncthreads();
+    // one red-black SOR sweep over the interior points of this block's planes
+    float rmax = 0.0f;
+    int nan_seen = 0;
+    const int ka = kz0 > 1 ? kz0 : 1, kb = kz1 < n2 - 1 ? kz1 : n2 - 1;
+    const int H = (mi0 + 1) / 2;
+    const int work = H * mi1 * (kb > ka ? kb - ka : 0);
+    for (int color = 0; color < 2; color++) {
+      for (int t = threadIdx.x; t < work; t += blockDim.x) {
+        const int ih = t % H, r = t / H;
+        const int j = 1 + r % mi1, k = ka + r / mi1;
+        const int i = 1 + ((color + 1 + j + k) & 1) + 2 * ih;
+        if (i >= n0 - 1) continue;
+        const float c0 = E(i, j, k);
+        const float lv = (E(i + 1, j, k) - 2.0f * c0 + E(i - 1, j, k)) * ix2 +
+                         (E(i, j + 1, k) - 2.0f * c0 + E(i, j - 1, k)) * iy2 +
+                         (E(i, j, k + 1) - 2.0f * c0 + E(i, j, k - 1)) * iz2;
+        const int q = own(i, j, k);
+        float op, dop;
+        corr_op<EQ>(lv, dl, c0, ca[q], ciq[q], EQ == 1 ? cd[q] : 0.0f, EQ == 1 ? ce5[q] : 0.0f, op, dop);
+        const float R = op - cs[q];
+        const float en = c0 - omega * (R * rcp_fast(dop));
+        E(i, j, k) = en;
+        rmax = fmaxf(rmax, fabsf(R));
+        if (!(en == en)) nan_seen = 1;
+      }
+      if (color == 0) cl.sync();   // colour 1 reads colour 0 of the neighbouring blocks
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+      nan_seen |= __shfl_xor_sync(0xffffffffu, nan_seen, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[threadIdx.x >> 5] = rmax;
+      red_nan[threadIdx.x >> 5] = nan_seen;
+    }
+    __syncthreads();
+    const int par = it & 1;
+    if (threadIdx.x == 0) {
+      float m = 0.0f;
+      int nn = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+        m = fmaxf(m, red[w]);
+        nn |= red_nan[w];
+      }
+      s_part[par][0] = m;
+      s_part[par][1] = nn ? 1.0f : 0.0f;
+    }
+    cl.sync();   // every block's colour 1 and partial norm are done
+    // the slot of this parity is written again two iterations later, after
+    // two more cluster barriers that this block must reach first
+    float m = 0.0f, nanv = 0.0f;
+#pragma unroll
+    for (int r = 0; r < NCTA; r++) {
+      const float *pr = cl.map_shared_rank(&s_part[par][0], r);
+      m = fmaxf(m, pr[0]);
+      nanv = fmaxf(nanv, pr[1]);
+    }
+    norm = m;
+    it++;
+    if (first < 0.0f) first = norm;
+    if (nanv > 0.0f) {
+      if (rank == 0 && threadIdx.x == 0) atomicOr(nan_flag, 1);
+      break;                                       // the same decision in every block
+    }
+    if (norm <= rtol * first) break;
+  } while (norm > 0.0f && prev != norm && it < max_it);
+  cl.sync();   // every block is done reading the others' shared memory
+  for (int p = threadIdx.x; p < slab; p += blockDim.x) ge[g0 + p] = se[p];
+  if (rank == 0 && threadIdx.x == 0) *iters_out = it;
+}
+
 }  // namespace olgpu
 
 namespace olgpu {

@@ -54,6 +54,7 @@ constexpr int kThreads = 256;
 // wave of 256-thread blocks, so smaller blocks spread it more evenly
 constexpr int kSmoothThreads = 128;
 constexpr size_t kCoarseSmemMax = 200 * 1024;   // dynamic shared memory of the coarse solves
+constexpr size_t kCoarse32ClusterSmem = 96 * 1024;   // ... of a block of k_coarse32_cluster
 // iterations of one W-cycle level's loop in one call (OLGPU_WCYCLE_LEVEL_CAP)
 constexpr int kWcycleLevelCap = OLGPU_WCYCLE_LEVEL_CAP;
 
@@ -303,6 +304,7 @@ struct olgpu_hierarchy {
   std::vector<int> fine_count;
   bool is_union = false;
   bool mixed_ready = false;         // FP32 fields, plans and Anderson history are set up
+  bool coarse32_clusters = false;   // FP32 coarsest solves may run as clusters (k_coarse32_cluster)
   bool owns_arena = true, owns_arena32 = true, owns_stats = true;
   bool pooled_hstats = false;   // h_stats from the recycled pinned records (one Stats)
   bool live = false;            // counted among the device's live hierarchies
@@ -1369,6 +1371,48 @@ void dispatch_robin32(olgpu_hierarchy *h, int level, int mode, bool whole = fals
   else launch_robin32<4>(h, level, mode, whole);
 }
 
+// Whether k_coarse32_cluster<EQ> runs here: its shared-memory limit set (the
+// same for every hierarchy, so that none lowers it below what another's
+// captured cycle launches with) and one cluster resident.
+template <int EQ>
+bool coarse32_cluster_fits()
+{
+  auto kern = k_coarse32_cluster<EQ, kCoarse32Ncta>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoarse32ClusterSmem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(kCoarse32Ncta, 1, 1);
+  cfg.blockDim = dim3(256, 1, 1);
+  cfg.dynamicSmemBytes = kCoarse32ClusterSmem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kCoarse32Ncta;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return n >= 1;
+}
+
+// Shared memory of a block of k_coarse32_cluster for a coarsest box, or 0
+// where the kernel does not take it (one ghost layer, 6..64 planes, rows of
+// at most 64 points, arrays within kCoarse32ClusterSmem).
+size_t coarse32_cluster_smem(const DevBox &B, int eq)
+{
+  if (B.buf != 1 || B.n[2] < 6 || B.n[0] > 64 || B.n[1] > 64 || B.n[2] > 64) return 0;
+  const size_t bytes =
+      sizeof(float) * (size_t)coarse32_cluster_slab(B.n[0], B.n[1], B.n[2], kCoarse32Ncta) * (eq == 1 ? 6 : 4);
+  return bytes <= kCoarse32ClusterSmem ? bytes : 0;
+}
+
 template <int EQ>
 void emit_fasn32(olgpu_hierarchy *h, int k)
 {
@@ -1412,12 +1456,34 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
     launch_ew32(h, k - 1, EW32_W_PLUS_EQ_R_WW_EQ_E, true);   // WW = E: nothing writes E before set_in
     launch_transfer32(h, h->set_in32[k]);
   }
-  // a union: members whose coarsest level is k - 1 solve it (one block each,
-  // side by side: one launch for those whose coefficients fit in shared
-  // memory beside e, one for the others), the others descend
+  // a union: members whose coarsest level is k - 1 solve it, side by side:
+  // one launch of a cluster per box for the boxes k_coarse32_cluster takes,
+  // one of a block per box for those whose coefficients fit in shared memory
+  // beside e, one for the others; the other members descend
   bool deeper = false;
-  BoxList Ls{}, Lg{};
-  size_t smem_s = 0, smem_g = 0;
+  BoxList Ls{}, Lg{}, Lc{};
+  size_t smem_s = 0, smem_g = 0, smem_c = 0;
+  auto flush_cluster = [&]() {   // one cluster of kCoarse32Ncta blocks per box
+    if (Lc.count == 0) return;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(Lc.count * kCoarse32Ncta), 1, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.dynamicSmemBytes = smem_c;
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kCoarse32Ncta;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_coarse32_cluster<EQ, kCoarse32Ncta>, (const DevBox *)h->d_boxes, Lc, h->F32,
+                       (const double *)h->d_coords, h->coarse_max_iters, (float)h->coarse_omega, 1e-4f,
+                       h->d_stats0);
+    h->launches_mixed++;
+    Lc.count = 0;
+    smem_c = 0;
+  };
   auto flush = [&](BoxList &BL, size_t smem, bool staged_coeffs) {
     if (BL.count == 0) return;
     if (staged_coeffs)
@@ -1437,6 +1503,13 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
       continue;
     }
     const DevBox &B = h->hboxes[M.coarse_box];
+    const size_t csm = h->coarse32_clusters ? coarse32_cluster_smem(B, EQ) : 0;
+    if (csm > 0) {   // every box the cluster kernel takes runs there, alone or in a batch
+      Lc.box[Lc.count++] = M.coarse_box;
+      smem_c = std::max(smem_c, csm);
+      if (Lc.count == kMaxBoxesPerLevel) flush_cluster();
+      continue;
+    }
     const size_t np = (size_t)B.n[0] * B.n[1] * B.n[2];
     const size_t staged = sizeof(float) * np * (EQ == 1 ? 6 : 4);
     const bool st = staged <= kCoarseSmemMax;
@@ -1448,6 +1521,7 @@ void emit_fasn32(olgpu_hierarchy *h, int k)
   }
   flush(Ls, smem_s, true);
   flush(Lg, smem_g, false);
+  flush_cluster();
   if (deeper) emit_fasn32<EQ>(h, k - 1);
   if (k > mg && launch_prolong_ghost<float>(h, h->prolong_v32[k], h->ghost_e[k], h->F32, G_E, G_WW)) {
     h->launches_mixed++;
@@ -1654,7 +1728,11 @@ olgpu_status prepare_mixed(olgpu_hierarchy *h, float *arena32, long long stride,
   for (const void *kern : {(const void *)k_coarse32<0, true>, (const void *)k_coarse32<1, true>,
                            (const void *)k_coarse32<0, false>, (const void *)k_coarse32<1, false>})
     CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCoarseSmemMax));
-  if (!member) choose_smooth_clusters(h);
+  if (!member) {
+    choose_smooth_clusters(h);
+    h->coarse32_clusters =
+        !std::getenv("OLGPU_COARSE32_ONE_BLOCK") && coarse32_cluster_fits<0>() && coarse32_cluster_fits<1>();
+  }
   h->mixed_ready = true;
   return OLGPU_OK;
 }
