@@ -464,6 +464,65 @@ def run_approx_start():
     return out
 
 
+def run_bowen_york():
+    """The Bowen-York momentum-constraint test (four unknowns V1, V2, V3,
+    lambda) of tests/golden/bowen_york/o4.npz (two punctures with momenta,
+    N = 25, 3 levels, O4, Robin with falloff 2): GPU solves/s from zero
+    (FP64 cycles with FP64 Anderson mixing as in the headline solve, each
+    variable to the problem's residual 1e-10 and a change of at most 1e-11;
+    device time, five solves after a warm-up), the largest distance from the
+    reference's own fixed point over the fixture's samples, and as the CPU
+    baseline the oracle restatement's single-threaded solve of the same case
+    under the reference's stop rule."""
+    import numpy as np
+    import ollipticid_gb300 as og
+    from ollipticid_gb300 import _abi
+    path = os.path.join(ROOT, "tests", "golden", "bowen_york", "o4.npz")
+    G = np.load(path)
+    P = og.parse_olliptic_args(str(G["args"]).split())
+    rule = dict(stop=_abi.STOP_ERROR, max_cycles=400, tol=P.tol, du_tol=0.1 * P.tol)
+    with og.Elliptic(P) as E:
+        E.set_fp64_acceleration(ACCEL)
+        E.Solve(**rule)
+        ms, cycles = 0.0, 0
+        for _ in range(5):
+            E.reset()
+            rep = E.Solve(**rule)
+            ms += E.last_device_ms
+            cycles += rep.cycles
+        err = 0.0
+        for g, b in enumerate(E.boxes):
+            idx = G[f"idx_b{g}"]
+            nx, ny, nz = b.n
+            k, j, i = np.unravel_index(idx, (nz, ny, nx))
+            keep = np.ones(len(idx), dtype=bool)
+            if b.level < E.mgrid_levels:   # a multigrid grid's ghost layers are not fixed by the system
+                keep = (i >= b.buf) & (i < nx - b.buf) & (j >= b.buf) & (j < ny - b.buf) & (k >= b.buf) & (
+                    k < nz - b.buf)
+            for v in og.BY_VARS:
+                got = E.get_field(g, v).ravel()[idx]
+                err = max(err, float(np.max(np.abs(got[keep] - G[f"{v}_b{g}"][keep]))))
+    from oracle import oracle as oracle_mod
+    t = time.perf_counter()
+    solved, ocycles = [], []
+    for v in range(4):
+        o = oracle_mod.Oracle(dict(P.oracle_dict(), equation=oracle_mod.BOWEN_YORK, by_var=v))
+        if v == 3:
+            o.L.orc_set_divergence_source(o._s, *(s._s for s in solved))
+        ocycles.append(o.solve()[0])
+        solved.append(o)
+    cpu_s = time.perf_counter() - t
+    return {"workload": "Bowen-York momentum-constraint test, 2 punctures with momenta, N = 25, 3 levels, O4, "
+                        "Robin falloff 2 (tests/golden/bowen_york/o4.npz)",
+            "value": 5 / (ms / 1000.0), "unit": UNIT, "ms_per_solve": ms / 5, "cycles_per_solve": cycles / 5,
+            "max_abs_minus_reference_fixed_point": err,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"one solve by the oracle restatement under the reference's stop rule "
+                                       f"({sum(ocycles)} V-cycles over the four variables) in {cpu_s:.1f} s"},
+            "iteration": f"each variable: FP64 V-cycles with FP64 Anderson mixing of depth {ACCEL}",
+            "timing": "device time of olgpu_solve (CUDA events), five solves from zero after a warm-up"}
+
+
 def fp32_smoother_roofline(peak: float, peak_kind: str):
     """The mixed cycle's dominant kernel, the cluster-resident FP32 smoother
     (k_smooth32_cluster), on the finest level of the benchmark binary, 20
@@ -863,7 +922,7 @@ def run_gpu(args, rank: int, world: int, local: int):
     mixed = run_mixed(E, P, args, dev, u_fix, fx)
 
     concurrent = batched = served = served_binaries = served_binaries_batching = None
-    config3 = convergence = approx_start = None
+    config3 = convergence = approx_start = bowen_york = None
     if rank == 0 and world == 1 and not args.no_extra:
         from ollipticid_gb300 import autotune
         concurrent = run_concurrent(E, P, fx, value / world)
@@ -875,6 +934,7 @@ def run_gpu(args, rank: int, world: int, local: int):
         config3 = run_config3()
         convergence = run_convergence()
         approx_start = run_approx_start()
+        bowen_york = run_bowen_york()
         served = run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]))   # layout follows the load
         served += run_served(inner_sweeps=tuple(concurrent["inner_sweeps"]), native=True)
         served_binaries = run_served_binaries(
@@ -933,7 +993,7 @@ def run_gpu(args, rank: int, world: int, local: int):
             "mixed": mixed, "concurrent": concurrent, "batched": batched, "served": served,
             "served_binaries": served_binaries, "served_binaries_batching": served_binaries_batching,
             "config3": config3,
-            "convergence": convergence, "approx_start": approx_start,
+            "convergence": convergence, "approx_start": approx_start, "bowen_york": bowen_york,
             "roofline": roof, "roofline_fp32_smoother": roof32, "fma_peaks": fma, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
