@@ -395,14 +395,15 @@ long long blocks_faces(const DevBox &B)
 }
 
 // The stencil terms of a box descriptor, shared by the hierarchy's boxes and
-// the single caller-owned box of olgpu_smooth_box_noalloc: 1/dx and 1/dx^2
-// per axis, whether every axis has the same spacing, and the diagonal of the
-// order's Laplacian (duLapc2/4/6/8, include/ffunction.h:1310-1313,
-// 1382-1385, 1466-1469, 1521-1524).
+// the single caller-owned box of olgpu_smooth_box_noalloc: the spacing, 1/dx
+// and 1/dx^2 per axis, whether every axis has the same spacing, and the
+// diagonal of the order's Laplacian (duLapc2/4/6/8, include/ffunction.h:
+// 1310-1313, 1382-1385, 1466-1469, 1521-1524).
 void set_box_stencil(DevBox &B, int order, const double d[3])
 {
   B.order = order;
   for (int a = 0; a < 3; a++) {
+    B.d[a] = d[a];
     B.idx[a] = 1.0 / d[a];
     B.idx2[a] = B.idx[a] * B.idx[a];
   }
@@ -2042,7 +2043,6 @@ static olgpu_status plan_hierarchy(const olgpu_problem *p, olgpu_hierarchy *h)
     B.active = 1;
     B.mg_coarse = D.level < h->G.mgrid_levels ? 1 : 0;
     B.falloff = h->equation == OLGPU_EQ_BOWEN_YORK ? 2 : 1;   // src/operator.cc:789, 1393-1399
-    for (int a = 0; a < 3; a++) B.d[a] = D.d[a];
     set_box_stencil(B, D.order, D.d);
     // x, y, z of the box's nodes, then their reciprocals (ghost nodes lie on
     // the outer faces; a node at 0 gets 0, it is never a Robin point)
@@ -3710,6 +3710,7 @@ extern "C" olgpu_status olgpu_smooth_box_noalloc(const olgpu_box_fields *f, int 
   B.level = 0;
   B.solve = 0;
   B.active = 1;
+  B.falloff = 1;
   const double d[3] = {f->dx, f->dy, f->dz};
   set_box_stencil(B, f->order, d);
   // the descriptor and the zeroed accumulators go into the fixed scratch
