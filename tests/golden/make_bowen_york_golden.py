@@ -34,7 +34,7 @@ CLI_FILES = ("V1.X", "V2.Y", "V3.Z", "lambda.X", "lambda-l3b0-0.x")
 
 BY_ARGS = ("-eq Bowen-York -B Robin -NumBH 2 -bhx1 -1.5 -bhx2 1.5 -bhpx1 0.05 -bhpy1 0.1 -bhpy2 -0.1 "
            "-bhpz2 0.03 -L 20 -N 25 -l 3 -s 1e-10")
-CASES = {"o2": BY_ARGS + " -O 2", "o4": BY_ARGS + " -O 4",
+CASES = {"o2": BY_ARGS + " -O 2", "o4": BY_ARGS + " -O 4", "o6": BY_ARGS + " -O 6",
          "o2_dirichlet": BY_ARGS.replace("-B Robin", "-B Dirichlet") + " -O 2"}
 VARS = ("V1", "V2", "V3", "lambda")
 

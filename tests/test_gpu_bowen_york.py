@@ -126,3 +126,22 @@ def test_cli_prints_the_reference_cuts(tmp_path):
             tol = np.where(level_of(pts) < mg, np.inf if name.startswith("lambda") else 1e-6, 1e-10)
         err = np.abs(ours[:, 1] - want[rows])
         assert (err <= tol).all(), (name, float(err.max()))
+
+
+def test_wcycle_reaches_the_same_fixed_point():
+    """-m Wcycle: each variable's W-cycles (every level repeated until its
+    own norm is <= 1e-12) end within 1e-10 of the reference's fixed point on
+    the solution levels."""
+    G = np.load(GOLD[0])
+    P = og.parse_olliptic_args(str(G["args"]).split())
+    P.method = "Wcycle"
+    with og.Elliptic(P) as E:
+        rep = E.Solve(max_cycles=200, tol=1e-12)
+        assert rep.status == 0 and rep.final_res <= 1e-12
+        for g, b in enumerate(E.boxes):
+            if b.level < E.mgrid_levels:
+                continue
+            idx = G[f"idx_b{g}"]
+            for v in VARS:
+                err = np.max(np.abs(E.get_field(g, v).ravel()[idx] - G[f"{v}_b{g}"]))
+                assert err <= 1e-10, (v, g, err)
