@@ -12,7 +12,9 @@
 //
 // Ownership keeps the Robin update local: block 0 owns the low ghost plane
 // and the two interior planes above it, the last block the mirror image, and
-// the others share the planes in between.  A face point reads interior points
+// the others share the planes in between (cslab_begin; the balanced layout,
+// cslab_begin_bal, moves one of those planes to the next block and separates
+// the Robin phases by cluster barriers instead).  A face point reads interior points
 // of its own plane (or, on a z face, the two planes next to it); an edge
 // point reads face points, a corner edge points, all in planes its block
 // owns.  So faces -> edges -> corners need only block barriers, and since
@@ -41,11 +43,33 @@ __host__ __device__ inline int cslab_begin(int r, int n2, int ncta)
   return 3 + rr * base + (rr < rem ? rr : rem);
 }
 
+// The balanced layout (bal = 1): block 0 holds [0, 2), the ghost plane and
+// one interior plane, block ncta-1 [n2-2, n2), blocks 1..ncta-2 share
+// [2, n2-2) evenly, so that on 16 blocks no block sweeps more than about one
+// plane.  A z-face Robin point then reads plane 2 (n2-3) of the next block,
+// and the edges and corners beside it read that block's face and edge
+// points: faces, edges and corners are separated by cluster barriers
+// instead of block barriers.  The updates are the same.
+__host__ __device__ inline int cslab_begin_bal(int r, int n2, int ncta)
+{
+  if (r <= 0) return 0;
+  if (r >= ncta) return n2;
+  if (r == ncta - 1) return n2 - 2;
+  const int m = n2 - 4, k = ncta - 2, rr = r - 1;
+  const int base = m / k, rem = m % k;
+  return 2 + rr * base + (rr < rem ? rr : rem);
+}
+
+__host__ __device__ inline int cslab_at(int r, int n2, int ncta, int bal)
+{
+  return bal ? cslab_begin_bal(r, n2, ncta) : cslab_begin(r, n2, ncta);
+}
+
 template <int EQ, int NCTA>
 __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict__ boxes, int box, DevFields F,
                                                         const double *__restrict__ crd, double eps, int max_it,
                                                         double omega, double rtol, double *norm_out,
-                                                        int *iters_out, int *nan_flag, int dirichlet)
+                                                        int *iters_out, int *nan_flag, int dirichlet, int bal)
 {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -61,11 +85,11 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
   if (!B.active) return;   // every block of the cluster reads the same box: all leave
   const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2];
   const int n01 = n0 * n1;
-  const int kz0 = cslab_begin(rank, n2, NCTA), kz1 = cslab_begin(rank + 1, n2, NCTA);
+  const int kz0 = cslab_at(rank, n2, NCTA, bal), kz1 = cslab_at(rank + 1, n2, NCTA, bal);
   for (int k = threadIdx.x; k < n2; k += blockDim.x) {
     int r = 0;
-    while (cslab_begin(r + 1, n2, NCTA) <= k) r++;
-    plane[k] = cl.map_shared_rank(su, r) + (k - cslab_begin(r, n2, NCTA)) * n01;
+    while (cslab_at(r + 1, n2, NCTA, bal) <= k) r++;
+    plane[k] = cl.map_shared_rank(su, r) + (k - cslab_at(r, n2, NCTA, bal)) * n01;
   }
   double *gu = F.f[F_U] + B.off;
   const double *gb = F.f[F_B] + B.off, *gc = F.f[F_C] + B.off, *gs = F.f[F_RHO] + B.off;
@@ -155,7 +179,8 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         }
       }
     }
-    __syncthreads();
+    if (bal) cl.sync();   // the edges at a z face read the next block's faces
+    else __syncthreads();
     for (int k = kz0; k < kz1; k++) {
       if (k == 0 || k == n2 - 1) {
         for (int t = threadIdx.x; t < 2 * mi1 + 2 * mi0; t += blockDim.x) {
@@ -169,7 +194,8 @@ __global__ void __launch_bounds__(256) k_coarse_cluster(const DevBox *__restrict
         robin(3, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);   // XY edges
       }
     }
-    __syncthreads();
+    if (bal) cl.sync();   // the corners at a z face read the next block's edges
+    else __syncthreads();
     for (int k = kz0; k < kz1; k++)
       if ((k == 0 || k == n2 - 1) && threadIdx.x < 4)
         robin(7, (threadIdx.x & 1) ? n0 - 1 : 0, (threadIdx.x & 2) ? n1 - 1 : 0, k);

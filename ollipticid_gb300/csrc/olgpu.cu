@@ -216,6 +216,7 @@ struct olgpu_hierarchy {
   double adm[OLGPU_MAX_BH] = {0};
   int coarse_max_iters = 2000;
   int coarse_ncta = 0;            // blocks of the coarse-solve cluster (0: one block)
+  int coarse_bal = 0;             // its slab layout: 1 the balanced one (cslab_begin_bal)
   size_t coarse_cluster_smem = 0;
   double coarse_omega = 1.9;
   double coarse_rtol = 1e-4;
@@ -295,7 +296,8 @@ struct olgpu_hierarchy {
     Stats *d_stats = nullptr;       // its stats (this table's stats[solve])
     AdmJob *d_adm = nullptr;        // its ADM jobs, box indices of this table
     int nadm = 0;
-    int coarse_ncta = 0;            // its coarsest solve: cluster blocks and shared memory
+    int coarse_ncta = 0;            // its coarsest solve: cluster blocks, layout and shared memory
+    int coarse_bal = 0;
     size_t coarse_smem = 0;
   };
   std::vector<Member> members;
@@ -860,7 +862,7 @@ cudaError_t launch_coarse_cluster_n(olgpu_hierarchy *h, const olgpu_hierarchy::M
   return cudaLaunchKernelEx(&cfg, k_coarse_cluster<EQ, NCTA>, (const DevBox *)h->d_boxes, M.coarse_box, h->F,
                             (const double *)h->d_coords, h->eps_coarse, h->coarse_max_iters, h->coarse_omega,
                             h->coarse_rtol, &M.d_stats->coarse_norm, &M.d_stats->coarse_iters,
-                            &M.d_stats->nan_flag, h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0);
+                            &M.d_stats->nan_flag, h->P.boundary == OLGPU_BC_DIRICHLET ? 1 : 0, M.coarse_bal);
 }
 
 template <int EQ>
@@ -914,33 +916,48 @@ bool cluster_fits(olgpu_hierarchy *h, size_t smem)
   return n >= 1;
 }
 
+// The coarse solve's cluster: of 8 or 16 blocks (non-portable size) in the
+// plain or the balanced slab layout, the one whose busiest block has the
+// least FP64 work between two barriers -- its interior planes, plus a
+// quarter plane for the z-face Robin points of blocks 0 and ncta-1 -- and
+// of equal ones the fewer blocks, then the plain layout.  OLGPU_COARSE_BAL=0
+// keeps the plain layout.
 void choose_coarse_cluster(olgpu_hierarchy *h)
 {
   const DevBox &B = h->hboxes[h->G.first_box[0]];
   if (B.n[2] > 64 || B.n[2] < 6 || B.buf != 1) return;
-  // the critical path between two barriers is the largest number of interior
-  // planes a block sweeps; of equal ones the smaller cluster is taken
-  auto crit = [&](int ncta) {
-    int m = 0;
+  const int n2 = B.n[2];
+  auto work = [&](int ncta, int bal) {
+    double m = 0;
     for (int r = 0; r < ncta; r++) {
-      const int a = std::max(cslab_begin(r, B.n[2], ncta), 1), b = std::min(cslab_begin(r + 1, B.n[2], ncta), B.n[2] - 1);
-      m = std::max(m, b - a);
+      const int a = std::max(cslab_at(r, n2, ncta, bal), 1), b = std::min(cslab_at(r + 1, n2, ncta, bal), n2 - 1);
+      m = std::max(m, (b > a ? b - a : 0) + (r == 0 || r == ncta - 1 ? 0.25 : 0.0));
     }
     return m;
   };
-  const int c8 = crit(8), c16 = crit(16);
-  const int order[2] = {c16 < c8 ? 16 : 8, c16 < c8 ? 8 : 16};
-  for (int ncta : order) {
+  const char *bal_env = std::getenv("OLGPU_COARSE_BAL");
+  const bool allow_bal = !(bal_env && std::atoi(bal_env) == 0);
+  struct Cand {
+    int ncta, bal;
+    double w;
+  };
+  std::vector<Cand> cands;
+  for (int ncta : {8, 16})
+    for (int bal : {0, 1})
+      if (!bal || allow_bal) cands.push_back({ncta, bal, work(ncta, bal)});
+  std::stable_sort(cands.begin(), cands.end(), [](const Cand &x, const Cand &y) { return x.w < y.w; });
+  for (const Cand &c : cands) {
     int planes = 0;
-    for (int r = 0; r < ncta; r++)
-      planes = std::max(planes, cslab_begin(r + 1, B.n[2], ncta) - cslab_begin(r, B.n[2], ncta));
+    for (int r = 0; r < c.ncta; r++)
+      planes = std::max(planes, cslab_at(r + 1, n2, c.ncta, c.bal) - cslab_at(r, n2, c.ncta, c.bal));
     const size_t smem = sizeof(double) * (size_t)planes * B.n[0] * B.n[1];
-    const bool ok = ncta == 16 ? (cluster_fits<0, 16>(h, smem) && cluster_fits<1, 16>(h, smem) &&
-                                  cluster_fits<2, 16>(h, smem))
-                               : (cluster_fits<0, 8>(h, smem) && cluster_fits<1, 8>(h, smem) &&
-                                  cluster_fits<2, 8>(h, smem));
+    const bool ok = c.ncta == 16 ? (cluster_fits<0, 16>(h, smem) && cluster_fits<1, 16>(h, smem) &&
+                                    cluster_fits<2, 16>(h, smem))
+                                 : (cluster_fits<0, 8>(h, smem) && cluster_fits<1, 8>(h, smem) &&
+                                    cluster_fits<2, 8>(h, smem));
     if (ok) {
-      h->coarse_ncta = ncta;
+      h->coarse_ncta = c.ncta;
+      h->coarse_bal = c.bal;
       h->coarse_cluster_smem = smem;
       return;
     }
@@ -2220,6 +2237,7 @@ static olgpu_status setup_device(olgpu_hierarchy *h, double *arena, long long st
     M.d_adm = h->d_adm;
     M.nadm = (int)h->hadm.size();
     M.coarse_ncta = h->coarse_ncta;
+    M.coarse_bal = h->coarse_bal;
     M.coarse_smem = h->coarse_cluster_smem;
   }
   if (capture) {
@@ -3368,6 +3386,7 @@ static olgpu_status build_union(std::vector<olgpu_hierarchy *> ms, int precision
     M.pt_base = base[i];
     M.d_stats = U->d_stats + i;
     M.coarse_ncta = m->coarse_ncta;
+    M.coarse_bal = m->coarse_bal;
     M.coarse_smem = m->coarse_cluster_smem;
     std::vector<AdmJob> adm = m->hadm;
     for (auto &J : adm) J.box = map[i][J.box];

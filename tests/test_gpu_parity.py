@@ -101,6 +101,7 @@ LAYOUTS = {
     "fp64_two_points": {"OLGPU_SMOOTH_PTS": "2"},
     "fp32_per_colour": {"OLGPU_SMOOTH32_LAUNCHES": "1"},
     "fp32_per_colour_two_points": {"OLGPU_SMOOTH32_LAUNCHES": "1", "OLGPU_SMOOTH32_PTS": "2"},
+    "fp64_coarse_plain_slabs": {"OLGPU_COARSE_BAL": "0"},
 }
 
 
@@ -110,10 +111,12 @@ LAYOUTS = {
 @pytest.mark.parametrize("variant", sorted(LAYOUTS))
 def test_launch_layouts_give_the_same_bits(case, mixed, variant, monkeypatch):
     """The Robin walk as separate face, edge and corner launches, the FP64
-    smoother with two points a thread, and the FP32 smoother as per-colour
-    launches (two points or one a thread) instead of cluster-resident give
-    the default launches' u bit for bit, over five cycles (a difference of
-    the compiler's fusion between two kernels once showed from the third)."""
+    smoother with two points a thread, the FP32 smoother as per-colour
+    launches (two points or one a thread) instead of cluster-resident, and
+    the FP64 coarsest solve in the plain slab layout instead of the balanced
+    one give the default launches' u bit for bit, over five cycles (a
+    difference of the compiler's fusion between two kernels once showed from
+    the third)."""
     import ollipticid_gb300 as og
     P = problem(case)
     out = []
