@@ -25,9 +25,15 @@ def settle(E, tol=1e-14, max_cycles=300):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("coarse", ["cluster", "one_block"])
 @pytest.mark.parametrize("case", ["o2_single", "o4_binary_merge", "o8_offset", "sf_binary"])
-def test_mixed_fixed_point_matches_oracle(case, oracle_mod):
+def test_mixed_fixed_point_matches_oracle(case, coarse, oracle_mod, monkeypatch):
+    """coarse: the coarsest FP32 correction on a cluster of 8 blocks (the
+    default) or in one block (k_coarse32, which takes the boxes the cluster
+    kernel does not)."""
     import ollipticid_gb300 as og
+    if coarse == "one_block":
+        monkeypatch.setenv("OLGPU_COARSE32_ONE_BLOCK", "1")
     P = problem(case)
     orc = oracle_mod.Oracle(P.oracle_dict())
     orc.fixed_point(tol=1e-14)

@@ -38,9 +38,14 @@ def gpu_fixed_point(E, tol=1e-14, max_cycles=300):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("coarse", ["cluster", "one_block"])
 @pytest.mark.parametrize("case", sorted(CASES))
-def test_fixed_point_matches_oracle(case, oracle_mod):
+def test_fixed_point_matches_oracle(case, coarse, oracle_mod, monkeypatch):
+    """coarse: the coarsest solve on a cluster (the default) or in one block
+    (k_coarse_solve, which takes the grids no cluster does)."""
     import ollipticid_gb300 as og
+    if coarse == "one_block":
+        monkeypatch.setenv("OLGPU_COARSE_ONE_BLOCK", "1")
     P = problem(case)
     orc = oracle_mod.Oracle(P.oracle_dict())
     dorc = orc.fixed_point(tol=1e-14)
