@@ -31,3 +31,11 @@ def test_plan_is_the_reference_geometry(path):
     _abi.check(lib.olgpu_plan_boxes(C.byref(cp), out, 64, C.byref(nb), C.byref(nl), C.byref(mg)))
     assert [[out[g].nx, out[g].ny, out[g].nz] for g in range(nb.value)] == G["box_n"].tolist()
     assert [out[g].level for g in range(nb.value)] == G["box_level"].tolist()
+
+
+def test_header_and_host_agree_on_the_equation_codes():
+    import re
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "olgpu.h")).read()
+    codes = {m.group(1): int(m.group(2)) for m in re.finditer(r"OLGPU_EQ_(\w+)\s*=\s*(\d+)", hdr)}
+    assert codes["BOWEN_YORK"] == og.EQUATIONS["Bowen-York"] == 5
+    assert codes["POISSON"] == og.EQUATIONS["Poisson"]
